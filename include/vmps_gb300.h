@@ -1,0 +1,224 @@
+/*
+ * vmps_gb300.h -- C ABI of the GB300 effective-Hamiltonian engine.
+ *
+ * The engine replaces the block-sparse tensor contractions that VMPS runs inside
+ * its Lanczos / GMRES loops:
+ *
+ *   HxV(PivotMatrix1, PivotVector, PivotVector)   pivot/DmrgPivotMatrix1.h:123-332
+ *   HxV(PivotMatrix2, PivotVector, PivotVector)   pivot/DmrgPivotMatrix2.h:78-273
+ *   HxV(PivotMatrix0, PivotVector, PivotVector)   pivot/DmrgPivotMatrix0.h:31-96
+ *   contract_L(Tripod, A, W, A, qloc, qOp, Tripod) tensors/DmrgContractions.h:34-158
+ *   contract_R(Tripod, A, W, A, qloc, qOp, Tripod) tensors/DmrgContractions.h:179-311
+ *   precalc_blockStructure(...)                    tensors/DmrgIndexGymnastics.h:487-590,699-856
+ *   PivotVector dot / norm / addScale              pivot/DmrgPivotVector.h:121-358
+ *
+ * Everything crosses this boundary as plain pointers and sizes.  Block-sparse
+ * tensors are described by `vmps_blocks` tables (one row per dense block, data
+ * column-major with leading dimension = rows, exactly the storage of an Eigen
+ * MatrixXd) and the MPO site tensor W by a COO table `vmps_mpo_site`.
+ *
+ * Error convention: every entry point returns 0 on success or a negative
+ * VMPS_E_* code; the library never aborts.  vmps_last_error() returns a
+ * thread-local message for the last failure.  The reference itself has no
+ * error channel (asserts only, pivot/DmrgPivotVector.h:307-318).
+ *
+ * Threading: a context owns one CUDA stream.  Different contexts may be used
+ * concurrently from different host threads (VUMPS runs HAC/HC solves for
+ * several sites from OpenMP threads, VUMPS/VumpsSolver.h:1168-1171).
+ */
+#ifndef VMPS_GB300_H
+#define VMPS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ---------------------------------------------------------- */
+#define VMPS_OK              0
+#define VMPS_E_ARG          -1   /* invalid argument / inconsistent tables      */
+#define VMPS_E_CUDA         -2   /* CUDA runtime error                         */
+#define VMPS_E_NOMEM        -3   /* device or host allocation failed           */
+#define VMPS_E_SHAPE        -4   /* block shapes do not chain                  */
+#define VMPS_E_TIMEOUT      -5   /* a bounded device wait gave up              */
+#define VMPS_E_NONFINITE    -6   /* NaN/Inf detected in an input vector        */
+#define VMPS_E_UNSUPPORTED  -7
+
+/* ---- arithmetic of the block products --------------------------------------*/
+#define VMPS_PREC_FP64       0   /* plain FP64 (DMMA), parity with the Eigen path */
+#define VMPS_PREC_BF16X3     1   /* hi*hi + hi*lo + lo*hi bf16 products, FP32 accumulate */
+
+/* ---- symmetry descriptor ----------------------------------------------------
+ * A quantum number is nq int32 values.  kind[i] says how component i fuses:
+ *   VMPS_SYM_U1  : additive (symmetry/U1.h:170-176), vacuum 0
+ *   VMPS_SYM_SU2 : q = 2S+1, |q1-q2|+1 .. q1+q2-1 step 2 (symmetry/SU2.h:174-183), vacuum 1
+ * Products of components follow symmetry/S1xS2.h:192-208.                     */
+#define VMPS_SYM_U1  0
+#define VMPS_SYM_SU2 1
+typedef struct {
+    int32_t nq;
+    int32_t kind[4];
+} vmps_symmetry;
+
+/* ---- block table -------------------------------------------------------------
+ * One row per dense block.  For a site tensor / PivotVector, `leg` is the
+ * physical index s (block = A[s].block[q]); for a Tripod, `leg` is the MPO
+ * auxiliary index a (block = T.block[q][a][0]) and qmid holds the middle QN.
+ * Blocks of size 0 are simply omitted.  offset is in elements of the
+ * accompanying data array; storage is column-major with ld = rows.           */
+typedef struct {
+    int64_t        nblocks;
+    const int32_t* qin;     /* [nblocks*nq] */
+    const int32_t* qout;    /* [nblocks*nq] */
+    const int32_t* qmid;    /* [nblocks*nq] for Tripods, NULL otherwise */
+    const int32_t* leg;     /* [nblocks] */
+    const int64_t* rows;    /* [nblocks] */
+    const int64_t* cols;    /* [nblocks] */
+    const int64_t* offset;  /* [nblocks] */
+} vmps_blocks;
+
+/* ---- MPO site tensor W[s1][s2][k].block[qW](row,col) as COO ------------------
+ * Mirrors Biped<Symmetry,SparseMatrix> W[s1][s2][k] of MpoTerms.h:1175-1232:
+ * s1 = bra (row of the local operator), s2 = ket, k indexes qop, (qin,qout)
+ * the auxiliary QNs of the block, (row,col) the position inside the block.   */
+typedef struct {
+    int64_t        nnz;
+    const int32_t* s1;
+    const int32_t* s2;
+    const int32_t* k;
+    const int32_t* qin;     /* [nnz*nq] */
+    const int32_t* qout;    /* [nnz*nq] */
+    const int32_t* row;
+    const int32_t* col;
+    const double*  val;
+    int32_t        nloc;
+    const int32_t* qloc;    /* [nloc*nq] local basis QNs */
+    int32_t        nop;
+    const int32_t* qop;     /* [nop*nq] operator QNs */
+} vmps_mpo_site;
+
+/* ---- cost / structure report of a prepared contraction ----------------------*/
+typedef struct {
+    int64_t n_tasks;          /* reference task count: sum_q qrhs[q].size()             */
+    int64_t n_chains;         /* (out, X, Y, Z) triple products after merging duplicates */
+    int64_t n_chains_raw;     /* triple products the reference loop evaluates            */
+    int64_t n_intermediates;  /* shared first-stage products                             */
+    int64_t n_out_blocks;
+    int64_t n_tiles_phase1;
+    int64_t n_tiles_phase2;
+    double  flops_reference;  /* sum over raw chains of 2*min(mkn+mnp, knp+mkp)          */
+    double  flops_merged;     /* same rule on the merged chain list (algorithmic count)  */
+    double  flops_executed;   /* flops the two grouped-GEMM phases perform                */
+    double  flops_phase1;
+    double  flops_phase2;
+    double  bytes_algorithmic;/* 8*(distinct X,Z blocks used + |Y| + |out|)              */
+    int32_t association;      /* 0: (X*Y)*Z first, 1: X*(Y*Z) first                      */
+    int32_t reserved;
+} vmps_plan_stats;
+
+typedef struct vmps_ctx_s   vmps_ctx;
+typedef struct vmps_pivot_s vmps_pivot;
+typedef struct vmps_env_s   vmps_env;
+typedef struct vmps_dvec_s  vmps_dvec;
+
+/* ---- context ----------------------------------------------------------------*/
+int         vmps_ctx_create(int device, vmps_ctx** out);
+int         vmps_ctx_destroy(vmps_ctx* ctx);
+const char* vmps_last_error(void);
+const char* vmps_version(void);
+
+/* ---- effective Hamiltonians (PivotMatrix1 / PivotMatrix2 / PivotMatrix0) -------
+ * Builds the task list once on the host (restating precalc_blockStructure,
+ * tensors/DmrgIndexGymnastics.h:487-590 and :699-856), folds every W value and
+ * SU(2) prefactor into one scalar per (out, L_a, V, R_b) chain, merges
+ * duplicates, plans the grouped GEMMs and uploads L and R to the device.
+ * V describes the PivotVector layout (Vin and Vout share it, as the reference's
+ * `Vout = Vin; OxV(...)` does, pivot/DmrgPivotMatrix1.h:127).
+ * For pivot2, V.leg is the combined index s1s3 of Qbasis::combine
+ * (tensors/Qbasis.h:685-798) of qloc12 x qloc34.                               */
+int vmps_pivot1_create(vmps_ctx* ctx, const vmps_symmetry* sym,
+                       const vmps_blocks* L, const double* Ldata,
+                       const vmps_blocks* R, const double* Rdata,
+                       const vmps_mpo_site* W, const vmps_blocks* V,
+                       vmps_pivot** out);
+int vmps_pivot2_create(vmps_ctx* ctx, const vmps_symmetry* sym,
+                       const vmps_blocks* L, const double* Ldata,
+                       const vmps_blocks* R, const double* Rdata,
+                       const vmps_mpo_site* W12, const vmps_mpo_site* W34,
+                       const vmps_blocks* V, vmps_pivot** out);
+int vmps_pivot0_create(vmps_ctx* ctx, const vmps_symmetry* sym,
+                       const vmps_blocks* L, const double* Ldata,
+                       const vmps_blocks* R, const double* Rdata,
+                       const vmps_blocks* V, vmps_pivot** out);
+int vmps_pivot_destroy(vmps_pivot* p);
+int vmps_pivot_stats(const vmps_pivot* p, int precision, vmps_plan_stats* out);
+/* number of doubles of a PivotVector in the compact layout of V */
+int vmps_pivot_dim(const vmps_pivot* p, int64_t* out);
+
+/* HxV with host buffers in the compact layout of V: Vout = H * Vin.
+ * Host->device copy, the product and the device->host copy all happen here.
+ * Replaces HxV(PivotMatrixN, Vin, Vout), pivot/DmrgPivotMatrix1.h:124-129.  */
+int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int precision);
+
+/* ---- device-resident PivotVectors (Lanczos vectors) ---------------------------*/
+int vmps_dvec_create(vmps_pivot* p, vmps_dvec** out);
+int vmps_dvec_destroy(vmps_dvec* v);
+int vmps_dvec_upload(vmps_dvec* v, const double* host);     /* compact layout */
+int vmps_dvec_download(const vmps_dvec* v, double* host);
+/* Vout = H * Vin, both on the device (no host copies). */
+int vmps_hxv_device(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int precision);
+/* dot with the SU(2) weight coeff_dot(qout) of pivot/DmrgPivotVector.h:296-339 */
+int vmps_dvec_dot(const vmps_dvec* a, const vmps_dvec* b, double* out);
+/* y += alpha*x (addScale, pivot/DmrgPivotVector.h:289-293) */
+int vmps_dvec_axpy(double alpha, const vmps_dvec* x, vmps_dvec* y);
+int vmps_dvec_scale(vmps_dvec* x, double alpha);
+int vmps_dvec_copy(const vmps_dvec* src, vmps_dvec* dst);
+/* synchronise the pivot's stream and time n device HxVs with CUDA events */
+int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int precision,
+                  int n_iter, int use_graph, double* ms_per_hxv, double* ms_phase2);
+
+/* ---- Lanczos ground state on the device ----------------------------------------
+ * Full-reorthogonalisation Lanczos (the reference calls the external
+ * LanczosSolver<PivotMatrix,PivotVector>::edgeState, solvers/DmrgSolver.h:1306-1313).
+ * precision VMPS_PREC_BF16X3 runs the Krylov phase with split-precision HxV and
+ * then `refine_iters` closing Lanczos steps with FP64 HxV, restarted from the
+ * split-precision eigenvector.  Krylov vectors, dots and the tridiagonal solve are
+ * FP64 throughout.  v (compact layout) is the start vector on entry and the
+ * ground state on exit.                                                          */
+typedef struct {
+    int32_t iterations;        /* Krylov steps in the first phase            */
+    int32_t refine_iterations; /* FP64 closing steps                          */
+    int32_t hxv_fp64;
+    int32_t hxv_split;
+    double  energy_first;      /* eigenvalue after the first phase            */
+    double  residual;          /* ||H v - E v|| with FP64 HxV at exit         */
+    double  ms_total;
+} vmps_lanczos_stats;
+int vmps_lanczos_ground(vmps_pivot* p, double* v, int precision, int max_iter,
+                        double tol_eigval, double tol_state, int refine_iters,
+                        double* energy, vmps_lanczos_stats* stats);
+
+/* ---- environment updates (contract_L / contract_R, FULL mode) -----------------
+ * Step 1 builds the task list and the output Tripod layout; the caller reads the
+ * layout, allocates the output data, and step 2 runs the contraction.
+ * Replaces contract_L / contract_R of tensors/DmrgContractions.h:34-311.        */
+#define VMPS_ENV_LEFT  0
+#define VMPS_ENV_RIGHT 1
+int vmps_env_create(vmps_ctx* ctx, const vmps_symmetry* sym, int side,
+                    const vmps_blocks* Eold, const vmps_blocks* Abra,
+                    const vmps_mpo_site* W, const vmps_blocks* Aket,
+                    vmps_env** out);
+/* output layout; arrays must hold nblocks (and nblocks*nq for QNs) entries     */
+int vmps_env_layout(const vmps_env* e, int64_t* nblocks, int64_t* total_elems);
+int vmps_env_layout_get(const vmps_env* e, int32_t* qin, int32_t* qout, int32_t* qmid,
+                        int32_t* leg, int64_t* rows, int64_t* cols, int64_t* offset);
+int vmps_env_stats(const vmps_env* e, int precision, vmps_plan_stats* out);
+int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra,
+                 const double* Aket, double* Enew, int precision);
+int vmps_env_destroy(vmps_env* e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VMPS_GB300_H */

@@ -1,0 +1,173 @@
+"""ORACLE -- test infrastructure, not product code.
+
+CPU restatement of the VMPS effective-Hamiltonian path (oracle.cpp) and the
+dense exact-diagonalisation pins (ed.py).  Only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use this
+package, as the checker.  The GPU engine never imports it.
+
+Parity status: the reference (header-only C++ over Eigen, Boost, GSL and the
+TNWorkers TOOLS/ALGS headers) cannot be compiled in this environment, and it
+ships no numeric golden vectors for this path.  The restatement is therefore
+pinned against the reference's own test mechanisms, restated: exact
+diagonalisation of small chains (programs/test_Hubbard/test_Hubbard.cc:227-300),
+the dense effective Hamiltonian P^T H P of small systems, and
+variance / Hermiticity properties (programs/test_Heisenberg/test_Heisenberg.cc:189-192).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import glob
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "oracle.cpp")
+
+_lib = None
+_blas_kind = "inhouse"
+
+
+def build(force=False):
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(SRC) > os.path.getmtime(LIB):
+        tmp = LIB + ".tmp"
+        subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", SRC, "-o", tmp, "-ldl"],
+                       check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def find_openblas():
+    """OpenBLAS shared library bundled with the numpy wheel, if any."""
+    try:
+        d = os.path.dirname(np.__file__)
+    except Exception:
+        return None
+    for pat in ("../numpy.libs/libscipy_openblas*.so*", "../numpy.libs/libopenblas*.so*", ".libs/libopenblas*.so*"):
+        hits = sorted(glob.glob(os.path.join(d, pat)))
+        if hits:
+            return hits[0]
+    return None
+
+
+def lib(use_blas=True):
+    global _lib, _blas_kind
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB)
+        _lib.oracle_pivot_create.restype = C.c_void_p
+        _lib.oracle_env_create.restype = C.c_void_p
+        _lib.oracle_pivot_tasks.restype = C.c_int64
+        _lib.oracle_env_nblocks.restype = C.c_int64
+        _lib.oracle_max_threads.restype = C.c_int
+        for f in ("oracle_hxv", "oracle_pivot_destroy", "oracle_env_run", "oracle_env_destroy",
+                  "oracle_env_layout", "oracle_pivot_tasks", "oracle_env_nblocks"):
+            getattr(_lib, f).argtypes = None
+        _lib.oracle_set_blas.argtypes = [C.c_char_p]
+        _lib.oracle_set_threads.argtypes = [C.c_int]
+        if use_blas:
+            p = find_openblas()
+            if p and _lib.oracle_set_blas(p.encode()) > 0:
+                _blas_kind = "openblas:" + os.path.basename(p)
+    return _lib
+
+
+def blas_kind():
+    lib()
+    return _blas_kind
+
+
+def set_threads(n):
+    lib().oracle_set_threads(int(n))
+
+
+def max_threads():
+    return lib().oracle_max_threads()
+
+
+def _p(a, t=C.c_int32):
+    return a.ctypes.data_as(C.POINTER(t)) if a is not None else None
+
+
+def _tab(B, mid=True):
+    args = [C.c_int64(B.n), _p(B.qin), _p(B.qout)]
+    if mid:
+        args.append(_p(B.qmid))
+    args += [_p(B.leg), _p(B.rows, C.c_int64), _p(B.cols, C.c_int64), _p(B.offset, C.c_int64)]
+    return args
+
+
+def _mpo(W):
+    if W is None:
+        return [C.c_int64(0)] + [None] * 8 + [C.c_int(0), None, C.c_int(0), None]
+    a = W.arrays()
+    return [C.c_int64(W.nnz), _p(a["s1"]), _p(a["s2"]), _p(a["k"]), _p(a["qin"]), _p(a["qout"]), _p(a["row"]),
+            _p(a["col"]), _p(a["val"], C.c_double), C.c_int(len(W.qloc)), _p(a["qloc"]), C.c_int(len(W.qop)),
+            _p(a["qop"])]
+
+
+class OraclePivot:
+    """kind 1: PivotMatrix1 (W), kind 2: PivotMatrix2 (W, W34), kind 0: PivotMatrix0."""
+
+    def __init__(self, kind, nq, L, R, V, W=None, W34=None):
+        self.V = V
+        self._keep = (L, R, V, W, W34)
+        args = [C.c_int(kind), C.c_int(nq)] + _tab(L) + [_p(L.data, C.c_double)] + _tab(R) + \
+               [_p(R.data, C.c_double)] + _tab(V, mid=False) + _mpo(W) + _mpo(W34)
+        self._h = C.c_void_p(lib().oracle_pivot_create(*args))
+
+    @property
+    def n_tasks(self):
+        return lib().oracle_pivot_tasks(self._h)
+
+    def hxv(self, vin):
+        vin = np.ascontiguousarray(vin, dtype=np.float64)
+        out = np.zeros_like(vin)
+        lib().oracle_hxv(self._h, _p(vin, C.c_double), _p(out, C.c_double))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_pivot_destroy(self._h)
+            self._h = None
+
+
+class OracleEnv:
+    """contract_L (side 'L') / contract_R (side 'R'), FULL mode."""
+
+    def __init__(self, side, nq, E, B, W, K):
+        from vmps_gb300.blocks import Blocks
+        self._keep = (E, B, W, K)
+        args = [C.c_int(0 if side == "L" else 1), C.c_int(nq)] + _tab(E) + _tab(B, mid=False) + \
+               _tab(K, mid=False) + _mpo(W)[:]
+        self._h = C.c_void_p(lib().oracle_env_create(*args))
+        n = lib().oracle_env_nblocks(self._h)
+        qin = np.zeros((n, nq), np.int32); qout = np.zeros((n, nq), np.int32); qmid = np.zeros((n, nq), np.int32)
+        leg = np.zeros(n, np.int32); rows = np.zeros(n, np.int64); cols = np.zeros(n, np.int64)
+        off = np.zeros(n, np.int64)
+        lib().oracle_env_layout(self._h, _p(qin), _p(qout), _p(qmid), _p(leg), _p(rows, C.c_int64),
+                                _p(cols, C.c_int64), _p(off, C.c_int64))
+        self.layout = Blocks(nq, qin, qout, leg, rows, cols, qmid=qmid, offset=off)
+
+    def run(self, E, B, K):
+        out = self.layout.like()
+        lib().oracle_env_run(self._h, _p(E.data, C.c_double), _p(B.data, C.c_double), _p(K.data, C.c_double),
+                             _p(out.data, C.c_double))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_env_destroy(self._h)
+            self._h = None
+
+
+def contract_L(nq, Lold, Abra, W, Aket):
+    return OracleEnv("L", nq, Lold, Abra, W, Aket).run(Lold, Abra, Aket)
+
+
+def contract_R(nq, Rold, Abra, W, Aket):
+    return OracleEnv("R", nq, Rold, Abra, W, Aket).run(Rold, Abra, Aket)

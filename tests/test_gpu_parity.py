@@ -1,0 +1,147 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle on the
+same seeded inputs.
+
+Tolerances (relative, Frobenius norm of the whole output vector / Tripod):
+  FP64 (DMMA)        : 1e-12   (the spec bar for the plain drop-in form)
+  BF16x3 split       : 2e-4    (two bf16 slices per operand ~ 2^-16 per product,
+                                FP32 accumulation; the chain has two products)
+Energies after FP64 refinement: 1e-10 relative.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from vmps_gb300 import _native as N
+from vmps_gb300.blocks import Blocks
+from vmps_gb300.pivot import (DeviceVector, EnvUpdate, PivotMatrix0, PivotMatrix1, PivotMatrix2, hxv_device,
+                              time_hxv)
+
+from helpers import compare_tripods, make_model, oracle_envs, pivot1_case, pivot2_case, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-12
+TOL_SPLIT = 2e-4
+
+
+@pytest.mark.parametrize("kind,L,D,site", [("heis", 8, 16, 3), ("heis", 32, 64, 15), ("hubb", 8, 32, 3),
+                                           ("heis", 10, 8, 0), ("heis", 10, 8, 9)])
+def test_hxv1_parity(gpu_ctx, kind, L, D, site):
+    model, mps, Lenv, Renv, W, V = pivot1_case(kind, L=L, D=D, site=site, seed=21)
+    H = PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V)
+    op = oracle.OraclePivot(1, model.sym.nq, Lenv, Renv, V, W)
+    rng = np.random.default_rng(7)
+    for _ in range(2):
+        v = rng.standard_normal(V.data.size)
+        ref = op.hxv(v)
+        assert rel_err(H.apply(v, "fp64"), ref) < TOL_FP64
+        assert rel_err(H.apply(v, "bf16x3"), ref) < TOL_SPLIT
+
+
+@pytest.mark.parametrize("kind,L,D,site,profile", [("hubb", 6, 24, 2, "even"), ("hubb", 16, 128, 7, "gaussian"),
+                                                   ("heis", 16, 64, 7, "even")])
+def test_hxv2_parity(gpu_ctx, kind, L, D, site, profile):
+    model, mps, Lenv, Renv, W1, W2, V = pivot2_case(kind, L=L, D=D, site=site, seed=22, profile=profile)
+    H = PivotMatrix2(gpu_ctx, model.sym, Lenv, Renv, W1, W2, V)
+    op = oracle.OraclePivot(2, model.sym.nq, Lenv, Renv, V, W1, W2)
+    v = np.random.default_rng(8).standard_normal(V.data.size)
+    ref = op.hxv(v)
+    assert rel_err(H.apply(v, "fp64"), ref) < TOL_FP64
+    assert rel_err(H.apply(v, "bf16x3"), ref) < TOL_SPLIT
+
+
+def test_hxv0_parity(gpu_ctx):
+    model, Q = make_model("hubb", 8)
+    from vmps_gb300.mps import RandomMPS
+    mps = RandomMPS(model, Q, 32, seed=5).canonicalize(4, 3)
+    Lenv, Renv = oracle_envs(model, mps, 4, 3)
+    ent = [(0, q, q, np.zeros((d, d))) for q, d in sorted(mps.dims[4].items())]
+    Cb = Blocks.from_entries(2, ent)
+    H = PivotMatrix0(gpu_ctx, model.sym, Lenv, Renv, Cb)
+    op = oracle.OraclePivot(0, 2, Lenv, Renv, Cb)
+    v = np.random.default_rng(9).standard_normal(Cb.data.size)
+    ref = op.hxv(v)
+    assert rel_err(H.apply(v, "fp64"), ref) < TOL_FP64
+    assert rel_err(H.apply(v, "bf16x3"), ref) < TOL_SPLIT
+
+
+@pytest.mark.parametrize("kind,L,D", [("heis", 12, 32), ("hubb", 10, 48)])
+def test_env_parity(gpu_ctx, kind, L, D):
+    model, Q = make_model(kind, L)
+    from vmps_gb300.mps import RandomMPS
+    mps = RandomMPS(model, Q, D, seed=6, profile="gaussian").canonicalize(L // 2, L // 2)
+    Lenv, Renv = oracle_envs(model, mps, L // 2 - 1, L // 2 + 1)
+    nq = model.sym.nq
+    for side, E, l in (("L", Lenv, L // 2 - 1), ("R", Renv, L // 2 + 1)):
+        ref = oracle.OracleEnv(side, nq, E, mps.A[l], model.W[l], mps.A[l]).run(E, mps.A[l], mps.A[l])
+        e = EnvUpdate(gpu_ctx, model.sym, side, E, mps.A[l], model.W[l], mps.A[l])
+        got = e.run(E, mps.A[l], mps.A[l], "fp64")
+        assert compare_tripods(got, ref) < TOL_FP64
+        got32 = e.run(E, mps.A[l], mps.A[l], "bf16x3")
+        assert compare_tripods(got32, ref) < TOL_SPLIT
+
+
+def test_env_chain_matches_oracle_chain(gpu_ctx):
+    """A whole left sweep of contract_L on the GPU equals the oracle's."""
+    from vmps_gb300.pivot import contract_L, left_vacuum
+    model, Q = make_model("heis", 16)
+    from vmps_gb300.mps import RandomMPS
+    mps = RandomMPS(model, Q, 32, seed=3).canonicalize(8, 8)
+    E = left_vacuum(model.sym)
+    Eo = E
+    for l in range(8):
+        E = contract_L(gpu_ctx, model.sym, E, mps.A[l], model.W[l], mps.A[l])
+        Eo = oracle.contract_L(1, Eo, mps.A[l], model.W[l], mps.A[l])
+    assert compare_tripods(E, Eo) < TOL_FP64
+
+
+def test_device_vectors_and_dot(gpu_ctx):
+    model, mps, Lenv, Renv, W, V = pivot1_case("heis", L=12, D=32, site=5, seed=2)
+    H = PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V)
+    rng = np.random.default_rng(1)
+    a, b = rng.standard_normal(H.dim), rng.standard_normal(H.dim)
+    da, db = DeviceVector(H, a), DeviceVector(H, b)
+    assert abs(da.dot(db) - a @ b) < 1e-12 * np.linalg.norm(a) * np.linalg.norm(b)
+    assert np.array_equal(da.download(), a)
+    hxv_device(H, da, db, "fp64")
+    ref = oracle.OraclePivot(1, 1, Lenv, Renv, V, W).hxv(a)
+    assert rel_err(db.download(), ref) < TOL_FP64
+    ms, ms2 = time_hxv(H, da, db, "fp64", n_iter=3, use_graph=True)
+    assert ms > 0 and ms2 > 0
+    assert rel_err(db.download(), ref) < TOL_FP64
+
+
+def test_nonfinite_input_is_rejected(gpu_ctx):
+    model, mps, Lenv, Renv, W, V = pivot1_case("heis", L=8, D=8, site=3, seed=2)
+    H = PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V)
+    v = np.zeros(H.dim)
+    v[3] = np.nan
+    with pytest.raises(N.VmpsError) as ei:
+        DeviceVector(H, v)
+    assert ei.value.code == -6
+
+
+def _oracle_ground(op, n):
+    Heff = np.column_stack([op.hxv(np.eye(n)[:, j]) for j in range(n)])
+    return np.linalg.eigvalsh(0.5 * (Heff + Heff.T))[0]
+
+
+@pytest.mark.parametrize("case", ["heis1", "hubb2"])
+def test_lanczos_energy(gpu_ctx, case):
+    if case == "heis1":
+        model, mps, Lenv, Renv, W, V = pivot1_case("heis", L=16, D=16, site=7, seed=31)
+        H = PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V)
+        op = oracle.OraclePivot(1, 1, Lenv, Renv, V, W)
+    else:
+        model, mps, Lenv, Renv, W1, W2, V = pivot2_case("hubb", L=8, D=16, site=3, seed=32)
+        H = PivotMatrix2(gpu_ctx, model.sym, Lenv, Renv, W1, W2, V)
+        op = oracle.OraclePivot(2, 2, Lenv, Renv, V, W1, W2)
+    n = H.dim
+    assert n <= 3000
+    e_ref = _oracle_ground(op, n)
+    v0 = np.random.default_rng(3).standard_normal(n)
+    e64, v64, st64 = H.lanczos(v0, "fp64", max_iter=300, tol_eigval=1e-13, tol_state=1e-9)
+    assert abs(e64 - e_ref) < 1e-10 * abs(e_ref), (e64, e_ref, st64)
+    es, vs, sts = H.lanczos(v0, "bf16x3", max_iter=300, tol_eigval=1e-9, tol_state=1e-5, refine_iters=30)
+    assert abs(es - e_ref) < 1e-10 * abs(e_ref), (es, e_ref, sts)
+    assert sts["hxv_split"] > 0 and sts["refine_iterations"] > 0

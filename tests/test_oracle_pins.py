@@ -1,0 +1,142 @@
+"""Pins of the CPU oracle (no GPU): the oracle's HxV / environments against
+dense constructions that share no code with it."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import ed
+from vmps_gb300 import models
+from vmps_gb300.mps import two_site_layout
+
+from helpers import make_model, pivot1_case, pivot2_case, rel_err
+
+
+def test_mpo_matches_dense_heisenberg():
+    m = models.heisenberg_u1(6)
+    H = ed.mpo_to_dense(m)
+    Href = models.dense_heisenberg(6)
+    assert np.allclose(H, Href, atol=1e-13)
+
+
+def test_mpo_matches_dense_hubbard():
+    m = models.hubbard_u1xu1(3, t=1.0, U=4.0)
+    H = ed.permute_to_reference(ed.mpo_to_dense(m), m)
+    Href = models.dense_hubbard(3, t=1.0, U=4.0)
+    assert np.allclose(H, Href, atol=1e-13)
+
+
+def test_heisenberg_ground_energy_known_small():
+    # two-site XXX: singlet energy -3/4 J
+    H = models.dense_heisenberg(2)
+    assert abs(np.linalg.eigvalsh(H)[0] + 0.75) < 1e-14
+
+
+@pytest.mark.parametrize("site", [0, 3, 7])
+def test_oracle_hxv1_equals_dense_effective_hamiltonian(site):
+    model, mps, Lenv, Renv, W, V = pivot1_case("heis", L=8, D=16, site=site, seed=11)
+    H = ed.mpo_to_dense(model)
+    P = ed.pivot1_isometry(mps, V, site)
+    Heff = P.T @ H @ P
+    op = oracle.OraclePivot(1, 1, Lenv, Renv, V, W)
+    rng = np.random.default_rng(5)
+    for _ in range(3):
+        v = rng.standard_normal(V.data.size)
+        assert rel_err(op.hxv(v), Heff @ v) < 1e-12
+
+
+def test_oracle_hxv1_hubbard_dense():
+    model, mps, Lenv, Renv, W, V = pivot1_case("hubb", L=4, D=8, site=1, seed=3)
+    H = ed.mpo_to_dense(model)
+    P = ed.pivot1_isometry(mps, V, 1)
+    op = oracle.OraclePivot(1, 2, Lenv, Renv, V, W)
+    v = np.random.default_rng(1).standard_normal(V.data.size)
+    assert rel_err(op.hxv(v), P.T @ H @ P @ v) < 1e-12
+
+
+def test_oracle_hxv2_hubbard_dense():
+    model, mps, Lenv, Renv, W1, W2, V = pivot2_case("hubb", L=4, D=8, site=1, seed=4)
+    H = ed.mpo_to_dense(model)
+    din = {tuple(mps.A[1].qin[i]): int(mps.A[1].rows[i]) for i in range(mps.A[1].n)}
+    dout = {tuple(mps.A[2].qout[i]): int(mps.A[2].cols[i]) for i in range(mps.A[2].n)}
+    _, comb = two_site_layout(model.sym, model.qloc, model.qloc, din, dout, 2)
+    P = ed.pivot2_isometry(mps, V, comb, 1)
+    op = oracle.OraclePivot(2, 2, Lenv, Renv, V, W1, W2)
+    v = np.random.default_rng(2).standard_normal(V.data.size)
+    assert rel_err(op.hxv(v), P.T @ H @ P @ v) < 1e-12
+
+
+def test_oracle_hxv2_heisenberg_dense():
+    model, mps, Lenv, Renv, W1, W2, V = pivot2_case("heis", L=8, D=16, site=3, seed=9)
+    H = ed.mpo_to_dense(model)
+    din = {tuple(mps.A[3].qin[i]): int(mps.A[3].rows[i]) for i in range(mps.A[3].n)}
+    dout = {tuple(mps.A[4].qout[i]): int(mps.A[4].cols[i]) for i in range(mps.A[4].n)}
+    _, comb = two_site_layout(model.sym, model.qloc, model.qloc, din, dout, 1)
+    P = ed.pivot2_isometry(mps, V, comb, 3)
+    op = oracle.OraclePivot(2, 1, Lenv, Renv, V, W1, W2)
+    v = np.random.default_rng(3).standard_normal(V.data.size)
+    assert rel_err(op.hxv(v), P.T @ H @ P @ v) < 1e-12
+
+
+def test_oracle_two_site_ground_state_is_exact():
+    # with complete bond bases the two-site effective problem contains the ground state
+    model, mps, Lenv, Renv, W1, W2, V = pivot2_case("hubb", L=4, D=64, site=1, seed=5)
+    op = oracle.OraclePivot(2, 2, Lenv, Renv, V, W1, W2)
+    n = V.data.size
+    Heff = np.column_stack([op.hxv(np.eye(n)[:, j]) for j in range(n)])
+    assert np.allclose(Heff, Heff.T, atol=1e-12)
+    H = models.dense_hubbard(4, 1.0, 4.0)
+    # sector N=4, Sz=0 of the dense reference
+    nm = 8
+    mask = []
+    for s in range(2 ** nm):
+        bits = [(s >> (nm - 1 - j)) & 1 for j in range(nm)]
+        N = sum(bits)
+        M = sum(bits[0::2]) - sum(bits[1::2])
+        mask.append(N == 4 and M == 0)
+    e_ed = ed.ground_energy(H, np.array(mask))
+    # the random MPS is not orthonormal here in general -> generalized problem; canonical form makes it standard
+    e = np.linalg.eigvalsh(Heff)[0]
+    assert abs(e - e_ed) < 1e-10 * abs(e_ed)
+
+
+def test_oracle_pivot0_dense():
+    model, Q = make_model("heis", 6)
+    from vmps_gb300.mps import RandomMPS
+    mps = RandomMPS(model, Q, 8, seed=7).canonicalize(3, 2)   # sites<3 left-, sites>2 right-normalised
+    from helpers import oracle_envs
+    Lenv, Renv = oracle_envs(model, mps, 3, 2)   # L at bond 3, R at bond 3
+    # bond matrix C: diagonal blocks (q,q) of the bond-3 basis
+    from vmps_gb300.blocks import Blocks
+    ent = [(0, q, q, np.zeros((d, d))) for q, d in sorted(mps.dims[3].items())]
+    C = Blocks.from_entries(1, ent)
+    H = ed.mpo_to_dense(model)
+    UL = ed.left_isometry(mps, 3)
+    UR = ed.right_isometry(mps, 3)
+    off, cur = {}, 0
+    for q, d in sorted(mps.dims[3].items()):
+        off[q] = cur
+        cur += d
+    P = np.zeros((UL.shape[0] * UR.shape[1], C.data.size))
+    for b in range(C.n):
+        q = tuple(C.qin[b])
+        r, c, o = int(C.rows[b]), int(C.cols[b]), int(C.offset[b])
+        for j in range(c):
+            for i in range(r):
+                P[:, o + i + j * r] = np.kron(UL[:, off[q] + i], UR[off[q] + j, :])
+    op = oracle.OraclePivot(0, 1, Lenv, Renv, C)
+    v = np.random.default_rng(8).standard_normal(C.data.size)
+    assert rel_err(op.hxv(v), P.T @ H @ P @ v) < 1e-12
+
+
+def test_oracle_blas_and_inhouse_agree():
+    model, mps, Lenv, Renv, W1, W2, V = pivot2_case("hubb", L=6, D=24, site=2, seed=6)
+    op = oracle.OraclePivot(2, 2, Lenv, Renv, V, W1, W2)
+    v = np.random.default_rng(4).standard_normal(V.data.size)
+    a = op.hxv(v)
+    lib = oracle.lib()
+    lib.oracle_set_blas(b"")
+    b = op.hxv(v)
+    p = oracle.find_openblas()
+    if p:
+        lib.oracle_set_blas(p.encode())
+    assert rel_err(a, b) < 1e-13

@@ -1,0 +1,135 @@
+"""ctypes binding of the C ABI in ``include/vmps_gb300.h``.
+
+The native library is the product: there is no Python or CPU fallback.  If
+``libvmps_gb300.so`` is missing or fails to load, importing the compute entry
+points raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libvmps_gb300.so")
+
+VMPS_OK = 0
+PREC_FP64 = 0
+PREC_BF16X3 = 1
+SYM_U1 = 0
+SYM_SU2 = 1
+ENV_LEFT = 0
+ENV_RIGHT = 1
+
+ERRORS = {-1: "VMPS_E_ARG", -2: "VMPS_E_CUDA", -3: "VMPS_E_NOMEM", -4: "VMPS_E_SHAPE",
+          -5: "VMPS_E_TIMEOUT", -6: "VMPS_E_NONFINITE", -7: "VMPS_E_UNSUPPORTED"}
+
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+f64p = C.POINTER(C.c_double)
+
+
+class vmps_symmetry(C.Structure):
+    _fields_ = [("nq", C.c_int32), ("kind", C.c_int32 * 4)]
+
+
+class vmps_blocks(C.Structure):
+    _fields_ = [("nblocks", C.c_int64), ("qin", i32p), ("qout", i32p), ("qmid", i32p), ("leg", i32p),
+                ("rows", i64p), ("cols", i64p), ("offset", i64p)]
+
+
+class vmps_mpo_site(C.Structure):
+    _fields_ = [("nnz", C.c_int64), ("s1", i32p), ("s2", i32p), ("k", i32p), ("qin", i32p), ("qout", i32p),
+                ("row", i32p), ("col", i32p), ("val", f64p), ("nloc", C.c_int32), ("qloc", i32p),
+                ("nop", C.c_int32), ("qop", i32p)]
+
+
+class vmps_plan_stats(C.Structure):
+    _fields_ = [("n_tasks", C.c_int64), ("n_chains", C.c_int64), ("n_chains_raw", C.c_int64),
+                ("n_intermediates", C.c_int64), ("n_out_blocks", C.c_int64), ("n_tiles_phase1", C.c_int64),
+                ("n_tiles_phase2", C.c_int64), ("flops_reference", C.c_double), ("flops_merged", C.c_double),
+                ("flops_executed", C.c_double), ("flops_phase1", C.c_double), ("flops_phase2", C.c_double),
+                ("bytes_algorithmic", C.c_double), ("association", C.c_int32), ("reserved", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class vmps_lanczos_stats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("refine_iterations", C.c_int32), ("hxv_fp64", C.c_int32),
+                ("hxv_split", C.c_int32), ("energy_first", C.c_double), ("residual", C.c_double),
+                ("ms_total", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# (name, restype, argtypes)
+_PROTOS = [
+    ("vmps_last_error", C.c_char_p, []),
+    ("vmps_version", C.c_char_p, []),
+    ("vmps_ctx_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    ("vmps_ctx_destroy", C.c_int, [C.c_void_p]),
+    ("vmps_pivot1_create", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
+                                     C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_mpo_site),
+                                     C.POINTER(vmps_blocks), C.POINTER(C.c_void_p)]),
+    ("vmps_pivot2_create", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
+                                     C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_mpo_site),
+                                     C.POINTER(vmps_mpo_site), C.POINTER(vmps_blocks), C.POINTER(C.c_void_p)]),
+    ("vmps_pivot0_create", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
+                                     C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks),
+                                     C.POINTER(C.c_void_p)]),
+    ("vmps_pivot_destroy", C.c_int, [C.c_void_p]),
+    ("vmps_pivot_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),
+    ("vmps_pivot_dim", C.c_int, [C.c_void_p, i64p]),
+    ("vmps_hxv", C.c_int, [C.c_void_p, f64p, f64p, C.c_int]),
+    ("vmps_dvec_create", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("vmps_dvec_destroy", C.c_int, [C.c_void_p]),
+    ("vmps_dvec_upload", C.c_int, [C.c_void_p, f64p]),
+    ("vmps_dvec_download", C.c_int, [C.c_void_p, f64p]),
+    ("vmps_hxv_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    ("vmps_dvec_dot", C.c_int, [C.c_void_p, C.c_void_p, f64p]),
+    ("vmps_dvec_axpy", C.c_int, [C.c_double, C.c_void_p, C.c_void_p]),
+    ("vmps_dvec_scale", C.c_int, [C.c_void_p, C.c_double]),
+    ("vmps_dvec_copy", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("vmps_hxv_time", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, f64p, f64p]),
+    ("vmps_lanczos_ground", C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                      f64p, C.POINTER(vmps_lanczos_stats)]),
+    ("vmps_env_create", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.c_int, C.POINTER(vmps_blocks),
+                                  C.POINTER(vmps_blocks), C.POINTER(vmps_mpo_site), C.POINTER(vmps_blocks),
+                                  C.POINTER(C.c_void_p)]),
+    ("vmps_env_layout", C.c_int, [C.c_void_p, i64p, i64p]),
+    ("vmps_env_layout_get", C.c_int, [C.c_void_p, i32p, i32p, i32p, i32p, i64p, i64p, i64p]),
+    ("vmps_env_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),
+    ("vmps_env_run", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, C.c_int]),
+    ("vmps_env_destroy", C.c_int, [C.c_void_p]),
+]
+
+EXPORTED = [p[0] for p in _PROTOS]
+
+_lib = None
+
+
+class VmpsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """Load the native library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in _PROTOS:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != VMPS_OK:
+        raise VmpsError(rc, lib().vmps_last_error().decode(errors="replace"))

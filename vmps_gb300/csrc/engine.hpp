@@ -1,0 +1,141 @@
+// Internal interfaces shared by the host task-list builder (tasks.cpp), the
+// device runtime / C ABI (runtime.cpp) and the kernels (kernels.cu).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "qn.hpp"
+#include "../../include/vmps_gb300.h"
+
+namespace vmps {
+
+// ---------------------------------------------------------------------------
+// Host views of the C-ABI tables
+// ---------------------------------------------------------------------------
+struct BlockTable {
+    int64_t n = 0;
+    std::vector<QN> qin, qout, qmid;
+    std::vector<int32_t> leg;
+    std::vector<int64_t> rows, cols, off;   // compact (host) layout
+    bool has_mid = false;
+    int64_t total = 0;                      // elements in the compact data array
+};
+BlockTable parse_blocks(const Symmetry& sym, const vmps_blocks* b, bool need_mid);
+
+// Tripod = Multipede<3>: blocks keyed by {qin,qout,qmid}, each an array over
+// the auxiliary index a (tensors/Multipede.h:77-95, access T.block[q][a][0]).
+struct TripodView {
+    std::vector<QN3> keys;
+    std::unordered_map<QN3, int, QNTupleHash<3>> dict;
+    std::vector<std::vector<int64_t>> aux;    // aux[q][a] -> block row, -1 = empty
+    int64_t at(int q, int a) const {
+        const auto& v = aux[q];
+        return (a >= 0 && a < (int)v.size()) ? v[a] : -1;
+    }
+};
+TripodView make_tripod_view(const BlockTable& t);
+
+// vector<Biped> (site tensor A[s] or PivotVector::data[s]); dict[s] maps {qin,qout}
+struct BipedsView {
+    std::vector<std::unordered_map<QN2, int64_t, QNTupleHash<2>>> dict;
+    int64_t find(int s, const QN& a, const QN& b) const {
+        if (s < 0 || s >= (int)dict.size()) return -1;
+        auto it = dict[s].find(QN2{{a, b}});
+        return it == dict[s].end() ? -1 : it->second;
+    }
+};
+BipedsView make_bipeds_view(const BlockTable& t, int nlegs);
+
+struct MpoNz { int32_t row, col; double val; };
+struct MpoView {
+    int nloc = 0, nop = 0;
+    std::vector<QN> qloc, qop;
+    // blocks[(s1*nloc+s2)*nop+k] : {qin,qout} -> nonzeros of W[s1][s2][k].block[qW]
+    std::vector<std::unordered_map<QN2, std::vector<MpoNz>, QNTupleHash<2>>> blocks;
+    const std::vector<MpoNz>* find(int s1, int s2, int k, const QN& a, const QN& b) const {
+        const auto& m = blocks[((size_t)s1 * nloc + s2) * nop + k];
+        auto it = m.find(QN2{{a, b}});
+        return it == m.end() ? nullptr : &it->second;
+    }
+};
+MpoView parse_mpo(const Symmetry& sym, const vmps_mpo_site* W);
+
+// ---------------------------------------------------------------------------
+// Chains: out[o] += c * op(X[x]) * Y[y] * op(Z[z])
+//   HxV (1-,2-,0-site): X = L_a, Y = V, Z = R_b          (no transposes)
+//   contract_L        : X = Abra^dagger, Y = Lold_a, Z = Aket
+//   contract_R        : X = Aket, Y = Rold_b, Z = Abra^dagger
+// ---------------------------------------------------------------------------
+struct Chain { int64_t out, x, y, z; double c; };
+
+struct ChainSet {
+    std::vector<Chain> chains;
+    int64_t n_tasks = 0;        // sum_q qrhs[q].size() of the reference task list
+    int64_t n_chains_raw = 0;   // (task, W-nonzero) products the reference evaluates
+    double flops_reference = 0; // 2*min(...) summed over those raw products
+};
+
+// builders (tasks.cpp)
+ChainSet build_pivot1(const Symmetry& sym, const BlockTable& L, const BlockTable& R,
+                      const MpoView& W, const BlockTable& V);
+ChainSet build_pivot2(const Symmetry& sym, const BlockTable& L, const BlockTable& R,
+                      const MpoView& W12, const MpoView& W34, const BlockTable& V);
+ChainSet build_pivot0(const Symmetry& sym, const BlockTable& L, const BlockTable& R,
+                      const BlockTable& V);
+// contract_L / contract_R: also derives the output Tripod layout
+ChainSet build_env(const Symmetry& sym, int side, const BlockTable& Eold, const BlockTable& Abra,
+                   const MpoView& W, const BlockTable& Aket, BlockTable* Enew);
+
+// combined two-site index s1s3 of Qbasis::combine (tensors/Qbasis.h:685-798)
+struct CombinedBasis {
+    int n = 0;
+    // index[(s1*n34+s3)] -> vector of (qmerge, s1s3)
+    std::vector<std::vector<std::pair<QN, int>>> index;
+    std::vector<QN> q_of;   // QN of combined state
+};
+CombinedBasis combine_bases(const Symmetry& sym, const std::vector<QN>& q12, const std::vector<QN>& q34);
+
+// ---------------------------------------------------------------------------
+// Grouped-GEMM plan (device work lists)
+// ---------------------------------------------------------------------------
+// Device block layout: column-major, ld = rows rounded up to 8, block starts
+// aligned to 32 elements; padding stays zero.
+inline int64_t pad_ld(int64_t rows) { return (rows + 7) / 8 * 8; }
+inline int64_t pad_off(int64_t x) { return (x + 31) / 32 * 32; }
+
+struct DevLayout {             // one arena (L, R, V, T ...)
+    std::vector<int64_t> off, rows, cols, ld;
+    int64_t total = 0;         // elements incl. padding
+};
+DevLayout make_dev_layout(const std::vector<int64_t>& rows, const std::vector<int64_t>& cols);
+
+// GPU work items (POD, copied verbatim to the device)
+struct GTerm { int64_t off; double coef; };
+struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, K, pad; };
+struct GTile { int64_t c_off; int32_t ldc, m, n, row0, col0, seg_begin, seg_end, pad; };
+
+struct PhasePlan {
+    std::vector<GTerm> terms;
+    std::vector<GSeg>  segs;
+    std::vector<GTile> tiles;
+    bool transA = false, transB = false, transC = false;
+    int  slotA = 0, slotB = 0, slotC = 0;   // arena ids
+    double flops = 0;
+};
+
+enum Slot { SLOT_X = 0, SLOT_Y = 1, SLOT_Z = 2, SLOT_OUT = 3, SLOT_T = 4 };
+
+struct Plan {
+    PhasePlan p1, p2;
+    DevLayout T;               // intermediate arena layout
+    int association = 0;       // 0: T = op(X)*Y first; 1: U = Y*op(Z) first
+    int64_t n_chains = 0, n_intermediates = 0, n_out_blocks = 0;
+    double flops_merged = 0, bytes_alg = 0;
+};
+// tile edge used by the planner for a precision mode
+Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
+               const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n);
+
+}  // namespace vmps

@@ -1,0 +1,39 @@
+// Host-callable launchers of kernels.cu
+#pragma once
+#include <cuda_runtime.h>
+
+#include "engine.hpp"
+
+namespace vmps {
+
+struct GGArgs {
+    const void* A;
+    const void* B;
+    void* C;
+    const GTile* tiles;
+    const GSeg* segs;
+    const GTerm* terms;
+    int ntiles;
+    int transA, transB, transC;
+};
+
+struct PackBlock { int64_t coff, doff, rows, cols, ld; double scale; };
+
+cudaError_t kernels_init();
+// operand type codes for the split kernel: 0 = double, 1 = float
+cudaError_t launch_gg(int prec, int ta, int tb, int tc, const GGArgs& a, cudaStream_t st);
+cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, double* dst, int to_padded,
+                        cudaStream_t st);
+cudaError_t launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
+int64_t dot_chunk(int64_t n);
+int dot_nchunk(int64_t n);
+cudaError_t launch_dot(const double* x, const double* y, int64_t n, double* part, double* out, cudaStream_t st);
+cudaError_t launch_mdot(const double* V, int nv, int64_t n, const double* w, double* part, double* out,
+                        cudaStream_t st);
+cudaError_t launch_mgs(const double* V, int nv, int64_t n, const double* coef, double* w, cudaStream_t st);
+cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t st);
+cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t st);
+cudaError_t launch_combine(const double* V, int nv, int64_t n, const double* c, double* y, cudaStream_t st);
+cudaError_t launch_finite(const double* x, int64_t n, int* bad, cudaStream_t st);
+
+}  // namespace vmps

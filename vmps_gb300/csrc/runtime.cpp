@@ -1,0 +1,916 @@
+// Device runtime and C ABI (include/vmps_gb300.h).
+//
+// One vmps_ctx = one CUDA stream on one device.  A vmps_pivot owns the device
+// copies of L and R for one site (the reference's PivotMatrix owns value copies
+// of L, R, W and its task list, pivot/DmrgPivotMatrix1.h:12-20,56-61), the
+// grouped-GEMM work lists for each precision, and scratch for the intermediate
+// products.  PivotVectors live on the device in a padded block layout
+// (engine.hpp: ld multiple of 8, 32-element aligned starts, zero padding) and
+// are scaled per block by sqrt(coeff_dot(qout)) so that the SU(2)-weighted
+// inner product of pivot/DmrgPivotVector.h:323 becomes a plain dot product.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+#include "kernels.hpp"
+
+using namespace vmps;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+static int set_err(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+struct CudaFail : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+#define CK(call)                                                                                         \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess)                                                                           \
+            throw CudaFail(std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + __FILE__ + ":" + \
+                           std::to_string(__LINE__) + ")");                                              \
+    } while (0)
+
+#define API_BEGIN try {
+#define API_END                                                                 \
+    }                                                                           \
+    catch (const CudaFail& e) { return set_err(VMPS_E_CUDA, e.what()); }        \
+    catch (const std::bad_alloc& e) { return set_err(VMPS_E_NOMEM, e.what()); } \
+    catch (const std::domain_error& e) { return set_err(VMPS_E_SHAPE, e.what()); } \
+    catch (const std::invalid_argument& e) { return set_err(VMPS_E_ARG, e.what()); } \
+    catch (const std::exception& e) { return set_err(VMPS_E_ARG, e.what()); }   \
+    return VMPS_OK;
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+    void alloc(size_t b, cudaStream_t st = 0, bool zero = true) {
+        if (p && bytes >= b) { if (zero) CK(cudaMemsetAsync(p, 0, b, st)); return; }
+        if (p) { cudaFree(p); p = nullptr; }
+        bytes = std::max<size_t>(b, 256);
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) { p = nullptr; throw std::bad_alloc(); }
+        if (zero) CK(cudaMemsetAsync(p, 0, bytes, st));
+    }
+    template <typename T> T* as() const { return (T*)p; }
+};
+
+template <typename T> static void upload_vec(DBuf& d, const std::vector<T>& v, cudaStream_t st) {
+    d.alloc(std::max<size_t>(1, v.size()) * sizeof(T), st, false);
+    if (!v.empty()) CK(cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
+struct vmps_ctx_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+};
+
+// device copy of one phase's work lists
+struct DevPhase {
+    DBuf tiles, segs, terms;
+    int ntiles = 0;
+    const PhasePlan* host = nullptr;
+    void upload(const PhasePlan& ph, cudaStream_t st) {
+        host = &ph;
+        ntiles = (int)ph.tiles.size();
+        upload_vec(tiles, ph.tiles, st);
+        upload_vec(segs, ph.segs, st);
+        upload_vec(terms, ph.terms, st);
+    }
+};
+
+struct DevPlan {
+    Plan plan;
+    DevPhase p1, p2;
+    DBuf T;   // intermediate arena (double or float)
+    bool ready = false;
+};
+
+// compact <-> padded copy descriptors of one block table
+static std::vector<PackBlock> pack_blocks(const BlockTable& t, const DevLayout& d, const std::vector<double>* scale) {
+    std::vector<PackBlock> v(t.n);
+    for (int64_t i = 0; i < t.n; ++i)
+        v[i] = PackBlock{t.off[i], d.off[i], t.rows[i], t.cols[i], d.ld[i], scale ? (*scale)[i] : 1.0};
+    return v;
+}
+
+// operand arenas for one grouped-GEMM problem
+struct Operands {
+    const void* X = nullptr; int tx = 0;   // type code 0 double / 1 float
+    const void* Y = nullptr; int ty = 0;
+    const void* Z = nullptr; int tz = 0;
+    void* O = nullptr; int to = 0;
+};
+
+static void run_plan(const DevPlan& dp, int prec, const Operands& ops, cudaStream_t st) {
+    auto slot_ptr = [&](int slot, int& tcode) -> const void* {
+        switch (slot) {
+            case SLOT_X: tcode = ops.tx; return ops.X;
+            case SLOT_Y: tcode = ops.ty; return ops.Y;
+            case SLOT_Z: tcode = ops.tz; return ops.Z;
+            case SLOT_OUT: tcode = ops.to; return ops.O;
+            case SLOT_T: tcode = prec == VMPS_PREC_FP64 ? 0 : 1; return dp.T.p;
+        }
+        tcode = 0;
+        return nullptr;
+    };
+    for (int ph = 0; ph < 2; ++ph) {
+        const DevPhase& d = ph == 0 ? dp.p1 : dp.p2;
+        const PhasePlan& h = ph == 0 ? dp.plan.p1 : dp.plan.p2;
+        GGArgs a{};
+        int ta, tb, tc;
+        a.A = slot_ptr(h.slotA, ta);
+        a.B = slot_ptr(h.slotB, tb);
+        a.C = const_cast<void*>(slot_ptr(h.slotC, tc));
+        a.tiles = d.tiles.as<GTile>();
+        a.segs = d.segs.as<GSeg>();
+        a.terms = d.terms.as<GTerm>();
+        a.ntiles = d.ntiles;
+        a.transA = h.transA; a.transB = h.transB; a.transC = h.transC;
+        if (prec == VMPS_PREC_FP64 && (ta | tb | tc)) throw std::invalid_argument("FP64 plan with float operand");
+        CK(launch_gg(prec, ta, tb, tc, a, st));
+    }
+}
+
+static void fill_stats(const ChainSet& cs, const Plan& p, vmps_plan_stats* s) {
+    std::memset(s, 0, sizeof(*s));
+    s->n_tasks = cs.n_tasks;
+    s->n_chains = p.n_chains;
+    s->n_chains_raw = cs.n_chains_raw;
+    s->n_intermediates = p.n_intermediates;
+    s->n_out_blocks = p.n_out_blocks;
+    s->n_tiles_phase1 = (int64_t)p.p1.tiles.size();
+    s->n_tiles_phase2 = (int64_t)p.p2.tiles.size();
+    s->flops_reference = cs.flops_reference;
+    s->flops_merged = p.flops_merged;
+    s->flops_phase1 = p.p1.flops;
+    s->flops_phase2 = p.p2.flops;
+    s->flops_executed = p.p1.flops + p.p2.flops;
+    s->bytes_algorithmic = p.bytes_alg;
+    s->association = p.association;
+}
+
+static int tile_edge(int prec) { return prec == VMPS_PREC_FP64 ? 64 : 128; }
+
+// ---------------------------------------------------------------------------
+// pivot (PivotMatrix0/1/2)
+// ---------------------------------------------------------------------------
+struct vmps_pivot_s {
+    vmps_ctx* ctx = nullptr;
+    Symmetry sym;
+    BlockTable Lt, Rt, Vt;
+    DevLayout Ld, Rd, Vd;
+    ChainSet cs;
+    DevPlan plans[2];
+    DBuf dL, dR, dL32, dR32;
+    DBuf dPack;                 // PackBlock[] of the vector layout
+    int npack = 0;
+    std::vector<double> vscale; // sqrt(coeff_dot(qout)) per V block
+    DBuf stage_in, stage_out;   // compact vectors for host-buffer HxV
+    DBuf vin, vout;             // padded vectors for host-buffer HxV
+    DBuf part, scal;            // reduction scratch
+    DBuf flag;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    const void* graph_in[2] = {nullptr, nullptr};
+    const void* graph_out[2] = {nullptr, nullptr};
+    ~vmps_pivot_s() {
+        for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
+    }
+    cudaStream_t st() const { return ctx->stream; }
+};
+
+struct vmps_dvec_s {
+    vmps_pivot* p = nullptr;
+    DBuf d;
+    int64_t n = 0;   // padded length
+};
+
+static DevPlan& get_plan(vmps_pivot* p, int prec) {
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
+    DevPlan& dp = p->plans[prec];
+    if (dp.ready) return dp;
+    const int te = tile_edge(prec);
+    dp.plan = make_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, te, te);
+    if (p->ctx->device < 0) { dp.ready = true; return dp; }   // host-only: plan without device copies
+    dp.p1.upload(dp.plan.p1, p->st());
+    dp.p2.upload(dp.plan.p2, p->st());
+    dp.T.alloc((size_t)dp.plan.T.total * (prec == VMPS_PREC_FP64 ? 8 : 4), p->st(), true);
+    if (prec == VMPS_PREC_BF16X3 && !p->dL32.p) {
+        p->dL32.alloc((size_t)p->Ld.total * 4, p->st(), true);
+        p->dR32.alloc((size_t)p->Rd.total * 4, p->st(), true);
+        CK(launch_to_f32(p->dL.as<double>(), p->dL32.as<float>(), p->Ld.total, p->st()));
+        CK(launch_to_f32(p->dR.as<double>(), p->dR32.as<float>(), p->Rd.total, p->st()));
+    }
+    CK(cudaStreamSynchronize(p->st()));
+    dp.ready = true;
+    return dp;
+}
+
+static void require_device(const vmps_ctx* c) {
+    if (!c || c->device < 0) throw std::invalid_argument("operation needs a device context (this one is host-only)");
+}
+
+static void pivot_hxv_dev(vmps_pivot* p, int prec, const double* vin, double* vout) {
+    require_device(p->ctx);
+    DevPlan& dp = get_plan(p, prec);
+    Operands ops;
+    if (prec == VMPS_PREC_FP64) {
+        ops.X = p->dL.p; ops.Z = p->dR.p;
+    } else {
+        ops.X = p->dL32.p; ops.tx = 1; ops.Z = p->dR32.p; ops.tz = 1;
+    }
+    ops.Y = vin; ops.O = vout;
+    run_plan(dp, prec, ops, p->st());
+}
+
+static void upload_blocks_padded(const BlockTable& t, const DevLayout& d, const double* host, DBuf& dst,
+                                 cudaStream_t st) {
+    dst.alloc((size_t)d.total * 8, st, true);
+    if (t.n == 0) return;
+    DBuf tmp, pk;
+    tmp.alloc((size_t)std::max<int64_t>(t.total, 1) * 8, st, false);
+    CK(cudaMemcpyAsync(tmp.p, host, (size_t)t.total * 8, cudaMemcpyHostToDevice, st));
+    auto pb = pack_blocks(t, d, nullptr);
+    upload_vec(pk, pb, st);
+    CK(launch_pack(pk.as<PackBlock>(), (int)t.n, tmp.as<double>(), dst.as<double>(), 1, st));
+    CK(cudaStreamSynchronize(st));   // tmp and pk are released on return
+}
+
+static Symmetry make_sym(const vmps_symmetry* s) {
+    if (!s || s->nq < 1 || s->nq > kMaxNq) throw std::invalid_argument("symmetry needs 1 <= nq <= 4");
+    Symmetry y;
+    y.nq = s->nq;
+    for (int i = 0; i < s->nq; ++i) {
+        if (s->kind[i] != VMPS_SYM_U1 && s->kind[i] != VMPS_SYM_SU2) throw std::invalid_argument("unknown QN kind");
+        y.kind[i] = s->kind[i];
+    }
+    return y;
+}
+
+static int pivot_create_common(vmps_ctx* ctx, const Symmetry& sym, const vmps_blocks* L, const double* Ldata,
+                               const vmps_blocks* R, const double* Rdata, const vmps_blocks* V,
+                               std::unique_ptr<vmps_pivot>& p) {
+    if (!ctx) throw std::invalid_argument("null context");
+    if (!Ldata || !Rdata) throw std::invalid_argument("null L/R data");
+    p.reset(new vmps_pivot_s());
+    p->ctx = ctx;
+    p->sym = sym;
+    p->Lt = parse_blocks(sym, L, true);
+    p->Rt = parse_blocks(sym, R, true);
+    p->Vt = parse_blocks(sym, V, false);
+    p->Ld = make_dev_layout(p->Lt.rows, p->Lt.cols);
+    p->Rd = make_dev_layout(p->Rt.rows, p->Rt.cols);
+    p->Vd = make_dev_layout(p->Vt.rows, p->Vt.cols);
+    return 0;
+}
+
+static void pivot_finish(vmps_pivot* p, const double* Ldata, const double* Rdata) {
+    // SU(2): fold sqrt(w_out / w_in) into each chain (weighted dot -> plain dot)
+    p->vscale.assign(p->Vt.n, 1.0);
+    if (p->sym.nonabelian()) {
+        for (int64_t i = 0; i < p->Vt.n; ++i) p->vscale[i] = std::sqrt(p->sym.coeff_dot(p->Vt.qout[i]));
+        for (auto& c : p->cs.chains) c.c *= p->vscale[c.out] / p->vscale[c.y];
+    }
+    if (p->ctx->device < 0) return;
+    CK(cudaSetDevice(p->ctx->device));
+    upload_blocks_padded(p->Lt, p->Ld, Ldata, p->dL, p->st());
+    upload_blocks_padded(p->Rt, p->Rd, Rdata, p->dR, p->st());
+    auto pb = pack_blocks(p->Vt, p->Vd, &p->vscale);
+    p->npack = (int)pb.size();
+    upload_vec(p->dPack, pb, p->st());
+    const int nc = dot_nchunk(p->Vd.total);
+    p->part.alloc((size_t)std::max(nc, 1) * 8 * 1024, p->st(), true);
+    p->scal.alloc(4096 * 8, p->st(), true);
+    p->flag.alloc(64, p->st(), true);
+    CK(cudaStreamSynchronize(p->st()));
+}
+
+extern "C" {
+
+const char* vmps_last_error(void) { return g_last_error.c_str(); }
+const char* vmps_version(void) { return "vmps_gb300 0.1 (sm_103a)"; }
+
+int vmps_ctx_create(int device, vmps_ctx** out) {
+    API_BEGIN
+    if (!out) return set_err(VMPS_E_ARG, "null out");
+    if (device == -1) {   // host-only context: task lists and plans, no device work
+        auto* c = new vmps_ctx_s();
+        c->device = -1;
+        *out = c;
+        return VMPS_OK;
+    }
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return set_err(VMPS_E_ARG, "device index out of range");
+    CK(cudaSetDevice(device));
+    CK(kernels_init());
+    auto* c = new vmps_ctx_s();
+    c->device = device;
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+    CK(cudaEventCreate(&c->ev2));
+    *out = c;
+    API_END
+}
+
+int vmps_ctx_destroy(vmps_ctx* ctx) {
+    if (!ctx) return VMPS_OK;
+    if (ctx->device < 0) { delete ctx; return VMPS_OK; }
+    cudaStreamSynchronize(ctx->stream);
+    cudaEventDestroy(ctx->ev0);
+    cudaEventDestroy(ctx->ev1);
+    cudaEventDestroy(ctx->ev2);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return VMPS_OK;
+}
+
+int vmps_pivot1_create(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* L, const double* Ldata,
+                       const vmps_blocks* R, const double* Rdata, const vmps_mpo_site* W, const vmps_blocks* V,
+                       vmps_pivot** out) {
+    API_BEGIN
+    if (!out) return set_err(VMPS_E_ARG, "null out");
+    Symmetry sym = make_sym(symd);
+    std::unique_ptr<vmps_pivot> p;
+    pivot_create_common(ctx, sym, L, Ldata, R, Rdata, V, p);
+    MpoView Wv = parse_mpo(sym, W);
+    p->cs = build_pivot1(sym, p->Lt, p->Rt, Wv, p->Vt);
+    pivot_finish(p.get(), Ldata, Rdata);
+    *out = p.release();
+    API_END
+}
+
+int vmps_pivot2_create(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* L, const double* Ldata,
+                       const vmps_blocks* R, const double* Rdata, const vmps_mpo_site* W12,
+                       const vmps_mpo_site* W34, const vmps_blocks* V, vmps_pivot** out) {
+    API_BEGIN
+    if (!out) return set_err(VMPS_E_ARG, "null out");
+    Symmetry sym = make_sym(symd);
+    std::unique_ptr<vmps_pivot> p;
+    pivot_create_common(ctx, sym, L, Ldata, R, Rdata, V, p);
+    MpoView W1 = parse_mpo(sym, W12), W2 = parse_mpo(sym, W34);
+    p->cs = build_pivot2(sym, p->Lt, p->Rt, W1, W2, p->Vt);
+    pivot_finish(p.get(), Ldata, Rdata);
+    *out = p.release();
+    API_END
+}
+
+int vmps_pivot0_create(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* L, const double* Ldata,
+                       const vmps_blocks* R, const double* Rdata, const vmps_blocks* V, vmps_pivot** out) {
+    API_BEGIN
+    if (!out) return set_err(VMPS_E_ARG, "null out");
+    Symmetry sym = make_sym(symd);
+    std::unique_ptr<vmps_pivot> p;
+    pivot_create_common(ctx, sym, L, Ldata, R, Rdata, V, p);
+    p->cs = build_pivot0(sym, p->Lt, p->Rt, p->Vt);
+    pivot_finish(p.get(), Ldata, Rdata);
+    *out = p.release();
+    API_END
+}
+
+int vmps_pivot_destroy(vmps_pivot* p) {
+    if (!p) return VMPS_OK;
+    cudaStreamSynchronize(p->st());
+    delete p;
+    return VMPS_OK;
+}
+
+int vmps_pivot_stats(const vmps_pivot* pc, int prec, vmps_plan_stats* out) {
+    API_BEGIN
+    if (!pc || !out) return set_err(VMPS_E_ARG, "null argument");
+    auto* p = const_cast<vmps_pivot*>(pc);
+    DevPlan& dp = get_plan(p, prec);
+    fill_stats(p->cs, dp.plan, out);
+    API_END
+}
+
+int vmps_pivot_dim(const vmps_pivot* p, int64_t* out) {
+    if (!p || !out) return set_err(VMPS_E_ARG, "null argument");
+    *out = p->Vt.total;
+    return VMPS_OK;
+}
+
+int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int prec) {
+    API_BEGIN
+    if (!p || !vin || !vout) return set_err(VMPS_E_ARG, "null argument");
+    require_device(p->ctx);
+    cudaStream_t st = p->st();
+    const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
+    if (!p->stage_in.p) {
+        p->stage_in.alloc(cb, st, false);
+        p->stage_out.alloc(cb, st, false);
+        p->vin.alloc((size_t)p->Vd.total * 8, st, true);
+        p->vout.alloc((size_t)p->Vd.total * 8, st, true);
+    }
+    CK(cudaMemcpyAsync(p->stage_in.p, vin, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
+    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), p->vin.as<double>(), 1, st));
+    pivot_hxv_dev(p, prec, p->vin.as<double>(), p->vout.as<double>());
+    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->vout.as<double>(), p->stage_out.as<double>(), 0, st));
+    CK(cudaMemcpyAsync(vout, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    API_END
+}
+
+// ---- device vectors ---------------------------------------------------------
+int vmps_dvec_create(vmps_pivot* p, vmps_dvec** out) {
+    API_BEGIN
+    if (!p || !out) return set_err(VMPS_E_ARG, "null argument");
+    require_device(p->ctx);
+    auto* v = new vmps_dvec_s();
+    v->p = p;
+    v->n = p->Vd.total;
+    try { v->d.alloc((size_t)v->n * 8, p->st(), true); } catch (...) { delete v; throw; }
+    *out = v;
+    API_END
+}
+int vmps_dvec_destroy(vmps_dvec* v) {
+    if (v) { cudaStreamSynchronize(v->p->st()); delete v; }
+    return VMPS_OK;
+}
+int vmps_dvec_upload(vmps_dvec* v, const double* host) {
+    API_BEGIN
+    if (!v || !host) return set_err(VMPS_E_ARG, "null argument");
+    vmps_pivot* p = v->p;
+    cudaStream_t st = p->st();
+    if (!p->stage_in.p) {
+        const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
+        p->stage_in.alloc(cb, st, false);
+        p->stage_out.alloc(cb, st, false);
+    }
+    CK(cudaMemcpyAsync(p->stage_in.p, host, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
+    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), v->d.as<double>(), 1, st));
+    CK(cudaMemsetAsync(p->flag.p, 0, 4, st));
+    CK(launch_finite(v->d.as<double>(), v->n, p->flag.as<int>(), st));
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, p->flag.p, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (bad) return set_err(VMPS_E_NONFINITE, "input vector holds NaN or Inf");
+    API_END
+}
+int vmps_dvec_download(const vmps_dvec* v, double* host) {
+    API_BEGIN
+    if (!v || !host) return set_err(VMPS_E_ARG, "null argument");
+    vmps_pivot* p = v->p;
+    cudaStream_t st = p->st();
+    if (!p->stage_out.p) {
+        const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
+        p->stage_in.alloc(cb, st, false);
+        p->stage_out.alloc(cb, st, false);
+    }
+    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, v->d.as<double>(), p->stage_out.as<double>(), 0, st));
+    CK(cudaMemcpyAsync(host, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    API_END
+}
+int vmps_hxv_device(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec) {
+    API_BEGIN
+    if (!p || !vin || !vout || vin->p != p || vout->p != p) return set_err(VMPS_E_ARG, "vectors of another pivot");
+    if (vin == vout) return set_err(VMPS_E_ARG, "HxV needs distinct input and output vectors");
+    pivot_hxv_dev(p, prec, vin->d.as<double>(), vout->d.as<double>());
+    API_END
+}
+int vmps_dvec_dot(const vmps_dvec* a, const vmps_dvec* b, double* out) {
+    API_BEGIN
+    if (!a || !b || !out || a->p != b->p) return set_err(VMPS_E_ARG, "bad vectors");
+    vmps_pivot* p = a->p;
+    CK(launch_dot(a->d.as<double>(), b->d.as<double>(), a->n, p->part.as<double>(), p->scal.as<double>(), p->st()));
+    CK(cudaMemcpyAsync(out, p->scal.p, 8, cudaMemcpyDeviceToHost, p->st()));
+    CK(cudaStreamSynchronize(p->st()));
+    API_END
+}
+int vmps_dvec_axpy(double alpha, const vmps_dvec* x, vmps_dvec* y) {
+    API_BEGIN
+    if (!x || !y || x->p != y->p) return set_err(VMPS_E_ARG, "bad vectors");
+    CK(launch_axpy(alpha, x->d.as<double>(), y->d.as<double>(), x->n, x->p->st()));
+    API_END
+}
+int vmps_dvec_scale(vmps_dvec* x, double alpha) {
+    API_BEGIN
+    if (!x) return set_err(VMPS_E_ARG, "bad vector");
+    CK(launch_scale(alpha, x->d.as<double>(), x->n, x->p->st()));
+    API_END
+}
+int vmps_dvec_copy(const vmps_dvec* s, vmps_dvec* d) {
+    API_BEGIN
+    if (!s || !d || s->p != d->p) return set_err(VMPS_E_ARG, "bad vectors");
+    CK(cudaMemcpyAsync(d->d.p, s->d.p, (size_t)s->n * 8, cudaMemcpyDeviceToDevice, s->p->st()));
+    API_END
+}
+
+int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec, int n_iter, int use_graph,
+                  double* ms_per_hxv, double* ms_phase2) {
+    API_BEGIN
+    if (!p || !vin || !vout || n_iter <= 0) return set_err(VMPS_E_ARG, "bad argument");
+    cudaStream_t st = p->st();
+    DevPlan& dp = get_plan(p, prec);
+    const double* vi = vin->d.as<double>();
+    double* vo = vout->d.as<double>();
+    // phase-2 share: time phase 2 alone once
+    Operands ops;
+    if (prec == VMPS_PREC_FP64) { ops.X = p->dL.p; ops.Z = p->dR.p; }
+    else { ops.X = p->dL32.p; ops.tx = 1; ops.Z = p->dR32.p; ops.tz = 1; }
+    ops.Y = vi; ops.O = vo;
+    if (use_graph) {
+        if (!p->graph[prec] || p->graph_in[prec] != vi || p->graph_out[prec] != vo) {
+            if (p->graph[prec]) { cudaGraphExecDestroy(p->graph[prec]); p->graph[prec] = nullptr; }
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            run_plan(dp, prec, ops, st);
+            CK(cudaStreamEndCapture(st, &g));
+            cudaGraphExec_t ge;
+            CK(cudaGraphInstantiate(&ge, g, 0));
+            cudaGraphDestroy(g);
+            p->graph[prec] = ge;
+            p->graph_in[prec] = vi;
+            p->graph_out[prec] = vo;
+        }
+    }
+    auto one = [&]() {
+        if (use_graph) CK(cudaGraphLaunch(p->graph[prec], st));
+        else run_plan(dp, prec, ops, st);
+    };
+    one();
+    CK(cudaStreamSynchronize(st));
+    CK(cudaEventRecord(p->ctx->ev0, st));
+    for (int i = 0; i < n_iter; ++i) one();
+    CK(cudaEventRecord(p->ctx->ev1, st));
+    CK(cudaEventSynchronize(p->ctx->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, p->ctx->ev0, p->ctx->ev1));
+    if (ms_per_hxv) *ms_per_hxv = ms / n_iter;
+    if (ms_phase2) {
+        // time phase 2 alone: run phase 1 once to fill T, then phase 2 n_iter times
+        GGArgs a{};
+        const PhasePlan& h = dp.plan.p2;
+        int ta = prec == VMPS_PREC_FP64 ? 0 : 1, tb, tc = 0;
+        a.A = dp.T.p;
+        a.B = h.slotB == SLOT_Z ? ops.Z : ops.X;
+        tb = h.slotB == SLOT_Z ? ops.tz : ops.tx;
+        a.C = vo;
+        a.tiles = dp.p2.tiles.as<GTile>();
+        a.segs = dp.p2.segs.as<GSeg>();
+        a.terms = dp.p2.terms.as<GTerm>();
+        a.ntiles = dp.p2.ntiles;
+        a.transA = h.transA; a.transB = h.transB; a.transC = h.transC;
+        CK(cudaEventRecord(p->ctx->ev0, st));
+        for (int i = 0; i < n_iter; ++i) CK(launch_gg(prec, ta, tb, tc, a, st));
+        CK(cudaEventRecord(p->ctx->ev2, st));
+        CK(cudaEventSynchronize(p->ctx->ev2));
+        float ms2 = 0;
+        CK(cudaEventElapsedTime(&ms2, p->ctx->ev0, p->ctx->ev2));
+        *ms_phase2 = ms2 / n_iter;
+    }
+    API_END
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Lanczos (FP64 Krylov vectors, host tridiagonal solve)
+// ---------------------------------------------------------------------------
+namespace {
+// lowest eigenpair of the symmetric tridiagonal matrix (a: diagonal, b: off-diagonal)
+// Sturm-sequence bisection for the eigenvalue, inverse iteration for the vector.
+double sturm_count_below(const std::vector<double>& a, const std::vector<double>& b, double x) {
+    int cnt = 0;
+    double d = 1.0;
+    const size_t n = a.size();
+    for (size_t i = 0; i < n; ++i) {
+        double bb = i ? b[i - 1] * b[i - 1] : 0.0;
+        d = (a[i] - x) - (i ? bb / d : 0.0);
+        if (d == 0.0) d = -1e-300;
+        if (d < 0) ++cnt;
+    }
+    return cnt;
+}
+void tridiag_lowest(const std::vector<double>& a, const std::vector<double>& b, double& theta, std::vector<double>& y) {
+    const size_t n = a.size();
+    double lo = a[0], hi = a[0];
+    for (size_t i = 0; i < n; ++i) {
+        double r = (i ? std::abs(b[i - 1]) : 0.0) + (i + 1 < n ? std::abs(b[i]) : 0.0);
+        lo = std::min(lo, a[i] - r);
+        hi = std::max(hi, a[i] + r);
+    }
+    double scale = std::max(std::abs(lo), std::abs(hi)) + 1e-300;
+    for (int it = 0; it < 200 && hi - lo > 1e-16 * scale; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (sturm_count_below(a, b, mid) >= 1) hi = mid; else lo = mid;
+    }
+    theta = 0.5 * (lo + hi);
+    // inverse iteration on (T - shift): tridiagonal LU with partial pivoting
+    // (the elimination of LAPACK dgttrf/dgtts2, restated)
+    y.assign(n, 1.0 / std::sqrt((double)n));
+    const double shift = theta - 1e-13 * scale;
+    std::vector<double> d(n), du(n, 0.0), du2(n, 0.0), dl(n, 0.0);
+    std::vector<char> swp(n, 0);
+    for (size_t i = 0; i < n; ++i) d[i] = a[i] - shift;
+    for (size_t i = 0; i + 1 < n; ++i) { du[i] = b[i]; dl[i] = b[i]; }
+    for (size_t i = 0; i + 1 < n; ++i) {
+        if (std::abs(d[i]) >= std::abs(dl[i])) {
+            const double f = d[i] != 0.0 ? dl[i] / d[i] : 0.0;
+            dl[i] = f;
+            d[i + 1] -= f * du[i];
+        } else {
+            const double f = d[i] / dl[i];
+            d[i] = dl[i];
+            dl[i] = f;
+            const double t = du[i];
+            du[i] = d[i + 1];
+            d[i + 1] = t - f * d[i + 1];
+            if (i + 2 < n) { du2[i] = du[i + 1]; du[i + 1] = -f * du[i + 1]; }
+            swp[i] = 1;
+        }
+    }
+    for (size_t i = 0; i < n; ++i) if (d[i] == 0.0) d[i] = 1e-300;
+    for (int it = 0; it < 3; ++it) {
+        std::vector<double> x = y;
+        for (size_t i = 0; i + 1 < n; ++i) {
+            if (!swp[i]) x[i + 1] -= dl[i] * x[i];
+            else { const double t = x[i]; x[i] = x[i + 1]; x[i + 1] = t - dl[i] * x[i]; }
+        }
+        for (size_t ii = n; ii-- > 0;) {
+            double s = x[ii];
+            if (ii + 1 < n) s -= du[ii] * x[ii + 1];
+            if (ii + 2 < n) s -= du2[ii] * x[ii + 2];
+            x[ii] = s / d[ii];
+        }
+        double nrm = 0;
+        for (double v : x) nrm += v * v;
+        nrm = std::sqrt(nrm);
+        for (size_t i = 0; i < n; ++i) y[i] = x[i] / nrm;
+    }
+    // fix sign convention: largest component positive
+    size_t im = 0;
+    for (size_t i = 1; i < n; ++i) if (std::abs(y[i]) > std::abs(y[im])) im = i;
+    if (y[im] < 0) for (double& v : y) v = -v;
+}
+
+struct Krylov {
+    vmps_pivot* p;
+    int64_t n;
+    DBuf basis;     // [kmax+1][n]
+    DBuf w, tmp;
+    DBuf coef;      // device coefficients
+    int kmax;
+    double* K(int j) const { return basis.as<double>() + (int64_t)j * n; }
+};
+
+double dev_dot(vmps_pivot* p, const double* x, const double* y, int64_t n) {
+    CK(launch_dot(x, y, n, p->part.as<double>(), p->scal.as<double>(), p->st()));
+    double r;
+    CK(cudaMemcpyAsync(&r, p->scal.p, 8, cudaMemcpyDeviceToHost, p->st()));
+    CK(cudaStreamSynchronize(p->st()));
+    return r;
+}
+
+// one Lanczos run from K(0) (normalised on entry); returns the Ritz value and
+// leaves the Ritz vector in `x`
+double lanczos_run(Krylov& kr, int prec, int max_iter, double tol_eigval, double tol_state, double* x, int* iters,
+                   int* hxvs) {
+    vmps_pivot* p = kr.p;
+    cudaStream_t st = p->st();
+    const int64_t n = kr.n;
+    std::vector<double> alpha, beta;
+    double theta = 0, theta_prev = 1e300;
+    std::vector<double> y;
+    int j = 0;
+    const int kmax = std::min(max_iter, kr.kmax);
+    for (j = 0; j < kmax; ++j) {
+        double* w = kr.w.as<double>();
+        pivot_hxv_dev(p, prec, kr.K(j), w);
+        (*hxvs)++;
+        // full reorthogonalisation against K(0..j) twice (classical Gram-Schmidt, "twice is enough")
+        double a_j = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+            CK(launch_mdot(kr.basis.as<double>(), j + 1, n, w, p->part.as<double>(), kr.coef.as<double>(), st));
+            CK(launch_mgs(kr.basis.as<double>(), j + 1, n, kr.coef.as<double>(), w, st));
+            double cj;
+            CK(cudaMemcpyAsync(&cj, kr.coef.as<double>() + j, 8, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            a_j += cj;
+        }
+        alpha.push_back(a_j);
+        double b_j = std::sqrt(std::max(0.0, dev_dot(p, w, w, n)));
+        tridiag_lowest(alpha, beta, theta, y);
+        const double res = std::abs(b_j * y.back());
+        const bool conv_e = std::abs(theta - theta_prev) <= tol_eigval * std::max(1.0, std::abs(theta));
+        theta_prev = theta;
+        if ((conv_e && res <= tol_state) || b_j <= 1e-14 * std::max(1.0, std::abs(theta)) || j + 1 == kmax) {
+            ++j;
+            break;
+        }
+        beta.push_back(b_j);
+        CK(cudaMemcpyAsync(kr.K(j + 1), w, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        CK(launch_scale(1.0 / b_j, kr.K(j + 1), n, st));
+    }
+    *iters = j;
+    // Ritz vector x = K y
+    CK(cudaMemcpyAsync(kr.coef.p, y.data(), y.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(launch_combine(kr.basis.as<double>(), (int)y.size(), n, kr.coef.as<double>(), x, st));
+    double nx = std::sqrt(dev_dot(p, x, x, n));
+    CK(launch_scale(1.0 / nx, x, n, st));
+    return theta;
+}
+}  // namespace
+
+extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_iter, double tol_eigval,
+                                   double tol_state, int refine_iters, double* energy, vmps_lanczos_stats* stats) {
+    API_BEGIN
+    if (!p || !v || !energy || max_iter <= 0) return set_err(VMPS_E_ARG, "bad argument");
+    require_device(p->ctx);
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t st = p->st();
+    Krylov kr;
+    kr.p = p;
+    kr.n = p->Vd.total;
+    kr.kmax = std::max(max_iter, refine_iters) + 1;
+    kr.basis.alloc((size_t)(kr.kmax + 1) * kr.n * 8, st, true);
+    kr.w.alloc((size_t)kr.n * 8, st, true);
+    kr.tmp.alloc((size_t)kr.n * 8, st, true);
+    kr.coef.alloc((size_t)(kr.kmax + 2) * 8, st, true);
+    // start vector
+    const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
+    if (!p->stage_in.p) { p->stage_in.alloc(cb, st, false); p->stage_out.alloc(cb, st, false); }
+    CK(cudaMemcpyAsync(p->stage_in.p, v, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
+    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), kr.K(0), 1, st));
+    double n0 = std::sqrt(dev_dot(p, kr.K(0), kr.K(0), kr.n));
+    if (!(n0 > 0) || !std::isfinite(n0)) return set_err(VMPS_E_NONFINITE, "start vector is zero or not finite");
+    CK(launch_scale(1.0 / n0, kr.K(0), kr.n, st));
+    vmps_lanczos_stats s{};
+    int it = 0, hx = 0;
+    double* x = kr.tmp.as<double>();
+    double e = lanczos_run(kr, prec, max_iter, tol_eigval, tol_state, x, &it, &hx);
+    s.iterations = it;
+    s.energy_first = e;
+    if (prec == VMPS_PREC_FP64) s.hxv_fp64 = hx; else s.hxv_split = hx;
+    if (prec != VMPS_PREC_FP64 && refine_iters > 0) {
+        // FP64 refinement: restart Lanczos from the split-precision Ritz vector with FP64 HxV
+        CK(cudaMemcpyAsync(kr.K(0), x, (size_t)kr.n * 8, cudaMemcpyDeviceToDevice, st));
+        int it2 = 0, hx2 = 0;
+        e = lanczos_run(kr, VMPS_PREC_FP64, refine_iters, tol_eigval, tol_state, x, &it2, &hx2);
+        s.refine_iterations = it2;
+        s.hxv_fp64 += hx2;
+    }
+    // residual ||H x - E x|| with FP64 HxV
+    pivot_hxv_dev(p, VMPS_PREC_FP64, x, kr.w.as<double>());
+    s.hxv_fp64++;
+    CK(launch_axpy(-e, x, kr.w.as<double>(), kr.n, st));
+    s.residual = std::sqrt(dev_dot(p, kr.w.as<double>(), kr.w.as<double>(), kr.n));
+    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, x, p->stage_out.as<double>(), 0, st));
+    CK(cudaMemcpyAsync(v, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *energy = e;
+    s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = s;
+    API_END
+}
+
+// ---------------------------------------------------------------------------
+// environment updates
+// ---------------------------------------------------------------------------
+struct vmps_env_s {
+    vmps_ctx* ctx = nullptr;
+    Symmetry sym;
+    int side = 0;
+    BlockTable Et, Bt, Kt, Nt;   // old env, bra, ket, new env
+    DevLayout Ed, Bd, Kd, Nd;
+    ChainSet cs;
+    DevPlan plans[2];
+    DBuf dE, dB, dK, dN, stage, pkN;
+    cudaStream_t st() const { return ctx->stream; }
+};
+
+static DevPlan& env_plan(vmps_env* e, int prec) {
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
+    DevPlan& dp = e->plans[prec];
+    if (dp.ready) return dp;
+    const int te = tile_edge(prec);
+    if (e->side == VMPS_ENV_LEFT)   // X = Abra^dagger, Y = Eold, Z = Aket
+        dp.plan = make_plan(e->cs, e->Bd, e->Ed, e->Kd, e->Nd, true, false, te, te);
+    else                            // X = Aket, Y = Eold, Z = Abra^dagger
+        dp.plan = make_plan(e->cs, e->Kd, e->Ed, e->Bd, e->Nd, false, true, te, te);
+    if (e->ctx->device < 0) { dp.ready = true; return dp; }
+    dp.p1.upload(dp.plan.p1, e->st());
+    dp.p2.upload(dp.plan.p2, e->st());
+    dp.T.alloc((size_t)dp.plan.T.total * (prec == VMPS_PREC_FP64 ? 8 : 4), e->st(), true);
+    CK(cudaStreamSynchronize(e->st()));
+    dp.ready = true;
+    return dp;
+}
+
+extern "C" {
+
+int vmps_env_create(vmps_ctx* ctx, const vmps_symmetry* symd, int side, const vmps_blocks* Eold,
+                    const vmps_blocks* Abra, const vmps_mpo_site* W, const vmps_blocks* Aket, vmps_env** out) {
+    API_BEGIN
+    if (!ctx || !out) return set_err(VMPS_E_ARG, "null argument");
+    if (side != VMPS_ENV_LEFT && side != VMPS_ENV_RIGHT) return set_err(VMPS_E_ARG, "side must be LEFT or RIGHT");
+    Symmetry sym = make_sym(symd);
+    std::unique_ptr<vmps_env> e(new vmps_env_s());
+    e->ctx = ctx;
+    e->sym = sym;
+    e->side = side;
+    e->Et = parse_blocks(sym, Eold, true);
+    e->Bt = parse_blocks(sym, Abra, false);
+    e->Kt = parse_blocks(sym, Aket, false);
+    MpoView Wv = parse_mpo(sym, W);
+    e->cs = build_env(sym, side, e->Et, e->Bt, Wv, e->Kt, &e->Nt);
+    e->Ed = make_dev_layout(e->Et.rows, e->Et.cols);
+    e->Bd = make_dev_layout(e->Bt.rows, e->Bt.cols);
+    e->Kd = make_dev_layout(e->Kt.rows, e->Kt.cols);
+    e->Nd = make_dev_layout(e->Nt.rows, e->Nt.cols);
+    *out = e.release();
+    API_END
+}
+
+int vmps_env_layout(const vmps_env* e, int64_t* nblocks, int64_t* total) {
+    if (!e || !nblocks || !total) return set_err(VMPS_E_ARG, "null argument");
+    *nblocks = e->Nt.n;
+    *total = e->Nt.total;
+    return VMPS_OK;
+}
+
+int vmps_env_layout_get(const vmps_env* e, int32_t* qin, int32_t* qout, int32_t* qmid, int32_t* leg, int64_t* rows,
+                        int64_t* cols, int64_t* offset) {
+    if (!e) return set_err(VMPS_E_ARG, "null argument");
+    const int nq = e->sym.nq;
+    for (int64_t i = 0; i < e->Nt.n; ++i) {
+        for (int c = 0; c < nq; ++c) {
+            if (qin) qin[i * nq + c] = e->Nt.qin[i].v[c];
+            if (qout) qout[i * nq + c] = e->Nt.qout[i].v[c];
+            if (qmid) qmid[i * nq + c] = e->Nt.qmid[i].v[c];
+        }
+        if (leg) leg[i] = e->Nt.leg[i];
+        if (rows) rows[i] = e->Nt.rows[i];
+        if (cols) cols[i] = e->Nt.cols[i];
+        if (offset) offset[i] = e->Nt.off[i];
+    }
+    return VMPS_OK;
+}
+
+int vmps_env_stats(const vmps_env* ec, int prec, vmps_plan_stats* out) {
+    API_BEGIN
+    if (!ec || !out) return set_err(VMPS_E_ARG, "null argument");
+    auto* e = const_cast<vmps_env*>(ec);
+    DevPlan& dp = env_plan(e, prec);
+    fill_stats(e->cs, dp.plan, out);
+    API_END
+}
+
+int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra, const double* Aket, double* Enew, int prec) {
+    API_BEGIN
+    if (!e || !Eold || !Abra || !Aket || !Enew) return set_err(VMPS_E_ARG, "null argument");
+    require_device(e->ctx);
+    CK(cudaSetDevice(e->ctx->device));
+    cudaStream_t st = e->st();
+    DevPlan& dp = env_plan(e, prec);
+    upload_blocks_padded(e->Et, e->Ed, Eold, e->dE, st);
+    upload_blocks_padded(e->Bt, e->Bd, Abra, e->dB, st);
+    upload_blocks_padded(e->Kt, e->Kd, Aket, e->dK, st);
+    e->dN.alloc((size_t)e->Nd.total * 8, st, true);
+    Operands ops;
+    if (e->side == VMPS_ENV_LEFT) { ops.X = e->dB.p; ops.Z = e->dK.p; }
+    else { ops.X = e->dK.p; ops.Z = e->dB.p; }
+    ops.Y = e->dE.p;
+    ops.O = e->dN.p;
+    run_plan(dp, prec, ops, st);
+    if (!e->pkN.p) {
+        auto pb = pack_blocks(e->Nt, e->Nd, nullptr);
+        upload_vec(e->pkN, pb, st);
+    }
+    e->stage.alloc((size_t)std::max<int64_t>(e->Nt.total, 1) * 8, st, false);
+    CK(launch_pack(e->pkN.as<PackBlock>(), (int)e->Nt.n, e->dN.as<double>(), e->stage.as<double>(), 0, st));
+    if (e->Nt.total > 0)
+        CK(cudaMemcpyAsync(Enew, e->stage.p, (size_t)e->Nt.total * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    API_END
+}
+
+int vmps_env_destroy(vmps_env* e) {
+    if (e) { cudaStreamSynchronize(e->st()); delete e; }
+    return VMPS_OK;
+}
+
+}  // extern "C"

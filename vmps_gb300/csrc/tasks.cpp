@@ -1,0 +1,834 @@
+// Host-side task-list builder and grouped-GEMM planner.
+//
+// The builders restate the quantum-number matching of VMPS:
+//   LAWA    tensors/DmrgIndexGymnastics.h:32-77
+//   AWAR    tensors/DmrgIndexGymnastics.h:79-124
+//   AAWWAA  tensors/DmrgIndexGymnastics.h:198-262
+//   precalc_blockStructure (1-site) :487-590, (2-site) :699-856
+//   OxV loops pivot/DmrgPivotMatrix1.h:222-266, pivot/DmrgPivotMatrix2.h:182-230
+//   HxV(PivotMatrix0) pivot/DmrgPivotMatrix0.h:37-95
+//   contract_L tensors/DmrgContractions.h:35-158, contract_R :180-311
+// and emit one Chain per (task, W nonzero) product with the SU(2) prefactor and
+// the W value folded into a single scalar.  The planner then merges duplicate
+// chains, shares first-stage products and lays the work out as tile lists.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <stdexcept>
+#include <tuple>
+
+#include "engine.hpp"
+
+namespace vmps {
+
+// ===========================================================================
+// SU(2) recoupling symbols: Racah formula for 6j, 9j as a sum of 6j products
+// ===========================================================================
+namespace {
+struct Factorials {
+    std::vector<long double> lf;   // log factorials
+    Factorials() {
+        lf.resize(512);
+        lf[0] = 0;
+        for (int i = 1; i < 512; ++i) lf[i] = lf[i - 1] + std::log((long double)i);
+    }
+};
+const Factorials& facts() { static Factorials f; return f; }
+
+bool tri2(int a, int b, int c) {   // arguments are 2j
+    if (a < 0 || b < 0 || c < 0) return false;
+    if ((a + b + c) & 1) return false;
+    return c >= std::abs(a - b) && c <= a + b;
+}
+long double log_delta(int a, int b, int c) {   // 2j arguments, triangle already checked
+    const auto& f = facts().lf;
+    return 0.5L * (f[(a + b - c) / 2] + f[(a - b + c) / 2] + f[(-a + b + c) / 2] - f[(a + b + c) / 2 + 1]);
+}
+}  // namespace
+
+double coupling_6j(int j1, int j2, int j3, int j4, int j5, int j6) {
+    if (!tri2(j1, j2, j3) || !tri2(j1, j5, j6) || !tri2(j4, j2, j6) || !tri2(j4, j5, j3)) return 0.0;
+    const auto& f = facts().lf;
+    const int a1 = (j1 + j2 + j3) / 2, a2 = (j1 + j5 + j6) / 2, a3 = (j4 + j2 + j6) / 2, a4 = (j4 + j5 + j3) / 2;
+    const int b1 = (j1 + j2 + j4 + j5) / 2, b2 = (j2 + j3 + j5 + j6) / 2, b3 = (j3 + j1 + j6 + j4) / 2;
+    const int tmin = std::max(std::max(a1, a2), std::max(a3, a4));
+    const int tmax = std::min(b1, std::min(b2, b3));
+    const long double pre = log_delta(j1, j2, j3) + log_delta(j1, j5, j6) + log_delta(j4, j2, j6) + log_delta(j4, j5, j3);
+    long double sum = 0;
+    for (int t = tmin; t <= tmax; ++t) {
+        long double lt = f[t + 1] - f[t - a1] - f[t - a2] - f[t - a3] - f[t - a4] - f[b1 - t] - f[b2 - t] - f[b3 - t];
+        long double term = std::exp(lt + pre);
+        sum += (t & 1) ? -term : term;
+    }
+    return (double)sum;
+}
+
+double coupling_9j(int j1, int j2, int j3, int j4, int j5, int j6, int j7, int j8, int j9) {
+    // {j1 j2 j3; j4 j5 j6; j7 j8 j9} = sum_x (-1)^{2x} (2x+1) {j1 j4 j7; j8 j9 x}{j2 j5 j8; j4 x j6}{j3 j6 j9; x j1 j2}
+    if (!tri2(j1, j2, j3) || !tri2(j4, j5, j6) || !tri2(j7, j8, j9) || !tri2(j1, j4, j7) || !tri2(j2, j5, j8) ||
+        !tri2(j3, j6, j9))
+        return 0.0;
+    int xmin = std::max(std::abs(j1 - j9), std::max(std::abs(j4 - j8), std::abs(j2 - j6)));
+    int xmax = std::min(j1 + j9, std::min(j4 + j8, j2 + j6));
+    long double sum = 0;
+    for (int x = xmin; x <= xmax; x += 2) {
+        long double t = (long double)(x + 1) * coupling_6j(j1, j4, j7, j8, j9, x) * coupling_6j(j2, j5, j8, j4, x, j6) *
+                        coupling_6j(j3, j6, j9, x, j1, j2);
+        sum += (x & 1) ? -t : t;   // (-1)^{2x} with 2x = x here
+    }
+    return (double)sum;
+}
+
+// ===========================================================================
+// parsing
+// ===========================================================================
+static QN read_qn(const Symmetry& sym, const int32_t* p, int64_t i) {
+    QN q;
+    for (int c = 0; c < sym.nq; ++c) q.v[c] = p[i * sym.nq + c];
+    return q;
+}
+
+BlockTable parse_blocks(const Symmetry& sym, const vmps_blocks* b, bool need_mid) {
+    BlockTable t;
+    if (!b) throw std::invalid_argument("null block table");
+    t.n = b->nblocks;
+    if (t.n < 0) throw std::invalid_argument("negative block count");
+    if (t.n > 0 && (!b->qin || !b->qout || !b->leg || !b->rows || !b->cols || !b->offset))
+        throw std::invalid_argument("block table with null arrays");
+    if (need_mid && t.n > 0 && !b->qmid) throw std::invalid_argument("Tripod table needs qmid");
+    t.has_mid = b->qmid != nullptr;
+    t.qin.resize(t.n); t.qout.resize(t.n); t.leg.resize(t.n);
+    t.rows.resize(t.n); t.cols.resize(t.n); t.off.resize(t.n);
+    if (t.has_mid) t.qmid.resize(t.n);
+    for (int64_t i = 0; i < t.n; ++i) {
+        t.qin[i] = read_qn(sym, b->qin, i);
+        t.qout[i] = read_qn(sym, b->qout, i);
+        if (t.has_mid) t.qmid[i] = read_qn(sym, b->qmid, i);
+        t.leg[i] = b->leg[i];
+        t.rows[i] = b->rows[i];
+        t.cols[i] = b->cols[i];
+        t.off[i] = b->offset[i];
+        if (t.rows[i] <= 0 || t.cols[i] <= 0 || t.off[i] < 0 || t.leg[i] < 0)
+            throw std::invalid_argument("block " + std::to_string(i) + " has non-positive shape or negative offset/leg");
+        t.total = std::max(t.total, t.off[i] + t.rows[i] * t.cols[i]);
+    }
+    return t;
+}
+
+TripodView make_tripod_view(const BlockTable& t) {
+    TripodView v;
+    for (int64_t i = 0; i < t.n; ++i) {
+        QN3 key{{t.qin[i], t.qout[i], t.qmid[i]}};
+        auto it = v.dict.find(key);
+        int q;
+        if (it == v.dict.end()) {
+            q = (int)v.keys.size();
+            v.dict.emplace(key, q);
+            v.keys.push_back(key);
+            v.aux.emplace_back();
+        } else {
+            q = it->second;
+        }
+        auto& a = v.aux[q];
+        if ((int)a.size() <= t.leg[i]) a.resize(t.leg[i] + 1, -1);
+        if (a[t.leg[i]] != -1) throw std::invalid_argument("duplicate Tripod block");
+        a[t.leg[i]] = i;
+    }
+    return v;
+}
+
+BipedsView make_bipeds_view(const BlockTable& t, int nlegs) {
+    BipedsView v;
+    int maxleg = nlegs;
+    for (int64_t i = 0; i < t.n; ++i) maxleg = std::max(maxleg, t.leg[i] + 1);
+    v.dict.resize(maxleg);
+    for (int64_t i = 0; i < t.n; ++i) {
+        auto r = v.dict[t.leg[i]].emplace(QN2{{t.qin[i], t.qout[i]}}, i);
+        if (!r.second) throw std::invalid_argument("duplicate Biped block");
+    }
+    return v;
+}
+
+MpoView parse_mpo(const Symmetry& sym, const vmps_mpo_site* W) {
+    if (!W) throw std::invalid_argument("null MPO site");
+    MpoView m;
+    m.nloc = W->nloc;
+    m.nop = W->nop;
+    if (m.nloc <= 0 || m.nop <= 0) throw std::invalid_argument("MPO site needs nloc>0 and nop>0");
+    for (int i = 0; i < m.nloc; ++i) m.qloc.push_back(read_qn(sym, W->qloc, i));
+    for (int i = 0; i < m.nop; ++i) m.qop.push_back(read_qn(sym, W->qop, i));
+    m.blocks.resize((size_t)m.nloc * m.nloc * m.nop);
+    for (int64_t i = 0; i < W->nnz; ++i) {
+        int s1 = W->s1[i], s2 = W->s2[i], k = W->k[i];
+        if (s1 < 0 || s1 >= m.nloc || s2 < 0 || s2 >= m.nloc || k < 0 || k >= m.nop || W->row[i] < 0 || W->col[i] < 0)
+            throw std::invalid_argument("MPO entry out of range");
+        QN2 key{{read_qn(sym, W->qin, i), read_qn(sym, W->qout, i)}};
+        m.blocks[((size_t)s1 * m.nloc + s2) * m.nop + k][key].push_back(MpoNz{W->row[i], W->col[i], W->val[i]});
+    }
+    return m;
+}
+
+// ===========================================================================
+// chain cost (DmrgExternal.h:147-159): (AB)C = mkn + mnp, A(BC) = knp + mkp
+// ===========================================================================
+static inline double chain_flops(double m, double k, double n, double p) {
+    return 2.0 * std::min(m * k * n + m * n * p, k * n * p + m * k * p);
+}
+
+// ===========================================================================
+// 1-site effective Hamiltonian (PivotMatrix1)
+// ===========================================================================
+ChainSet build_pivot1(const Symmetry& sym, const BlockTable& L, const BlockTable& R, const MpoView& W,
+                      const BlockTable& V) {
+    ChainSet cs;
+    TripodView Lv = make_tripod_view(L), Rv = make_tripod_view(R);
+    BipedsView Vv = make_bipeds_view(V, W.nloc);
+    const double eps = 2.220446049250313e-16;
+    for (int s1 = 0; s1 < W.nloc; ++s1)
+    for (int s2 = 0; s2 < W.nloc; ++s2)
+    for (int k = 0; k < W.nop; ++k) {
+        if (!sym.triangle(W.qloc[s2], W.qop[k], W.qloc[s1])) continue;
+        for (int qL = 0; qL < (int)Lv.keys.size(); ++qL) {
+            const QN& Lin = Lv.keys[qL].q[0];
+            const QN& Lout = Lv.keys[qL].q[1];
+            const QN& Lmid = Lv.keys[qL].q[2];
+            // LAWA (tensors/DmrgIndexGymnastics.h:32-77) with Abra = Aket = Vin
+            for (const QN& Rout : sym.reduce(Lin, W.qloc[s1])) {
+                int64_t qAbra = Vv.find(s1, Lin, Rout);
+                if (qAbra < 0) continue;
+                for (const QN& Rin : sym.reduce(Lout, W.qloc[s2])) {
+                    int64_t qAket = Vv.find(s2, Lout, Rin);
+                    if (qAket < 0) continue;
+                    for (const QN& Rmid : sym.reduce(Lmid, W.qop[k])) {
+                        const auto* nz = W.find(s1, s2, k, Lmid, Rmid);
+                        if (!nz) continue;
+                        if (!sym.triangle(Rin, Rmid, Rout)) continue;
+                        auto itR = Rv.dict.find(QN3{{Rin, Rout, Rmid}});
+                        if (itR == Rv.dict.end()) continue;
+                        const int qR = itR->second;
+                        bool any = false;
+                        for (const auto& e : *nz)
+                            if (Lv.at(qL, e.row) >= 0 && Rv.at(qR, e.col) >= 0) { any = true; break; }
+                        if (!any) continue;
+                        double cgc = 1.0;
+                        if (sym.nonabelian()) {
+                            QN q9[9] = {V.qin[qAket], W.qloc[s2], V.qout[qAket], Lmid, W.qop[k], Rmid,
+                                        V.qin[qAbra], W.qloc[s1], V.qout[qAbra]};
+                            cgc = sym.coeff_HPsi(q9);
+                        }
+                        if (std::abs(cgc) < eps) continue;
+                        cs.n_tasks++;
+                        for (const auto& e : *nz) {
+                            int64_t la = Lv.at(qL, e.row), rb = Rv.at(qR, e.col);
+                            if (la < 0 || rb < 0) continue;
+                            cs.n_chains_raw++;
+                            cs.flops_reference += chain_flops((double)L.rows[la], (double)L.cols[la],
+                                                              (double)V.cols[qAket], (double)R.cols[rb]);
+                            cs.chains.push_back(Chain{qAbra, la, qAket, rb, cgc * e.val});
+                        }
+                    }
+                }
+            }
+        }
+    }
+    return cs;
+}
+
+// ===========================================================================
+// Qbasis::combine of two local bases and the combined index s1s3
+// (tensors/Qbasis.h:685-798, leftOffset :438-463, tensors/Basis.h:79-124)
+// ===========================================================================
+CombinedBasis combine_bases(const Symmetry& sym, const std::vector<QN>& q12, const std::vector<QN>& q34) {
+    // Qbasis::pullData(qs): one entry per distinct QN in order of first appearance,
+    // repeated QNs enlarge that entry's plain basis (inner index = order of appearance)
+    auto pull = [](const std::vector<QN>& qs, std::vector<QN>& distinct, std::vector<int>& dim,
+                   std::vector<int>& inner, std::vector<int>& which) {
+        inner.resize(qs.size());
+        which.resize(qs.size());
+        for (size_t s = 0; s < qs.size(); ++s) {
+            auto it = std::find(distinct.begin(), distinct.end(), qs[s]);
+            int d;
+            if (it == distinct.end()) { d = (int)distinct.size(); distinct.push_back(qs[s]); dim.push_back(0); }
+            else d = (int)(it - distinct.begin());
+            inner[s] = dim[d]++;
+            which[s] = d;
+        }
+    };
+    std::vector<QN> d1, d2;
+    std::vector<int> dim1, dim2, in1, in2, w1, w2;
+    pull(q12, d1, dim1, in1, w1);
+    pull(q34, d2, dim2, in2, w2);
+    struct Src { QN a, b; int da, db; };
+    std::map<QN, std::vector<Src>> hist;   // keyed by merged QN
+    for (size_t i = 0; i < d1.size(); ++i)
+        for (size_t j = 0; j < d2.size(); ++j)
+            for (const QN& q : sym.reduce(d1[i], d2[j])) {
+                auto& h = hist[q];
+                bool dup = false;
+                for (auto& e : h) if (e.a == d1[i] && e.b == d2[j]) dup = true;
+                if (!dup) h.push_back(Src{d1[i], d2[j], dim1[i], dim2[j]});
+            }
+    // sort sources lexicographically (Symmetry::compare on std::array{q1,q2})
+    for (auto& kv : hist)
+        std::sort(kv.second.begin(), kv.second.end(), [](const Src& x, const Src& y) {
+            if (x.a != y.a) return x.a < y.a;
+            return x.b < y.b;
+        });
+    CombinedBasis cb;
+    std::map<QN, int> start;
+    int cur = 0;
+    for (auto& kv : hist) {   // std::map iterates QNs in ascending order (Qbasis::sort)
+        start[kv.first] = cur;
+        int tot = 0;
+        for (auto& e : kv.second) tot += e.da * e.db;
+        for (int t = 0; t < tot; ++t) cb.q_of.push_back(kv.first);
+        cur += tot;
+    }
+    cb.n = cur;
+    cb.index.resize(q12.size() * q34.size());
+    for (size_t s1 = 0; s1 < q12.size(); ++s1)
+        for (size_t s3 = 0; s3 < q34.size(); ++s3)
+            for (const QN& q : sym.reduce(q12[s1], q34[s3])) {
+                int off = 0;
+                for (auto& e : hist[q]) {
+                    if (e.a == q12[s1] && e.b == q34[s3]) {
+                        off += in1[s1] + e.da * in2[s3];   // Basis::fuseData::source: j = i1 + dim1*i2
+                        break;
+                    }
+                    off += e.da * e.db;
+                }
+                cb.index[s1 * q34.size() + s3].push_back({q, start[q] + off});
+            }
+    return cb;
+}
+
+// ===========================================================================
+// 2-site effective Hamiltonian (PivotMatrix2)
+// ===========================================================================
+ChainSet build_pivot2(const Symmetry& sym, const BlockTable& L, const BlockTable& R, const MpoView& W12,
+                      const MpoView& W34, const BlockTable& V) {
+    ChainSet cs;
+    TripodView Lv = make_tripod_view(L), Rv = make_tripod_view(R);
+    CombinedBasis cb = combine_bases(sym, W12.qloc, W34.qloc);
+    BipedsView Vv = make_bipeds_view(V, cb.n);
+    const double eps = 2.220446049250313e-16;
+    const int n12 = W12.nloc, n34 = W34.nloc;
+    for (int s1 = 0; s1 < n12; ++s1)
+    for (int s2 = 0; s2 < n12; ++s2)
+    for (int k12 = 0; k12 < W12.nop; ++k12) {
+        if (!sym.triangle(W12.qloc[s2], W12.qop[k12], W12.qloc[s1])) continue;
+        for (int s3 = 0; s3 < n34; ++s3)
+        for (int s4 = 0; s4 < n34; ++s4)
+        for (int k34 = 0; k34 < W34.nop; ++k34) {
+            if (!sym.triangle(W34.qloc[s4], W34.qop[k34], W34.qloc[s3])) continue;
+            for (const QN& qOp : sym.reduce(W12.qop[k12], W34.qop[k34])) {
+                for (const auto& m13 : cb.index[s1 * n34 + s3])
+                for (const auto& m24 : cb.index[s2 * n34 + s4]) {
+                    const QN& qmerge13 = m13.first;
+                    const QN& qmerge24 = m24.first;
+                    const int s1s3 = m13.second, s2s4 = m24.second;
+                    double cgc9 = 1.0;
+                    if (sym.nonabelian()) {
+                        QN q9[9] = {W12.qloc[s2], W34.qloc[s4], qmerge24, W12.qop[k12], W34.qop[k34], qOp,
+                                    W12.qloc[s1], W34.qloc[s3], qmerge13};
+                        cgc9 = sym.coeff_tensorProd(q9);
+                    }
+                    if (std::abs(cgc9) < eps) continue;
+                    for (int qL = 0; qL < (int)Lv.keys.size(); ++qL) {
+                        const QN& Lin = Lv.keys[qL].q[0];
+                        const QN& Lout = Lv.keys[qL].q[1];
+                        const QN& Lmid = Lv.keys[qL].q[2];
+                        // AAWWAA (tensors/DmrgIndexGymnastics.h:198-262)
+                        for (const QN& qRout : sym.reduce(Lin, qmerge13)) {
+                            int64_t q13 = Vv.find(s1s3, Lin, qRout);
+                            if (q13 < 0) continue;
+                            for (const QN& qRin : sym.reduce(Lout, qmerge24)) {
+                                int64_t q24 = Vv.find(s2s4, Lout, qRin);
+                                if (q24 < 0) continue;
+                                for (const QN& qW : sym.reduce(Lmid, W12.qop[k12])) {
+                                    const auto* nz12 = W12.find(s1, s2, k12, Lmid, qW);
+                                    if (!nz12) continue;
+                                    for (const QN& qRmid : sym.reduce(qW, W34.qop[k34])) {
+                                        const auto* nz34 = W34.find(s3, s4, k34, qW, qRmid);
+                                        if (!nz34) continue;
+                                        if (!sym.triangle(qRin, qRmid, qRout)) continue;
+                                        double cgc6 = 1.0;
+                                        if (sym.nonabelian()) {
+                                            QN q6[6] = {Lmid, W12.qop[k12], qW, W34.qop[k34], qRmid, qOp};
+                                            cgc6 = sym.coeff_Apair(q6);
+                                        }
+                                        if (std::abs(cgc6) < eps) continue;
+                                        auto itR = Rv.dict.find(QN3{{qRin, qRout, qRmid}});
+                                        if (itR == Rv.dict.end()) continue;
+                                        const int qR = itR->second;
+                                        double cgcH = 1.0;
+                                        if (sym.nonabelian()) {
+                                            QN q9[9] = {V.qin[q24], qmerge24, V.qout[q24], Lmid, qOp, qRmid,
+                                                        V.qin[q13], qmerge13, V.qout[q13]};
+                                            cgcH = sym.coeff_HPsi(q9);
+                                        }
+                                        const double cgc = cgc6 * cgc9 * cgcH;
+                                        cs.n_tasks++;
+                                        // OxV(PivotMatrix2) inner loop, pivot/DmrgPivotMatrix2.h:202-228
+                                        for (const auto& e12 : *nz12)
+                                            for (const auto& e34 : *nz34) {
+                                                if (e12.col != e34.row) continue;
+                                                int64_t la = Lv.at(qL, e12.row), rb = Rv.at(qR, e34.col);
+                                                if (la < 0 || rb < 0) continue;
+                                                cs.n_chains_raw++;
+                                                cs.flops_reference +=
+                                                    chain_flops((double)L.rows[la], (double)L.cols[la],
+                                                                (double)V.cols[q24], (double)R.cols[rb]);
+                                                cs.chains.push_back(Chain{q13, la, q24, rb, cgc * e12.val * e34.val});
+                                            }
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    return cs;
+}
+
+// ===========================================================================
+// 0-site effective Hamiltonian (PivotMatrix0), pivot/DmrgPivotMatrix0.h:37-95
+// ===========================================================================
+ChainSet build_pivot0(const Symmetry& sym, const BlockTable& L, const BlockTable& R, const BlockTable& V) {
+    (void)sym;
+    ChainSet cs;
+    TripodView Lv = make_tripod_view(L), Rv = make_tripod_view(R);
+    BipedsView Vv = make_bipeds_view(V, 1);
+    for (int qL = 0; qL < (int)Lv.keys.size(); ++qL) {
+        const QN& Lin = Lv.keys[qL].q[0];
+        const QN& Lout = Lv.keys[qL].q[1];
+        const QN& Lmid = Lv.keys[qL].q[2];
+        auto itR = Rv.dict.find(QN3{{Lout, Lin, Lmid}});
+        if (itR == Rv.dict.end()) continue;
+        const int qR = itR->second;
+        int64_t qAin = Vv.find(0, Lout, Lout);
+        if (qAin < 0) continue;
+        const QN& Rout = Rv.keys[qR].q[1];
+        int64_t qAout = Vv.find(0, Rout, Rout);
+        if (qAout < 0) continue;
+        cs.n_tasks++;
+        const int na = (int)std::max(Lv.aux[qL].size(), Rv.aux[qR].size());
+        for (int a = 0; a < na; ++a) {
+            int64_t la = Lv.at(qL, a), ra = Rv.at(qR, a);
+            if (la < 0 || ra < 0) continue;
+            cs.n_chains_raw++;
+            cs.flops_reference += chain_flops((double)L.rows[la], (double)L.cols[la], (double)V.cols[qAin],
+                                              (double)R.cols[ra]);
+            cs.chains.push_back(Chain{qAout, la, qAin, ra, 1.0});
+        }
+    }
+    return cs;
+}
+
+// ===========================================================================
+// contract_L / contract_R (FULL mode), tensors/DmrgContractions.h:35-311
+// ===========================================================================
+ChainSet build_env(const Symmetry& sym, int side, const BlockTable& E, const BlockTable& Abra, const MpoView& W,
+                   const BlockTable& Aket, BlockTable* Enew) {
+    ChainSet cs;
+    TripodView Ev = make_tripod_view(E);
+    BipedsView Bv = make_bipeds_view(Abra, W.nloc), Kv = make_bipeds_view(Aket, W.nloc);
+    const double eps = 2.220446049250313e-16;
+    // output blocks keyed by (quple, aux index)
+    std::unordered_map<QN3, int, QNTupleHash<3>> odict;
+    std::vector<QN3> okeys;
+    std::vector<std::vector<int64_t>> oaux;   // -> output block id
+    std::vector<int64_t> orows, ocols;
+    std::vector<QN> oin, oout, omid;
+    std::vector<int32_t> oleg;
+    auto out_block = [&](const QN3& quple, int a, int64_t rows, int64_t cols) -> int64_t {
+        auto it = odict.find(quple);
+        int q;
+        if (it == odict.end()) {
+            q = (int)okeys.size();
+            odict.emplace(quple, q);
+            okeys.push_back(quple);
+            oaux.emplace_back();
+        } else q = it->second;
+        auto& v = oaux[q];
+        if ((int)v.size() <= a) v.resize(a + 1, -1);
+        if (v[a] < 0) {
+            v[a] = (int64_t)orows.size();
+            orows.push_back(rows); ocols.push_back(cols);
+            oin.push_back(quple.q[0]); oout.push_back(quple.q[1]); omid.push_back(quple.q[2]);
+            oleg.push_back(a);
+        } else if (orows[v[a]] != rows || ocols[v[a]] != cols) {
+            throw std::invalid_argument("inconsistent output block shapes in environment update");
+        }
+        return v[a];
+    };
+    for (int s1 = 0; s1 < W.nloc; ++s1)
+    for (int s2 = 0; s2 < W.nloc; ++s2)
+    for (int k = 0; k < W.nop; ++k) {
+        if (!sym.triangle(W.qloc[s2], W.qop[k], W.qloc[s1])) continue;
+        for (int qE = 0; qE < (int)Ev.keys.size(); ++qE) {
+            const QN& Ein = Ev.keys[qE].q[0];
+            const QN& Eout = Ev.keys[qE].q[1];
+            const QN& Emid = Ev.keys[qE].q[2];
+            if (side == VMPS_ENV_LEFT) {
+                // LAWA -> quple {Rout, Rin, Rmid}
+                for (const QN& Rout : sym.reduce(Ein, W.qloc[s1])) {
+                    int64_t qAbra = Bv.find(s1, Ein, Rout);
+                    if (qAbra < 0) continue;
+                    for (const QN& Rin : sym.reduce(Eout, W.qloc[s2])) {
+                        int64_t qAket = Kv.find(s2, Eout, Rin);
+                        if (qAket < 0) continue;
+                        for (const QN& Rmid : sym.reduce(Emid, W.qop[k])) {
+                            const auto* nz = W.find(s1, s2, k, Emid, Rmid);
+                            if (!nz) continue;
+                            if (!sym.triangle(Rin, Rmid, Rout)) continue;
+                            double cgc = 1.0;
+                            if (sym.nonabelian()) {
+                                QN q9[9] = {Aket.qin[qAket], W.qloc[s2], Aket.qout[qAket], Emid, W.qop[k], Rmid,
+                                            Abra.qin[qAbra], W.qloc[s1], Abra.qout[qAbra]};
+                                cgc = sym.coeff_buildL(q9);
+                            }
+                            if (std::abs(cgc) < eps) continue;
+                            cs.n_tasks++;
+                            QN3 quple{{Rout, Rin, Rmid}};
+                            for (const auto& e : *nz) {
+                                int64_t la = Ev.at(qE, e.row);
+                                if (la < 0) continue;
+                                // Abra^dagger (cols_bra x rows_bra) * L (rows_bra x rows_ket) * Aket
+                                int64_t o = out_block(quple, e.col, Abra.cols[qAbra], Aket.cols[qAket]);
+                                cs.n_chains_raw++;
+                                cs.flops_reference += chain_flops((double)Abra.cols[qAbra], (double)Abra.rows[qAbra],
+                                                                  (double)E.cols[la], (double)Aket.cols[qAket]);
+                                cs.chains.push_back(Chain{o, qAbra, la, qAket, cgc * e.val});
+                            }
+                        }
+                    }
+                }
+            } else {
+                // AWAR (tensors/DmrgIndexGymnastics.h:79-124) -> quple {Lout, Lin, Lmid}
+                const QN& Rin = Ein;
+                const QN& Rout = Eout;
+                const QN& Rmid = Emid;
+                for (const QN& Lin : sym.reduce(Rout, sym.flip(W.qloc[s1]))) {
+                    int64_t qAbra = Bv.find(s1, Lin, Rout);
+                    if (qAbra < 0) continue;
+                    for (const QN& Lout : sym.reduce(Rin, sym.flip(W.qloc[s2]))) {
+                        int64_t qAket = Kv.find(s2, Lout, Rin);
+                        if (qAket < 0) continue;
+                        for (const QN& Lmid : sym.reduce(Rmid, sym.flip(W.qop[k]))) {
+                            const auto* nz = W.find(s1, s2, k, Lmid, Rmid);
+                            if (!nz) continue;
+                            if (!sym.triangle(Lout, Lmid, Lin)) continue;
+                            double cgc = 1.0;
+                            if (sym.nonabelian()) {
+                                QN q9[9] = {Aket.qin[qAket], W.qloc[s2], Aket.qout[qAket], Lmid, W.qop[k], Rmid,
+                                            Abra.qin[qAbra], W.qloc[s1], Abra.qout[qAbra]};
+                                cgc = sym.coeff_buildR(q9);
+                            }
+                            if (std::abs(cgc) < eps) continue;
+                            cs.n_tasks++;
+                            QN3 quple{{Lout, Lin, Lmid}};
+                            for (const auto& e : *nz) {
+                                int64_t rb = Ev.at(qE, e.col);
+                                if (rb < 0) continue;
+                                // Aket (rows_ket x cols_ket) * R (cols_ket x cols_bra) * Abra^dagger
+                                int64_t o = out_block(quple, e.row, Aket.rows[qAket], Abra.rows[qAbra]);
+                                cs.n_chains_raw++;
+                                cs.flops_reference += chain_flops((double)Aket.rows[qAket], (double)Aket.cols[qAket],
+                                                                  (double)E.cols[rb], (double)Abra.rows[qAbra]);
+                                cs.chains.push_back(Chain{o, qAket, rb, qAbra, cgc * e.val});
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    // compact output layout, blocks in creation order
+    BlockTable& t = *Enew;
+    t = BlockTable();
+    t.n = (int64_t)orows.size();
+    t.has_mid = true;
+    t.qin = oin; t.qout = oout; t.qmid = omid; t.leg = oleg; t.rows = orows; t.cols = ocols;
+    t.off.resize(t.n);
+    int64_t cur = 0;
+    for (int64_t i = 0; i < t.n; ++i) { t.off[i] = cur; cur += orows[i] * ocols[i]; }
+    t.total = cur;
+    return cs;
+}
+
+// ===========================================================================
+// planner
+// ===========================================================================
+DevLayout make_dev_layout(const std::vector<int64_t>& rows, const std::vector<int64_t>& cols) {
+    DevLayout d;
+    const size_t n = rows.size();
+    d.off.resize(n); d.rows = rows; d.cols = cols; d.ld.resize(n);
+    int64_t cur = 0;
+    for (size_t i = 0; i < n; ++i) {
+        d.ld[i] = pad_ld(rows[i]);
+        d.off[i] = cur;
+        cur = pad_off(cur + d.ld[i] * cols[i]);
+    }
+    d.total = std::max<int64_t>(cur, 32);
+    return d;
+}
+
+namespace {
+struct Key4 {
+    int64_t a, b, c, d;
+    bool operator==(const Key4& o) const { return a == o.a && b == o.b && c == o.c && d == o.d; }
+};
+struct Key4Hash {
+    size_t operator()(const Key4& k) const {
+        uint64_t h = (uint64_t)k.a * 0x9E3779B97F4A7C15ull;
+        h ^= (uint64_t)k.b + 0x7F4A7C159E3779B9ull + (h << 6) + (h >> 2);
+        h ^= (uint64_t)k.c + 0x94D049BB133111EBull + (h << 6) + (h >> 2);
+        h ^= (uint64_t)k.d + 0xBF58476D1CE4E5B9ull + (h << 6) + (h >> 2);
+        return (size_t)h;
+    }
+};
+
+// append tiles of an m x n output block whose segments are [sb, se)
+void add_tiles(PhasePlan& ph, int64_t c_off, int64_t ldc, int64_t m, int64_t n, int32_t sb, int32_t se, int tm,
+               int tn) {
+    for (int64_t r0 = 0; r0 < m; r0 += tm)
+        for (int64_t c0 = 0; c0 < n; c0 += tn) {
+            GTile t{};
+            t.c_off = c_off;
+            t.ldc = (int32_t)ldc;
+            t.m = (int32_t)m;
+            t.n = (int32_t)n;
+            t.row0 = (int32_t)r0;
+            t.col0 = (int32_t)c0;
+            t.seg_begin = sb;
+            t.seg_end = se;
+            ph.tiles.push_back(t);
+        }
+}
+
+// order tiles by descending work so that the hardware block scheduler runs the
+// largest first (longest-processing-time list scheduling)
+void sort_tiles(PhasePlan& ph) {
+    std::vector<double> cost(ph.tiles.size());
+    for (size_t i = 0; i < ph.tiles.size(); ++i) {
+        const GTile& t = ph.tiles[i];
+        double k = 0;
+        for (int s = t.seg_begin; s < t.seg_end; ++s) k += ph.segs[s].K * (double)ph.segs[s].term_count;
+        cost[i] = k * std::min(64, t.m - t.row0) * std::min(64, t.n - t.col0) + 1.0;
+    }
+    std::vector<size_t> idx(ph.tiles.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+    std::vector<GTile> t2(ph.tiles.size());
+    for (size_t i = 0; i < idx.size(); ++i) t2[i] = ph.tiles[idx[i]];
+    ph.tiles.swap(t2);
+}
+}  // namespace
+
+Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z, const DevLayout& O,
+               bool transX, bool transZ, int tile_m, int tile_n) {
+    Plan P;
+    // shapes: op(X) m x k, Y k x n, op(Z) n x p, out m x p
+    auto xm = [&](int64_t x) { return transX ? X.cols[x] : X.rows[x]; };
+    auto xk = [&](int64_t x) { return transX ? X.rows[x] : X.cols[x]; };
+    auto zn = [&](int64_t z) { return transZ ? Z.cols[z] : Z.rows[z]; };
+    auto zp = [&](int64_t z) { return transZ ? Z.rows[z] : Z.cols[z]; };
+
+    // ---- merge duplicate chains (same out, X, Y, Z): coefficients add
+    std::unordered_map<Key4, size_t, Key4Hash> mdict;
+    std::vector<Chain> ch;
+    ch.reserve(cs.chains.size());
+    for (const Chain& c : cs.chains) {
+        if (c.out < 0 || c.out >= (int64_t)O.rows.size() || c.x < 0 || c.x >= (int64_t)X.rows.size() || c.y < 0 ||
+            c.y >= (int64_t)Y.rows.size() || c.z < 0 || c.z >= (int64_t)Z.rows.size())
+            throw std::invalid_argument("chain references a block outside its table");
+        if (xk(c.x) != Y.rows[c.y] || Y.cols[c.y] != zn(c.z) || O.rows[c.out] != xm(c.x) || O.cols[c.out] != zp(c.z))
+            throw std::domain_error("block shapes do not chain: out " + std::to_string(c.out));
+        Key4 k{c.out, c.x, c.y, c.z};
+        auto it = mdict.find(k);
+        if (it == mdict.end()) { mdict.emplace(k, ch.size()); ch.push_back(c); }
+        else ch[it->second].c += c.c;
+    }
+    P.n_chains = (int64_t)ch.size();
+
+    // algorithmic counts on the merged list
+    {
+        std::vector<char> ux(X.rows.size(), 0), uz(Z.rows.size(), 0), uo(O.rows.size(), 0);
+        double bytes = 0;
+        for (const Chain& c : ch) {
+            P.flops_merged += chain_flops((double)xm(c.x), (double)xk(c.x), (double)Y.cols[c.y], (double)zp(c.z));
+            if (!ux[c.x]) { ux[c.x] = 1; bytes += 8.0 * X.rows[c.x] * X.cols[c.x]; }
+            if (!uz[c.z]) { uz[c.z] = 1; bytes += 8.0 * Z.rows[c.z] * Z.cols[c.z]; }
+            if (!uo[c.out]) { uo[c.out] = 1; }
+        }
+        for (size_t i = 0; i < Y.rows.size(); ++i) bytes += 8.0 * Y.rows[i] * Y.cols[i];
+        for (size_t i = 0; i < O.rows.size(); ++i) if (uo[i]) bytes += 8.0 * O.rows[i] * O.cols[i];
+        P.bytes_alg = bytes;
+        int64_t no = 0;
+        for (char u : uo) no += u;
+        P.n_out_blocks = no;
+    }
+
+    // ---- choose the association with fewer executed flops (shared intermediates counted once)
+    double f_xy = 0, f_yz = 0;
+    {
+        std::unordered_map<Key4, char, Key4Hash> sxy, syz;
+        for (const Chain& c : ch) {
+            const double m = (double)xm(c.x), k = (double)xk(c.x), n = (double)Y.cols[c.y], p = (double)zp(c.z);
+            if (sxy.emplace(Key4{c.x, c.y, 0, 0}, 1).second) f_xy += 2 * m * k * n;
+            if (syz.emplace(Key4{c.y, c.z, 0, 0}, 1).second) f_yz += 2 * k * n * p;
+        }
+        // second stage after summing all first-stage products that share (out, Z) resp. (out, X)
+        std::unordered_map<Key4, char, Key4Hash> oz, ox;
+        for (const Chain& c : ch) {
+            const double m = (double)xm(c.x), k = (double)xk(c.x), n = (double)Y.cols[c.y], p = (double)zp(c.z);
+            if (oz.emplace(Key4{c.out, c.z, 0, 0}, 1).second) f_xy += 2 * m * n * p;
+            if (ox.emplace(Key4{c.out, c.x, 0, 0}, 1).second) f_yz += 2 * m * k * p;
+        }
+    }
+    P.association = (f_yz < f_xy) ? 1 : 0;
+
+    // ---- intermediates
+    std::unordered_map<Key4, int64_t, Key4Hash> idict;
+    std::vector<std::pair<int64_t, int64_t>> ipairs;   // (x,y) or (y,z)
+    std::vector<int64_t> trows, tcols;
+    std::vector<int64_t> chain_t(ch.size());
+    for (size_t i = 0; i < ch.size(); ++i) {
+        const Chain& c = ch[i];
+        Key4 k = P.association == 0 ? Key4{c.x, c.y, 0, 0} : Key4{c.y, c.z, 0, 0};
+        auto it = idict.find(k);
+        if (it == idict.end()) {
+            int64_t id = (int64_t)ipairs.size();
+            idict.emplace(k, id);
+            if (P.association == 0) {
+                ipairs.push_back({c.x, c.y});
+                trows.push_back(xm(c.x));
+                tcols.push_back(Y.cols[c.y]);
+            } else {
+                ipairs.push_back({c.y, c.z});
+                trows.push_back(Y.rows[c.y]);
+                tcols.push_back(zp(c.z));
+            }
+            chain_t[i] = id;
+        } else chain_t[i] = it->second;
+    }
+    P.n_intermediates = (int64_t)ipairs.size();
+    P.T = make_dev_layout(trows, tcols);
+
+    // ---- phase 1: T = op(X)*Y  (association 0)  or  U = Y*op(Z)  (association 1)
+    PhasePlan& p1 = P.p1;
+    if (P.association == 0) {
+        p1.slotA = SLOT_X; p1.transA = transX; p1.slotB = SLOT_Y; p1.transB = false;
+    } else {
+        p1.slotA = SLOT_Y; p1.transA = false; p1.slotB = SLOT_Z; p1.transB = transZ;
+    }
+    p1.slotC = SLOT_T;
+    p1.transC = false;
+    for (size_t j = 0; j < ipairs.size(); ++j) {
+        int64_t a = ipairs[j].first, b = ipairs[j].second;
+        const DevLayout& LA = P.association == 0 ? X : Y;
+        const DevLayout& LB = P.association == 0 ? Y : Z;
+        int64_t K = P.association == 0 ? xk(a) : Y.cols[a];
+        GSeg s{};
+        s.b_off = LB.off[b];
+        s.ldb = (int32_t)LB.ld[b];
+        s.lda = (int32_t)LA.ld[a];
+        s.K = (int32_t)K;
+        s.term_begin = (int32_t)p1.terms.size();
+        s.term_count = 1;
+        p1.terms.push_back(GTerm{LA.off[a], 1.0});
+        int32_t sb = (int32_t)p1.segs.size();
+        p1.segs.push_back(s);
+        p1.flops += 2.0 * trows[j] * tcols[j] * K;
+        add_tiles(p1, P.T.off[j], P.T.ld[j], trows[j], tcols[j], sb, sb + 1, tile_m, tile_n);
+    }
+    sort_tiles(p1);
+
+    // ---- phase 2
+    PhasePlan& p2 = P.p2;
+    p2.slotC = SLOT_OUT;
+    // group chains by output block, then by the operand that is not an intermediate
+    std::vector<size_t> order(ch.size());
+    std::iota(order.begin(), order.end(), 0);
+    if (P.association == 0) {
+        // out = sum_z (sum_t c_t T_t) * op(Z_z) ;  A = T (multi-term), B = op(Z)
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            if (ch[a].out != ch[b].out) return ch[a].out < ch[b].out;
+            if (ch[a].z != ch[b].z) return ch[a].z < ch[b].z;
+            return chain_t[a] < chain_t[b];
+        });
+        p2.slotA = SLOT_T; p2.transA = false; p2.slotB = SLOT_Z; p2.transB = transZ; p2.transC = false;
+    } else {
+        // out^T = sum_x (sum_t c_t U_t)^T * op(X_x)^T ;  A = U^T (multi-term), B = op(X)^T, C stored transposed
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            if (ch[a].out != ch[b].out) return ch[a].out < ch[b].out;
+            if (ch[a].x != ch[b].x) return ch[a].x < ch[b].x;
+            return chain_t[a] < chain_t[b];
+        });
+        p2.slotA = SLOT_T; p2.transA = true; p2.slotB = SLOT_X; p2.transB = !transX; p2.transC = true;
+    }
+    size_t i = 0;
+    while (i < order.size()) {
+        const int64_t o = ch[order[i]].out;
+        int32_t sb = (int32_t)p2.segs.size();
+        size_t j = i;
+        while (j < order.size() && ch[order[j]].out == o) {
+            const int64_t other = P.association == 0 ? ch[order[j]].z : ch[order[j]].x;
+            GSeg s{};
+            s.term_begin = (int32_t)p2.terms.size();
+            size_t jj = j;
+            while (jj < order.size() && ch[order[jj]].out == o &&
+                   (P.association == 0 ? ch[order[jj]].z : ch[order[jj]].x) == other) {
+                const int64_t t = chain_t[order[jj]];
+                if (!p2.terms.empty() && (int32_t)p2.terms.size() > s.term_begin && p2.terms.back().off == P.T.off[t])
+                    p2.terms.back().coef += ch[order[jj]].c;
+                else
+                    p2.terms.push_back(GTerm{P.T.off[t], ch[order[jj]].c});
+                s.lda = (int32_t)P.T.ld[t];
+                ++jj;
+            }
+            s.term_count = (int32_t)p2.terms.size() - s.term_begin;
+            if (P.association == 0) {
+                s.b_off = Z.off[other];
+                s.ldb = (int32_t)Z.ld[other];
+                s.K = (int32_t)zn(other);
+            } else {
+                s.b_off = X.off[other];
+                s.ldb = (int32_t)X.ld[other];
+                s.K = (int32_t)xk(other);
+            }
+            p2.segs.push_back(s);
+            j = jj;
+        }
+        int32_t se = (int32_t)p2.segs.size();
+        // tile space: association 0 -> (m x p) of out; association 1 -> (p x m) (transposed store)
+        const int64_t m = O.rows[o], p = O.cols[o];
+        double kk = 0;
+        for (int32_t s = sb; s < se; ++s) kk += p2.segs[s].K;
+        p2.flops += 2.0 * m * p * kk;
+        if (P.association == 0) add_tiles(p2, O.off[o], O.ld[o], m, p, sb, se, tile_m, tile_n);
+        else add_tiles(p2, O.off[o], O.ld[o], p, m, sb, se, tile_m, tile_n);
+        i = j;
+    }
+    // output blocks that receive no product are still written (with zeros), as the
+    // reference's OxV starts from a zeroed copy of Vin (pivot/DmrgPivotMatrix1.h:127,134)
+    {
+        std::vector<char> seen(O.rows.size(), 0);
+        for (const Chain& c : ch) seen[c.out] = 1;
+        const int32_t sb = (int32_t)p2.segs.size();
+        for (size_t o = 0; o < O.rows.size(); ++o)
+            if (!seen[o]) {
+                if (P.association == 0) add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, sb, tile_m, tile_n);
+                else add_tiles(p2, O.off[o], O.ld[o], O.cols[o], O.rows[o], sb, sb, tile_m, tile_n);
+            }
+    }
+    sort_tiles(p2);
+    return P;
+}
+
+}  // namespace vmps

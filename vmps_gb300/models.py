@@ -1,0 +1,189 @@
+"""Nearest-neighbour chain Hamiltonians as MPOs (host-side model layer).
+
+The reference builds W through MpoTerms (MpoTerms.h:1175-1232) from the site
+operator algebras of bases/SpinBase.h and bases/FermionBase.h.  This module
+produces the same object -- W[s1][s2][k] blocks keyed by auxiliary QNs -- for
+the chains the benchmark configurations use, from a finite-state-machine MPO:
+
+    aux states at every inner bond: IDLE, OPEN_t (one per two-site term t), DONE
+    W[IDLE->IDLE] = 1,  W[IDLE->OPEN_t] = A_t,  W[OPEN_t->DONE] = c_t B_t,
+    W[IDLE->DONE] = onsite,  W[DONE->DONE] = 1
+
+so H = sum_i (onsite_i + sum_t c_t A_t,i B_t,i+1).  An auxiliary state carries
+the QN of the operators placed to its left (vacuum for IDLE and DONE), which
+makes every W block QN-conserving: qout_aux = qin_aux + q(operator).
+
+Local bases (QN conventions of the reference's U(1) kinds, M = 2 S^z):
+  spin-1/2, U(1) M            : s=0 |up> M=+1, s=1 |dn> M=-1
+  Hubbard, U(1)xU(1) (N, M)   : s=0 |0> (0,0), s=1 |up> (1,1), s=2 |dn> (1,-1), s=3 |updn> (2,0)
+with |updn> = c+_up c+_dn |0>; fermion signs by Jordan-Wigner (site order,
+up before down inside a site).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .blocks import MpoSite, Symmetry
+
+
+class ChainModel:
+    """MPO of a chain: sites W[l], aux bases aux[l] (l = 0..L), local bases."""
+
+    def __init__(self, sym, L, qloc, ops, terms, onsite, name=""):
+        self.sym = sym
+        self.L = L
+        self.qloc = qloc            # list of QN tuples (same on every site)
+        self.name = name
+        self.ops = ops              # name -> (matrix, QN)
+        self.terms = terms          # list of (opA, opB, coef)
+        self.onsite = onsite        # list of (op, coef)
+        self._build()
+
+    @property
+    def d(self):
+        return len(self.qloc)
+
+    def _build(self):
+        vac = self.sym.vacuum()
+        inner = [("IDLE", vac)] + [(f"OPEN{t}", self.ops[a][1]) for t, (a, b, c) in enumerate(self.terms)] + \
+                [("DONE", vac)]
+        self.aux = []
+        for l in range(self.L + 1):
+            if l == 0:
+                self.aux.append([("IDLE", vac)])
+            elif l == self.L:
+                self.aux.append([("DONE", vac)])
+            else:
+                self.aux.append(list(inner))
+        self.W = [self._site(l) for l in range(self.L)]
+        self.wdim = len(inner)
+
+    @staticmethod
+    def _sector_index(aux):
+        cnt, idx = {}, {}
+        for name, q in aux:
+            idx[name] = (q, cnt.get(q, 0))
+            cnt[q] = cnt.get(q, 0) + 1
+        return idx
+
+    def _site(self, l):
+        d = self.d
+        ain, aout = self._sector_index(self.aux[l]), self._sector_index(self.aux[l + 1])
+        I = np.eye(d)
+        entries = []   # (state_in, state_out, matrix)
+        if "IDLE" in ain and "IDLE" in aout:
+            entries.append(("IDLE", "IDLE", I))
+        if "DONE" in ain and "DONE" in aout:
+            entries.append(("DONE", "DONE", I))
+        if "IDLE" in ain and "DONE" in aout and self.onsite:
+            h = sum(c * self.ops[o][0] for o, c in self.onsite)
+            entries.append(("IDLE", "DONE", h))
+        for t, (a, b, c) in enumerate(self.terms):
+            if "IDLE" in ain and f"OPEN{t}" in aout:
+                entries.append(("IDLE", f"OPEN{t}", self.ops[a][0]))
+            if f"OPEN{t}" in ain and "DONE" in aout:
+                entries.append((f"OPEN{t}", "DONE", c * self.ops[b][0]))
+        # operator QNs: distinct q(s1) - q(s2) over nonzeros, sorted (a std::set in the reference)
+        qops = set()
+        nz = []
+        for sin, sout, M in entries:
+            for s1 in range(d):
+                for s2 in range(d):
+                    v = M[s1, s2]
+                    if abs(v) < 1e-15:
+                        continue
+                    qop = tuple(x - y for x, y in zip(self.qloc[s1], self.qloc[s2]))
+                    qops.add(qop)
+                    nz.append((s1, s2, qop, ain[sin], aout[sout], v))
+        qop_list = sorted(qops)
+        kidx = {q: i for i, q in enumerate(qop_list)}
+        site = MpoSite(nq=self.sym.nq, qloc=list(self.qloc), qop=qop_list)
+        for s1, s2, qop, (qi, ri), (qo, co), v in nz:
+            # QN conservation of the aux flow: qout_aux = qin_aux + qop
+            assert tuple(x + y for x, y in zip(qi, qop)) == tuple(qo), (qi, qop, qo)
+            site.add(s1, s2, kidx[qop], qi, qo, ri, co, v)
+        return site
+
+    # dense representation (tests, exact diagonalisation)
+    def aux_qns(self, l):
+        return [q for _, q in self.aux[l]]
+
+    def dense_W(self, l):
+        return self.W[l].dense(self.aux_qns(l), self.aux_qns(l + 1))
+
+
+def heisenberg_u1(L, J=1.0):
+    """Spin-1/2 XXX chain, H = J sum (Sz Sz + (S+S- + S-S+)/2), U(1) M = 2 S^z."""
+    sym = Symmetry(("U1",))
+    qloc = [(1,), (-1,)]
+    Sz = np.diag([0.5, -0.5])
+    Sp = np.array([[0.0, 1.0], [0.0, 0.0]])   # |up><dn|
+    Sm = Sp.T.copy()
+    ops = {"Sz": (Sz, (0,)), "Sp": (Sp, (2,)), "Sm": (Sm, (-2,))}
+    terms = [("Sp", "Sm", 0.5 * J), ("Sm", "Sp", 0.5 * J), ("Sz", "Sz", J)]
+    return ChainModel(sym, L, qloc, ops, terms, [], name=f"HeisenbergU1(L={L},J={J})")
+
+
+def hubbard_u1xu1(L, t=1.0, U=4.0):
+    """Hubbard chain, H = -t sum_s (c+_i,s c_i+1,s + h.c.) + U sum n_up n_dn, U(1)xU(1) (N, M)."""
+    sym = Symmetry(("U1", "U1"))
+    qloc = [(0, 0), (1, 1), (1, -1), (2, 0)]
+    cdu = np.zeros((4, 4)); cdu[1, 0] = 1.0; cdu[3, 2] = 1.0           # c+_up
+    cdd = np.zeros((4, 4)); cdd[2, 0] = 1.0; cdd[3, 1] = -1.0          # c+_dn (sign from c+_dn c+_up = -c+_up c+_dn)
+    F = np.diag([1.0, -1.0, -1.0, 1.0])
+    cu, cd = cdu.T.copy(), cdd.T.copy()
+    nupdn = np.diag([0.0, 0.0, 0.0, 1.0])
+    ops = {
+        "cdu_F": (cdu @ F, (1, 1)), "cdd_F": (cdd @ F, (1, -1)),
+        "F_cu": (F @ cu, (-1, -1)), "F_cd": (F @ cd, (-1, 1)),
+        "cu": (cu, (-1, -1)), "cd": (cd, (-1, 1)), "cdu": (cdu, (1, 1)), "cdd": (cdd, (1, -1)),
+        "nupdn": (nupdn, (0, 0)),
+    }
+    # c+_i c_i+1 = (c+ F)_i (c)_i+1 ;  c+_i+1 c_i = (F c)_i (c+)_i+1
+    terms = [("cdu_F", "cu", -t), ("cdd_F", "cd", -t), ("F_cu", "cdu", -t), ("F_cd", "cdd", -t)]
+    onsite = [("nupdn", U)] if U != 0 else []
+    return ChainModel(sym, L, qloc, ops, terms, onsite, name=f"HubbardU1xU1(L={L},t={t},U={U})")
+
+
+# ---------------------------------------------------------------------------
+# exact dense Hamiltonians (independent of the MPO), for the oracle's pins
+# ---------------------------------------------------------------------------
+def dense_heisenberg(L, J=1.0):
+    """Full 2^L x 2^L XXX Hamiltonian, basis index = sum_i s_i 2^(L-1-i), s=0 up."""
+    Sz = np.diag([0.5, -0.5]); Sp = np.array([[0.0, 1.0], [0.0, 0.0]]); Sm = Sp.T
+    I = np.eye(2)
+
+    def op(o, i):
+        m = np.array([[1.0]])
+        for j in range(L):
+            m = np.kron(m, o if j == i else I)
+        return m
+    H = np.zeros((2 ** L, 2 ** L))
+    for i in range(L - 1):
+        H += J * (op(Sz, i) @ op(Sz, i + 1) + 0.5 * (op(Sp, i) @ op(Sm, i + 1) + op(Sm, i) @ op(Sp, i + 1)))
+    return H
+
+
+def dense_hubbard(L, t=1.0, U=4.0):
+    """Full 4^L Hubbard Hamiltonian built from fermion modes (i,up),(i,dn) in order
+    (0,up),(0,dn),(1,up),... with explicit Jordan-Wigner strings over all modes."""
+    nm = 2 * L
+    a = np.array([[0.0, 1.0], [0.0, 0.0]])   # annihilator on one mode (|0>,|1>)
+    Z = np.diag([1.0, -1.0])
+    I = np.eye(2)
+
+    def ann(m):
+        o = np.array([[1.0]])
+        for j in range(nm):
+            o = np.kron(o, Z if j < m else (a if j == m else I))
+        return o
+    c = [ann(m) for m in range(nm)]
+    H = np.zeros((2 ** nm, 2 ** nm))
+    for i in range(L - 1):
+        for s in range(2):
+            m1, m2 = 2 * i + s, 2 * (i + 1) + s
+            hop = c[m1].T @ c[m2]
+            H += -t * (hop + hop.T)
+    for i in range(L):
+        H += U * (c[2 * i].T @ c[2 * i]) @ (c[2 * i + 1].T @ c[2 * i + 1])
+    return H

@@ -1,0 +1,288 @@
+"""Random block-sparse MPS with U(1)-type bond bases (host-side state layer).
+
+The reference initialises an Mps through outerResize/innerResize and
+setRandom (Mps.h:1124-1262, :1380-1560, :1639-1665) and grows the bond bases
+during its sweeps.  The synthetic states used here fix the bond bases up front:
+
+* the QNs allowed at bond l are those reachable from the left vacuum and from
+  the right target Qtot (the quantum-number graph of Mps::outerResize);
+* sector dimensions follow either the reference's innerResize rule (Dmax split
+  evenly over the sectors, capped by the Hilbert-space count) -- profile
+  "even" -- or a Gaussian profile around the mean filling -- profile
+  "gaussian", the shape of the Schmidt spectrum of a ground state, used for the
+  large-D frozen-site workloads;
+* blocks are N(0,1) from a seeded generator, then left-normalised (QR) left of
+  the pivot and right-normalised (LQ) right of it.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .blocks import Blocks
+
+
+def _add(a, b):
+    return tuple(x + y for x, y in zip(a, b))
+
+
+def _sub(a, b):
+    return tuple(x - y for x, y in zip(a, b))
+
+
+def bond_bases(qloc, L, Qtot, Dmax, profile="even", sigma=None):
+    """dims[l] : dict QN -> sector dimension at bond l (l = 0..L)."""
+    vac = tuple(0 for _ in Qtot)
+    # exact Hilbert-space counts from the left and from the right (capped to avoid huge ints)
+    cap = 10 ** 12
+    fromL = [dict() for _ in range(L + 1)]
+    fromL[0][vac] = 1
+    for l in range(L):
+        for q, n in fromL[l].items():
+            for s in qloc:
+                q2 = _add(q, s)
+                fromL[l + 1][q2] = min(cap, fromL[l + 1].get(q2, 0) + n)
+    fromR = [dict() for _ in range(L + 1)]
+    fromR[L][tuple(Qtot)] = 1
+    for l in range(L, 0, -1):
+        for q, n in fromR[l].items():
+            for s in qloc:
+                q2 = _sub(q, s)
+                fromR[l - 1][q2] = min(cap, fromR[l - 1].get(q2, 0) + n)
+    dims = []
+    for l in range(L + 1):
+        allowed = {q: min(fromL[l][q], fromR[l][q]) for q in fromL[l] if q in fromR[l]}
+        if l == 0 or l == L:
+            dims.append({q: 1 for q in allowed})
+            continue
+        qs = sorted(allowed)
+        if profile == "even":
+            per = max(1, Dmax // len(qs))
+            d = {q: min(allowed[q], per) for q in qs}
+        else:
+            mean = [Qtot[i] * l / L for i in range(len(Qtot))]
+            sig = sigma if sigma is not None else [2.5] * len(Qtot)
+            w = {q: math.exp(-sum(((q[i] - mean[i]) / sig[i]) ** 2 for i in range(len(q))) / 2.0) for q in qs}
+            tot = sum(w.values())
+            d = {}
+            for q in qs:
+                x = int(round(Dmax * w[q] / tot))
+                if x > 0:
+                    d[q] = min(allowed[q], x)
+            if not d:
+                q0 = max(qs, key=lambda q: w[q])
+                d[q0] = 1
+        dims.append(d)
+    # make neighbouring bonds consistent: dim_{l+1}(q) <= sum_s dim_l(q - s) and vice versa
+    for _ in range(4):
+        changed = False
+        for l in range(1, L + 1):
+            for q in list(dims[l]):
+                lim = sum(dims[l - 1].get(_sub(q, s), 0) for s in qloc)
+                if dims[l][q] > lim:
+                    changed = True
+                    if lim == 0:
+                        del dims[l][q]
+                    else:
+                        dims[l][q] = lim
+        for l in range(L - 1, -1, -1):
+            for q in list(dims[l]):
+                lim = sum(dims[l + 1].get(_add(q, s), 0) for s in qloc)
+                if dims[l][q] > lim:
+                    changed = True
+                    if lim == 0:
+                        del dims[l][q]
+                    else:
+                        dims[l][q] = lim
+        if not changed:
+            break
+    return dims
+
+
+def site_layout(qloc, din, dout, nq):
+    """Block table of A[s] with blocks (qin -> qin + qloc[s]) present in both bases."""
+    ent = []
+    for s, qs in enumerate(qloc):
+        for qin in sorted(din):
+            qout = _add(qin, qs)
+            if qout in dout:
+                ent.append((s, qin, qout, din[qin], dout[qout]))
+    return Blocks(nq, [e[1] for e in ent], [e[2] for e in ent], [e[0] for e in ent],
+                  [e[3] for e in ent], [e[4] for e in ent])
+
+
+def random_site(qloc, din, dout, nq, rng):
+    A = site_layout(qloc, din, dout, nq)
+    A.data[:] = rng.standard_normal(A.data.size)
+    return A
+
+
+def left_normalize(A, nq, carry=None):
+    """QR per outgoing sector: A -> Q (left-orthonormal), returns (Q, R dict qout->R).
+    `carry` (dict qin -> matrix) multiplies the incoming bond first."""
+    A = A.like(A.data.copy())
+    if carry is not None:
+        for i in range(A.n):
+            qin = tuple(A.qin[i])
+            A.block(i)[...] = carry[qin] @ A.block(i) if qin in carry else A.block(i)
+    groups = {}
+    for i in range(A.n):
+        groups.setdefault(tuple(A.qout[i]), []).append(i)
+    Rs = {}
+    for qout, idx in groups.items():
+        M = np.vstack([A.block(i) for i in idx])
+        Q, R = np.linalg.qr(M)
+        r0 = 0
+        for i in idx:
+            r = A.block(i).shape[0]
+            A.block(i)[...] = Q[r0:r0 + r]
+            r0 += r
+        Rs[qout] = R
+    return A, Rs
+
+
+def right_normalize(A, nq, carry=None):
+    """LQ per incoming sector: A -> Q (right-orthonormal), returns (Q, Lfac dict qin->L).
+    `carry` (dict qout -> matrix) multiplies the outgoing bond first (A @ carry)."""
+    A = A.like(A.data.copy())
+    if carry is not None:
+        for i in range(A.n):
+            qout = tuple(A.qout[i])
+            if qout in carry:
+                A.block(i)[...] = A.block(i) @ carry[qout]
+    groups = {}
+    for i in range(A.n):
+        groups.setdefault(tuple(A.qin[i]), []).append(i)
+    Ls = {}
+    for qin, idx in groups.items():
+        M = np.hstack([A.block(i) for i in idx])
+        Q, R = np.linalg.qr(M.T)
+        Qt = Q.T
+        c0 = 0
+        for i in idx:
+            c = A.block(i).shape[1]
+            A.block(i)[...] = Qt[:, c0:c0 + c]
+            c0 += c
+        Ls[qin] = R.T
+    return A, Ls
+
+
+class RandomMPS:
+    """Seeded random MPS, mixed-canonical about a pivot bond range."""
+
+    def __init__(self, model, Qtot, Dmax, seed=1, profile="even", sigma=None):
+        self.model = model
+        self.L = model.L
+        self.nq = model.sym.nq
+        self.qloc = model.qloc
+        self.Qtot = tuple(Qtot)
+        self.dims = bond_bases(model.qloc, model.L, Qtot, Dmax, profile=profile, sigma=sigma)
+        rng = np.random.default_rng(seed)
+        self.A = [random_site(self.qloc, self.dims[l], self.dims[l + 1], self.nq, rng) for l in range(self.L)]
+
+    def canonicalize(self, pivot_lo, pivot_hi):
+        """Sites < pivot_lo left-normalised, sites > pivot_hi right-normalised;
+        the factors are pushed into the pivot sites."""
+        carry = None
+        for l in range(pivot_lo):
+            self.A[l], carry = left_normalize(self.A[l], self.nq, carry)
+        if carry is not None:
+            A = self.A[pivot_lo]
+            for i in range(A.n):
+                q = tuple(A.qin[i])
+                A.block(i)[...] = carry[q] @ A.block(i)
+        carry = None
+        for l in range(self.L - 1, pivot_hi, -1):
+            self.A[l], carry = right_normalize(self.A[l], self.nq, carry)
+        if carry is not None:
+            A = self.A[pivot_hi]
+            for i in range(A.n):
+                q = tuple(A.qout[i])
+                A.block(i)[...] = A.block(i) @ carry[q]
+        return self
+
+    def bond_dim(self, l):
+        return sum(self.dims[l].values())
+
+
+def two_site_layout(sym, qloc12, qloc34, din, dout, nq):
+    """PivotVector layout of a two-site tensor: leg = combined index s1s3 of
+    Qbasis::combine (tensors/Qbasis.h:685-798); QNs of combined states in the
+    order the combined basis lists them."""
+    comb = combined_basis(sym, qloc12, qloc34)
+    ent = []
+    for s13, qm in enumerate(comb["q_of"]):
+        for qin in sorted(din):
+            for qout in sym.fuse(qin, qm):
+                if qout in dout:
+                    ent.append((s13, qin, qout, din[qin], dout[qout]))
+    return Blocks(nq, [e[1] for e in ent], [e[2] for e in ent], [e[0] for e in ent],
+                  [e[3] for e in ent], [e[4] for e in ent]), comb
+
+
+def combined_basis(sym, q12, q34):
+    """Combined basis of two local bases (restating Qbasis::combine + leftOffset
+    for bases whose QNs are pairwise distinct or repeated)."""
+    def pull(qs):
+        distinct, dim, inner = [], [], []
+        for q in qs:
+            if q not in distinct:
+                distinct.append(q)
+                dim.append(0)
+            d = distinct.index(q)
+            inner.append(dim[d])
+            dim[d] += 1
+        return distinct, dim, inner
+    d1, dim1, in1 = pull([tuple(q) for q in q12])
+    d2, dim2, in2 = pull([tuple(q) for q in q34])
+    hist = {}
+    for i, a in enumerate(d1):
+        for j, b in enumerate(d2):
+            for q in sym.fuse(a, b):
+                h = hist.setdefault(q, [])
+                if not any(e[0] == a and e[1] == b for e in h):
+                    h.append((a, b, dim1[i], dim2[j]))
+    for q in hist:
+        hist[q].sort(key=lambda e: (e[0], e[1]))
+    start, q_of, cur = {}, [], 0
+    for q in sorted(hist):
+        start[q] = cur
+        tot = sum(e[2] * e[3] for e in hist[q])
+        q_of += [q] * tot
+        cur += tot
+    index = {}
+    for s1, a in enumerate(q12):
+        for s3, b in enumerate(q34):
+            for q in sym.fuse(tuple(a), tuple(b)):
+                off = 0
+                for e in hist[q]:
+                    if e[0] == tuple(a) and e[1] == tuple(b):
+                        off += in1[s1] + e[2] * in2[s3]
+                        break
+                    off += e[2] * e[3]
+                index.setdefault((s1, s3), []).append((q, start[q] + off))
+    return {"q_of": q_of, "index": index, "n": cur}
+
+
+def contract_two_sites(sym, A1, A2, qloc12, qloc34, nq):
+    """Two-site tensor AA[s1s3](qin, qout) = sum_qmid A1[s1](qin,qmid) A2[s3](qmid,qout)
+    (abelian case of contract_AA2, tensors/DmrgContractions.h:1870-1927)."""
+    din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
+    dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
+    V, comb = two_site_layout(sym, qloc12, qloc34, din, dout, nq)
+    for (s1, s3), lst in comb["index"].items():
+        for qm, s13 in lst:
+            for i in range(A1.n):
+                if A1.leg[i] != s1:
+                    continue
+                qin = tuple(A1.qin[i])
+                qmid = tuple(A1.qout[i])
+                for j in range(A2.n):
+                    if A2.leg[j] != s3 or tuple(A2.qin[j]) != qmid:
+                        continue
+                    qout = tuple(A2.qout[j])
+                    k = V.find(s13, qin, qout)
+                    if k >= 0:
+                        V.block(k)[...] += A1.block(i) @ A2.block(j)
+    return V
