@@ -1,0 +1,339 @@
+"""Benchmark: two-site HxV throughput of the GB300 engine.
+
+Workload (one GPU, N=1): Hubbard chain t=1, U/t=4, L=64, open boundaries,
+U(1)xU(1) at half filling (N=64, Sz=0), two-site pivot in the middle of a
+seeded random MPS at bond dimension D=4096 (N(0,1) blocks, QR/LQ normalised
+towards the pivot), environments built by the engine's contract_L/contract_R.
+A step is one HxV of that pivot (Lanczos' inner operation).
+
+  value : HxV/s, split precision (BF16x3, FP32 accumulate), vectors resident in
+          HBM, timed with CUDA events on the engine's stream, CUDA graph replay
+  e2e   : HxV/s through the C ABI call vmps_hxv with pinned host buffers: the
+          host->device copy of Vin, the HxV and the device->host copy of Vout
+          are inside the timed region of every step
+
+Also reported: the plain FP64 HxV/s, the ground-state energy of the pivot
+problem from FP64 Lanczos vs split-precision Lanczos + FP64 refinement, the
+roofline of the dominant kernel and the CPU oracle (reference restatement)
+timed on the host cores.
+
+--gpus N runs N independent replicas (the path does not shard; one process
+per GPU under torchrun); value is the sum over ranks with max-over-ranks time.
+--impl reference times the CPU restatement of the reference path instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "HxV/s (two-site effective Hamiltonian, split-precision BF16x3 GPU vs FP64 GPU vs CPU)"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, local, ws, dist
+
+
+def reduce_max(dist, x, local):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_oracle_hxv_rate(L, R, V, W1, W2, threads, n_hxv, warm=1):
+    import oracle
+    oracle.set_threads(threads)
+    op = oracle.OraclePivot(2, 2, L, R, V, W1, W2)
+    v = np.random.default_rng(5).standard_normal(V.data.size)
+    for _ in range(warm):
+        op.hxv(v)
+    t0 = time.perf_counter()
+    for _ in range(n_hxv):
+        op.hxv(v)
+    dt = time.perf_counter() - t0
+    return n_hxv / dt, dt, oracle.blas_kind()
+
+
+def run_reference(args):
+    """CPU restatement of the reference path (the oracle), all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    from vmps_gb300.pivot import Context
+    from vmps_gb300.workloads import hubbard_two_site
+    oracle.build()
+    # environments need the engine once (setup, untimed); the timed work is CPU only
+    ctx = Context(0)
+    model, mps, L, R, W1, W2, V, info = hubbard_two_site(ctx, L=args.L, D=args.D, seed=args.seed)
+    ctx.close()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    op = oracle.OraclePivot(2, 2, L, R, V, W1, W2)
+    v = np.random.default_rng(5).standard_normal(V.data.size)
+    for _ in range(args.warmup):
+        op.hxv(v)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        op.hxv(v)
+    dt = time.perf_counter() - t0
+    rate = args.steps / dt
+    line = {"metric": METRIC, "value": rate, "unit": "HxV/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"hubbard_u1xu1_L{args.L}_D{args.D}_two_site_middle", "L": args.L, "D": args.D,
+                       "seed": args.seed, "D_left": info["D_left"], "dim_V": info["dim_V"]},
+            "cpu_baseline": {"value": rate, "unit": "HxV/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full HxV of the workload", "gemm": oracle.blas_kind()},
+            "e2e": {"value": rate, "unit": "HxV/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--L", type=int, default=64)
+    ap.add_argument("--D", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--precision", default="bf16x3")
+    ap.add_argument("--cpu-hxv", type=int, default=3, help="HxV applications in the CPU-baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-energy", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    rank, local, world, dist = dist_init()
+    import __graft_entry__
+    __graft_entry__.build()
+    import ctypes as C
+    import torch
+    from vmps_gb300.pivot import Context, DeviceVector, PivotMatrix2, time_hxv
+    from vmps_gb300.workloads import hubbard_two_site
+    from vmps_gb300 import _native as N
+
+    ctx = Context(local)
+    model, mps, Lenv, Renv, W1, W2, V, info = hubbard_two_site(ctx, L=args.L, D=args.D, seed=args.seed)
+    H = PivotMatrix2(ctx, model.sym, Lenv, Renv, W1, W2, V)
+    st_split = H.stats(args.precision)
+    st64 = H.stats("fp64")
+    n = H.dim
+    rng = np.random.default_rng(7)
+    v0 = rng.standard_normal(n)
+    vin = DeviceVector(H, v0)
+    vout = DeviceVector(H, None)
+    working_set = 2 * 8 * n + st_split["bytes_intermediate"] + 4 * (Lenv.data.size + Renv.data.size)
+    l2_note = "inputs larger than L2" if working_set > L2_BYTES else "working set fits L2"
+
+    # ---- device-resident HxV (value)
+    time_hxv(H, vin, vout, args.precision, n_iter=args.warmup, use_graph=True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(dist)
+    torch.cuda.synchronize(local)
+    ms, ms2 = time_hxv(H, vin, vout, args.precision, n_iter=args.steps, use_graph=True)
+    torch.cuda.synchronize(local)
+    barrier(dist)
+    clk = clocks.stop()
+    ms = reduce_max(dist, ms, local)
+    value = world * 1000.0 / ms
+
+    # ---- FP64 plain form
+    n64 = max(3, args.steps // 5)
+    time_hxv(H, vin, vout, "fp64", n_iter=2, use_graph=True)
+    ms64, ms64_2 = time_hxv(H, vin, vout, "fp64", n_iter=n64, use_graph=True)
+    ms64 = reduce_max(dist, ms64, local)
+
+    # ---- e2e through the C ABI with pinned host buffers
+    hin = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    hout = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    hin.copy_(torch.from_numpy(v0))
+    lib = N.lib()
+    pin = C.cast(C.c_void_p(hin.data_ptr()), N.f64p)
+    pout = C.cast(C.c_void_p(hout.data_ptr()), N.f64p)
+    prec = 1 if args.precision == "bf16x3" else 0
+    for _ in range(args.warmup):
+        N.check(lib.vmps_hxv(H._h, pin, pout, prec))
+    barrier(dist)
+    torch.cuda.synchronize(local)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        N.check(lib.vmps_hxv(H._h, pin, pout, prec))
+    torch.cuda.synchronize(local)
+    e2e_s = reduce_max(dist, time.perf_counter() - t0, local)
+    barrier(dist)
+    e2e = world * args.steps / e2e_s
+
+    # ---- split vs FP64 numerics on this input
+    h64 = H.apply(v0, "fp64")
+    hsp = H.apply(v0, args.precision)
+    hxv_rel_err = float(np.linalg.norm(hsp - h64) / np.linalg.norm(h64))
+
+    energy = None
+    if not args.no_energy and rank == 0:
+        e64, _, s64 = H.lanczos(v0, "fp64", max_iter=120, tol_eigval=1e-13, tol_state=1e-7)
+        es, _, ss = H.lanczos(v0, args.precision, max_iter=120, tol_eigval=1e-9, tol_state=1e-5, refine_iters=40)
+        energy = {"E_fp64": e64, "E_split_refined": es, "rel_diff": abs(es - e64) / abs(e64),
+                  "fp64": {k: s64[k] for k in ("iterations", "hxv_fp64", "residual", "ms_total")},
+                  "split": {k: ss[k] for k in ("iterations", "refine_iterations", "hxv_split", "hxv_fp64",
+                                               "residual", "energy_first", "ms_total")}}
+
+    # ---- roofline of the dominant kernel (the larger of the two grouped-GEMM phases)
+    hbm, bf16, peak_kind = load_peaks()
+    ms1 = max(ms - ms2, 1e-9)
+    phase = "phase2" if ms2 >= ms1 else "phase1"
+    flops_phase = st_split["flops_phase2"] if phase == "phase2" else st_split["flops_phase1"]
+    t_phase = ms2 if phase == "phase2" else ms1
+    tensor_flops = 3.0 * flops_phase / (t_phase * 1e-3) / 1e12     # bf16 tensor-core flops issued
+    prof = None
+    pf = os.path.join(ROOT, "profiles", "gg_split_hubbard_D4096.json")
+    if os.path.exists(pf):
+        with open(pf) as f:
+            prof = json.load(f)
+    roofline = {"bound": "tensor", "achieved": tensor_flops, "peak": bf16, "unit": "TFLOP/s",
+                "frac": tensor_flops / bf16, "traffic": (prof or {}).get(f"traffic_{phase}"),
+                "kernel": f"gg_split_kernel ({phase})", "peak_source": f"bf16_tflops of {peak_kind}",
+                "useful_tflops": flops_phase / (t_phase * 1e-3) / 1e12,
+                "note": "3 bf16 products per useful FMA (hi*hi + hi*lo + lo*hi)"}
+
+    cpu = None
+    if not args.no_cpu and world == 1 and rank == 0:
+        threads = os.cpu_count() or 1
+        rate, dt, gemm = cpu_oracle_hxv_rate(Lenv, Renv, V, W1, W2, threads, args.cpu_hxv)
+        cpu = {"value": rate, "unit": "HxV/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_hxv} full HxV of the workload ({dt:.1f} s)", "gemm": gemm,
+               "flops_per_hxv": st_split["flops_reference"]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "HxV/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3->f32 (f64 vectors)", "data": "synthetic",
+            "config": {"workload": f"hubbard_u1xu1_L{args.L}_D{args.D}_two_site_middle", "L": args.L, "D": args.D,
+                       "U": 4.0, "seed": args.seed, "D_left": info["D_left"], "sectors": info["sectors_left"],
+                       "dim_V": n, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": l2_note, "working_set_MB": round(working_set / 2 ** 20, 1),
+                       "graph": "CUDA graph per HxV (2 grouped-GEMM launches)"},
+            "e2e": {"value": e2e, "unit": "HxV/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+            "gpu_launches": 2 * args.steps,
+            "fp64": {"value": world * 1000.0 / ms64, "unit": "HxV/s", "ms_per_step": ms64,
+                     "phase2_ms": ms64_2, "flops_executed": st64["flops_executed"]},
+            "split_over_fp64": ms64 / ms,
+            "hxv_split_rel_err_vs_fp64": hxv_rel_err,
+            "energy": energy,
+            "plan": {k: st_split[k] for k in ("n_tasks", "n_chains", "n_intermediates", "n_out_blocks",
+                                              "n_tiles_phase1", "n_tiles_phase2", "flops_reference",
+                                              "flops_merged", "flops_executed", "flops_phase1", "flops_phase2",
+                                              "bytes_intermediate")},
+            "phase_ms": {"phase1": ms1, "phase2": ms2},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    vin.close()
+    vout.close()
+    H.close()
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

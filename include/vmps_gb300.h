@@ -113,6 +113,7 @@ typedef struct {
     double  flops_phase1;
     double  flops_phase2;
     double  bytes_algorithmic;/* 8*(distinct X,Z blocks used + |Y| + |out|)              */
+    double  bytes_intermediate;/* device bytes of the shared first-stage products          */
     int32_t association;      /* 0: (X*Y)*Z first, 1: X*(Y*Z) first                      */
     int32_t reserved;
 } vmps_plan_stats;

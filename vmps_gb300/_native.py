@@ -48,7 +48,8 @@ class vmps_plan_stats(C.Structure):
                 ("n_intermediates", C.c_int64), ("n_out_blocks", C.c_int64), ("n_tiles_phase1", C.c_int64),
                 ("n_tiles_phase2", C.c_int64), ("flops_reference", C.c_double), ("flops_merged", C.c_double),
                 ("flops_executed", C.c_double), ("flops_phase1", C.c_double), ("flops_phase2", C.c_double),
-                ("bytes_algorithmic", C.c_double), ("association", C.c_int32), ("reserved", C.c_int32)]
+                ("bytes_algorithmic", C.c_double), ("bytes_intermediate", C.c_double),
+                ("association", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

@@ -153,7 +153,7 @@ static void run_plan(const DevPlan& dp, int prec, const Operands& ops, cudaStrea
     }
 }
 
-static void fill_stats(const ChainSet& cs, const Plan& p, vmps_plan_stats* s) {
+static void fill_stats(const ChainSet& cs, const Plan& p, int prec, vmps_plan_stats* s) {
     std::memset(s, 0, sizeof(*s));
     s->n_tasks = cs.n_tasks;
     s->n_chains = p.n_chains;
@@ -168,6 +168,7 @@ static void fill_stats(const ChainSet& cs, const Plan& p, vmps_plan_stats* s) {
     s->flops_phase2 = p.p2.flops;
     s->flops_executed = p.p1.flops + p.p2.flops;
     s->bytes_algorithmic = p.bytes_alg;
+    s->bytes_intermediate = (double)p.T.total * (prec == VMPS_PREC_FP64 ? 8.0 : 4.0);
     s->association = p.association;
 }
 
@@ -390,9 +391,10 @@ int vmps_pivot0_create(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_bloc
     API_END
 }
 
+// Destroy functions never touch the owning context or pivot: callers (and
+// garbage collectors) may release objects in any order.  cudaFree waits for
+// the device work that still uses the memory.
 int vmps_pivot_destroy(vmps_pivot* p) {
-    if (!p) return VMPS_OK;
-    cudaStreamSynchronize(p->st());
     delete p;
     return VMPS_OK;
 }
@@ -402,7 +404,7 @@ int vmps_pivot_stats(const vmps_pivot* pc, int prec, vmps_plan_stats* out) {
     if (!pc || !out) return set_err(VMPS_E_ARG, "null argument");
     auto* p = const_cast<vmps_pivot*>(pc);
     DevPlan& dp = get_plan(p, prec);
-    fill_stats(p->cs, dp.plan, out);
+    fill_stats(p->cs, dp.plan, prec, out);
     API_END
 }
 
@@ -446,7 +448,7 @@ int vmps_dvec_create(vmps_pivot* p, vmps_dvec** out) {
     API_END
 }
 int vmps_dvec_destroy(vmps_dvec* v) {
-    if (v) { cudaStreamSynchronize(v->p->st()); delete v; }
+    delete v;
     return VMPS_OK;
 }
 int vmps_dvec_upload(vmps_dvec* v, const double* host) {
@@ -875,7 +877,7 @@ int vmps_env_stats(const vmps_env* ec, int prec, vmps_plan_stats* out) {
     if (!ec || !out) return set_err(VMPS_E_ARG, "null argument");
     auto* e = const_cast<vmps_env*>(ec);
     DevPlan& dp = env_plan(e, prec);
-    fill_stats(e->cs, dp.plan, out);
+    fill_stats(e->cs, dp.plan, prec, out);
     API_END
 }
 
@@ -909,7 +911,7 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra, const doub
 }
 
 int vmps_env_destroy(vmps_env* e) {
-    if (e) { cudaStreamSynchronize(e->st()); delete e; }
+    delete e;
     return VMPS_OK;
 }
 

@@ -146,7 +146,11 @@ class DeviceVector:
         self._h = C.c_void_p()
         N.check(N.lib().vmps_dvec_create(H._h, C.byref(self._h)))
         if host is not None:
-            self.upload(host)
+            try:
+                self.upload(host)
+            except Exception:
+                self.close()
+                raise
 
     def upload(self, host):
         host = np.ascontiguousarray(host, dtype=np.float64)

@@ -1,0 +1,60 @@
+"""Synthetic frozen-site workloads (seeded) for benchmarks and tests.
+
+A frozen site is the middle of a chain: a random MPS (N(0,1) blocks, QR/LQ
+normalised towards the pivot), its left and right environments built with the
+engine's own contract_L / contract_R on the GPU, the MPO tensors of the pivot
+sites, and the pivot vector layout.  The reference publishes no benchmark data;
+these inputs stand in for the BASELINE configurations with their shapes.
+"""
+from __future__ import annotations
+
+import time
+
+from . import models
+from .mps import RandomMPS, contract_two_sites
+from .pivot import EnvUpdate, left_vacuum, right_target
+
+
+def build_envs(ctx, model, mps, lo, hi, precision="fp64"):
+    """L env at bond lo (sites < lo) and R env at bond hi+1 (sites > hi) on the GPU."""
+    sym = model.sym
+    Lenv = left_vacuum(sym)
+    for l in range(lo):
+        e = EnvUpdate(ctx, sym, "L", Lenv, mps.A[l], model.W[l], mps.A[l])
+        Lenv = e.run(Lenv, mps.A[l], mps.A[l], precision)
+        e.close()
+    Renv = right_target(sym, mps.Qtot)
+    for l in range(model.L - 1, hi, -1):
+        e = EnvUpdate(ctx, sym, "R", Renv, mps.A[l], model.W[l], mps.A[l])
+        Renv = e.run(Renv, mps.A[l], mps.A[l], precision)
+        e.close()
+    return Lenv, Renv
+
+
+def hubbard_two_site(ctx, L=64, D=4096, U=4.0, seed=2, sigma=2.5, verbose=False):
+    """Hubbard U(1)xU(1) chain at half filling, Sz = 0; two-site pivot at the middle."""
+    t0 = time.time()
+    model = models.hubbard_u1xu1(L, t=1.0, U=U)
+    site = L // 2 - 1
+    mps = RandomMPS(model, (L, 0), D, seed=seed, profile="gaussian", sigma=[sigma, sigma])
+    mps.canonicalize(site, site + 1)
+    t1 = time.time()
+    Lenv, Renv = build_envs(ctx, model, mps, site, site + 1)
+    t2 = time.time()
+    V = contract_two_sites(model.sym, mps.A[site], mps.A[site + 1], model.qloc, model.qloc, model.sym.nq)
+    info = dict(model=model.name, L=L, D=D, site=site, seed=seed, sigma=sigma,
+                D_left=mps.bond_dim(site), D_right=mps.bond_dim(site + 2),
+                sectors_left=len(mps.dims[site]), dim_V=int(V.data.size),
+                setup_mps_s=round(t1 - t0, 2), setup_env_s=round(t2 - t1, 2))
+    if verbose:
+        print("workload", info, flush=True)
+    return model, mps, Lenv, Renv, model.W[site], model.W[site + 1], V, info
+
+
+def heisenberg_one_site(ctx, L=32, D=64, seed=1, site=None):
+    """Heisenberg U(1) chain, Sz = 0; one-site pivot (default: the middle)."""
+    model = models.heisenberg_u1(L)
+    site = L // 2 - 1 if site is None else site
+    mps = RandomMPS(model, (0,), D, seed=seed, profile="gaussian", sigma=[4.0]).canonicalize(site, site)
+    Lenv, Renv = build_envs(ctx, model, mps, site, site)
+    return model, mps, Lenv, Renv, model.W[site], mps.A[site]
