@@ -35,7 +35,11 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+import faulthandler  # noqa: E402
+
 import numpy as np  # noqa: E402
+
+faulthandler.enable()
 
 METRIC = "HxV/s (two-site effective Hamiltonian, split-precision BF16x3 GPU vs FP64 GPU vs CPU)"
 L2_BYTES = 129 * 1024 * 1024

@@ -111,6 +111,19 @@ def test_device_vectors_and_dot(gpu_ctx):
     assert rel_err(db.download(), ref) < TOL_FP64
 
 
+def test_host_hxv_after_device_vector_upload(gpu_ctx):
+    # regression: a device-vector upload must not leave the host-buffer HxV path
+    # with unallocated I/O vectors
+    model, mps, Lenv, Renv, W, V = pivot1_case("heis", L=10, D=16, site=4, seed=2)
+    H = PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V)
+    v = np.random.default_rng(4).standard_normal(H.dim)
+    dv = DeviceVector(H, v)
+    ref = oracle.OraclePivot(1, 1, Lenv, Renv, V, W).hxv(v)
+    assert rel_err(H.apply(v, "fp64"), ref) < TOL_FP64
+    assert np.array_equal(dv.download(), v)
+    dv.close()
+
+
 def test_nonfinite_input_is_rejected(gpu_ctx):
     model, mps, Lenv, Renv, W, V = pivot1_case("heis", L=8, D=8, site=3, seed=2)
     H = PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V)

@@ -495,6 +495,7 @@ cudaError_t launch_gg(int prec, int ta, int tb, int tc, const GGArgs& a, cudaStr
 
 cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, double* dst, int to_padded, cudaStream_t st) {
     if (nb <= 0) return cudaSuccess;
+    if (!blocks || !src || !dst) return cudaErrorInvalidValue;   // never launch on an unallocated buffer
     pack_kernel<<<min(nb, 4096), 256, 0, st>>>(blocks, nb, src, dst, to_padded);
     return cudaGetLastError();
 }

@@ -149,6 +149,10 @@ static void run_plan(const DevPlan& dp, int prec, const Operands& ops, cudaStrea
         a.ntiles = d.ntiles;
         a.transA = h.transA; a.transB = h.transB; a.transC = h.transC;
         if (prec == VMPS_PREC_FP64 && (ta | tb | tc)) throw std::invalid_argument("FP64 plan with float operand");
+        // every operand of a non-empty phase must be a live device buffer
+        if (d.ntiles > 0 && (!a.C || !a.tiles || !a.segs || !a.terms ||
+                             (!h.segs.empty() && (!a.A || !a.B))))
+            throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
         CK(launch_gg(prec, ta, tb, tc, a, st));
     }
 }
@@ -206,6 +210,18 @@ struct vmps_dvec_s {
     DBuf d;
     int64_t n = 0;   // padded length
 };
+
+// compact staging vectors (host layout) and padded I/O vectors of a pivot,
+// each allocated on first use and independently of the other
+static void ensure_staging(vmps_pivot* p) {
+    const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
+    if (!p->stage_in.p) p->stage_in.alloc(cb, p->st(), false);
+    if (!p->stage_out.p) p->stage_out.alloc(cb, p->st(), false);
+}
+static void ensure_io(vmps_pivot* p) {
+    if (!p->vin.p) p->vin.alloc((size_t)p->Vd.total * 8, p->st(), true);
+    if (!p->vout.p) p->vout.alloc((size_t)p->Vd.total * 8, p->st(), true);
+}
 
 static DevPlan& get_plan(vmps_pivot* p, int prec) {
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
@@ -419,13 +435,8 @@ int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int prec) {
     if (!p || !vin || !vout) return set_err(VMPS_E_ARG, "null argument");
     require_device(p->ctx);
     cudaStream_t st = p->st();
-    const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
-    if (!p->stage_in.p) {
-        p->stage_in.alloc(cb, st, false);
-        p->stage_out.alloc(cb, st, false);
-        p->vin.alloc((size_t)p->Vd.total * 8, st, true);
-        p->vout.alloc((size_t)p->Vd.total * 8, st, true);
-    }
+    ensure_staging(p);
+    ensure_io(p);
     CK(cudaMemcpyAsync(p->stage_in.p, vin, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
     CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), p->vin.as<double>(), 1, st));
     pivot_hxv_dev(p, prec, p->vin.as<double>(), p->vout.as<double>());
@@ -456,11 +467,7 @@ int vmps_dvec_upload(vmps_dvec* v, const double* host) {
     if (!v || !host) return set_err(VMPS_E_ARG, "null argument");
     vmps_pivot* p = v->p;
     cudaStream_t st = p->st();
-    if (!p->stage_in.p) {
-        const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
-        p->stage_in.alloc(cb, st, false);
-        p->stage_out.alloc(cb, st, false);
-    }
+    ensure_staging(p);
     CK(cudaMemcpyAsync(p->stage_in.p, host, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
     CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), v->d.as<double>(), 1, st));
     CK(cudaMemsetAsync(p->flag.p, 0, 4, st));
@@ -476,11 +483,7 @@ int vmps_dvec_download(const vmps_dvec* v, double* host) {
     if (!v || !host) return set_err(VMPS_E_ARG, "null argument");
     vmps_pivot* p = v->p;
     cudaStream_t st = p->st();
-    if (!p->stage_out.p) {
-        const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
-        p->stage_in.alloc(cb, st, false);
-        p->stage_out.alloc(cb, st, false);
-    }
+    ensure_staging(p);
     CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, v->d.as<double>(), p->stage_out.as<double>(), 0, st));
     CK(cudaMemcpyAsync(host, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -753,8 +756,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     kr.tmp.alloc((size_t)kr.n * 8, st, true);
     kr.coef.alloc((size_t)(kr.kmax + 2) * 8, st, true);
     // start vector
-    const size_t cb = (size_t)std::max<int64_t>(p->Vt.total, 1) * 8;
-    if (!p->stage_in.p) { p->stage_in.alloc(cb, st, false); p->stage_out.alloc(cb, st, false); }
+    ensure_staging(p);
     CK(cudaMemcpyAsync(p->stage_in.p, v, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
     CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), kr.K(0), 1, st));
     double n0 = std::sqrt(dev_dot(p, kr.K(0), kr.K(0), kr.n));
