@@ -114,7 +114,12 @@ DevLayout make_dev_layout(const std::vector<int64_t>& rows, const std::vector<in
 // GPU work items (POD, copied verbatim to the device)
 struct GTerm { int64_t off; double coef; };
 struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, K, pad; };
-struct GTile { int64_t c_off; int32_t ldc, m, n, row0, col0, seg_begin, seg_end, pad; };
+// one output tile: rows [row0, row0+tm) x cols [col0, col0+tn) of a block
+struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, pad; };
+// at most this many A terms per segment (the kernels stage them in shared memory)
+constexpr int kMaxTerms = 16;
+// tile edges: at most 64 x 64, rows split on multiples of 16, columns on multiples of 8
+constexpr int kTileMax = 64;
 
 struct PhasePlan {
     std::vector<GTerm> terms;

@@ -25,33 +25,41 @@ namespace vmps {
 // ---------------------------------------------------------------------------
 // operand access helpers
 // ---------------------------------------------------------------------------
-template <typename T> __device__ __forceinline__ double ld_d(const T* p) { return (double)__ldg(p); }
-template <typename T> __device__ __forceinline__ float ld_f(const T* p) { return (float)__ldg(p); }
-
-// A(i,k) of the segment, summed over its terms; (i,k) relative to the block
-template <typename TA, typename Acc>
-__device__ __forceinline__ Acc load_A(const TA* A, const GTerm* terms, int tb, int tc, int lda, bool trans, int i,
-                                      int k) {
-    Acc v = 0;
-    const int64_t e = trans ? ((int64_t)k + (int64_t)i * lda) : ((int64_t)i + (int64_t)k * lda);
-    for (int t = 0; t < tc; ++t) {
-        const GTerm tm = terms[tb + t];
-        v += (Acc)tm.coef * (Acc)__ldg(A + tm.off + e);
-    }
-    return v;
+// ---------------------------------------------------------------------------
+// Operand staging.  Device blocks are column-major with ld a multiple of 8,
+// start offsets aligned to 32 elements and zero padding, and tile origins are
+// multiples of 16 (rows) / 8 (columns), so every 4-element group read below is
+// 16-byte aligned and stays inside its block's padded storage.  Groups whose
+// first element lies outside the tile are replaced by zeros; elements past the
+// block edge inside a group are either zero padding or rows/columns that only
+// reach output entries the epilogue masks off.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void ldg4(const float* p, float (&v)[4]) {
+    const float4 x = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
 }
-template <typename TB, typename Acc>
-__device__ __forceinline__ Acc load_B(const TB* B, int64_t off, int ldb, bool trans, int k, int j) {
-    const int64_t e = trans ? ((int64_t)j + (int64_t)k * ldb) : ((int64_t)k + (int64_t)j * ldb);
-    return (Acc)__ldg(B + off + e);
+__device__ __forceinline__ void ldg4(const double* p, float (&v)[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    v[0] = (float)a.x; v[1] = (float)a.y; v[2] = (float)b.x; v[3] = (float)b.y;
+}
+__device__ __forceinline__ void ldg2(const double* p, double (&v)[2]) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    v[0] = a.x; v[1] = a.y;
 }
 
 // ===========================================================================
-// FP64 grouped GEMM, 64x64 tile, 128 threads (2x2 warps of 32x32), BK = 16
+// FP64 grouped GEMM: tile <= 64x64, 128 threads (2x2 warps of 32x32), BK = 16,
+// DMMA m8n8k4.  Shared layouts follow the contiguous global dimension:
+//   A row-contiguous  -> As[k][m] (stride 68)   A k-contiguous -> As[m][k] (stride 20)
+//   B k-contiguous    -> Bs[n][k] (stride 20)   B col-contiguous -> Bs[k][n] (stride 68)
+// (strides keep every half-warp of fragment reads on distinct banks).
 // ===========================================================================
 namespace f64k {
 constexpr int BM = 64, BN = 64, BK = 16, NT = 128;
-constexpr int SA = BM + 4, SB = BN + 4;   // padded strides: conflict-free fragment reads
+constexpr int SMN = 68;   // [k][m] / [k][n] row stride (doubles)
+constexpr int SKK = 20;   // [m][k] / [n][k] row stride (doubles)
+constexpr int OP_ELEMS = BM * SKK > BK * SMN ? BM * SKK : BK * SMN;   // 1280 vs 1088
 }
 
 __device__ __forceinline__ void dmma(double& d0, double& d1, double a, double b) {
@@ -60,16 +68,17 @@ __device__ __forceinline__ void dmma(double& d0, double& d1, double a, double b)
                  : "d"(a), "d"(b));
 }
 
-__global__ void __launch_bounds__(f64k::NT) gg_fp64_kernel(GGArgs g) {
+__global__ void __launch_bounds__(f64k::NT, 3) gg_fp64_kernel(GGArgs g) {
     using namespace f64k;
-    __shared__ double As[2][BK][SA];
-    __shared__ double Bs[2][BK][SB];
+    __shared__ __align__(16) double As[2][OP_ELEMS];
+    __shared__ __align__(16) double Bs[2][OP_ELEMS];
     const GTile tile = g.tiles[blockIdx.x];
     const double* __restrict__ A = (const double*)g.A;
     const double* __restrict__ B = (const double*)g.B;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-    const int mrem = min(BM, tile.m - tile.row0), nrem = min(BN, tile.n - tile.col0);
+    const int mrem = tile.tm, nrem = tile.tn;
+    const bool tA = g.transA, tB = g.transB;
 
     double acc[4][4][2];
 #pragma unroll
@@ -77,109 +86,135 @@ __global__ void __launch_bounds__(f64k::NT) gg_fp64_kernel(GGArgs g) {
 #pragma unroll
         for (int b = 0; b < 4; ++b) acc[a][b][0] = acc[a][b][1] = 0.0;
 
-    double ra[8], rb[8];
-    int seg = tile.seg_begin, k0 = 0;
-    // staged load of (seg, k0) into registers
-    auto stage = [&](int s, int kk0) {
+    // each thread stages 4 double2 of A and 4 of B per BK step
+    double ra[4][2], rb[4][2];
+    auto stage = [&](int s, int k0) {
         const GSeg sg = g.segs[s];
-        const int krem = sg.K - kk0;
+        const int krem = sg.K - k0;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
+        for (int r = 0; r < 4; ++r) {
+            const int v = tid + NT * r;   // 512 pairs per operand tile
             int i, k;
-            if (!g.transA) { i = tid & 63; k = (tid >> 6) + 2 * r; }
-            else { k = tid & 15; i = (tid >> 4) + 8 * r; }
-            ra[r] = (i < mrem && k < krem)
-                        ? load_A<double, double>(A, g.terms, sg.term_begin, sg.term_count, sg.lda, g.transA,
-                                                 tile.row0 + i, kk0 + k)
-                        : 0.0;
+            if (!tA) { i = (v & 31) * 2; k = v >> 5; }      // m-pairs along rows, 16 k columns
+            else     { k = (v & 7) * 2;  i = v >> 3; }      // k-pairs, 64 rows
+            ra[r][0] = ra[r][1] = 0.0;
+            if (i < mrem && k < krem) {
+                const int64_t e = tA ? ((int64_t)(k0 + k) + (int64_t)(tile.row0 + i) * sg.lda)
+                                     : ((int64_t)(tile.row0 + i) + (int64_t)(k0 + k) * sg.lda);
+                for (int t = 0; t < sg.term_count; ++t) {
+                    const GTerm tm = g.terms[sg.term_begin + t];
+                    double x[2];
+                    ldg2(A + tm.off + e, x);
+                    ra[r][0] = fma(tm.coef, x[0], ra[r][0]);
+                    ra[r][1] = fma(tm.coef, x[1], ra[r][1]);
+                }
+            }
             int j, kb;
-            if (!g.transB) { kb = tid & 15; j = (tid >> 4) + 8 * r; }
-            else { j = tid & 63; kb = (tid >> 6) + 2 * r; }
-            rb[r] = (j < nrem && kb < krem) ? load_B<double, double>(B, sg.b_off, sg.ldb, g.transB, kk0 + kb,
-                                                                      tile.col0 + j)
-                                            : 0.0;
+            if (!tB) { kb = (v & 7) * 2;  j = v >> 3; }
+            else     { j = (v & 31) * 2;  kb = v >> 5; }
+            rb[r][0] = rb[r][1] = 0.0;
+            if (j < nrem && kb < krem) {
+                const int64_t e = tB ? ((int64_t)(tile.col0 + j) + (int64_t)(k0 + kb) * sg.ldb)
+                                     : ((int64_t)(k0 + kb) + (int64_t)(tile.col0 + j) * sg.ldb);
+                ldg2(B + sg.b_off + e, rb[r]);
+            }
         }
     };
     auto commit = [&](int buf) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            int i, k;
-            if (!g.transA) { i = tid & 63; k = (tid >> 6) + 2 * r; }
-            else { k = tid & 15; i = (tid >> 4) + 8 * r; }
-            As[buf][k][i] = ra[r];
-            int j, kb;
-            if (!g.transB) { kb = tid & 15; j = (tid >> 4) + 8 * r; }
-            else { j = tid & 63; kb = (tid >> 6) + 2 * r; }
-            Bs[buf][kb][j] = rb[r];
+        for (int r = 0; r < 4; ++r) {
+            const int v = tid + NT * r;
+            if (!tA) { const int i = (v & 31) * 2, k = v >> 5;
+                       *reinterpret_cast<double2*>(&As[buf][k * SMN + i]) = make_double2(ra[r][0], ra[r][1]); }
+            else     { const int k = (v & 7) * 2, i = v >> 3;
+                       *reinterpret_cast<double2*>(&As[buf][i * SKK + k]) = make_double2(ra[r][0], ra[r][1]); }
+            if (!tB) { const int kb = (v & 7) * 2, j = v >> 3;
+                       *reinterpret_cast<double2*>(&Bs[buf][j * SKK + kb]) = make_double2(rb[r][0], rb[r][1]); }
+            else     { const int j = (v & 31) * 2, kb = v >> 5;
+                       *reinterpret_cast<double2*>(&Bs[buf][kb * SMN + j]) = make_double2(rb[r][0], rb[r][1]); }
         }
     };
-    auto advance = [&](int& s, int& kk0) {
-        kk0 += BK;
-        if (kk0 >= g.segs[s].K) { kk0 = 0; ++s; }
-    };
 
+    int seg = tile.seg_begin, k0 = 0;
+    // warps whose 32x32 sub-tile is entirely outside the tile skip the MMAs
+    const bool warp_live = wm < mrem && wn < nrem;
     if (seg < tile.seg_end) {
         stage(seg, k0);
         int buf = 0;
         while (true) {
             commit(buf);
             __syncthreads();
-            int ns = seg, nk = k0;
-            advance(ns, nk);
+            int ns = seg, nk = k0 + BK;
+            if (nk >= g.segs[seg].K) { nk = 0; ++ns; }
             const bool more = ns < tile.seg_end;
             if (more) stage(ns, nk);
-            const int g4 = lane >> 2, t4 = lane & 3;
+            if (warp_live) {
+                const int g4 = lane >> 2, t4 = lane & 3;
 #pragma unroll
-            for (int kq = 0; kq < BK; kq += 4) {
-                double af[4], bf[4];
+                for (int kq = 0; kq < BK; kq += 4) {
+                    double af[4], bf[4];
 #pragma unroll
-                for (int mi = 0; mi < 4; ++mi) af[mi] = As[buf][kq + t4][wm + mi * 8 + g4];
+                    for (int mi = 0; mi < 4; ++mi) {
+                        const int m = wm + mi * 8 + g4, k = kq + t4;
+                        af[mi] = tA ? As[buf][m * SKK + k] : As[buf][k * SMN + m];
+                    }
 #pragma unroll
-                for (int ni = 0; ni < 4; ++ni) bf[ni] = Bs[buf][kq + t4][wn + ni * 8 + g4];
+                    for (int ni = 0; ni < 4; ++ni) {
+                        const int n = wn + ni * 8 + g4, k = kq + t4;
+                        bf[ni] = tB ? Bs[buf][k * SMN + n] : Bs[buf][n * SKK + k];
+                    }
 #pragma unroll
-                for (int mi = 0; mi < 4; ++mi)
+                    for (int mi = 0; mi < 4; ++mi)
 #pragma unroll
-                    for (int ni = 0; ni < 4; ++ni) dmma(acc[mi][ni][0], acc[mi][ni][1], af[mi], bf[ni]);
+                        for (int ni = 0; ni < 4; ++ni) dmma(acc[mi][ni][0], acc[mi][ni][1], af[mi], bf[ni]);
+                }
             }
             if (!more) break;
             seg = ns; k0 = nk;
             buf ^= 1;
         }
     }
-    {
-        double* __restrict__ C = (double*)g.C;
-        const int g4 = lane >> 2, t4 = lane & 3;
+    double* __restrict__ C = (double*)g.C;
+    const int g4 = lane >> 2, t4 = lane & 3;
 #pragma unroll
-        for (int mi = 0; mi < 4; ++mi)
+    for (int mi = 0; mi < 4; ++mi)
 #pragma unroll
-            for (int ni = 0; ni < 4; ++ni)
+        for (int ni = 0; ni < 4; ++ni)
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int r = wm + mi * 8 + g4, c = wn + ni * 8 + t4 * 2 + h;
-                    if (r < mrem && c < nrem) {
-                        const int64_t gr = tile.row0 + r, gc = tile.col0 + c;
-                        const int64_t e = g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc);
-                        C[tile.c_off + e] = acc[mi][ni][h];
-                    }
+            for (int h = 0; h < 2; ++h) {
+                const int r = wm + mi * 8 + g4, c = wn + ni * 8 + t4 * 2 + h;
+                if (r < mrem && c < nrem) {
+                    const int64_t gr = tile.row0 + r, gc = tile.col0 + c;
+                    const int64_t e = g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc);
+                    C[tile.c_off + e] = acc[mi][ni][h];
                 }
-    }
+            }
 }
 
 // ===========================================================================
-// BF16x3 split-precision grouped GEMM, 128x128 tile, 256 threads (2x4 warps of
-// 64x32), BK = 32, mma.sync m16n8k16 bf16 -> f32
+// BF16x3 split-precision grouped GEMM: tile <= 64x64, 128 threads (2x2 warps
+// of 32x32), BK = 32, mma.sync m16n8k16 bf16 -> f32.  Operands are read as
+// fp32/fp64 16-byte groups, scaled and summed over the segment's terms in
+// fp32, split into hi/lo bf16 and stored in shared memory in the layout that
+// matches the contiguous global dimension; fragments come from ldmatrix
+// (k-contiguous layouts) or ldmatrix.trans (row-/column-contiguous layouts).
 // ===========================================================================
 namespace spk {
-constexpr int BM = 128, BN = 128, BK = 32, NT = 256;
-constexpr int LDS = BK + 8;   // 80-byte rows: ldmatrix reads are conflict-free
-constexpr int TILE_ELEMS = BM * LDS;
-constexpr int SMEM_BYTES = 2 /*stages*/ * 4 /*Ahi,Alo,Bhi,Blo*/ * TILE_ELEMS * 2 /*bytes*/;
+constexpr int BM = 64, BN = 64, BK = 32, NT = 128;
+constexpr int SMN = BM + 8;   // [k][m] / [k][n] row stride (bf16): 144 B, conflict-free ldmatrix
+constexpr int SKK = BK + 8;   // [m][k] / [n][k] row stride (bf16): 80 B
+constexpr int OP_ELEMS = BM * SKK > BK * SMN ? BM * SKK : BK * SMN;   // 2560
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, uint32_t addr) {
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, uint32_t addr) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
                  : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
                  : "r"(addr));
 }
@@ -190,84 +225,100 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
-// split two fp32 values into packed bf16x2 hi and lo words
-__device__ __forceinline__ void split2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
-    __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
-    __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
-    __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
-    hi = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-    lo = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+// split four fp32 values into packed hi and lo bf16 quadruples
+__device__ __forceinline__ void split4(const float (&x)[4], uint2& hi, uint2& lo) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const __nv_bfloat16 bh = __float2bfloat16_rn(x[i]);
+        const __nv_bfloat16 bl = __float2bfloat16_rn(x[i] - __bfloat162float(bh));
+        h[i] = __bfloat16_as_ushort(bh);
+        l[i] = __bfloat16_as_ushort(bl);
+    }
+    hi = make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
+    lo = make_uint2(l[0] | (l[1] << 16), l[2] | (l[3] << 16));
 }
 
 template <typename TA, typename TB, typename TC>
-__global__ void __launch_bounds__(spk::NT) gg_split_kernel(GGArgs g) {
+__global__ void __launch_bounds__(spk::NT, 4) gg_split_kernel(GGArgs g) {
     using namespace spk;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __nv_bfloat16* sm = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    // stage s: [Ahi | Alo | Bhi | Blo], each BM x LDS (A rows = m, B rows = n, k contiguous)
-    auto tileptr = [&](int stage, int which) { return sm + (stage * 4 + which) * TILE_ELEMS; };
-
+    // [stage][Ahi, Alo, Bhi, Blo]
+    __shared__ __align__(128) __nv_bfloat16 sm[2][4][OP_ELEMS];
     const GTile tile = g.tiles[blockIdx.x];
     const TA* __restrict__ A = (const TA*)g.A;
     const TB* __restrict__ B = (const TB*)g.B;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = (warp >> 2) * 64, wn = (warp & 3) * 32;
-    const int mrem = min(BM, tile.m - tile.row0), nrem = min(BN, tile.n - tile.col0);
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int mrem = tile.tm, nrem = tile.tn;
+    const bool tA = g.transA, tB = g.transB;
 
-    float acc[4][4][4];
+    float acc[2][4][4];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int a = 0; a < 2; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b)
 #pragma unroll
             for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
 
-    // staging registers: 8 pairs for A, 8 pairs for B (fp32)
-    float ra[8][2], rb[8][2];
-    auto stage = [&](int s, int kk0) {
+    // 512 groups of 4 per operand tile (64 x 32): 4 per thread
+    float ra[4][4], rb[4][4];
+    auto stage = [&](int s, int k0) {
         const GSeg sg = g.segs[s];
-        const int krem = sg.K - kk0;
+        const int krem = sg.K - k0;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            int i, kp;
-            if (!g.transA) { i = tid & 127; kp = ((tid >> 7) + 2 * r) * 2; }
-            else { kp = (tid & 15) * 2; i = (tid >> 4) + 16 * r; }
+        for (int r = 0; r < 4; ++r) {
+            const int v = tid + NT * r;
+            int i, k;
+            if (!tA) { i = (v & 15) * 4; k = v >> 4; }     // row quads, 32 k columns
+            else     { k = (v & 7) * 4;  i = v >> 3; }     // k quads, 64 rows
 #pragma unroll
-            for (int h = 0; h < 2; ++h)
-                ra[r][h] = (i < mrem && kp + h < krem)
-                               ? load_A<TA, float>(A, g.terms, sg.term_begin, sg.term_count, sg.lda, g.transA,
-                                                   tile.row0 + i, kk0 + kp + h)
-                               : 0.f;
-            int j, kq;
-            if (!g.transB) { kq = (tid & 15) * 2; j = (tid >> 4) + 16 * r; }
-            else { j = tid & 127; kq = ((tid >> 7) + 2 * r) * 2; }
+            for (int q = 0; q < 4; ++q) ra[r][q] = 0.f;
+            if (i < mrem && k < krem) {
+                const int64_t e = tA ? ((int64_t)(k0 + k) + (int64_t)(tile.row0 + i) * sg.lda)
+                                     : ((int64_t)(tile.row0 + i) + (int64_t)(k0 + k) * sg.lda);
+                for (int t = 0; t < sg.term_count; ++t) {
+                    const GTerm tm = g.terms[sg.term_begin + t];
+                    const float c = (float)tm.coef;
+                    float x[4];
+                    ldg4(A + tm.off + e, x);
 #pragma unroll
-            for (int h = 0; h < 2; ++h)
-                rb[r][h] = (j < nrem && kq + h < krem)
-                               ? load_B<TB, float>(B, sg.b_off, sg.ldb, g.transB, kk0 + kq + h, tile.col0 + j)
-                               : 0.f;
+                    for (int q = 0; q < 4; ++q) ra[r][q] = fmaf(c, x[q], ra[r][q]);
+                }
+            }
+            int j, kb;
+            if (!tB) { kb = (v & 7) * 4;  j = v >> 3; }    // k quads, 64 columns
+            else     { j = (v & 15) * 4;  kb = v >> 4; }   // column quads, 32 k rows
+#pragma unroll
+            for (int q = 0; q < 4; ++q) rb[r][q] = 0.f;
+            if (j < nrem && kb < krem) {
+                const int64_t e = tB ? ((int64_t)(tile.col0 + j) + (int64_t)(k0 + kb) * sg.ldb)
+                                     : ((int64_t)(k0 + kb) + (int64_t)(tile.col0 + j) * sg.ldb);
+                ldg4(B + sg.b_off + e, rb[r]);
+            }
         }
     };
     auto commit = [&](int st) {
-        __nv_bfloat16 *Ah = tileptr(st, 0), *Al = tileptr(st, 1), *Bh = tileptr(st, 2), *Bl = tileptr(st, 3);
+        __nv_bfloat16 *Ah = sm[st][0], *Al = sm[st][1], *Bh = sm[st][2], *Bl = sm[st][3];
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            int i, kp;
-            if (!g.transA) { i = tid & 127; kp = ((tid >> 7) + 2 * r) * 2; }
-            else { kp = (tid & 15) * 2; i = (tid >> 4) + 16 * r; }
-            uint32_t hi, lo;
-            split2(ra[r][0], ra[r][1], hi, lo);
-            *reinterpret_cast<uint32_t*>(Ah + i * LDS + kp) = hi;
-            *reinterpret_cast<uint32_t*>(Al + i * LDS + kp) = lo;
-            int j, kq;
-            if (!g.transB) { kq = (tid & 15) * 2; j = (tid >> 4) + 16 * r; }
-            else { j = tid & 127; kq = ((tid >> 7) + 2 * r) * 2; }
-            split2(rb[r][0], rb[r][1], hi, lo);
-            *reinterpret_cast<uint32_t*>(Bh + j * LDS + kq) = hi;
-            *reinterpret_cast<uint32_t*>(Bl + j * LDS + kq) = lo;
+        for (int r = 0; r < 4; ++r) {
+            const int v = tid + NT * r;
+            uint2 hi, lo;
+            split4(ra[r], hi, lo);
+            int ia;
+            if (!tA) { const int i = (v & 15) * 4, k = v >> 4; ia = k * SMN + i; }
+            else     { const int k = (v & 7) * 4, i = v >> 3;  ia = i * SKK + k; }
+            *reinterpret_cast<uint2*>(Ah + ia) = hi;
+            *reinterpret_cast<uint2*>(Al + ia) = lo;
+            split4(rb[r], hi, lo);
+            int ib;
+            if (!tB) { const int kb = (v & 7) * 4, j = v >> 3; ib = j * SKK + kb; }
+            else     { const int j = (v & 15) * 4, kb = v >> 4; ib = kb * SMN + j; }
+            *reinterpret_cast<uint2*>(Bh + ib) = hi;
+            *reinterpret_cast<uint2*>(Bl + ib) = lo;
         }
     };
 
+    const bool warp_live = wm < mrem && wn < nrem;
     int seg = tile.seg_begin, k0 = 0;
     if (seg < tile.seg_end) {
         stage(seg, k0);
@@ -279,35 +330,46 @@ __global__ void __launch_bounds__(spk::NT) gg_split_kernel(GGArgs g) {
             if (nk >= g.segs[seg].K) { nk = 0; ++ns; }
             const bool more = ns < tile.seg_end;
             if (more) stage(ns, nk);
-            const __nv_bfloat16 *Ah = tileptr(st, 0), *Al = tileptr(st, 1), *Bh = tileptr(st, 2),
-                                *Bl = tileptr(st, 3);
+            if (warp_live) {
+                const __nv_bfloat16 *Ah = sm[st][0], *Al = sm[st][1], *Bh = sm[st][2], *Bl = sm[st][3];
 #pragma unroll
-            for (int kk = 0; kk < BK; kk += 16) {
-                uint32_t ah[4][4], al[4][4], bh[4][2], bl[4][2];
+                for (int kk = 0; kk < BK; kk += 16) {
+                    uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
 #pragma unroll
-                for (int mi = 0; mi < 4; ++mi) {
-                    const int row = wm + mi * 16 + (lane & 15);
-                    const int col = kk + (lane >> 4) * 8;
-                    ldsm_x4(ah[mi][0], ah[mi][1], ah[mi][2], ah[mi][3], smem_u32(Ah + row * LDS + col));
-                    ldsm_x4(al[mi][0], al[mi][1], al[mi][2], al[mi][3], smem_u32(Al + row * LDS + col));
-                }
-#pragma unroll
-                for (int np = 0; np < 2; ++np) {
-                    const int row = wn + np * 16 + (lane & 7) + ((lane >> 4) << 3);
-                    const int col = kk + ((lane >> 3) & 1) * 8;
-                    ldsm_x4(bh[2 * np][0], bh[2 * np][1], bh[2 * np + 1][0], bh[2 * np + 1][1],
-                            smem_u32(Bh + row * LDS + col));
-                    ldsm_x4(bl[2 * np][0], bl[2 * np][1], bl[2 * np + 1][0], bl[2 * np + 1][1],
-                            smem_u32(Bl + row * LDS + col));
-                }
-#pragma unroll
-                for (int mi = 0; mi < 4; ++mi)
-#pragma unroll
-                    for (int ni = 0; ni < 4; ++ni) {
-                        mma_bf16(acc[mi][ni], al[mi], bh[ni][0], bh[ni][1]);
-                        mma_bf16(acc[mi][ni], ah[mi], bl[ni][0], bl[ni][1]);
-                        mma_bf16(acc[mi][ni], ah[mi], bh[ni][0], bh[ni][1]);
+                    for (int mi = 0; mi < 2; ++mi) {
+                        const int mb = wm + mi * 16;
+                        if (tA) {   // [m][k]: plain ldmatrix
+                            const int off = (mb + (lane & 15)) * SKK + kk + (lane >> 4) * 8;
+                            ldsm_x4(ah[mi][0], ah[mi][1], ah[mi][2], ah[mi][3], smem_u32(Ah + off));
+                            ldsm_x4(al[mi][0], al[mi][1], al[mi][2], al[mi][3], smem_u32(Al + off));
+                        } else {    // [k][m]: transposing ldmatrix
+                            const int off = (kk + (lane & 7) + ((lane >> 4) & 1) * 8) * SMN + mb + ((lane >> 3) & 1) * 8;
+                            ldsm_x4_t(ah[mi][0], ah[mi][1], ah[mi][2], ah[mi][3], smem_u32(Ah + off));
+                            ldsm_x4_t(al[mi][0], al[mi][1], al[mi][2], al[mi][3], smem_u32(Al + off));
+                        }
                     }
+#pragma unroll
+                    for (int np = 0; np < 2; ++np) {
+                        const int nb = wn + np * 16;
+                        if (!tB) {  // [n][k]: plain ldmatrix
+                            const int off = (nb + (lane & 7) + ((lane >> 4) << 3)) * SKK + kk + ((lane >> 3) & 1) * 8;
+                            ldsm_x4(bh[2 * np][0], bh[2 * np][1], bh[2 * np + 1][0], bh[2 * np + 1][1], smem_u32(Bh + off));
+                            ldsm_x4(bl[2 * np][0], bl[2 * np][1], bl[2 * np + 1][0], bl[2 * np + 1][1], smem_u32(Bl + off));
+                        } else {    // [k][n]: transposing ldmatrix
+                            const int off = (kk + (lane & 7) + ((lane >> 3) & 1) * 8) * SMN + nb + (lane >> 4) * 8;
+                            ldsm_x4_t(bh[2 * np][0], bh[2 * np][1], bh[2 * np + 1][0], bh[2 * np + 1][1], smem_u32(Bh + off));
+                            ldsm_x4_t(bl[2 * np][0], bl[2 * np][1], bl[2 * np + 1][0], bl[2 * np + 1][1], smem_u32(Bl + off));
+                        }
+                    }
+#pragma unroll
+                    for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+                        for (int ni = 0; ni < 4; ++ni) {
+                            mma_bf16(acc[mi][ni], al[mi], bh[ni][0], bh[ni][1]);
+                            mma_bf16(acc[mi][ni], ah[mi], bl[ni][0], bl[ni][1]);
+                            mma_bf16(acc[mi][ni], ah[mi], bh[ni][0], bh[ni][1]);
+                        }
+                }
             }
             if (!more) break;
             seg = ns; k0 = nk;
@@ -318,7 +380,7 @@ __global__ void __launch_bounds__(spk::NT) gg_split_kernel(GGArgs g) {
     TC* __restrict__ C = (TC*)g.C;
     const int g4 = lane >> 2, t4 = lane & 3;
 #pragma unroll
-    for (int mi = 0; mi < 4; ++mi)
+    for (int mi = 0; mi < 2; ++mi)
 #pragma unroll
         for (int ni = 0; ni < 4; ++ni)
 #pragma unroll
@@ -456,20 +518,8 @@ static int grid_for(int64_t n, int threads, int cap) {
 // opt the split kernels into their dynamic shared memory size (once per process,
 // before any launch or stream capture)
 cudaError_t kernels_init() {
-    cudaError_t e = cudaSuccess;
-    auto set = [&](const void* f) {
-        cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, spk::SMEM_BYTES);
-        if (r != cudaSuccess) e = r;
-    };
-    set((const void*)gg_split_kernel<double, double, double>);
-    set((const void*)gg_split_kernel<double, double, float>);
-    set((const void*)gg_split_kernel<double, float, double>);
-    set((const void*)gg_split_kernel<double, float, float>);
-    set((const void*)gg_split_kernel<float, double, double>);
-    set((const void*)gg_split_kernel<float, double, float>);
-    set((const void*)gg_split_kernel<float, float, double>);
-    set((const void*)gg_split_kernel<float, float, float>);
-    return e;
+    // all grouped-GEMM kernels use static shared memory below 48 KB
+    return cudaSuccess;
 }
 
 cudaError_t launch_gg(int prec, int ta, int tb, int tc, const GGArgs& a, cudaStream_t st) {
@@ -481,14 +531,14 @@ cudaError_t launch_gg(int prec, int ta, int tb, int tc, const GGArgs& a, cudaStr
     // split precision: type codes 0 = double, 1 = float
     const int code = ta * 4 + tb * 2 + tc;
     switch (code) {
-        case 0: gg_split_kernel<double, double, double><<<a.ntiles, spk::NT, spk::SMEM_BYTES, st>>>(a); break;
-        case 1: gg_split_kernel<double, double, float><<<a.ntiles, spk::NT, spk::SMEM_BYTES, st>>>(a); break;
-        case 2: gg_split_kernel<double, float, double><<<a.ntiles, spk::NT, spk::SMEM_BYTES, st>>>(a); break;
-        case 3: gg_split_kernel<double, float, float><<<a.ntiles, spk::NT, spk::SMEM_BYTES, st>>>(a); break;
-        case 4: gg_split_kernel<float, double, double><<<a.ntiles, spk::NT, spk::SMEM_BYTES, st>>>(a); break;
-        case 5: gg_split_kernel<float, double, float><<<a.ntiles, spk::NT, spk::SMEM_BYTES, st>>>(a); break;
-        case 6: gg_split_kernel<float, float, double><<<a.ntiles, spk::NT, spk::SMEM_BYTES, st>>>(a); break;
-        case 7: gg_split_kernel<float, float, float><<<a.ntiles, spk::NT, spk::SMEM_BYTES, st>>>(a); break;
+        case 0: gg_split_kernel<double, double, double><<<a.ntiles, spk::NT, 0, st>>>(a); break;
+        case 1: gg_split_kernel<double, double, float><<<a.ntiles, spk::NT, 0, st>>>(a); break;
+        case 2: gg_split_kernel<double, float, double><<<a.ntiles, spk::NT, 0, st>>>(a); break;
+        case 3: gg_split_kernel<double, float, float><<<a.ntiles, spk::NT, 0, st>>>(a); break;
+        case 4: gg_split_kernel<float, double, double><<<a.ntiles, spk::NT, 0, st>>>(a); break;
+        case 5: gg_split_kernel<float, double, float><<<a.ntiles, spk::NT, 0, st>>>(a); break;
+        case 6: gg_split_kernel<float, float, double><<<a.ntiles, spk::NT, 0, st>>>(a); break;
+        case 7: gg_split_kernel<float, float, float><<<a.ntiles, spk::NT, 0, st>>>(a); break;
     }
     return cudaGetLastError();
 }

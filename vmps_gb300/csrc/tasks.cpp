@@ -593,18 +593,33 @@ struct Key4Hash {
     }
 };
 
+// split an extent into balanced pieces of at most kTileMax, each a multiple of
+// `gran` except the last: 193 -> 48,48,48,49 rather than 64,64,64,1
+static std::vector<std::pair<int64_t, int64_t>> split_extent(int64_t m, int64_t gran) {
+    std::vector<std::pair<int64_t, int64_t>> out;
+    const int64_t nt = (m + kTileMax - 1) / kTileMax;
+    int64_t base = gran * (m / (nt * gran));
+    if (base < gran || m - base * (nt - 1) > kTileMax) base = gran * ((m + nt * gran - 1) / (nt * gran));
+    int64_t r = 0;
+    for (int64_t i = 0; i < nt && r < m; ++i) {
+        const int64_t len = (i + 1 == nt) ? m - r : std::min(base, m - r);
+        out.push_back({r, len});
+        r += len;
+    }
+    return out;
+}
+
 // append tiles of an m x n output block whose segments are [sb, se)
-void add_tiles(PhasePlan& ph, int64_t c_off, int64_t ldc, int64_t m, int64_t n, int32_t sb, int32_t se, int tm,
-               int tn) {
-    for (int64_t r0 = 0; r0 < m; r0 += tm)
-        for (int64_t c0 = 0; c0 < n; c0 += tn) {
+void add_tiles(PhasePlan& ph, int64_t c_off, int64_t ldc, int64_t m, int64_t n, int32_t sb, int32_t se, int, int) {
+    for (const auto& rs : split_extent(m, 16))
+        for (const auto& cs : split_extent(n, 8)) {
             GTile t{};
             t.c_off = c_off;
             t.ldc = (int32_t)ldc;
-            t.m = (int32_t)m;
-            t.n = (int32_t)n;
-            t.row0 = (int32_t)r0;
-            t.col0 = (int32_t)c0;
+            t.row0 = (int32_t)rs.first;
+            t.tm = (int32_t)rs.second;
+            t.col0 = (int32_t)cs.first;
+            t.tn = (int32_t)cs.second;
             t.seg_begin = sb;
             t.seg_end = se;
             ph.tiles.push_back(t);
@@ -619,7 +634,7 @@ void sort_tiles(PhasePlan& ph) {
         const GTile& t = ph.tiles[i];
         double k = 0;
         for (int s = t.seg_begin; s < t.seg_end; ++s) k += ph.segs[s].K * (double)ph.segs[s].term_count;
-        cost[i] = k * std::min(64, t.m - t.row0) * std::min(64, t.n - t.col0) + 1.0;
+        cost[i] = k * t.tm * t.tn + 1.0;
     }
     std::vector<size_t> idx(ph.tiles.size());
     std::iota(idx.begin(), idx.end(), 0);
@@ -792,7 +807,7 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
                 s.lda = (int32_t)P.T.ld[t];
                 ++jj;
             }
-            s.term_count = (int32_t)p2.terms.size() - s.term_begin;
+            const int32_t tend = (int32_t)p2.terms.size();
             if (P.association == 0) {
                 s.b_off = Z.off[other];
                 s.ldb = (int32_t)Z.ld[other];
@@ -802,7 +817,14 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
                 s.ldb = (int32_t)X.ld[other];
                 s.K = (int32_t)xk(other);
             }
-            p2.segs.push_back(s);
+            // a segment carries at most kMaxTerms terms: longer sums become several
+            // segments with the same B operand
+            for (int32_t tb = s.term_begin; tb < tend; tb += kMaxTerms) {
+                GSeg part = s;
+                part.term_begin = tb;
+                part.term_count = std::min<int32_t>(kMaxTerms, tend - tb);
+                p2.segs.push_back(part);
+            }
             j = jj;
         }
         int32_t se = (int32_t)p2.segs.size();
