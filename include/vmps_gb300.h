@@ -114,6 +114,9 @@ typedef struct {
     double  flops_phase2;
     double  bytes_algorithmic;/* 8*(distinct X,Z blocks used + |Y| + |out|)              */
     double  bytes_intermediate;/* device bytes of the shared first-stage products          */
+    int64_t n_segments_phase2;/* (out, B-operand) groups of the second stage              */
+    int64_t n_terms_phase2;   /* first-stage products summed into them                    */
+    double  flops_phase2_unsummed; /* second stage without summing first-stage products    */
     int32_t association;      /* 0: (X*Y)*Z first, 1: X*(Y*Z) first                      */
     int32_t reserved;
 } vmps_plan_stats;

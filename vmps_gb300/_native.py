@@ -49,6 +49,8 @@ class vmps_plan_stats(C.Structure):
                 ("n_tiles_phase2", C.c_int64), ("flops_reference", C.c_double), ("flops_merged", C.c_double),
                 ("flops_executed", C.c_double), ("flops_phase1", C.c_double), ("flops_phase2", C.c_double),
                 ("bytes_algorithmic", C.c_double), ("bytes_intermediate", C.c_double),
+                ("n_segments_phase2", C.c_int64), ("n_terms_phase2", C.c_int64),
+                ("flops_phase2_unsummed", C.c_double),
                 ("association", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self):

@@ -132,15 +132,31 @@ struct PhasePlan {
 
 enum Slot { SLOT_X = 0, SLOT_Y = 1, SLOT_Z = 2, SLOT_OUT = 3, SLOT_T = 4 };
 
+// Split-precision operand preparation: one block of a column-major FP64 source
+// (rows x cols, leading dimension src_ld) written as bf16 hi/lo pairs in the
+// K-contiguous layout the tensor-core kernels read.  trans = 0: destination row
+// j holds source column j; trans = 1: destination row i holds source row i.
+struct PrepBlock { int64_t src_off, dst_off; int32_t src_ld, dst_ld, rows, cols, trans, pad; double scale; };
+
 struct Plan {
     PhasePlan p1, p2;
     DevLayout T;               // intermediate arena layout
     int association = 0;       // 0: T = op(X)*Y first; 1: U = Y*op(Z) first
     int64_t n_chains = 0, n_intermediates = 0, n_out_blocks = 0;
     double flops_merged = 0, bytes_alg = 0;
+    double flops_p2_unsummed = 0;
+    // split-precision plans only
+    bool split = false;
+    int64_t Xp_total = 0, Zp_total = 0;           // prepared-operand arena sizes (elements)
+    std::vector<PrepBlock> prepX, prepZ;          // X blocks, and c*op(Z) copies
 };
-// tile edge used by the planner for a precision mode
+// FP64 plan: two phases, the second sums first-stage products on the fly
 Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
                const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n);
+// split-precision plan: every operand pre-split into K-contiguous bf16 hi/lo
+// copies; the chain coefficient rides on a scaled copy of op(Z); the second
+// phase is a K-concatenation over chains
+Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
+                     const DevLayout& O, bool transX, bool transZ);
 
 }  // namespace vmps

@@ -192,18 +192,19 @@ __global__ void __launch_bounds__(f64k::NT, 3) gg_fp64_kernel(GGArgs g) {
 }
 
 // ===========================================================================
-// BF16x3 split-precision grouped GEMM: tile <= 64x64, 128 threads (2x2 warps
-// of 32x32), BK = 32, mma.sync m16n8k16 bf16 -> f32.  Operands are read as
-// fp32/fp64 16-byte groups, scaled and summed over the segment's terms in
-// fp32, split into hi/lo bf16 and stored in shared memory in the layout that
-// matches the contiguous global dimension; fragments come from ldmatrix
-// (k-contiguous layouts) or ldmatrix.trans (row-/column-contiguous layouts).
+// BF16x3 split-precision grouped GEMM on pre-split operands.
+//   A: M x K, B: K x N, both stored K-contiguous as separate bf16 hi and lo
+//   arrays (rows of A / columns of B padded to a multiple of 8 with zeros).
+//   Tile <= 64 x 64, 128 threads (2 x 2 warps of 32 x 32), BK = 32, 3-stage
+//   cp.async pipeline; hi*hi + hi*lo + lo*hi products on mma.sync m16n8k16
+//   bf16 with FP32 accumulation.
 // ===========================================================================
-namespace spk {
-constexpr int BM = 64, BN = 64, BK = 32, NT = 128;
-constexpr int SMN = BM + 8;   // [k][m] / [k][n] row stride (bf16): 144 B, conflict-free ldmatrix
-constexpr int SKK = BK + 8;   // [m][k] / [n][k] row stride (bf16): 80 B
-constexpr int OP_ELEMS = BM * SKK > BK * SMN ? BM * SKK : BK * SMN;   // 2560
+namespace sp3 {
+constexpr int BM = 64, BN = 64, BK = 32, NT = 128, STAGES = 3;
+constexpr int LDS = BK + 8;              // 80-byte shared rows: conflict-free ldmatrix
+constexpr int PART = BM * LDS;           // one of Ahi, Alo, Bhi, Blo
+constexpr int STAGE = 4 * PART;
+constexpr int SMEM_BYTES = STAGES * STAGE * 2;
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -213,44 +214,67 @@ __device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2
                  : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
                  : "r"(addr));
 }
-__device__ __forceinline__ void ldsm_x4_t(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, uint32_t addr) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(addr));
-}
 __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
         "{%0,%1,%2,%3};\n"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
-// split four fp32 values into packed hi and lo bf16 quadruples
-__device__ __forceinline__ void split4(const float (&x)[4], uint2& hi, uint2& lo) {
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const __nv_bfloat16 bh = __float2bfloat16_rn(x[i]);
-        const __nv_bfloat16 bl = __float2bfloat16_rn(x[i] - __bfloat162float(bh));
-        h[i] = __bfloat16_as_ushort(bh);
-        l[i] = __bfloat16_as_ushort(bl);
-    }
-    hi = make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
-    lo = make_uint2(l[0] | (l[1] << 16), l[2] | (l[3] << 16));
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
 
-template <typename TA, typename TB, typename TC>
-__global__ void __launch_bounds__(spk::NT, 4) gg_split_kernel(GGArgs g) {
-    using namespace spk;
-    // [stage][Ahi, Alo, Bhi, Blo]
-    __shared__ __align__(128) __nv_bfloat16 sm[2][4][OP_ELEMS];
+template <int OUT_SPLIT>
+__global__ void __launch_bounds__(sp3::NT, 3) gg_split_kernel(GGArgs g) {
+    using namespace sp3;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    __nv_bfloat16* sm = reinterpret_cast<__nv_bfloat16*>(smraw);
     const GTile tile = g.tiles[blockIdx.x];
-    const TA* __restrict__ A = (const TA*)g.A;
-    const TB* __restrict__ B = (const TB*)g.B;
+    const __nv_bfloat16* __restrict__ Ah = (const __nv_bfloat16*)g.A;
+    const __nv_bfloat16* __restrict__ Al = (const __nv_bfloat16*)g.A2;
+    const __nv_bfloat16* __restrict__ Bh = (const __nv_bfloat16*)g.B;
+    const __nv_bfloat16* __restrict__ Bl = (const __nv_bfloat16*)g.B2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     const int mrem = tile.tm, nrem = tile.tn;
-    const bool tA = g.transA, tB = g.transB;
+
+    int nsteps = 0;
+    for (int s = tile.seg_begin; s < tile.seg_end; ++s) nsteps += (g.segs[s].K + BK - 1) / BK;
+
+    // producer cursor
+    int lseg = tile.seg_begin, lk0 = 0;
+    GSeg lsg{};
+    int64_t laoff = 0;
+    if (lseg < tile.seg_end) { lsg = g.segs[lseg]; laoff = g.terms[lsg.term_begin].off; }
+    // 1024 16-byte chunks per stage (4 parts x 64 rows x 4 chunks): 8 per thread
+    auto load_step = [&](int stage) {
+        if (lseg < tile.seg_end) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int c = tid + NT * r;
+                const int part = c >> 8, row = (c >> 2) & 63, kc = c & 3;
+                const int k = lk0 + kc * 8;
+                const bool isA = part < 2;
+                const bool ok = (isA ? row < mrem : row < nrem) && k < lsg.K;
+                const __nv_bfloat16* base = part == 0 ? Ah : part == 1 ? Al : part == 2 ? Bh : Bl;
+                const __nv_bfloat16* src =
+                    isA ? base + laoff + (int64_t)(tile.row0 + (ok ? row : 0)) * lsg.lda + (ok ? k : 0)
+                        : base + lsg.b_off + (int64_t)(tile.col0 + (ok ? row : 0)) * lsg.ldb + (ok ? k : 0);
+                const uint32_t dst = smem_u32(sm + stage * STAGE + part * PART + row * LDS + kc * 8);
+                cp_async16(dst, src, ok ? 16 : 0);
+            }
+            lk0 += BK;
+            if (lk0 >= lsg.K) {
+                lk0 = 0;
+                if (++lseg < tile.seg_end) { lsg = g.segs[lseg]; laoff = g.terms[lsg.term_begin].off; }
+            }
+        }
+        cp_async_commit();
+    };
 
     float acc[2][4][4];
 #pragma unroll
@@ -260,138 +284,119 @@ __global__ void __launch_bounds__(spk::NT, 4) gg_split_kernel(GGArgs g) {
 #pragma unroll
             for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
 
-    // 512 groups of 4 per operand tile (64 x 32): 4 per thread
-    float ra[4][4], rb[4][4];
-    auto stage = [&](int s, int k0) {
-        const GSeg sg = g.segs[s];
-        const int krem = sg.K - k0;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int v = tid + NT * r;
-            int i, k;
-            if (!tA) { i = (v & 15) * 4; k = v >> 4; }     // row quads, 32 k columns
-            else     { k = (v & 7) * 4;  i = v >> 3; }     // k quads, 64 rows
-#pragma unroll
-            for (int q = 0; q < 4; ++q) ra[r][q] = 0.f;
-            if (i < mrem && k < krem) {
-                const int64_t e = tA ? ((int64_t)(k0 + k) + (int64_t)(tile.row0 + i) * sg.lda)
-                                     : ((int64_t)(tile.row0 + i) + (int64_t)(k0 + k) * sg.lda);
-                for (int t = 0; t < sg.term_count; ++t) {
-                    const GTerm tm = g.terms[sg.term_begin + t];
-                    const float c = (float)tm.coef;
-                    float x[4];
-                    ldg4(A + tm.off + e, x);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) ra[r][q] = fmaf(c, x[q], ra[r][q]);
-                }
-            }
-            int j, kb;
-            if (!tB) { kb = (v & 7) * 4;  j = v >> 3; }    // k quads, 64 columns
-            else     { j = (v & 15) * 4;  kb = v >> 4; }   // column quads, 32 k rows
-#pragma unroll
-            for (int q = 0; q < 4; ++q) rb[r][q] = 0.f;
-            if (j < nrem && kb < krem) {
-                const int64_t e = tB ? ((int64_t)(tile.col0 + j) + (int64_t)(k0 + kb) * sg.ldb)
-                                     : ((int64_t)(k0 + kb) + (int64_t)(tile.col0 + j) * sg.ldb);
-                ldg4(B + sg.b_off + e, rb[r]);
-            }
-        }
-    };
-    auto commit = [&](int st) {
-        __nv_bfloat16 *Ah = sm[st][0], *Al = sm[st][1], *Bh = sm[st][2], *Bl = sm[st][3];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int v = tid + NT * r;
-            uint2 hi, lo;
-            split4(ra[r], hi, lo);
-            int ia;
-            if (!tA) { const int i = (v & 15) * 4, k = v >> 4; ia = k * SMN + i; }
-            else     { const int k = (v & 7) * 4, i = v >> 3;  ia = i * SKK + k; }
-            *reinterpret_cast<uint2*>(Ah + ia) = hi;
-            *reinterpret_cast<uint2*>(Al + ia) = lo;
-            split4(rb[r], hi, lo);
-            int ib;
-            if (!tB) { const int kb = (v & 7) * 4, j = v >> 3; ib = j * SKK + kb; }
-            else     { const int j = (v & 15) * 4, kb = v >> 4; ib = kb * SMN + j; }
-            *reinterpret_cast<uint2*>(Bh + ib) = hi;
-            *reinterpret_cast<uint2*>(Bl + ib) = lo;
-        }
-    };
-
     const bool warp_live = wm < mrem && wn < nrem;
-    int seg = tile.seg_begin, k0 = 0;
-    if (seg < tile.seg_end) {
-        stage(seg, k0);
-        int st = 0;
-        while (true) {
-            commit(st);
-            __syncthreads();
-            int ns = seg, nk = k0 + BK;
-            if (nk >= g.segs[seg].K) { nk = 0; ++ns; }
-            const bool more = ns < tile.seg_end;
-            if (more) stage(ns, nk);
-            if (warp_live) {
-                const __nv_bfloat16 *Ah = sm[st][0], *Al = sm[st][1], *Bh = sm[st][2], *Bl = sm[st][3];
 #pragma unroll
-                for (int kk = 0; kk < BK; kk += 16) {
-                    uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
+    for (int s = 0; s < STAGES - 1; ++s) load_step(s);
+    for (int step = 0; step < nsteps; ++step) {
+        cp_async_wait<STAGES - 2>();
+        __syncthreads();
+        load_step((step + STAGES - 1) % STAGES);
+        if (warp_live) {
+            const __nv_bfloat16* st = sm + (step % STAGES) * STAGE;
+            const __nv_bfloat16 *sAh = st, *sAl = st + PART, *sBh = st + 2 * PART, *sBl = st + 3 * PART;
 #pragma unroll
-                    for (int mi = 0; mi < 2; ++mi) {
-                        const int mb = wm + mi * 16;
-                        if (tA) {   // [m][k]: plain ldmatrix
-                            const int off = (mb + (lane & 15)) * SKK + kk + (lane >> 4) * 8;
-                            ldsm_x4(ah[mi][0], ah[mi][1], ah[mi][2], ah[mi][3], smem_u32(Ah + off));
-                            ldsm_x4(al[mi][0], al[mi][1], al[mi][2], al[mi][3], smem_u32(Al + off));
-                        } else {    // [k][m]: transposing ldmatrix
-                            const int off = (kk + (lane & 7) + ((lane >> 4) & 1) * 8) * SMN + mb + ((lane >> 3) & 1) * 8;
-                            ldsm_x4_t(ah[mi][0], ah[mi][1], ah[mi][2], ah[mi][3], smem_u32(Ah + off));
-                            ldsm_x4_t(al[mi][0], al[mi][1], al[mi][2], al[mi][3], smem_u32(Al + off));
-                        }
-                    }
+            for (int kk = 0; kk < BK; kk += 16) {
+                uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
 #pragma unroll
-                    for (int np = 0; np < 2; ++np) {
-                        const int nb = wn + np * 16;
-                        if (!tB) {  // [n][k]: plain ldmatrix
-                            const int off = (nb + (lane & 7) + ((lane >> 4) << 3)) * SKK + kk + ((lane >> 3) & 1) * 8;
-                            ldsm_x4(bh[2 * np][0], bh[2 * np][1], bh[2 * np + 1][0], bh[2 * np + 1][1], smem_u32(Bh + off));
-                            ldsm_x4(bl[2 * np][0], bl[2 * np][1], bl[2 * np + 1][0], bl[2 * np + 1][1], smem_u32(Bl + off));
-                        } else {    // [k][n]: transposing ldmatrix
-                            const int off = (kk + (lane & 7) + ((lane >> 3) & 1) * 8) * SMN + nb + (lane >> 4) * 8;
-                            ldsm_x4_t(bh[2 * np][0], bh[2 * np][1], bh[2 * np + 1][0], bh[2 * np + 1][1], smem_u32(Bh + off));
-                            ldsm_x4_t(bl[2 * np][0], bl[2 * np][1], bl[2 * np + 1][0], bl[2 * np + 1][1], smem_u32(Bl + off));
-                        }
-                    }
-#pragma unroll
-                    for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-                        for (int ni = 0; ni < 4; ++ni) {
-                            mma_bf16(acc[mi][ni], al[mi], bh[ni][0], bh[ni][1]);
-                            mma_bf16(acc[mi][ni], ah[mi], bl[ni][0], bl[ni][1]);
-                            mma_bf16(acc[mi][ni], ah[mi], bh[ni][0], bh[ni][1]);
-                        }
+                for (int mi = 0; mi < 2; ++mi) {
+                    const int off = (wm + mi * 16 + (lane & 15)) * LDS + kk + (lane >> 4) * 8;
+                    ldsm_x4(ah[mi][0], ah[mi][1], ah[mi][2], ah[mi][3], smem_u32(sAh + off));
+                    ldsm_x4(al[mi][0], al[mi][1], al[mi][2], al[mi][3], smem_u32(sAl + off));
                 }
+#pragma unroll
+                for (int np = 0; np < 2; ++np) {
+                    const int off = (wn + np * 16 + (lane & 7) + ((lane >> 4) << 3)) * LDS + kk + ((lane >> 3) & 1) * 8;
+                    ldsm_x4(bh[2 * np][0], bh[2 * np][1], bh[2 * np + 1][0], bh[2 * np + 1][1], smem_u32(sBh + off));
+                    ldsm_x4(bl[2 * np][0], bl[2 * np][1], bl[2 * np + 1][0], bl[2 * np + 1][1], smem_u32(sBl + off));
+                }
+                // small cross terms first, then hi*hi; independent accumulators in between
+#pragma unroll
+                for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+                    for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], al[mi], bh[ni][0], bh[ni][1]);
+#pragma unroll
+                for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+                    for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], ah[mi], bl[ni][0], bl[ni][1]);
+#pragma unroll
+                for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+                    for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], ah[mi], bh[ni][0], bh[ni][1]);
             }
-            if (!more) break;
-            seg = ns; k0 = nk;
-            st ^= 1;
         }
     }
+    cp_async_wait<0>();
+
     // epilogue: c0,c1 -> (g, 2t..2t+1), c2,c3 -> (g+8, 2t..2t+1)
-    TC* __restrict__ C = (TC*)g.C;
     const int g4 = lane >> 2, t4 = lane & 3;
 #pragma unroll
     for (int mi = 0; mi < 2; ++mi)
 #pragma unroll
         for (int ni = 0; ni < 4; ++ni)
 #pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                const int r = wm + mi * 16 + g4 + (h >> 1) * 8, c = wn + ni * 8 + t4 * 2 + (h & 1);
-                if (r < mrem && c < nrem) {
-                    const int64_t gr = tile.row0 + r, gc = tile.col0 + c;
-                    const int64_t e = g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc);
-                    C[tile.c_off + e] = (TC)acc[mi][ni][h];
+            for (int hh = 0; hh < 2; ++hh) {
+                const int r = wm + mi * 16 + g4 + hh * 8, c = wn + ni * 8 + t4 * 2;
+                if (r >= mrem) continue;
+                const float v0 = acc[mi][ni][2 * hh], v1 = acc[mi][ni][2 * hh + 1];
+                const int64_t gr = tile.row0 + r, gc = tile.col0 + c;
+                if (OUT_SPLIT) {
+                    __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
+                    __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
+                    const __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
+                    const __nv_bfloat16 l0 = __float2bfloat16_rn(v0 - __bfloat162float(h0));
+                    const __nv_bfloat16 l1 = __float2bfloat16_rn(v1 - __bfloat162float(h1));
+                    if (g.transC) {   // row-major: the two columns are adjacent
+                        const int64_t e = gc + gr * tile.ldc;
+                        if (c + 1 < nrem) {
+                            *reinterpret_cast<__nv_bfloat162*>(Ch + tile.c_off + e) = __halves2bfloat162(h0, h1);
+                            *reinterpret_cast<__nv_bfloat162*>(Cl + tile.c_off + e) = __halves2bfloat162(l0, l1);
+                        } else if (c < nrem) {
+                            Ch[tile.c_off + e] = h0;
+                            Cl[tile.c_off + e] = l0;
+                        }
+                    } else {
+                        if (c < nrem) { const int64_t e = gr + gc * tile.ldc; Ch[tile.c_off + e] = h0; Cl[tile.c_off + e] = l0; }
+                        if (c + 1 < nrem) { const int64_t e = gr + (gc + 1) * tile.ldc; Ch[tile.c_off + e] = h1; Cl[tile.c_off + e] = l1; }
+                    }
+                } else {
+                    double* C = (double*)g.C;
+                    if (c < nrem) {
+                        const int64_t e = g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc);
+                        C[tile.c_off + e] = (double)v0;
+                    }
+                    if (c + 1 < nrem) {
+                        const int64_t e = g.transC ? (gc + 1 + gr * tile.ldc) : (gr + (gc + 1) * tile.ldc);
+                        C[tile.c_off + e] = (double)v1;
+                    }
                 }
             }
+}
+
+// operand preparation: scale, split into bf16 hi/lo, write K-contiguous
+__global__ void prep_kernel(const PrepBlock* __restrict__ pbs, int nb, const double* __restrict__ src,
+                            __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        const PrepBlock pb = pbs[b];
+        const int64_t n = (int64_t)pb.rows * pb.cols;
+        for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+            const int64_t i = e % pb.rows, j = e / pb.rows;
+            const float v = (float)(pb.scale * src[pb.src_off + i + j * pb.src_ld]);
+            const int64_t d = pb.trans ? (pb.dst_off + i * pb.dst_ld + j) : (pb.dst_off + j * pb.dst_ld + i);
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            hi[d] = h;
+            lo[d] = __float2bfloat16_rn(v - __bfloat162float(h));
+        }
+    }
+}
+// elementwise split of a whole arena (same layout in and out)
+__global__ void split_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ hi,
+                             __nv_bfloat16* __restrict__ lo, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = (float)src[i];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[i] = h;
+        lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
 }
 
 // ===========================================================================
@@ -411,10 +416,6 @@ __global__ void pack_kernel(const PackBlock* blocks, int nb, const double* __res
     }
 }
 
-__global__ void to_f32_kernel(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        dst[i] = (float)src[i];
-}
 
 // partial dot products: fixed chunking -> deterministic two-pass reduction
 constexpr int kDotThreads = 256;
@@ -518,28 +519,35 @@ static int grid_for(int64_t n, int threads, int cap) {
 // opt the split kernels into their dynamic shared memory size (once per process,
 // before any launch or stream capture)
 cudaError_t kernels_init() {
-    // all grouped-GEMM kernels use static shared memory below 48 KB
-    return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(gg_split_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp3::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(gg_split_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp3::SMEM_BYTES);
 }
 
-cudaError_t launch_gg(int prec, int ta, int tb, int tc, const GGArgs& a, cudaStream_t st) {
+cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
-    if (prec == VMPS_PREC_FP64) {
-        gg_fp64_kernel<<<a.ntiles, f64k::NT, 0, st>>>(a);
-        return cudaGetLastError();
-    }
-    // split precision: type codes 0 = double, 1 = float
-    const int code = ta * 4 + tb * 2 + tc;
-    switch (code) {
-        case 0: gg_split_kernel<double, double, double><<<a.ntiles, spk::NT, 0, st>>>(a); break;
-        case 1: gg_split_kernel<double, double, float><<<a.ntiles, spk::NT, 0, st>>>(a); break;
-        case 2: gg_split_kernel<double, float, double><<<a.ntiles, spk::NT, 0, st>>>(a); break;
-        case 3: gg_split_kernel<double, float, float><<<a.ntiles, spk::NT, 0, st>>>(a); break;
-        case 4: gg_split_kernel<float, double, double><<<a.ntiles, spk::NT, 0, st>>>(a); break;
-        case 5: gg_split_kernel<float, double, float><<<a.ntiles, spk::NT, 0, st>>>(a); break;
-        case 6: gg_split_kernel<float, float, double><<<a.ntiles, spk::NT, 0, st>>>(a); break;
-        case 7: gg_split_kernel<float, float, float><<<a.ntiles, spk::NT, 0, st>>>(a); break;
-    }
+    gg_fp64_kernel<<<a.ntiles, f64k::NT, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gg_split(int out_split, const GGArgs& a, cudaStream_t st) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    if (out_split) gg_split_kernel<1><<<a.ntiles, sp3::NT, sp3::SMEM_BYTES, st>>>(a);
+    else gg_split_kernel<0><<<a.ntiles, sp3::NT, sp3::SMEM_BYTES, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* hi, void* lo, cudaStream_t st) {
+    if (nb <= 0) return cudaSuccess;
+    if (!pb || !src || !hi || !lo) return cudaErrorInvalidValue;
+    prep_kernel<<<min(nb, 8192), 256, 0, st>>>(pb, nb, src, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split(const double* src, void* hi, void* lo, int64_t n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (!src || !hi || !lo) return cudaErrorInvalidValue;
+    split_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(src, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo, n);
     return cudaGetLastError();
 }
 
@@ -547,10 +555,6 @@ cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, doub
     if (nb <= 0) return cudaSuccess;
     if (!blocks || !src || !dst) return cudaErrorInvalidValue;   // never launch on an unallocated buffer
     pack_kernel<<<min(nb, 4096), 256, 0, st>>>(blocks, nb, src, dst, to_padded);
-    return cudaGetLastError();
-}
-cudaError_t launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st) {
-    to_f32_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(src, dst, n);
     return cudaGetLastError();
 }
 // chunked dot: part must hold nchunk doubles

@@ -10,6 +10,9 @@ struct GGArgs {
     const void* A;
     const void* B;
     void* C;
+    const void* A2;   // split precision: lo halves of A, B (hi in A, B)
+    const void* B2;
+    void* C2;         // split precision with a split output: lo half of C
     const GTile* tiles;
     const GSeg* segs;
     const GTerm* terms;
@@ -20,11 +23,15 @@ struct GGArgs {
 struct PackBlock { int64_t coff, doff, rows, cols, ld; double scale; };
 
 cudaError_t kernels_init();
-// operand type codes for the split kernel: 0 = double, 1 = float
-cudaError_t launch_gg(int prec, int ta, int tb, int tc, const GGArgs& a, cudaStream_t st);
+// FP64 grouped GEMM (DMMA)
+cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st);
+// split-precision grouped GEMM on pre-split K-contiguous operands;
+// out_split = 1: C/C2 are bf16 hi/lo, 0: C is double
+cudaError_t launch_gg_split(int out_split, const GGArgs& a, cudaStream_t st);
+cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* hi, void* lo, cudaStream_t st);
+cudaError_t launch_split(const double* src, void* hi, void* lo, int64_t n, cudaStream_t st);
 cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, double* dst, int to_padded,
                         cudaStream_t st);
-cudaError_t launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
 int64_t dot_chunk(int64_t n);
 int dot_nchunk(int64_t n);
 cudaError_t launch_dot(const double* x, const double* y, int64_t n, double* part, double* out, cudaStream_t st);

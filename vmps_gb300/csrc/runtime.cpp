@@ -103,7 +103,11 @@ struct DevPhase {
 struct DevPlan {
     Plan plan;
     DevPhase p1, p2;
-    DBuf T;   // intermediate arena (double or float)
+    DBuf T, T2;                   // FP64: T (double); split: T hi / lo (bf16)
+    DBuf Xh, Xl, Zh, Zl, Yh, Yl;  // split: prepared operands
+    DBuf prepX, prepZ;            // PrepBlock lists
+    int nprepX = 0, nprepZ = 0;
+    int64_t ytotal = 0;           // elements of the Y arena (split per call)
     bool ready = false;
 };
 
@@ -115,46 +119,88 @@ static std::vector<PackBlock> pack_blocks(const BlockTable& t, const DevLayout& 
     return v;
 }
 
-// operand arenas for one grouped-GEMM problem
+// FP64 device arenas of one grouped-GEMM problem
 struct Operands {
-    const void* X = nullptr; int tx = 0;   // type code 0 double / 1 float
-    const void* Y = nullptr; int ty = 0;
-    const void* Z = nullptr; int tz = 0;
-    void* O = nullptr; int to = 0;
+    const double* X = nullptr;
+    const double* Y = nullptr;
+    const double* Z = nullptr;
+    double* O = nullptr;
 };
 
-static void run_plan(const DevPlan& dp, int prec, const Operands& ops, cudaStream_t st) {
-    auto slot_ptr = [&](int slot, int& tcode) -> const void* {
-        switch (slot) {
-            case SLOT_X: tcode = ops.tx; return ops.X;
-            case SLOT_Y: tcode = ops.ty; return ops.Y;
-            case SLOT_Z: tcode = ops.tz; return ops.Z;
-            case SLOT_OUT: tcode = ops.to; return ops.O;
-            case SLOT_T: tcode = prec == VMPS_PREC_FP64 ? 0 : 1; return dp.T.p;
-        }
-        tcode = 0;
-        return nullptr;
-    };
-    for (int ph = 0; ph < 2; ++ph) {
-        const DevPhase& d = ph == 0 ? dp.p1 : dp.p2;
-        const PhasePlan& h = ph == 0 ? dp.plan.p1 : dp.plan.p2;
-        GGArgs a{};
-        int ta, tb, tc;
-        a.A = slot_ptr(h.slotA, ta);
-        a.B = slot_ptr(h.slotB, tb);
-        a.C = const_cast<void*>(slot_ptr(h.slotC, tc));
-        a.tiles = d.tiles.as<GTile>();
-        a.segs = d.segs.as<GSeg>();
-        a.terms = d.terms.as<GTerm>();
-        a.ntiles = d.ntiles;
-        a.transA = h.transA; a.transB = h.transB; a.transC = h.transC;
-        if (prec == VMPS_PREC_FP64 && (ta | tb | tc)) throw std::invalid_argument("FP64 plan with float operand");
-        // every operand of a non-empty phase must be a live device buffer
-        if (d.ntiles > 0 && (!a.C || !a.tiles || !a.segs || !a.terms ||
-                             (!h.segs.empty() && (!a.A || !a.B))))
-            throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
-        CK(launch_gg(prec, ta, tb, tc, a, st));
+// device buffers and work lists of a freshly made plan
+static void plan_to_device(DevPlan& dp, int64_t ytotal, cudaStream_t st) {
+    dp.p1.upload(dp.plan.p1, st);
+    dp.p2.upload(dp.plan.p2, st);
+    if (!dp.plan.split) {
+        dp.T.alloc((size_t)dp.plan.T.total * 8, st, true);
+        return;
     }
+    dp.T.alloc((size_t)dp.plan.T.total * 2, st, true);
+    dp.T2.alloc((size_t)dp.plan.T.total * 2, st, true);
+    dp.Xh.alloc((size_t)dp.plan.Xp_total * 2, st, true);
+    dp.Xl.alloc((size_t)dp.plan.Xp_total * 2, st, true);
+    dp.Zh.alloc((size_t)dp.plan.Zp_total * 2, st, true);
+    dp.Zl.alloc((size_t)dp.plan.Zp_total * 2, st, true);
+    dp.ytotal = ytotal;
+    dp.Yh.alloc((size_t)std::max<int64_t>(ytotal, 32) * 2, st, true);
+    dp.Yl.alloc((size_t)std::max<int64_t>(ytotal, 32) * 2, st, true);
+    upload_vec(dp.prepX, dp.plan.prepX, st);
+    upload_vec(dp.prepZ, dp.plan.prepZ, st);
+    dp.nprepX = (int)dp.plan.prepX.size();
+    dp.nprepZ = (int)dp.plan.prepZ.size();
+}
+
+// split plans: scaled bf16 hi/lo copies of the X and Z operands
+static void split_prepare(DevPlan& dp, const double* X, const double* Z, cudaStream_t st) {
+    if (!dp.plan.split) return;
+    CK(launch_prep(dp.prepX.as<PrepBlock>(), dp.nprepX, X, dp.Xh.p, dp.Xl.p, st));
+    CK(launch_prep(dp.prepZ.as<PrepBlock>(), dp.nprepZ, Z, dp.Zh.p, dp.Zl.p, st));
+}
+
+static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream_t st) {
+    const DevPhase& d = ph == 1 ? dp.p1 : dp.p2;
+    const PhasePlan& h = ph == 1 ? dp.plan.p1 : dp.plan.p2;
+    GGArgs a{};
+    a.tiles = d.tiles.as<GTile>();
+    a.segs = d.segs.as<GSeg>();
+    a.terms = d.terms.as<GTerm>();
+    a.ntiles = d.ntiles;
+    a.transA = h.transA; a.transB = h.transB; a.transC = h.transC;
+    if (!dp.plan.split) {
+        auto slot = [&](int s) -> const void* {
+            switch (s) {
+                case SLOT_X: return ops.X;
+                case SLOT_Y: return ops.Y;
+                case SLOT_Z: return ops.Z;
+                case SLOT_OUT: return ops.O;
+                case SLOT_T: return dp.T.p;
+            }
+            return nullptr;
+        };
+        a.A = slot(h.slotA);
+        a.B = slot(h.slotB);
+        a.C = const_cast<void*>(slot(h.slotC));
+    } else if (ph == 1) {
+        a.A = dp.Xh.p; a.A2 = dp.Xl.p;
+        a.B = dp.Yh.p; a.B2 = dp.Yl.p;
+        a.C = dp.T.p; a.C2 = dp.T2.p;
+    } else {
+        a.A = dp.T.p; a.A2 = dp.T2.p;
+        a.B = dp.Zh.p; a.B2 = dp.Zl.p;
+        a.C = ops.O;
+    }
+    // every operand of a non-empty phase must be a live device buffer
+    if (d.ntiles > 0 && (!a.C || !a.tiles || !a.segs || !a.terms || (!h.segs.empty() && (!a.A || !a.B))))
+        throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
+    if (!dp.plan.split) CK(launch_gg64(a, st));
+    else CK(launch_gg_split(ph == 1 ? 1 : 0, a, st));
+}
+
+// one application of a planned contraction: (split plans) split Y, phase 1, phase 2
+static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
+    if (dp.plan.split) CK(launch_split(ops.Y, dp.Yh.p, dp.Yl.p, dp.ytotal, st));
+    run_phase(dp, 1, ops, st);
+    run_phase(dp, 2, ops, st);
 }
 
 static void fill_stats(const ChainSet& cs, const Plan& p, int prec, vmps_plan_stats* s) {
@@ -172,11 +218,14 @@ static void fill_stats(const ChainSet& cs, const Plan& p, int prec, vmps_plan_st
     s->flops_phase2 = p.p2.flops;
     s->flops_executed = p.p1.flops + p.p2.flops;
     s->bytes_algorithmic = p.bytes_alg;
-    s->bytes_intermediate = (double)p.T.total * (prec == VMPS_PREC_FP64 ? 8.0 : 4.0);
+    s->bytes_intermediate = (double)p.T.total * (p.split ? 4.0 : 8.0);
+    (void)prec;
+    s->n_segments_phase2 = (int64_t)p.p2.segs.size();
+    s->n_terms_phase2 = (int64_t)p.p2.terms.size();
+    s->flops_phase2_unsummed = p.flops_p2_unsummed;
     s->association = p.association;
 }
 
-static int tile_edge(int prec) { return prec == VMPS_PREC_FP64 ? 64 : 128; }
 
 // ---------------------------------------------------------------------------
 // pivot (PivotMatrix0/1/2)
@@ -188,7 +237,7 @@ struct vmps_pivot_s {
     DevLayout Ld, Rd, Vd;
     ChainSet cs;
     DevPlan plans[2];
-    DBuf dL, dR, dL32, dR32;
+    DBuf dL, dR;
     DBuf dPack;                 // PackBlock[] of the vector layout
     int npack = 0;
     std::vector<double> vscale; // sqrt(coeff_dot(qout)) per V block
@@ -227,18 +276,11 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
     DevPlan& dp = p->plans[prec];
     if (dp.ready) return dp;
-    const int te = tile_edge(prec);
-    dp.plan = make_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, te, te);
+    if (prec == VMPS_PREC_FP64) dp.plan = make_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 64, 64);
+    else dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false);
     if (p->ctx->device < 0) { dp.ready = true; return dp; }   // host-only: plan without device copies
-    dp.p1.upload(dp.plan.p1, p->st());
-    dp.p2.upload(dp.plan.p2, p->st());
-    dp.T.alloc((size_t)dp.plan.T.total * (prec == VMPS_PREC_FP64 ? 8 : 4), p->st(), true);
-    if (prec == VMPS_PREC_BF16X3 && !p->dL32.p) {
-        p->dL32.alloc((size_t)p->Ld.total * 4, p->st(), true);
-        p->dR32.alloc((size_t)p->Rd.total * 4, p->st(), true);
-        CK(launch_to_f32(p->dL.as<double>(), p->dL32.as<float>(), p->Ld.total, p->st()));
-        CK(launch_to_f32(p->dR.as<double>(), p->dR32.as<float>(), p->Rd.total, p->st()));
-    }
+    plan_to_device(dp, p->Vd.total, p->st());
+    split_prepare(dp, p->dL.as<double>(), p->dR.as<double>(), p->st());
     CK(cudaStreamSynchronize(p->st()));
     dp.ready = true;
     return dp;
@@ -252,13 +294,11 @@ static void pivot_hxv_dev(vmps_pivot* p, int prec, const double* vin, double* vo
     require_device(p->ctx);
     DevPlan& dp = get_plan(p, prec);
     Operands ops;
-    if (prec == VMPS_PREC_FP64) {
-        ops.X = p->dL.p; ops.Z = p->dR.p;
-    } else {
-        ops.X = p->dL32.p; ops.tx = 1; ops.Z = p->dR32.p; ops.tz = 1;
-    }
-    ops.Y = vin; ops.O = vout;
-    run_plan(dp, prec, ops, p->st());
+    ops.X = p->dL.as<double>();
+    ops.Z = p->dR.as<double>();
+    ops.Y = vin;
+    ops.O = vout;
+    run_plan(dp, ops, p->st());
 }
 
 static void upload_blocks_padded(const BlockTable& t, const DevLayout& d, const double* host, DBuf& dst,
@@ -532,17 +572,17 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
     DevPlan& dp = get_plan(p, prec);
     const double* vi = vin->d.as<double>();
     double* vo = vout->d.as<double>();
-    // phase-2 share: time phase 2 alone once
     Operands ops;
-    if (prec == VMPS_PREC_FP64) { ops.X = p->dL.p; ops.Z = p->dR.p; }
-    else { ops.X = p->dL32.p; ops.tx = 1; ops.Z = p->dR32.p; ops.tz = 1; }
-    ops.Y = vi; ops.O = vo;
+    ops.X = p->dL.as<double>();
+    ops.Z = p->dR.as<double>();
+    ops.Y = vi;
+    ops.O = vo;
     if (use_graph) {
         if (!p->graph[prec] || p->graph_in[prec] != vi || p->graph_out[prec] != vo) {
             if (p->graph[prec]) { cudaGraphExecDestroy(p->graph[prec]); p->graph[prec] = nullptr; }
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            run_plan(dp, prec, ops, st);
+            run_plan(dp, ops, st);
             CK(cudaStreamEndCapture(st, &g));
             cudaGraphExec_t ge;
             CK(cudaGraphInstantiate(&ge, g, 0));
@@ -554,7 +594,7 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
     }
     auto one = [&]() {
         if (use_graph) CK(cudaGraphLaunch(p->graph[prec], st));
-        else run_plan(dp, prec, ops, st);
+        else run_plan(dp, ops, st);
     };
     one();
     CK(cudaStreamSynchronize(st));
@@ -566,21 +606,9 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
     CK(cudaEventElapsedTime(&ms, p->ctx->ev0, p->ctx->ev1));
     if (ms_per_hxv) *ms_per_hxv = ms / n_iter;
     if (ms_phase2) {
-        // time phase 2 alone: run phase 1 once to fill T, then phase 2 n_iter times
-        GGArgs a{};
-        const PhasePlan& h = dp.plan.p2;
-        int ta = prec == VMPS_PREC_FP64 ? 0 : 1, tb, tc = 0;
-        a.A = dp.T.p;
-        a.B = h.slotB == SLOT_Z ? ops.Z : ops.X;
-        tb = h.slotB == SLOT_Z ? ops.tz : ops.tx;
-        a.C = vo;
-        a.tiles = dp.p2.tiles.as<GTile>();
-        a.segs = dp.p2.segs.as<GSeg>();
-        a.terms = dp.p2.terms.as<GTerm>();
-        a.ntiles = dp.p2.ntiles;
-        a.transA = h.transA; a.transB = h.transB; a.transC = h.transC;
+        // second grouped-GEMM phase alone (its inputs are in place from the runs above)
         CK(cudaEventRecord(p->ctx->ev0, st));
-        for (int i = 0; i < n_iter; ++i) CK(launch_gg(prec, ta, tb, tc, a, st));
+        for (int i = 0; i < n_iter; ++i) run_phase(dp, 2, ops, st);
         CK(cudaEventRecord(p->ctx->ev2, st));
         CK(cudaEventSynchronize(p->ctx->ev2));
         float ms2 = 0;
@@ -810,15 +838,14 @@ static DevPlan& env_plan(vmps_env* e, int prec) {
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
     DevPlan& dp = e->plans[prec];
     if (dp.ready) return dp;
-    const int te = tile_edge(prec);
-    if (e->side == VMPS_ENV_LEFT)   // X = Abra^dagger, Y = Eold, Z = Aket
-        dp.plan = make_plan(e->cs, e->Bd, e->Ed, e->Kd, e->Nd, true, false, te, te);
-    else                            // X = Aket, Y = Eold, Z = Abra^dagger
-        dp.plan = make_plan(e->cs, e->Kd, e->Ed, e->Bd, e->Nd, false, true, te, te);
+    const bool L = e->side == VMPS_ENV_LEFT;
+    // left: X = Abra^dagger, Y = Eold, Z = Aket;  right: X = Aket, Y = Eold, Z = Abra^dagger
+    const DevLayout& X = L ? e->Bd : e->Kd;
+    const DevLayout& Z = L ? e->Kd : e->Bd;
+    if (prec == VMPS_PREC_FP64) dp.plan = make_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L, 64, 64);
+    else dp.plan = make_split_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L);
     if (e->ctx->device < 0) { dp.ready = true; return dp; }
-    dp.p1.upload(dp.plan.p1, e->st());
-    dp.p2.upload(dp.plan.p2, e->st());
-    dp.T.alloc((size_t)dp.plan.T.total * (prec == VMPS_PREC_FP64 ? 8 : 4), e->st(), true);
+    plan_to_device(dp, e->Ed.total, e->st());
     CK(cudaStreamSynchronize(e->st()));
     dp.ready = true;
     return dp;
@@ -895,11 +922,12 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra, const doub
     upload_blocks_padded(e->Kt, e->Kd, Aket, e->dK, st);
     e->dN.alloc((size_t)e->Nd.total * 8, st, true);
     Operands ops;
-    if (e->side == VMPS_ENV_LEFT) { ops.X = e->dB.p; ops.Z = e->dK.p; }
-    else { ops.X = e->dK.p; ops.Z = e->dB.p; }
-    ops.Y = e->dE.p;
-    ops.O = e->dN.p;
-    run_plan(dp, prec, ops, st);
+    if (e->side == VMPS_ENV_LEFT) { ops.X = e->dB.as<double>(); ops.Z = e->dK.as<double>(); }
+    else { ops.X = e->dK.as<double>(); ops.Z = e->dB.as<double>(); }
+    ops.Y = e->dE.as<double>();
+    ops.O = e->dN.as<double>();
+    split_prepare(dp, ops.X, ops.Z, st);
+    run_plan(dp, ops, st);
     if (!e->pkN.p) {
         auto pb = pack_blocks(e->Nt, e->Nd, nullptr);
         upload_vec(e->pkN, pb, st);

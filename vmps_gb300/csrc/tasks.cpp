@@ -830,9 +830,10 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
         int32_t se = (int32_t)p2.segs.size();
         // tile space: association 0 -> (m x p) of out; association 1 -> (p x m) (transposed store)
         const int64_t m = O.rows[o], p = O.cols[o];
-        double kk = 0;
-        for (int32_t s = sb; s < se; ++s) kk += p2.segs[s].K;
+        double kk = 0, kt = 0;
+        for (int32_t s = sb; s < se; ++s) { kk += p2.segs[s].K; kt += (double)p2.segs[s].K * p2.segs[s].term_count; }
         p2.flops += 2.0 * m * p * kk;
+        P.flops_p2_unsummed += 2.0 * m * p * kt;
         if (P.association == 0) add_tiles(p2, O.off[o], O.ld[o], m, p, sb, se, tile_m, tile_n);
         else add_tiles(p2, O.off[o], O.ld[o], p, m, sb, se, tile_m, tile_n);
         i = j;
@@ -849,6 +850,186 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
                 else add_tiles(p2, O.off[o], O.ld[o], O.cols[o], O.rows[o], sb, sb, tile_m, tile_n);
             }
     }
+    sort_tiles(p2);
+    return P;
+}
+
+// ===========================================================================
+// split-precision planner
+// ===========================================================================
+Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
+                     const DevLayout& O, bool transX, bool transZ) {
+    Plan P;
+    P.split = true;
+    P.association = 0;
+    auto xm = [&](int64_t x) { return transX ? X.cols[x] : X.rows[x]; };
+    auto xk = [&](int64_t x) { return transX ? X.rows[x] : X.cols[x]; };
+    auto zn = [&](int64_t z) { return transZ ? Z.cols[z] : Z.rows[z]; };
+    auto zp = [&](int64_t z) { return transZ ? Z.rows[z] : Z.cols[z]; };
+
+    // merge duplicate chains
+    std::unordered_map<Key4, size_t, Key4Hash> mdict;
+    std::vector<Chain> ch;
+    ch.reserve(cs.chains.size());
+    for (const Chain& c : cs.chains) {
+        if (c.out < 0 || c.out >= (int64_t)O.rows.size() || c.x < 0 || c.x >= (int64_t)X.rows.size() || c.y < 0 ||
+            c.y >= (int64_t)Y.rows.size() || c.z < 0 || c.z >= (int64_t)Z.rows.size())
+            throw std::invalid_argument("chain references a block outside its table");
+        if (xk(c.x) != Y.rows[c.y] || Y.cols[c.y] != zn(c.z) || O.rows[c.out] != xm(c.x) || O.cols[c.out] != zp(c.z))
+            throw std::domain_error("block shapes do not chain: out " + std::to_string(c.out));
+        Key4 k{c.out, c.x, c.y, c.z};
+        auto it = mdict.find(k);
+        if (it == mdict.end()) { mdict.emplace(k, ch.size()); ch.push_back(c); }
+        else ch[it->second].c += c.c;
+    }
+    P.n_chains = (int64_t)ch.size();
+    {
+        std::vector<char> ux(X.rows.size(), 0), uz(Z.rows.size(), 0), uo(O.rows.size(), 0);
+        double bytes = 0;
+        for (const Chain& c : ch) {
+            P.flops_merged += chain_flops((double)xm(c.x), (double)xk(c.x), (double)Y.cols[c.y], (double)zp(c.z));
+            if (!ux[c.x]) { ux[c.x] = 1; bytes += 8.0 * X.rows[c.x] * X.cols[c.x]; }
+            if (!uz[c.z]) { uz[c.z] = 1; bytes += 8.0 * Z.rows[c.z] * Z.cols[c.z]; }
+            uo[c.out] = 1;
+        }
+        for (size_t i = 0; i < Y.rows.size(); ++i) bytes += 8.0 * Y.rows[i] * Y.cols[i];
+        int64_t no = 0;
+        for (size_t i = 0; i < O.rows.size(); ++i) if (uo[i]) { bytes += 8.0 * O.rows[i] * O.cols[i]; ++no; }
+        P.bytes_alg = bytes;
+        P.n_out_blocks = no;
+    }
+
+    // prepared X blocks: op(X) (m x k) stored row-major, row stride pad8(k)
+    std::vector<int64_t> xp_off(X.rows.size(), -1), xp_ld(X.rows.size(), 0);
+    int64_t cur = 0;
+    for (const Chain& c : ch) {
+        if (xp_off[c.x] >= 0) continue;
+        const int64_t m = xm(c.x), k = xk(c.x), ld = pad_ld(k);
+        xp_off[c.x] = cur;
+        xp_ld[c.x] = ld;
+        PrepBlock pb{};
+        pb.src_off = X.off[c.x]; pb.src_ld = (int32_t)X.ld[c.x];
+        pb.rows = (int32_t)X.rows[c.x]; pb.cols = (int32_t)X.cols[c.x];
+        pb.dst_off = cur; pb.dst_ld = (int32_t)ld;
+        pb.trans = transX ? 0 : 1;   // op(X) = X: rows of X become rows; op(X) = X^T: columns of X
+        pb.scale = 1.0;
+        P.prepX.push_back(pb);
+        cur = pad_off(cur + ld * m);
+    }
+    P.Xp_total = std::max<int64_t>(cur, 32);
+
+    // scaled copies c * op(Z) (n x p) stored column-major, column stride pad8(n)
+    struct CZ { uint64_t cbits; int64_t z; bool operator==(const CZ& o) const { return cbits == o.cbits && z == o.z; } };
+    struct CZH { size_t operator()(const CZ& a) const { return std::hash<uint64_t>()(a.cbits * 0x9E3779B97F4A7C15ull ^ (uint64_t)a.z); } };
+    std::unordered_map<CZ, int64_t, CZH> zdict;
+    std::vector<int64_t> zp_off, zp_ld;
+    std::vector<int64_t> chain_zp(ch.size());
+    cur = 0;
+    for (size_t i = 0; i < ch.size(); ++i) {
+        uint64_t bits;
+        std::memcpy(&bits, &ch[i].c, 8);
+        CZ key{bits, ch[i].z};
+        auto it = zdict.find(key);
+        if (it != zdict.end()) { chain_zp[i] = it->second; continue; }
+        const int64_t n = zn(ch[i].z), p = zp(ch[i].z), ld = pad_ld(n);
+        const int64_t id = (int64_t)zp_off.size();
+        zdict.emplace(key, id);
+        zp_off.push_back(cur);
+        zp_ld.push_back(ld);
+        PrepBlock pb{};
+        pb.src_off = Z.off[ch[i].z]; pb.src_ld = (int32_t)Z.ld[ch[i].z];
+        pb.rows = (int32_t)Z.rows[ch[i].z]; pb.cols = (int32_t)Z.cols[ch[i].z];
+        pb.dst_off = cur; pb.dst_ld = (int32_t)ld;
+        pb.trans = transZ ? 1 : 0;   // op(Z) = Z: columns stay columns; op(Z) = Z^T: rows of Z become columns
+        pb.scale = ch[i].c;
+        P.prepZ.push_back(pb);
+        chain_zp[i] = id;
+        cur = pad_off(cur + ld * p);
+    }
+    P.Zp_total = std::max<int64_t>(cur, 32);
+
+    // intermediates T = op(X) * Y (m x n), stored row-major (row stride pad8(n)) for phase 2
+    std::unordered_map<Key4, int64_t, Key4Hash> idict;
+    std::vector<std::pair<int64_t, int64_t>> ipairs;
+    std::vector<int64_t> chain_t(ch.size());
+    DevLayout& T = P.T;
+    cur = 0;
+    for (size_t i = 0; i < ch.size(); ++i) {
+        Key4 k{ch[i].x, ch[i].y, 0, 0};
+        auto it = idict.find(k);
+        if (it != idict.end()) { chain_t[i] = it->second; continue; }
+        const int64_t id = (int64_t)ipairs.size();
+        idict.emplace(k, id);
+        ipairs.push_back({ch[i].x, ch[i].y});
+        const int64_t m = xm(ch[i].x), n = Y.cols[ch[i].y], ld = pad_ld(n);
+        T.off.push_back(cur); T.rows.push_back(m); T.cols.push_back(n); T.ld.push_back(ld);
+        cur = pad_off(cur + ld * m);
+        chain_t[i] = id;
+    }
+    T.total = std::max<int64_t>(cur, 32);
+    P.n_intermediates = (int64_t)ipairs.size();
+
+    // phase 1: T_j = Xp[x] * Yp[y]   (A rows = m, B columns = n, K = k), stored transposed
+    PhasePlan& p1 = P.p1;
+    p1.slotA = SLOT_X; p1.slotB = SLOT_Y; p1.slotC = SLOT_T;
+    p1.transA = false; p1.transB = false; p1.transC = true;
+    for (size_t j = 0; j < ipairs.size(); ++j) {
+        const int64_t x = ipairs[j].first, y = ipairs[j].second;
+        GSeg s{};
+        s.term_begin = (int32_t)p1.terms.size();
+        s.term_count = 1;
+        p1.terms.push_back(GTerm{xp_off[x], 1.0});
+        s.lda = (int32_t)xp_ld[x];
+        s.b_off = Y.off[y];
+        s.ldb = (int32_t)Y.ld[y];
+        s.K = (int32_t)xk(x);
+        const int32_t sb = (int32_t)p1.segs.size();
+        p1.segs.push_back(s);
+        p1.flops += 2.0 * T.rows[j] * T.cols[j] * s.K;
+        add_tiles(p1, T.off[j], T.ld[j], T.rows[j], T.cols[j], sb, sb + 1, 0, 0);
+    }
+    sort_tiles(p1);
+
+    // phase 2: out_o = sum over chains T_t * (c op(Z_z))  (K-concatenation, one segment per chain)
+    PhasePlan& p2 = P.p2;
+    p2.slotA = SLOT_T; p2.slotB = SLOT_Z; p2.slotC = SLOT_OUT;
+    p2.transA = false; p2.transB = false; p2.transC = false;
+    std::vector<size_t> order(ch.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        if (ch[a].out != ch[b].out) return ch[a].out < ch[b].out;
+        if (ch[a].z != ch[b].z) return ch[a].z < ch[b].z;
+        return chain_t[a] < chain_t[b];
+    });
+    std::vector<char> seen(O.rows.size(), 0);
+    size_t i = 0;
+    while (i < order.size()) {
+        const int64_t o = ch[order[i]].out;
+        seen[o] = 1;
+        const int32_t sb = (int32_t)p2.segs.size();
+        double kk = 0;
+        while (i < order.size() && ch[order[i]].out == o) {
+            const size_t c = order[i];
+            const int64_t t = chain_t[c], zq = chain_zp[c];
+            GSeg s{};
+            s.term_begin = (int32_t)p2.terms.size();
+            s.term_count = 1;
+            p2.terms.push_back(GTerm{T.off[t], 1.0});
+            s.lda = (int32_t)T.ld[t];
+            s.b_off = zp_off[zq];
+            s.ldb = (int32_t)zp_ld[zq];
+            s.K = (int32_t)T.cols[t];
+            kk += s.K;
+            p2.segs.push_back(s);
+            ++i;
+        }
+        p2.flops += 2.0 * O.rows[o] * O.cols[o] * kk;
+        add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, (int32_t)p2.segs.size(), 0, 0);
+    }
+    P.flops_p2_unsummed = p2.flops;
+    const int32_t sb = (int32_t)p2.segs.size();
+    for (size_t o = 0; o < O.rows.size(); ++o)
+        if (!seen[o]) add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, sb, 0, 0);
     sort_tiles(p2);
     return P;
 }
