@@ -222,6 +222,25 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra,
                  const double* Aket, double* Enew, int precision);
 int vmps_env_destroy(vmps_env* e);
 
+/* ---- allocation-free chain product -------------------------------------------
+ * No counterpart in the reference: an extra entry point of this library.
+ * out (m x p) = alpha * op(X) * Y * op(Z) in FP64 for single dense blocks
+ * (op = transpose when trans* != 0), all column-major with leading dimension =
+ * rows, all pointers device pointers on the calling thread's current device.
+ * It allocates nothing: the intermediate op(X) * Y sits in a fixed 8 MiB array
+ * inside the library (2^20 doubles, present on every GPU that loads the library
+ * until the process exits), for callers that cannot call cudaMalloc at that
+ * point -- a framework that has given all device memory to its own pool, or a
+ * loop that cannot afford the device synchronisation of cudaMalloc/cudaFree.
+ * m * n above 2^20 returns VMPS_E_ARG.  All calls on a device share that array:
+ * calls that overlap on the GPU race.  The first call on a device looks up the
+ * array's address; make it outside any stream capture.  `stream` is a
+ * cudaStream_t (NULL = default stream); the work is asynchronous on it. */
+int vmps_chain_fp64_noalloc(const double* X, int64_t x_rows, int64_t x_cols, int32_t transX,
+                            const double* Y, int64_t y_rows, int64_t y_cols,
+                            const double* Z, int64_t z_rows, int64_t z_cols, int32_t transZ,
+                            double alpha, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -105,6 +105,9 @@ _PROTOS = [
     ("vmps_env_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),
     ("vmps_env_run", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, C.c_int]),
     ("vmps_env_destroy", C.c_int, [C.c_void_p]),
+    ("vmps_chain_fp64_noalloc", C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
+                                          C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_int32, C.c_double,
+                                          C.c_void_p, C.c_void_p]),
 ]
 
 EXPORTED = [p[0] for p in _PROTOS]

@@ -33,6 +33,9 @@ static int set_err(int code, const std::string& msg) {
     g_last_error = msg;
     return code;
 }
+namespace vmps {
+void set_last_error_message(const std::string& msg) { g_last_error = msg; }
+}
 struct CudaFail : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
