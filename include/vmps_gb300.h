@@ -213,6 +213,24 @@ int vmps_env_create(vmps_ctx* ctx, const vmps_symmetry* sym, int side,
                     const vmps_blocks* Eold, const vmps_blocks* Abra,
                     const vmps_mpo_site* W, const vmps_blocks* Aket,
                     vmps_env** out);
+/* CONTRACT_LR_MODE (tensors/DmrgContractions.h:13): restrict the W nonzeros by
+ * the position of an auxiliary index in the full MPO basis, as the VUMPS
+ * transfer operator does (VUMPS/VumpsMpoTransferMatrix.h:99-155):
+ *   TRIANGULAR : left: order(Lold.mid, a) > fixed_ab;  right: fixed_ab > order(Rold.mid, b)
+ *   FIXED_ROWS : left: order(Lold.mid, a) == fixed_ab; right: order(Lnew.mid, a) == fixed_ab
+ *   FIXED_COLS : left: order(Lnew.mid, b) == fixed_ab; right: order(Rold.mid, b) == fixed_ab
+ * The order map (basis_order_map) has n_order entries: QN order_qn[i*nq..],
+ * index inside that QN sector order_index[i], position order_value[i].       */
+#define VMPS_ENV_FULL       0
+#define VMPS_ENV_TRIANGULAR 1
+#define VMPS_ENV_FIXED_ROWS 2
+#define VMPS_ENV_FIXED_COLS 3
+int vmps_env_create_mode(vmps_ctx* ctx, const vmps_symmetry* sym, int side, int mode, int64_t fixed_ab,
+                         int64_t n_order, const int32_t* order_qn, const int32_t* order_index,
+                         const int64_t* order_value,
+                         const vmps_blocks* Eold, const vmps_blocks* Abra,
+                         const vmps_mpo_site* W, const vmps_blocks* Aket,
+                         vmps_env** out);
 /* output layout; arrays must hold nblocks (and nblocks*nq for QNs) entries     */
 int vmps_env_layout(const vmps_env* e, int64_t* nblocks, int64_t* total_elems);
 int vmps_env_layout_get(const vmps_env* e, int32_t* qin, int32_t* qout, int32_t* qmid,

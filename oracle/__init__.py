@@ -136,14 +136,28 @@ class OraclePivot:
             self._h = None
 
 
-class OracleEnv:
-    """contract_L (side 'L') / contract_R (side 'R'), FULL mode."""
+def order_arrays(nq, order):
+    """basis_order_map {(QN tuple, index in sector): position} as flat arrays"""
+    items = sorted(order.items())
+    qn = np.array([list(k[0]) for k, _ in items], dtype=np.int32).reshape(-1, nq) if items else np.zeros((0, nq), np.int32)
+    idx = np.array([k[1] for k, _ in items], dtype=np.int32)
+    val = np.array([v for _, v in items], dtype=np.int64)
+    return np.ascontiguousarray(qn), idx, val
 
-    def __init__(self, side, nq, E, B, W, K):
+
+MODES = {"FULL": 0, "TRIANGULAR": 1, "FIXED_ROWS": 2, "FIXED_COLS": 3}
+
+
+class OracleEnv:
+    """contract_L (side 'L') / contract_R (side 'R'), with CONTRACT_LR_MODE."""
+
+    def __init__(self, side, nq, E, B, W, K, mode="FULL", fixed_ab=0, order=None):
         from vmps_gb300.blocks import Blocks
-        self._keep = (E, B, W, K)
+        qn, idx, val = order_arrays(nq, order or {})
+        self._keep = (E, B, W, K, qn, idx, val)
         args = [C.c_int(0 if side == "L" else 1), C.c_int(nq)] + _tab(E) + _tab(B, mid=False) + \
-               _tab(K, mid=False) + _mpo(W)[:]
+               _tab(K, mid=False) + _mpo(W)[:] + [C.c_int(MODES[mode]), C.c_int64(fixed_ab), C.c_int64(len(val)),
+                                                  _p(qn), _p(idx), _p(val, C.c_int64)]
         self._h = C.c_void_p(lib().oracle_env_create(*args))
         n = lib().oracle_env_nblocks(self._h)
         qin = np.zeros((n, nq), np.int32); qout = np.zeros((n, nq), np.int32); qmid = np.zeros((n, nq), np.int32)

@@ -415,6 +415,10 @@ void hxv0(const Pivot& P, const double* vin, double* vout) {
 // contract_L / contract_R, FULL mode
 struct Env {
     int side = 0, nq = 1;
+    int mode = 0;              // CONTRACT_LR_MODE: 0 FULL, 1 TRIANGULAR, 2 FIXED_ROWS, 3 FIXED_COLS
+    int64_t fixed_ab = 0;
+    std::map<std::pair<Q, int>, int64_t> order;   // basis_order_map
+    int64_t at(const Q& q, int i) const { return order.at(std::make_pair(q, i)); }
     Tab E, B, K;
     Mpo W;
     Tab out;   // output layout (creation order)
@@ -452,6 +456,9 @@ void env_plan(Env& V) {
                 const auto* nz = W.find(s1, s2, k, Emid, Rmid);
                 if (!nz || !tri(Rin, Rmid, Rout)) continue;
                 for (const auto& e : *nz) {
+                    if (V.mode == 1 && !(V.at(Emid, e.row) > V.fixed_ab)) continue;
+                    if (V.mode == 3 && V.at(Rmid, e.col) != V.fixed_ab) continue;
+                    if (V.mode == 2 && V.at(Emid, e.row) != V.fixed_ab) continue;
                     int64_t la = aux_at(Et, qE, e.row);
                     if (la < 0) continue;
                     int64_t o = oblock(Q3{Rout, Rin, Rmid}, e.col, V.B.cols[qb], V.K.cols[qk]);
@@ -465,6 +472,9 @@ void env_plan(Env& V) {
                 const auto* nz = W.find(s1, s2, k, Lmid, Rmid);
                 if (!nz || !tri(Lout, Lmid, Lin)) continue;
                 for (const auto& e : *nz) {
+                    if (V.mode == 1 && !(V.fixed_ab > V.at(Rmid, e.col))) continue;
+                    if (V.mode == 2 && V.at(Lmid, e.row) != V.fixed_ab) continue;
+                    if (V.mode == 3 && V.at(Rmid, e.col) != V.fixed_ab) continue;
                     int64_t rb = aux_at(Et, qE, e.col);
                     if (rb < 0) continue;
                     int64_t o = oblock(Q3{Lout, Lin, Lmid}, e.row, V.K.rows[qk], V.B.rows[qb]);
@@ -578,10 +588,18 @@ void* oracle_env_create(int side, int nq, int64_t nE, const int32_t* Eqin, const
                         const int64_t* Kcols, const int64_t* Koff, int64_t nnz, const int32_t* s1, const int32_t* s2,
                         const int32_t* k, const int32_t* qin, const int32_t* qout, const int32_t* row,
                         const int32_t* col, const double* val, int nloc, const int32_t* qloc, int nop,
-                        const int32_t* qop) {
+                        const int32_t* qop, int mode, int64_t fixed_ab, int64_t n_order, const int32_t* order_qn,
+                        const int32_t* order_index, const int64_t* order_value) {
     Env* V = new Env();
     V->side = side;
     V->nq = nq;
+    V->mode = mode;
+    V->fixed_ab = fixed_ab;
+    for (int64_t i = 0; i < n_order; ++i) {
+        Q q{0, 0, 0, 0};
+        for (int c = 0; c < nq; ++c) q[c] = order_qn[i * nq + c];
+        V->order[std::make_pair(q, order_index[i])] = order_value[i];
+    }
     V->E = read_tab(nq, nE, Eqin, Eqout, Eqmid, Eleg, Erows, Ecols, Eoff);
     V->B = read_tab(nq, nB, Bqin, Bqout, nullptr, Bleg, Brows, Bcols, Boff);
     V->K = read_tab(nq, nK, Kqin, Kqout, nullptr, Kleg, Krows, Kcols, Koff);

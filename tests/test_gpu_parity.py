@@ -158,3 +158,21 @@ def test_lanczos_energy(gpu_ctx, case):
     es, vs, sts = H.lanczos(v0, "bf16x3", max_iter=300, tol_eigval=1e-9, tol_state=1e-5, refine_iters=30)
     assert abs(es - e_ref) < 1e-10 * abs(e_ref), (es, e_ref, sts)
     assert sts["hxv_split"] > 0 and sts["refine_iterations"] > 0
+
+
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("mode,ab", [("FIXED_ROWS", 0), ("FIXED_COLS", 5), ("TRIANGULAR", 1)])
+def test_env_mode_parity(gpu_ctx, side, mode, ab):
+    model, Q = make_model("hubb", 8)
+    from vmps_gb300.mps import RandomMPS
+    mps = RandomMPS(model, Q, 24, seed=13).canonicalize(4, 4)
+    Lenv, Renv = oracle_envs(model, mps, 3, 5)
+    l = 3 if side == "L" else 5
+    E = Lenv if side == "L" else Renv
+    order = dict(model.basis_order_map(l))
+    order.update(model.basis_order_map(l + 1))
+    A = mps.A[l]
+    ref = oracle.OracleEnv(side, 2, E, A, model.W[l], A, mode=mode, fixed_ab=ab, order=order).run(E, A, A)
+    e = EnvUpdate(gpu_ctx, model.sym, side, E, A, model.W[l], A, mode=mode, fixed_ab=ab, order=order)
+    assert compare_tripods(e.run(E, A, A, "fp64"), ref) < TOL_FP64
+    assert compare_tripods(e.run(E, A, A, "bf16x3"), ref) < TOL_SPLIT

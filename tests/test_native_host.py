@@ -126,3 +126,32 @@ def test_invalid_tables_are_rejected(host_ctx):
     rc = N.lib().vmps_pivot1_create(None, None, None, None, None, None, None, None, C.byref(h))
     assert rc == -1
     assert N.lib().vmps_last_error()
+
+
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("mode,ab", [("FIXED_ROWS", 0), ("FIXED_ROWS", 2), ("FIXED_COLS", 1), ("FIXED_COLS", 5),
+                                     ("TRIANGULAR", 1), ("TRIANGULAR", 4)])
+def test_env_mode_layout_matches_oracle(host_ctx, side, mode, ab):
+    model, Q = make_model("hubb", 8)
+    from vmps_gb300.mps import RandomMPS
+    mps = RandomMPS(model, Q, 24, seed=13).canonicalize(4, 4)
+    Lenv, Renv = oracle_envs(model, mps, 3, 5)
+    l = 3 if side == "L" else 5
+    E = Lenv if side == "L" else Renv
+    order = dict(model.basis_order_map(l))
+    order.update(model.basis_order_map(l + 1))
+    e = EnvUpdate(host_ctx, model.sym, side, E, mps.A[l], model.W[l], mps.A[l], mode=mode, fixed_ab=ab, order=order)
+    ref = oracle.OracleEnv(side, 2, E, mps.A[l], model.W[l], mps.A[l], mode=mode, fixed_ab=ab, order=order).layout
+    got = {e.out_layout.key(i): (e.out_layout.rows[i], e.out_layout.cols[i]) for i in range(e.out_layout.n)}
+    exp = {ref.key(i): (ref.rows[i], ref.cols[i]) for i in range(ref.n)}
+    assert got == exp
+
+
+def test_env_mode_without_order_map_is_rejected(host_ctx):
+    model, Q = make_model("heis", 6)
+    from vmps_gb300.mps import RandomMPS
+    mps = RandomMPS(model, Q, 8, seed=1).canonicalize(3, 3)
+    Lenv, _ = oracle_envs(model, mps, 2, 4)
+    with pytest.raises(N.VmpsError) as ei:
+        EnvUpdate(host_ctx, model.sym, "L", Lenv, mps.A[2], model.W[2], mps.A[2], mode="FIXED_COLS", fixed_ab=0)
+    assert ei.value.code == -1

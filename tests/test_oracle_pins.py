@@ -140,3 +140,43 @@ def test_oracle_blas_and_inhouse_agree():
     if p:
         lib.oracle_set_blas(p.encode())
     assert rel_err(a, b) < 1e-13
+
+
+def _env_case(side):
+    from helpers import make_model, oracle_envs
+    from vmps_gb300.mps import RandomMPS
+    model, Q = make_model("hubb", 8)
+    mps = RandomMPS(model, Q, 24, seed=13).canonicalize(4, 4)
+    Lenv, Renv = oracle_envs(model, mps, 3, 5)
+    l = 3 if side == "L" else 5
+    E = Lenv if side == "L" else Renv
+    # the order map of the auxiliary bond the mode refers to
+    return model, mps, E, l
+
+
+@pytest.mark.parametrize("side", ["L", "R"])
+def test_oracle_env_modes_partition_full(side):
+    """FIXED_COLS / FIXED_ROWS over all positions partition the W nonzeros, so their
+    sum is the FULL contraction; TRIANGULAR(ab) is the sum of FIXED_ROWS (left) or
+    FIXED_COLS (right) over the positions it keeps."""
+    from helpers import blocks_by_key
+    model, mps, E, l = _env_case(side)
+    W, A = model.W[l], mps.A[l]
+    full = blocks_by_key(oracle.OracleEnv(side, 2, E, A, W, A).run(E, A, A))
+    # positions: the incoming (Lold/Rold) and outgoing (Lnew/Rnew) auxiliary bonds
+    old_bond, new_bond = (l, l + 1) if side == "L" else (l + 1, l)
+    order = dict(model.basis_order_map(old_bond))
+    order.update(model.basis_order_map(new_bond))   # same QN/index labels on inner bonds
+    npos = len(model.aux[new_bond])
+    for mode in ("FIXED_COLS", "FIXED_ROWS"):
+        acc = {}
+        for ab in range(max(npos, len(model.aux[old_bond]))):
+            part = oracle.OracleEnv(side, 2, E, A, W, A, mode=mode, fixed_ab=ab, order=order).run(E, A, A)
+            for k, v in blocks_by_key(part).items():
+                acc[k] = acc.get(k, 0) + v
+        assert set(acc) == set(full)
+        for k in full:
+            assert np.allclose(acc[k], full[k], atol=1e-12 * max(1.0, np.abs(full[k]).max()))
+    # TRIANGULAR keeps a strict subset of FULL
+    tri = blocks_by_key(oracle.OracleEnv(side, 2, E, A, W, A, mode="TRIANGULAR", fixed_ab=1, order=order).run(E, A, A))
+    assert set(tri) <= set(full)

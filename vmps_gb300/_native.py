@@ -19,6 +19,7 @@ SYM_U1 = 0
 SYM_SU2 = 1
 ENV_LEFT = 0
 ENV_RIGHT = 1
+ENV_MODES = {"FULL": 0, "TRIANGULAR": 1, "FIXED_ROWS": 2, "FIXED_COLS": 3}
 
 ERRORS = {-1: "VMPS_E_ARG", -2: "VMPS_E_CUDA", -3: "VMPS_E_NOMEM", -4: "VMPS_E_SHAPE",
           -5: "VMPS_E_TIMEOUT", -6: "VMPS_E_NONFINITE", -7: "VMPS_E_UNSUPPORTED"}
@@ -100,6 +101,9 @@ _PROTOS = [
     ("vmps_env_create", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.c_int, C.POINTER(vmps_blocks),
                                   C.POINTER(vmps_blocks), C.POINTER(vmps_mpo_site), C.POINTER(vmps_blocks),
                                   C.POINTER(C.c_void_p)]),
+    ("vmps_env_create_mode", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.c_int, C.c_int, C.c_int64,
+                                       C.c_int64, i32p, i32p, i64p, C.POINTER(vmps_blocks), C.POINTER(vmps_blocks),
+                                       C.POINTER(vmps_mpo_site), C.POINTER(vmps_blocks), C.POINTER(C.c_void_p)]),
     ("vmps_env_layout", C.c_int, [C.c_void_p, i64p, i64p]),
     ("vmps_env_layout_get", C.c_int, [C.c_void_p, i32p, i32p, i32p, i32p, i64p, i64p, i64p]),
     ("vmps_env_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),

@@ -6,6 +6,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <stdexcept>
+
 #include "qn.hpp"
 #include "../../include/vmps_gb300.h"
 
@@ -84,9 +86,28 @@ ChainSet build_pivot2(const Symmetry& sym, const BlockTable& L, const BlockTable
                       const MpoView& W12, const MpoView& W34, const BlockTable& V);
 ChainSet build_pivot0(const Symmetry& sym, const BlockTable& L, const BlockTable& R,
                       const BlockTable& V);
+// contract_L / contract_R modes (tensors/DmrgContractions.h:13, :100-104, :245-249):
+// basis_order_map (MPO auxiliary QN, index inside its sector) -> position in the full auxiliary basis
+struct AuxKey {
+    QN q; int32_t idx;
+    bool operator==(const AuxKey& o) const { return q == o.q && idx == o.idx; }
+};
+struct AuxKeyHash {
+    size_t operator()(const AuxKey& k) const { return QNHash()(k.q) * 1000003u ^ (size_t)(uint32_t)k.idx; }
+};
+struct EnvMode {
+    int mode = VMPS_ENV_FULL;
+    int64_t fixed_ab = 0;
+    std::unordered_map<AuxKey, int64_t, AuxKeyHash> order;
+    int64_t at(const QN& q, int32_t idx) const {
+        auto it = order.find(AuxKey{q, idx});
+        if (it == order.end()) throw std::invalid_argument("basis_order_map has no entry for an auxiliary index in use");
+        return it->second;
+    }
+};
 // contract_L / contract_R: also derives the output Tripod layout
 ChainSet build_env(const Symmetry& sym, int side, const BlockTable& Eold, const BlockTable& Abra,
-                   const MpoView& W, const BlockTable& Aket, BlockTable* Enew);
+                   const MpoView& W, const BlockTable& Aket, BlockTable* Enew, const EnvMode& mode = EnvMode());
 
 // combined two-site index s1s3 of Qbasis::combine (tensors/Qbasis.h:685-798)
 struct CombinedBasis {
@@ -118,8 +139,10 @@ struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, 
 struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, pad; };
 // at most this many A terms per segment (the kernels stage them in shared memory)
 constexpr int kMaxTerms = 16;
-// tile edges: at most 64 x 64, rows split on multiples of 16, columns on multiples of 8
+// tile edges (rows split on multiples of 16, columns on multiples of 8):
+// mma.sync engines at most 64 x 64, the tcgen05 engine at most 128 x 64
 constexpr int kTileMax = 64;
+constexpr int kUmmaTileM = 128, kUmmaTileN = 64;
 
 struct PhasePlan {
     std::vector<GTerm> terms;
@@ -147,6 +170,7 @@ struct Plan {
     double flops_p2_unsummed = 0;
     // split-precision plans only
     bool split = false;
+    int split_kernel = 0;                         // 0: mma.sync engine, 1: tcgen05 engine
     int64_t Xp_total = 0, Zp_total = 0;           // prepared-operand arena sizes (elements)
     std::vector<PrepBlock> prepX, prepZ;          // X blocks, and c*op(Z) copies
 };
@@ -157,6 +181,6 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // copies; the chain coefficient rides on a scaled copy of op(Z); the second
 // phase is a K-concatenation over chains
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ);
+                     const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n);
 
 }  // namespace vmps

@@ -521,7 +521,9 @@ static int grid_for(int64_t n, int threads, int cap) {
 cudaError_t kernels_init() {
     cudaError_t e = cudaFuncSetAttribute(gg_split_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp3::SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(gg_split_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp3::SMEM_BYTES);
+    e = cudaFuncSetAttribute(gg_split_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp3::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    return umma_init();
 }
 
 cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st) {

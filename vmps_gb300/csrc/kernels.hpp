@@ -13,6 +13,7 @@ struct GGArgs {
     const void* A2;   // split precision: lo halves of A, B (hi in A, B)
     const void* B2;
     void* C2;         // split precision with a split output: lo half of C
+    int* err;         // device error word: bit 0 = a bounded wait ran out (tcgen05 engine)
     const GTile* tiles;
     const GSeg* segs;
     const GTerm* terms;
@@ -28,6 +29,9 @@ cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st);
 // split-precision grouped GEMM on pre-split K-contiguous operands;
 // out_split = 1: C/C2 are bf16 hi/lo, 0: C is double
 cudaError_t launch_gg_split(int out_split, const GGArgs& a, cudaStream_t st);
+// tcgen05 engine (umma.cu): same arguments as launch_gg_split, tiles up to 128 x 64
+cudaError_t umma_init();
+cudaError_t launch_gg_umma(int out_split, const GGArgs& a, cudaStream_t st);
 cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* hi, void* lo, cudaStream_t st);
 cudaError_t launch_split(const double* src, void* hi, void* lo, int64_t n, cudaStream_t st);
 cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, double* dst, int to_padded,

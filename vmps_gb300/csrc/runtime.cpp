@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -87,7 +88,29 @@ struct vmps_ctx_s {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    int* err = nullptr;   // device error word written by the tcgen05 engine
 };
+
+// split-precision engine: tcgen05 (default) or mma.sync (VMPS_SPLIT_ENGINE=mma)
+static int split_engine() {
+    static int e = [] {
+        const char* s = std::getenv("VMPS_SPLIT_ENGINE");
+        return (s && std::string(s) == "mma") ? 0 : 1;
+    }();
+    return e;
+}
+
+// read and clear the device error word (after the stream has been synchronised)
+static void check_device_error(vmps_ctx* c) {
+    if (!c || !c->err) return;
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, c->err, 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (h) {
+        CK(cudaMemsetAsync(c->err, 0, 4, c->stream));
+        throw CudaFail("a bounded device wait in the tcgen05 engine ran out (error word " + std::to_string(h) + ")");
+    }
+}
 
 // device copy of one phase's work lists
 struct DevPhase {
@@ -128,6 +151,7 @@ struct Operands {
     const double* Y = nullptr;
     const double* Z = nullptr;
     double* O = nullptr;
+    int* err = nullptr;
 };
 
 // device buffers and work lists of a freshly made plan
@@ -169,6 +193,7 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
     a.terms = d.terms.as<GTerm>();
     a.ntiles = d.ntiles;
     a.transA = h.transA; a.transB = h.transB; a.transC = h.transC;
+    a.err = ops.err;
     if (!dp.plan.split) {
         auto slot = [&](int s) -> const void* {
             switch (s) {
@@ -196,6 +221,7 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
     if (d.ntiles > 0 && (!a.C || !a.tiles || !a.segs || !a.terms || (!h.segs.empty() && (!a.A || !a.B))))
         throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
     if (!dp.plan.split) CK(launch_gg64(a, st));
+    else if (dp.plan.split_kernel) CK(launch_gg_umma(ph == 1 ? 1 : 0, a, st));
     else CK(launch_gg_split(ph == 1 ? 1 : 0, a, st));
 }
 
@@ -280,7 +306,12 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
     DevPlan& dp = p->plans[prec];
     if (dp.ready) return dp;
     if (prec == VMPS_PREC_FP64) dp.plan = make_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 64, 64);
-    else dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false);
+    else {
+        const int eng = split_engine();
+        dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, eng ? kUmmaTileM : kTileMax,
+                                  eng ? kUmmaTileN : kTileMax);
+        dp.plan.split_kernel = eng;
+    }
     if (p->ctx->device < 0) { dp.ready = true; return dp; }   // host-only: plan without device copies
     plan_to_device(dp, p->Vd.total, p->st());
     split_prepare(dp, p->dL.as<double>(), p->dR.as<double>(), p->st());
@@ -301,6 +332,7 @@ static void pivot_hxv_dev(vmps_pivot* p, int prec, const double* vin, double* vo
     ops.Z = p->dR.as<double>();
     ops.Y = vin;
     ops.O = vout;
+    ops.err = p->ctx->err;
     run_plan(dp, ops, p->st());
 }
 
@@ -391,6 +423,8 @@ int vmps_ctx_create(int device, vmps_ctx** out) {
     CK(cudaEventCreate(&c->ev0));
     CK(cudaEventCreate(&c->ev1));
     CK(cudaEventCreate(&c->ev2));
+    CK(cudaMalloc((void**)&c->err, 64));
+    CK(cudaMemset(c->err, 0, 64));
     *out = c;
     API_END
 }
@@ -402,6 +436,7 @@ int vmps_ctx_destroy(vmps_ctx* ctx) {
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
     cudaEventDestroy(ctx->ev2);
+    if (ctx->err) cudaFree(ctx->err);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return VMPS_OK;
@@ -486,6 +521,7 @@ int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int prec) {
     CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->vout.as<double>(), p->stage_out.as<double>(), 0, st));
     CK(cudaMemcpyAsync(vout, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    check_device_error(p->ctx);
     API_END
 }
 
@@ -580,6 +616,7 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
     ops.Z = p->dR.as<double>();
     ops.Y = vi;
     ops.O = vo;
+    ops.err = p->ctx->err;
     if (use_graph) {
         if (!p->graph[prec] || p->graph_in[prec] != vi || p->graph_out[prec] != vo) {
             if (p->graph[prec]) { cudaGraphExecDestroy(p->graph[prec]); p->graph[prec] = nullptr; }
@@ -607,6 +644,7 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
     CK(cudaEventSynchronize(p->ctx->ev1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, p->ctx->ev0, p->ctx->ev1));
+    check_device_error(p->ctx);
     if (ms_per_hxv) *ms_per_hxv = ms / n_iter;
     if (ms_phase2) {
         // second grouped-GEMM phase alone (its inputs are in place from the runs above)
@@ -816,6 +854,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, x, p->stage_out.as<double>(), 0, st));
     CK(cudaMemcpyAsync(v, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    check_device_error(p->ctx);
     *energy = e;
     s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = s;
@@ -846,7 +885,12 @@ static DevPlan& env_plan(vmps_env* e, int prec) {
     const DevLayout& X = L ? e->Bd : e->Kd;
     const DevLayout& Z = L ? e->Kd : e->Bd;
     if (prec == VMPS_PREC_FP64) dp.plan = make_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L, 64, 64);
-    else dp.plan = make_split_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L);
+    else {
+        const int eng = split_engine();
+        dp.plan = make_split_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L, eng ? kUmmaTileM : kTileMax,
+                                  eng ? kUmmaTileN : kTileMax);
+        dp.plan.split_kernel = eng;
+    }
     if (e->ctx->device < 0) { dp.ready = true; return dp; }
     plan_to_device(dp, e->Ed.total, e->st());
     CK(cudaStreamSynchronize(e->st()));
@@ -858,10 +902,31 @@ extern "C" {
 
 int vmps_env_create(vmps_ctx* ctx, const vmps_symmetry* symd, int side, const vmps_blocks* Eold,
                     const vmps_blocks* Abra, const vmps_mpo_site* W, const vmps_blocks* Aket, vmps_env** out) {
+    return vmps_env_create_mode(ctx, symd, side, VMPS_ENV_FULL, 0, 0, nullptr, nullptr, nullptr, Eold, Abra, W, Aket,
+                                out);
+}
+
+int vmps_env_create_mode(vmps_ctx* ctx, const vmps_symmetry* symd, int side, int mode, int64_t fixed_ab,
+                         int64_t n_order, const int32_t* order_qn, const int32_t* order_index,
+                         const int64_t* order_value, const vmps_blocks* Eold, const vmps_blocks* Abra,
+                         const vmps_mpo_site* W, const vmps_blocks* Aket, vmps_env** out) {
     API_BEGIN
     if (!ctx || !out) return set_err(VMPS_E_ARG, "null argument");
     if (side != VMPS_ENV_LEFT && side != VMPS_ENV_RIGHT) return set_err(VMPS_E_ARG, "side must be LEFT or RIGHT");
+    if (mode < VMPS_ENV_FULL || mode > VMPS_ENV_FIXED_COLS) return set_err(VMPS_E_ARG, "unknown contraction mode");
     Symmetry sym = make_sym(symd);
+    EnvMode md;
+    md.mode = mode;
+    md.fixed_ab = fixed_ab;
+    if (mode != VMPS_ENV_FULL) {
+        if (n_order <= 0 || !order_qn || !order_index || !order_value)
+            return set_err(VMPS_E_ARG, "modes other than FULL need the basis order map");
+        for (int64_t i = 0; i < n_order; ++i) {
+            QN q;
+            for (int c = 0; c < sym.nq; ++c) q.v[c] = order_qn[i * sym.nq + c];
+            md.order[AuxKey{q, order_index[i]}] = order_value[i];
+        }
+    }
     std::unique_ptr<vmps_env> e(new vmps_env_s());
     e->ctx = ctx;
     e->sym = sym;
@@ -870,7 +935,7 @@ int vmps_env_create(vmps_ctx* ctx, const vmps_symmetry* symd, int side, const vm
     e->Bt = parse_blocks(sym, Abra, false);
     e->Kt = parse_blocks(sym, Aket, false);
     MpoView Wv = parse_mpo(sym, W);
-    e->cs = build_env(sym, side, e->Et, e->Bt, Wv, e->Kt, &e->Nt);
+    e->cs = build_env(sym, side, e->Et, e->Bt, Wv, e->Kt, &e->Nt, md);
     e->Ed = make_dev_layout(e->Et.rows, e->Et.cols);
     e->Bd = make_dev_layout(e->Bt.rows, e->Bt.cols);
     e->Kd = make_dev_layout(e->Kt.rows, e->Kt.cols);
@@ -929,6 +994,7 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra, const doub
     else { ops.X = e->dK.as<double>(); ops.Z = e->dB.as<double>(); }
     ops.Y = e->dE.as<double>();
     ops.O = e->dN.as<double>();
+    ops.err = e->ctx->err;
     split_prepare(dp, ops.X, ops.Z, st);
     run_plan(dp, ops, st);
     if (!e->pkN.p) {
@@ -940,6 +1006,7 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra, const doub
     if (e->Nt.total > 0)
         CK(cudaMemcpyAsync(Enew, e->stage.p, (size_t)e->Nt.total * 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    check_device_error(e->ctx);
     API_END
 }
 

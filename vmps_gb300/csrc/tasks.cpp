@@ -433,7 +433,7 @@ ChainSet build_pivot0(const Symmetry& sym, const BlockTable& L, const BlockTable
 // contract_L / contract_R (FULL mode), tensors/DmrgContractions.h:35-311
 // ===========================================================================
 ChainSet build_env(const Symmetry& sym, int side, const BlockTable& E, const BlockTable& Abra, const MpoView& W,
-                   const BlockTable& Aket, BlockTable* Enew) {
+                   const BlockTable& Aket, BlockTable* Enew, const EnvMode& md) {
     ChainSet cs;
     TripodView Ev = make_tripod_view(E);
     BipedsView Bv = make_bipeds_view(Abra, W.nloc), Kv = make_bipeds_view(Aket, W.nloc);
@@ -496,6 +496,10 @@ ChainSet build_env(const Symmetry& sym, int side, const BlockTable& E, const Blo
                             cs.n_tasks++;
                             QN3 quple{{Rout, Rin, Rmid}};
                             for (const auto& e : *nz) {
+                                // mode filter of contract_L (tensors/DmrgContractions.h:100-104)
+                                if (md.mode == VMPS_ENV_TRIANGULAR && !(md.at(Emid, e.row) > md.fixed_ab)) continue;
+                                if (md.mode == VMPS_ENV_FIXED_COLS && md.at(Rmid, e.col) != md.fixed_ab) continue;
+                                if (md.mode == VMPS_ENV_FIXED_ROWS && md.at(Emid, e.row) != md.fixed_ab) continue;
                                 int64_t la = Ev.at(qE, e.row);
                                 if (la < 0) continue;
                                 // Abra^dagger (cols_bra x rows_bra) * L (rows_bra x rows_ket) * Aket
@@ -533,6 +537,10 @@ ChainSet build_env(const Symmetry& sym, int side, const BlockTable& E, const Blo
                             cs.n_tasks++;
                             QN3 quple{{Lout, Lin, Lmid}};
                             for (const auto& e : *nz) {
+                                // mode filter of contract_R (tensors/DmrgContractions.h:245-249)
+                                if (md.mode == VMPS_ENV_TRIANGULAR && !(md.fixed_ab > md.at(Rmid, e.col))) continue;
+                                if (md.mode == VMPS_ENV_FIXED_ROWS && md.at(Lmid, e.row) != md.fixed_ab) continue;
+                                if (md.mode == VMPS_ENV_FIXED_COLS && md.at(Rmid, e.col) != md.fixed_ab) continue;
                                 int64_t rb = Ev.at(qE, e.col);
                                 if (rb < 0) continue;
                                 // Aket (rows_ket x cols_ket) * R (cols_ket x cols_bra) * Abra^dagger
@@ -593,13 +601,13 @@ struct Key4Hash {
     }
 };
 
-// split an extent into balanced pieces of at most kTileMax, each a multiple of
+// split an extent into balanced pieces of at most tmax, each a multiple of
 // `gran` except the last: 193 -> 48,48,48,49 rather than 64,64,64,1
-static std::vector<std::pair<int64_t, int64_t>> split_extent(int64_t m, int64_t gran) {
+static std::vector<std::pair<int64_t, int64_t>> split_extent(int64_t m, int64_t gran, int64_t tmax) {
     std::vector<std::pair<int64_t, int64_t>> out;
-    const int64_t nt = (m + kTileMax - 1) / kTileMax;
+    const int64_t nt = (m + tmax - 1) / tmax;
     int64_t base = gran * (m / (nt * gran));
-    if (base < gran || m - base * (nt - 1) > kTileMax) base = gran * ((m + nt * gran - 1) / (nt * gran));
+    if (base < gran || m - base * (nt - 1) > tmax) base = gran * ((m + nt * gran - 1) / (nt * gran));
     int64_t r = 0;
     for (int64_t i = 0; i < nt && r < m; ++i) {
         const int64_t len = (i + 1 == nt) ? m - r : std::min(base, m - r);
@@ -610,9 +618,10 @@ static std::vector<std::pair<int64_t, int64_t>> split_extent(int64_t m, int64_t 
 }
 
 // append tiles of an m x n output block whose segments are [sb, se)
-void add_tiles(PhasePlan& ph, int64_t c_off, int64_t ldc, int64_t m, int64_t n, int32_t sb, int32_t se, int, int) {
-    for (const auto& rs : split_extent(m, 16))
-        for (const auto& cs : split_extent(n, 8)) {
+void add_tiles(PhasePlan& ph, int64_t c_off, int64_t ldc, int64_t m, int64_t n, int32_t sb, int32_t se, int tile_m,
+               int tile_n) {
+    for (const auto& rs : split_extent(m, 16, tile_m))
+        for (const auto& cs : split_extent(n, 8, tile_n)) {
             GTile t{};
             t.c_off = c_off;
             t.ldc = (int32_t)ldc;
@@ -858,7 +867,7 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // split-precision planner
 // ===========================================================================
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ) {
+                     const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n) {
     Plan P;
     P.split = true;
     P.association = 0;
@@ -986,7 +995,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         const int32_t sb = (int32_t)p1.segs.size();
         p1.segs.push_back(s);
         p1.flops += 2.0 * T.rows[j] * T.cols[j] * s.K;
-        add_tiles(p1, T.off[j], T.ld[j], T.rows[j], T.cols[j], sb, sb + 1, 0, 0);
+        add_tiles(p1, T.off[j], T.ld[j], T.rows[j], T.cols[j], sb, sb + 1, tile_m, tile_n);
     }
     sort_tiles(p1);
 
@@ -1024,12 +1033,12 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
             ++i;
         }
         p2.flops += 2.0 * O.rows[o] * O.cols[o] * kk;
-        add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, (int32_t)p2.segs.size(), 0, 0);
+        add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, (int32_t)p2.segs.size(), tile_m, tile_n);
     }
     P.flops_p2_unsummed = p2.flops;
     const int32_t sb = (int32_t)p2.segs.size();
     for (size_t o = 0; o < O.rows.size(); ++o)
-        if (!seen[o]) add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, sb, 0, 0);
+        if (!seen[o]) add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, sb, tile_m, tile_n);
     sort_tiles(p2);
     return P;
 }

@@ -104,6 +104,15 @@ class ChainModel:
             site.add(s1, s2, kidx[qop], qi, qo, ri, co, v)
         return site
 
+    def basis_order_map(self, l):
+        """basis_order_map of bond l: (aux QN, index inside its QN sector) -> position in the bond's aux list"""
+        cnt, out = {}, {}
+        for pos, (_, q) in enumerate(self.aux[l]):
+            q = tuple(q)
+            out[(q, cnt.get(q, 0))] = pos
+            cnt[q] = cnt.get(q, 0) + 1
+        return out
+
     # dense representation (tests, exact diagonalisation)
     def aux_qns(self, l):
         return [q for _, q in self.aux[l]]

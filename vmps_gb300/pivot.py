@@ -193,13 +193,22 @@ def time_hxv(H: _Pivot, vin: DeviceVector, vout: DeviceVector, precision="fp64",
 class EnvUpdate:
     """Prepared contract_L / contract_R for fixed block layouts."""
 
-    def __init__(self, ctx: Context, sym: Symmetry, side: str, Eold: Blocks, Abra: Blocks, W: MpoSite, Aket: Blocks):
+    def __init__(self, ctx: Context, sym: Symmetry, side: str, Eold: Blocks, Abra: Blocks, W: MpoSite, Aket: Blocks,
+                 mode: str = "FULL", fixed_ab: int = 0, order: dict | None = None):
+        """mode: CONTRACT_LR_MODE (FULL, TRIANGULAR, FIXED_ROWS, FIXED_COLS); order: basis_order_map
+        {(aux QN, index inside the sector): position in the full auxiliary basis}."""
         self.ctx, self.sym = ctx, sym
         self._h = C.c_void_p()
         s, eb, bb, kb, wb = sym.c_struct(), Eold.c_struct(), Abra.c_struct(), Aket.c_struct(), W.c_struct()
         sd = N.ENV_LEFT if side == "L" else N.ENV_RIGHT
-        N.check(N.lib().vmps_env_create(ctx._h, C.byref(s), sd, C.byref(eb), C.byref(bb), C.byref(wb), C.byref(kb),
-                                        C.byref(self._h)))
+        items = sorted((order or {}).items())
+        qn = np.ascontiguousarray(np.array([list(k[0]) for k, _ in items], dtype=np.int32).reshape(-1, sym.nq))
+        idx = np.ascontiguousarray([k[1] for k, _ in items], dtype=np.int32)
+        val = np.ascontiguousarray([v for _, v in items], dtype=np.int64)
+        N.check(N.lib().vmps_env_create_mode(ctx._h, C.byref(s), sd, N.ENV_MODES[mode], fixed_ab, len(val),
+                                             qn.ctypes.data_as(N.i32p), idx.ctypes.data_as(N.i32p),
+                                             val.ctypes.data_as(N.i64p), C.byref(eb), C.byref(bb), C.byref(wb),
+                                             C.byref(kb), C.byref(self._h)))
         nb, tot = C.c_int64(), C.c_int64()
         N.check(N.lib().vmps_env_layout(self._h, C.byref(nb), C.byref(tot)))
         nq, n = sym.nq, nb.value
