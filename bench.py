@@ -147,6 +147,39 @@ def cpu_oracle_hxv_rate(L, R, V, W1, W2, threads, n_hxv, warm=1):
     return n_hxv / dt, dt, oracle.blas_kind()
 
 
+def sweep_bench(ctx, args, with_cpu=True):
+    """Single-site DMRG sweep times: Heisenberg L=32, D=64 (GPU FP64 and the CPU
+    oracle, 2 sweeps) and Hubbard L=64, D=1024 (GPU, split precision + FP64
+    refinement, 1 sweep).  HxV, Lanczos and contract_L/R on the GPU; the QR
+    gauge step on the host."""
+    import copy
+
+    from vmps_gb300 import models
+    from vmps_gb300.dmrg import dmrg1
+    from vmps_gb300.mps import RandomMPS
+    out = {}
+    model = models.heisenberg_u1(32)
+    mps = RandomMPS(model, (0,), 64, seed=1, profile="gaussian", sigma=[4.0]).canonicalize(0, 0)
+    mps_cpu = copy.deepcopy(mps)
+    g = dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", tol_eigval=1e-12, tol_state=1e-8)
+    out["heisenberg_L32_D64"] = {"gpu_fp64_s_per_sweep": g["sweep_times"], "E_gpu": g["energies"],
+                                 "hxv": g["hxv"]}
+    if with_cpu:
+        from oracle.dmrg_cpu import dmrg1_cpu
+        c = dmrg1_cpu(model, mps_cpu, n_sweeps=2)
+        out["heisenberg_L32_D64"].update({"cpu_s_per_sweep": c["sweep_times"], "E_cpu": c["energies"],
+                                          "E_rel_diff": abs(c["energies"][-1] - g["energies"][-1]) /
+                                          abs(c["energies"][-1])})
+    if args.D >= 1024:
+        model = models.hubbard_u1xu1(64, t=1.0, U=4.0)
+        mps = RandomMPS(model, (64, 0), 1024, seed=2, profile="gaussian", sigma=[2.5, 2.5]).canonicalize(0, 0)
+        h = dmrg1(ctx, model, mps, n_sweeps=1, precision=args.precision, tol_eigval=1e-10, tol_state=1e-6,
+                  refine_iters=20)
+        out["hubbard_L64_D1024"] = {"gpu_split_s_per_sweep": h["sweep_times"], "E": h["energies"],
+                                    "hxv": h["hxv"], "env_init_s": h["init_time"]}
+    return out
+
+
 def run_reference(args):
     """CPU restatement of the reference path (the oracle), all host threads."""
     rank = int(os.environ.get("RANK", "0"))
@@ -196,6 +229,7 @@ def main():
     ap.add_argument("--cpu-hxv", type=int, default=3, help="HxV applications in the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-energy", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -296,6 +330,10 @@ def main():
                 "useful_tflops": flops_phase / (t_phase * 1e-3) / 1e12,
                 "note": "3 bf16 products per useful FMA (hi*hi + hi*lo + lo*hi)"}
 
+    sweep = None
+    if not args.no_sweep and rank == 0:
+        sweep = sweep_bench(ctx, args, with_cpu=not args.no_cpu and world == 1)
+
     cpu = None
     if not args.no_cpu and world == 1 and rank == 0:
         threads = os.cpu_count() or 1
@@ -328,6 +366,7 @@ def main():
             "phase_ms": {"phase1": ms1, "phase2": ms2},
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "dmrg_sweep": sweep,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -180,3 +180,17 @@ def test_oracle_env_modes_partition_full(side):
     # TRIANGULAR keeps a strict subset of FULL
     tri = blocks_by_key(oracle.OracleEnv(side, 2, E, A, W, A, mode="TRIANGULAR", fixed_ab=1, order=order).run(E, A, A))
     assert set(tri) <= set(full)
+
+
+def test_oracle_dmrg1_heisenberg_matches_ed():
+    """single-site DMRG on the oracle with complete bond bases reaches the ED energy"""
+    from oracle.dmrg_cpu import dmrg1_cpu
+    from vmps_gb300.mps import RandomMPS
+    L = 10
+    model = models.heisenberg_u1(L)
+    mps = RandomMPS(model, (0,), 64, seed=3).canonicalize(0, 0)
+    res = dmrg1_cpu(model, mps, n_sweeps=2)
+    H = models.dense_heisenberg(L)
+    M = np.array([sum(1 if ((s >> (L - 1 - j)) & 1) == 0 else -1 for j in range(L)) for s in range(2 ** L)])
+    e_ed = ed.ground_energy(H, M == 0)
+    assert abs(res["energies"][-1] - e_ed) < 1e-10 * abs(e_ed)
