@@ -148,12 +148,19 @@ struct PhasePlan {
     std::vector<GTerm> terms;
     std::vector<GSeg>  segs;
     std::vector<GTile> tiles;
+    // split plans: per segment, the prepared-operand block of A and of B (TMA descriptor index)
+    std::vector<int32_t> seg_amap, seg_bmap;
     bool transA = false, transB = false, transC = false;
     int  slotA = 0, slotB = 0, slotC = 0;   // arena ids
     double flops = 0;
 };
 
 enum Slot { SLOT_X = 0, SLOT_Y = 1, SLOT_Z = 2, SLOT_OUT = 3, SLOT_T = 4 };
+
+// A prepared split-precision operand block: `outer` rows (rows of A / columns of
+// B) of K contiguous elements, row stride ld, at element offset off of its
+// [hi | lo] arena (lo half at +total)
+struct OpBlock { int64_t off; int32_t outer, K, ld, pad; };
 
 // Split-precision operand preparation: one block of a column-major FP64 source
 // (rows x cols, leading dimension src_ld) written as bf16 hi/lo pairs in the
@@ -173,6 +180,7 @@ struct Plan {
     int split_kernel = 0;                         // 0: mma.sync engine, 1: tcgen05 engine
     int64_t Xp_total = 0, Zp_total = 0;           // prepared-operand arena sizes (elements)
     std::vector<PrepBlock> prepX, prepZ;          // X blocks, and c*op(Z) copies
+    std::vector<OpBlock> opX, opY, opZ, opT;      // prepared blocks of each arena
 };
 // FP64 plan: two phases, the second sums first-stage products on the fly
 Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,

@@ -14,6 +14,12 @@ struct GGArgs {
     const void* B2;
     void* C2;         // split precision with a split output: lo half of C
     int* err;         // device error word: bit 0 = a bounded wait ran out (tcgen05 engine)
+    // tcgen05 engine: TMA descriptors (128 bytes each) of the prepared A / B blocks and,
+    // per segment, which descriptor its A and B use
+    const void* amaps;
+    const void* bmaps;
+    const int32_t* seg_amap;
+    const int32_t* seg_bmap;
     const GTile* tiles;
     const GSeg* segs;
     const GTerm* terms;
@@ -29,7 +35,7 @@ cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st);
 // split-precision grouped GEMM on pre-split K-contiguous operands;
 // out_split = 1: C/C2 are bf16 hi/lo, 0: C is double
 cudaError_t launch_gg_split(int out_split, const GGArgs& a, cudaStream_t st);
-// tcgen05 engine (umma.cu): same arguments as launch_gg_split, tiles up to 128 x 64
+// tcgen05 engine (umma.cu): persistent, TMA-fed; tiles up to 128 x 64
 cudaError_t umma_init();
 cudaError_t launch_gg_umma(int out_split, const GGArgs& a, cudaStream_t st);
 cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* hi, void* lo, cudaStream_t st);

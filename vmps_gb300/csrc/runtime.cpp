@@ -8,6 +8,7 @@
 // (engine.hpp: ld multiple of 8, 32-element aligned starts, zero padding) and
 // are scaled per block by sqrt(coeff_dot(qout)) so that the SU(2)-weighted
 // inner product of pivot/DmrgPivotVector.h:323 becomes a plain dot product.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -115,6 +116,7 @@ static void check_device_error(vmps_ctx* c) {
 // device copy of one phase's work lists
 struct DevPhase {
     DBuf tiles, segs, terms;
+    DBuf seg_amap, seg_bmap;   // tcgen05 engine: TMA descriptor of each segment's A and B block
     int ntiles = 0;
     const PhasePlan* host = nullptr;
     void upload(const PhasePlan& ph, cudaStream_t st) {
@@ -123,19 +125,76 @@ struct DevPhase {
         upload_vec(tiles, ph.tiles, st);
         upload_vec(segs, ph.segs, st);
         upload_vec(terms, ph.terms, st);
+        if (!ph.seg_amap.empty()) {
+            upload_vec(seg_amap, ph.seg_amap, st);
+            upload_vec(seg_bmap, ph.seg_bmap, st);
+        }
     }
 };
 
+// Split plans keep each bf16 operand as one arena [hi | lo]: the lo half of
+// element e sits at e + lo, with lo = the arena's element count (a multiple of
+// 32, so both halves start on 64-byte boundaries).
 struct DevPlan {
     Plan plan;
     DevPhase p1, p2;
-    DBuf T, T2;                   // FP64: T (double); split: T hi / lo (bf16)
-    DBuf Xh, Xl, Zh, Zl, Yh, Yl;  // split: prepared operands
-    DBuf prepX, prepZ;            // PrepBlock lists
+    DBuf T;                        // FP64: T (double); split: T [hi | lo] (bf16)
+    DBuf X2, Z2, Y2;               // split: prepared operands [hi | lo]
+    DBuf prepX, prepZ;             // PrepBlock lists
+    DBuf mapX, mapY, mapT, mapZ;   // tcgen05 engine: one 128-byte TMA descriptor per operand block
     int nprepX = 0, nprepZ = 0;
-    int64_t ytotal = 0;           // elements of the Y arena (split per call)
+    int64_t ytotal = 0;            // elements of the Y arena (split per call)
     bool ready = false;
 };
+
+static void* lo_half(const DBuf& b, int64_t total) { return b.as<uint16_t>() + total; }
+
+// ---------------------------------------------------------------------------
+// TMA descriptors of the tcgen05 engine
+// ---------------------------------------------------------------------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !f)
+            throw CudaFail("cuTensorMapEncodeTiled is not available from the driver");
+        return reinterpret_cast<EncodeTiledFn>(f);
+    }();
+    return fn;
+}
+
+// One descriptor per block of a [hi | lo] bf16 arena: a 3-d tensor (K, outer,
+// hi/lo) with K contiguous, rows `ld` elements apart, halves `lo` elements
+// apart.  Boxes are 64 x box_rows x 2 with 128-byte swizzle and zero fill
+// outside the block, which is what the engine's shared-memory stages expect.
+static void build_maps(DBuf& maps, const std::vector<OpBlock>& blocks, const DBuf& arena, int64_t lo, int box_rows,
+                       cudaStream_t st) {
+    if (lo % 8 != 0) throw std::logic_error("split arena size is not a multiple of 8 elements");
+    std::vector<CUtensorMap> h(std::max<size_t>(1, blocks.size()));
+    std::memset(h.data(), 0, h.size() * sizeof(CUtensorMap));
+    EncodeTiledFn enc = encode_tiled();
+    for (size_t i = 0; i < blocks.size(); ++i) {
+        const OpBlock& b = blocks[i];
+        if (b.off % 32 != 0 || b.ld % 8 != 0) throw std::logic_error("operand block is not 16-byte aligned");
+        const cuuint64_t dims[3] = {(cuuint64_t)std::max(1, b.K), (cuuint64_t)std::max(1, b.outer), 2};
+        const cuuint64_t strides[2] = {(cuuint64_t)b.ld * 2, (cuuint64_t)lo * 2};
+        const cuuint32_t box[3] = {64, (cuuint32_t)box_rows, 2};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        void* base = arena.as<uint16_t>() + b.off;
+        CUresult res = enc(&h[i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (res != CUDA_SUCCESS)
+            throw CudaFail("cuTensorMapEncodeTiled failed (" + std::to_string((int)res) + ") for a block of " +
+                           std::to_string(b.outer) + " x " + std::to_string(b.K) + ", ld " + std::to_string(b.ld));
+    }
+    upload_vec(maps, h, st);
+}
 
 // compact <-> padded copy descriptors of one block table
 static std::vector<PackBlock> pack_blocks(const BlockTable& t, const DevLayout& d, const std::vector<double>* scale) {
@@ -154,6 +213,36 @@ struct Operands {
     int* err = nullptr;
 };
 
+// Invariants the tcgen05 engine relies on, checked on the host once per plan:
+// every segment names an A and a B descriptor that exist and share its K,
+// every tile lies inside the A rows / B columns of each of its segments and
+// fits the 128 x 64 accumulator.
+static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B) {
+    if (ph.seg_amap.size() != ph.segs.size() || ph.seg_bmap.size() != ph.segs.size())
+        throw std::logic_error("tcgen05 plan: segment descriptor maps missing");
+    for (size_t s = 0; s < ph.segs.size(); ++s) {
+        const int32_t a = ph.seg_amap[s], b = ph.seg_bmap[s];
+        if (a < 0 || a >= (int32_t)A.size() || b < 0 || b >= (int32_t)B.size())
+            throw std::logic_error("tcgen05 plan: descriptor index out of range");
+        if (A[a].K != ph.segs[s].K || B[b].K != ph.segs[s].K || ph.segs[s].K <= 0)
+            throw std::logic_error("tcgen05 plan: contraction length mismatch");
+    }
+    for (const GTile& t : ph.tiles) {
+        if (t.tm <= 0 || t.tn <= 0 || t.tm > kUmmaTileM || t.tn > kUmmaTileN || t.row0 < 0 || t.col0 < 0)
+            throw std::logic_error("tcgen05 plan: tile shape out of range");
+        if (t.seg_begin < 0 || t.seg_end < t.seg_begin || t.seg_end > (int32_t)ph.segs.size())
+            throw std::logic_error("tcgen05 plan: tile segment range out of range");
+        for (int32_t s = t.seg_begin; s < t.seg_end; ++s)
+            if (t.row0 + t.tm > A[ph.seg_amap[s]].outer || t.col0 + t.tn > B[ph.seg_bmap[s]].outer)
+                throw std::logic_error("tcgen05 plan: tile outside its operand blocks");
+    }
+}
+
+static void validate_tma_plan(const Plan& p) {
+    validate_tma_plan(p.p1, p.opX, p.opY);
+    validate_tma_plan(p.p2, p.opT, p.opZ);
+}
+
 // device buffers and work lists of a freshly made plan
 static void plan_to_device(DevPlan& dp, int64_t ytotal, cudaStream_t st) {
     dp.p1.upload(dp.plan.p1, st);
@@ -162,26 +251,28 @@ static void plan_to_device(DevPlan& dp, int64_t ytotal, cudaStream_t st) {
         dp.T.alloc((size_t)dp.plan.T.total * 8, st, true);
         return;
     }
-    dp.T.alloc((size_t)dp.plan.T.total * 2, st, true);
-    dp.T2.alloc((size_t)dp.plan.T.total * 2, st, true);
-    dp.Xh.alloc((size_t)dp.plan.Xp_total * 2, st, true);
-    dp.Xl.alloc((size_t)dp.plan.Xp_total * 2, st, true);
-    dp.Zh.alloc((size_t)dp.plan.Zp_total * 2, st, true);
-    dp.Zl.alloc((size_t)dp.plan.Zp_total * 2, st, true);
+    dp.T.alloc((size_t)dp.plan.T.total * 4, st, true);
+    dp.X2.alloc((size_t)dp.plan.Xp_total * 4, st, true);
+    dp.Z2.alloc((size_t)dp.plan.Zp_total * 4, st, true);
     dp.ytotal = ytotal;
-    dp.Yh.alloc((size_t)std::max<int64_t>(ytotal, 32) * 2, st, true);
-    dp.Yl.alloc((size_t)std::max<int64_t>(ytotal, 32) * 2, st, true);
+    dp.Y2.alloc((size_t)std::max<int64_t>(ytotal, 32) * 4, st, true);
     upload_vec(dp.prepX, dp.plan.prepX, st);
     upload_vec(dp.prepZ, dp.plan.prepZ, st);
     dp.nprepX = (int)dp.plan.prepX.size();
     dp.nprepZ = (int)dp.plan.prepZ.size();
+    if (dp.plan.split_kernel) {
+        build_maps(dp.mapX, dp.plan.opX, dp.X2, dp.plan.Xp_total, kUmmaTileM, st);
+        build_maps(dp.mapY, dp.plan.opY, dp.Y2, dp.ytotal, kUmmaTileN, st);
+        build_maps(dp.mapT, dp.plan.opT, dp.T, dp.plan.T.total, kUmmaTileM, st);
+        build_maps(dp.mapZ, dp.plan.opZ, dp.Z2, dp.plan.Zp_total, kUmmaTileN, st);
+    }
 }
 
 // split plans: scaled bf16 hi/lo copies of the X and Z operands
 static void split_prepare(DevPlan& dp, const double* X, const double* Z, cudaStream_t st) {
     if (!dp.plan.split) return;
-    CK(launch_prep(dp.prepX.as<PrepBlock>(), dp.nprepX, X, dp.Xh.p, dp.Xl.p, st));
-    CK(launch_prep(dp.prepZ.as<PrepBlock>(), dp.nprepZ, Z, dp.Zh.p, dp.Zl.p, st));
+    CK(launch_prep(dp.prepX.as<PrepBlock>(), dp.nprepX, X, dp.X2.p, lo_half(dp.X2, dp.plan.Xp_total), st));
+    CK(launch_prep(dp.prepZ.as<PrepBlock>(), dp.nprepZ, Z, dp.Z2.p, lo_half(dp.Z2, dp.plan.Zp_total), st));
 }
 
 static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream_t st) {
@@ -209,14 +300,18 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
         a.B = slot(h.slotB);
         a.C = const_cast<void*>(slot(h.slotC));
     } else if (ph == 1) {
-        a.A = dp.Xh.p; a.A2 = dp.Xl.p;
-        a.B = dp.Yh.p; a.B2 = dp.Yl.p;
-        a.C = dp.T.p; a.C2 = dp.T2.p;
+        a.A = dp.X2.p; a.A2 = lo_half(dp.X2, dp.plan.Xp_total);
+        a.B = dp.Y2.p; a.B2 = lo_half(dp.Y2, dp.ytotal);
+        a.C = dp.T.p; a.C2 = lo_half(dp.T, dp.plan.T.total);
+        a.amaps = dp.mapX.p; a.bmaps = dp.mapY.p;
     } else {
-        a.A = dp.T.p; a.A2 = dp.T2.p;
-        a.B = dp.Zh.p; a.B2 = dp.Zl.p;
+        a.A = dp.T.p; a.A2 = lo_half(dp.T, dp.plan.T.total);
+        a.B = dp.Z2.p; a.B2 = lo_half(dp.Z2, dp.plan.Zp_total);
         a.C = ops.O;
+        a.amaps = dp.mapT.p; a.bmaps = dp.mapZ.p;
     }
+    a.seg_amap = d.seg_amap.as<int32_t>();
+    a.seg_bmap = d.seg_bmap.as<int32_t>();
     // every operand of a non-empty phase must be a live device buffer
     if (d.ntiles > 0 && (!a.C || !a.tiles || !a.segs || !a.terms || (!h.segs.empty() && (!a.A || !a.B))))
         throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
@@ -227,7 +322,7 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
 
 // one application of a planned contraction: (split plans) split Y, phase 1, phase 2
 static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
-    if (dp.plan.split) CK(launch_split(ops.Y, dp.Yh.p, dp.Yl.p, dp.ytotal, st));
+    if (dp.plan.split) CK(launch_split(ops.Y, dp.Y2.p, lo_half(dp.Y2, dp.ytotal), dp.ytotal, st));
     run_phase(dp, 1, ops, st);
     run_phase(dp, 2, ops, st);
 }
@@ -311,6 +406,7 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
         dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, eng ? kUmmaTileM : kTileMax,
                                   eng ? kUmmaTileN : kTileMax);
         dp.plan.split_kernel = eng;
+        if (eng) validate_tma_plan(dp.plan);
     }
     if (p->ctx->device < 0) { dp.ready = true; return dp; }   // host-only: plan without device copies
     plan_to_device(dp, p->Vd.total, p->st());
@@ -890,6 +986,7 @@ static DevPlan& env_plan(vmps_env* e, int prec) {
         dp.plan = make_split_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L, eng ? kUmmaTileM : kTileMax,
                                   eng ? kUmmaTileN : kTileMax);
         dp.plan.split_kernel = eng;
+        if (eng) validate_tma_plan(dp.plan);
     }
     if (e->ctx->device < 0) { dp.ready = true; return dp; }
     plan_to_device(dp, e->Ed.total, e->st());

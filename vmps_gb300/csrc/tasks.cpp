@@ -910,6 +910,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
 
     // prepared X blocks: op(X) (m x k) stored row-major, row stride pad8(k)
     std::vector<int64_t> xp_off(X.rows.size(), -1), xp_ld(X.rows.size(), 0);
+    std::vector<int32_t> xp_idx(X.rows.size(), -1);
     int64_t cur = 0;
     for (const Chain& c : ch) {
         if (xp_off[c.x] >= 0) continue;
@@ -923,6 +924,8 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         pb.trans = transX ? 0 : 1;   // op(X) = X: rows of X become rows; op(X) = X^T: columns of X
         pb.scale = 1.0;
         P.prepX.push_back(pb);
+        xp_idx[c.x] = (int32_t)P.opX.size();
+        P.opX.push_back(OpBlock{cur, (int32_t)m, (int32_t)k, (int32_t)ld, 0});
         cur = pad_off(cur + ld * m);
     }
     P.Xp_total = std::max<int64_t>(cur, 32);
@@ -952,6 +955,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         pb.trans = transZ ? 1 : 0;   // op(Z) = Z: columns stay columns; op(Z) = Z^T: rows of Z become columns
         pb.scale = ch[i].c;
         P.prepZ.push_back(pb);
+        P.opZ.push_back(OpBlock{cur, (int32_t)p, (int32_t)n, (int32_t)ld, 0});
         chain_zp[i] = id;
         cur = pad_off(cur + ld * p);
     }
@@ -972,11 +976,16 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         ipairs.push_back({ch[i].x, ch[i].y});
         const int64_t m = xm(ch[i].x), n = Y.cols[ch[i].y], ld = pad_ld(n);
         T.off.push_back(cur); T.rows.push_back(m); T.cols.push_back(n); T.ld.push_back(ld);
+        P.opT.push_back(OpBlock{cur, (int32_t)m, (int32_t)n, (int32_t)ld, 0});
         cur = pad_off(cur + ld * m);
         chain_t[i] = id;
     }
     T.total = std::max<int64_t>(cur, 32);
     P.n_intermediates = (int64_t)ipairs.size();
+
+    // the vector arena Y is split in place: its blocks are K (= rows) contiguous already
+    for (size_t y = 0; y < Y.rows.size(); ++y)
+        P.opY.push_back(OpBlock{Y.off[y], (int32_t)Y.cols[y], (int32_t)Y.rows[y], (int32_t)Y.ld[y], 0});
 
     // phase 1: T_j = Xp[x] * Yp[y]   (A rows = m, B columns = n, K = k), stored transposed
     PhasePlan& p1 = P.p1;
@@ -994,6 +1003,8 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         s.K = (int32_t)xk(x);
         const int32_t sb = (int32_t)p1.segs.size();
         p1.segs.push_back(s);
+        p1.seg_amap.push_back(xp_idx[x]);
+        p1.seg_bmap.push_back((int32_t)y);
         p1.flops += 2.0 * T.rows[j] * T.cols[j] * s.K;
         add_tiles(p1, T.off[j], T.ld[j], T.rows[j], T.cols[j], sb, sb + 1, tile_m, tile_n);
     }
@@ -1030,6 +1041,8 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
             s.K = (int32_t)T.cols[t];
             kk += s.K;
             p2.segs.push_back(s);
+            p2.seg_amap.push_back((int32_t)t);
+            p2.seg_bmap.push_back((int32_t)zq);
             ++i;
         }
         p2.flops += 2.0 * O.rows[o] * O.cols[o] * kk;

@@ -1,25 +1,17 @@
 // tcgen05 (UMMA) engine of the split-precision grouped GEMM (sm_103a).
 //
-// Same work lists and operand layout as gg_split_kernel in kernels.cu: every
-// operand is pre-split into bf16 hi and lo arrays, stored K-contiguous (rows of
-// A, columns of B) with rows padded to 8 elements and zero padding.  One CTA
-// owns one output tile of up to 128 x 64 and walks its segments' K ranges in
-// steps of 64:
+// Same work lists as gg_split_kernel in kernels.cu.  Operands are pre-split
+// into bf16 hi and lo halves of one arena ([hi | lo]), stored K-contiguous
+// (rows of A, columns of B, row stride a multiple of 8 elements).  Every
+// prepared block has a TMA descriptor (K, rows, hi/lo) built on the host, so a
+// K step of one operand is one 3-d box copy that lands both halves in the
+// 128-byte-swizzled K-major layout the UMMA shared-memory descriptors read,
+// with zeros outside the block.  Tiles are up to 128 x 64 (UMMA M = 128,
+// N = 64, K = 16 per instruction), accumulated in FP32 in tensor memory.
 //
-//   * all 128 threads stage the step's four 64-wide slices (A hi/lo: 128 rows,
-//     B hi/lo: 64 rows) with cp.async into a 4-deep ring of shared-memory
-//     stages, in the 128-byte-swizzled K-major layout the UMMA descriptors
-//     describe (16-byte chunk c of row r stored at chunk c ^ (r % 8));
-//   * one thread issues, per 16-wide K slice, tcgen05.mma lo*hi, hi*lo, hi*hi
-//     (kind::f16, bf16 inputs, FP32 accumulator of 128 lanes x 64 columns in
-//     tensor memory) and tcgen05.commit to the stage's mbarrier, which tells
-//     the producers when the stage may be refilled;
-//   * the epilogue reads the accumulator with tcgen05.ld (each warp its 32
-//     lanes) and writes FP64, or bf16 hi/lo for the next phase.
-//
-// Every mbarrier wait is bounded by a clock budget; a wait that runs out sets
-// the error word, the kernel skips the remaining MMAs, releases its tensor
-// memory and returns.
+// Every barrier wait is bounded by a clock budget; when one runs out the
+// kernel records it in the error word, the roles leave their loops, the tensor
+// memory is released and the kernel returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -28,17 +20,19 @@
 
 namespace vmps {
 namespace um {
-constexpr int BM = 128, BN = 64, BK = 64, NT = 128, STAGES = 4;
+constexpr int BM = 128, BN = 64, BK = 64, STAGES = 4;
+constexpr int NT = 192;                                    // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int A_BYTES = BM * BK * 2;                       // one of A hi / A lo: 16 KB
 constexpr int B_BYTES = BN * BK * 2;                       // one of B hi / B lo: 8 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;     // 48 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
-constexpr uint32_t TMEM_COLS = 64;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr uint32_t ACC_COLS = 64;                          // one FP32 accumulator: 128 lanes x 64 columns
+constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two, so an epilogue overlaps the next tile
 // kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1),
 // both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
-constexpr long long WAIT_BUDGET = 4000000000LL;           // clock cycles (~2 s) per mbarrier wait
+constexpr long long WAIT_BUDGET = 4000000000LL;           // clock cycles (~2 s) per barrier wait
 }  // namespace um
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -53,16 +47,6 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     d |= (uint64_t)2 << 61;                    // 128-byte swizzle
     return d;
 }
-// byte offset of (row, 16-byte chunk) inside a swizzled K-major tile
-__device__ __forceinline__ uint32_t swz(int r, int c) {
-    return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
-}
-
-__device__ __forceinline__ void cp16(uint32_t dst, const void* src, int bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes));
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count));
@@ -76,12 +60,42 @@ __device__ __forceinline__ uint32_t mbar_test(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok;
 }
-// bounded wait: false when the clock budget ran out
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// wait for the phase of the given parity, bounded by the clock budget only
+// (used to drain copies and MMAs in flight before the CTA exits)
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity, volatile int* fail) {
     const long long t0 = clock64();
     while (!mbar_test(bar, parity))
-        if (clock64() - t0 > um::WAIT_BUDGET) return false;
+        if (clock64() - t0 > um::WAIT_BUDGET) { *fail = 1; return; }
+}
+// bounded wait on the phase of the given parity; false when the clock budget ran
+// out or another role has already given up (the failure word is then set)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* fail) {
+    const long long t0 = clock64();
+    while (!mbar_test(bar, parity)) {
+        if (*fail) return false;
+        if (clock64() - t0 > um::WAIT_BUDGET) { *fail = 1; return false; }
+    }
     return true;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+// 3-d tile copy (K, rows, hi/lo) global -> shared, completion counted on an mbarrier
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const void* tmap, int x, int y, int z, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(dst),
+        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+// descriptors are written to global memory by the host, and a later plan may reuse
+// an address: acquire the current contents for the tensor-map proxy before use
+__device__ __forceinline__ void tmap_acquire(const void* tmap) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(tmap) : "memory");
 }
 
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
@@ -110,33 +124,45 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ int tile_steps(const GGArgs& g, const GTile& t) {
+    int n = 0;
+    for (int s = t.seg_begin; s < t.seg_end; ++s) n += (g.segs[s].K + um::BK - 1) / um::BK;
+    return n;
+}
+
+// Persistent, warp-specialised grouped GEMM on pre-split operands.
+//   warp 0 (one lane): TMA loads of each 64-wide K step -- one 3-d box (K, rows,
+//     hi/lo) per operand, 128-byte swizzle, zero fill outside the block -- into
+//     a 4-deep ring of stages ("full" barriers carry the byte count);
+//   warp 1 (one lane): per K step 4 x (lo*hi, hi*lo, hi*hi) tcgen05.mma into one
+//     of two TMEM accumulators, commit to the stage's "empty" barrier, and at
+//     the end of a tile to the accumulator's "full" barrier;
+//   warps 2-5: epilogue -- tcgen05.ld of their 32 accumulator lanes, store,
+//     release the accumulator -- overlapping the next tile's main loop.
+// CTAs take tiles b, b + gridDim.x, ... (tiles are sorted by descending work).
 template <int OUT_SPLIT>
 __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
     using namespace um;
     extern __shared__ __align__(1024) unsigned char smraw[];
-    // 1024-byte aligned stage ring (the swizzle pattern is anchored to 1024-byte boundaries)
     const uint32_t raw = su32(smraw);
     const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
-    unsigned char* ring = smraw + pad;
-    const uint32_t ring_s = raw + pad;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(ring + STAGES * STAGE_BYTES);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + STAGES);
-    __shared__ int s_fail;
-
-    const GTile tile = g.tiles[blockIdx.x];
+    const uint32_t ring = raw + pad;   // 1024-aligned: the swizzle pattern is anchored to 1024-byte boundaries
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smraw + pad + STAGES * STAGE_BYTES);
+    // bars[0..S) full, [S..2S) empty, [2S..2S+2) accumulator full, [2S+2..2S+4) accumulator empty,
+    // [2S+4] drain of the MMAs issued
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+    __shared__ volatile int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int mrem = tile.tm, nrem = tile.tn;
-    const __nv_bfloat16* __restrict__ Ah = (const __nv_bfloat16*)g.A;
-    const __nv_bfloat16* __restrict__ Al = (const __nv_bfloat16*)g.A2;
-    const __nv_bfloat16* __restrict__ Bh = (const __nv_bfloat16*)g.B;
-    const __nv_bfloat16* __restrict__ Bl = (const __nv_bfloat16*)g.B2;
+    auto bar = [&](int i) { return su32(&bars[i]); };
 
     if (tid == 0) {
         s_fail = 0;
-        for (int s = 0; s < STAGES; ++s) mbar_init(su32(&bars[s]), 1);
+        for (int s = 0; s < STAGES; ++s) { mbar_init(bar(s), 1); mbar_init(bar(STAGES + s), 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(bar(2 * STAGES + b), 1); mbar_init(bar(2 * STAGES + 2 + b), 4); }
+        mbar_init(bar(2 * STAGES + 4), 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tmem_slot)),
                      "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
@@ -144,148 +170,164 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    const int G = gridDim.x;
 
-    int nsteps = 0;
-    for (int s = tile.seg_begin; s < tile.seg_end; ++s) nsteps += (g.segs[s].K + BK - 1) / BK;
-
-    // producer cursor (segment, k offset)
-    int lseg = tile.seg_begin, lk0 = 0;
-    GSeg lsg{};
-    int64_t laoff = 0;
-    if (lseg < tile.seg_end) { lsg = g.segs[lseg]; laoff = g.terms[lsg.term_begin].off; }
-    // 3072 16-byte chunks per stage: A hi, A lo (128 rows x 8), B hi, B lo (64 rows x 8)
-    auto load_step = [&](int stage) {
-        const uint32_t sb = ring_s + stage * STAGE_BYTES;
-#pragma unroll 4
-        for (int i = 0; i < 24; ++i) {
-            const int cid = tid + NT * i;
-            int part, r, c;
-            if (cid < 2048) { part = cid >> 10; r = (cid >> 3) & 127; c = cid & 7; }
-            else { const int c2 = cid - 2048; part = 2 + (c2 >> 9); r = (c2 >> 3) & 63; c = c2 & 7; }
-            const int k = lk0 + c * 8;
-            const bool isA = part < 2;
-            const bool ok = (isA ? r < mrem : r < nrem) && k < lsg.K;
-            const __nv_bfloat16* src;
-            uint32_t dst;
-            if (isA) {
-                src = (part == 0 ? Ah : Al) + laoff + (int64_t)(tile.row0 + (ok ? r : 0)) * lsg.lda + (ok ? k : 0);
-                dst = sb + part * A_BYTES + swz(r, c);
-            } else {
-                src = (part == 2 ? Bh : Bl) + lsg.b_off + (int64_t)(tile.col0 + (ok ? r : 0)) * lsg.ldb + (ok ? k : 0);
-                dst = sb + 2 * A_BYTES + (part - 2) * B_BYTES + swz(r, c);
+    if (warp == 0 && lane == 0) {
+        // ---------------- TMA producer
+        const char* amaps = (const char*)g.amaps;
+        const char* bmaps = (const char*)g.bmaps;
+        int it = 0;
+        const void* last_a = nullptr;
+        const void* last_b = nullptr;
+        for (int t = blockIdx.x; t < g.ntiles && !s_fail; t += G) {
+            const GTile tile = g.tiles[t];
+            for (int s = tile.seg_begin; s < tile.seg_end && !s_fail; ++s) {
+                const int K = g.segs[s].K;
+                const void* am = amaps + (size_t)g.seg_amap[s] * 128;
+                const void* bm = bmaps + (size_t)g.seg_bmap[s] * 128;
+                if (am != last_a) { tmap_acquire(am); last_a = am; }
+                if (bm != last_b) { tmap_acquire(bm); last_b = bm; }
+                for (int k0 = 0; k0 < K; k0 += BK, ++it) {
+                    const int st = it % STAGES, use = it / STAGES;
+                    if (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), &s_fail)) break;
+                    const uint32_t sb = ring + st * STAGE_BYTES;
+                    mbar_expect_tx(bar(st), STAGE_BYTES);
+                    tma_load_3d(sb, am, k0, tile.row0, 0, bar(st));
+                    tma_load_3d(sb + 2 * A_BYTES, bm, k0, tile.col0, 0, bar(st));
+                }
             }
-            cp16(dst, src, ok ? 16 : 0);
         }
-        lk0 += BK;
-        if (lk0 >= lsg.K) {
-            lk0 = 0;
-            if (++lseg < tile.seg_end) { lsg = g.segs[lseg]; laoff = g.terms[lsg.term_begin].off; }
-        }
-    };
-
-#pragma unroll 1
-    for (int s = 0; s < STAGES - 1; ++s) {
-        if (s < nsteps) load_step(s);
-        cp_commit();
-    }
-    // Per step: (A) the step's slices have landed in every thread -> thread 0
-    // queues the step's MMAs and commits them to the stage barrier, then waits
-    // (bounded) for the previous step's MMAs, whose stage is refilled next ->
-    // (B) everyone refills that stage.  The wait comes after the new MMAs are
-    // queued, so the tensor pipe never drains between steps.
-#pragma unroll 1
-    for (int step = 0; step < nsteps; ++step) {
-        const int st = step % STAGES;
-        const int nxt = step + STAGES - 1;
-        cp_wait<STAGES - 2>();
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");   // cp.async data -> async proxy
-        __syncthreads();                                                  // (A)
-        if (tid == 0) {
+        // copies still in flight land before the CTA exits (a no-op when the MMA warp consumed them)
+        for (int i = it - 1; i >= 0 && i >= it - STAGES; --i)
+            mbar_drain(bar(i % STAGES), (uint32_t)((i / STAGES) & 1), &s_fail);
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer
+        int it = 0, lt = 0;
+        for (int t = blockIdx.x; t < g.ntiles && !s_fail; t += G, ++lt) {
+            const GTile tile = g.tiles[t];
+            const int buf = lt & 1, buse = lt >> 1;
+            if (buse >= 1 && !mbar_wait(bar(2 * STAGES + 2 + buf), (uint32_t)((buse - 1) & 1), &s_fail)) break;
             tc_fence_after();
-            const uint32_t sb = ring_s + st * STAGE_BYTES;
-            const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + A_BYTES);
-            const uint64_t bh = sw128_desc(sb + 2 * A_BYTES), bl = sw128_desc(sb + 2 * A_BYTES + B_BYTES);
+            const uint32_t dacc = tmem + (uint32_t)buf * ACC_COLS;
+            bool first = true;
+            const int nsteps = tile_steps(g, tile);
+            for (int k = 0; k < nsteps; ++k, ++it) {
+                const int st = it % STAGES, use = it / STAGES;
+                if (!mbar_wait(bar(st), (uint32_t)(use & 1), &s_fail)) break;
+                tc_fence_after();
+                const uint32_t sb = ring + st * STAGE_BYTES;
+                const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + A_BYTES);
+                const uint64_t bh = sw128_desc(sb + 2 * A_BYTES), bl = sw128_desc(sb + 2 * A_BYTES + B_BYTES);
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
-                const uint64_t adv = (uint64_t)(kk * 32) >> 4;   // 16 bf16 = 32 bytes along K
-                umma_bf16(tmem, al + adv, bh + adv, (step | kk) != 0);
-                umma_bf16(tmem, ah + adv, bl + adv, 1);
-                umma_bf16(tmem, ah + adv, bh + adv, 1);
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint64_t adv = (uint64_t)(kk * 32) >> 4;   // 16 bf16 = 32 bytes along K
+                    umma_bf16(dacc, al + adv, bh + adv, first ? 0u : 1u);
+                    first = false;
+                    umma_bf16(dacc, ah + adv, bl + adv, 1);
+                    umma_bf16(dacc, ah + adv, bh + adv, 1);
+                }
+                umma_commit(bar(STAGES + st));
             }
-            umma_commit(su32(&bars[st]));
-            if (step >= 1 && nxt < nsteps) {
-                const int ps = (step - 1) % STAGES;
-                if (!mbar_wait(su32(&bars[ps]), (uint32_t)(((step - 1) / STAGES) & 1))) s_fail = 1;
-            }
+            umma_commit(bar(2 * STAGES + buf));
         }
-        __syncthreads();                                                  // (B)
-        if (s_fail) break;
-        if (nxt < nsteps) load_step(nxt % STAGES);
-        cp_commit();
-    }
-    if (tid == 0 && nsteps > 0 && !s_fail) {
-        const int ls = (nsteps - 1) % STAGES;
-        if (!mbar_wait(su32(&bars[ls]), (uint32_t)(((nsteps - 1) / STAGES) & 1))) s_fail = 1;
-    }
-    cp_wait<0>();
-    __syncthreads();
-    tc_fence_after();
-    const bool bad = s_fail != 0;
-    if (bad && tid == 0 && g.err) atomicOr(g.err, 1);
-
-    // epilogue: warp w owns accumulator lanes (rows) 32w .. 32w+31
-    const int r = warp * 32 + lane;
+        umma_commit(bar(2 * STAGES + 4));
+        mbar_drain(bar(2 * STAGES + 4), 0, &s_fail);
+    } else if (warp >= 2) {
+        // ---------------- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
+        const int sp = warp & 3;
+        const int r = sp * 32 + lane;
+        int lt = 0;
+        for (int t = blockIdx.x; t < g.ntiles; t += G, ++lt) {
+            const GTile tile = g.tiles[t];
+            const int buf = lt & 1, buse = lt >> 1;
+            // warp-uniform outcome: the tensor-memory loads below are warp-collective
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(bar(2 * STAGES + buf), (uint32_t)(buse & 1), &s_fail));
+            if (!ok) break;
+            tc_fence_after();
+            const bool any = tile.seg_end > tile.seg_begin;
+            const int mrem = tile.tm, nrem = tile.tn;
+            const int64_t gr = tile.row0 + r;
 #pragma unroll 1
-    for (int j0 = 0; j0 < BN; j0 += 16) {
-        float v[16];
-        if (nsteps > 0 && !bad) {
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)j0, v);
-        } else {
+            for (int j0 = 0; j0 < BN; j0 += 16) {
+                float v[16];
+                if (any) tmem_ld16(tmem + ((uint32_t)(sp * 32) << 16) + (uint32_t)(buf * ACC_COLS + j0), v);
+                else {
 #pragma unroll
-            for (int i = 0; i < 16; ++i) v[i] = 0.f;
-        }
-        if (r >= mrem || j0 >= nrem) continue;
-        const int64_t gr = tile.row0 + r;
-        if (OUT_SPLIT) {
-            __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
-            __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
+                    for (int i = 0; i < 16; ++i) v[i] = 0.f;
+                }
+                if (r >= mrem || j0 >= nrem) continue;
+                const int64_t gc0 = tile.col0 + j0;
+                if (OUT_SPLIT) {
+                    __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
+                    __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
+                    if (g.transC && j0 + 16 <= nrem) {   // 16 consecutive elements of one row: two 16-byte stores
+                        uint32_t h[8], l[8];
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const int c = j0 + i;
-                if (c >= nrem) break;
-                const int64_t gc = tile.col0 + c;
-                const int64_t e = g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc);
-                const __nv_bfloat16 h = __float2bfloat16_rn(v[i]);
-                Ch[tile.c_off + e] = h;
-                Cl[tile.c_off + e] = __float2bfloat16_rn(v[i] - __bfloat162float(h));
+                        for (int i = 0; i < 8; ++i) {
+                            const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * i]), h1 = __float2bfloat16_rn(v[2 * i + 1]);
+                            const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * i] - __bfloat162float(h0));
+                            const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * i + 1] - __bfloat162float(h1));
+                            h[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                            l[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                        }
+                        const int64_t e = tile.c_off + gc0 + gr * tile.ldc;
+                        uint4* ph = reinterpret_cast<uint4*>(Ch + e);
+                        uint4* pl = reinterpret_cast<uint4*>(Cl + e);
+                        ph[0] = make_uint4(h[0], h[1], h[2], h[3]);
+                        ph[1] = make_uint4(h[4], h[5], h[6], h[7]);
+                        pl[0] = make_uint4(l[0], l[1], l[2], l[3]);
+                        pl[1] = make_uint4(l[4], l[5], l[6], l[7]);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) {
+                            if (j0 + i >= nrem) break;
+                            const int64_t gc = gc0 + i;
+                            const int64_t e = tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc));
+                            const __nv_bfloat16 hh = __float2bfloat16_rn(v[i]);
+                            Ch[e] = hh;
+                            Cl[e] = __float2bfloat16_rn(v[i] - __bfloat162float(hh));
+                        }
+                    }
+                } else {
+                    double* C = (double*)g.C;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        if (j0 + i >= nrem) break;
+                        const int64_t gc = gc0 + i;
+                        C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] = (double)v[i];
+                    }
+                }
             }
-        } else {
-            double* C = (double*)g.C;
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const int c = j0 + i;
-                if (c >= nrem) break;
-                const int64_t gc = tile.col0 + c;
-                const int64_t e = g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc);
-                C[tile.c_off + e] = (double)v[i];
-            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
         }
     }
-    tc_fence_before();
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
+    if (s_fail && tid == 0 && g.err) atomicOr(g.err, 1);
+    tc_fence_after();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
+static int g_num_sms = 0;
+
 cudaError_t umma_init() {
-    cudaError_t e = cudaFuncSetAttribute(gg_umma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(gg_umma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(gg_umma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
 }
 
 cudaError_t launch_gg_umma(int out_split, const GGArgs& a, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
-    if (out_split) gg_umma_kernel<1><<<a.ntiles, um::NT, um::SMEM_BYTES, st>>>(a);
-    else gg_umma_kernel<0><<<a.ntiles, um::NT, um::SMEM_BYTES, st>>>(a);
+    if (!a.amaps || !a.bmaps || !a.seg_amap || !a.seg_bmap) return cudaErrorInvalidValue;
+    const int grid = a.ntiles < g_num_sms ? a.ntiles : (g_num_sms > 0 ? g_num_sms : 148);
+    if (out_split) gg_umma_kernel<1><<<grid, um::NT, um::SMEM_BYTES, st>>>(a);
+    else gg_umma_kernel<0><<<grid, um::NT, um::SMEM_BYTES, st>>>(a);
     return cudaGetLastError();
 }
 
