@@ -136,7 +136,13 @@ DevLayout make_dev_layout(const std::vector<int64_t>& rows, const std::vector<in
 struct GTerm { int64_t off; double coef; };
 struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, K, pad; };
 // one output tile: rows [row0, row0+tm) x cols [col0, col0+tn) of a block
-struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, pad; };
+// (tcgen05 engine: step0 / nsteps index its K steps in PhasePlan::steps)
+struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, step0, nsteps; };
+// one K step of the tcgen05 engine: TMA descriptors of A and B, the K offset in
+// the segment and the tile origin; flags bit 0 / bit 1: first use of the A / B
+// descriptor by this CTA (acquire it for the tensor-map proxy)
+struct TStep { int32_t amap, bmap, k0, row0, col0, flags, pad0, pad1; };
+constexpr int kUmmaBK = 64;   // K extent of one tcgen05 engine step
 // at most this many A terms per segment (the kernels stage them in shared memory)
 constexpr int kMaxTerms = 16;
 // tile edges (rows split on multiples of 16, columns on multiples of 8):
@@ -150,6 +156,11 @@ struct PhasePlan {
     std::vector<GTile> tiles;
     // split plans: per segment, the prepared-operand block of A and of B (TMA descriptor index)
     std::vector<int32_t> seg_amap, seg_bmap;
+    // tcgen05 engine schedule (schedule_tma): K steps, and the tiles of CTA b are
+    // tiles[cta_tiles[b] .. cta_tiles[b+1])
+    std::vector<TStep> steps;
+    std::vector<int32_t> cta_tiles;
+    int ncta = 0;
     bool transA = false, transB = false, transC = false;
     int  slotA = 0, slotB = 0, slotC = 0;   // arena ids
     double flops = 0;
@@ -188,6 +199,10 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // split-precision plan: every operand pre-split into K-contiguous bf16 hi/lo
 // copies; the chain coefficient rides on a scaled copy of op(Z); the second
 // phase is a K-concatenation over chains
+// Static schedule of a split phase for the persistent tcgen05 engine on ncta
+// CTAs: K steps of kUmmaBK per segment, tiles assigned longest-first to the
+// least-loaded CTA and stored CTA by CTA.
+void schedule_tma(PhasePlan& ph, int ncta);
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
                      const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n);
 

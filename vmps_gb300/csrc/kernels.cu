@@ -407,11 +407,14 @@ __global__ void pack_kernel(const PackBlock* blocks, int nb, const double* __res
                             int to_padded) {
     for (int b = blockIdx.x; b < nb; b += gridDim.x) {
         const PackBlock pb = blocks[b];
-        const int64_t n = pb.rows * pb.cols;
-        for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
-            const int64_t r = e % pb.rows, c = e / pb.rows;
-            if (to_padded) dst[pb.doff + r + c * pb.ld] = pb.scale * src[pb.coff + e];
-            else dst[pb.coff + e] = src[pb.doff + r + c * pb.ld] / pb.scale;
+        // pieces hold at most a few thousand elements: 32-bit index arithmetic
+        const int rows = (int)pb.rows, n = (int)(pb.rows * pb.cols), ld = (int)pb.ld;
+        const double* s = src + (to_padded ? pb.coff : pb.doff);
+        double* d = dst + (to_padded ? pb.doff : pb.coff);
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int c = e / rows, r = e - c * rows;
+            if (to_padded) d[r + c * ld] = pb.scale * s[e];
+            else d[e] = s[r + c * ld] / pb.scale;
         }
     }
 }

@@ -14,12 +14,13 @@ struct GGArgs {
     const void* B2;
     void* C2;         // split precision with a split output: lo half of C
     int* err;         // device error word: bit 0 = a bounded wait ran out (tcgen05 engine)
-    // tcgen05 engine: TMA descriptors (128 bytes each) of the prepared A / B blocks and,
-    // per segment, which descriptor its A and B use
+    // tcgen05 engine: TMA descriptors (128 bytes each) of the prepared A / B blocks,
+    // the K steps and the per-CTA tile ranges of the schedule (ncta CTAs)
     const void* amaps;
     const void* bmaps;
-    const int32_t* seg_amap;
-    const int32_t* seg_bmap;
+    const TStep* steps;
+    const int32_t* cta_tiles;
+    int ncta;
     const GTile* tiles;
     const GSeg* segs;
     const GTerm* terms;

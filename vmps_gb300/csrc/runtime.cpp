@@ -90,6 +90,8 @@ struct vmps_ctx_s {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     int* err = nullptr;   // device error word written by the tcgen05 engine
+    bool pageable_access = false;   // the device reads pageable host memory in place
+    int num_sms = 152;              // CTAs of the persistent tcgen05 engine (host-only: GB300's count)
 };
 
 // split-precision engine: tcgen05 (default) or mma.sync (VMPS_SPLIT_ENGINE=mma)
@@ -116,8 +118,8 @@ static void check_device_error(vmps_ctx* c) {
 // device copy of one phase's work lists
 struct DevPhase {
     DBuf tiles, segs, terms;
-    DBuf seg_amap, seg_bmap;   // tcgen05 engine: TMA descriptor of each segment's A and B block
-    int ntiles = 0;
+    DBuf steps, cta_tiles;   // tcgen05 engine schedule
+    int ntiles = 0, ncta = 0;
     const PhasePlan* host = nullptr;
     void upload(const PhasePlan& ph, cudaStream_t st) {
         host = &ph;
@@ -125,9 +127,10 @@ struct DevPhase {
         upload_vec(tiles, ph.tiles, st);
         upload_vec(segs, ph.segs, st);
         upload_vec(terms, ph.terms, st);
-        if (!ph.seg_amap.empty()) {
-            upload_vec(seg_amap, ph.seg_amap, st);
-            upload_vec(seg_bmap, ph.seg_bmap, st);
+        ncta = ph.ncta;
+        if (ph.ncta > 0) {
+            upload_vec(steps, ph.steps, st);
+            upload_vec(cta_tiles, ph.cta_tiles, st);
         }
     }
 };
@@ -196,12 +199,70 @@ static void build_maps(DBuf& maps, const std::vector<OpBlock>& blocks, const DBu
     upload_vec(maps, h, st);
 }
 
-// compact <-> padded copy descriptors of one block table
+// compact <-> padded copy descriptors of one block table.  Blocks are cut into
+// pieces of whole columns holding at most kPackPiece elements, so that large
+// blocks spread over many thread blocks of the copy kernel.
+constexpr int64_t kPackPiece = 8192;
 static std::vector<PackBlock> pack_blocks(const BlockTable& t, const DevLayout& d, const std::vector<double>* scale) {
-    std::vector<PackBlock> v(t.n);
-    for (int64_t i = 0; i < t.n; ++i)
-        v[i] = PackBlock{t.off[i], d.off[i], t.rows[i], t.cols[i], d.ld[i], scale ? (*scale)[i] : 1.0};
+    std::vector<PackBlock> v;
+    v.reserve((size_t)t.n);
+    for (int64_t i = 0; i < t.n; ++i) {
+        const int64_t rows = t.rows[i], cols = t.cols[i];
+        if (rows <= 0 || cols <= 0) continue;
+        const int64_t per = std::max<int64_t>(1, kPackPiece / rows);   // columns per piece
+        for (int64_t c0 = 0; c0 < cols; c0 += per) {
+            const int64_t nc = std::min(per, cols - c0);
+            v.push_back(PackBlock{t.off[i] + c0 * rows, d.off[i] + c0 * d.ld[i], rows, nc, d.ld[i],
+                                  scale ? (*scale)[i] : 1.0});
+        }
+    }
     return v;
+}
+
+// A pointer the device may dereference for a caller's host buffer, or null when
+// the buffer must be staged with a copy: page-locked (registered) memory has a
+// device mapping; pageable memory is read in place when the device walks the
+// host page tables (coherent CPU-GPU systems such as Grace with NVLink-C2C).
+static const void* device_view(const vmps_ctx* c, const void* host) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    switch (a.type) {
+        case cudaMemoryTypeHost: return a.devicePointer;
+        case cudaMemoryTypeDevice:
+        case cudaMemoryTypeManaged: return a.device == c->device ? host : nullptr;
+        default: return c->pageable_access ? host : nullptr;
+    }
+}
+
+// compact host vector -> padded device arena (scaled per block), no staging
+// copy when the device can read the host buffer
+static void pack_in(const vmps_ctx* c, const DBuf& pk, int npk, const double* host, int64_t total, DBuf& stage,
+                    double* dst, cudaStream_t st) {
+    if (npk == 0) return;
+    const double* src = static_cast<const double*>(device_view(c, host));
+    if (!src) {
+        stage.alloc((size_t)std::max<int64_t>(total, 1) * 8, st, false);
+        CK(cudaMemcpyAsync(stage.p, host, (size_t)total * 8, cudaMemcpyHostToDevice, st));
+        src = stage.as<double>();
+    }
+    CK(launch_pack(pk.as<PackBlock>(), npk, src, dst, 1, st));
+}
+
+// padded device arena -> compact host vector
+static void pack_out(const vmps_ctx* c, const DBuf& pk, int npk, const double* src, int64_t total, DBuf& stage,
+                     double* host, cudaStream_t st) {
+    if (npk == 0) return;
+    double* dst = static_cast<double*>(const_cast<void*>(device_view(c, host)));
+    if (dst) {
+        CK(launch_pack(pk.as<PackBlock>(), npk, src, dst, 0, st));
+        return;
+    }
+    stage.alloc((size_t)std::max<int64_t>(total, 1) * 8, st, false);
+    CK(launch_pack(pk.as<PackBlock>(), npk, src, stage.as<double>(), 0, st));
+    CK(cudaMemcpyAsync(host, stage.p, (size_t)total * 8, cudaMemcpyDeviceToHost, st));
 }
 
 // FP64 device arenas of one grouped-GEMM problem
@@ -217,7 +278,8 @@ struct Operands {
 // every segment names an A and a B descriptor that exist and share its K,
 // every tile lies inside the A rows / B columns of each of its segments and
 // fits the 128 x 64 accumulator.
-static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B) {
+static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B,
+                              bool split_out) {
     if (ph.seg_amap.size() != ph.segs.size() || ph.seg_bmap.size() != ph.segs.size())
         throw std::logic_error("tcgen05 plan: segment descriptor maps missing");
     for (size_t s = 0; s < ph.segs.size(); ++s) {
@@ -235,12 +297,40 @@ static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A
         for (int32_t s = t.seg_begin; s < t.seg_end; ++s)
             if (t.row0 + t.tm > A[ph.seg_amap[s]].outer || t.col0 + t.tn > B[ph.seg_bmap[s]].outer)
                 throw std::logic_error("tcgen05 plan: tile outside its operand blocks");
+        // a split output is stored in 16-byte row chunks (8 bf16) of a row-major tile
+        if (split_out && (!ph.transC || t.c_off % 8 != 0 || t.ldc % 8 != 0 || t.col0 % 8 != 0 ||
+                          t.ldc < ((t.col0 + t.tn + 7) / 8) * 8))
+            throw std::logic_error("tcgen05 plan: split-output tile not 16-byte aligned");
     }
 }
 
-static void validate_tma_plan(const Plan& p) {
-    validate_tma_plan(p.p1, p.opX, p.opY);
-    validate_tma_plan(p.p2, p.opT, p.opZ);
+// the schedule: CTA tile ranges partition the tiles, every tile's steps lie in
+// the step list, K offsets stay inside their segments' contraction length
+static void validate_tma_schedule(const PhasePlan& ph, const std::vector<OpBlock>& A) {
+    if (ph.tiles.empty()) return;
+    if (ph.ncta <= 0 || (int)ph.cta_tiles.size() != ph.ncta + 1 || ph.cta_tiles.front() != 0 ||
+        ph.cta_tiles.back() != (int32_t)ph.tiles.size())
+        throw std::logic_error("tcgen05 plan: CTA ranges do not cover the tiles");
+    for (int b = 0; b < ph.ncta; ++b)
+        if (ph.cta_tiles[b + 1] < ph.cta_tiles[b]) throw std::logic_error("tcgen05 plan: CTA ranges out of order");
+    int64_t next = 0;
+    for (const GTile& t : ph.tiles) {
+        if (t.step0 != next || t.nsteps < 0) throw std::logic_error("tcgen05 plan: tile steps not contiguous");
+        next += t.nsteps;
+    }
+    if (next != (int64_t)ph.steps.size()) throw std::logic_error("tcgen05 plan: step count mismatch");
+    for (const TStep& s : ph.steps)
+        if (s.amap < 0 || s.amap >= (int32_t)A.size() || s.k0 < 0 || s.k0 >= A[s.amap].K || s.k0 % kUmmaBK != 0)
+            throw std::logic_error("tcgen05 plan: step outside its operand block");
+}
+
+static void schedule_and_validate(Plan& p, int ncta) {
+    validate_tma_plan(p.p1, p.opX, p.opY, true);
+    validate_tma_plan(p.p2, p.opT, p.opZ, false);
+    schedule_tma(p.p1, ncta);
+    schedule_tma(p.p2, ncta);
+    validate_tma_schedule(p.p1, p.opX);
+    validate_tma_schedule(p.p2, p.opT);
 }
 
 // device buffers and work lists of a freshly made plan
@@ -310,8 +400,9 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
         a.C = ops.O;
         a.amaps = dp.mapT.p; a.bmaps = dp.mapZ.p;
     }
-    a.seg_amap = d.seg_amap.as<int32_t>();
-    a.seg_bmap = d.seg_bmap.as<int32_t>();
+    a.steps = d.steps.as<TStep>();
+    a.cta_tiles = d.cta_tiles.as<int32_t>();
+    a.ncta = d.ncta;
     // every operand of a non-empty phase must be a live device buffer
     if (d.ntiles > 0 && (!a.C || !a.tiles || !a.segs || !a.terms || (!h.segs.empty() && (!a.A || !a.B))))
         throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
@@ -406,7 +497,7 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
         dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, eng ? kUmmaTileM : kTileMax,
                                   eng ? kUmmaTileN : kTileMax);
         dp.plan.split_kernel = eng;
-        if (eng) validate_tma_plan(dp.plan);
+        if (eng) schedule_and_validate(dp.plan, p->ctx->num_sms);
     }
     if (p->ctx->device < 0) { dp.ready = true; return dp; }   // host-only: plan without device copies
     plan_to_device(dp, p->Vd.total, p->st());
@@ -432,16 +523,14 @@ static void pivot_hxv_dev(vmps_pivot* p, int prec, const double* vin, double* vo
     run_plan(dp, ops, p->st());
 }
 
-static void upload_blocks_padded(const BlockTable& t, const DevLayout& d, const double* host, DBuf& dst,
+static void upload_blocks_padded(const vmps_ctx* c, const BlockTable& t, const DevLayout& d, const double* host, DBuf& dst,
                                  cudaStream_t st) {
     dst.alloc((size_t)d.total * 8, st, true);
     if (t.n == 0) return;
     DBuf tmp, pk;
-    tmp.alloc((size_t)std::max<int64_t>(t.total, 1) * 8, st, false);
-    CK(cudaMemcpyAsync(tmp.p, host, (size_t)t.total * 8, cudaMemcpyHostToDevice, st));
     auto pb = pack_blocks(t, d, nullptr);
     upload_vec(pk, pb, st);
-    CK(launch_pack(pk.as<PackBlock>(), (int)t.n, tmp.as<double>(), dst.as<double>(), 1, st));
+    pack_in(c, pk, (int)pb.size(), host, t.total, tmp, dst.as<double>(), st);
     CK(cudaStreamSynchronize(st));   // tmp and pk are released on return
 }
 
@@ -482,8 +571,8 @@ static void pivot_finish(vmps_pivot* p, const double* Ldata, const double* Rdata
     }
     if (p->ctx->device < 0) return;
     CK(cudaSetDevice(p->ctx->device));
-    upload_blocks_padded(p->Lt, p->Ld, Ldata, p->dL, p->st());
-    upload_blocks_padded(p->Rt, p->Rd, Rdata, p->dR, p->st());
+    upload_blocks_padded(p->ctx, p->Lt, p->Ld, Ldata, p->dL, p->st());
+    upload_blocks_padded(p->ctx, p->Rt, p->Rd, Rdata, p->dR, p->st());
     auto pb = pack_blocks(p->Vt, p->Vd, &p->vscale);
     p->npack = (int)pb.size();
     upload_vec(p->dPack, pb, p->st());
@@ -521,6 +610,14 @@ int vmps_ctx_create(int device, vmps_ctx** out) {
     CK(cudaEventCreate(&c->ev2));
     CK(cudaMalloc((void**)&c->err, 64));
     CK(cudaMemset(c->err, 0, 64));
+    int pma = 0, pmt = 0;
+    if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pmt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) {
+        (void)cudaGetLastError();
+        pma = pmt = 0;
+    }
+    c->pageable_access = pma && pmt;
+    CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
     *out = c;
     API_END
 }
@@ -611,11 +708,9 @@ int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int prec) {
     cudaStream_t st = p->st();
     ensure_staging(p);
     ensure_io(p);
-    CK(cudaMemcpyAsync(p->stage_in.p, vin, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
-    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), p->vin.as<double>(), 1, st));
+    pack_in(p->ctx, p->dPack, p->npack, vin, p->Vt.total, p->stage_in, p->vin.as<double>(), st);
     pivot_hxv_dev(p, prec, p->vin.as<double>(), p->vout.as<double>());
-    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->vout.as<double>(), p->stage_out.as<double>(), 0, st));
-    CK(cudaMemcpyAsync(vout, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
+    pack_out(p->ctx, p->dPack, p->npack, p->vout.as<double>(), p->Vt.total, p->stage_out, vout, st);
     CK(cudaStreamSynchronize(st));
     check_device_error(p->ctx);
     API_END
@@ -643,8 +738,7 @@ int vmps_dvec_upload(vmps_dvec* v, const double* host) {
     vmps_pivot* p = v->p;
     cudaStream_t st = p->st();
     ensure_staging(p);
-    CK(cudaMemcpyAsync(p->stage_in.p, host, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
-    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), v->d.as<double>(), 1, st));
+    pack_in(p->ctx, p->dPack, p->npack, host, p->Vt.total, p->stage_in, v->d.as<double>(), st);
     CK(cudaMemsetAsync(p->flag.p, 0, 4, st));
     CK(launch_finite(v->d.as<double>(), v->n, p->flag.as<int>(), st));
     int bad = 0;
@@ -659,8 +753,7 @@ int vmps_dvec_download(const vmps_dvec* v, double* host) {
     vmps_pivot* p = v->p;
     cudaStream_t st = p->st();
     ensure_staging(p);
-    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, v->d.as<double>(), p->stage_out.as<double>(), 0, st));
-    CK(cudaMemcpyAsync(host, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
+    pack_out(p->ctx, p->dPack, p->npack, v->d.as<double>(), p->Vt.total, p->stage_out, host, st);
     CK(cudaStreamSynchronize(st));
     API_END
 }
@@ -922,8 +1015,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     kr.coef.alloc((size_t)(kr.kmax + 2) * 8, st, true);
     // start vector
     ensure_staging(p);
-    CK(cudaMemcpyAsync(p->stage_in.p, v, (size_t)p->Vt.total * 8, cudaMemcpyHostToDevice, st));
-    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, p->stage_in.as<double>(), kr.K(0), 1, st));
+    pack_in(p->ctx, p->dPack, p->npack, v, p->Vt.total, p->stage_in, kr.K(0), st);
     double n0 = std::sqrt(dev_dot(p, kr.K(0), kr.K(0), kr.n));
     if (!(n0 > 0) || !std::isfinite(n0)) return set_err(VMPS_E_NONFINITE, "start vector is zero or not finite");
     CK(launch_scale(1.0 / n0, kr.K(0), kr.n, st));
@@ -947,8 +1039,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     s.hxv_fp64++;
     CK(launch_axpy(-e, x, kr.w.as<double>(), kr.n, st));
     s.residual = std::sqrt(dev_dot(p, kr.w.as<double>(), kr.w.as<double>(), kr.n));
-    CK(launch_pack(p->dPack.as<PackBlock>(), p->npack, x, p->stage_out.as<double>(), 0, st));
-    CK(cudaMemcpyAsync(v, p->stage_out.p, (size_t)p->Vt.total * 8, cudaMemcpyDeviceToHost, st));
+    pack_out(p->ctx, p->dPack, p->npack, x, p->Vt.total, p->stage_out, v, st);
     CK(cudaStreamSynchronize(st));
     check_device_error(p->ctx);
     *energy = e;
@@ -969,6 +1060,7 @@ struct vmps_env_s {
     ChainSet cs;
     DevPlan plans[2];
     DBuf dE, dB, dK, dN, stage, pkN;
+    int npkN = 0;
     cudaStream_t st() const { return ctx->stream; }
 };
 
@@ -986,7 +1078,7 @@ static DevPlan& env_plan(vmps_env* e, int prec) {
         dp.plan = make_split_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L, eng ? kUmmaTileM : kTileMax,
                                   eng ? kUmmaTileN : kTileMax);
         dp.plan.split_kernel = eng;
-        if (eng) validate_tma_plan(dp.plan);
+        if (eng) schedule_and_validate(dp.plan, e->ctx->num_sms);
     }
     if (e->ctx->device < 0) { dp.ready = true; return dp; }
     plan_to_device(dp, e->Ed.total, e->st());
@@ -1082,9 +1174,9 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra, const doub
     CK(cudaSetDevice(e->ctx->device));
     cudaStream_t st = e->st();
     DevPlan& dp = env_plan(e, prec);
-    upload_blocks_padded(e->Et, e->Ed, Eold, e->dE, st);
-    upload_blocks_padded(e->Bt, e->Bd, Abra, e->dB, st);
-    upload_blocks_padded(e->Kt, e->Kd, Aket, e->dK, st);
+    upload_blocks_padded(e->ctx, e->Et, e->Ed, Eold, e->dE, st);
+    upload_blocks_padded(e->ctx, e->Bt, e->Bd, Abra, e->dB, st);
+    upload_blocks_padded(e->ctx, e->Kt, e->Kd, Aket, e->dK, st);
     e->dN.alloc((size_t)e->Nd.total * 8, st, true);
     Operands ops;
     if (e->side == VMPS_ENV_LEFT) { ops.X = e->dB.as<double>(); ops.Z = e->dK.as<double>(); }
@@ -1096,12 +1188,10 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra, const doub
     run_plan(dp, ops, st);
     if (!e->pkN.p) {
         auto pb = pack_blocks(e->Nt, e->Nd, nullptr);
+        e->npkN = (int)pb.size();
         upload_vec(e->pkN, pb, st);
     }
-    e->stage.alloc((size_t)std::max<int64_t>(e->Nt.total, 1) * 8, st, false);
-    CK(launch_pack(e->pkN.as<PackBlock>(), (int)e->Nt.n, e->dN.as<double>(), e->stage.as<double>(), 0, st));
-    if (e->Nt.total > 0)
-        CK(cudaMemcpyAsync(Enew, e->stage.p, (size_t)e->Nt.total * 8, cudaMemcpyDeviceToHost, st));
+    pack_out(e->ctx, e->pkN, e->npkN, e->dN.as<double>(), e->Nt.total, e->stage, Enew, st);
     CK(cudaStreamSynchronize(st));
     check_device_error(e->ctx);
     API_END

@@ -16,6 +16,8 @@
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <queue>
+#include <unordered_set>
 #include <stdexcept>
 #include <tuple>
 
@@ -653,6 +655,67 @@ void sort_tiles(PhasePlan& ph) {
     ph.tiles.swap(t2);
 }
 }  // namespace
+
+void schedule_tma(PhasePlan& ph, int ncta) {
+    const size_t nt = ph.tiles.size();
+    ph.steps.clear();
+    ph.cta_tiles.assign(1, 0);
+    ph.ncta = 0;
+    if (nt == 0 || ncta <= 0) return;
+    ncta = (int)std::min<size_t>((size_t)ncta, nt);
+    // cost of a tile: its K steps plus the epilogue (about one step's time)
+    std::vector<int32_t> nsteps(nt, 0);
+    std::vector<double> cost(nt);
+    for (size_t i = 0; i < nt; ++i) {
+        const GTile& t = ph.tiles[i];
+        int32_t n = 0;
+        for (int s = t.seg_begin; s < t.seg_end; ++s) n += (ph.segs[s].K + kUmmaBK - 1) / kUmmaBK;
+        nsteps[i] = n;
+        cost[i] = n + 1.0;
+    }
+    std::vector<size_t> order(nt);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+    // least-loaded CTA first; ties to the lower index (deterministic)
+    using Load = std::pair<double, int>;
+    std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+    for (int b = 0; b < ncta; ++b) heap.push({0.0, b});
+    std::vector<std::vector<size_t>> per(ncta);
+    for (size_t i : order) {
+        Load l = heap.top();
+        heap.pop();
+        per[l.second].push_back(i);
+        heap.push({l.first + cost[i], l.second});
+    }
+    std::vector<GTile> tiles;
+    tiles.reserve(nt);
+    ph.cta_tiles.assign(ncta + 1, 0);
+    for (int b = 0; b < ncta; ++b) {
+        std::unordered_set<int32_t> seen_a, seen_b;
+        for (size_t i : per[b]) {
+            GTile t = ph.tiles[i];
+            t.step0 = (int32_t)ph.steps.size();
+            t.nsteps = nsteps[i];
+            for (int s = t.seg_begin; s < t.seg_end; ++s) {
+                const int32_t am = ph.seg_amap[s], bm = ph.seg_bmap[s];
+                for (int32_t k0 = 0; k0 < ph.segs[s].K; k0 += kUmmaBK) {
+                    TStep st{};
+                    st.amap = am;
+                    st.bmap = bm;
+                    st.k0 = k0;
+                    st.row0 = t.row0;
+                    st.col0 = t.col0;
+                    st.flags = (seen_a.insert(am).second ? 1 : 0) | (seen_b.insert(bm).second ? 2 : 0);
+                    ph.steps.push_back(st);
+                }
+            }
+            tiles.push_back(t);
+        }
+        ph.cta_tiles[b + 1] = (int32_t)tiles.size();
+    }
+    ph.tiles.swap(tiles);
+    ph.ncta = ncta;
+}
 
 Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z, const DevLayout& O,
                bool transX, bool transZ, int tile_m, int tile_n) {

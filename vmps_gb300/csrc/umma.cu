@@ -20,12 +20,13 @@
 
 namespace vmps {
 namespace um {
-constexpr int BM = 128, BN = 64, BK = 64, STAGES = 4;
+constexpr int BM = 128, BN = 64, BK = kUmmaBK, STAGES = 4;
 constexpr int NT = 192;                                    // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int A_BYTES = BM * BK * 2;                       // one of A hi / A lo: 16 KB
 constexpr int B_BYTES = BN * BK * 2;                       // one of B hi / B lo: 8 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;     // 48 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int STAGE_OUT_BYTES = 4 * 8192;                  // split-output epilogue: 32 rows x 64 cols x hi/lo per warp
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGE_OUT_BYTES + 1024 + 256;
 constexpr uint32_t ACC_COLS = 64;                          // one FP32 accumulator: 128 lanes x 64 columns
 constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two, so an epilogue overlaps the next tile
 // kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1),
@@ -33,6 +34,7 @@ constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two, so an epilogu
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
 constexpr long long WAIT_BUDGET = 4000000000LL;           // clock cycles (~2 s) per barrier wait
+constexpr int LOOKAHEAD = STAGES;                          // descriptors acquired this many steps ahead
 }  // namespace um
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -111,35 +113,61 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 
-// 32 lanes x 16 consecutive 32-bit columns of tensor memory
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
+// 32 lanes x 16 consecutive 32-bit columns of tensor memory (completion: tmem_wait_ld)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+// registers loaded by tmem_ld16 are read only after tmem_wait_ld: this empty
+// statement redefines them in program order after the wait
+__device__ __forceinline__ void reg_fence16(uint32_t* r) {
+    asm volatile(""
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]));
 }
 
-__device__ __forceinline__ int tile_steps(const GGArgs& g, const GTile& t) {
-    int n = 0;
-    for (int s = t.seg_begin; s < t.seg_end; ++s) n += (g.segs[s].K + um::BK - 1) / um::BK;
-    return n;
+__device__ __forceinline__ void tmap_prefetch(const void* tmap) {
+    asm volatile("prefetch.tensormap [%0];\n" ::"l"(tmap) : "memory");
+}
+// first use of a descriptor by this CTA: acquire it for the tensor-map proxy and
+// start fetching it
+__device__ __forceinline__ void acquire_step(const GGArgs& g, int j) {
+    const TStep s = g.steps[j];
+    if (s.flags & 1) {
+        const void* m = (const char*)g.amaps + (size_t)s.amap * 128;
+        tmap_acquire(m);
+        tmap_prefetch(m);
+    }
+    if (s.flags & 2) {
+        const void* m = (const char*)g.bmaps + (size_t)s.bmap * 128;
+        tmap_acquire(m);
+        tmap_prefetch(m);
+    }
 }
 
-// Persistent, warp-specialised grouped GEMM on pre-split operands.
-//   warp 0 (one lane): TMA loads of each 64-wide K step -- one 3-d box (K, rows,
-//     hi/lo) per operand, 128-byte swizzle, zero fill outside the block -- into
-//     a 4-deep ring of stages ("full" barriers carry the byte count);
-//   warp 1 (one lane): per K step 4 x (lo*hi, hi*lo, hi*hi) tcgen05.mma into one
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(a)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(b)) << 16);
+}
+
+// Persistent, warp-specialised grouped GEMM on pre-split operands.  CTA b runs
+// tiles[cta_tiles[b] .. cta_tiles[b+1]) (a host-side longest-first schedule),
+// whose K steps are steps[tiles[.].step0 ...], contiguous per CTA.
+//   warp 0 (one lane): per step one TMA 3-d box (K, rows, hi/lo) of A and one
+//     of B -- 128-byte swizzle, zero fill outside the block -- into a 4-deep
+//     ring of stages ("full" barriers count the bytes); descriptors are
+//     acquired and prefetched LOOKAHEAD steps ahead of their first use;
+//   warp 1 (one lane): per step 4 x (lo*hi, hi*lo, hi*hi) tcgen05.mma into one
 //     of two TMEM accumulators, commit to the stage's "empty" barrier, and at
 //     the end of a tile to the accumulator's "full" barrier;
-//   warps 2-5: epilogue -- tcgen05.ld of their 32 accumulator lanes, store,
-//     release the accumulator -- overlapping the next tile's main loop.
-// CTAs take tiles b, b + gridDim.x, ... (tiles are sorted by descending work).
+//   warps 2-5: epilogue of their 32 accumulator lanes, overlapping the next
+//     tile's main loop.  A split (bf16 hi/lo, row-major) output is staged
+//     through swizzled shared memory so that global stores are whole rows.
 template <int OUT_SPLIT>
 __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
     using namespace um;
@@ -147,16 +175,17 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
     const uint32_t raw = su32(smraw);
     const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
     const uint32_t ring = raw + pad;   // 1024-aligned: the swizzle pattern is anchored to 1024-byte boundaries
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smraw + pad + STAGES * STAGE_BYTES);
+    unsigned char* stage_out = smraw + pad + STAGES * STAGE_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(stage_out + STAGE_OUT_BYTES);
     // bars[0..S) full, [S..2S) empty, [2S..2S+2) accumulator full, [2S+2..2S+4) accumulator empty,
     // [2S+4] drain of the MMAs issued
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
-    __shared__ volatile int s_fail;
+    volatile int* s_fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     auto bar = [&](int i) { return su32(&bars[i]); };
 
     if (tid == 0) {
-        s_fail = 0;
+        *s_fail = 0;
         for (int s = 0; s < STAGES; ++s) { mbar_init(bar(s), 1); mbar_init(bar(STAGES + s), 1); }
         for (int b = 0; b < 2; ++b) { mbar_init(bar(2 * STAGES + b), 1); mbar_init(bar(2 * STAGES + 2 + b), 4); }
         mbar_init(bar(2 * STAGES + 4), 1);
@@ -170,50 +199,44 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int G = gridDim.x;
+    const int t0 = g.cta_tiles[blockIdx.x], t1 = g.cta_tiles[blockIdx.x + 1];
 
     if (warp == 0 && lane == 0) {
         // ---------------- TMA producer
         const char* amaps = (const char*)g.amaps;
         const char* bmaps = (const char*)g.bmaps;
+        int S0 = 0, S1 = 0;
+        if (t0 < t1) {
+            S0 = g.tiles[t0].step0;
+            S1 = g.tiles[t1 - 1].step0 + g.tiles[t1 - 1].nsteps;
+        }
+        for (int j = S0; j < S1 && j < S0 + LOOKAHEAD; ++j) acquire_step(g, j);
         int it = 0;
-        const void* last_a = nullptr;
-        const void* last_b = nullptr;
-        for (int t = blockIdx.x; t < g.ntiles && !s_fail; t += G) {
-            const GTile tile = g.tiles[t];
-            for (int s = tile.seg_begin; s < tile.seg_end && !s_fail; ++s) {
-                const int K = g.segs[s].K;
-                const void* am = amaps + (size_t)g.seg_amap[s] * 128;
-                const void* bm = bmaps + (size_t)g.seg_bmap[s] * 128;
-                if (am != last_a) { tmap_acquire(am); last_a = am; }
-                if (bm != last_b) { tmap_acquire(bm); last_b = bm; }
-                for (int k0 = 0; k0 < K; k0 += BK, ++it) {
-                    const int st = it % STAGES, use = it / STAGES;
-                    if (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), &s_fail)) break;
-                    const uint32_t sb = ring + st * STAGE_BYTES;
-                    mbar_expect_tx(bar(st), STAGE_BYTES);
-                    tma_load_3d(sb, am, k0, tile.row0, 0, bar(st));
-                    tma_load_3d(sb + 2 * A_BYTES, bm, k0, tile.col0, 0, bar(st));
-                }
-            }
+        for (int j = S0; j < S1 && !*s_fail; ++j, ++it) {
+            if (j + LOOKAHEAD < S1) acquire_step(g, j + LOOKAHEAD);
+            const TStep s = g.steps[j];
+            const int st = it % STAGES, use = it / STAGES;
+            if (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), s_fail)) break;
+            const uint32_t sb = ring + st * STAGE_BYTES;
+            mbar_expect_tx(bar(st), STAGE_BYTES);
+            tma_load_3d(sb, amaps + (size_t)s.amap * 128, s.k0, s.row0, 0, bar(st));
+            tma_load_3d(sb + 2 * A_BYTES, bmaps + (size_t)s.bmap * 128, s.k0, s.col0, 0, bar(st));
         }
         // copies still in flight land before the CTA exits (a no-op when the MMA warp consumed them)
         for (int i = it - 1; i >= 0 && i >= it - STAGES; --i)
-            mbar_drain(bar(i % STAGES), (uint32_t)((i / STAGES) & 1), &s_fail);
+            mbar_drain(bar(i % STAGES), (uint32_t)((i / STAGES) & 1), s_fail);
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer
         int it = 0, lt = 0;
-        for (int t = blockIdx.x; t < g.ntiles && !s_fail; t += G, ++lt) {
-            const GTile tile = g.tiles[t];
+        for (int t = t0; t < t1 && !*s_fail; ++t, ++lt) {
+            const int nsteps = g.tiles[t].nsteps;
             const int buf = lt & 1, buse = lt >> 1;
-            if (buse >= 1 && !mbar_wait(bar(2 * STAGES + 2 + buf), (uint32_t)((buse - 1) & 1), &s_fail)) break;
+            if (buse >= 1 && !mbar_wait(bar(2 * STAGES + 2 + buf), (uint32_t)((buse - 1) & 1), s_fail)) break;
             tc_fence_after();
             const uint32_t dacc = tmem + (uint32_t)buf * ACC_COLS;
-            bool first = true;
-            const int nsteps = tile_steps(g, tile);
             for (int k = 0; k < nsteps; ++k, ++it) {
                 const int st = it % STAGES, use = it / STAGES;
-                if (!mbar_wait(bar(st), (uint32_t)(use & 1), &s_fail)) break;
+                if (!mbar_wait(bar(st), (uint32_t)(use & 1), s_fail)) break;
                 tc_fence_after();
                 const uint32_t sb = ring + st * STAGE_BYTES;
                 const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + A_BYTES);
@@ -221,8 +244,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
                     const uint64_t adv = (uint64_t)(kk * 32) >> 4;   // 16 bf16 = 32 bytes along K
-                    umma_bf16(dacc, al + adv, bh + adv, first ? 0u : 1u);
-                    first = false;
+                    umma_bf16(dacc, al + adv, bh + adv, (k | kk) != 0 ? 1u : 0u);
                     umma_bf16(dacc, ah + adv, bl + adv, 1);
                     umma_bf16(dacc, ah + adv, bh + adv, 1);
                 }
@@ -231,101 +253,108 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
             umma_commit(bar(2 * STAGES + buf));
         }
         umma_commit(bar(2 * STAGES + 4));
-        mbar_drain(bar(2 * STAGES + 4), 0, &s_fail);
+        mbar_drain(bar(2 * STAGES + 4), 0, s_fail);
     } else if (warp >= 2) {
         // ---------------- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
         const int sp = warp & 3;
-        const int r = sp * 32 + lane;
+        const int rl = sp * 32 + lane;   // tile row of this lane
+        unsigned char* so = stage_out + (warp - 2) * 8192;   // this warp's staging: hi rows, then lo rows
         int lt = 0;
-        for (int t = blockIdx.x; t < g.ntiles; t += G, ++lt) {
+        for (int t = t0; t < t1; ++t, ++lt) {
             const GTile tile = g.tiles[t];
             const int buf = lt & 1, buse = lt >> 1;
             // warp-uniform outcome: the tensor-memory loads below are warp-collective
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(bar(2 * STAGES + buf), (uint32_t)(buse & 1), &s_fail));
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(bar(2 * STAGES + buf), (uint32_t)(buse & 1), s_fail));
             if (!ok) break;
             tc_fence_after();
-            const bool any = tile.seg_end > tile.seg_begin;
-            const int mrem = tile.tm, nrem = tile.tn;
-            const int64_t gr = tile.row0 + r;
-#pragma unroll 1
-            for (int j0 = 0; j0 < BN; j0 += 16) {
-                float v[16];
-                if (any) tmem_ld16(tmem + ((uint32_t)(sp * 32) << 16) + (uint32_t)(buf * ACC_COLS + j0), v);
-                else {
+            uint32_t v[64];
+            if (tile.nsteps > 0) {
+                const uint32_t ta = tmem + ((uint32_t)(sp * 32) << 16) + (uint32_t)(buf * ACC_COLS);
+                tmem_ld16(ta, v);
+                tmem_ld16(ta + 16, v + 16);
+                tmem_ld16(ta + 32, v + 32);
+                tmem_ld16(ta + 48, v + 48);
+                tmem_wait_ld();
+                reg_fence16(v);
+                reg_fence16(v + 16);
+                reg_fence16(v + 32);
+                reg_fence16(v + 48);
+            } else {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) v[i] = 0.f;
-                }
-                if (r >= mrem || j0 >= nrem) continue;
-                const int64_t gc0 = tile.col0 + j0;
-                if (OUT_SPLIT) {
-                    __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
-                    __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
-                    if (g.transC && j0 + 16 <= nrem) {   // 16 consecutive elements of one row: two 16-byte stores
-                        uint32_t h[8], l[8];
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * i]), h1 = __float2bfloat16_rn(v[2 * i + 1]);
-                            const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * i] - __bfloat162float(h0));
-                            const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * i + 1] - __bfloat162float(h1));
-                            h[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-                            l[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-                        }
-                        const int64_t e = tile.c_off + gc0 + gr * tile.ldc;
-                        uint4* ph = reinterpret_cast<uint4*>(Ch + e);
-                        uint4* pl = reinterpret_cast<uint4*>(Cl + e);
-                        ph[0] = make_uint4(h[0], h[1], h[2], h[3]);
-                        ph[1] = make_uint4(h[4], h[5], h[6], h[7]);
-                        pl[0] = make_uint4(l[0], l[1], l[2], l[3]);
-                        pl[1] = make_uint4(l[4], l[5], l[6], l[7]);
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < 16; ++i) {
-                            if (j0 + i >= nrem) break;
-                            const int64_t gc = gc0 + i;
-                            const int64_t e = tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc));
-                            const __nv_bfloat16 hh = __float2bfloat16_rn(v[i]);
-                            Ch[e] = hh;
-                            Cl[e] = __float2bfloat16_rn(v[i] - __bfloat162float(hh));
-                        }
-                    }
-                } else {
-                    double* C = (double*)g.C;
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        if (j0 + i >= nrem) break;
-                        const int64_t gc = gc0 + i;
-                        C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] = (double)v[i];
-                    }
-                }
+                for (int i = 0; i < 64; ++i) v[i] = 0u;
             }
+            // the accumulator is free once it sits in registers
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
+            if (OUT_SPLIT) {
+                // row-major bf16 hi / lo: stage 32 rows x 64 columns (chunk c of row r at
+                // r*128 + ((c ^ (r & 7)) << 4)), then store 4 whole 128-byte rows per instruction
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    uint32_t h[4], l[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float a = __uint_as_float(v[c * 8 + 2 * i]), b = __uint_as_float(v[c * 8 + 2 * i + 1]);
+                        const float ha = __bfloat162float(__float2bfloat16_rn(a));
+                        const float hb = __bfloat162float(__float2bfloat16_rn(b));
+                        h[i] = pack_bf16x2(a, b);
+                        l[i] = pack_bf16x2(a - ha, b - hb);
+                    }
+                    const int off = lane * 128 + ((c ^ (lane & 7)) << 4);
+                    *reinterpret_cast<uint4*>(so + off) = make_uint4(h[0], h[1], h[2], h[3]);
+                    *reinterpret_cast<uint4*>(so + 4096 + off) = make_uint4(l[0], l[1], l[2], l[3]);
+                }
+                __syncwarp();
+                __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
+                __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
+                const int c = lane & 7;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int row = i * 4 + (lane >> 3);
+                    const int off = row * 128 + ((c ^ (row & 7)) << 4);
+                    const uint4 hv = *reinterpret_cast<const uint4*>(so + off);
+                    const uint4 lv = *reinterpret_cast<const uint4*>(so + 4096 + off);
+                    if (sp * 32 + row < tile.tm && c * 8 < tile.tn) {
+                        const int64_t e = tile.c_off + (int64_t)(tile.row0 + sp * 32 + row) * tile.ldc + tile.col0 + c * 8;
+                        *reinterpret_cast<uint4*>(Ch + e) = hv;
+                        *reinterpret_cast<uint4*>(Cl + e) = lv;
+                    }
+                }
+                __syncwarp();   // the staging area is rewritten by the next tile
+            } else {
+                double* C = (double*)g.C;
+                if (rl < tile.tm) {
+                    const int64_t gr = tile.row0 + rl;
+#pragma unroll
+                    for (int j = 0; j < 64; ++j) {
+                        if (j < tile.tn) {
+                            const int64_t gc = tile.col0 + j;
+                            C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] =
+                                (double)__uint_as_float(v[j]);
+                        }
+                    }
+                }
+            }
         }
     }
     __syncthreads();
-    if (s_fail && tid == 0 && g.err) atomicOr(g.err, 1);
+    if (*s_fail && tid == 0 && g.err) atomicOr(g.err, 1);
     tc_fence_after();
     if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
-static int g_num_sms = 0;
-
 cudaError_t umma_init() {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(gg_umma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(gg_umma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(gg_umma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
 }
 
 cudaError_t launch_gg_umma(int out_split, const GGArgs& a, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
-    if (!a.amaps || !a.bmaps || !a.seg_amap || !a.seg_bmap) return cudaErrorInvalidValue;
-    const int grid = a.ntiles < g_num_sms ? a.ntiles : (g_num_sms > 0 ? g_num_sms : 148);
+    if (!a.amaps || !a.bmaps || !a.steps || !a.cta_tiles || a.ncta <= 0) return cudaErrorInvalidValue;
+    if (out_split && !a.transC) return cudaErrorInvalidValue;   // the staged epilogue writes row-major tiles
+    const int grid = a.ncta;
     if (out_split) gg_umma_kernel<1><<<grid, um::NT, um::SMEM_BYTES, st>>>(a);
     else gg_umma_kernel<0><<<grid, um::NT, um::SMEM_BYTES, st>>>(a);
     return cudaGetLastError();
