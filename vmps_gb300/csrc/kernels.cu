@@ -18,6 +18,7 @@
 
 #include <algorithm>
 
+#include "convert.hpp"
 #include "kernels.hpp"
 
 namespace vmps {
@@ -392,7 +393,7 @@ __global__ void prep_kernel(const PrepBlock* __restrict__ pbs, int nb, const dou
 __global__ void split_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ hi,
                              __nv_bfloat16* __restrict__ lo, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float v = (float)src[i];
+        const float v = f64_to_f32_rn(src[i]);
         const __nv_bfloat16 h = __float2bfloat16_rn(v);
         hi[i] = h;
         lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
@@ -411,14 +412,62 @@ __global__ void pack_kernel(const PackBlock* blocks, int nb, const double* __res
         const int rows = (int)pb.rows, n = (int)(pb.rows * pb.cols), ld = (int)pb.ld;
         const double* s = src + (to_padded ? pb.coff : pb.doff);
         double* d = dst + (to_padded ? pb.doff : pb.coff);
-        for (int e = threadIdx.x; e < n; e += blockDim.x) {
-            const int c = e / rows, r = e - c * rows;
-            if (to_padded) d[r + c * ld] = pb.scale * s[e];
-            else d[e] = s[r + c * ld] / pb.scale;
+        // four independent loads in flight per thread, then the four stores
+        const bool unit = pb.scale == 1.0;   // U(1) blocks: a plain copy, no FP64 arithmetic
+        for (int e0 = threadIdx.x; e0 < n; e0 += 4 * blockDim.x) {
+            double x[4];
+            int at[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * blockDim.x;
+                const int c = e / rows, r = e - c * rows;
+                const int pe = r + c * ld;
+                at[u] = to_padded ? pe : e;
+                x[u] = e < n ? s[to_padded ? e : pe] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (e0 + u * blockDim.x >= n) break;
+                d[at[u]] = unit ? x[u] : (to_padded ? pb.scale * x[u] : x[u] / pb.scale);
+            }
         }
     }
 }
 
+
+// compact vector -> padded bf16 hi / lo arena in one pass: the padded FP64
+// vector that pack_kernel followed by split_kernel would go through is never
+// stored, and each element gets the same value (scale * x rounded to float,
+// then hi = bf16(v), lo = bf16(v - hi))
+__global__ void pack_split_kernel(const PackBlock* blocks, int nb, const double* __restrict__ src,
+                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        const PackBlock pb = blocks[b];
+        const int rows = (int)pb.rows, n = (int)(pb.rows * pb.cols), ld = (int)pb.ld;
+        const double* s = src + pb.coff;
+        __nv_bfloat16* h = hi + pb.doff;
+        __nv_bfloat16* l = lo + pb.doff;
+        const bool unit = pb.scale == 1.0;
+        for (int e0 = threadIdx.x; e0 < n; e0 += 4 * blockDim.x) {
+            double x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * blockDim.x;
+                x[u] = e < n ? s[e] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * blockDim.x;
+                if (e >= n) break;
+                const int c = e / rows, r = e - c * rows;
+                const float v = f64_to_f32_rn(unit ? x[u] : pb.scale * x[u]);
+                const __nv_bfloat16 vh = __float2bfloat16_rn(v);
+                h[r + c * ld] = vh;
+                l[r + c * ld] = __float2bfloat16_rn(v - __bfloat162float(vh));
+            }
+        }
+    }
+}
 
 // partial dot products: fixed chunking -> deterministic two-pass reduction
 constexpr int kDotThreads = 256;
@@ -553,6 +602,13 @@ cudaError_t launch_split(const double* src, void* hi, void* lo, int64_t n, cudaS
     if (n <= 0) return cudaSuccess;
     if (!src || !hi || !lo) return cudaErrorInvalidValue;
     split_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(src, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_split(const PackBlock* blocks, int nb, const double* src, void* hi, void* lo, cudaStream_t st) {
+    if (nb <= 0) return cudaSuccess;
+    if (!blocks || !src || !hi || !lo) return cudaErrorInvalidValue;
+    pack_split_kernel<<<min(nb, 4096), 256, 0, st>>>(blocks, nb, src, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo);
     return cudaGetLastError();
 }
 

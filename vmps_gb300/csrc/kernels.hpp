@@ -41,6 +41,8 @@ cudaError_t umma_init();
 cudaError_t launch_gg_umma(int out_split, const GGArgs& a, cudaStream_t st);
 cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* hi, void* lo, cudaStream_t st);
 cudaError_t launch_split(const double* src, void* hi, void* lo, int64_t n, cudaStream_t st);
+// compact (scaled per block) -> padded bf16 hi / lo, the values launch_pack + launch_split give
+cudaError_t launch_pack_split(const PackBlock* blocks, int nb, const double* src, void* hi, void* lo, cudaStream_t st);
 cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, double* dst, int to_padded,
                         cudaStream_t st);
 int64_t dot_chunk(int64_t n);

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -88,6 +89,7 @@ template <typename T> static void upload_vec(DBuf& d, const std::vector<T>& v, c
 struct vmps_ctx_s {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   // host<->device transfers overlapped with compute
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     int* err = nullptr;   // device error word written by the tcgen05 engine
     bool pageable_access = false;   // the device reads pageable host memory in place
@@ -135,6 +137,30 @@ struct DevPhase {
     }
 };
 
+// Host-buffer HxV pipeline: the vector's blocks in k contiguous chunks (the same
+// cut for input and output), and each phase of the split plan cut into one
+// launch per chunk -- phase 1 by the chunk of its V block, phase 2 by the chunk
+// of its output block -- so that transfers of one chunk overlap the compute of
+// another.
+struct VecChunk {
+    int64_t coff, clen;    // compact (host) element range
+    int64_t doff, dlen;    // padded (device) element range
+    int piece0, piece1;    // pack pieces
+};
+struct DevChunked {
+    std::vector<VecChunk> io;
+    bool compact_out = false;         // phase 2 writes the compact (host-layout) vector directly
+    std::deque<PhasePlan> p1h, p2h;   // host sub-plans (DevPhase::host points here)
+    std::deque<DevPhase> p1, p2;
+    std::vector<cudaEvent_t> ev_in, ev_out;
+    cudaEvent_t ev_start = nullptr;
+    ~DevChunked() {
+        for (auto e : ev_in) cudaEventDestroy(e);
+        for (auto e : ev_out) cudaEventDestroy(e);
+        if (ev_start) cudaEventDestroy(ev_start);
+    }
+};
+
 // Split plans keep each bf16 operand as one arena [hi | lo]: the lo half of
 // element e sits at e + lo, with lo = the arena's element count (a multiple of
 // 32, so both halves start on 64-byte boundaries).
@@ -147,6 +173,7 @@ struct DevPlan {
     DBuf mapX, mapY, mapT, mapZ;   // tcgen05 engine: one 128-byte TMA descriptor per operand block
     int nprepX = 0, nprepZ = 0;
     int64_t ytotal = 0;            // elements of the Y arena (split per call)
+    std::unique_ptr<DevChunked> chunks;   // host-buffer pipeline (tcgen05 split plans of pivots)
     bool ready = false;
 };
 
@@ -200,9 +227,10 @@ static void build_maps(DBuf& maps, const std::vector<OpBlock>& blocks, const DBu
 }
 
 // compact <-> padded copy descriptors of one block table.  Blocks are cut into
-// pieces of whole columns holding at most kPackPiece elements, so that large
-// blocks spread over many thread blocks of the copy kernel.
-constexpr int64_t kPackPiece = 8192;
+// pieces of whole columns holding at most kPackPiece elements (one pass of a
+// 256-thread block with four loads in flight per thread), so that large blocks
+// spread over many thread blocks of the copy kernels.
+constexpr int64_t kPackPiece = 1024;
 static std::vector<PackBlock> pack_blocks(const BlockTable& t, const DevLayout& d, const std::vector<double>* scale) {
     std::vector<PackBlock> v;
     v.reserve((size_t)t.n);
@@ -217,6 +245,22 @@ static std::vector<PackBlock> pack_blocks(const BlockTable& t, const DevLayout& 
         }
     }
     return v;
+}
+
+// index of the first pack piece of every block (and the total at the end), with
+// the same cut as pack_blocks
+static std::vector<int> pack_piece_starts(const BlockTable& t) {
+    std::vector<int> s((size_t)t.n + 1, 0);
+    for (int64_t i = 0; i < t.n; ++i) {
+        const int64_t rows = t.rows[i], cols = t.cols[i];
+        int64_t np = 0;
+        if (rows > 0 && cols > 0) {
+            const int64_t per = std::max<int64_t>(1, kPackPiece / rows);
+            np = (cols + per - 1) / per;
+        }
+        s[i + 1] = s[i] + (int)np;
+    }
+    return s;
 }
 
 // A pointer the device may dereference for a caller's host buffer, or null when
@@ -365,9 +409,8 @@ static void split_prepare(DevPlan& dp, const double* X, const double* Z, cudaStr
     CK(launch_prep(dp.prepZ.as<PrepBlock>(), dp.nprepZ, Z, dp.Z2.p, lo_half(dp.Z2, dp.plan.Zp_total), st));
 }
 
-static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream_t st) {
-    const DevPhase& d = ph == 1 ? dp.p1 : dp.p2;
-    const PhasePlan& h = ph == 1 ? dp.plan.p1 : dp.plan.p2;
+static void run_phase_on(const DevPlan& dp, int ph, const DevPhase& d, const PhasePlan& h, const Operands& ops,
+                         cudaStream_t st) {
     GGArgs a{};
     a.tiles = d.tiles.as<GTile>();
     a.segs = d.segs.as<GSeg>();
@@ -409,6 +452,11 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
     if (!dp.plan.split) CK(launch_gg64(a, st));
     else if (dp.plan.split_kernel) CK(launch_gg_umma(ph == 1 ? 1 : 0, a, st));
     else CK(launch_gg_split(ph == 1 ? 1 : 0, a, st));
+}
+
+static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream_t st) {
+    if (ph == 1) run_phase_on(dp, 1, dp.p1, dp.plan.p1, ops, st);
+    else run_phase_on(dp, 2, dp.p2, dp.plan.p2, ops, st);
 }
 
 // one application of a planned contraction: (split plans) split Y, phase 1, phase 2
@@ -487,6 +535,8 @@ static void ensure_io(vmps_pivot* p) {
     if (!p->vout.p) p->vout.alloc((size_t)p->Vd.total * 8, p->st(), true);
 }
 
+static void make_chunks(vmps_pivot* p, DevPlan& dp);
+
 static DevPlan& get_plan(vmps_pivot* p, int prec) {
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
     DevPlan& dp = p->plans[prec];
@@ -502,9 +552,149 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
     if (p->ctx->device < 0) { dp.ready = true; return dp; }   // host-only: plan without device copies
     plan_to_device(dp, p->Vd.total, p->st());
     split_prepare(dp, p->dL.as<double>(), p->dR.as<double>(), p->st());
+    if (prec == VMPS_PREC_BF16X3) make_chunks(p, dp);
     CK(cudaStreamSynchronize(p->st()));
     dp.ready = true;
     return dp;
+}
+
+// Cut a pivot's split plan into the host-buffer pipeline (see DevChunked).  Only
+// for the tcgen05 engine, vectors of at least kChunkBytes per chunk, and a
+// compact layout whose blocks are stored in order without gaps.
+constexpr int64_t kChunkBytes = 4 << 20;
+constexpr int kMaxChunks = 6;
+static void make_chunks(vmps_pivot* p, DevPlan& dp) {
+    const BlockTable& t = p->Vt;
+    const int64_t nb = t.n;
+    if (!dp.plan.split_kernel || nb < 2) return;
+    const int k = (int)std::min<int64_t>(kMaxChunks, std::min<int64_t>(nb, t.total * 8 / kChunkBytes));
+    if (k < 2) return;
+    for (int64_t b = 0; b < nb; ++b) {
+        const int64_t next = b + 1 < nb ? t.off[b + 1] : t.total;
+        if (t.off[b] + t.rows[b] * t.cols[b] != next) return;   // not in order / gaps: no pipeline
+    }
+    if (t.off[0] != 0) return;
+    auto ch = std::make_unique<DevChunked>();
+    const std::vector<int> ps = pack_piece_starts(t);
+    std::vector<int> chunk_of((size_t)nb, 0);
+    int64_t b0 = 0;
+    for (int c = 0; c < k && b0 < nb; ++c) {
+        const int64_t target = (t.total * (c + 1)) / k;
+        int64_t b1 = b0 + 1;
+        while (b1 < nb && (c == k - 1 || t.off[b1] < target)) ++b1;
+        VecChunk v{};
+        v.coff = t.off[b0];
+        v.clen = (b1 < nb ? t.off[b1] : t.total) - v.coff;
+        v.doff = p->Vd.off[b0];
+        v.dlen = (b1 < nb ? p->Vd.off[b1] : p->Vd.total) - v.doff;
+        v.piece0 = ps[b0];
+        v.piece1 = ps[b1];
+        for (int64_t b = b0; b < b1; ++b) chunk_of[b] = (int)ch->io.size();
+        ch->io.push_back(v);
+        b0 = b1;
+    }
+    const int kk = (int)ch->io.size();
+    if (kk < 2) return;
+    std::unordered_map<int64_t, int64_t> block_of_off;
+    for (int64_t b = 0; b < nb; ++b) block_of_off[p->Vd.off[b]] = b;
+    // with unit block scales the output needs no unscaling: phase 2 stores into
+    // the compact layout (column-major blocks, ld = rows) and the unpack pass goes
+    ch->compact_out = std::all_of(p->vscale.begin(), p->vscale.end(), [](double s) { return s == 1.0; });
+    auto cut = [&](const PhasePlan& full, int ph, std::deque<PhasePlan>& hs, std::deque<DevPhase>& ds) {
+        std::vector<std::vector<GTile>> per(kk);
+        for (const GTile& tl : full.tiles) {
+            int64_t blk;
+            if (ph == 1) {
+                if (tl.seg_end <= tl.seg_begin) throw std::logic_error("phase-1 tile without a segment");
+                blk = full.seg_bmap[tl.seg_begin];   // the V block this intermediate multiplies
+            } else {
+                auto it = block_of_off.find(tl.c_off);
+                if (it == block_of_off.end()) throw std::logic_error("phase-2 tile outside the vector layout");
+                blk = it->second;
+                if (ch->compact_out) {
+                    GTile c = tl;
+                    c.c_off = t.off[blk];
+                    c.ldc = (int32_t)t.rows[blk];
+                    per[chunk_of[blk]].push_back(c);
+                    continue;
+                }
+            }
+            per[chunk_of[blk]].push_back(tl);
+        }
+        const std::vector<OpBlock>& A = ph == 1 ? dp.plan.opX : dp.plan.opT;
+        for (int c = 0; c < kk; ++c) {
+            hs.emplace_back();
+            PhasePlan& sp = hs.back();
+            sp.terms = full.terms;
+            sp.segs = full.segs;
+            sp.seg_amap = full.seg_amap;
+            sp.seg_bmap = full.seg_bmap;
+            sp.transA = full.transA; sp.transB = full.transB; sp.transC = full.transC;
+            sp.slotA = full.slotA; sp.slotB = full.slotB; sp.slotC = full.slotC;
+            sp.tiles = std::move(per[c]);
+            schedule_tma(sp, p->ctx->num_sms);
+            validate_tma_schedule(sp, A);
+            ds.emplace_back();
+            ds.back().upload(sp, p->st());
+        }
+    };
+    cut(dp.plan.p1, 1, ch->p1h, ch->p1);
+    cut(dp.plan.p2, 2, ch->p2h, ch->p2);
+    ch->ev_in.resize(kk, nullptr);
+    ch->ev_out.resize(kk, nullptr);
+    for (int c = 0; c < kk; ++c) {
+        CK(cudaEventCreateWithFlags(&ch->ev_in[c], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ch->ev_out[c], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&ch->ev_start, cudaEventDisableTiming));
+    dp.chunks = std::move(ch);
+}
+
+// host-buffer HxV through the chunk pipeline: copies on the copy stream, compute
+// on the context stream, ordered by events
+static void hxv_host_pipelined(vmps_pivot* p, DevPlan& dp, const double* vin, double* vout) {
+    DevChunked& ch = *dp.chunks;
+    cudaStream_t cs = p->st(), xs = p->ctx->copy_stream;
+    double* din = p->vin.as<double>();
+    double* dout = p->vout.as<double>();
+    double* sin = p->stage_in.as<double>();
+    double* sout = p->stage_out.as<double>();
+    const PackBlock* pk = p->dPack.as<PackBlock>();
+    Operands ops;
+    ops.X = p->dL.as<double>();
+    ops.Z = p->dR.as<double>();
+    ops.Y = din;
+    ops.O = ch.compact_out ? sout : dout;
+    ops.err = p->ctx->err;
+    const int k = (int)ch.io.size();
+    // the copy stream starts after everything already queued on the compute stream
+    CK(cudaEventRecord(ch.ev_start, cs));
+    CK(cudaStreamWaitEvent(xs, ch.ev_start, 0));
+    for (int c = 0; c < k; ++c) {
+        const VecChunk& v = ch.io[c];
+        CK(cudaMemcpyAsync(sin + v.coff, vin + v.coff, (size_t)v.clen * 8, cudaMemcpyHostToDevice, xs));
+        CK(cudaEventRecord(ch.ev_in[c], xs));
+        CK(cudaStreamWaitEvent(cs, ch.ev_in[c], 0));
+        CK(launch_pack_split(pk + v.piece0, v.piece1 - v.piece0, sin, dp.Y2.p, lo_half(dp.Y2, dp.ytotal), cs));
+        run_phase_on(dp, 1, ch.p1[c], ch.p1h[c], ops, cs);
+    }
+    // phase 2 of chunk o is queued before the copy-out of chunk o-1, so that a
+    // copy call that blocks the host (pageable memory) does not hold back compute
+    for (int o = 0; o <= k; ++o) {
+        if (o < k) {
+            const VecChunk& v = ch.io[o];
+            run_phase_on(dp, 2, ch.p2[o], ch.p2h[o], ops, cs);
+            if (!ch.compact_out) CK(launch_pack(pk + v.piece0, v.piece1 - v.piece0, dout, sout, 0, cs));
+            CK(cudaEventRecord(ch.ev_out[o], cs));
+        }
+        if (o >= 1) {
+            const VecChunk& w = ch.io[o - 1];
+            CK(cudaStreamWaitEvent(xs, ch.ev_out[o - 1], 0));
+            CK(cudaMemcpyAsync(vout + w.coff, sout + w.coff, (size_t)w.clen * 8, cudaMemcpyDeviceToHost, xs));
+        }
+    }
+    CK(cudaStreamSynchronize(xs));
+    CK(cudaStreamSynchronize(cs));
 }
 
 static void require_device(const vmps_ctx* c) {
@@ -605,6 +795,7 @@ int vmps_ctx_create(int device, vmps_ctx** out) {
     auto* c = new vmps_ctx_s();
     c->device = device;
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&c->ev0));
     CK(cudaEventCreate(&c->ev1));
     CK(cudaEventCreate(&c->ev2));
@@ -630,6 +821,8 @@ int vmps_ctx_destroy(vmps_ctx* ctx) {
     cudaEventDestroy(ctx->ev1);
     cudaEventDestroy(ctx->ev2);
     if (ctx->err) cudaFree(ctx->err);
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return VMPS_OK;
@@ -708,6 +901,12 @@ int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int prec) {
     cudaStream_t st = p->st();
     ensure_staging(p);
     ensure_io(p);
+    DevPlan& dp = get_plan(p, prec);
+    if (dp.chunks) {
+        hxv_host_pipelined(p, dp, vin, vout);
+        check_device_error(p->ctx);
+        return VMPS_OK;
+    }
     pack_in(p->ctx, p->dPack, p->npack, vin, p->Vt.total, p->stage_in, p->vin.as<double>(), st);
     pivot_hxv_dev(p, prec, p->vin.as<double>(), p->vout.as<double>());
     pack_out(p->ctx, p->dPack, p->npack, p->vout.as<double>(), p->Vt.total, p->stage_out, vout, st);

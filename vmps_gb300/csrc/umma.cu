@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "convert.hpp"
 #include "kernels.hpp"
 
 namespace vmps {
@@ -331,7 +332,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
                         if (j < tile.tn) {
                             const int64_t gc = tile.col0 + j;
                             C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] =
-                                (double)__uint_as_float(v[j]);
+                                f32_to_f64(__uint_as_float(v[j]));
                         }
                     }
                 }
