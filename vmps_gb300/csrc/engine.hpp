@@ -140,15 +140,16 @@ struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, 
 struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, step0, nsteps; };
 // one K step of the tcgen05 engine: TMA descriptors of A and B, the K offset in
 // the segment and the tile origin; flags bit 0 / bit 1: first use of the A / B
-// descriptor by this CTA (acquire it for the tensor-map proxy)
-struct TStep { int32_t amap, bmap, k0, row0, col0, flags, pad0, pad1; };
-constexpr int kUmmaBK = 64;   // K extent of one tcgen05 engine step
+// descriptor by this CTA (acquire it for the tensor-map proxy); brows: rows of
+// the B box (the tile's MMA N, a multiple of 16, is at most this)
+struct TStep { int32_t amap, bmap, k0, row0, col0, flags, brows, pad; };
+constexpr int kUmmaBK = 32;   // K extent of one tcgen05 engine step
 // at most this many A terms per segment (the kernels stage them in shared memory)
 constexpr int kMaxTerms = 16;
 // tile edges (rows split on multiples of 16, columns on multiples of 8):
 // mma.sync engines at most 64 x 64, the tcgen05 engine at most 128 x 64
 constexpr int kTileMax = 64;
-constexpr int kUmmaTileM = 128, kUmmaTileN = 64;
+constexpr int kUmmaTileM = 128, kUmmaTileN = 256;
 
 struct PhasePlan {
     std::vector<GTerm> terms;
@@ -170,8 +171,8 @@ enum Slot { SLOT_X = 0, SLOT_Y = 1, SLOT_Z = 2, SLOT_OUT = 3, SLOT_T = 4 };
 
 // A prepared split-precision operand block: `outer` rows (rows of A / columns of
 // B) of K contiguous elements, row stride ld, at element offset off of its
-// [hi | lo] arena (lo half at +total)
-struct OpBlock { int64_t off; int32_t outer, K, ld, pad; };
+// [hi | lo] arena (lo half at +total); box: rows of its TMA box (tcgen05 engine)
+struct OpBlock { int64_t off; int32_t outer, K, ld, box; };
 
 // Split-precision operand preparation: one block of a column-major FP64 source
 // (rows x cols, leading dimension src_ld) written as bf16 hi/lo pairs in the
@@ -202,7 +203,10 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // Static schedule of a split phase for the persistent tcgen05 engine on ncta
 // CTAs: K steps of kUmmaBK per segment, tiles assigned longest-first to the
 // least-loaded CTA and stored CTA by CTA.
-void schedule_tma(PhasePlan& ph, int ncta);
+void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& B);
+// rows of the TMA box of a B operand block with `outer` rows, tiled by
+// split_extent(outer, 8, tile_n): the largest tile extent rounded up to 16
+int32_t b_box_rows(int64_t outer, int tile_n);
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
                      const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n);
 

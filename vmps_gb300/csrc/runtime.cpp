@@ -137,18 +137,19 @@ struct DevPhase {
     }
 };
 
-// Host-buffer HxV pipeline: the vector's blocks in k contiguous chunks (the same
-// cut for input and output), and each phase of the split plan cut into one
-// launch per chunk -- phase 1 by the chunk of its V block, phase 2 by the chunk
-// of its output block -- so that transfers of one chunk overlap the compute of
-// another.
+// Host-buffer HxV pipeline: the vector's blocks in contiguous chunks, and each
+// phase of the split plan cut into one launch per chunk -- phase 1 by the input
+// chunk of its V block, phase 2 by the output chunk of its output block -- so
+// that transfers of one chunk overlap the compute of another.  The output side
+// uses fewer, larger chunks: a phase-2 launch must hold enough tiles per CTA to
+// stay balanced.
 struct VecChunk {
     int64_t coff, clen;    // compact (host) element range
     int64_t doff, dlen;    // padded (device) element range
     int piece0, piece1;    // pack pieces
 };
 struct DevChunked {
-    std::vector<VecChunk> io;
+    std::vector<VecChunk> in, out;    // input chunks (phase 1 cut), output chunks (phase 2 cut)
     bool compact_out = false;         // phase 2 writes the compact (host-layout) vector directly
     std::deque<PhasePlan> p1h, p2h;   // host sub-plans (DevPhase::host points here)
     std::deque<DevPhase> p1, p2;
@@ -200,9 +201,10 @@ static EncodeTiledFn encode_tiled() {
 
 // One descriptor per block of a [hi | lo] bf16 arena: a 3-d tensor (K, outer,
 // hi/lo) with K contiguous, rows `ld` elements apart, halves `lo` elements
-// apart.  Boxes are 64 x box_rows x 2 with 128-byte swizzle and zero fill
-// outside the block, which is what the engine's shared-memory stages expect.
-static void build_maps(DBuf& maps, const std::vector<OpBlock>& blocks, const DBuf& arena, int64_t lo, int box_rows,
+// apart.  Boxes are kUmmaBK (32 elements = 64 bytes) x the block's box rows x 2
+// with 64-byte swizzle and zero fill outside the block, which is what the
+// engine's shared-memory stages expect.
+static void build_maps(DBuf& maps, const std::vector<OpBlock>& blocks, const DBuf& arena, int64_t lo,
                        cudaStream_t st) {
     if (lo % 8 != 0) throw std::logic_error("split arena size is not a multiple of 8 elements");
     std::vector<CUtensorMap> h(std::max<size_t>(1, blocks.size()));
@@ -213,11 +215,12 @@ static void build_maps(DBuf& maps, const std::vector<OpBlock>& blocks, const DBu
         if (b.off % 32 != 0 || b.ld % 8 != 0) throw std::logic_error("operand block is not 16-byte aligned");
         const cuuint64_t dims[3] = {(cuuint64_t)std::max(1, b.K), (cuuint64_t)std::max(1, b.outer), 2};
         const cuuint64_t strides[2] = {(cuuint64_t)b.ld * 2, (cuuint64_t)lo * 2};
-        const cuuint32_t box[3] = {64, (cuuint32_t)box_rows, 2};
+        if (b.box < 16 || b.box > 256 || b.box % 16 != 0) throw std::logic_error("TMA box rows out of range");
+        const cuuint32_t box[3] = {(cuuint32_t)kUmmaBK, (cuuint32_t)b.box, 2};
         const cuuint32_t estr[3] = {1, 1, 1};
         void* base = arena.as<uint16_t>() + b.off;
         CUresult res = enc(&h[i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (res != CUDA_SUCCESS)
             throw CudaFail("cuTensorMapEncodeTiled failed (" + std::to_string((int)res) + ") for a block of " +
@@ -338,9 +341,13 @@ static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A
             throw std::logic_error("tcgen05 plan: tile shape out of range");
         if (t.seg_begin < 0 || t.seg_end < t.seg_begin || t.seg_end > (int32_t)ph.segs.size())
             throw std::logic_error("tcgen05 plan: tile segment range out of range");
-        for (int32_t s = t.seg_begin; s < t.seg_end; ++s)
+        for (int32_t s = t.seg_begin; s < t.seg_end; ++s) {
             if (t.row0 + t.tm > A[ph.seg_amap[s]].outer || t.col0 + t.tn > B[ph.seg_bmap[s]].outer)
                 throw std::logic_error("tcgen05 plan: tile outside its operand blocks");
+            // the MMA reads round16(tn) rows of the B box and all 128 rows of the A box
+            if (((t.tn + 15) / 16) * 16 > B[ph.seg_bmap[s]].box || A[ph.seg_amap[s]].box != kUmmaTileM)
+                throw std::logic_error("tcgen05 plan: tile wider than its TMA box");
+        }
         // a split output is stored in 16-byte row chunks (8 bf16) of a row-major tile
         if (split_out && (!ph.transC || t.c_off % 8 != 0 || t.ldc % 8 != 0 || t.col0 % 8 != 0 ||
                           t.ldc < ((t.col0 + t.tn + 7) / 8) * 8))
@@ -361,6 +368,10 @@ static void validate_tma_schedule(const PhasePlan& ph, const std::vector<OpBlock
     for (const GTile& t : ph.tiles) {
         if (t.step0 != next || t.nsteps < 0) throw std::logic_error("tcgen05 plan: tile steps not contiguous");
         next += t.nsteps;
+        // the MMA issuer takes the B box height of a tile from its first step
+        for (int j = t.step0; j < t.step0 + t.nsteps && j < (int)ph.steps.size(); ++j)
+            if (ph.steps[j].brows != ph.steps[t.step0].brows || ph.steps[j].brows < ((t.tn + 15) / 16) * 16)
+                throw std::logic_error("tcgen05 plan: B box height varies within a tile");
     }
     if (next != (int64_t)ph.steps.size()) throw std::logic_error("tcgen05 plan: step count mismatch");
     for (const TStep& s : ph.steps)
@@ -371,8 +382,8 @@ static void validate_tma_schedule(const PhasePlan& ph, const std::vector<OpBlock
 static void schedule_and_validate(Plan& p, int ncta) {
     validate_tma_plan(p.p1, p.opX, p.opY, true);
     validate_tma_plan(p.p2, p.opT, p.opZ, false);
-    schedule_tma(p.p1, ncta);
-    schedule_tma(p.p2, ncta);
+    schedule_tma(p.p1, ncta, p.opY);
+    schedule_tma(p.p2, ncta, p.opZ);
     validate_tma_schedule(p.p1, p.opX);
     validate_tma_schedule(p.p2, p.opT);
 }
@@ -395,10 +406,10 @@ static void plan_to_device(DevPlan& dp, int64_t ytotal, cudaStream_t st) {
     dp.nprepX = (int)dp.plan.prepX.size();
     dp.nprepZ = (int)dp.plan.prepZ.size();
     if (dp.plan.split_kernel) {
-        build_maps(dp.mapX, dp.plan.opX, dp.X2, dp.plan.Xp_total, kUmmaTileM, st);
-        build_maps(dp.mapY, dp.plan.opY, dp.Y2, dp.ytotal, kUmmaTileN, st);
-        build_maps(dp.mapT, dp.plan.opT, dp.T, dp.plan.T.total, kUmmaTileM, st);
-        build_maps(dp.mapZ, dp.plan.opZ, dp.Z2, dp.plan.Zp_total, kUmmaTileN, st);
+        build_maps(dp.mapX, dp.plan.opX, dp.X2, dp.plan.Xp_total, st);
+        build_maps(dp.mapY, dp.plan.opY, dp.Y2, dp.ytotal, st);
+        build_maps(dp.mapT, dp.plan.opT, dp.T, dp.plan.T.total, st);
+        build_maps(dp.mapZ, dp.plan.opZ, dp.Z2, dp.plan.Zp_total, st);
     }
 }
 
@@ -562,13 +573,13 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
 // for the tcgen05 engine, vectors of at least kChunkBytes per chunk, and a
 // compact layout whose blocks are stored in order without gaps.
 constexpr int64_t kChunkBytes = 4 << 20;
-constexpr int kMaxChunks = 6;
+constexpr int kMaxChunksIn = 4, kMaxChunksOut = 3;
 static void make_chunks(vmps_pivot* p, DevPlan& dp) {
     const BlockTable& t = p->Vt;
     const int64_t nb = t.n;
     if (!dp.plan.split_kernel || nb < 2) return;
-    const int k = (int)std::min<int64_t>(kMaxChunks, std::min<int64_t>(nb, t.total * 8 / kChunkBytes));
-    if (k < 2) return;
+    const int64_t kmax = std::min<int64_t>(nb, t.total * 8 / kChunkBytes);
+    if (kmax < 2) return;
     for (int64_t b = 0; b < nb; ++b) {
         const int64_t next = b + 1 < nb ? t.off[b + 1] : t.total;
         if (t.off[b] + t.rows[b] * t.cols[b] != next) return;   // not in order / gaps: no pipeline
@@ -576,31 +587,38 @@ static void make_chunks(vmps_pivot* p, DevPlan& dp) {
     if (t.off[0] != 0) return;
     auto ch = std::make_unique<DevChunked>();
     const std::vector<int> ps = pack_piece_starts(t);
-    std::vector<int> chunk_of((size_t)nb, 0);
-    int64_t b0 = 0;
-    for (int c = 0; c < k && b0 < nb; ++c) {
-        const int64_t target = (t.total * (c + 1)) / k;
-        int64_t b1 = b0 + 1;
-        while (b1 < nb && (c == k - 1 || t.off[b1] < target)) ++b1;
-        VecChunk v{};
-        v.coff = t.off[b0];
-        v.clen = (b1 < nb ? t.off[b1] : t.total) - v.coff;
-        v.doff = p->Vd.off[b0];
-        v.dlen = (b1 < nb ? p->Vd.off[b1] : p->Vd.total) - v.doff;
-        v.piece0 = ps[b0];
-        v.piece1 = ps[b1];
-        for (int64_t b = b0; b < b1; ++b) chunk_of[b] = (int)ch->io.size();
-        ch->io.push_back(v);
-        b0 = b1;
-    }
-    const int kk = (int)ch->io.size();
-    if (kk < 2) return;
+    // k chunks of about equal compact size; chunk_of[block]
+    auto partition = [&](int k, std::vector<VecChunk>& io, std::vector<int>& chunk_of) {
+        chunk_of.assign((size_t)nb, 0);
+        int64_t b0 = 0;
+        for (int c = 0; c < k && b0 < nb; ++c) {
+            const int64_t target = (t.total * (c + 1)) / k;
+            int64_t b1 = b0 + 1;
+            while (b1 < nb && (c == k - 1 || t.off[b1] < target)) ++b1;
+            VecChunk v{};
+            v.coff = t.off[b0];
+            v.clen = (b1 < nb ? t.off[b1] : t.total) - v.coff;
+            v.doff = p->Vd.off[b0];
+            v.dlen = (b1 < nb ? p->Vd.off[b1] : p->Vd.total) - v.doff;
+            v.piece0 = ps[b0];
+            v.piece1 = ps[b1];
+            for (int64_t b = b0; b < b1; ++b) chunk_of[b] = (int)io.size();
+            io.push_back(v);
+            b0 = b1;
+        }
+    };
+    std::vector<int> in_of, out_of;
+    partition((int)std::min<int64_t>(kMaxChunksIn, kmax), ch->in, in_of);
+    partition((int)std::min<int64_t>(kMaxChunksOut, kmax), ch->out, out_of);
+    if (ch->in.size() < 2 || ch->out.size() < 2) return;
     std::unordered_map<int64_t, int64_t> block_of_off;
     for (int64_t b = 0; b < nb; ++b) block_of_off[p->Vd.off[b]] = b;
     // with unit block scales the output needs no unscaling: phase 2 stores into
     // the compact layout (column-major blocks, ld = rows) and the unpack pass goes
     ch->compact_out = std::all_of(p->vscale.begin(), p->vscale.end(), [](double s) { return s == 1.0; });
     auto cut = [&](const PhasePlan& full, int ph, std::deque<PhasePlan>& hs, std::deque<DevPhase>& ds) {
+        const std::vector<int>& chunk_of = ph == 1 ? in_of : out_of;
+        const int kk = (int)(ph == 1 ? ch->in.size() : ch->out.size());
         std::vector<std::vector<GTile>> per(kk);
         for (const GTile& tl : full.tiles) {
             int64_t blk;
@@ -632,7 +650,7 @@ static void make_chunks(vmps_pivot* p, DevPlan& dp) {
             sp.transA = full.transA; sp.transB = full.transB; sp.transC = full.transC;
             sp.slotA = full.slotA; sp.slotB = full.slotB; sp.slotC = full.slotC;
             sp.tiles = std::move(per[c]);
-            schedule_tma(sp, p->ctx->num_sms);
+            schedule_tma(sp, p->ctx->num_sms, ph == 1 ? dp.plan.opY : dp.plan.opZ);
             validate_tma_schedule(sp, A);
             ds.emplace_back();
             ds.back().upload(sp, p->st());
@@ -640,12 +658,10 @@ static void make_chunks(vmps_pivot* p, DevPlan& dp) {
     };
     cut(dp.plan.p1, 1, ch->p1h, ch->p1);
     cut(dp.plan.p2, 2, ch->p2h, ch->p2);
-    ch->ev_in.resize(kk, nullptr);
-    ch->ev_out.resize(kk, nullptr);
-    for (int c = 0; c < kk; ++c) {
-        CK(cudaEventCreateWithFlags(&ch->ev_in[c], cudaEventDisableTiming));
-        CK(cudaEventCreateWithFlags(&ch->ev_out[c], cudaEventDisableTiming));
-    }
+    ch->ev_in.resize(ch->in.size(), nullptr);
+    ch->ev_out.resize(ch->out.size(), nullptr);
+    for (auto& ev : ch->ev_in) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    for (auto& ev : ch->ev_out) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ch->ev_start, cudaEventDisableTiming));
     dp.chunks = std::move(ch);
 }
@@ -666,12 +682,12 @@ static void hxv_host_pipelined(vmps_pivot* p, DevPlan& dp, const double* vin, do
     ops.Y = din;
     ops.O = ch.compact_out ? sout : dout;
     ops.err = p->ctx->err;
-    const int k = (int)ch.io.size();
+    const int kin = (int)ch.in.size(), kout = (int)ch.out.size();
     // the copy stream starts after everything already queued on the compute stream
     CK(cudaEventRecord(ch.ev_start, cs));
     CK(cudaStreamWaitEvent(xs, ch.ev_start, 0));
-    for (int c = 0; c < k; ++c) {
-        const VecChunk& v = ch.io[c];
+    for (int c = 0; c < kin; ++c) {
+        const VecChunk& v = ch.in[c];
         CK(cudaMemcpyAsync(sin + v.coff, vin + v.coff, (size_t)v.clen * 8, cudaMemcpyHostToDevice, xs));
         CK(cudaEventRecord(ch.ev_in[c], xs));
         CK(cudaStreamWaitEvent(cs, ch.ev_in[c], 0));
@@ -680,15 +696,15 @@ static void hxv_host_pipelined(vmps_pivot* p, DevPlan& dp, const double* vin, do
     }
     // phase 2 of chunk o is queued before the copy-out of chunk o-1, so that a
     // copy call that blocks the host (pageable memory) does not hold back compute
-    for (int o = 0; o <= k; ++o) {
-        if (o < k) {
-            const VecChunk& v = ch.io[o];
+    for (int o = 0; o <= kout; ++o) {
+        if (o < kout) {
+            const VecChunk& v = ch.out[o];
             run_phase_on(dp, 2, ch.p2[o], ch.p2h[o], ops, cs);
             if (!ch.compact_out) CK(launch_pack(pk + v.piece0, v.piece1 - v.piece0, dout, sout, 0, cs));
             CK(cudaEventRecord(ch.ev_out[o], cs));
         }
         if (o >= 1) {
-            const VecChunk& w = ch.io[o - 1];
+            const VecChunk& w = ch.out[o - 1];
             CK(cudaStreamWaitEvent(xs, ch.ev_out[o - 1], 0));
             CK(cudaMemcpyAsync(vout + w.coff, sout + w.coff, (size_t)w.clen * 8, cudaMemcpyDeviceToHost, xs));
         }

@@ -656,7 +656,13 @@ void sort_tiles(PhasePlan& ph) {
 }
 }  // namespace
 
-void schedule_tma(PhasePlan& ph, int ncta) {
+int32_t b_box_rows(int64_t outer, int tile_n) {
+    int64_t mx = 0;
+    for (const auto& r : split_extent(std::max<int64_t>(outer, 1), 8, tile_n)) mx = std::max(mx, r.second);
+    return (int32_t)std::min<int64_t>(((mx + 15) / 16) * 16, 256);
+}
+
+void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& B) {
     const size_t nt = ph.tiles.size();
     ph.steps.clear();
     ph.cta_tiles.assign(1, 0);
@@ -706,6 +712,7 @@ void schedule_tma(PhasePlan& ph, int ncta) {
                     st.row0 = t.row0;
                     st.col0 = t.col0;
                     st.flags = (seen_a.insert(am).second ? 1 : 0) | (seen_b.insert(bm).second ? 2 : 0);
+                    st.brows = B[bm].box;
                     ph.steps.push_back(st);
                 }
             }
@@ -988,7 +995,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         pb.scale = 1.0;
         P.prepX.push_back(pb);
         xp_idx[c.x] = (int32_t)P.opX.size();
-        P.opX.push_back(OpBlock{cur, (int32_t)m, (int32_t)k, (int32_t)ld, 0});
+        P.opX.push_back(OpBlock{cur, (int32_t)m, (int32_t)k, (int32_t)ld, tile_m});
         cur = pad_off(cur + ld * m);
     }
     P.Xp_total = std::max<int64_t>(cur, 32);
@@ -1018,7 +1025,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         pb.trans = transZ ? 1 : 0;   // op(Z) = Z: columns stay columns; op(Z) = Z^T: rows of Z become columns
         pb.scale = ch[i].c;
         P.prepZ.push_back(pb);
-        P.opZ.push_back(OpBlock{cur, (int32_t)p, (int32_t)n, (int32_t)ld, 0});
+        P.opZ.push_back(OpBlock{cur, (int32_t)p, (int32_t)n, (int32_t)ld, b_box_rows(p, tile_n)});
         chain_zp[i] = id;
         cur = pad_off(cur + ld * p);
     }
@@ -1039,7 +1046,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         ipairs.push_back({ch[i].x, ch[i].y});
         const int64_t m = xm(ch[i].x), n = Y.cols[ch[i].y], ld = pad_ld(n);
         T.off.push_back(cur); T.rows.push_back(m); T.cols.push_back(n); T.ld.push_back(ld);
-        P.opT.push_back(OpBlock{cur, (int32_t)m, (int32_t)n, (int32_t)ld, 0});
+        P.opT.push_back(OpBlock{cur, (int32_t)m, (int32_t)n, (int32_t)ld, tile_m});
         cur = pad_off(cur + ld * m);
         chain_t[i] = id;
     }
@@ -1048,7 +1055,8 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
 
     // the vector arena Y is split in place: its blocks are K (= rows) contiguous already
     for (size_t y = 0; y < Y.rows.size(); ++y)
-        P.opY.push_back(OpBlock{Y.off[y], (int32_t)Y.cols[y], (int32_t)Y.rows[y], (int32_t)Y.ld[y], 0});
+        P.opY.push_back(OpBlock{Y.off[y], (int32_t)Y.cols[y], (int32_t)Y.rows[y], (int32_t)Y.ld[y],
+                                b_box_rows(Y.cols[y], tile_n)});
 
     // phase 1: T_j = Xp[x] * Yp[y]   (A rows = m, B columns = n, K = k), stored transposed
     PhasePlan& p1 = P.p1;

@@ -21,33 +21,34 @@
 
 namespace vmps {
 namespace um {
-constexpr int BM = 128, BN = 64, BK = kUmmaBK, STAGES = 4;
+constexpr int BM = kUmmaTileM, BN = kUmmaTileN, BK = kUmmaBK, STAGES = 4;   // 128 x (<= 256) x 32
 constexpr int NT = 192;                                    // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
-constexpr int A_BYTES = BM * BK * 2;                       // one of A hi / A lo: 16 KB
-constexpr int B_BYTES = BN * BK * 2;                       // one of B hi / B lo: 8 KB
+constexpr int ROW_BYTES = BK * 2;                          // one K step of one row: 64 bytes
+constexpr int A_BYTES = BM * ROW_BYTES;                    // one of A hi / A lo: 8 KB
+constexpr int B_BYTES = BN * ROW_BYTES;                    // one of B hi / B lo, at most: 16 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;     // 48 KB
 constexpr int STAGE_OUT_BYTES = 4 * 8192;                  // split-output epilogue: 32 rows x 64 cols x hi/lo per warp
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGE_OUT_BYTES + 1024 + 256;
-constexpr uint32_t ACC_COLS = 64;                          // one FP32 accumulator: 128 lanes x 64 columns
-constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two, so an epilogue overlaps the next tile
+constexpr uint32_t ACC_COLS = BN;                          // one FP32 accumulator: 128 lanes x 256 columns
+constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two (all of TMEM), so an epilogue overlaps the next tile
 // kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1),
-// both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+// both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22 (per tile), M >> 4 in bits 24-28
+constexpr uint32_t IDESC_BASE = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BM >> 4) << 24);
 constexpr long long WAIT_BUDGET = 4000000000LL;           // clock cycles (~2 s) per barrier wait
 constexpr int LOOKAHEAD = STAGES;                          // descriptors acquired this many steps ahead
 }  // namespace um
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+// shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of one 32-element
+// K step), 8-row groups 512 B apart
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFFu);   // start address >> 4
     d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset between 8-row groups
+    d |= (uint64_t)(512 >> 4) << 32;           // stride byte offset between 8-row groups
     d |= (uint64_t)1 << 46;                    // descriptor version (tcgen05)
-    d |= (uint64_t)2 << 61;                    // 128-byte swizzle
+    d |= (uint64_t)4 << 61;                    // 64-byte swizzle
     return d;
 }
 
@@ -101,11 +102,12 @@ __device__ __forceinline__ void tmap_acquire(const void* tmap) {
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(tmap) : "memory");
 }
 
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t acc) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(um::IDESC), "r"(acc));
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
             const int st = it % STAGES, use = it / STAGES;
             if (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), s_fail)) break;
             const uint32_t sb = ring + st * STAGE_BYTES;
-            mbar_expect_tx(bar(st), STAGE_BYTES);
+            mbar_expect_tx(bar(st), (uint32_t)(2 * A_BYTES + 2 * s.brows * ROW_BYTES));
             tma_load_3d(sb, amaps + (size_t)s.amap * 128, s.k0, s.row0, 0, bar(st));
             tma_load_3d(sb + 2 * A_BYTES, bmaps + (size_t)s.bmap * 128, s.k0, s.col0, 0, bar(st));
         }
@@ -230,7 +232,10 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
         // ---------------- MMA issuer
         int it = 0, lt = 0;
         for (int t = t0; t < t1 && !*s_fail; ++t, ++lt) {
-            const int nsteps = g.tiles[t].nsteps;
+            const GTile tile = g.tiles[t];
+            const int nsteps = tile.nsteps;
+            const int brows = nsteps > 0 ? g.steps[tile.step0].brows : 16;
+            const uint32_t idesc = IDESC_BASE | ((uint32_t)(((tile.tn + 15) & ~15) >> 3) << 17);   // N = round16(tn)
             const int buf = lt & 1, buse = lt >> 1;
             if (buse >= 1 && !mbar_wait(bar(2 * STAGES + 2 + buf), (uint32_t)((buse - 1) & 1), s_fail)) break;
             tc_fence_after();
@@ -240,14 +245,14 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
                 if (!mbar_wait(bar(st), (uint32_t)(use & 1), s_fail)) break;
                 tc_fence_after();
                 const uint32_t sb = ring + st * STAGE_BYTES;
-                const uint64_t ah = sw128_desc(sb), al = sw128_desc(sb + A_BYTES);
-                const uint64_t bh = sw128_desc(sb + 2 * A_BYTES), bl = sw128_desc(sb + 2 * A_BYTES + B_BYTES);
+                const uint64_t ah = sw64_desc(sb), al = sw64_desc(sb + A_BYTES);
+                const uint64_t bh = sw64_desc(sb + 2 * A_BYTES), bl = sw64_desc(sb + 2 * A_BYTES + brows * ROW_BYTES);
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
                     const uint64_t adv = (uint64_t)(kk * 32) >> 4;   // 16 bf16 = 32 bytes along K
-                    umma_bf16(dacc, al + adv, bh + adv, (k | kk) != 0 ? 1u : 0u);
-                    umma_bf16(dacc, ah + adv, bl + adv, 1);
-                    umma_bf16(dacc, ah + adv, bh + adv, 1);
+                    umma_bf16(dacc, al + adv, bh + adv, idesc, (k | kk) != 0 ? 1u : 0u);
+                    umma_bf16(dacc, ah + adv, bl + adv, idesc, 1);
+                    umma_bf16(dacc, ah + adv, bh + adv, idesc, 1);
                 }
                 umma_commit(bar(STAGES + st));
             }
@@ -268,71 +273,79 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
             const bool ok = __all_sync(0xffffffffu, mbar_wait(bar(2 * STAGES + buf), (uint32_t)(buse & 1), s_fail));
             if (!ok) break;
             tc_fence_after();
-            uint32_t v[64];
-            if (tile.nsteps > 0) {
-                const uint32_t ta = tmem + ((uint32_t)(sp * 32) << 16) + (uint32_t)(buf * ACC_COLS);
-                tmem_ld16(ta, v);
-                tmem_ld16(ta + 16, v + 16);
-                tmem_ld16(ta + 32, v + 32);
-                tmem_ld16(ta + 48, v + 48);
-                tmem_wait_ld();
-                reg_fence16(v);
-                reg_fence16(v + 16);
-                reg_fence16(v + 32);
-                reg_fence16(v + 48);
-            } else {
+            const int ncols = tile.tn;
+#pragma unroll 1
+            for (int c0 = 0; c0 < ncols; c0 += 64) {
+                uint32_t v[64];
+                if (tile.nsteps > 0) {
+                    const uint32_t ta = tmem + ((uint32_t)(sp * 32) << 16) + (uint32_t)(buf * ACC_COLS + c0);
+                    tmem_ld16(ta, v);
+                    tmem_ld16(ta + 16, v + 16);
+                    tmem_ld16(ta + 32, v + 32);
+                    tmem_ld16(ta + 48, v + 48);
+                    tmem_wait_ld();
+                    reg_fence16(v);
+                    reg_fence16(v + 16);
+                    reg_fence16(v + 32);
+                    reg_fence16(v + 48);
+                } else {
 #pragma unroll
-                for (int i = 0; i < 64; ++i) v[i] = 0u;
-            }
-            // the accumulator is free once it sits in registers
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
-            if (OUT_SPLIT) {
-                // row-major bf16 hi / lo: stage 32 rows x 64 columns (chunk c of row r at
-                // r*128 + ((c ^ (r & 7)) << 4)), then store 4 whole 128-byte rows per instruction
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    uint32_t h[4], l[4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const float a = __uint_as_float(v[c * 8 + 2 * i]), b = __uint_as_float(v[c * 8 + 2 * i + 1]);
-                        const float ha = __bfloat162float(__float2bfloat16_rn(a));
-                        const float hb = __bfloat162float(__float2bfloat16_rn(b));
-                        h[i] = pack_bf16x2(a, b);
-                        l[i] = pack_bf16x2(a - ha, b - hb);
-                    }
-                    const int off = lane * 128 + ((c ^ (lane & 7)) << 4);
-                    *reinterpret_cast<uint4*>(so + off) = make_uint4(h[0], h[1], h[2], h[3]);
-                    *reinterpret_cast<uint4*>(so + 4096 + off) = make_uint4(l[0], l[1], l[2], l[3]);
+                    for (int i = 0; i < 64; ++i) v[i] = 0u;
                 }
-                __syncwarp();
-                __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
-                __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
-                const int c = lane & 7;
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int row = i * 4 + (lane >> 3);
-                    const int off = row * 128 + ((c ^ (row & 7)) << 4);
-                    const uint4 hv = *reinterpret_cast<const uint4*>(so + off);
-                    const uint4 lv = *reinterpret_cast<const uint4*>(so + 4096 + off);
-                    if (sp * 32 + row < tile.tm && c * 8 < tile.tn) {
-                        const int64_t e = tile.c_off + (int64_t)(tile.row0 + sp * 32 + row) * tile.ldc + tile.col0 + c * 8;
-                        *reinterpret_cast<uint4*>(Ch + e) = hv;
-                        *reinterpret_cast<uint4*>(Cl + e) = lv;
-                    }
+                if (c0 + 64 >= ncols) {
+                    // the accumulator is free once its last columns sit in registers
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
                 }
-                __syncwarp();   // the staging area is rewritten by the next tile
-            } else {
-                double* C = (double*)g.C;
-                if (rl < tile.tm) {
-                    const int64_t gr = tile.row0 + rl;
+                const int tn = ncols - c0 < 64 ? ncols - c0 : 64;   // columns of this chunk
+                const int col0 = tile.col0 + c0;
+                if (OUT_SPLIT) {
+                    // row-major bf16 hi / lo: stage 32 rows x 64 columns (chunk c of row r at
+                    // r*128 + ((c ^ (r & 7)) << 4)), then store 4 whole 128-byte rows per instruction
 #pragma unroll
-                    for (int j = 0; j < 64; ++j) {
-                        if (j < tile.tn) {
-                            const int64_t gc = tile.col0 + j;
-                            C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] =
-                                f32_to_f64(__uint_as_float(v[j]));
+                    for (int c = 0; c < 8; ++c) {
+                        uint32_t h[4], l[4];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const float a = __uint_as_float(v[c * 8 + 2 * i]), b = __uint_as_float(v[c * 8 + 2 * i + 1]);
+                            const float ha = __bfloat162float(__float2bfloat16_rn(a));
+                            const float hb = __bfloat162float(__float2bfloat16_rn(b));
+                            h[i] = pack_bf16x2(a, b);
+                            l[i] = pack_bf16x2(a - ha, b - hb);
+                        }
+                        const int off = lane * 128 + ((c ^ (lane & 7)) << 4);
+                        *reinterpret_cast<uint4*>(so + off) = make_uint4(h[0], h[1], h[2], h[3]);
+                        *reinterpret_cast<uint4*>(so + 4096 + off) = make_uint4(l[0], l[1], l[2], l[3]);
+                    }
+                    __syncwarp();
+                    __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
+                    __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
+                    const int c = lane & 7;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int row = i * 4 + (lane >> 3);
+                        const int off = row * 128 + ((c ^ (row & 7)) << 4);
+                        const uint4 hv = *reinterpret_cast<const uint4*>(so + off);
+                        const uint4 lv = *reinterpret_cast<const uint4*>(so + 4096 + off);
+                        if (sp * 32 + row < tile.tm && c * 8 < tn) {
+                            const int64_t e = tile.c_off + (int64_t)(tile.row0 + sp * 32 + row) * tile.ldc + col0 + c * 8;
+                            *reinterpret_cast<uint4*>(Ch + e) = hv;
+                            *reinterpret_cast<uint4*>(Cl + e) = lv;
+                        }
+                    }
+                    __syncwarp();   // the staging area is rewritten by the next chunk
+                } else {
+                    double* C = (double*)g.C;
+                    if (rl < tile.tm) {
+                        const int64_t gr = tile.row0 + rl;
+#pragma unroll
+                        for (int j = 0; j < 64; ++j) {
+                            if (j < tn) {
+                                const int64_t gc = col0 + j;
+                                C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] =
+                                    f32_to_f64(__uint_as_float(v[j]));
+                            }
                         }
                     }
                 }
