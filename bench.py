@@ -320,13 +320,14 @@ def main():
     t_phase = ms2 if phase == "phase2" else ms1
     tensor_flops = 3.0 * flops_phase / (t_phase * 1e-3) / 1e12     # bf16 tensor-core flops issued
     prof = None
-    pf = os.path.join(ROOT, "profiles", "gg_split_hubbard_D4096.json")
+    engine = "gg_split_kernel" if os.environ.get("VMPS_SPLIT_ENGINE") == "mma" else "gg_umma_kernel"
+    pf = os.path.join(ROOT, "profiles", f"{engine}_hubbard_D4096.json")
     if os.path.exists(pf):
         with open(pf) as f:
             prof = json.load(f)
     roofline = {"bound": "tensor", "achieved": tensor_flops, "peak": bf16, "unit": "TFLOP/s",
                 "frac": tensor_flops / bf16, "traffic": (prof or {}).get(f"traffic_{phase}"),
-                "kernel": f"gg_split_kernel ({phase})", "peak_source": f"bf16_tflops of {peak_kind}",
+                "kernel": f"{engine} ({phase})", "peak_source": f"bf16_tflops of {peak_kind}",
                 "useful_tflops": flops_phase / (t_phase * 1e-3) / 1e12,
                 "note": "3 bf16 products per useful FMA (hi*hi + hi*lo + lo*hi)"}
 
@@ -351,9 +352,9 @@ def main():
                        "U": 4.0, "seed": args.seed, "D_left": info["D_left"], "sectors": info["sectors_left"],
                        "dim_V": n, "parallelism": "replicas" if world > 1 else "single",
                        "l2": l2_note, "working_set_MB": round(working_set / 2 ** 20, 1),
-                       "graph": "CUDA graph per HxV (2 grouped-GEMM launches)"},
+                       "graph": "CUDA graph per HxV (vector split + 2 grouped-GEMM launches)"},
             "e2e": {"value": e2e, "unit": "HxV/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": (3 if args.precision == "bf16x3" else 2) * args.steps,
             "fp64": {"value": world * 1000.0 / ms64, "unit": "HxV/s", "ms_per_step": ms64,
                      "phase2_ms": ms64_2, "flops_executed": st64["flops_executed"]},
             "split_over_fp64": ms64 / ms,

@@ -119,6 +119,10 @@ typedef struct {
     double  flops_phase2_unsummed; /* second stage without summing first-stage products    */
     int32_t association;      /* 0: (X*Y)*Z first, 1: X*(Y*Z) first                      */
     int32_t reserved;
+    /* split precision: bf16 tensor-core flops the MMAs issue per phase, tile
+     * padding included (3 products x 2 x 128 x round16(tile width) x 32 per K step) */
+    double  tensor_flops_phase1;
+    double  tensor_flops_phase2;
 } vmps_plan_stats;
 
 typedef struct vmps_ctx_s   vmps_ctx;

@@ -52,7 +52,8 @@ class vmps_plan_stats(C.Structure):
                 ("bytes_algorithmic", C.c_double), ("bytes_intermediate", C.c_double),
                 ("n_segments_phase2", C.c_int64), ("n_terms_phase2", C.c_int64),
                 ("flops_phase2_unsummed", C.c_double),
-                ("association", C.c_int32), ("reserved", C.c_int32)]
+                ("association", C.c_int32), ("reserved", C.c_int32),
+                ("tensor_flops_phase1", C.c_double), ("tensor_flops_phase2", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

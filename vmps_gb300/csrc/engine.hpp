@@ -136,30 +136,56 @@ DevLayout make_dev_layout(const std::vector<int64_t>& rows, const std::vector<in
 struct GTerm { int64_t off; double coef; };
 struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, K, pad; };
 // one output tile: rows [row0, row0+tm) x cols [col0, col0+tn) of a block
-// (tcgen05 engine: step0 / nsteps index its K steps in PhasePlan::steps)
-struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, step0, nsteps; };
-// one K step of the tcgen05 engine: TMA descriptors of A and B, the K offset in
-// the segment and the tile origin; flags bit 0 / bit 1: first use of the A / B
-// descriptor by this CTA (acquire it for the tensor-map proxy); brows: rows of
-// the B box (the tile's MMA N, a multiple of 16, is at most this)
-struct TStep { int32_t amap, bmap, k0, row0, col0, flags, brows, pad; };
-constexpr int kUmmaBK = 32;   // K extent of one tcgen05 engine step
-// at most this many A terms per segment (the kernels stage them in shared memory)
+// (split plans: step0 / nsteps index its K steps in PhasePlan::steps)
+struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, step0, nsteps, pad0, pad1; };
+// at most this many A terms per segment (the FP64 kernel stages them in shared memory)
 constexpr int kMaxTerms = 16;
-// tile edges (rows split on multiples of 16, columns on multiples of 8):
-// mma.sync engines at most 64 x 64, the tcgen05 engine at most 128 x 64
+// FP64 engine tiles are at most 64 x 64 (rows split on multiples of 16, columns
+// on multiples of 8); tcgen05 engine tiles at most 128 x 256
 constexpr int kTileMax = 64;
 constexpr int kUmmaTileM = 128, kUmmaTileN = 256;
+constexpr int kUmmaBK = 32;   // K extent of one tcgen05 engine step
+
+// ---------------------------------------------------------------------------
+// Split-precision operand panels
+// ---------------------------------------------------------------------------
+// Every split operand lives in one bf16 arena made of "class panels".  Blocks
+// with the same padded contraction length kpad (panel_kpad(K)) are stacked as
+// consecutive rows of one row-major matrix whose rows are kpad/32 chunks of
+// [32 hi | 32 lo] elements, so row pitch = 2*kpad elements:
+//     element (row i, k) of a block:  hi at off + i*pitch + (k/32)*64 + k%32,
+//                                     lo at the same position + 32.
+// One 128-byte row segment holds the hi and lo halves of one 32-wide K step,
+// which is exactly one TMA request per row and one 128-byte-swizzled row of the
+// tensor-core operand.  Padding (k >= K) is zero.
+int32_t panel_kpad(int64_t K);
+struct PanelClass { int32_t kpad; int64_t base, rows; };   // base: element offset; rows: stacked rows
+struct PanelArena {
+    std::vector<PanelClass> cls;
+    int64_t total = 0;                                      // elements (hi and lo together)
+};
+// a block of a panel arena: `outer` rows of contraction length K, at row `row`
+// of class `cls`; off = element offset of its row 0, pitch = 2*kpad of the class
+struct OpBlock { int64_t off; int32_t outer, K, cls, row, pitch, pad; };
+
+// one K step of the tcgen05 engine: TMA descriptors (indices into the phase's
+// descriptor lists) of A and B, x = 2*k0 (column of the [hi|lo] panel), the
+// panel rows the A and B boxes start at, and the box heights
+struct TStep { int32_t amap, bmap, x, ay, by, arows, brows, pad; };
+// a TMA descriptor of a phase: box of `rows` rows over the panel matrix of class `cls`
+struct MapKey { int32_t cls, rows; };
+constexpr int kMaxMapsA = 64, kMaxMapsB = 128;
 
 struct PhasePlan {
     std::vector<GTerm> terms;
     std::vector<GSeg>  segs;
     std::vector<GTile> tiles;
-    // split plans: per segment, the prepared-operand block of A and of B (TMA descriptor index)
+    // split plans: per segment, the A and B operand block (OpBlock index)
     std::vector<int32_t> seg_amap, seg_bmap;
-    // tcgen05 engine schedule (schedule_tma): K steps, and the tiles of CTA b are
-    // tiles[cta_tiles[b] .. cta_tiles[b+1])
+    // tcgen05 engine schedule (schedule_tma): K steps, descriptors, and the tiles
+    // of CTA b are tiles[cta_tiles[b] .. cta_tiles[b+1])
     std::vector<TStep> steps;
+    std::vector<MapKey> amaps, bmaps;
     std::vector<int32_t> cta_tiles;
     int ncta = 0;
     bool transA = false, transB = false, transC = false;
@@ -169,45 +195,40 @@ struct PhasePlan {
 
 enum Slot { SLOT_X = 0, SLOT_Y = 1, SLOT_Z = 2, SLOT_OUT = 3, SLOT_T = 4 };
 
-// A prepared split-precision operand block: `outer` rows (rows of A / columns of
-// B) of K contiguous elements, row stride ld, at element offset off of its
-// [hi | lo] arena (lo half at +total); box: rows of its TMA box (tcgen05 engine)
-struct OpBlock { int64_t off; int32_t outer, K, ld, box; };
-
 // Split-precision operand preparation: one block of a column-major FP64 source
-// (rows x cols, leading dimension src_ld) written as bf16 hi/lo pairs in the
-// K-contiguous layout the tensor-core kernels read.  trans = 0: destination row
-// j holds source column j; trans = 1: destination row i holds source row i.
+// (rows x cols, leading dimension src_ld) written into its panel (dst_off,
+// dst_ld = panel pitch).  trans = 0: panel row j holds source column j (K runs
+// down the column); trans = 1: panel row i holds source row i.
 struct PrepBlock { int64_t src_off, dst_off; int32_t src_ld, dst_ld, rows, cols, trans, pad; double scale; };
 
 struct Plan {
     PhasePlan p1, p2;
-    DevLayout T;               // intermediate arena layout
+    DevLayout T;               // FP64 plans: intermediate arena layout
     int association = 0;       // 0: T = op(X)*Y first; 1: U = Y*op(Z) first
     int64_t n_chains = 0, n_intermediates = 0, n_out_blocks = 0;
     double flops_merged = 0, bytes_alg = 0;
     double flops_p2_unsummed = 0;
     // split-precision plans only
     bool split = false;
-    int split_kernel = 0;                         // 0: mma.sync engine, 1: tcgen05 engine
-    int64_t Xp_total = 0, Zp_total = 0;           // prepared-operand arena sizes (elements)
+    PanelArena ax, ay, at, az;                    // panels of op(X), Y, T = op(X)Y, c*op(Z)
     std::vector<PrepBlock> prepX, prepZ;          // X blocks, and c*op(Z) copies
-    std::vector<OpBlock> opX, opY, opZ, opT;      // prepared blocks of each arena
+    std::vector<OpBlock> opX, opY, opZ, opT;      // blocks of each panel arena
 };
 // FP64 plan: two phases, the second sums first-stage products on the fly
 Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
                const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n);
-// split-precision plan: every operand pre-split into K-contiguous bf16 hi/lo
-// copies; the chain coefficient rides on a scaled copy of op(Z); the second
-// phase is a K-concatenation over chains
-// Static schedule of a split phase for the persistent tcgen05 engine on ncta
-// CTAs: K steps of kUmmaBK per segment, tiles assigned longest-first to the
-// least-loaded CTA and stored CTA by CTA.
-void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& B);
-// rows of the TMA box of a B operand block with `outer` rows, tiled by
-// split_extent(outer, 8, tile_n): the largest tile extent rounded up to 16
-int32_t b_box_rows(int64_t outer, int tile_n);
+// Split-precision plan for the tcgen05 engine: op(X), Y and the chain-scaled
+// copies c*op(Z) in panels; phase 1 computes the intermediates T = op(X)Y into
+// panels, phase 2 the outputs as K-concatenations over chains.
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n);
+                     const DevLayout& O, bool transX, bool transZ);
+// Static schedule of a split phase for the persistent tcgen05 engine on ncta
+// CTAs: K steps of kUmmaBK per segment with their TMA boxes, tiles assigned
+// longest-first to the least-loaded CTA and stored CTA by CTA.
+void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B);
+// TMA box heights: A boxes 16/32/64/128 rows, B boxes a multiple of 32 up to
+// 256 (16 for the narrowest), the smallest that covers the tile
+int32_t box_rows_a(int32_t tm);
+int32_t box_rows_b(int32_t tn);
 
 }  // namespace vmps

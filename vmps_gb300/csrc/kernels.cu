@@ -3,9 +3,9 @@
 // gg_fp64  : grouped GEMM, FP64 operands, DMMA (mma.sync m8n8k4 f64) -- the
 //            plain drop-in form, bit-for-bit the same arithmetic type as the
 //            Eigen path of pivot/DmrgPivotMatrix1.h:236-262.
-// gg_split : grouped GEMM, operands split into bf16 hi/lo on the fly while
-//            staging to shared memory, hi*hi + hi*lo + lo*hi products on the
-//            tensor cores (mma.sync m16n8k16 bf16, FP32 accumulate).
+// The split-precision (BF16x3) grouped GEMM is the tcgen05 engine in
+// umma.cu; this file holds its operand preparation (FP64 -> bf16 hi/lo
+// panels) and the vector kernels.
 //
 // Work layout (planned on the host, engine.hpp): every CTA owns one output tile
 // and loops over that tile's segments; a segment is one GEMM of K columns
@@ -24,26 +24,14 @@
 namespace vmps {
 
 // ---------------------------------------------------------------------------
-// operand access helpers
-// ---------------------------------------------------------------------------
-// ---------------------------------------------------------------------------
-// Operand staging.  Device blocks are column-major with ld a multiple of 8,
-// start offsets aligned to 32 elements and zero padding, and tile origins are
-// multiples of 16 (rows) / 8 (columns), so every 4-element group read below is
-// 16-byte aligned and stays inside its block's padded storage.  Groups whose
+// Operand staging of the FP64 engine.  Device blocks are column-major with ld a
+// multiple of 8, start offsets aligned to 32 elements and zero padding, and tile
+// origins are multiples of 16 (rows) / 8 (columns), so every 2-element (16-byte)
+// group read below is aligned and stays inside its block's padded storage.  Groups whose
 // first element lies outside the tile are replaced by zeros; elements past the
 // block edge inside a group are either zero padding or rows/columns that only
 // reach output entries the epilogue masks off.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void ldg4(const float* p, float (&v)[4]) {
-    const float4 x = __ldg(reinterpret_cast<const float4*>(p));
-    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
-}
-__device__ __forceinline__ void ldg4(const double* p, float (&v)[4]) {
-    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
-    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
-    v[0] = (float)a.x; v[1] = (float)a.y; v[2] = (float)b.x; v[3] = (float)b.y;
-}
 __device__ __forceinline__ void ldg2(const double* p, double (&v)[2]) {
     const double2 a = __ldg(reinterpret_cast<const double2*>(p));
     v[0] = a.x; v[1] = a.y;
@@ -192,211 +180,68 @@ __global__ void __launch_bounds__(f64k::NT, 3) gg_fp64_kernel(GGArgs g) {
             }
 }
 
-// ===========================================================================
-// BF16x3 split-precision grouped GEMM on pre-split operands.
-//   A: M x K, B: K x N, both stored K-contiguous as separate bf16 hi and lo
-//   arrays (rows of A / columns of B padded to a multiple of 8 with zeros).
-//   Tile <= 64 x 64, 128 threads (2 x 2 warps of 32 x 32), BK = 32, 3-stage
-//   cp.async pipeline; hi*hi + hi*lo + lo*hi products on mma.sync m16n8k16
-//   bf16 with FP32 accumulation.
-// ===========================================================================
-namespace sp3 {
-constexpr int BM = 64, BN = 64, BK = 32, NT = 128, STAGES = 3;
-constexpr int LDS = BK + 8;              // 80-byte shared rows: conflict-free ldmatrix
-constexpr int PART = BM * LDS;           // one of Ahi, Alo, Bhi, Blo
-constexpr int STAGE = 4 * PART;
-constexpr int SMEM_BYTES = STAGES * STAGE * 2;
+// ---------------------------------------------------------------------------
+// split-precision panels (engine.hpp): element k of panel row i at
+// i*pitch + (k/32)*64 + k%32 (hi) and + 32 (lo)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int panel_pos(int k) { return ((k >> 5) << 6) | (k & 31); }
+
+// v -> bf16 hi = bf16(v), lo = bf16(v - hi)
+__device__ __forceinline__ void split_store(__nv_bfloat16* row, int k, float v) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    const int p = panel_pos(k);
+    row[p] = h;
+    row[p + 32] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, uint32_t addr) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(addr));
-}
-__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
-    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int src_bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(src_bytes));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
-}
-
-template <int OUT_SPLIT>
-__global__ void __launch_bounds__(sp3::NT, 3) gg_split_kernel(GGArgs g) {
-    using namespace sp3;
-    extern __shared__ __align__(128) unsigned char smraw[];
-    __nv_bfloat16* sm = reinterpret_cast<__nv_bfloat16*>(smraw);
-    const GTile tile = g.tiles[blockIdx.x];
-    const __nv_bfloat16* __restrict__ Ah = (const __nv_bfloat16*)g.A;
-    const __nv_bfloat16* __restrict__ Al = (const __nv_bfloat16*)g.A2;
-    const __nv_bfloat16* __restrict__ Bh = (const __nv_bfloat16*)g.B;
-    const __nv_bfloat16* __restrict__ Bl = (const __nv_bfloat16*)g.B2;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-    const int mrem = tile.tm, nrem = tile.tn;
-
-    int nsteps = 0;
-    for (int s = tile.seg_begin; s < tile.seg_end; ++s) nsteps += (g.segs[s].K + BK - 1) / BK;
-
-    // producer cursor
-    int lseg = tile.seg_begin, lk0 = 0;
-    GSeg lsg{};
-    int64_t laoff = 0;
-    if (lseg < tile.seg_end) { lsg = g.segs[lseg]; laoff = g.terms[lsg.term_begin].off; }
-    // 1024 16-byte chunks per stage (4 parts x 64 rows x 4 chunks): 8 per thread
-    auto load_step = [&](int stage) {
-        if (lseg < tile.seg_end) {
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                const int c = tid + NT * r;
-                const int part = c >> 8, row = (c >> 2) & 63, kc = c & 3;
-                const int k = lk0 + kc * 8;
-                const bool isA = part < 2;
-                const bool ok = (isA ? row < mrem : row < nrem) && k < lsg.K;
-                const __nv_bfloat16* base = part == 0 ? Ah : part == 1 ? Al : part == 2 ? Bh : Bl;
-                const __nv_bfloat16* src =
-                    isA ? base + laoff + (int64_t)(tile.row0 + (ok ? row : 0)) * lsg.lda + (ok ? k : 0)
-                        : base + lsg.b_off + (int64_t)(tile.col0 + (ok ? row : 0)) * lsg.ldb + (ok ? k : 0);
-                const uint32_t dst = smem_u32(sm + stage * STAGE + part * PART + row * LDS + kc * 8);
-                cp_async16(dst, src, ok ? 16 : 0);
-            }
-            lk0 += BK;
-            if (lk0 >= lsg.K) {
-                lk0 = 0;
-                if (++lseg < tile.seg_end) { lsg = g.segs[lseg]; laoff = g.terms[lsg.term_begin].off; }
-            }
-        }
-        cp_async_commit();
-    };
-
-    float acc[2][4][4];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
-
-    const bool warp_live = wm < mrem && wn < nrem;
-#pragma unroll
-    for (int s = 0; s < STAGES - 1; ++s) load_step(s);
-    for (int step = 0; step < nsteps; ++step) {
-        cp_async_wait<STAGES - 2>();
-        __syncthreads();
-        load_step((step + STAGES - 1) % STAGES);
-        if (warp_live) {
-            const __nv_bfloat16* st = sm + (step % STAGES) * STAGE;
-            const __nv_bfloat16 *sAh = st, *sAl = st + PART, *sBh = st + 2 * PART, *sBl = st + 3 * PART;
-#pragma unroll
-            for (int kk = 0; kk < BK; kk += 16) {
-                uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
-#pragma unroll
-                for (int mi = 0; mi < 2; ++mi) {
-                    const int off = (wm + mi * 16 + (lane & 15)) * LDS + kk + (lane >> 4) * 8;
-                    ldsm_x4(ah[mi][0], ah[mi][1], ah[mi][2], ah[mi][3], smem_u32(sAh + off));
-                    ldsm_x4(al[mi][0], al[mi][1], al[mi][2], al[mi][3], smem_u32(sAl + off));
-                }
-#pragma unroll
-                for (int np = 0; np < 2; ++np) {
-                    const int off = (wn + np * 16 + (lane & 7) + ((lane >> 4) << 3)) * LDS + kk + ((lane >> 3) & 1) * 8;
-                    ldsm_x4(bh[2 * np][0], bh[2 * np][1], bh[2 * np + 1][0], bh[2 * np + 1][1], smem_u32(sBh + off));
-                    ldsm_x4(bl[2 * np][0], bl[2 * np][1], bl[2 * np + 1][0], bl[2 * np + 1][1], smem_u32(sBl + off));
-                }
-                // small cross terms first, then hi*hi; independent accumulators in between
-#pragma unroll
-                for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-                    for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], al[mi], bh[ni][0], bh[ni][1]);
-#pragma unroll
-                for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-                    for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], ah[mi], bl[ni][0], bl[ni][1]);
-#pragma unroll
-                for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-                    for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], ah[mi], bh[ni][0], bh[ni][1]);
-            }
-        }
-    }
-    cp_async_wait<0>();
-
-    // epilogue: c0,c1 -> (g, 2t..2t+1), c2,c3 -> (g+8, 2t..2t+1)
-    const int g4 = lane >> 2, t4 = lane & 3;
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-        for (int ni = 0; ni < 4; ++ni)
-#pragma unroll
-            for (int hh = 0; hh < 2; ++hh) {
-                const int r = wm + mi * 16 + g4 + hh * 8, c = wn + ni * 8 + t4 * 2;
-                if (r >= mrem) continue;
-                const float v0 = acc[mi][ni][2 * hh], v1 = acc[mi][ni][2 * hh + 1];
-                const int64_t gr = tile.row0 + r, gc = tile.col0 + c;
-                if (OUT_SPLIT) {
-                    __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
-                    __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
-                    const __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
-                    const __nv_bfloat16 l0 = __float2bfloat16_rn(v0 - __bfloat162float(h0));
-                    const __nv_bfloat16 l1 = __float2bfloat16_rn(v1 - __bfloat162float(h1));
-                    if (g.transC) {   // row-major: the two columns are adjacent
-                        const int64_t e = gc + gr * tile.ldc;
-                        if (c + 1 < nrem) {
-                            *reinterpret_cast<__nv_bfloat162*>(Ch + tile.c_off + e) = __halves2bfloat162(h0, h1);
-                            *reinterpret_cast<__nv_bfloat162*>(Cl + tile.c_off + e) = __halves2bfloat162(l0, l1);
-                        } else if (c < nrem) {
-                            Ch[tile.c_off + e] = h0;
-                            Cl[tile.c_off + e] = l0;
-                        }
-                    } else {
-                        if (c < nrem) { const int64_t e = gr + gc * tile.ldc; Ch[tile.c_off + e] = h0; Cl[tile.c_off + e] = l0; }
-                        if (c + 1 < nrem) { const int64_t e = gr + (gc + 1) * tile.ldc; Ch[tile.c_off + e] = h1; Cl[tile.c_off + e] = l1; }
-                    }
-                } else {
-                    double* C = (double*)g.C;
-                    if (c < nrem) {
-                        const int64_t e = g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc);
-                        C[tile.c_off + e] = (double)v0;
-                    }
-                    if (c + 1 < nrem) {
-                        const int64_t e = g.transC ? (gc + 1 + gr * tile.ldc) : (gr + (gc + 1) * tile.ldc);
-                        C[tile.c_off + e] = (double)v1;
-                    }
-                }
-            }
-}
-
-// operand preparation: scale, split into bf16 hi/lo, write K-contiguous
+// operand preparation: scale, split into bf16 hi/lo, write the block's panel rows
 __global__ void prep_kernel(const PrepBlock* __restrict__ pbs, int nb, const double* __restrict__ src,
-                            __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+                            __nv_bfloat16* __restrict__ dst) {
     for (int b = blockIdx.x; b < nb; b += gridDim.x) {
         const PrepBlock pb = pbs[b];
-        const int64_t n = (int64_t)pb.rows * pb.cols;
-        for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
-            const int64_t i = e % pb.rows, j = e / pb.rows;
-            const float v = (float)(pb.scale * src[pb.src_off + i + j * pb.src_ld]);
-            const int64_t d = pb.trans ? (pb.dst_off + i * pb.dst_ld + j) : (pb.dst_off + j * pb.dst_ld + i);
-            const __nv_bfloat16 h = __float2bfloat16_rn(v);
-            hi[d] = h;
-            lo[d] = __float2bfloat16_rn(v - __bfloat162float(h));
+        const int rows = pb.rows, n = pb.rows * pb.cols;
+        const bool unit = pb.scale == 1.0;
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int j = e / rows, i = e - j * rows;   // source (i, j), column-major
+            const double x = src[pb.src_off + i + (int64_t)j * pb.src_ld];
+            const float v = f64_to_f32_rn(unit ? x : pb.scale * x);
+            // trans = 1: panel row i, K index j;  trans = 0: panel row j, K index i
+            const int r = pb.trans ? i : j, k = pb.trans ? j : i;
+            split_store(dst + pb.dst_off + (int64_t)r * pb.dst_ld, k, v);
         }
     }
 }
-// elementwise split of a whole arena (same layout in and out)
-__global__ void split_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ hi,
-                             __nv_bfloat16* __restrict__ lo, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float v = f64_to_f32_rn(src[i]);
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        hi[i] = h;
-        lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+
+// column pieces of a column-major FP64 source into panels: column c of the
+// piece is panel row c, its element r is K index r; four loads in flight
+__global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np, const double* __restrict__ src,
+                                   __nv_bfloat16* __restrict__ dst) {
+    for (int b = blockIdx.x; b < np; b += gridDim.x) {
+        const PanelPiece pc = pieces[b];
+        const int rows = pc.rows, n = pc.rows * pc.cols;
+        const double* s = src + pc.src_off;
+        __nv_bfloat16* d = dst + pc.dst_off;
+        const bool unit = pc.scale == 1.0;
+        for (int e0 = threadIdx.x; e0 < n; e0 += 4 * blockDim.x) {
+            double x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * blockDim.x;
+                if (e < n) {
+                    const int c = e / rows, r = e - c * rows;
+                    x[u] = s[r + c * pc.src_ld];
+                } else {
+                    x[u] = 0.0;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * blockDim.x;
+                if (e >= n) break;
+                const int c = e / rows, r = e - c * rows;
+                split_store(d + (int64_t)c * pc.dst_pitch, r, f64_to_f32_rn(unit ? x[u] : pc.scale * x[u]));
+            }
+        }
     }
 }
 
@@ -434,40 +279,6 @@ __global__ void pack_kernel(const PackBlock* blocks, int nb, const double* __res
     }
 }
 
-
-// compact vector -> padded bf16 hi / lo arena in one pass: the padded FP64
-// vector that pack_kernel followed by split_kernel would go through is never
-// stored, and each element gets the same value (scale * x rounded to float,
-// then hi = bf16(v), lo = bf16(v - hi))
-__global__ void pack_split_kernel(const PackBlock* blocks, int nb, const double* __restrict__ src,
-                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
-    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-        const PackBlock pb = blocks[b];
-        const int rows = (int)pb.rows, n = (int)(pb.rows * pb.cols), ld = (int)pb.ld;
-        const double* s = src + pb.coff;
-        __nv_bfloat16* h = hi + pb.doff;
-        __nv_bfloat16* l = lo + pb.doff;
-        const bool unit = pb.scale == 1.0;
-        for (int e0 = threadIdx.x; e0 < n; e0 += 4 * blockDim.x) {
-            double x[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int e = e0 + u * blockDim.x;
-                x[u] = e < n ? s[e] : 0.0;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int e = e0 + u * blockDim.x;
-                if (e >= n) break;
-                const int c = e / rows, r = e - c * rows;
-                const float v = f64_to_f32_rn(unit ? x[u] : pb.scale * x[u]);
-                const __nv_bfloat16 vh = __float2bfloat16_rn(v);
-                h[r + c * ld] = vh;
-                l[r + c * ld] = __float2bfloat16_rn(v - __bfloat162float(vh));
-            }
-        }
-    }
-}
 
 // partial dot products: fixed chunking -> deterministic two-pass reduction
 constexpr int kDotThreads = 256;
@@ -570,13 +381,7 @@ static int grid_for(int64_t n, int threads, int cap) {
 
 // opt the split kernels into their dynamic shared memory size (once per process,
 // before any launch or stream capture)
-cudaError_t kernels_init() {
-    cudaError_t e = cudaFuncSetAttribute(gg_split_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp3::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(gg_split_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sp3::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    return umma_init();
-}
+cudaError_t kernels_init() { return umma_init(); }
 
 cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
@@ -584,31 +389,17 @@ cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_gg_split(int out_split, const GGArgs& a, cudaStream_t st) {
-    if (a.ntiles <= 0) return cudaSuccess;
-    if (out_split) gg_split_kernel<1><<<a.ntiles, sp3::NT, sp3::SMEM_BYTES, st>>>(a);
-    else gg_split_kernel<0><<<a.ntiles, sp3::NT, sp3::SMEM_BYTES, st>>>(a);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* hi, void* lo, cudaStream_t st) {
+cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* dst, cudaStream_t st) {
     if (nb <= 0) return cudaSuccess;
-    if (!pb || !src || !hi || !lo) return cudaErrorInvalidValue;
-    prep_kernel<<<min(nb, 8192), 256, 0, st>>>(pb, nb, src, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo);
+    if (!pb || !src || !dst) return cudaErrorInvalidValue;
+    prep_kernel<<<min(nb, 8192), 256, 0, st>>>(pb, nb, src, (__nv_bfloat16*)dst);
     return cudaGetLastError();
 }
 
-cudaError_t launch_split(const double* src, void* hi, void* lo, int64_t n, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    if (!src || !hi || !lo) return cudaErrorInvalidValue;
-    split_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(src, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo, n);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_pack_split(const PackBlock* blocks, int nb, const double* src, void* hi, void* lo, cudaStream_t st) {
-    if (nb <= 0) return cudaSuccess;
-    if (!blocks || !src || !hi || !lo) return cudaErrorInvalidValue;
-    pack_split_kernel<<<min(nb, 4096), 256, 0, st>>>(blocks, nb, src, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo);
+cudaError_t launch_panel_split(const PanelPiece* pieces, int np, const double* src, void* dst, cudaStream_t st) {
+    if (np <= 0) return cudaSuccess;
+    if (!pieces || !src || !dst) return cudaErrorInvalidValue;
+    panel_split_kernel<<<min(np, 4096), 256, 0, st>>>(pieces, np, src, (__nv_bfloat16*)dst);
     return cudaGetLastError();
 }
 

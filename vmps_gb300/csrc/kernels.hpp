@@ -1,5 +1,6 @@
 // Host-callable launchers of kernels.cu
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "engine.hpp"
@@ -10,14 +11,8 @@ struct GGArgs {
     const void* A;
     const void* B;
     void* C;
-    const void* A2;   // split precision: lo halves of A, B (hi in A, B)
-    const void* B2;
-    void* C2;         // split precision with a split output: lo half of C
     int* err;         // device error word: bit 0 = a bounded wait ran out (tcgen05 engine)
-    // tcgen05 engine: TMA descriptors (128 bytes each) of the prepared A / B blocks,
-    // the K steps and the per-CTA tile ranges of the schedule (ncta CTAs)
-    const void* amaps;
-    const void* bmaps;
+    // tcgen05 engine: the K steps and the per-CTA tile ranges of the schedule (ncta CTAs)
     const TStep* steps;
     const int32_t* cta_tiles;
     int ncta;
@@ -28,21 +23,30 @@ struct GGArgs {
     int transA, transB, transC;
 };
 
+// tcgen05 engine: TMA descriptors of a phase, passed by value as a grid-constant
+// kernel parameter (parameter-space descriptors need no tensor-map proxy fence)
+struct TmaMaps {
+    CUtensorMap a[kMaxMapsA];
+    CUtensorMap b[kMaxMapsB];
+};
+
+// one column piece of a column-major FP64 block written into its panel rows:
+// column c -> panel row c (dst_off + c*dst_pitch), element r -> K index r
+struct PanelPiece { int64_t src_off, dst_off; int32_t rows, cols, src_ld, dst_pitch; double scale; };
+
 struct PackBlock { int64_t coff, doff, rows, cols, ld; double scale; };
 
 cudaError_t kernels_init();
 // FP64 grouped GEMM (DMMA)
 cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st);
-// split-precision grouped GEMM on pre-split K-contiguous operands;
-// out_split = 1: C/C2 are bf16 hi/lo, 0: C is double
-cudaError_t launch_gg_split(int out_split, const GGArgs& a, cudaStream_t st);
-// tcgen05 engine (umma.cu): persistent, TMA-fed; tiles up to 128 x 64
+// split-precision (BF16x3) grouped GEMM, tcgen05 engine (umma.cu): persistent,
+// TMA-fed, tiles up to 128 x 256; out_split = 1: C is a bf16 [hi|lo] panel arena,
+// 0: C is double
 cudaError_t umma_init();
-cudaError_t launch_gg_umma(int out_split, const GGArgs& a, cudaStream_t st);
-cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* hi, void* lo, cudaStream_t st);
-cudaError_t launch_split(const double* src, void* hi, void* lo, int64_t n, cudaStream_t st);
-// compact (scaled per block) -> padded bf16 hi / lo, the values launch_pack + launch_split give
-cudaError_t launch_pack_split(const PackBlock* blocks, int nb, const double* src, void* hi, void* lo, cudaStream_t st);
+cudaError_t launch_gg_umma(int out_split, const GGArgs& a, const TmaMaps& maps, cudaStream_t st);
+// split operands: FP64 blocks -> bf16 [hi|lo] panels
+cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* dst, cudaStream_t st);
+cudaError_t launch_panel_split(const PanelPiece* pieces, int np, const double* src, void* dst, cudaStream_t st);
 cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, double* dst, int to_padded,
                         cudaStream_t st);
 int64_t dot_chunk(int64_t n);

@@ -96,15 +96,6 @@ struct vmps_ctx_s {
     int num_sms = 152;              // CTAs of the persistent tcgen05 engine (host-only: GB300's count)
 };
 
-// split-precision engine: tcgen05 (default) or mma.sync (VMPS_SPLIT_ENGINE=mma)
-static int split_engine() {
-    static int e = [] {
-        const char* s = std::getenv("VMPS_SPLIT_ENGINE");
-        return (s && std::string(s) == "mma") ? 0 : 1;
-    }();
-    return e;
-}
-
 // read and clear the device error word (after the stream has been synchronised)
 static void check_device_error(vmps_ctx* c) {
     if (!c || !c->err) return;
@@ -121,6 +112,7 @@ static void check_device_error(vmps_ctx* c) {
 struct DevPhase {
     DBuf tiles, segs, terms;
     DBuf steps, cta_tiles;   // tcgen05 engine schedule
+    std::unique_ptr<TmaMaps> maps;   // tcgen05 engine: the phase's TMA descriptors (kernel parameter)
     int ntiles = 0, ncta = 0;
     const PhasePlan* host = nullptr;
     void upload(const PhasePlan& ph, cudaStream_t st) {
@@ -151,6 +143,7 @@ struct VecChunk {
 struct DevChunked {
     std::vector<VecChunk> in, out;    // input chunks (phase 1 cut), output chunks (phase 2 cut)
     bool compact_out = false;         // phase 2 writes the compact (host-layout) vector directly
+    DBuf ypieces;                     // PanelPiece list: the compact vector (scaled per block) -> Y2
     std::deque<PhasePlan> p1h, p2h;   // host sub-plans (DevPhase::host points here)
     std::deque<DevPhase> p1, p2;
     std::vector<cudaEvent_t> ev_in, ev_out;
@@ -162,23 +155,20 @@ struct DevChunked {
     }
 };
 
-// Split plans keep each bf16 operand as one arena [hi | lo]: the lo half of
-// element e sits at e + lo, with lo = the arena's element count (a multiple of
-// 32, so both halves start on 64-byte boundaries).
+// Split plans keep each bf16 operand in a panel arena (engine.hpp): op(X) in
+// X2, the vector Y in Y2 (split per call), the intermediates in T, the scaled
+// copies c*op(Z) in Z2.
 struct DevPlan {
     Plan plan;
     DevPhase p1, p2;
-    DBuf T;                        // FP64: T (double); split: T [hi | lo] (bf16)
-    DBuf X2, Z2, Y2;               // split: prepared operands [hi | lo]
+    DBuf T;                        // FP64: T (double); split: T panels (bf16)
+    DBuf X2, Z2, Y2;               // split: operand panels (bf16)
     DBuf prepX, prepZ;             // PrepBlock lists
-    DBuf mapX, mapY, mapT, mapZ;   // tcgen05 engine: one 128-byte TMA descriptor per operand block
-    int nprepX = 0, nprepZ = 0;
-    int64_t ytotal = 0;            // elements of the Y arena (split per call)
-    std::unique_ptr<DevChunked> chunks;   // host-buffer pipeline (tcgen05 split plans of pivots)
+    DBuf ypieces;                  // PanelPiece list: the FP64 Y arena -> Y2
+    int nprepX = 0, nprepZ = 0, nypieces = 0;
+    std::unique_ptr<DevChunked> chunks;   // host-buffer pipeline (split plans of pivots)
     bool ready = false;
 };
-
-static void* lo_half(const DBuf& b, int64_t total) { return b.as<uint16_t>() + total; }
 
 // ---------------------------------------------------------------------------
 // TMA descriptors of the tcgen05 engine
@@ -199,35 +189,44 @@ static EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// One descriptor per block of a [hi | lo] bf16 arena: a 3-d tensor (K, outer,
-// hi/lo) with K contiguous, rows `ld` elements apart, halves `lo` elements
-// apart.  Boxes are kUmmaBK (32 elements = 64 bytes) x the block's box rows x 2
-// with 64-byte swizzle and zero fill outside the block, which is what the
-// engine's shared-memory stages expect.
-static void build_maps(DBuf& maps, const std::vector<OpBlock>& blocks, const DBuf& arena, int64_t lo,
-                       cudaStream_t st) {
-    if (lo % 8 != 0) throw std::logic_error("split arena size is not a multiple of 8 elements");
-    std::vector<CUtensorMap> h(std::max<size_t>(1, blocks.size()));
-    std::memset(h.data(), 0, h.size() * sizeof(CUtensorMap));
-    EncodeTiledFn enc = encode_tiled();
-    for (size_t i = 0; i < blocks.size(); ++i) {
-        const OpBlock& b = blocks[i];
-        if (b.off % 32 != 0 || b.ld % 8 != 0) throw std::logic_error("operand block is not 16-byte aligned");
-        const cuuint64_t dims[3] = {(cuuint64_t)std::max(1, b.K), (cuuint64_t)std::max(1, b.outer), 2};
-        const cuuint64_t strides[2] = {(cuuint64_t)b.ld * 2, (cuuint64_t)lo * 2};
-        if (b.box < 16 || b.box > 256 || b.box % 16 != 0) throw std::logic_error("TMA box rows out of range");
-        const cuuint32_t box[3] = {(cuuint32_t)kUmmaBK, (cuuint32_t)b.box, 2};
-        const cuuint32_t estr[3] = {1, 1, 1};
-        void* base = arena.as<uint16_t>() + b.off;
-        CUresult res = enc(&h[i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (res != CUDA_SUCCESS)
-            throw CudaFail("cuTensorMapEncodeTiled failed (" + std::to_string((int)res) + ") for a block of " +
-                           std::to_string(b.outer) + " x " + std::to_string(b.K) + ", ld " + std::to_string(b.ld));
-    }
-    upload_vec(maps, h, st);
+// The TMA descriptors of one split phase: for each (panel class, box height) key
+// a 2-d tensor over the class matrix (2*kpad bf16 columns, its stacked rows) with
+// boxes of 64 columns (one 32-wide K step, hi and lo) x the key's rows, 128-byte
+// swizzle and zero fill below the last row.
+static void encode_panel_map(CUtensorMap* m, const PanelArena& ar, const DBuf& arena, const MapKey& k) {
+    if (k.cls < 0 || k.cls >= (int)ar.cls.size()) throw std::logic_error("TMA descriptor of an unknown panel class");
+    const PanelClass& c = ar.cls[k.cls];
+    if (k.rows < 16 || k.rows > 256 || k.rows % 16 != 0) throw std::logic_error("TMA box rows out of range");
+    if (c.base % 64 != 0 || c.kpad % 32 != 0) throw std::logic_error("panel class not 128-byte aligned");
+    const cuuint64_t dims[2] = {(cuuint64_t)2 * c.kpad, (cuuint64_t)std::max<int64_t>(c.rows, 1)};
+    const cuuint64_t strides[1] = {(cuuint64_t)4 * c.kpad};
+    const cuuint32_t box[2] = {64, (cuuint32_t)k.rows};
+    const cuuint32_t estr[2] = {1, 1};
+    void* base = arena.as<uint16_t>() + c.base;
+    CUresult res = encode_tiled()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (res != CUDA_SUCCESS)
+        throw CudaFail("cuTensorMapEncodeTiled failed (" + std::to_string((int)res) + ") for a panel class of " +
+                       std::to_string(c.rows) + " rows x " + std::to_string(c.kpad));
 }
+
+static std::unique_ptr<TmaMaps> build_phase_maps(const PhasePlan& ph, const PanelArena& A, const DBuf& Aarena,
+                                                 const PanelArena& B, const DBuf& Barena) {
+    if ((int)ph.amaps.size() > kMaxMapsA || (int)ph.bmaps.size() > kMaxMapsB)
+        throw std::logic_error("tcgen05 plan: too many TMA descriptors in one phase");
+    auto m = std::make_unique<TmaMaps>();
+    std::memset(m.get(), 0, sizeof(TmaMaps));
+    for (size_t i = 0; i < ph.amaps.size(); ++i) encode_panel_map(&m->a[i], A, Aarena, ph.amaps[i]);
+    for (size_t i = 0; i < ph.bmaps.size(); ++i) encode_panel_map(&m->b[i], B, Barena, ph.bmaps[i]);
+    return m;
+}
+
+// column pieces (at most kPackPiece elements) of the blocks of a column-major
+// FP64 layout into the panels of opY: column c of block y -> panel row c
+static std::vector<PanelPiece> panel_pieces(const std::vector<int64_t>& off, const std::vector<int64_t>& rows,
+                                            const std::vector<int64_t>& cols, const std::vector<int64_t>& ld,
+                                            const std::vector<OpBlock>& op, const std::vector<double>* scale);
 
 // compact <-> padded copy descriptors of one block table.  Blocks are cut into
 // pieces of whole columns holding at most kPackPiece elements (one pass of a
@@ -264,6 +263,23 @@ static std::vector<int> pack_piece_starts(const BlockTable& t) {
         s[i + 1] = s[i] + (int)np;
     }
     return s;
+}
+
+static std::vector<PanelPiece> panel_pieces(const std::vector<int64_t>& off, const std::vector<int64_t>& rows,
+                                            const std::vector<int64_t>& cols, const std::vector<int64_t>& ld,
+                                            const std::vector<OpBlock>& op, const std::vector<double>* scale) {
+    std::vector<PanelPiece> v;
+    for (size_t i = 0; i < rows.size(); ++i) {
+        if (rows[i] <= 0 || cols[i] <= 0) continue;
+        if (op[i].K != rows[i] || op[i].outer != cols[i]) throw std::logic_error("vector panel does not match its block");
+        const int64_t per = std::max<int64_t>(1, kPackPiece / rows[i]);   // the cut of pack_blocks
+        for (int64_t c0 = 0; c0 < cols[i]; c0 += per) {
+            const int64_t nc = std::min(per, cols[i] - c0);
+            v.push_back(PanelPiece{off[i] + c0 * ld[i], op[i].off + c0 * op[i].pitch, (int32_t)rows[i], (int32_t)nc,
+                                   (int32_t)ld[i], op[i].pitch, scale ? (*scale)[i] : 1.0});
+        }
+    }
+    return v;
 }
 
 // A pointer the device may dereference for a caller's host buffer, or null when
@@ -322,17 +338,17 @@ struct Operands {
 };
 
 // Invariants the tcgen05 engine relies on, checked on the host once per plan:
-// every segment names an A and a B descriptor that exist and share its K,
-// every tile lies inside the A rows / B columns of each of its segments and
-// fits the 128 x 64 accumulator.
+// every segment names operand blocks that exist and share its K; every tile lies
+// inside its blocks, fits the 128 x 256 accumulator and its TMA boxes; split
+// outputs (T panels) are tiled on whole panel K steps.
 static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B,
                               bool split_out) {
     if (ph.seg_amap.size() != ph.segs.size() || ph.seg_bmap.size() != ph.segs.size())
-        throw std::logic_error("tcgen05 plan: segment descriptor maps missing");
+        throw std::logic_error("tcgen05 plan: segment operand maps missing");
     for (size_t s = 0; s < ph.segs.size(); ++s) {
         const int32_t a = ph.seg_amap[s], b = ph.seg_bmap[s];
         if (a < 0 || a >= (int32_t)A.size() || b < 0 || b >= (int32_t)B.size())
-            throw std::logic_error("tcgen05 plan: descriptor index out of range");
+            throw std::logic_error("tcgen05 plan: operand block index out of range");
         if (A[a].K != ph.segs[s].K || B[b].K != ph.segs[s].K || ph.segs[s].K <= 0)
             throw std::logic_error("tcgen05 plan: contraction length mismatch");
     }
@@ -341,83 +357,86 @@ static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A
             throw std::logic_error("tcgen05 plan: tile shape out of range");
         if (t.seg_begin < 0 || t.seg_end < t.seg_begin || t.seg_end > (int32_t)ph.segs.size())
             throw std::logic_error("tcgen05 plan: tile segment range out of range");
-        for (int32_t s = t.seg_begin; s < t.seg_end; ++s) {
+        for (int32_t s = t.seg_begin; s < t.seg_end; ++s)
             if (t.row0 + t.tm > A[ph.seg_amap[s]].outer || t.col0 + t.tn > B[ph.seg_bmap[s]].outer)
                 throw std::logic_error("tcgen05 plan: tile outside its operand blocks");
-            // the MMA reads round16(tn) rows of the B box and all 128 rows of the A box
-            if (((t.tn + 15) / 16) * 16 > B[ph.seg_bmap[s]].box || A[ph.seg_amap[s]].box != kUmmaTileM)
-                throw std::logic_error("tcgen05 plan: tile wider than its TMA box");
-        }
-        // a split output is stored in 16-byte row chunks (8 bf16) of a row-major tile
-        if (split_out && (!ph.transC || t.c_off % 8 != 0 || t.ldc % 8 != 0 || t.col0 % 8 != 0 ||
-                          t.ldc < ((t.col0 + t.tn + 7) / 8) * 8))
-            throw std::logic_error("tcgen05 plan: split-output tile not 16-byte aligned");
+        if (split_out && (!ph.transC || t.col0 % 32 != 0 || t.ldc % 64 != 0 || t.c_off % 64 != 0))
+            throw std::logic_error("tcgen05 plan: split-output tile not on whole panel K steps");
     }
 }
 
 // the schedule: CTA tile ranges partition the tiles, every tile's steps lie in
-// the step list, K offsets stay inside their segments' contraction length
-static void validate_tma_schedule(const PhasePlan& ph, const std::vector<OpBlock>& A) {
+// the step list, TMA coordinates are 128-byte aligned and inside their panel
+// classes' columns, boxes cover the tiles, descriptors exist
+static void validate_tma_schedule(const PhasePlan& ph, const PanelArena& A, const PanelArena& B) {
     if (ph.tiles.empty()) return;
     if (ph.ncta <= 0 || (int)ph.cta_tiles.size() != ph.ncta + 1 || ph.cta_tiles.front() != 0 ||
         ph.cta_tiles.back() != (int32_t)ph.tiles.size())
         throw std::logic_error("tcgen05 plan: CTA ranges do not cover the tiles");
     for (int b = 0; b < ph.ncta; ++b)
         if (ph.cta_tiles[b + 1] < ph.cta_tiles[b]) throw std::logic_error("tcgen05 plan: CTA ranges out of order");
+    if ((int)ph.amaps.size() > kMaxMapsA || (int)ph.bmaps.size() > kMaxMapsB)
+        throw std::logic_error("tcgen05 plan: too many TMA descriptors in one phase");
     int64_t next = 0;
     for (const GTile& t : ph.tiles) {
         if (t.step0 != next || t.nsteps < 0) throw std::logic_error("tcgen05 plan: tile steps not contiguous");
         next += t.nsteps;
-        // the MMA issuer takes the B box height of a tile from its first step
-        for (int j = t.step0; j < t.step0 + t.nsteps && j < (int)ph.steps.size(); ++j)
-            if (ph.steps[j].brows != ph.steps[t.step0].brows || ph.steps[j].brows < ((t.tn + 15) / 16) * 16)
-                throw std::logic_error("tcgen05 plan: B box height varies within a tile");
+        for (int j = t.step0; j < t.step0 + t.nsteps && j < (int)ph.steps.size(); ++j) {
+            const TStep& s = ph.steps[j];
+            if (s.amap < 0 || s.amap >= (int)ph.amaps.size() || s.bmap < 0 || s.bmap >= (int)ph.bmaps.size())
+                throw std::logic_error("tcgen05 plan: step descriptor out of range");
+            const MapKey& ka = ph.amaps[s.amap];
+            const MapKey& kb = ph.bmaps[s.bmap];
+            if (ka.rows != s.arows || kb.rows != s.brows || s.arows < t.tm || s.brows < ((t.tn + 15) / 16) * 16 ||
+                s.arows > kUmmaTileM || s.brows > kUmmaTileN)
+                throw std::logic_error("tcgen05 plan: TMA box does not cover its tile");
+            if (s.x % 64 != 0 || s.x < 0 || s.x >= 2 * A.cls[ka.cls].kpad || s.x >= 2 * B.cls[kb.cls].kpad ||
+                s.ay < 0 || s.by < 0 || s.ay >= A.cls[ka.cls].rows || s.by >= B.cls[kb.cls].rows)
+                throw std::logic_error("tcgen05 plan: TMA coordinate outside its panel");
+        }
     }
     if (next != (int64_t)ph.steps.size()) throw std::logic_error("tcgen05 plan: step count mismatch");
-    for (const TStep& s : ph.steps)
-        if (s.amap < 0 || s.amap >= (int32_t)A.size() || s.k0 < 0 || s.k0 >= A[s.amap].K || s.k0 % kUmmaBK != 0)
-            throw std::logic_error("tcgen05 plan: step outside its operand block");
 }
 
 static void schedule_and_validate(Plan& p, int ncta) {
     validate_tma_plan(p.p1, p.opX, p.opY, true);
     validate_tma_plan(p.p2, p.opT, p.opZ, false);
-    schedule_tma(p.p1, ncta, p.opY);
-    schedule_tma(p.p2, ncta, p.opZ);
-    validate_tma_schedule(p.p1, p.opX);
-    validate_tma_schedule(p.p2, p.opT);
+    schedule_tma(p.p1, ncta, p.opX, p.opY);
+    schedule_tma(p.p2, ncta, p.opT, p.opZ);
+    validate_tma_schedule(p.p1, p.ax, p.ay);
+    validate_tma_schedule(p.p2, p.at, p.az);
 }
 
-// device buffers and work lists of a freshly made plan
-static void plan_to_device(DevPlan& dp, int64_t ytotal, cudaStream_t st) {
+// device buffers and work lists of a freshly made plan; Y is the FP64 layout
+// the per-call vector split reads
+static void plan_to_device(DevPlan& dp, const DevLayout& Y, cudaStream_t st) {
     dp.p1.upload(dp.plan.p1, st);
     dp.p2.upload(dp.plan.p2, st);
     if (!dp.plan.split) {
         dp.T.alloc((size_t)dp.plan.T.total * 8, st, true);
         return;
     }
-    dp.T.alloc((size_t)dp.plan.T.total * 4, st, true);
-    dp.X2.alloc((size_t)dp.plan.Xp_total * 4, st, true);
-    dp.Z2.alloc((size_t)dp.plan.Zp_total * 4, st, true);
-    dp.ytotal = ytotal;
-    dp.Y2.alloc((size_t)std::max<int64_t>(ytotal, 32) * 4, st, true);
+    // zero-filled: panel padding stays zero
+    dp.T.alloc((size_t)dp.plan.at.total * 2, st, true);
+    dp.X2.alloc((size_t)dp.plan.ax.total * 2, st, true);
+    dp.Z2.alloc((size_t)dp.plan.az.total * 2, st, true);
+    dp.Y2.alloc((size_t)dp.plan.ay.total * 2, st, true);
     upload_vec(dp.prepX, dp.plan.prepX, st);
     upload_vec(dp.prepZ, dp.plan.prepZ, st);
     dp.nprepX = (int)dp.plan.prepX.size();
     dp.nprepZ = (int)dp.plan.prepZ.size();
-    if (dp.plan.split_kernel) {
-        build_maps(dp.mapX, dp.plan.opX, dp.X2, dp.plan.Xp_total, st);
-        build_maps(dp.mapY, dp.plan.opY, dp.Y2, dp.ytotal, st);
-        build_maps(dp.mapT, dp.plan.opT, dp.T, dp.plan.T.total, st);
-        build_maps(dp.mapZ, dp.plan.opZ, dp.Z2, dp.plan.Zp_total, st);
-    }
+    const auto yp = panel_pieces(Y.off, Y.rows, Y.cols, Y.ld, dp.plan.opY, nullptr);
+    upload_vec(dp.ypieces, yp, st);
+    dp.nypieces = (int)yp.size();
+    dp.p1.maps = build_phase_maps(dp.plan.p1, dp.plan.ax, dp.X2, dp.plan.ay, dp.Y2);
+    dp.p2.maps = build_phase_maps(dp.plan.p2, dp.plan.at, dp.T, dp.plan.az, dp.Z2);
 }
 
-// split plans: scaled bf16 hi/lo copies of the X and Z operands
+// split plans: the bf16 panels of the X and scaled Z operands
 static void split_prepare(DevPlan& dp, const double* X, const double* Z, cudaStream_t st) {
     if (!dp.plan.split) return;
-    CK(launch_prep(dp.prepX.as<PrepBlock>(), dp.nprepX, X, dp.X2.p, lo_half(dp.X2, dp.plan.Xp_total), st));
-    CK(launch_prep(dp.prepZ.as<PrepBlock>(), dp.nprepZ, Z, dp.Z2.p, lo_half(dp.Z2, dp.plan.Zp_total), st));
+    CK(launch_prep(dp.prepX.as<PrepBlock>(), dp.nprepX, X, dp.X2.p, st));
+    CK(launch_prep(dp.prepZ.as<PrepBlock>(), dp.nprepZ, Z, dp.Z2.p, st));
 }
 
 static void run_phase_on(const DevPlan& dp, int ph, const DevPhase& d, const PhasePlan& h, const Operands& ops,
@@ -443,26 +462,21 @@ static void run_phase_on(const DevPlan& dp, int ph, const DevPhase& d, const Pha
         a.A = slot(h.slotA);
         a.B = slot(h.slotB);
         a.C = const_cast<void*>(slot(h.slotC));
-    } else if (ph == 1) {
-        a.A = dp.X2.p; a.A2 = lo_half(dp.X2, dp.plan.Xp_total);
-        a.B = dp.Y2.p; a.B2 = lo_half(dp.Y2, dp.ytotal);
-        a.C = dp.T.p; a.C2 = lo_half(dp.T, dp.plan.T.total);
-        a.amaps = dp.mapX.p; a.bmaps = dp.mapY.p;
-    } else {
-        a.A = dp.T.p; a.A2 = lo_half(dp.T, dp.plan.T.total);
-        a.B = dp.Z2.p; a.B2 = lo_half(dp.Z2, dp.plan.Zp_total);
-        a.C = ops.O;
-        a.amaps = dp.mapT.p; a.bmaps = dp.mapZ.p;
+        // every operand of a non-empty phase must be a live device buffer
+        if (d.ntiles > 0 && (!a.C || !a.tiles || !a.segs || !a.terms || (!h.segs.empty() && (!a.A || !a.B))))
+            throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
+        CK(launch_gg64(a, st));
+        return;
     }
+    a.A = ph == 1 ? dp.X2.p : dp.T.p;
+    a.B = ph == 1 ? dp.Y2.p : dp.Z2.p;
+    a.C = ph == 1 ? dp.T.p : ops.O;
     a.steps = d.steps.as<TStep>();
     a.cta_tiles = d.cta_tiles.as<int32_t>();
     a.ncta = d.ncta;
-    // every operand of a non-empty phase must be a live device buffer
-    if (d.ntiles > 0 && (!a.C || !a.tiles || !a.segs || !a.terms || (!h.segs.empty() && (!a.A || !a.B))))
+    if (d.ntiles > 0 && (!a.A || !a.B || !a.C || !a.tiles || !a.steps || !a.cta_tiles || !d.maps))
         throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
-    if (!dp.plan.split) CK(launch_gg64(a, st));
-    else if (dp.plan.split_kernel) CK(launch_gg_umma(ph == 1 ? 1 : 0, a, st));
-    else CK(launch_gg_split(ph == 1 ? 1 : 0, a, st));
+    if (d.ntiles > 0) CK(launch_gg_umma(ph == 1 ? 1 : 0, a, *d.maps, st));
 }
 
 static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream_t st) {
@@ -472,7 +486,7 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
 
 // one application of a planned contraction: (split plans) split Y, phase 1, phase 2
 static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
-    if (dp.plan.split) CK(launch_split(ops.Y, dp.Y2.p, lo_half(dp.Y2, dp.ytotal), dp.ytotal, st));
+    if (dp.plan.split) CK(launch_panel_split(dp.ypieces.as<PanelPiece>(), dp.nypieces, ops.Y, dp.Y2.p, st));
     run_phase(dp, 1, ops, st);
     run_phase(dp, 2, ops, st);
 }
@@ -492,12 +506,21 @@ static void fill_stats(const ChainSet& cs, const Plan& p, int prec, vmps_plan_st
     s->flops_phase2 = p.p2.flops;
     s->flops_executed = p.p1.flops + p.p2.flops;
     s->bytes_algorithmic = p.bytes_alg;
-    s->bytes_intermediate = (double)p.T.total * (p.split ? 4.0 : 8.0);
+    s->bytes_intermediate = p.split ? 2.0 * (double)p.at.total : 8.0 * (double)p.T.total;
     (void)prec;
     s->n_segments_phase2 = (int64_t)p.p2.segs.size();
     s->n_terms_phase2 = (int64_t)p.p2.terms.size();
     s->flops_phase2_unsummed = p.flops_p2_unsummed;
     s->association = p.association;
+    if (p.split) {
+        auto tensor = [](const PhasePlan& ph) {
+            double f = 0;
+            for (const GTile& t : ph.tiles) f += (double)t.nsteps * 3.0 * 2.0 * kUmmaTileM * ((t.tn + 15) / 16 * 16) * kUmmaBK;
+            return f;
+        };
+        s->tensor_flops_phase1 = tensor(p.p1);
+        s->tensor_flops_phase2 = tensor(p.p2);
+    }
 }
 
 
@@ -554,14 +577,11 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
     if (dp.ready) return dp;
     if (prec == VMPS_PREC_FP64) dp.plan = make_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 64, 64);
     else {
-        const int eng = split_engine();
-        dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, eng ? kUmmaTileM : kTileMax,
-                                  eng ? kUmmaTileN : kTileMax);
-        dp.plan.split_kernel = eng;
-        if (eng) schedule_and_validate(dp.plan, p->ctx->num_sms);
+        dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false);
+        schedule_and_validate(dp.plan, p->ctx->num_sms);
     }
     if (p->ctx->device < 0) { dp.ready = true; return dp; }   // host-only: plan without device copies
-    plan_to_device(dp, p->Vd.total, p->st());
+    plan_to_device(dp, p->Vd, p->st());
     split_prepare(dp, p->dL.as<double>(), p->dR.as<double>(), p->st());
     if (prec == VMPS_PREC_BF16X3) make_chunks(p, dp);
     CK(cudaStreamSynchronize(p->st()));
@@ -570,14 +590,14 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
 }
 
 // Cut a pivot's split plan into the host-buffer pipeline (see DevChunked).  Only
-// for the tcgen05 engine, vectors of at least kChunkBytes per chunk, and a
-// compact layout whose blocks are stored in order without gaps.
+// for vectors of at least kChunkBytes per chunk and a compact layout whose
+// blocks are stored in order without gaps.
 constexpr int64_t kChunkBytes = 4 << 20;
 constexpr int kMaxChunksIn = 4, kMaxChunksOut = 3;
 static void make_chunks(vmps_pivot* p, DevPlan& dp) {
     const BlockTable& t = p->Vt;
     const int64_t nb = t.n;
-    if (!dp.plan.split_kernel || nb < 2) return;
+    if (!dp.plan.split || nb < 2) return;
     const int64_t kmax = std::min<int64_t>(nb, t.total * 8 / kChunkBytes);
     if (kmax < 2) return;
     for (int64_t b = 0; b < nb; ++b) {
@@ -639,7 +659,6 @@ static void make_chunks(vmps_pivot* p, DevPlan& dp) {
             }
             per[chunk_of[blk]].push_back(tl);
         }
-        const std::vector<OpBlock>& A = ph == 1 ? dp.plan.opX : dp.plan.opT;
         for (int c = 0; c < kk; ++c) {
             hs.emplace_back();
             PhasePlan& sp = hs.back();
@@ -650,14 +669,28 @@ static void make_chunks(vmps_pivot* p, DevPlan& dp) {
             sp.transA = full.transA; sp.transB = full.transB; sp.transC = full.transC;
             sp.slotA = full.slotA; sp.slotB = full.slotB; sp.slotC = full.slotC;
             sp.tiles = std::move(per[c]);
-            schedule_tma(sp, p->ctx->num_sms, ph == 1 ? dp.plan.opY : dp.plan.opZ);
-            validate_tma_schedule(sp, A);
+            if (ph == 1) {
+                schedule_tma(sp, p->ctx->num_sms, dp.plan.opX, dp.plan.opY);
+                validate_tma_schedule(sp, dp.plan.ax, dp.plan.ay);
+            } else {
+                schedule_tma(sp, p->ctx->num_sms, dp.plan.opT, dp.plan.opZ);
+                validate_tma_schedule(sp, dp.plan.at, dp.plan.az);
+            }
             ds.emplace_back();
             ds.back().upload(sp, p->st());
+            ds.back().maps = ph == 1 ? build_phase_maps(sp, dp.plan.ax, dp.X2, dp.plan.ay, dp.Y2)
+                                     : build_phase_maps(sp, dp.plan.at, dp.T, dp.plan.az, dp.Z2);
         }
     };
     cut(dp.plan.p1, 1, ch->p1h, ch->p1);
     cut(dp.plan.p2, 2, ch->p2h, ch->p2);
+    {
+        // the compact vector into Y2's panels, in the piece order of pack_piece_starts
+        std::vector<int64_t> ld(t.rows.begin(), t.rows.end());
+        const auto yp = panel_pieces(t.off, t.rows, t.cols, ld, dp.plan.opY, &p->vscale);
+        if ((int)yp.size() != ps[nb]) throw std::logic_error("vector pieces differ from the pack pieces");
+        upload_vec(ch->ypieces, yp, p->st());
+    }
     ch->ev_in.resize(ch->in.size(), nullptr);
     ch->ev_out.resize(ch->out.size(), nullptr);
     for (auto& ev : ch->ev_in) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
@@ -691,7 +724,7 @@ static void hxv_host_pipelined(vmps_pivot* p, DevPlan& dp, const double* vin, do
         CK(cudaMemcpyAsync(sin + v.coff, vin + v.coff, (size_t)v.clen * 8, cudaMemcpyHostToDevice, xs));
         CK(cudaEventRecord(ch.ev_in[c], xs));
         CK(cudaStreamWaitEvent(cs, ch.ev_in[c], 0));
-        CK(launch_pack_split(pk + v.piece0, v.piece1 - v.piece0, sin, dp.Y2.p, lo_half(dp.Y2, dp.ytotal), cs));
+        CK(launch_panel_split(ch.ypieces.as<PanelPiece>() + v.piece0, v.piece1 - v.piece0, sin, dp.Y2.p, cs));
         run_phase_on(dp, 1, ch.p1[c], ch.p1h[c], ops, cs);
     }
     // phase 2 of chunk o is queued before the copy-out of chunk o-1, so that a
@@ -1289,14 +1322,11 @@ static DevPlan& env_plan(vmps_env* e, int prec) {
     const DevLayout& Z = L ? e->Kd : e->Bd;
     if (prec == VMPS_PREC_FP64) dp.plan = make_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L, 64, 64);
     else {
-        const int eng = split_engine();
-        dp.plan = make_split_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L, eng ? kUmmaTileM : kTileMax,
-                                  eng ? kUmmaTileN : kTileMax);
-        dp.plan.split_kernel = eng;
-        if (eng) schedule_and_validate(dp.plan, e->ctx->num_sms);
+        dp.plan = make_split_plan(e->cs, X, e->Ed, Z, e->Nd, L, !L);
+        schedule_and_validate(dp.plan, e->ctx->num_sms);
     }
     if (e->ctx->device < 0) { dp.ready = true; return dp; }
-    plan_to_device(dp, e->Ed.total, e->st());
+    plan_to_device(dp, e->Ed, e->st());
     CK(cudaStreamSynchronize(e->st()));
     dp.ready = true;
     return dp;

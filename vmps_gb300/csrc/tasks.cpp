@@ -621,9 +621,9 @@ static std::vector<std::pair<int64_t, int64_t>> split_extent(int64_t m, int64_t 
 
 // append tiles of an m x n output block whose segments are [sb, se)
 void add_tiles(PhasePlan& ph, int64_t c_off, int64_t ldc, int64_t m, int64_t n, int32_t sb, int32_t se, int tile_m,
-               int tile_n) {
+               int tile_n, int col_gran = 8) {
     for (const auto& rs : split_extent(m, 16, tile_m))
-        for (const auto& cs : split_extent(n, 8, tile_n)) {
+        for (const auto& cs : split_extent(n, col_gran, tile_n)) {
             GTile t{};
             t.c_off = c_off;
             t.ldc = (int32_t)ldc;
@@ -656,15 +656,28 @@ void sort_tiles(PhasePlan& ph) {
 }
 }  // namespace
 
-int32_t b_box_rows(int64_t outer, int tile_n) {
-    int64_t mx = 0;
-    for (const auto& r : split_extent(std::max<int64_t>(outer, 1), 8, tile_n)) mx = std::max(mx, r.second);
-    return (int32_t)std::min<int64_t>(((mx + 15) / 16) * 16, 256);
+int32_t panel_kpad(int64_t K) {
+    K = std::max<int64_t>(K, 1);
+    int64_t q = K <= 256 ? 32 : K <= 1024 ? 128 : K <= 4096 ? 512 : 2048;
+    return (int32_t)((K + q - 1) / q * q);
 }
 
-void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& B) {
+int32_t box_rows_a(int32_t tm) {
+    for (int32_t h : {16, 32, 64, 128})
+        if (tm <= h) return h;
+    return 128;
+}
+
+int32_t box_rows_b(int32_t tn) {
+    if (tn <= 16) return 16;
+    return std::min<int32_t>(256, (tn + 31) / 32 * 32);
+}
+
+void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B) {
     const size_t nt = ph.tiles.size();
     ph.steps.clear();
+    ph.amaps.clear();
+    ph.bmaps.clear();
     ph.cta_tiles.assign(1, 0);
     ph.ncta = 0;
     if (nt == 0 || ncta <= 0) return;
@@ -693,26 +706,39 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& B) {
         per[l.second].push_back(i);
         heap.push({l.first + cost[i], l.second});
     }
+    // descriptors: one per (panel class, box height) used, for each side
+    std::map<std::pair<int32_t, int32_t>, int32_t> aidx, bidx;
+    auto map_of = [](std::map<std::pair<int32_t, int32_t>, int32_t>& idx, std::vector<MapKey>& keys, int32_t cls,
+                     int32_t rows) {
+        auto it = idx.find({cls, rows});
+        if (it != idx.end()) return it->second;
+        const int32_t i = (int32_t)keys.size();
+        keys.push_back(MapKey{cls, rows});
+        idx.emplace(std::make_pair(cls, rows), i);
+        return i;
+    };
     std::vector<GTile> tiles;
     tiles.reserve(nt);
     ph.cta_tiles.assign(ncta + 1, 0);
     for (int b = 0; b < ncta; ++b) {
-        std::unordered_set<int32_t> seen_a, seen_b;
         for (size_t i : per[b]) {
             GTile t = ph.tiles[i];
             t.step0 = (int32_t)ph.steps.size();
             t.nsteps = nsteps[i];
+            const int32_t ha = box_rows_a(t.tm), hb = box_rows_b(t.tn);
             for (int s = t.seg_begin; s < t.seg_end; ++s) {
-                const int32_t am = ph.seg_amap[s], bm = ph.seg_bmap[s];
+                const OpBlock& oa = A[ph.seg_amap[s]];
+                const OpBlock& ob = B[ph.seg_bmap[s]];
+                const int32_t am = map_of(aidx, ph.amaps, oa.cls, ha), bm = map_of(bidx, ph.bmaps, ob.cls, hb);
                 for (int32_t k0 = 0; k0 < ph.segs[s].K; k0 += kUmmaBK) {
                     TStep st{};
                     st.amap = am;
                     st.bmap = bm;
-                    st.k0 = k0;
-                    st.row0 = t.row0;
-                    st.col0 = t.col0;
-                    st.flags = (seen_a.insert(am).second ? 1 : 0) | (seen_b.insert(bm).second ? 2 : 0);
-                    st.brows = B[bm].box;
+                    st.x = 2 * k0;
+                    st.ay = oa.row + t.row0;
+                    st.by = ob.row + t.col0;
+                    st.arows = ha;
+                    st.brows = hb;
                     ph.steps.push_back(st);
                 }
             }
@@ -937,7 +963,7 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // split-precision planner
 // ===========================================================================
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ, int tile_m, int tile_n) {
+                     const DevLayout& O, bool transX, bool transZ) {
     Plan P;
     P.split = true;
     P.association = 0;
@@ -978,65 +1004,103 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         P.n_out_blocks = no;
     }
 
-    // prepared X blocks: op(X) (m x k) stored row-major, row stride pad8(k)
-    std::vector<int64_t> xp_off(X.rows.size(), -1), xp_ld(X.rows.size(), 0);
+    // panel arenas: blocks are added first (class and row), the class matrices
+    // are laid out afterwards, then every block gets its element offset
+    struct PanelBuilder {
+        PanelArena a;
+        std::map<int32_t, int32_t> cls_of_kpad;
+        std::vector<OpBlock>* ops;
+        int32_t add(int64_t outer, int64_t K) {
+            const int32_t kp = panel_kpad(K);
+            auto it = cls_of_kpad.find(kp);
+            int32_t c;
+            if (it == cls_of_kpad.end()) {
+                c = (int32_t)a.cls.size();
+                a.cls.push_back(PanelClass{kp, 0, 0});
+                cls_of_kpad.emplace(kp, c);
+            } else {
+                c = it->second;
+            }
+            OpBlock b{};
+            b.outer = (int32_t)outer;
+            b.K = (int32_t)K;
+            b.cls = c;
+            b.row = (int32_t)a.cls[c].rows;
+            b.pitch = 2 * kp;
+            a.cls[c].rows += outer;
+            ops->push_back(b);
+            return (int32_t)ops->size() - 1;
+        }
+        void finish() {
+            int64_t cur = 0;
+            for (PanelClass& c : a.cls) {
+                c.base = cur;
+                // whole 128-byte rows; each class starts on a 1 KiB boundary
+                cur = (cur + 2 * (int64_t)c.kpad * std::max<int64_t>(c.rows, 1) + 511) / 512 * 512;
+            }
+            a.total = std::max<int64_t>(cur, 512);
+            for (OpBlock& b : *ops) b.off = a.cls[b.cls].base + (int64_t)b.row * b.pitch;
+        }
+    };
+
+    // prepared X blocks: rows of op(X) (m x k)
+    PanelBuilder px{{}, {}, &P.opX};
     std::vector<int32_t> xp_idx(X.rows.size(), -1);
-    int64_t cur = 0;
     for (const Chain& c : ch) {
-        if (xp_off[c.x] >= 0) continue;
-        const int64_t m = xm(c.x), k = xk(c.x), ld = pad_ld(k);
-        xp_off[c.x] = cur;
-        xp_ld[c.x] = ld;
+        if (xp_idx[c.x] >= 0) continue;
+        xp_idx[c.x] = px.add(xm(c.x), xk(c.x));
+    }
+    px.finish();
+    P.ax = px.a;
+    for (size_t x = 0; x < X.rows.size(); ++x) {
+        if (xp_idx[x] < 0) continue;
+        const OpBlock& ob = P.opX[xp_idx[x]];
         PrepBlock pb{};
-        pb.src_off = X.off[c.x]; pb.src_ld = (int32_t)X.ld[c.x];
-        pb.rows = (int32_t)X.rows[c.x]; pb.cols = (int32_t)X.cols[c.x];
-        pb.dst_off = cur; pb.dst_ld = (int32_t)ld;
-        pb.trans = transX ? 0 : 1;   // op(X) = X: rows of X become rows; op(X) = X^T: columns of X
+        pb.src_off = X.off[x]; pb.src_ld = (int32_t)X.ld[x];
+        pb.rows = (int32_t)X.rows[x]; pb.cols = (int32_t)X.cols[x];
+        pb.dst_off = ob.off; pb.dst_ld = ob.pitch;
+        pb.trans = transX ? 0 : 1;   // op(X) = X: rows of X become panel rows; op(X) = X^T: columns of X
         pb.scale = 1.0;
         P.prepX.push_back(pb);
-        xp_idx[c.x] = (int32_t)P.opX.size();
-        P.opX.push_back(OpBlock{cur, (int32_t)m, (int32_t)k, (int32_t)ld, tile_m});
-        cur = pad_off(cur + ld * m);
     }
-    P.Xp_total = std::max<int64_t>(cur, 32);
 
-    // scaled copies c * op(Z) (n x p) stored column-major, column stride pad8(n)
+    // scaled copies c * op(Z) (n x p): panel rows are the p columns of op(Z)
     struct CZ { uint64_t cbits; int64_t z; bool operator==(const CZ& o) const { return cbits == o.cbits && z == o.z; } };
     struct CZH { size_t operator()(const CZ& a) const { return std::hash<uint64_t>()(a.cbits * 0x9E3779B97F4A7C15ull ^ (uint64_t)a.z); } };
-    std::unordered_map<CZ, int64_t, CZH> zdict;
-    std::vector<int64_t> zp_off, zp_ld;
-    std::vector<int64_t> chain_zp(ch.size());
-    cur = 0;
+    std::unordered_map<CZ, int32_t, CZH> zdict;
+    PanelBuilder pz{{}, {}, &P.opZ};
+    std::vector<int32_t> chain_zp(ch.size());
+    std::vector<std::pair<int64_t, double>> zsrc;   // (z, c) of each prepared copy
     for (size_t i = 0; i < ch.size(); ++i) {
         uint64_t bits;
         std::memcpy(&bits, &ch[i].c, 8);
         CZ key{bits, ch[i].z};
         auto it = zdict.find(key);
         if (it != zdict.end()) { chain_zp[i] = it->second; continue; }
-        const int64_t n = zn(ch[i].z), p = zp(ch[i].z), ld = pad_ld(n);
-        const int64_t id = (int64_t)zp_off.size();
+        const int32_t id = pz.add(zp(ch[i].z), zn(ch[i].z));
         zdict.emplace(key, id);
-        zp_off.push_back(cur);
-        zp_ld.push_back(ld);
-        PrepBlock pb{};
-        pb.src_off = Z.off[ch[i].z]; pb.src_ld = (int32_t)Z.ld[ch[i].z];
-        pb.rows = (int32_t)Z.rows[ch[i].z]; pb.cols = (int32_t)Z.cols[ch[i].z];
-        pb.dst_off = cur; pb.dst_ld = (int32_t)ld;
-        pb.trans = transZ ? 1 : 0;   // op(Z) = Z: columns stay columns; op(Z) = Z^T: rows of Z become columns
-        pb.scale = ch[i].c;
-        P.prepZ.push_back(pb);
-        P.opZ.push_back(OpBlock{cur, (int32_t)p, (int32_t)n, (int32_t)ld, b_box_rows(p, tile_n)});
+        zsrc.push_back({ch[i].z, ch[i].c});
         chain_zp[i] = id;
-        cur = pad_off(cur + ld * p);
     }
-    P.Zp_total = std::max<int64_t>(cur, 32);
+    pz.finish();
+    P.az = pz.a;
+    for (size_t q = 0; q < zsrc.size(); ++q) {
+        const int64_t z = zsrc[q].first;
+        const OpBlock& ob = P.opZ[q];
+        PrepBlock pb{};
+        pb.src_off = Z.off[z]; pb.src_ld = (int32_t)Z.ld[z];
+        pb.rows = (int32_t)Z.rows[z]; pb.cols = (int32_t)Z.cols[z];
+        pb.dst_off = ob.off; pb.dst_ld = ob.pitch;
+        pb.trans = transZ ? 1 : 0;   // op(Z) = Z: columns of Z become panel rows; op(Z) = Z^T: rows of Z
+        pb.scale = zsrc[q].second;
+        P.prepZ.push_back(pb);
+    }
 
-    // intermediates T = op(X) * Y (m x n), stored row-major (row stride pad8(n)) for phase 2
+    // intermediates T = op(X) * Y (m x n): panel rows are the m rows, K = n
     std::unordered_map<Key4, int64_t, Key4Hash> idict;
     std::vector<std::pair<int64_t, int64_t>> ipairs;
     std::vector<int64_t> chain_t(ch.size());
-    DevLayout& T = P.T;
-    cur = 0;
+    PanelBuilder pt{{}, {}, &P.opT};
     for (size_t i = 0; i < ch.size(); ++i) {
         Key4 k{ch[i].x, ch[i].y, 0, 0};
         auto it = idict.find(k);
@@ -1044,40 +1108,38 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         const int64_t id = (int64_t)ipairs.size();
         idict.emplace(k, id);
         ipairs.push_back({ch[i].x, ch[i].y});
-        const int64_t m = xm(ch[i].x), n = Y.cols[ch[i].y], ld = pad_ld(n);
-        T.off.push_back(cur); T.rows.push_back(m); T.cols.push_back(n); T.ld.push_back(ld);
-        P.opT.push_back(OpBlock{cur, (int32_t)m, (int32_t)n, (int32_t)ld, tile_m});
-        cur = pad_off(cur + ld * m);
+        pt.add(xm(ch[i].x), Y.cols[ch[i].y]);
         chain_t[i] = id;
     }
-    T.total = std::max<int64_t>(cur, 32);
+    pt.finish();
+    P.at = pt.a;
     P.n_intermediates = (int64_t)ipairs.size();
 
-    // the vector arena Y is split in place: its blocks are K (= rows) contiguous already
-    for (size_t y = 0; y < Y.rows.size(); ++y)
-        P.opY.push_back(OpBlock{Y.off[y], (int32_t)Y.cols[y], (int32_t)Y.rows[y], (int32_t)Y.ld[y],
-                                b_box_rows(Y.cols[y], tile_n)});
+    // the vector Y in panels: panel rows are its columns, K = its rows
+    PanelBuilder py{{}, {}, &P.opY};
+    for (size_t y = 0; y < Y.rows.size(); ++y) py.add(Y.cols[y], Y.rows[y]);
+    py.finish();
+    P.ay = py.a;
 
-    // phase 1: T_j = Xp[x] * Yp[y]   (A rows = m, B columns = n, K = k), stored transposed
+    // phase 1: T_j = op(X)[x] * Y[y]   (A rows = m, B rows = n, K = k), written into T's panels
     PhasePlan& p1 = P.p1;
     p1.slotA = SLOT_X; p1.slotB = SLOT_Y; p1.slotC = SLOT_T;
     p1.transA = false; p1.transB = false; p1.transC = true;
     for (size_t j = 0; j < ipairs.size(); ++j) {
         const int64_t x = ipairs[j].first, y = ipairs[j].second;
+        const OpBlock& ot = P.opT[j];
         GSeg s{};
         s.term_begin = (int32_t)p1.terms.size();
         s.term_count = 1;
-        p1.terms.push_back(GTerm{xp_off[x], 1.0});
-        s.lda = (int32_t)xp_ld[x];
-        s.b_off = Y.off[y];
-        s.ldb = (int32_t)Y.ld[y];
+        p1.terms.push_back(GTerm{P.opX[xp_idx[x]].off, 1.0});
         s.K = (int32_t)xk(x);
         const int32_t sb = (int32_t)p1.segs.size();
         p1.segs.push_back(s);
         p1.seg_amap.push_back(xp_idx[x]);
         p1.seg_bmap.push_back((int32_t)y);
-        p1.flops += 2.0 * T.rows[j] * T.cols[j] * s.K;
-        add_tiles(p1, T.off[j], T.ld[j], T.rows[j], T.cols[j], sb, sb + 1, tile_m, tile_n);
+        p1.flops += 2.0 * ot.outer * ot.K * s.K;
+        // column tiles start on panel K steps (multiples of 32): the epilogue writes whole row segments
+        add_tiles(p1, ot.off, ot.pitch, ot.outer, ot.K, sb, sb + 1, kUmmaTileM, kUmmaTileN, 32);
     }
     sort_tiles(p1);
 
@@ -1105,11 +1167,8 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
             GSeg s{};
             s.term_begin = (int32_t)p2.terms.size();
             s.term_count = 1;
-            p2.terms.push_back(GTerm{T.off[t], 1.0});
-            s.lda = (int32_t)T.ld[t];
-            s.b_off = zp_off[zq];
-            s.ldb = (int32_t)zp_ld[zq];
-            s.K = (int32_t)T.cols[t];
+            p2.terms.push_back(GTerm{P.opT[t].off, 1.0});
+            s.K = P.opT[t].K;
             kk += s.K;
             p2.segs.push_back(s);
             p2.seg_amap.push_back((int32_t)t);
@@ -1117,12 +1176,12 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
             ++i;
         }
         p2.flops += 2.0 * O.rows[o] * O.cols[o] * kk;
-        add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, (int32_t)p2.segs.size(), tile_m, tile_n);
+        add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, (int32_t)p2.segs.size(), kUmmaTileM, kUmmaTileN);
     }
     P.flops_p2_unsummed = p2.flops;
     const int32_t sb = (int32_t)p2.segs.size();
     for (size_t o = 0; o < O.rows.size(); ++o)
-        if (!seen[o]) add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, sb, tile_m, tile_n);
+        if (!seen[o]) add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, sb, kUmmaTileM, kUmmaTileN);
     sort_tiles(p2);
     return P;
 }

@@ -1,13 +1,18 @@
-// tcgen05 (UMMA) engine of the split-precision grouped GEMM (sm_103a).
+// tcgen05 (UMMA) engine of the split-precision (BF16x3) grouped GEMM (sm_103a).
 //
-// Same work lists as gg_split_kernel in kernels.cu.  Operands are pre-split
-// into bf16 hi and lo halves of one arena ([hi | lo]), stored K-contiguous
-// (rows of A, columns of B, row stride a multiple of 8 elements).  Every
-// prepared block has a TMA descriptor (K, rows, hi/lo) built on the host, so a
-// K step of one operand is one 3-d box copy that lands both halves in the
-// 128-byte-swizzled K-major layout the UMMA shared-memory descriptors read,
-// with zeros outside the block.  Tiles are up to 128 x 64 (UMMA M = 128,
-// N = 64, K = 16 per instruction), accumulated in FP32 in tensor memory.
+// Operands live in bf16 panels (engine.hpp): rows of A / of B, each 128-byte
+// row segment holding the hi and lo halves of one 32-wide K step.  A K step of
+// an operand is one 2-d TMA box of that panel (x = 2*k0, y = panel row, box
+// 64 elements x 16..256 rows) landing in the 128-byte-swizzled K-major layout
+// the UMMA shared-memory descriptors read: hi at K slices 0-1 of each row, lo
+// at K slices 2-3.  TMA descriptors, one per (panel class, box height), are a
+// grid-constant kernel parameter.  Tiles are up to 128 x 256 (UMMA M = 128,
+// N = round16(tile width), K = 16 per instruction), accumulated in FP32 in
+// tensor memory; per K step the products lo*hi + hi*lo + hi*hi.
+//
+// Panel rows next to a block belong to other blocks: they only reach rows or
+// columns of the accumulator the epilogue never stores, and the split epilogue
+// writes zeros past the tile width, so panel padding stays zero.
 //
 // Every barrier wait is bounded by a clock budget; when one runs out the
 // kernel records it in the error word, the roles leave their loops, the tensor
@@ -23,11 +28,11 @@ namespace vmps {
 namespace um {
 constexpr int BM = kUmmaTileM, BN = kUmmaTileN, BK = kUmmaBK, STAGES = 4;   // 128 x (<= 256) x 32
 constexpr int NT = 192;                                    // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
-constexpr int ROW_BYTES = BK * 2;                          // one K step of one row: 64 bytes
-constexpr int A_BYTES = BM * ROW_BYTES;                    // one of A hi / A lo: 8 KB
-constexpr int B_BYTES = BN * ROW_BYTES;                    // one of B hi / B lo, at most: 16 KB
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;     // 48 KB
-constexpr int STAGE_OUT_BYTES = 4 * 8192;                  // split-output epilogue: 32 rows x 64 cols x hi/lo per warp
+constexpr int ROW_BYTES = 128;                             // one K step of one row: 32 hi + 32 lo
+constexpr int A_BYTES = BM * ROW_BYTES;                    // A region: 16 KB
+constexpr int B_BYTES = BN * ROW_BYTES;                    // B region, at most: 32 KB
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;             // 48 KB
+constexpr int STAGE_OUT_BYTES = 4 * 8192;                  // split-output epilogue: 32 rows x 256 B per warp
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGE_OUT_BYTES + 1024 + 256;
 constexpr uint32_t ACC_COLS = BN;                          // one FP32 accumulator: 128 lanes x 256 columns
 constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two (all of TMEM), so an epilogue overlaps the next tile
@@ -35,20 +40,18 @@ constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two (all of TMEM),
 // both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22 (per tile), M >> 4 in bits 24-28
 constexpr uint32_t IDESC_BASE = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BM >> 4) << 24);
 constexpr long long WAIT_BUDGET = 4000000000LL;           // clock cycles (~2 s) per barrier wait
-constexpr int LOOKAHEAD = STAGES;                          // descriptors acquired this many steps ahead
 }  // namespace um
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of one 32-element
-// K step), 8-row groups 512 B apart
-__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFFu);   // start address >> 4
     d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(512 >> 4) << 32;           // stride byte offset between 8-row groups
+    d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset between 8-row groups
     d |= (uint64_t)1 << 46;                    // descriptor version (tcgen05)
-    d |= (uint64_t)4 << 61;                    // 64-byte swizzle
+    d |= (uint64_t)2 << 61;                    // 128-byte swizzle
     return d;
 }
 
@@ -87,19 +90,13 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
 }
-// 3-d tile copy (K, rows, hi/lo) global -> shared, completion counted on an mbarrier
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const void* tmap, int x, int y, int z, uint32_t bar) {
+// 2-d tile copy (panel columns, panel rows) global -> shared, completion counted on an mbarrier
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void* tmap, int x, int y, uint32_t bar) {
     asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];\n" ::"r"(dst),
-        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(bar)
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];\n" ::"r"(dst),
+        "l"(tmap), "r"(x), "r"(y), "r"(bar)
         : "memory");
-}
-
-// descriptors are written to global memory by the host, and a later plan may reuse
-// an address: acquire the current contents for the tensor-map proxy before use
-__device__ __forceinline__ void tmap_acquire(const void* tmap) {
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(tmap) : "memory");
 }
 
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -137,42 +134,26 @@ __device__ __forceinline__ void reg_fence16(uint32_t* r) {
 __device__ __forceinline__ void tmap_prefetch(const void* tmap) {
     asm volatile("prefetch.tensormap [%0];\n" ::"l"(tmap) : "memory");
 }
-// first use of a descriptor by this CTA: acquire it for the tensor-map proxy and
-// start fetching it
-__device__ __forceinline__ void acquire_step(const GGArgs& g, int j) {
-    const TStep s = g.steps[j];
-    if (s.flags & 1) {
-        const void* m = (const char*)g.amaps + (size_t)s.amap * 128;
-        tmap_acquire(m);
-        tmap_prefetch(m);
-    }
-    if (s.flags & 2) {
-        const void* m = (const char*)g.bmaps + (size_t)s.bmap * 128;
-        tmap_acquire(m);
-        tmap_prefetch(m);
-    }
-}
-
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(a)) |
            ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(b)) << 16);
 }
 
-// Persistent, warp-specialised grouped GEMM on pre-split operands.  CTA b runs
+// Persistent, warp-specialised grouped GEMM on panel operands.  CTA b runs
 // tiles[cta_tiles[b] .. cta_tiles[b+1]) (a host-side longest-first schedule),
 // whose K steps are steps[tiles[.].step0 ...], contiguous per CTA.
-//   warp 0 (one lane): per step one TMA 3-d box (K, rows, hi/lo) of A and one
-//     of B -- 128-byte swizzle, zero fill outside the block -- into a 4-deep
-//     ring of stages ("full" barriers count the bytes); descriptors are
-//     acquired and prefetched LOOKAHEAD steps ahead of their first use;
-//   warp 1 (one lane): per step 4 x (lo*hi, hi*lo, hi*hi) tcgen05.mma into one
+//   warp 0: keeps two windows of 32 step records in registers (one per lane,
+//     loaded one window ahead); lane 0 issues per step one TMA box of A and one
+//     of B into a 4-deep ring of stages ("full" barriers count the bytes);
+//   warp 1 (one lane): per step 2 x (lo*hi, hi*lo, hi*hi) tcgen05.mma into one
 //     of two TMEM accumulators, commit to the stage's "empty" barrier, and at
 //     the end of a tile to the accumulator's "full" barrier;
-//   warps 2-5: epilogue of their 32 accumulator lanes, overlapping the next
-//     tile's main loop.  A split (bf16 hi/lo, row-major) output is staged
-//     through swizzled shared memory so that global stores are whole rows.
+//   warps 2-5: epilogue of their 32 accumulator lanes in 64-column chunks,
+//     overlapping the next tile's main loop.  A split output (T panels) is
+//     staged through swizzled shared memory so that each panel row segment is
+//     one 256-byte store.
 template <int OUT_SPLIT>
-__global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
+__global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, const __grid_constant__ TmaMaps maps) {
     using namespace um;
     extern __shared__ __align__(1024) unsigned char smraw[];
     const uint32_t raw = su32(smraw);
@@ -204,37 +185,63 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
     const uint32_t tmem = *tmem_slot;
     const int t0 = g.cta_tiles[blockIdx.x], t1 = g.cta_tiles[blockIdx.x + 1];
 
-    if (warp == 0 && lane == 0) {
+    if (warp == 0) {
         // ---------------- TMA producer
-        const char* amaps = (const char*)g.amaps;
-        const char* bmaps = (const char*)g.bmaps;
+        for (int i = lane; i < kMaxMapsA; i += 32) tmap_prefetch(&maps.a[i]);
+        for (int i = lane; i < kMaxMapsB; i += 32) tmap_prefetch(&maps.b[i]);
         int S0 = 0, S1 = 0;
         if (t0 < t1) {
             S0 = g.tiles[t0].step0;
             S1 = g.tiles[t1 - 1].step0 + g.tiles[t1 - 1].nsteps;
         }
-        for (int j = S0; j < S1 && j < S0 + LOOKAHEAD; ++j) acquire_step(g, j);
+        auto load_rec = [&](int idx) {
+            TStep r{};
+            if (idx < S1) r = g.steps[idx];
+            return r;
+        };
+        TStep cur = load_rec(S0 + lane), nxt = load_rec(S0 + 32 + lane);
+        int B = S0;   // cur holds steps [B, B+32), nxt [B+32, B+64)
         int it = 0;
-        for (int j = S0; j < S1 && !*s_fail; ++j, ++it) {
-            if (j + LOOKAHEAD < S1) acquire_step(g, j + LOOKAHEAD);
-            const TStep s = g.steps[j];
-            const int st = it % STAGES, use = it / STAGES;
-            if (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), s_fail)) break;
-            const uint32_t sb = ring + st * STAGE_BYTES;
-            mbar_expect_tx(bar(st), (uint32_t)(2 * A_BYTES + 2 * s.brows * ROW_BYTES));
-            tma_load_3d(sb, amaps + (size_t)s.amap * 128, s.k0, s.row0, 0, bar(st));
-            tma_load_3d(sb + 2 * A_BYTES, bmaps + (size_t)s.bmap * 128, s.k0, s.col0, 0, bar(st));
+        for (int j = S0; j < S1; ++j, ++it) {
+            if (j == B + 32) {
+                cur = nxt;
+                B += 32;
+                nxt = load_rec(B + 32 + lane);
+            }
+            const int src = j - B;   // < 32
+            const int amap = __shfl_sync(0xffffffffu, cur.amap, src);
+            const int bmap = __shfl_sync(0xffffffffu, cur.bmap, src);
+            const int x = __shfl_sync(0xffffffffu, cur.x, src);
+            const int ay = __shfl_sync(0xffffffffu, cur.ay, src);
+            const int by = __shfl_sync(0xffffffffu, cur.by, src);
+            const int rows = __shfl_sync(0xffffffffu, cur.arows + cur.brows, src);
+            int go = 1;
+            if (lane == 0) {
+                const int st = it % STAGES, use = it / STAGES;
+                if (*s_fail || (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), s_fail))) {
+                    go = 0;
+                } else {
+                    const uint32_t sb = ring + st * STAGE_BYTES;
+                    mbar_expect_tx(bar(st), (uint32_t)(rows * ROW_BYTES));
+                    tma_load_2d(sb, &maps.a[amap], x, ay, bar(st));
+                    tma_load_2d(sb + A_BYTES, &maps.b[bmap], x, by, bar(st));
+                }
+            }
+            if (!__shfl_sync(0xffffffffu, go, 0)) break;
         }
         // copies still in flight land before the CTA exits (a no-op when the MMA warp consumed them)
-        for (int i = it - 1; i >= 0 && i >= it - STAGES; --i)
-            mbar_drain(bar(i % STAGES), (uint32_t)((i / STAGES) & 1), s_fail);
+        if (lane == 0)
+            for (int i = it - 1; i >= 0 && i >= it - STAGES; --i)
+                mbar_drain(bar(i % STAGES), (uint32_t)((i / STAGES) & 1), s_fail);
     } else if (warp == 1 && lane == 0) {
-        // ---------------- MMA issuer
+        // ---------------- MMA issuer (the next tile's record is fetched one tile ahead)
         int it = 0, lt = 0;
+        GTile tile{};
+        if (t0 < t1) tile = g.tiles[t0];
         for (int t = t0; t < t1 && !*s_fail; ++t, ++lt) {
-            const GTile tile = g.tiles[t];
+            GTile next{};
+            if (t + 1 < t1) next = g.tiles[t + 1];
             const int nsteps = tile.nsteps;
-            const int brows = nsteps > 0 ? g.steps[tile.step0].brows : 16;
             const uint32_t idesc = IDESC_BASE | ((uint32_t)(((tile.tn + 15) & ~15) >> 3) << 17);   // N = round16(tn)
             const int buf = lt & 1, buse = lt >> 1;
             if (buse >= 1 && !mbar_wait(bar(2 * STAGES + 2 + buf), (uint32_t)((buse - 1) & 1), s_fail)) break;
@@ -245,18 +252,19 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
                 if (!mbar_wait(bar(st), (uint32_t)(use & 1), s_fail)) break;
                 tc_fence_after();
                 const uint32_t sb = ring + st * STAGE_BYTES;
-                const uint64_t ah = sw64_desc(sb), al = sw64_desc(sb + A_BYTES);
-                const uint64_t bh = sw64_desc(sb + 2 * A_BYTES), bl = sw64_desc(sb + 2 * A_BYTES + brows * ROW_BYTES);
+                const uint64_t a = sw128_desc(sb), b = sw128_desc(sb + A_BYTES);
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
-                    const uint64_t adv = (uint64_t)(kk * 32) >> 4;   // 16 bf16 = 32 bytes along K
-                    umma_bf16(dacc, al + adv, bh + adv, idesc, (k | kk) != 0 ? 1u : 0u);
-                    umma_bf16(dacc, ah + adv, bl + adv, idesc, 1);
-                    umma_bf16(dacc, ah + adv, bh + adv, idesc, 1);
+                    // 16 bf16 = 32 bytes along K; the lo halves sit 64 bytes after the hi halves
+                    const uint64_t hi = (uint64_t)(kk * 32) >> 4, lo = (uint64_t)(64 + kk * 32) >> 4;
+                    umma_bf16(dacc, a + lo, b + hi, idesc, (k | kk) != 0 ? 1u : 0u);
+                    umma_bf16(dacc, a + hi, b + lo, idesc, 1);
+                    umma_bf16(dacc, a + hi, b + hi, idesc, 1);
                 }
                 umma_commit(bar(STAGES + st));
             }
             umma_commit(bar(2 * STAGES + buf));
+            tile = next;
         }
         umma_commit(bar(2 * STAGES + 4));
         mbar_drain(bar(2 * STAGES + 4), 0, s_fail);
@@ -264,7 +272,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
         // ---------------- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
         const int sp = warp & 3;
         const int rl = sp * 32 + lane;   // tile row of this lane
-        unsigned char* so = stage_out + (warp - 2) * 8192;   // this warp's staging: hi rows, then lo rows
+        unsigned char* so = stage_out + (warp - 2) * 8192;   // this warp's staging: 32 rows x 256 B
         int lt = 0;
         for (int t = t0; t < t1; ++t, ++lt) {
             const GTile tile = g.tiles[t];
@@ -299,39 +307,42 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
                     if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
                 }
                 const int tn = ncols - c0 < 64 ? ncols - c0 : 64;   // columns of this chunk
-                const int col0 = tile.col0 + c0;
                 if (OUT_SPLIT) {
-                    // row-major bf16 hi / lo: stage 32 rows x 64 columns (chunk c of row r at
-                    // r*128 + ((c ^ (r & 7)) << 4)), then store 4 whole 128-byte rows per instruction
+                    // T panel rows: columns col0+c0 .. +63 are two 32-wide K steps, i.e. the
+                    // 256-byte row segment [hi 0-31 | lo 0-31 | hi 32-63 | lo 32-63] (16-byte
+                    // units u = 8q + 4h + g: K step q, half h, columns 8g..8g+7).  Columns past
+                    // the tile are written as zeros.  Stage row r's unit u at r*256 + ((u ^ (r & 15)) << 4).
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) {
+                    for (int cg = 0; cg < 8; ++cg) {
                         uint32_t h[4], l[4];
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
-                            const float a = __uint_as_float(v[c * 8 + 2 * i]), b = __uint_as_float(v[c * 8 + 2 * i + 1]);
+                            const int j = cg * 8 + 2 * i;
+                            const float a = j < tn ? __uint_as_float(v[j]) : 0.f;
+                            const float b = j + 1 < tn ? __uint_as_float(v[j + 1]) : 0.f;
                             const float ha = __bfloat162float(__float2bfloat16_rn(a));
                             const float hb = __bfloat162float(__float2bfloat16_rn(b));
                             h[i] = pack_bf16x2(a, b);
                             l[i] = pack_bf16x2(a - ha, b - hb);
                         }
-                        const int off = lane * 128 + ((c ^ (lane & 7)) << 4);
-                        *reinterpret_cast<uint4*>(so + off) = make_uint4(h[0], h[1], h[2], h[3]);
-                        *reinterpret_cast<uint4*>(so + 4096 + off) = make_uint4(l[0], l[1], l[2], l[3]);
+                        const int q = cg >> 2, gq = cg & 3;
+                        const int uh = q * 8 + gq, ul = q * 8 + 4 + gq;
+                        *reinterpret_cast<uint4*>(so + lane * 256 + ((uh ^ (lane & 15)) << 4)) = make_uint4(h[0], h[1], h[2], h[3]);
+                        *reinterpret_cast<uint4*>(so + lane * 256 + ((ul ^ (lane & 15)) << 4)) = make_uint4(l[0], l[1], l[2], l[3]);
                     }
                     __syncwarp();
-                    __nv_bfloat16* Ch = (__nv_bfloat16*)g.C;
-                    __nv_bfloat16* Cl = (__nv_bfloat16*)g.C2;
-                    const int c = lane & 7;
+                    __nv_bfloat16* C = (__nv_bfloat16*)g.C;
+                    const int u = lane & 15;
+                    const int ucol = (u >> 3) * 32 + (u & 3) * 8;   // first column of unit u in the chunk
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const int row = i * 4 + (lane >> 3);
-                        const int off = row * 128 + ((c ^ (row & 7)) << 4);
-                        const uint4 hv = *reinterpret_cast<const uint4*>(so + off);
-                        const uint4 lv = *reinterpret_cast<const uint4*>(so + 4096 + off);
-                        if (sp * 32 + row < tile.tm && c * 8 < tn) {
-                            const int64_t e = tile.c_off + (int64_t)(tile.row0 + sp * 32 + row) * tile.ldc + col0 + c * 8;
-                            *reinterpret_cast<uint4*>(Ch + e) = hv;
-                            *reinterpret_cast<uint4*>(Cl + e) = lv;
+                    for (int i = 0; i < 16; ++i) {
+                        const int row = i * 2 + (lane >> 4);
+                        const uint4 val = *reinterpret_cast<const uint4*>(so + row * 256 + ((u ^ (row & 15)) << 4));
+                        if (sp * 32 + row < tile.tm && ucol < tn) {
+                            // (col0 + c0) is a multiple of 32: the chunk starts a panel K step
+                            const int64_t e = tile.c_off + (int64_t)(tile.row0 + sp * 32 + row) * tile.ldc +
+                                              (int64_t)((tile.col0 + c0) >> 5) * 64 + u * 8;
+                            *reinterpret_cast<uint4*>(C + e) = val;
                         }
                     }
                     __syncwarp();   // the staging area is rewritten by the next chunk
@@ -339,6 +350,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(GGArgs g) {
                     double* C = (double*)g.C;
                     if (rl < tile.tm) {
                         const int64_t gr = tile.row0 + rl;
+                        const int col0 = tile.col0 + c0;
 #pragma unroll
                         for (int j = 0; j < 64; ++j) {
                             if (j < tn) {
@@ -364,13 +376,12 @@ cudaError_t umma_init() {
     return cudaFuncSetAttribute(gg_umma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
 }
 
-cudaError_t launch_gg_umma(int out_split, const GGArgs& a, cudaStream_t st) {
+cudaError_t launch_gg_umma(int out_split, const GGArgs& a, const TmaMaps& maps, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
-    if (!a.amaps || !a.bmaps || !a.steps || !a.cta_tiles || a.ncta <= 0) return cudaErrorInvalidValue;
-    if (out_split && !a.transC) return cudaErrorInvalidValue;   // the staged epilogue writes row-major tiles
-    const int grid = a.ncta;
-    if (out_split) gg_umma_kernel<1><<<grid, um::NT, um::SMEM_BYTES, st>>>(a);
-    else gg_umma_kernel<0><<<grid, um::NT, um::SMEM_BYTES, st>>>(a);
+    if (!a.steps || !a.cta_tiles || a.ncta <= 0 || !a.C) return cudaErrorInvalidValue;
+    if (out_split && !a.transC) return cudaErrorInvalidValue;   // the staged epilogue writes panel rows
+    if (out_split) gg_umma_kernel<1><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    else gg_umma_kernel<0><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
     return cudaGetLastError();
 }
 
