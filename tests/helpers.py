@@ -61,3 +61,38 @@ def compare_tripods(A, B):
     num = sum(float(np.sum((ka[k] - kb[k]) ** 2)) for k in ka)
     den = sum(float(np.sum(kb[k] ** 2)) for k in kb)
     return np.sqrt(num / max(den, 1e-300))
+
+
+# ---- golden fixtures: block tables and MPO sites as flat npz arrays -----------
+def blocks_to_npz(prefix, B, out):
+    out[prefix + "_nq"] = np.array([B.nq])
+    for name in ("qin", "qout", "leg", "rows", "cols", "offset", "data"):
+        out[prefix + "_" + name] = getattr(B, name)
+    if B.qmid is not None:
+        out[prefix + "_qmid"] = B.qmid
+
+
+def blocks_from_npz(prefix, z):
+    from vmps_gb300.blocks import Blocks
+    nq = int(z[prefix + "_nq"][0])
+    qmid = z[prefix + "_qmid"] if prefix + "_qmid" in z else None
+    return Blocks(nq, z[prefix + "_qin"], z[prefix + "_qout"], z[prefix + "_leg"], z[prefix + "_rows"],
+                  z[prefix + "_cols"], data=z[prefix + "_data"], qmid=qmid, offset=z[prefix + "_offset"])
+
+
+def mpo_to_npz(prefix, W, out):
+    a = W.arrays()
+    out[prefix + "_nq"] = np.array([W.nq])
+    for name in ("s1", "s2", "k", "qin", "qout", "row", "col", "val", "qloc", "qop"):
+        out[prefix + "_" + name] = a[name]
+
+
+def mpo_from_npz(prefix, z):
+    from vmps_gb300.blocks import MpoSite
+    nq = int(z[prefix + "_nq"][0])
+    W = MpoSite(nq, [tuple(q) for q in z[prefix + "_qloc"]], [tuple(q) for q in z[prefix + "_qop"]])
+    for i in range(len(z[prefix + "_val"])):
+        W.add(int(z[prefix + "_s1"][i]), int(z[prefix + "_s2"][i]), int(z[prefix + "_k"][i]),
+              tuple(z[prefix + "_qin"][i]), tuple(z[prefix + "_qout"][i]), int(z[prefix + "_row"][i]),
+              int(z[prefix + "_col"][i]), float(z[prefix + "_val"][i]))
+    return W
