@@ -134,6 +134,8 @@ def test_engine_dmrg_heisenberg_4_closed_form(gpu_ctx):
     from vmps_gb300.dmrg import dmrg1
     from vmps_gb300.mps import RandomMPS
     m = models.heisenberg_u1(4)
-    mps = RandomMPS(m, (0,), 4, seed=3).canonicalize(0, 0)
+    # D = 8 gives complete bond bases (the middle bond needs Sz=0 twice); single-site
+    # sweeps keep the bases fixed, so smaller D cannot reach the exact state
+    mps = RandomMPS(m, (0,), 8, seed=3).canonicalize(0, 0)
     res = dmrg1(gpu_ctx, m, mps, n_sweeps=2, precision="fp64")
     assert abs(res["energies"][-1] - E_HEIS_4) < 1e-12
