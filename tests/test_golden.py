@@ -85,7 +85,6 @@ def test_known_hubbard_dimer():
 @pytest.mark.gpu
 @pytest.mark.parametrize("path", PIVOTS, ids=[os.path.basename(p) for p in PIVOTS])
 def test_engine_matches_golden_pivot(gpu_ctx, path):
-    from vmps_gb300.blocks import Symmetry  # noqa: F401
     from vmps_gb300.pivot import PivotMatrix0, PivotMatrix1, PivotMatrix2
     z = np.load(path)
     kind, L, R, V, W = _pivot(z)
