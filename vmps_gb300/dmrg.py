@@ -72,13 +72,13 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
             H.close()
             mps.A[l].data[:] = v
             if right and l < L - 1:
-                mps.A[l], Rf = left_normalize(mps.A[l], nq)
+                mps.A[l], Rf = left_normalize(mps.A[l], nq, sym=mps.sym)
                 _push_right(mps.A[l + 1], Rf)
                 e = EnvUpdate(ctx, sym, "L", envL[l], mps.A[l], model.W[l], mps.A[l])
                 envL[l + 1] = e.run(envL[l], mps.A[l], mps.A[l])
                 e.close()
             elif not right and l > 0:
-                mps.A[l], Lf = right_normalize(mps.A[l], nq)
+                mps.A[l], Lf = right_normalize(mps.A[l], nq, sym=mps.sym)
                 _push_left(mps.A[l - 1], Lf)
                 e = EnvUpdate(ctx, sym, "R", envR[l + 1], mps.A[l], model.W[l], mps.A[l])
                 envR[l] = e.run(envR[l + 1], mps.A[l], mps.A[l])

@@ -154,6 +154,58 @@ def hubbard_u1xu1(L, t=1.0, U=4.0):
     return ChainModel(sym, L, qloc, ops, terms, onsite, name=f"HubbardU1xU1(L={L},t={t},U={U})")
 
 
+class SU2ChainModel(ChainModel):
+    """A ChainModel whose local basis and operators are SU(2)-reduced: every
+    operator is (reduced matrix over the local multiplets, operator multiplet),
+    and W holds the reduced matrix elements, as MpoTerms::calc_W does
+    (MpoTerms.h:1175-1232: W[s1][s2][k](row, col) = op.data(s1, s2) with
+    qOp[k] = op.Q); the Clebsch-Gordan structure lives in the contraction
+    coefficients (coeff_HPsi, coeff_buildL/R)."""
+
+    def _site(self, l):
+        d = self.d
+        ain, aout = self._sector_index(self.aux[l]), self._sector_index(self.aux[l + 1])
+        entries = []   # (state_in, state_out, matrix, operator QN)
+        vac = self.sym.vacuum()
+        I = np.eye(d)
+        if "IDLE" in ain and "IDLE" in aout:
+            entries.append(("IDLE", "IDLE", I, vac))
+        if "DONE" in ain and "DONE" in aout:
+            entries.append(("DONE", "DONE", I, vac))
+        for t, (a, b, c) in enumerate(self.terms):
+            if "IDLE" in ain and f"OPEN{t}" in aout:
+                entries.append(("IDLE", f"OPEN{t}", c * self.ops[a][0], self.ops[a][1]))
+            if f"OPEN{t}" in ain and "DONE" in aout:
+                entries.append((f"OPEN{t}", "DONE", self.ops[b][0], self.ops[b][1]))
+        qop_list = sorted({tuple(e[3]) for e in entries})
+        kidx = {q: i for i, q in enumerate(qop_list)}
+        site = MpoSite(nq=self.sym.nq, qloc=list(self.qloc), qop=qop_list)
+        for sin, sout, M, qop in entries:
+            (qi, ri), (qo, co) = ain[sin], aout[sout]
+            assert tuple(qo) in self.sym.fuse(tuple(qi), tuple(qop)), (qi, qop, qo)
+            for s1 in range(d):
+                for s2 in range(d):
+                    if abs(M[s1, s2]) >= 1e-15:
+                        site.add(s1, s2, kidx[tuple(qop)], qi, qo, ri, co, M[s1, s2])
+        return site
+
+
+def heisenberg_su2(L, J=1.0):
+    """Spin-1/2 XXX chain with SU(2) symmetry, H = J sum S_i . S_i+1, as the reference's
+    HeisenbergSU2 builds it (models/HeisenbergSU2.h:270-283): the bond term is
+    sqrt(3) J (S^dagger_i x S_i+1) coupled to a singlet.  One local multiplet (q = 2);
+    reduced elements <1/2||S||1/2> = sqrt(S(S+1)) (sites/SpinSiteSU2.h:60) and
+    S^dagger = the adjoint with coeff_adjoint(2, 2, 3) = -1 (tensors/SiteOperatorQ.h:292-305,
+    symmetry/SU2.h:336-341)."""
+    sym = Symmetry(("SU2",))
+    qloc = [(2,)]
+    s = np.array([[np.sqrt(0.75)]])
+    sdag = -s
+    ops = {"Sdag": (sdag, (3,)), "S": (s, (3,))}
+    terms = [("Sdag", "S", np.sqrt(3.0) * J)]
+    return SU2ChainModel(sym, L, qloc, ops, terms, [], name=f"HeisenbergSU2(L={L},J={J})")
+
+
 # ---------------------------------------------------------------------------
 # exact dense Hamiltonians (independent of the MPO), for the oracle's pins
 # ---------------------------------------------------------------------------

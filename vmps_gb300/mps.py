@@ -1,4 +1,4 @@
-"""Random block-sparse MPS with U(1)-type bond bases (host-side state layer).
+"""Random block-sparse MPS (host-side state layer), abelian or SU(2) bond bases.
 
 The reference initialises an Mps through outerResize/innerResize and
 setRandom (Mps.h:1124-1262, :1380-1560, :1639-1665) and grows the bond bases
@@ -13,6 +13,13 @@ during its sweeps.  The synthetic states used here fix the bond bases up front:
   large-D frozen-site workloads;
 * blocks are N(0,1) from a seeded generator, then left-normalised (QR) left of
   the pivot and right-normalised (LQ) right of it.
+
+With SU(2) components the QNs are multiplets q = 2S+1 and fuse by the
+Clebsch-Gordan series; blocks are reduced matrices.  Right-normalisation then
+weights every block by sqrt(q_out/q_in) before the LQ and removes the weight
+after (Mps.h:2664-2692, Symmetry::coeff_leftSweep), so that
+sum_{s,qout} (q_out/q_in) A A^dagger = 1 (coeff_rightOrtho); left-normalisation
+is a plain QR per outgoing multiplet (Mps.h:2600-2616).
 """
 from __future__ import annotations
 
@@ -31,9 +38,31 @@ def _sub(a, b):
     return tuple(x - y for x, y in zip(a, b))
 
 
-def bond_bases(qloc, L, Qtot, Dmax, profile="even", sigma=None):
-    """dims[l] : dict QN -> sector dimension at bond l (l = 0..L)."""
-    vac = tuple(0 for _ in Qtot)
+def _fwd(sym, q, s):
+    """QNs reachable from bond QN q through local QN s"""
+    return [_add(q, s)] if sym is None else sym.fuse(tuple(q), tuple(s))
+
+
+def _bwd(sym, q, s):
+    """bond QNs q' with q reachable from q' through local QN s"""
+    return [_sub(q, s)] if sym is None else sym.fuse(tuple(q), sym.flip(tuple(s)))
+
+
+def _ortho_weight(sym, qin, qout):
+    """sqrt(q_out / q_in) over the SU(2) components (1 for abelian ones)"""
+    if sym is None:
+        return 1.0
+    w = 1.0
+    for a, b, k in zip(qin, qout, sym.kinds):
+        if k == "SU2":
+            w *= b / a
+    return math.sqrt(w)
+
+
+def bond_bases(qloc, L, Qtot, Dmax, profile="even", sigma=None, sym=None):
+    """dims[l] : dict QN -> sector dimension at bond l (l = 0..L).  sym = None:
+    additive (U(1)-type) QNs; otherwise the symmetry's fusion rules."""
+    vac = tuple(0 for _ in Qtot) if sym is None else sym.vacuum()
     # exact Hilbert-space counts from the left and from the right (capped to avoid huge ints)
     cap = 10 ** 12
     fromL = [dict() for _ in range(L + 1)]
@@ -41,15 +70,15 @@ def bond_bases(qloc, L, Qtot, Dmax, profile="even", sigma=None):
     for l in range(L):
         for q, n in fromL[l].items():
             for s in qloc:
-                q2 = _add(q, s)
-                fromL[l + 1][q2] = min(cap, fromL[l + 1].get(q2, 0) + n)
+                for q2 in _fwd(sym, q, s):
+                    fromL[l + 1][q2] = min(cap, fromL[l + 1].get(q2, 0) + n)
     fromR = [dict() for _ in range(L + 1)]
     fromR[L][tuple(Qtot)] = 1
     for l in range(L, 0, -1):
         for q, n in fromR[l].items():
             for s in qloc:
-                q2 = _sub(q, s)
-                fromR[l - 1][q2] = min(cap, fromR[l - 1].get(q2, 0) + n)
+                for q2 in _bwd(sym, q, s):
+                    fromR[l - 1][q2] = min(cap, fromR[l - 1].get(q2, 0) + n)
     dims = []
     for l in range(L + 1):
         allowed = {q: min(fromL[l][q], fromR[l][q]) for q in fromL[l] if q in fromR[l]}
@@ -79,7 +108,7 @@ def bond_bases(qloc, L, Qtot, Dmax, profile="even", sigma=None):
         changed = False
         for l in range(1, L + 1):
             for q in list(dims[l]):
-                lim = sum(dims[l - 1].get(_sub(q, s), 0) for s in qloc)
+                lim = sum(dims[l - 1].get(qp, 0) for s in qloc for qp in _bwd(sym, q, s))
                 if dims[l][q] > lim:
                     changed = True
                     if lim == 0:
@@ -88,7 +117,7 @@ def bond_bases(qloc, L, Qtot, Dmax, profile="even", sigma=None):
                         dims[l][q] = lim
         for l in range(L - 1, -1, -1):
             for q in list(dims[l]):
-                lim = sum(dims[l + 1].get(_add(q, s), 0) for s in qloc)
+                lim = sum(dims[l + 1].get(qn, 0) for s in qloc for qn in _fwd(sym, q, s))
                 if dims[l][q] > lim:
                     changed = True
                     if lim == 0:
@@ -100,25 +129,25 @@ def bond_bases(qloc, L, Qtot, Dmax, profile="even", sigma=None):
     return dims
 
 
-def site_layout(qloc, din, dout, nq):
-    """Block table of A[s] with blocks (qin -> qin + qloc[s]) present in both bases."""
+def site_layout(qloc, din, dout, nq, sym=None):
+    """Block table of A[s] with blocks (qin -> qout in qin x qloc[s]) present in both bases."""
     ent = []
     for s, qs in enumerate(qloc):
         for qin in sorted(din):
-            qout = _add(qin, qs)
-            if qout in dout:
-                ent.append((s, qin, qout, din[qin], dout[qout]))
+            for qout in _fwd(sym, qin, qs):
+                if qout in dout:
+                    ent.append((s, qin, qout, din[qin], dout[qout]))
     return Blocks(nq, [e[1] for e in ent], [e[2] for e in ent], [e[0] for e in ent],
                   [e[3] for e in ent], [e[4] for e in ent])
 
 
-def random_site(qloc, din, dout, nq, rng):
-    A = site_layout(qloc, din, dout, nq)
+def random_site(qloc, din, dout, nq, rng, sym=None):
+    A = site_layout(qloc, din, dout, nq, sym)
     A.data[:] = rng.standard_normal(A.data.size)
     return A
 
 
-def left_normalize(A, nq, carry=None):
+def left_normalize(A, nq, carry=None, sym=None):
     """QR per outgoing sector: A -> Q (left-orthonormal), returns (Q, R dict qout->R).
     `carry` (dict qin -> matrix) multiplies the incoming bond first."""
     A = A.like(A.data.copy())
@@ -142,9 +171,10 @@ def left_normalize(A, nq, carry=None):
     return A, Rs
 
 
-def right_normalize(A, nq, carry=None):
+def right_normalize(A, nq, carry=None, sym=None):
     """LQ per incoming sector: A -> Q (right-orthonormal), returns (Q, Lfac dict qin->L).
-    `carry` (dict qout -> matrix) multiplies the outgoing bond first (A @ carry)."""
+    `carry` (dict qout -> matrix) multiplies the outgoing bond first (A @ carry).
+    SU(2) blocks carry the weight sqrt(q_out/q_in) through the LQ."""
     A = A.like(A.data.copy())
     if carry is not None:
         for i in range(A.n):
@@ -156,13 +186,14 @@ def right_normalize(A, nq, carry=None):
         groups.setdefault(tuple(A.qin[i]), []).append(i)
     Ls = {}
     for qin, idx in groups.items():
-        M = np.hstack([A.block(i) for i in idx])
+        w = [_ortho_weight(sym, qin, tuple(A.qout[i])) for i in idx]
+        M = np.hstack([A.block(i) * wi for i, wi in zip(idx, w)])
         Q, R = np.linalg.qr(M.T)
         Qt = Q.T
         c0 = 0
-        for i in idx:
+        for i, wi in zip(idx, w):
             c = A.block(i).shape[1]
-            A.block(i)[...] = Qt[:, c0:c0 + c]
+            A.block(i)[...] = Qt[:, c0:c0 + c] / wi
             c0 += c
         Ls[qin] = R.T
     return A, Ls
@@ -177,16 +208,18 @@ class RandomMPS:
         self.nq = model.sym.nq
         self.qloc = model.qloc
         self.Qtot = tuple(Qtot)
-        self.dims = bond_bases(model.qloc, model.L, Qtot, Dmax, profile=profile, sigma=sigma)
+        self.sym = model.sym if model.sym.nonabelian else None
+        self.dims = bond_bases(model.qloc, model.L, Qtot, Dmax, profile=profile, sigma=sigma, sym=self.sym)
         rng = np.random.default_rng(seed)
-        self.A = [random_site(self.qloc, self.dims[l], self.dims[l + 1], self.nq, rng) for l in range(self.L)]
+        self.A = [random_site(self.qloc, self.dims[l], self.dims[l + 1], self.nq, rng, self.sym)
+                  for l in range(self.L)]
 
     def canonicalize(self, pivot_lo, pivot_hi):
         """Sites < pivot_lo left-normalised, sites > pivot_hi right-normalised;
         the factors are pushed into the pivot sites."""
         carry = None
         for l in range(pivot_lo):
-            self.A[l], carry = left_normalize(self.A[l], self.nq, carry)
+            self.A[l], carry = left_normalize(self.A[l], self.nq, carry, self.sym)
         if carry is not None:
             A = self.A[pivot_lo]
             for i in range(A.n):
@@ -194,7 +227,7 @@ class RandomMPS:
                 A.block(i)[...] = carry[q] @ A.block(i)
         carry = None
         for l in range(self.L - 1, pivot_hi, -1):
-            self.A[l], carry = right_normalize(self.A[l], self.nq, carry)
+            self.A[l], carry = right_normalize(self.A[l], self.nq, carry, self.sym)
         if carry is not None:
             A = self.A[pivot_hi]
             for i in range(A.n):
