@@ -244,6 +244,32 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra,
                  const double* Aket, double* Enew, int precision);
 int vmps_env_destroy(vmps_env* e);
 
+/* ---- VUMPS MpoTransferMatrix -----------------------------------------------
+ * The linear operator (1 - T_L + |R)(1|) (dir LEFT) or (1 - T_R + |1)(L|) (dir
+ * RIGHT) of the VUMPS environment equations, HxV(MpoTransferMatrix, Vin, Vout)
+ * of VUMPS/VumpsMpoTransferMatrix.h:99-212:
+ *   T V  = the chain of contract_L over the cell sites 0..ncell-1 (FIXED_ROWS on
+ *          site 0, FIXED_COLS on site ncell-1) or of contract_R over
+ *          ncell-1..0 (FIXED_COLS on site ncell-1, FIXED_ROWS on site 0);
+ *   Vout = Vin - T Vin + contract_LR(ab, Vin, LReigen) * 1 on the blocks of the
+ *          auxiliary slot ab (basis_order[ab], which must lie in the vacuum
+ *          sector) that T Vin and Vin share; zero elsewhere.
+ * Abra/Aket/W are arrays of ncell site tensors (indexed by cell site); LReigen
+ * is a Biped (qin, qout, rows, cols, offset); V is the Tripod layout of the
+ * transfer vector (Vin and Vout share it).  The site tensors are uploaded
+ * once; vmps_transfer_hxv takes host buffers in the layout of V.              */
+typedef struct vmps_transfer_s vmps_transfer;
+int vmps_transfer_create(vmps_ctx* ctx, const vmps_symmetry* sym, int dir, int ncell,
+                         const vmps_blocks* const* Abra, const double* const* Abra_data,
+                         const vmps_blocks* const* Aket, const double* const* Aket_data,
+                         const vmps_mpo_site* const* W,
+                         const vmps_blocks* LReigen, const double* LReigen_data,
+                         int64_t ab, int64_t n_order, const int32_t* order_qn,
+                         const int32_t* order_index, const int64_t* order_value,
+                         const vmps_blocks* V, vmps_transfer** out);
+int vmps_transfer_hxv(vmps_transfer* t, const double* vin, double* vout, int precision);
+int vmps_transfer_destroy(vmps_transfer* t);
+
 /* ---- allocation-free chain product -------------------------------------------
  * No counterpart in the reference: an extra entry point of this library.
  * out (m x p) = alpha * op(X) * Y * op(Z) in FP64 for single dense blocks

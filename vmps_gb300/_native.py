@@ -110,6 +110,14 @@ _PROTOS = [
     ("vmps_env_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),
     ("vmps_env_run", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, C.c_int]),
     ("vmps_env_destroy", C.c_int, [C.c_void_p]),
+    ("vmps_transfer_create", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.c_int, C.c_int,
+                                       C.POINTER(C.POINTER(vmps_blocks)), C.POINTER(f64p),
+                                       C.POINTER(C.POINTER(vmps_blocks)), C.POINTER(f64p),
+                                       C.POINTER(C.POINTER(vmps_mpo_site)), C.POINTER(vmps_blocks), f64p,
+                                       C.c_int64, C.c_int64, i32p, i32p, i64p, C.POINTER(vmps_blocks),
+                                       C.POINTER(C.c_void_p)]),
+    ("vmps_transfer_hxv", C.c_int, [C.c_void_p, f64p, f64p, C.c_int]),
+    ("vmps_transfer_destroy", C.c_int, [C.c_void_p]),
     ("vmps_chain_fp64_noalloc", C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
                                           C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_int32, C.c_double,
                                           C.c_void_p, C.c_void_p]),

@@ -369,6 +369,46 @@ __global__ void finite_kernel(const double* __restrict__ x, int64_t n, int* __re
         if (!isfinite(x[i])) { atomicOr(bad, 1); return; }
 }
 
+// ---------------------------------------------------------------------------
+// VUMPS transfer operator pieces
+// ---------------------------------------------------------------------------
+// part[b] = w_b * sum_ij V[i + j*v_ld] * LR[j + i*lr_ld]  (the trace of a block product)
+__global__ void trace_pairs_kernel(const TracePair* __restrict__ tp, int n, const double* __restrict__ V,
+                                   const double* __restrict__ LR, double* __restrict__ part) {
+    __shared__ double red[kDotThreads];
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const TracePair p = tp[b];
+        double s = 0;
+        for (int e = threadIdx.x; e < p.rows * p.cols; e += kDotThreads) {
+            const int j = e / p.rows, i = e - j * p.rows;
+            s = fma(V[p.v_off + i + (int64_t)j * p.v_ld], LR[p.lr_off + j + (int64_t)i * p.lr_ld], s);
+        }
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = kDotThreads / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) part[b] = p.weight * red[0];
+        __syncthreads();
+    }
+}
+
+// out[block] = V[block] - T[block] + (*s) * identity, per matched block pair
+__global__ void transfer_combine_kernel(const CombineBlock* __restrict__ cb, int n, const double* __restrict__ V,
+                                        const double* __restrict__ T, double* __restrict__ out,
+                                        const double* __restrict__ s) {
+    const double sc = *s;
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const CombineBlock c = cb[b];
+        for (int e = threadIdx.x; e < c.rows * c.cols; e += blockDim.x) {
+            const int j = e / c.rows, i = e - j * c.rows;
+            const int64_t vo = c.v_off + i + (int64_t)j * c.v_ld;
+            out[vo] = V[vo] - T[c.t_off + i + (int64_t)j * c.t_ld] + (i == j ? sc : 0.0);
+        }
+    }
+}
+
 // ===========================================================================
 // launchers
 // ===========================================================================
@@ -400,6 +440,25 @@ cudaError_t launch_panel_split(const PanelPiece* pieces, int np, const double* s
     if (np <= 0) return cudaSuccess;
     if (!pieces || !src || !dst) return cudaErrorInvalidValue;
     panel_split_kernel<<<min(np, 4096), 256, 0, st>>>(pieces, np, src, (__nv_bfloat16*)dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_pairs(const TracePair* tp, int n, const double* V, const double* LR, double* part, double* out,
+                               cudaStream_t st) {
+    if (!part || !out) return cudaErrorInvalidValue;
+    if (n > 0) {
+        if (!tp || !V || !LR) return cudaErrorInvalidValue;
+        trace_pairs_kernel<<<min(n, 4096), kDotThreads, 0, st>>>(tp, n, V, LR, part);
+    }
+    sum_partial_kernel<<<1, kDotThreads, 0, st>>>(part, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transfer_combine(const CombineBlock* cb, int n, const double* V, const double* T, double* out,
+                                    const double* s, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (!cb || !V || !T || !out || !s) return cudaErrorInvalidValue;
+    transfer_combine_kernel<<<min(n, 4096), 256, 0, st>>>(cb, n, V, T, out, s);
     return cudaGetLastError();
 }
 

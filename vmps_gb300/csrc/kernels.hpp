@@ -59,5 +59,12 @@ cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStr
 cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t st);
 cudaError_t launch_combine(const double* V, int nv, int64_t n, const double* c, double* y, cudaStream_t st);
 cudaError_t launch_finite(const double* x, int64_t n, int* bad, cudaStream_t st);
+// VUMPS transfer operator: out = sum_b w_b tr(V_b LR_b) (deterministic); out[V block] = V - T + s * 1
+struct TracePair { int64_t v_off, lr_off; int32_t rows, cols, v_ld, lr_ld; double weight; };
+struct CombineBlock { int64_t v_off, t_off; int32_t rows, cols, v_ld, t_ld; };
+cudaError_t launch_trace_pairs(const TracePair* tp, int n, const double* V, const double* LR, double* part, double* out,
+                               cudaStream_t st);
+cudaError_t launch_transfer_combine(const CombineBlock* cb, int n, const double* V, const double* T, double* out,
+                                    const double* s, cudaStream_t st);
 
 }  // namespace vmps

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -1444,6 +1445,213 @@ int vmps_env_run(vmps_env* e, const double* Eold, const double* Abra, const doub
 
 int vmps_env_destroy(vmps_env* e) {
     delete e;
+    return VMPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// VUMPS MpoTransferMatrix (VUMPS/VumpsMpoTransferMatrix.h:99-212)
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+// a vmps_blocks view of a block table (the table owns the storage it points into)
+struct BlocksView {
+    std::vector<int32_t> qin, qout, qmid, leg;
+    std::vector<int64_t> rows, cols, off;
+    vmps_blocks b{};
+    BlocksView(const BlockTable& t, int nq) {
+        for (int64_t i = 0; i < t.n; ++i)
+            for (int c = 0; c < nq; ++c) {
+                qin.push_back(t.qin[i].v[c]);
+                qout.push_back(t.qout[i].v[c]);
+                qmid.push_back(t.has_mid ? t.qmid[i].v[c] : 0);
+            }
+        leg.assign(t.leg.begin(), t.leg.end());
+        rows = t.rows; cols = t.cols; off = t.off;
+        b.nblocks = t.n;
+        b.qin = qin.data(); b.qout = qout.data(); b.qmid = qmid.data(); b.leg = leg.data();
+        b.rows = rows.data(); b.cols = cols.data(); b.offset = off.data();
+    }
+};
+
+struct vmps_transfer_s {
+    vmps_ctx* ctx = nullptr;
+    Symmetry sym;
+    std::vector<vmps_env*> chain;   // owned; chain[k+1] reads the output of chain[k]
+    BlockTable Vt;                  // transfer vector layout
+    DevLayout Vd;
+    BlockTable LRt;
+    DevLayout LRd;
+    DBuf dLR, dVout, stage_in, stage_out, pk, dTrace, dCombine, part, scal;
+    int npk = 0, ntrace = 0, ncombine = 0;
+    std::vector<char> prepped[2];
+    ~vmps_transfer_s() {
+        for (vmps_env* e : chain) delete e;
+    }
+    cudaStream_t st() const { return ctx->stream; }
+};
+
+static std::vector<int32_t> block_key(const BlockTable& t, int64_t i, int nq, bool with_leg) {
+    std::vector<int32_t> k;
+    for (int c = 0; c < nq; ++c) k.push_back(t.qin[i].v[c]);
+    for (int c = 0; c < nq; ++c) k.push_back(t.qout[i].v[c]);
+    if (t.has_mid)
+        for (int c = 0; c < nq; ++c) k.push_back(t.qmid[i].v[c]);
+    if (with_leg) k.push_back(t.leg[i]);
+    return k;
+}
+
+extern "C" {
+
+int vmps_transfer_create(vmps_ctx* ctx, const vmps_symmetry* symd, int dir, int ncell, const vmps_blocks* const* Abra,
+                         const double* const* Abra_data, const vmps_blocks* const* Aket,
+                         const double* const* Aket_data, const vmps_mpo_site* const* W, const vmps_blocks* LReigen,
+                         const double* LReigen_data, int64_t ab, int64_t n_order, const int32_t* order_qn,
+                         const int32_t* order_index, const int64_t* order_value, const vmps_blocks* V,
+                         vmps_transfer** out) {
+    API_BEGIN
+    if (!ctx || !symd || !out || !Abra || !Abra_data || !Aket || !Aket_data || !W || !LReigen || !LReigen_data || !V)
+        return set_err(VMPS_E_ARG, "null argument");
+    if (dir != VMPS_ENV_LEFT && dir != VMPS_ENV_RIGHT) return set_err(VMPS_E_ARG, "direction must be LEFT or RIGHT");
+    if (ncell < 1) return set_err(VMPS_E_ARG, "the unit cell needs at least one site");
+    if (n_order <= 0 || !order_qn || !order_index || !order_value)
+        return set_err(VMPS_E_ARG, "the transfer operator needs the basis order map");
+    require_device(ctx);
+    Symmetry sym = make_sym(symd);
+    const int nq = sym.nq;
+    // (QN, index) of auxiliary position ab (basis_order[ab]); contract_LR requires the vacuum sector
+    QN abq;
+    int32_t abi = -1;
+    for (int64_t i = 0; i < n_order; ++i)
+        if (order_value[i] == ab) {
+            for (int c = 0; c < nq; ++c) abq.v[c] = order_qn[i * nq + c];
+            abi = order_index[i];
+        }
+    if (abi < 0) return set_err(VMPS_E_ARG, "ab is not a position of the basis order map");
+    if (!(abq == sym.vacuum())) return set_err(VMPS_E_ARG, "contract_LR needs ab in the vacuum sector");
+    std::unique_ptr<vmps_transfer> t(new vmps_transfer_s());
+    t->ctx = ctx;
+    t->sym = sym;
+    t->Vt = parse_blocks(sym, V, true);
+    t->Vd = make_dev_layout(t->Vt.rows, t->Vt.cols);
+    t->LRt = parse_blocks(sym, LReigen, false);
+    t->LRd = make_dev_layout(t->LRt.rows, t->LRt.cols);
+    cudaStream_t st = ctx->stream;
+    CK(cudaSetDevice(ctx->device));
+    // the chain (VumpsMpoTransferMatrix.h:115-152): left: sites 0..n-1, FIXED_ROWS on the first and FIXED_COLS
+    // on the last (the last rule wins for one site); right: sites n-1..0, FIXED_ROWS on site 0 and FIXED_COLS
+    // on site n-1 (the site-0 rule wins for one site)
+    std::unique_ptr<BlocksView> cur(new BlocksView(t->Vt, nq));
+    for (int k = 0; k < ncell; ++k) {
+        const int l = dir == VMPS_ENV_LEFT ? k : ncell - 1 - k;
+        int mode = VMPS_ENV_FULL;
+        if (dir == VMPS_ENV_LEFT) mode = l == ncell - 1 ? VMPS_ENV_FIXED_COLS : (l == 0 ? VMPS_ENV_FIXED_ROWS : VMPS_ENV_FULL);
+        else mode = l == 0 ? VMPS_ENV_FIXED_ROWS : (l == ncell - 1 ? VMPS_ENV_FIXED_COLS : VMPS_ENV_FULL);
+        vmps_env* e = nullptr;
+        const int rc = vmps_env_create_mode(ctx, symd, dir, mode, ab, n_order, order_qn, order_index, order_value,
+                                            &cur->b, Abra[l], W[l], Aket[l], &e);
+        if (rc != VMPS_OK) return rc;
+        t->chain.push_back(e);
+        if (k > 0) {
+            const vmps_env* p = t->chain[k - 1];
+            if (p->Nd.total != e->Ed.total || p->Nd.rows != e->Ed.rows || p->Nd.cols != e->Ed.cols)
+                throw std::logic_error("transfer chain: layouts of consecutive environments differ");
+        }
+        upload_blocks_padded(ctx, e->Bt, e->Bd, Abra_data[l], e->dB, st);
+        upload_blocks_padded(ctx, e->Kt, e->Kd, Aket_data[l], e->dK, st);
+        e->dE.alloc((size_t)std::max<int64_t>(e->Ed.total, 1) * 8, st, true);
+        e->dN.alloc((size_t)std::max<int64_t>(e->Nd.total, 1) * 8, st, true);
+        cur.reset(new BlocksView(e->Nt, nq));
+    }
+    t->prepped[0].assign(ncell, 0);
+    t->prepped[1].assign(ncell, 0);
+    upload_blocks_padded(ctx, t->LRt, t->LRd, LReigen_data, t->dLR, st);
+    // contract_LR(ab, V, LReigen) (DmrgContractions.h:995-1053): vacuum-mid blocks of V at slot ab with
+    // in == out, against the LReigen block (out, in); weight coeff_dot(out)
+    std::map<std::vector<int32_t>, int64_t> lr_of;
+    for (int64_t i = 0; i < t->LRt.n; ++i) lr_of[block_key(t->LRt, i, nq, false)] = i;
+    std::vector<TracePair> tps;
+    const QN vac = sym.vacuum();
+    for (int64_t b = 0; b < t->Vt.n; ++b) {
+        if (!(t->Vt.qmid[b] == vac) || t->Vt.leg[b] != abi || !(t->Vt.qin[b] == t->Vt.qout[b])) continue;
+        std::vector<int32_t> key;
+        for (int c = 0; c < nq; ++c) key.push_back(t->Vt.qout[b].v[c]);
+        for (int c = 0; c < nq; ++c) key.push_back(t->Vt.qin[b].v[c]);
+        auto it = lr_of.find(key);
+        if (it == lr_of.end()) continue;
+        const int64_t j = it->second;
+        if (t->LRt.rows[j] != t->Vt.cols[b] || t->LRt.cols[j] != t->Vt.rows[b])
+            return set_err(VMPS_E_SHAPE, "LReigen block does not match the transfer vector");
+        tps.push_back(TracePair{t->Vd.off[b], t->LRd.off[j], (int32_t)t->Vt.rows[b], (int32_t)t->Vt.cols[b],
+                                (int32_t)t->Vd.ld[b], (int32_t)t->LRd.ld[j], sym.coeff_dot(t->Vt.qout[b])});
+    }
+    // Vout = Vin - T Vin + LdotR * 1 on the slot-ab blocks the chain's output shares with Vin
+    std::map<std::vector<int32_t>, int64_t> v_of;
+    for (int64_t i = 0; i < t->Vt.n; ++i) v_of[block_key(t->Vt, i, nq, true)] = i;
+    const vmps_env* last = t->chain.back();
+    std::vector<CombineBlock> cbs;
+    for (int64_t k = 0; k < last->Nt.n; ++k) {
+        if (!(last->Nt.qmid[k] == abq) || last->Nt.leg[k] != abi) continue;
+        auto it = v_of.find(block_key(last->Nt, k, nq, true));
+        if (it == v_of.end()) continue;
+        const int64_t b = it->second;
+        if (t->Vt.rows[b] != last->Nt.rows[k] || t->Vt.cols[b] != last->Nt.cols[k])
+            return set_err(VMPS_E_SHAPE, "transfer output block does not match the vector");
+        cbs.push_back(CombineBlock{t->Vd.off[b], last->Nd.off[k], (int32_t)t->Vt.rows[b], (int32_t)t->Vt.cols[b],
+                                   (int32_t)t->Vd.ld[b], (int32_t)last->Nd.ld[k]});
+    }
+    t->ntrace = (int)tps.size();
+    t->ncombine = (int)cbs.size();
+    upload_vec(t->dTrace, tps, st);
+    upload_vec(t->dCombine, cbs, st);
+    t->part.alloc((size_t)std::max(1, t->ntrace) * 8, st, true);
+    t->scal.alloc(64, st, true);
+    t->dVout.alloc((size_t)std::max<int64_t>(t->Vd.total, 1) * 8, st, true);
+    auto pb = pack_blocks(t->Vt, t->Vd, nullptr);
+    t->npk = (int)pb.size();
+    upload_vec(t->pk, pb, st);
+    CK(cudaStreamSynchronize(st));
+    *out = t.release();
+    API_END
+}
+
+int vmps_transfer_hxv(vmps_transfer* t, const double* vin, double* vout, int prec) {
+    API_BEGIN
+    if (!t || !vin || !vout) return set_err(VMPS_E_ARG, "null argument");
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
+    CK(cudaSetDevice(t->ctx->device));
+    cudaStream_t st = t->st();
+    vmps_env* first = t->chain.front();
+    pack_in(t->ctx, t->pk, t->npk, vin, t->Vt.total, t->stage_in, first->dE.as<double>(), st);
+    for (size_t k = 0; k < t->chain.size(); ++k) {
+        vmps_env* e = t->chain[k];
+        DevPlan& dp = env_plan(e, prec);
+        Operands ops;
+        if (e->side == VMPS_ENV_LEFT) { ops.X = e->dB.as<double>(); ops.Z = e->dK.as<double>(); }
+        else { ops.X = e->dK.as<double>(); ops.Z = e->dB.as<double>(); }
+        ops.Y = e->dE.as<double>();
+        ops.O = e->dN.as<double>();
+        ops.err = t->ctx->err;
+        if (!t->prepped[prec][k]) {   // the site tensors are fixed: their split panels are made once
+            split_prepare(dp, ops.X, ops.Z, st);
+            t->prepped[prec][k] = 1;
+        }
+        run_plan(dp, ops, st);
+        if (k + 1 < t->chain.size() && e->Nd.total > 0)
+            CK(cudaMemcpyAsync(t->chain[k + 1]->dE.p, e->dN.p, (size_t)e->Nd.total * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    CK(launch_trace_pairs(t->dTrace.as<TracePair>(), t->ntrace, first->dE.as<double>(), t->dLR.as<double>(),
+                          t->part.as<double>(), t->scal.as<double>(), st));
+    CK(cudaMemsetAsync(t->dVout.p, 0, (size_t)std::max<int64_t>(t->Vd.total, 1) * 8, st));
+    CK(launch_transfer_combine(t->dCombine.as<CombineBlock>(), t->ncombine, first->dE.as<double>(),
+                               t->chain.back()->dN.as<double>(), t->dVout.as<double>(), t->scal.as<double>(), st));
+    pack_out(t->ctx, t->pk, t->npk, t->dVout.as<double>(), t->Vt.total, t->stage_out, vout, st);
+    CK(cudaStreamSynchronize(st));
+    check_device_error(t->ctx);
+    API_END
+}
+
+int vmps_transfer_destroy(vmps_transfer* t) {
+    delete t;
     return VMPS_OK;
 }
 
