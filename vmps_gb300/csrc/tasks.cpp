@@ -1043,27 +1043,6 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         }
     };
 
-    // prepared X blocks: rows of op(X) (m x k)
-    PanelBuilder px{{}, {}, &P.opX};
-    std::vector<int32_t> xp_idx(X.rows.size(), -1);
-    for (const Chain& c : ch) {
-        if (xp_idx[c.x] >= 0) continue;
-        xp_idx[c.x] = px.add(xm(c.x), xk(c.x));
-    }
-    px.finish();
-    P.ax = px.a;
-    for (size_t x = 0; x < X.rows.size(); ++x) {
-        if (xp_idx[x] < 0) continue;
-        const OpBlock& ob = P.opX[xp_idx[x]];
-        PrepBlock pb{};
-        pb.src_off = X.off[x]; pb.src_ld = (int32_t)X.ld[x];
-        pb.rows = (int32_t)X.rows[x]; pb.cols = (int32_t)X.cols[x];
-        pb.dst_off = ob.off; pb.dst_ld = ob.pitch;
-        pb.trans = transX ? 0 : 1;   // op(X) = X: rows of X become panel rows; op(X) = X^T: columns of X
-        pb.scale = 1.0;
-        P.prepX.push_back(pb);
-    }
-
     // scaled copies c * op(Z) (n x p): panel rows are the p columns of op(Z)
     struct CZ { uint64_t cbits; int64_t z; bool operator==(const CZ& o) const { return cbits == o.cbits && z == o.z; } };
     struct CZH { size_t operator()(const CZ& a) const { return std::hash<uint64_t>()(a.cbits * 0x9E3779B97F4A7C15ull ^ (uint64_t)a.z); } };
@@ -1096,11 +1075,13 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         P.prepZ.push_back(pb);
     }
 
-    // intermediates T = op(X) * Y (m x n): panel rows are the m rows, K = n
+    // intermediates T_j = op(X_x) * Y_y (m x n), one per distinct (x, y).  All intermediates
+    // of one V block y share B = Y_y and K: phase 1 computes them as one stacked GEMM
+    // [op(X_x1); op(X_x2); ...] * Y_y = [T_j1; T_j2; ...], so op(X) is prepared once per
+    // (x, y) in a per-y stack of the X panels, and the T_j of one y are consecutive panel rows.
     std::unordered_map<Key4, int64_t, Key4Hash> idict;
     std::vector<std::pair<int64_t, int64_t>> ipairs;
     std::vector<int64_t> chain_t(ch.size());
-    PanelBuilder pt{{}, {}, &P.opT};
     for (size_t i = 0; i < ch.size(); ++i) {
         Key4 k{ch[i].x, ch[i].y, 0, 0};
         auto it = idict.find(k);
@@ -1108,12 +1089,55 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         const int64_t id = (int64_t)ipairs.size();
         idict.emplace(k, id);
         ipairs.push_back({ch[i].x, ch[i].y});
-        pt.add(xm(ch[i].x), Y.cols[ch[i].y]);
         chain_t[i] = id;
     }
+    P.n_intermediates = (int64_t)ipairs.size();
+    std::vector<std::vector<int64_t>> by_y(Y.rows.size());
+    for (size_t j = 0; j < ipairs.size(); ++j) by_y[ipairs[j].second].push_back((int64_t)j);
+    std::vector<int64_t> stack_rows(Y.rows.size(), 0), row_in_stack(ipairs.size(), 0);
+    for (size_t y = 0; y < Y.rows.size(); ++y)
+        for (int64_t j : by_y[y]) {
+            row_in_stack[j] = stack_rows[y];
+            stack_rows[y] += xm(ipairs[j].first);
+        }
+
+    // X panels: one stack per V block with intermediates
+    PanelBuilder px{{}, {}, &P.opX};
+    std::vector<int32_t> xstack(Y.rows.size(), -1);
+    for (size_t y = 0; y < Y.rows.size(); ++y)
+        if (!by_y[y].empty()) xstack[y] = px.add(stack_rows[y], Y.rows[y]);
+    px.finish();
+    P.ax = px.a;
+    for (size_t y = 0; y < Y.rows.size(); ++y)
+        for (int64_t j : by_y[y]) {
+            const int64_t x = ipairs[j].first;
+            const OpBlock& ob = P.opX[xstack[y]];
+            PrepBlock pb{};
+            pb.src_off = X.off[x]; pb.src_ld = (int32_t)X.ld[x];
+            pb.rows = (int32_t)X.rows[x]; pb.cols = (int32_t)X.cols[x];
+            pb.dst_off = ob.off + row_in_stack[j] * ob.pitch; pb.dst_ld = ob.pitch;
+            pb.trans = transX ? 0 : 1;   // op(X) = X: rows of X become panel rows; op(X) = X^T: columns of X
+            pb.scale = 1.0;
+            P.prepX.push_back(pb);
+        }
+
+    // T panels: the same stacks; T_j is rows [row_in_stack, +m) of its y's stack
+    std::vector<OpBlock> tstacks;
+    PanelBuilder pt{{}, {}, &tstacks};
+    std::vector<int32_t> tstack(Y.rows.size(), -1);
+    for (size_t y = 0; y < Y.rows.size(); ++y)
+        if (!by_y[y].empty()) tstack[y] = pt.add(stack_rows[y], Y.cols[y]);
     pt.finish();
     P.at = pt.a;
-    P.n_intermediates = (int64_t)ipairs.size();
+    P.opT.resize(ipairs.size());
+    for (size_t j = 0; j < ipairs.size(); ++j) {
+        const OpBlock& sk = tstacks[tstack[ipairs[j].second]];
+        OpBlock b = sk;
+        b.outer = (int32_t)xm(ipairs[j].first);
+        b.row = sk.row + (int32_t)row_in_stack[j];
+        b.off = sk.off + row_in_stack[j] * sk.pitch;
+        P.opT[j] = b;
+    }
 
     // the vector Y in panels: panel rows are its columns, K = its rows
     PanelBuilder py{{}, {}, &P.opY};
@@ -1121,25 +1145,27 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
     py.finish();
     P.ay = py.a;
 
-    // phase 1: T_j = op(X)[x] * Y[y]   (A rows = m, B rows = n, K = k), written into T's panels
+    // phase 1: per V block y, [T_j1; T_j2; ...] = [op(X_x1); ...] * Y_y  (A rows = sum m, B rows = n,
+    // K = k), written into T's panel stack
     PhasePlan& p1 = P.p1;
     p1.slotA = SLOT_X; p1.slotB = SLOT_Y; p1.slotC = SLOT_T;
     p1.transA = false; p1.transB = false; p1.transC = true;
-    for (size_t j = 0; j < ipairs.size(); ++j) {
-        const int64_t x = ipairs[j].first, y = ipairs[j].second;
-        const OpBlock& ot = P.opT[j];
+    for (size_t y = 0; y < Y.rows.size(); ++y) {
+        if (by_y[y].empty()) continue;
+        const OpBlock& sx = P.opX[xstack[y]];
+        const OpBlock& st = tstacks[tstack[y]];
         GSeg s{};
         s.term_begin = (int32_t)p1.terms.size();
         s.term_count = 1;
-        p1.terms.push_back(GTerm{P.opX[xp_idx[x]].off, 1.0});
-        s.K = (int32_t)xk(x);
+        p1.terms.push_back(GTerm{sx.off, 1.0});
+        s.K = (int32_t)Y.rows[y];
         const int32_t sb = (int32_t)p1.segs.size();
         p1.segs.push_back(s);
-        p1.seg_amap.push_back(xp_idx[x]);
+        p1.seg_amap.push_back(xstack[y]);
         p1.seg_bmap.push_back((int32_t)y);
-        p1.flops += 2.0 * ot.outer * ot.K * s.K;
+        p1.flops += 2.0 * st.outer * st.K * s.K;
         // column tiles start on panel K steps (multiples of 32): the epilogue writes whole row segments
-        add_tiles(p1, ot.off, ot.pitch, ot.outer, ot.K, sb, sb + 1, kUmmaTileM, kUmmaTileN, 32);
+        add_tiles(p1, st.off, st.pitch, st.outer, st.K, sb, sb + 1, kUmmaTileM, kUmmaTileN, 32);
     }
     sort_tiles(p1);
 
