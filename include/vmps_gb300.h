@@ -188,20 +188,30 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
 
 /* ---- Lanczos ground state on the device ----------------------------------------
  * Full-reorthogonalisation Lanczos (the reference calls the external
- * LanczosSolver<PivotMatrix,PivotVector>::edgeState, solvers/DmrgSolver.h:1306-1313).
- * precision VMPS_PREC_BF16X3 runs the Krylov phase with split-precision HxV and
- * then `refine_iters` closing Lanczos steps with FP64 HxV, restarted from the
- * split-precision eigenvector.  Krylov vectors, dots and the tridiagonal solve are
- * FP64 throughout.  v (compact layout) is the start vector on entry and the
- * ground state on exit.                                                          */
+ * LanczosSolver<PivotMatrix,PivotVector>::edgeState, solvers/DmrgSolver.h:1306-1313)
+ * run on the device: one iteration (HxV, the three-term recurrence, one full
+ * Gram-Schmidt pass, alpha, beta, the next Krylov vector) is a CUDA graph the host
+ * replays while it solves the tridiagonal problem one iteration behind.
+ * precision VMPS_PREC_BF16X3 runs the Krylov phase with split-precision HxV, then
+ * corrects the Ritz vector with one FP64 HxV: its FP64 residual, projected on the
+ * split Krylov space, drives the Jacobi-Davidson correction equation solved in
+ * that space; closing FP64 Lanczos steps (at most refine_iters - 1) start from the
+ * corrected vector.  refine_iters counts all FP64 HxVs of that refinement.
+ * Krylov vectors, dots and the tridiagonal solve are FP64 throughout.  v (compact
+ * layout) is the start vector on entry and the ground state on exit.
+ * max_iter and refine_iters are below 1024.                                     */
 typedef struct {
     int32_t iterations;        /* Krylov steps in the first phase            */
-    int32_t refine_iterations; /* FP64 closing steps                          */
+    int32_t refine_iterations; /* closing FP64 Lanczos steps                  */
     int32_t hxv_fp64;
     int32_t hxv_split;
     double  energy_first;      /* eigenvalue after the first phase            */
-    double  residual;          /* ||H v - E v|| with FP64 HxV at exit         */
+    double  residual;          /* |beta_m y_m| of the last Lanczos phase: the
+                                  residual ||H v - E v|| of the returned vector
+                                  for that phase's operator (FP64 when refined) */
     double  ms_total;
+    double  ms_wait;           /* host time blocked on the device's iterations */
+    double  ms_host;           /* host time in the tridiagonal solves          */
 } vmps_lanczos_stats;
 int vmps_lanczos_ground(vmps_pivot* p, double* v, int precision, int max_iter,
                         double tol_eigval, double tol_state, int refine_iters,

@@ -223,6 +223,29 @@ def test_lanczos_energy(gpu_ctx, case):
     assert sts["hxv_split"] > 0 and sts["refine_iterations"] > 0
 
 
+def test_lanczos_residual_estimate_and_determinism(gpu_ctx):
+    """The device Lanczos reports |beta_m y_m| as the residual: it equals the
+    explicit FP64 residual ||H v - E v|| of the returned vector.  Its
+    reductions are deterministic, so two runs agree bit for bit.  The split
+    run with the Krylov-space correction reaches the FP64 energy within
+    1e-10 relative using at most refine_iters FP64 HxVs."""
+    model, mps, Lenv, Renv, W, V = pivot1_case("hubb", L=10, D=32, site=4, seed=41)
+    H = PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V)
+    v0 = np.random.default_rng(7).standard_normal(H.dim)
+    e1, x1, st1 = H.lanczos(v0, "fp64", max_iter=200, tol_eigval=1e-12, tol_state=1e-8)
+    e2, x2, st2 = H.lanczos(v0, "fp64", max_iter=200, tol_eigval=1e-12, tol_state=1e-8)
+    assert e1 == e2 and np.array_equal(x1, x2) and st1["iterations"] == st2["iterations"]
+    assert abs(np.linalg.norm(x1) - 1) < 1e-12
+    true_res = np.linalg.norm(H.apply(x1, "fp64") - e1 * x1)
+    assert abs(true_res - st1["residual"]) <= 1e-11 + 0.05 * true_res, (true_res, st1)
+    es, xs, sts = H.lanczos(v0, "bf16x3", max_iter=200, tol_eigval=1e-10, tol_state=1e-6, refine_iters=12)
+    assert abs(es - e1) < 1e-10 * abs(e1), (es, e1, sts)
+    assert 1 <= sts["hxv_fp64"] <= 12
+    true_res = np.linalg.norm(H.apply(xs, "fp64") - es * xs)
+    assert abs(true_res - sts["residual"]) <= 1e-11 + 0.05 * true_res, (true_res, sts)
+    H.close()
+
+
 @pytest.mark.parametrize("side", ["L", "R"])
 @pytest.mark.parametrize("mode,ab", [("FIXED_ROWS", 0), ("FIXED_COLS", 5), ("TRIANGULAR", 1)])
 def test_env_mode_parity(gpu_ctx, side, mode, ab):

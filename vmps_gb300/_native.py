@@ -62,7 +62,7 @@ class vmps_plan_stats(C.Structure):
 class vmps_lanczos_stats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("refine_iterations", C.c_int32), ("hxv_fp64", C.c_int32),
                 ("hxv_split", C.c_int32), ("energy_first", C.c_double), ("residual", C.c_double),
-                ("ms_total", C.c_double)]
+                ("ms_total", C.c_double), ("ms_wait", C.c_double), ("ms_host", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

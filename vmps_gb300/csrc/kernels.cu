@@ -421,7 +421,10 @@ static int grid_for(int64_t n, int threads, int cap) {
 
 // opt the split kernels into their dynamic shared memory size (once per process,
 // before any launch or stream capture)
-cudaError_t kernels_init() { return umma_init(); }
+cudaError_t kernels_init() {
+    cudaError_t e = umma_init();
+    return e != cudaSuccess ? e : lz_init();
+}
 
 cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;

@@ -67,4 +67,31 @@ cudaError_t launch_trace_pairs(const TracePair* tp, int n, const double* V, cons
 cudaError_t launch_transfer_combine(const CombineBlock* cb, int n, const double* V, const double* T, double* out,
                                     const double* s, cudaStream_t st);
 
+// ---- device-resident Lanczos step (lanczos.cu) ----------------------------------
+constexpr int kLzMaxIter = 1024;       // Krylov dimension limit of the device step
+constexpr int kLzMaxPerThread = 16;    // vector elements per thread of one block chunk
+struct LzArgs {
+    double* K;          // basis, row i at K + i * ld; kmax + 1 rows
+    int64_t ld;
+    double* w;          // HxV output, orthogonalised in place
+    double* q;          // HxV input: copy of the newest basis vector
+    double* part;       // per-chunk partial sums [max(kmax, 2)][nchunk]
+    double* cl;         // [2]: <K_{j-1}, w>, <K_j, w>
+    double* coef;       // [kmax]: full-pass coefficients
+    double* ab;         // [3][kmax]: alpha, beta, 1/beta
+    double* host_ab;    // host-mapped mirror of alpha and beta [2][kmax], or null
+    unsigned* ctl;      // [0] iteration index j, [1..3] block counters (zero on entry)
+    int64_t n;          // vector length (padded layout)
+    int kmax;           // iterations the buffers hold
+    int nchunk;         // blocks per launch (chunks of per_thread * 256 elements)
+};
+struct LzShape { int per_thread = 1, chunk = 256, nchunk = 1; };
+LzShape lz_shape(int64_t n, int num_sms);
+cudaError_t lz_init();
+cudaError_t launch_lz_step(const LzArgs& a, int per_thread, cudaStream_t st);
+cudaError_t launch_lz_combine(const double* K, int64_t ld, int m, int64_t n, const double* c, double* y,
+                              cudaStream_t st);
+cudaError_t launch_lz_mdot(const double* K, int64_t ld, int m, int64_t n, const double* r, double* part,
+                           const LzShape& sh, unsigned* counter, double* out, cudaStream_t st);
+
 }  // namespace vmps

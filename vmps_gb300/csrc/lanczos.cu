@@ -1,0 +1,314 @@
+// Device-resident Lanczos step.
+//
+// One Lanczos iteration after the HxV w = H K_j is a fixed sequence of four
+// launches that keep every scalar on the device:
+//
+//   lz_local : c_{j-1} = <K_{j-1}, w>, c_j = <K_j, w>
+//   lz_proj  : w <- w - c_{j-1} K_{j-1} - c_j K_j  (the three-term recurrence),
+//              then d_i = <K_i, w> for all i <= j
+//   lz_orth  : w <- w - sum_i d_i K_i               (one full Gram-Schmidt pass),
+//              alpha_j = c_j + d_j, beta_j = |w|, j <- j + 1
+//   lz_next  : K_{j+1} = q = w / beta_j
+//
+// The local step removes the large components of w first, so the full pass
+// works on a vector that is already nearly orthogonal to the basis and one
+// pass keeps the basis orthogonal to working precision (the local step plus
+// one pass cost 2(j+1)+5 FP64 FMAs per element against 4(j+1) for two full
+// passes; on GB300 the FP64 rate, not HBM, bounds these loops).
+//
+// The iteration index lives in device memory, so the HxV plan and these
+// kernels form one CUDA graph that the host replays per iteration.  Reductions
+// are deterministic: each block writes the partial sums of its element chunk,
+// and the last block to finish (a device-scope counter incremented after a
+// fence) adds the partials in chunk order.  No block waits on another.
+#include <algorithm>
+
+#include "kernels.hpp"
+
+namespace vmps {
+
+namespace {
+constexpr int kLzThreads = 256, kLzWarps = kLzThreads / 32;
+
+__device__ __forceinline__ double lz_warp_sum(double s) {
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+}
+
+// true in the block that finishes last; its reads of the other blocks'
+// partials go through L2 (__ldcg)
+__device__ __forceinline__ bool lz_last_block(unsigned* counter) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// sum of part[row][0..nchunk) by one warp (lane 0 holds the result)
+__device__ __forceinline__ double lz_row_sum(const double* part, int row, int nchunk, int lane) {
+    double s = 0;
+    for (int c = lane; c < nchunk; c += 32) s += __ldcg(part + (int64_t)row * nchunk + c);
+    return lz_warp_sum(s);
+}
+
+template <int E>
+__global__ void __launch_bounds__(kLzThreads) lz_local_kernel(LzArgs a) {
+    const int j = (int)a.ctl[0];
+    if (j >= a.kmax) return;
+    __shared__ double red[2][kLzWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t e0 = (int64_t)blockIdx.x * (E * kLzThreads) + threadIdx.x;
+    const double* kj = a.K + (int64_t)j * a.ld;
+    const double* km = j > 0 ? a.K + (int64_t)(j - 1) * a.ld : nullptr;
+    double s0 = 0, s1 = 0;
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+        const int64_t e = e0 + u * kLzThreads;
+        if (e < a.n) {
+            const double w = a.w[e];
+            s1 = fma(kj[e], w, s1);
+            if (km) s0 = fma(km[e], w, s0);
+        }
+    }
+    s0 = lz_warp_sum(s0);
+    s1 = lz_warp_sum(s1);
+    if (lane == 0) { red[0][warp] = s0; red[1][warp] = s1; }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double s = 0;
+        for (int w = 0; w < kLzWarps; ++w) s += red[threadIdx.x][w];
+        a.part[(int64_t)threadIdx.x * a.nchunk + blockIdx.x] = s;
+    }
+    if (!lz_last_block(a.ctl + 1)) return;
+    if (warp < 2) {
+        const double s = lz_row_sum(a.part, warp, a.nchunk, lane);
+        if (lane == 0) a.cl[warp] = s;
+    }
+    if (threadIdx.x == 0) a.ctl[1] = 0;
+}
+
+// partial dot of basis row `ki` (chunk-relative) with the chunk of w staged in
+// shared memory: one warp, len valid elements, four independent accumulators
+template <int E>
+__device__ __forceinline__ double lz_chunk_dot(const double* __restrict__ ki, const double* wsh, int len, int lane) {
+    double s[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int t = 0; t < E * 8; ++t) {
+        const int x = lane + 32 * t;
+        if (x < len) s[t & 3] = fma(ki[x], wsh[x], s[t & 3]);
+    }
+    return lz_warp_sum((s[0] + s[1]) + (s[2] + s[3]));
+}
+
+template <int E>
+__global__ void __launch_bounds__(kLzThreads) lz_proj_kernel(LzArgs a) {
+    __shared__ double wsh[E * kLzThreads];   // this block's chunk of w after the local step
+    const int j = (int)a.ctl[0];
+    if (j >= a.kmax) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t cb = (int64_t)blockIdx.x * (E * kLzThreads);
+    const int len = (int)(a.n - cb < E * kLzThreads ? a.n - cb : E * kLzThreads);
+    const double c0 = a.cl[0], c1 = a.cl[1];
+    const double* kj = a.K + (int64_t)j * a.ld + cb;
+    const double* km = j > 0 ? a.K + (int64_t)(j - 1) * a.ld + cb : nullptr;
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+        const int x = threadIdx.x + u * kLzThreads;
+        double v = 0;
+        if (x < len) {
+            v = fma(-c1, kj[x], a.w[cb + x]);
+            if (km) v = fma(-c0, km[x], v);
+            a.w[cb + x] = v;
+        }
+        wsh[x] = v;
+    }
+    __syncthreads();
+    // one warp per basis row: d_i partial over this chunk
+    for (int i = warp; i <= j; i += kLzWarps) {
+        const double s = lz_chunk_dot<E>(a.K + (int64_t)i * a.ld + cb, wsh, len, lane);
+        if (lane == 0) a.part[(int64_t)i * a.nchunk + blockIdx.x] = s;
+    }
+    if (!lz_last_block(a.ctl + 2)) return;
+    for (int i = warp; i <= j; i += kLzWarps) {
+        const double s = lz_row_sum(a.part, i, a.nchunk, lane);
+        if (lane == 0) a.coef[i] = s;
+    }
+    if (threadIdx.x == 0) a.ctl[2] = 0;
+}
+
+template <int E>
+__global__ void __launch_bounds__(kLzThreads) lz_orth_kernel(LzArgs a) {
+    const int j = (int)a.ctl[0];
+    if (j >= a.kmax) return;
+    __shared__ double red[kLzWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t e0 = (int64_t)blockIdx.x * (E * kLzThreads) + threadIdx.x;
+    double wr[E];
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+        const int64_t e = e0 + u * kLzThreads;
+        wr[u] = e < a.n ? a.w[e] : 0.0;
+    }
+#pragma unroll 4
+    for (int i = 0; i <= j; ++i) {
+        const double* ki = a.K + (int64_t)i * a.ld;
+        const double d = a.coef[i];
+#pragma unroll
+        for (int u = 0; u < E; ++u) {
+            const int64_t e = e0 + u * kLzThreads;
+            if (e < a.n) wr[u] = fma(-d, ki[e], wr[u]);
+        }
+    }
+    double s = 0;
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+        const int64_t e = e0 + u * kLzThreads;
+        if (e < a.n) {
+            a.w[e] = wr[u];
+            s = fma(wr[u], wr[u], s);
+        }
+    }
+    s = lz_warp_sum(s);
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < kLzWarps; ++w) t += red[w];
+        a.part[blockIdx.x] = t;
+    }
+    if (!lz_last_block(a.ctl + 3)) return;
+    if (warp == 0) {
+        const double ww = lz_row_sum(a.part, 0, a.nchunk, lane);
+        if (lane == 0) {
+            const double alpha = a.cl[1] + a.coef[j];
+            const double beta = sqrt(ww);
+            a.ab[j] = alpha;
+            a.ab[a.kmax + j] = beta;
+            a.ab[2 * a.kmax + j] = beta > 1e-300 ? 1.0 / beta : 0.0;
+            if (a.host_ab) {
+                volatile double* h = a.host_ab;
+                h[j] = alpha;
+                h[a.kmax + j] = beta;
+            }
+            a.ctl[3] = 0;
+            a.ctl[0] = (unsigned)(j + 1);
+        }
+    }
+}
+
+__global__ void lz_next_kernel(LzArgs a) {
+    const int jn = (int)a.ctl[0];
+    if (jn < 1 || jn > a.kmax) return;
+    const double s = a.ab[2 * a.kmax + jn - 1];
+    double* k = a.K + (int64_t)jn * a.ld;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = a.w[i] * s;
+        k[i] = v;
+        a.q[i] = v;
+    }
+}
+
+// y[e] = sum_{i < m} c[i] K_i[e] + (y0 ? y0[e] : 0)   (Ritz vectors and corrections)
+__global__ void lz_combine_kernel(const double* __restrict__ K, int64_t ld, int m, int64_t n,
+                                  const double* __restrict__ c, double* __restrict__ y) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0;
+        for (int i = 0; i < m; ++i) s = fma(c[i], K[(int64_t)i * ld + e], s);
+        y[e] = s;
+    }
+}
+
+// out[i] = <K_i, r> for i < m, deterministic (partials per chunk, last block sums)
+template <int E>
+__global__ void __launch_bounds__(kLzThreads) lz_mdot_kernel(const double* __restrict__ K, int64_t ld, int m,
+                                                              int64_t n, const double* __restrict__ r,
+                                                              double* __restrict__ part, int nchunk,
+                                                              unsigned* counter, double* __restrict__ out) {
+    __shared__ double rsh[E * kLzThreads];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t cb = (int64_t)blockIdx.x * (E * kLzThreads);
+    const int len = (int)(n - cb < E * kLzThreads ? n - cb : E * kLzThreads);
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+        const int x = threadIdx.x + u * kLzThreads;
+        rsh[x] = x < len ? r[cb + x] : 0.0;
+    }
+    __syncthreads();
+    for (int i = warp; i < m; i += kLzWarps) {
+        const double s = lz_chunk_dot<E>(K + (int64_t)i * ld + cb, rsh, len, lane);
+        if (lane == 0) part[(int64_t)i * nchunk + blockIdx.x] = s;
+    }
+    if (!lz_last_block(counter)) return;
+    for (int i = warp; i < m; i += kLzWarps) {
+        const double s = lz_row_sum(part, i, nchunk, lane);
+        if (lane == 0) out[i] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0;
+}
+}  // namespace
+
+// elements per thread (E) and chunk count for a vector length: the smallest
+// E in {1, 2, 4, 8, 16} that keeps the grid within 8 blocks per SM
+LzShape lz_shape(int64_t n, int num_sms) {
+    LzShape s;
+    const int64_t cap = (int64_t)8 * (num_sms > 0 ? num_sms : 152);
+    s.per_thread = 1;
+    while (s.per_thread < kLzMaxPerThread && (n + (int64_t)s.per_thread * kLzThreads - 1) /
+                                                     ((int64_t)s.per_thread * kLzThreads) > cap)
+        s.per_thread *= 2;
+    s.chunk = s.per_thread * kLzThreads;
+    s.nchunk = (int)std::max<int64_t>(1, (n + s.chunk - 1) / s.chunk);
+    return s;
+}
+
+cudaError_t lz_init() { return cudaSuccess; }
+
+#define LZ_DISPATCH(PER, CALL)        \
+    switch (PER) {                    \
+        case 1: CALL(1); break;       \
+        case 2: CALL(2); break;       \
+        case 4: CALL(4); break;       \
+        case 8: CALL(8); break;       \
+        case 16: CALL(16); break;     \
+        default: return cudaErrorInvalidValue; \
+    }
+
+cudaError_t launch_lz_step(const LzArgs& a, int per_thread, cudaStream_t st) {
+    if (a.kmax < 1 || a.kmax > kLzMaxIter || a.n <= 0 || a.nchunk < 1 || !a.K || !a.w || !a.q || !a.part ||
+        !a.coef || !a.cl || !a.ab || !a.ctl)
+        return cudaErrorInvalidValue;
+    if ((int64_t)a.nchunk * per_thread * kLzThreads < a.n) return cudaErrorInvalidValue;
+#define LZ_CALL(EE)                                                     \
+    lz_local_kernel<EE><<<a.nchunk, kLzThreads, 0, st>>>(a);            \
+    lz_proj_kernel<EE><<<a.nchunk, kLzThreads, 0, st>>>(a);             \
+    lz_orth_kernel<EE><<<a.nchunk, kLzThreads, 0, st>>>(a);
+    LZ_DISPATCH(per_thread, LZ_CALL)
+#undef LZ_CALL
+    int g = (int)std::min<int64_t>((a.n + 255) / 256, 152 * 8);
+    lz_next_kernel<<<g, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lz_combine(const double* K, int64_t ld, int m, int64_t n, const double* c, double* y,
+                              cudaStream_t st) {
+    if (m < 1 || n <= 0 || !K || !c || !y) return cudaErrorInvalidValue;
+    int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    lz_combine_kernel<<<g, 256, 0, st>>>(K, ld, m, n, c, y);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lz_mdot(const double* K, int64_t ld, int m, int64_t n, const double* r, double* part,
+                           const LzShape& sh, unsigned* counter, double* out, cudaStream_t st) {
+    if (m < 1 || m > kLzMaxIter || n <= 0 || !K || !r || !part || !counter || !out) return cudaErrorInvalidValue;
+    if ((int64_t)sh.nchunk * sh.chunk < n) return cudaErrorInvalidValue;
+#define LZ_CALL(EE) lz_mdot_kernel<EE><<<sh.nchunk, kLzThreads, 0, st>>>(K, ld, m, n, r, part, sh.nchunk, counter, out);
+    LZ_DISPATCH(sh.per_thread, LZ_CALL)
+#undef LZ_CALL
+    return cudaGetLastError();
+}
+#undef LZ_DISPATCH
+
+}  // namespace vmps

@@ -20,6 +20,7 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -87,7 +88,36 @@ template <typename T> static void upload_vec(DBuf& d, const std::vector<T>& v, c
     if (!v.empty()) CK(cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
 }
 
+// Krylov workspace of a context: basis, work vectors, reduction scratch and a
+// host-mapped mirror of the recurrence coefficients; grown on demand and kept
+// for later Lanczos runs (a DMRG sweep runs one per site).
+struct LzWork {
+    DBuf K, w, q, x, u, part, small;
+    double* host = nullptr;       // pinned, mapped: alpha [cap] | beta [cap]
+    double* host_dev = nullptr;   // its device address
+    int cap = 0;                  // iterations the buffers hold (cap + 1 basis rows)
+    int host_cap = 0;             // cap the host mirror was allocated for
+    int64_t n = 0, ld = 0;        // vector length and basis row stride
+    LzShape sh;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    LzWork() = default;
+    LzWork(const LzWork&) = delete;
+    LzWork& operator=(const LzWork&) = delete;
+    ~LzWork() {
+        if (host) cudaFreeHost(host);
+        for (auto& e : ev) if (e) cudaEventDestroy(e);
+    }
+    // `small` (doubles): cl[2] | coef[cap] | ab[3 cap] | g[cap] | ctl (8 unsigned)
+    double* cl() const { return small.as<double>(); }
+    double* coef() const { return cl() + 2; }
+    double* ab() const { return coef() + cap; }
+    double* g() const { return ab() + 3 * cap; }
+    unsigned* ctl() const { return (unsigned*)(g() + cap); }
+};
+
 struct vmps_ctx_s {
+    std::unique_ptr<LzWork> lz;   // Lanczos workspace (vmps_lanczos_ground)
+    std::mutex lz_mu;             // one Lanczos run at a time per context
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;   // host<->device transfers overlapped with compute
@@ -1125,16 +1155,20 @@ void tridiag_lowest(const std::vector<double>& a, const std::vector<double>& b, 
         lo = std::min(lo, a[i] - r);
         hi = std::max(hi, a[i] + r);
     }
-    double scale = std::max(std::abs(lo), std::abs(hi)) + 1e-300;
-    for (int it = 0; it < 200 && hi - lo > 1e-16 * scale; ++it) {
-        double mid = 0.5 * (lo + hi);
+    const double scale = std::max(std::abs(lo), std::abs(hi)) + 1e-300;
+    // bisection to 1e-9 of the spectral scale; inverse iteration then converges
+    // at the ratio (shift distance) / (gap) per step and the Rayleigh quotient of
+    // its vector carries the eigenvalue to working precision
+    for (int it = 0; it < 80 && hi - lo > 1e-9 * scale; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
         if (sturm_count_below(a, b, mid) >= 1) hi = mid; else lo = mid;
     }
     theta = 0.5 * (lo + hi);
     // inverse iteration on (T - shift): tridiagonal LU with partial pivoting
     // (the elimination of LAPACK dgttrf/dgtts2, restated)
     y.assign(n, 1.0 / std::sqrt((double)n));
-    const double shift = theta - 1e-13 * scale;
+    const double shift = lo - 1e-9 * scale;
     std::vector<double> d(n), du(n, 0.0), du2(n, 0.0), dl(n, 0.0);
     std::vector<char> swp(n, 0);
     for (size_t i = 0; i < n; ++i) d[i] = a[i] - shift;
@@ -1156,8 +1190,9 @@ void tridiag_lowest(const std::vector<double>& a, const std::vector<double>& b, 
         }
     }
     for (size_t i = 0; i < n; ++i) if (d[i] == 0.0) d[i] = 1e-300;
+    std::vector<double> x(n);
     for (int it = 0; it < 3; ++it) {
-        std::vector<double> x = y;
+        x = y;
         for (size_t i = 0; i + 1 < n; ++i) {
             if (!swp[i]) x[i + 1] -= dl[i] * x[i];
             else { const double t = x[i]; x[i] = x[i + 1]; x[i + 1] = t - dl[i] * x[i]; }
@@ -1177,17 +1212,16 @@ void tridiag_lowest(const std::vector<double>& a, const std::vector<double>& b, 
     size_t im = 0;
     for (size_t i = 1; i < n; ++i) if (std::abs(y[i]) > std::abs(y[im])) im = i;
     if (y[im] < 0) for (double& v : y) v = -v;
+    // Rayleigh quotient y^T T y (y has unit norm)
+    double rq = 0;
+    for (size_t i = 0; i < n; ++i) {
+        double t = a[i] * y[i];
+        if (i > 0) t += b[i - 1] * y[i - 1];
+        if (i + 1 < n) t += b[i] * y[i + 1];
+        rq += y[i] * t;
+    }
+    if (rq >= lo - 1e-9 * scale && rq <= hi + 1e-9 * scale) theta = rq;
 }
-
-struct Krylov {
-    vmps_pivot* p;
-    int64_t n;
-    DBuf basis;     // [kmax+1][n]
-    DBuf w, tmp;
-    DBuf coef;      // device coefficients
-    int kmax;
-    double* K(int j) const { return basis.as<double>() + (int64_t)j * n; }
-};
 
 double dev_dot(vmps_pivot* p, const double* x, const double* y, int64_t n) {
     CK(launch_dot(x, y, n, p->part.as<double>(), p->scal.as<double>(), p->st()));
@@ -1197,97 +1231,272 @@ double dev_dot(vmps_pivot* p, const double* x, const double* y, int64_t n) {
     return r;
 }
 
-// one Lanczos run from K(0) (normalised on entry); returns the Ritz value and
-// leaves the Ritz vector in `x`
-double lanczos_run(Krylov& kr, int prec, int max_iter, double tol_eigval, double tol_state, double* x, int* iters,
-                   int* hxvs) {
-    vmps_pivot* p = kr.p;
-    cudaStream_t st = p->st();
-    const int64_t n = kr.n;
-    std::vector<double> alpha, beta;
-    double theta = 0, theta_prev = 1e300;
-    std::vector<double> y;
-    int j = 0;
-    const int kmax = std::min(max_iter, kr.kmax);
-    for (j = 0; j < kmax; ++j) {
-        double* w = kr.w.as<double>();
-        pivot_hxv_dev(p, prec, kr.K(j), w);
-        (*hxvs)++;
-        // full reorthogonalisation against K(0..j) twice (classical Gram-Schmidt, "twice is enough")
-        double a_j = 0;
-        for (int pass = 0; pass < 2; ++pass) {
-            CK(launch_mdot(kr.basis.as<double>(), j + 1, n, w, p->part.as<double>(), kr.coef.as<double>(), st));
-            CK(launch_mgs(kr.basis.as<double>(), j + 1, n, kr.coef.as<double>(), w, st));
-            double cj;
-            CK(cudaMemcpyAsync(&cj, kr.coef.as<double>() + j, 8, cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            a_j += cj;
+// The Krylov workspace of a context (LzWork, declared with the context) for
+// vectors of length n and `cap` iterations.
+LzWork& lz_work(vmps_ctx* c, int64_t n, int cap) {
+    if (!c->lz) c->lz.reset(new LzWork());
+    LzWork& W = *c->lz;
+    cudaStream_t st = c->stream;
+    if (W.n != n || W.cap < cap) {
+        W.n = n;
+        W.ld = (n + 31) / 32 * 32;
+        W.cap = std::max(W.cap, (cap + 31) / 32 * 32);
+        W.sh = lz_shape(n, c->num_sms);
+        W.K.alloc((size_t)(W.cap + 1) * W.ld * 8, st, false);
+        for (DBuf* b : {&W.w, &W.q, &W.x, &W.u}) b->alloc((size_t)W.ld * 8, st, false);
+        W.part.alloc((size_t)std::max(W.cap, 2) * W.sh.nchunk * 8, st, false);
+        W.small.alloc(((size_t)6 * W.cap + 8) * 8, st, true);
+        if (W.host_cap < W.cap) {
+            if (W.host) cudaFreeHost(W.host);
+            W.host = nullptr;
+            W.host_cap = 0;
+            CK(cudaHostAlloc((void**)&W.host, (size_t)2 * W.cap * 8, cudaHostAllocMapped));
+            CK(cudaHostGetDevicePointer((void**)&W.host_dev, W.host, 0));
+            W.host_cap = W.cap;
         }
-        alpha.push_back(a_j);
-        double b_j = std::sqrt(std::max(0.0, dev_dot(p, w, w, n)));
-        tridiag_lowest(alpha, beta, theta, y);
-        const double res = std::abs(b_j * y.back());
+    }
+    for (auto& e : W.ev)
+        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return W;
+}
+
+// one Lanczos run from K_0 (= q, normalised), at most kmax iterations
+struct LzResult {
+    int m = 0;          // basis vectors of the Ritz space
+    int launched = 0;   // HxV iterations the device ran (the last may run past convergence)
+    double theta = 0, res = 0;
+    double ms_wait = 0, ms_host = 0;   // host time blocked on the device / in the tridiagonal solves
+    std::vector<double> alpha, beta, y;
+};
+
+LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval, double tol_state) {
+    cudaStream_t st = p->st();
+    DevPlan& dp = get_plan(p, prec);
+    LzArgs a{};
+    a.K = W.K.as<double>();
+    a.ld = W.ld;
+    a.w = W.w.as<double>();
+    a.q = W.q.as<double>();
+    a.part = W.part.as<double>();
+    a.cl = W.cl();
+    a.coef = W.coef();
+    a.ab = W.ab();
+    a.host_ab = W.host_dev;
+    a.ctl = W.ctl();
+    a.n = W.n;
+    a.kmax = W.cap;
+    a.nchunk = W.sh.nchunk;
+    CK(cudaMemsetAsync(W.ctl(), 0, 8 * sizeof(unsigned), st));
+    Operands ops;
+    ops.X = p->dL.as<double>();
+    ops.Z = p->dR.as<double>();
+    ops.Y = W.q.as<double>();
+    ops.O = W.w.as<double>();
+    ops.err = p->ctx->err;
+    // one iteration = the HxV plan + the four step kernels, captured once
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+        run_plan(dp, ops, st);
+        CK(launch_lz_step(a, W.sh.per_thread, st));
+    } catch (...) {
+        if (cudaStreamEndCapture(st, &g) == cudaSuccess && g) cudaGraphDestroy(g);
+        throw;
+    }
+    CK(cudaStreamEndCapture(st, &g));
+    cudaGraphExec_t ge = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    CK(ie);
+    struct ExecGuard {
+        cudaGraphExec_t e;
+        ~ExecGuard() { cudaGraphExecDestroy(e); }
+    } guard{ge};
+
+    // The host trails the device by one iteration: iteration j+1 is queued
+    // before the host waits for alpha_j, beta_j and solves the tridiagonal
+    // problem, so the device never idles on the host.
+    LzResult r;
+    volatile const double* hab = W.host;
+    double theta = 0, theta_prev = 1e300, res = 0;
+    std::vector<double> y;
+    auto launch = [&]() {
+        CK(cudaGraphLaunch(ge, st));
+        CK(cudaEventRecord(W.ev[r.launched & 1], st));
+        ++r.launched;
+    };
+    launch();
+    int j = 0;
+    for (j = 0; j < kmax; ++j) {
+        if (r.launched < kmax) launch();
+        const auto tw = std::chrono::steady_clock::now();
+        CK(cudaEventSynchronize(W.ev[j & 1]));
+        const auto th = std::chrono::steady_clock::now();
+        r.ms_wait += std::chrono::duration<double, std::milli>(th - tw).count();
+        struct HostTimer {
+            std::chrono::steady_clock::time_point t;
+            double* acc;
+            ~HostTimer() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count(); }
+        } host_timer{th, &r.ms_host};
+        const double a_j = hab[j], b_j = hab[W.cap + j];
+        r.alpha.push_back(a_j);
+        tridiag_lowest(r.alpha, r.beta, theta, y);
+        res = std::abs(b_j * y.back());
         const bool conv_e = std::abs(theta - theta_prev) <= tol_eigval * std::max(1.0, std::abs(theta));
         theta_prev = theta;
         if ((conv_e && res <= tol_state) || b_j <= 1e-14 * std::max(1.0, std::abs(theta)) || j + 1 == kmax) {
             ++j;
             break;
         }
-        beta.push_back(b_j);
-        CK(cudaMemcpyAsync(kr.K(j + 1), w, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-        CK(launch_scale(1.0 / b_j, kr.K(j + 1), n, st));
+        r.beta.push_back(b_j);
     }
-    *iters = j;
-    // Ritz vector x = K y
-    CK(cudaMemcpyAsync(kr.coef.p, y.data(), y.size() * 8, cudaMemcpyHostToDevice, st));
-    CK(launch_combine(kr.basis.as<double>(), (int)y.size(), n, kr.coef.as<double>(), x, st));
-    double nx = std::sqrt(dev_dot(p, x, x, n));
-    CK(launch_scale(1.0 / nx, x, n, st));
-    return theta;
+    r.m = j;
+    r.theta = theta;
+    r.res = res;
+    r.y = y;
+    return r;
+}
+
+// x = K y / |K y| for the Ritz coefficients of a run
+void lz_ritz(vmps_pivot* p, LzWork& W, const std::vector<double>& y, double* x) {
+    cudaStream_t st = p->st();
+    CK(cudaMemcpyAsync(W.g(), y.data(), y.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(launch_lz_combine(W.K.as<double>(), W.ld, (int)y.size(), W.n, W.g(), x, st));
+    const double nx = std::sqrt(dev_dot(p, x, x, W.n));
+    if (!(nx > 0) || !std::isfinite(nx)) throw CudaFail("Ritz vector is zero or not finite");
+    CK(launch_scale(1.0 / nx, x, W.n, st));
+}
+
+// Correction of a Ritz vector y (unit norm, lowest eigenvector of the
+// tridiagonal T = tridiag(beta, alpha, beta)) inside the Krylov space: the
+// Jacobi-Davidson correction equation restricted to span(K),
+//     P (T - th) P z = -P g,   P = 1 - y y^T,   z orthogonal to y,
+// with g = K^T r the projection of the residual r = H x - th x.  Solved by
+// conjugate gradients on the m-dimensional system (positive definite on y's
+// complement while th lies below the second Ritz value; the iteration stops
+// at the first direction of non-positive curvature).  `model` returns the
+// second-order energy change 2 g.z + z.(T - th) z of the step.
+std::vector<double> krylov_correction(const std::vector<double>& a, const std::vector<double>& b, double th,
+                                      const std::vector<double>& y, const std::vector<double>& g, double* model) {
+    const size_t m = a.size();
+    auto Tv = [&](const std::vector<double>& v, std::vector<double>& out) {
+        for (size_t i = 0; i < m; ++i) {
+            double s = (a[i] - th) * v[i];
+            if (i > 0) s += b[i - 1] * v[i - 1];
+            if (i + 1 < m) s += b[i] * v[i + 1];
+            out[i] = s;
+        }
+    };
+    auto proj = [&](std::vector<double>& v) {
+        double d = 0;
+        for (size_t i = 0; i < m; ++i) d += y[i] * v[i];
+        for (size_t i = 0; i < m; ++i) v[i] -= d * y[i];
+    };
+    auto dot = [&](const std::vector<double>& u, const std::vector<double>& v) {
+        double s = 0;
+        for (size_t i = 0; i < m; ++i) s += u[i] * v[i];
+        return s;
+    };
+    std::vector<double> z(m, 0.0), r(g), p, Ap(m);
+    for (double& v : r) v = -v;
+    proj(r);
+    p = r;
+    double rr = dot(r, r);
+    const double r0 = std::sqrt(rr);
+    for (size_t it = 0; it < 2 * m + 10 && rr > 0 && std::sqrt(rr) > 1e-14 * r0; ++it) {
+        Tv(p, Ap);
+        proj(Ap);
+        const double pAp = dot(p, Ap);
+        if (!(pAp > 0)) break;
+        const double al = rr / pAp;
+        for (size_t i = 0; i < m; ++i) {
+            z[i] += al * p[i];
+            r[i] -= al * Ap[i];
+        }
+        proj(r);
+        const double rr2 = dot(r, r);
+        for (size_t i = 0; i < m; ++i) p[i] = r[i] + (rr2 / rr) * p[i];
+        rr = rr2;
+    }
+    proj(z);
+    std::vector<double> Tz(m);
+    Tv(z, Tz);
+    *model = 2 * dot(g, z) + dot(z, Tz);
+    return z;
 }
 }  // namespace
 
 extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_iter, double tol_eigval,
                                    double tol_state, int refine_iters, double* energy, vmps_lanczos_stats* stats) {
     API_BEGIN
-    if (!p || !v || !energy || max_iter <= 0) return set_err(VMPS_E_ARG, "bad argument");
+    if (!p || !v || !energy || max_iter <= 0 || refine_iters < 0) return set_err(VMPS_E_ARG, "bad argument");
+    if (max_iter >= kLzMaxIter || refine_iters >= kLzMaxIter)
+        return set_err(VMPS_E_ARG, "max_iter and refine_iters must be below " + std::to_string(kLzMaxIter));
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
     require_device(p->ctx);
+    std::lock_guard<std::mutex> lock(p->ctx->lz_mu);
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t st = p->st();
-    Krylov kr;
-    kr.p = p;
-    kr.n = p->Vd.total;
-    kr.kmax = std::max(max_iter, refine_iters) + 1;
-    kr.basis.alloc((size_t)(kr.kmax + 1) * kr.n * 8, st, true);
-    kr.w.alloc((size_t)kr.n * 8, st, true);
-    kr.tmp.alloc((size_t)kr.n * 8, st, true);
-    kr.coef.alloc((size_t)(kr.kmax + 2) * 8, st, true);
-    // start vector
+    const bool refine = prec != VMPS_PREC_FP64 && refine_iters > 0;
+    get_plan(p, prec);
+    if (refine) get_plan(p, VMPS_PREC_FP64);
+    const int64_t n = p->Vd.total;
+    LzWork& W = lz_work(p->ctx, n, std::max(max_iter, refine_iters));
+    // padding positions of the layout stay zero in every vector
+    for (double* b : {W.K.as<double>(), W.w.as<double>(), W.q.as<double>(), W.x.as<double>(), W.u.as<double>()})
+        CK(cudaMemsetAsync(b, 0, (size_t)W.ld * 8, st));
+    double* K0 = W.K.as<double>();
     ensure_staging(p);
-    pack_in(p->ctx, p->dPack, p->npack, v, p->Vt.total, p->stage_in, kr.K(0), st);
-    double n0 = std::sqrt(dev_dot(p, kr.K(0), kr.K(0), kr.n));
+    pack_in(p->ctx, p->dPack, p->npack, v, p->Vt.total, p->stage_in, K0, st);
+    const double n0 = std::sqrt(dev_dot(p, K0, K0, n));
     if (!(n0 > 0) || !std::isfinite(n0)) return set_err(VMPS_E_NONFINITE, "start vector is zero or not finite");
-    CK(launch_scale(1.0 / n0, kr.K(0), kr.n, st));
+    CK(launch_scale(1.0 / n0, K0, n, st));
+    CK(cudaMemcpyAsync(W.q.p, K0, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+
     vmps_lanczos_stats s{};
-    int it = 0, hx = 0;
-    double* x = kr.tmp.as<double>();
-    double e = lanczos_run(kr, prec, max_iter, tol_eigval, tol_state, x, &it, &hx);
-    s.iterations = it;
-    s.energy_first = e;
-    if (prec == VMPS_PREC_FP64) s.hxv_fp64 = hx; else s.hxv_split = hx;
-    if (prec != VMPS_PREC_FP64 && refine_iters > 0) {
-        // FP64 refinement: restart Lanczos from the split-precision Ritz vector with FP64 HxV
-        CK(cudaMemcpyAsync(kr.K(0), x, (size_t)kr.n * 8, cudaMemcpyDeviceToDevice, st));
-        int it2 = 0, hx2 = 0;
-        e = lanczos_run(kr, VMPS_PREC_FP64, refine_iters, tol_eigval, tol_state, x, &it2, &hx2);
-        s.refine_iterations = it2;
-        s.hxv_fp64 += hx2;
+    LzResult r1 = lz_run(p, W, prec, max_iter, tol_eigval, tol_state);
+    s.iterations = r1.m;
+    s.energy_first = r1.theta;
+    s.ms_wait = r1.ms_wait;
+    s.ms_host = r1.ms_host;
+    if (prec == VMPS_PREC_FP64) s.hxv_fp64 = r1.launched; else s.hxv_split = r1.launched;
+    double e = r1.theta, res = r1.res;
+    double* x = W.x.as<double>();
+    lz_ritz(p, W, r1.y, x);
+    if (refine) {
+        // FP64 residual of the split-precision Ritz vector, corrected inside
+        // the split Krylov space where its error lies (the low-lying part of
+        // the spectrum), then closing FP64 Lanczos steps from the result
+        double* u = W.u.as<double>();
+        pivot_hxv_dev(p, VMPS_PREC_FP64, x, u);
+        s.hxv_fp64++;
+        const double th0 = dev_dot(p, x, u, n);
+        CK(launch_axpy(-th0, x, u, n, st));
+        CK(launch_lz_mdot(W.K.as<double>(), W.ld, r1.m, n, u, W.part.as<double>(), W.sh, W.ctl() + 4, W.g(), st));
+        std::vector<double> g(r1.m);
+        CK(cudaMemcpyAsync(g.data(), W.g(), (size_t)r1.m * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        double model = 0;
+        std::vector<double> z = krylov_correction(r1.alpha, r1.beta, th0, r1.y, g, &model);
+        double zn = 0;
+        for (double t : z) zn += t * t;
+        if (model < 0 && std::sqrt(zn) < 0.5) {
+            std::vector<double> yz(r1.y);
+            for (size_t i = 0; i < yz.size(); ++i) yz[i] += z[i];
+            lz_ritz(p, W, yz, x);
+        }
+        CK(cudaMemcpyAsync(K0, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(W.q.p, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        LzResult r2 = lz_run(p, W, VMPS_PREC_FP64, std::max(1, refine_iters - 1), tol_eigval, tol_state);
+        s.refine_iterations = r2.m;
+        s.hxv_fp64 += r2.launched;
+        s.ms_wait += r2.ms_wait;
+        s.ms_host += r2.ms_host;
+        lz_ritz(p, W, r2.y, x);
+        e = r2.theta;
+        res = r2.res;
     }
-    // residual ||H x - E x|| with FP64 HxV
-    pivot_hxv_dev(p, VMPS_PREC_FP64, x, kr.w.as<double>());
-    s.hxv_fp64++;
-    CK(launch_axpy(-e, x, kr.w.as<double>(), kr.n, st));
-    s.residual = std::sqrt(dev_dot(p, kr.w.as<double>(), kr.w.as<double>(), kr.n));
+    s.residual = res;
     pack_out(p->ctx, p->dPack, p->npack, x, p->Vt.total, p->stage_out, v, st);
     CK(cudaStreamSynchronize(st));
     check_device_error(p->ctx);

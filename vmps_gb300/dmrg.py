@@ -12,6 +12,11 @@ The sweep logic follows DmrgSolver::halfsweep / iteration_one
 HxV, Lanczos and contract_L/R run on the GPU.  The gauge step is a host QR per
 QN sector, as in Biped::QR (tensors/Biped.h:901-932).  Bond dimensions stay
 fixed (no subspace expansion).
+
+Each sweep's wall time is split like the reference's halfsweep timer
+(solvers/DmrgSolver.h:837-845): "lanczos" (the local eigensolver), "precalc"
+(the pivot's task lists and plans), "gauge" (QR / LQ and the push to the next
+site) and "lr" (contract_L / contract_R).
 """
 from __future__ import annotations
 
@@ -58,33 +63,49 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
         envR[l] = e.run(envR[l + 1], mps.A[l], mps.A[l])
         e.close()
     t_init = time.perf_counter() - t0
-    energies, sweep_times, hxv = [], [], 0
+    energies, sweep_times, timers, hxv = [], [], [], 0
     E = None
+    clock = time.perf_counter
     for sweep in range(n_sweeps):
-        ts = time.perf_counter()
+        ts = clock()
+        tm = dict(lanczos=0.0, precalc=0.0, gauge=0.0, lr=0.0)
         order = list(range(L)) + list(range(L - 1, -1, -1))
         for step, l in enumerate(order):
             right = step < L
+            t = clock()
             H = PivotMatrix1(ctx, sym, envL[l], envR[l + 1], model.W[l], mps.A[l])
+            H.prepare(precision, refine_iters > 0)
+            t1 = clock()
             E, v, st = H.lanczos(mps.A[l].data, precision, max_iter=max_iter, tol_eigval=tol_eigval,
                                  tol_state=tol_state, refine_iters=refine_iters)
             hxv += st["hxv_fp64"] + st["hxv_split"]
             H.close()
+            t2 = clock()
+            tm["precalc"] += t1 - t
+            tm["lanczos"] += t2 - t1
             mps.A[l].data[:] = v
             if right and l < L - 1:
                 mps.A[l], Rf = left_normalize(mps.A[l], nq, sym=mps.sym)
                 _push_right(mps.A[l + 1], Rf)
+                t3 = clock()
                 e = EnvUpdate(ctx, sym, "L", envL[l], mps.A[l], model.W[l], mps.A[l])
                 envL[l + 1] = e.run(envL[l], mps.A[l], mps.A[l])
                 e.close()
             elif not right and l > 0:
                 mps.A[l], Lf = right_normalize(mps.A[l], nq, sym=mps.sym)
                 _push_left(mps.A[l - 1], Lf)
+                t3 = clock()
                 e = EnvUpdate(ctx, sym, "R", envR[l + 1], mps.A[l], model.W[l], mps.A[l])
                 envR[l] = e.run(envR[l + 1], mps.A[l], mps.A[l])
                 e.close()
-        sweep_times.append(time.perf_counter() - ts)
+            else:
+                t3 = clock()
+            t4 = clock()
+            tm["gauge"] += t3 - t2
+            tm["lr"] += t4 - t3
+        sweep_times.append(clock() - ts)
+        timers.append(tm)
         energies.append(E)
         if verbose:
             print(f"sweep {sweep}: E = {E:.14f}  ({sweep_times[-1]:.2f} s)", flush=True)
-    return SweepResult(energies=energies, sweep_times=sweep_times, init_time=t_init, hxv=hxv)
+    return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv)

@@ -77,6 +77,13 @@ class _Pivot:
         N.check(N.lib().vmps_pivot_stats(self._h, _prec(precision), C.byref(s)))
         return s.as_dict()
 
+    def prepare(self, precision="fp64", fp64_too=False):
+        """Build the device work lists of `precision` now instead of at the first
+        HxV (and the FP64 ones as well when the FP64 refinement will need them)."""
+        self.stats(precision)
+        if fp64_too and _prec(precision) != _prec("fp64"):
+            self.stats("fp64")
+
     def apply(self, vin: np.ndarray, precision="fp64", out: np.ndarray | None = None) -> np.ndarray:
         """Vout = H * Vin on compact host arrays (host->device->host inside)."""
         vin = np.ascontiguousarray(vin, dtype=np.float64)
