@@ -192,11 +192,14 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
  * run on the device: one iteration (HxV, the three-term recurrence, one full
  * Gram-Schmidt pass, alpha, beta, the next Krylov vector) is a CUDA graph the host
  * replays while it solves the tridiagonal problem one iteration behind.
- * precision VMPS_PREC_BF16X3 runs the Krylov phase with split-precision HxV, then
- * corrects the Ritz vector with one FP64 HxV: its FP64 residual, projected on the
- * split Krylov space, drives the Jacobi-Davidson correction equation solved in
- * that space; closing FP64 Lanczos steps (at most refine_iters - 1) start from the
- * corrected vector.  refine_iters counts all FP64 HxVs of that refinement.
+ * precision VMPS_PREC_BF16X3 first applies FP64 HxV once to the start vector: if its
+ * residual is below 1e-5 of its energy (a converged neighbourhood the split
+ * operator cannot resolve) the solve continues as FP64 Lanczos.  Otherwise it runs
+ * the Krylov phase with split-precision HxV, then corrects the Ritz vector with one
+ * FP64 HxV: its FP64 residual, projected on the split Krylov space, drives the
+ * Jacobi-Davidson correction equation solved in that space; closing FP64 Lanczos
+ * steps (at most refine_iters - 1) start from the corrected vector.  refine_iters
+ * counts the FP64 HxVs of that refinement (the probe is one more).
  * Krylov vectors, dots and the tridiagonal solve are FP64 throughout.  v (compact
  * layout) is the start vector on entry and the ground state on exit.
  * max_iter and refine_iters are below 1024.                                     */

@@ -228,7 +228,9 @@ def test_lanczos_residual_estimate_and_determinism(gpu_ctx):
     explicit FP64 residual ||H v - E v|| of the returned vector.  Its
     reductions are deterministic, so two runs agree bit for bit.  The split
     run with the Krylov-space correction reaches the FP64 energy within
-    1e-10 relative using at most refine_iters FP64 HxVs."""
+    1e-10 relative using at most refine_iters FP64 HxVs after the probe.
+    From a start vector that is already an eigenvector the split run is the
+    FP64 run."""
     model, mps, Lenv, Renv, W, V = pivot1_case("hubb", L=10, D=32, site=4, seed=41)
     H = PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V)
     v0 = np.random.default_rng(7).standard_normal(H.dim)
@@ -240,9 +242,12 @@ def test_lanczos_residual_estimate_and_determinism(gpu_ctx):
     assert abs(true_res - st1["residual"]) <= 1e-11 + 0.05 * true_res, (true_res, st1)
     es, xs, sts = H.lanczos(v0, "bf16x3", max_iter=200, tol_eigval=1e-10, tol_state=1e-6, refine_iters=12)
     assert abs(es - e1) < 1e-10 * abs(e1), (es, e1, sts)
-    assert 1 <= sts["hxv_fp64"] <= 12
+    assert sts["hxv_split"] > 0 and 2 <= sts["hxv_fp64"] <= 1 + 12
     true_res = np.linalg.norm(H.apply(xs, "fp64") - es * xs)
     assert abs(true_res - sts["residual"]) <= 1e-11 + 0.05 * true_res, (true_res, sts)
+    # near-converged start: the FP64 probe continues as the FP64 solve
+    ec, xc, stc = H.lanczos(x1, "bf16x3", max_iter=200, tol_eigval=1e-12, tol_state=1e-8, refine_iters=12)
+    assert stc["hxv_split"] == 0 and abs(ec - e1) < 1e-12 * abs(e1), stc
     H.close()
 
 

@@ -1260,16 +1260,26 @@ LzWork& lz_work(vmps_ctx* c, int64_t n, int cap) {
     return W;
 }
 
+// Start-vector residual (relative to its energy) below which a split-precision
+// solve runs as FP64 Lanczos: about twice the residual that the BF16x3
+// operator's rounding noise (4e-6 relative) leaves on an exact eigenvector.
+constexpr double kSplitProbeRel = 1e-5;
+
 // one Lanczos run from K_0 (= q, normalised), at most kmax iterations
 struct LzResult {
     int m = 0;          // basis vectors of the Ritz space
     int launched = 0;   // HxV iterations the device ran (the last may run past convergence)
     double theta = 0, res = 0;
     double ms_wait = 0, ms_host = 0;   // host time blocked on the device / in the tridiagonal solves
+    bool aborted = false;              // stopped by the probe after iteration 0
     std::vector<double> alpha, beta, y;
 };
 
-LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval, double tol_state) {
+// probe_rel > 0: iteration 0 runs alone first, and the run stops after it
+// (aborted = true) when beta_0 > probe_rel * max(1, |alpha_0|), i.e. when the
+// start vector's residual is above that fraction of its energy
+LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval, double tol_state,
+                double probe_rel = 0) {
     cudaStream_t st = p->st();
     DevPlan& dp = get_plan(p, prec);
     LzArgs a{};
@@ -1328,7 +1338,7 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
     launch();
     int j = 0;
     for (j = 0; j < kmax; ++j) {
-        if (r.launched < kmax) launch();
+        if (r.launched < kmax && !(probe_rel > 0 && j == 0)) launch();
         const auto tw = std::chrono::steady_clock::now();
         CK(cudaEventSynchronize(W.ev[j & 1]));
         const auto th = std::chrono::steady_clock::now();
@@ -1339,6 +1349,15 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
             ~HostTimer() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count(); }
         } host_timer{th, &r.ms_host};
         const double a_j = hab[j], b_j = hab[W.cap + j];
+        if (probe_rel > 0 && j == 0) {
+            if (b_j > probe_rel * std::max(1.0, std::abs(a_j))) {
+                r.aborted = true;
+                r.theta = a_j;
+                r.res = b_j;
+                return r;
+            }
+            if (r.launched < kmax) launch();
+        }
         r.alpha.push_back(a_j);
         tridiag_lowest(r.alpha, r.beta, theta, y);
         res = std::abs(b_j * y.back());
@@ -1454,47 +1473,73 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     CK(cudaMemcpyAsync(W.q.p, K0, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
 
     vmps_lanczos_stats s{};
-    LzResult r1 = lz_run(p, W, prec, max_iter, tol_eigval, tol_state);
-    s.iterations = r1.m;
-    s.energy_first = r1.theta;
-    s.ms_wait = r1.ms_wait;
-    s.ms_host = r1.ms_host;
-    if (prec == VMPS_PREC_FP64) s.hxv_fp64 = r1.launched; else s.hxv_split = r1.launched;
-    double e = r1.theta, res = r1.res;
     double* x = W.x.as<double>();
-    lz_ritz(p, W, r1.y, x);
+    double e = 0, res = 0;
+    auto account = [&](const LzResult& r, int run_prec) {
+        (run_prec == VMPS_PREC_FP64 ? s.hxv_fp64 : s.hxv_split) += r.launched;
+        s.ms_wait += r.ms_wait;
+        s.ms_host += r.ms_host;
+    };
+    bool split_phase = true;
     if (refine) {
-        // FP64 residual of the split-precision Ritz vector, corrected inside
-        // the split Krylov space where its error lies (the low-lying part of
-        // the spectrum), then closing FP64 Lanczos steps from the result
-        double* u = W.u.as<double>();
-        pivot_hxv_dev(p, VMPS_PREC_FP64, x, u);
-        s.hxv_fp64++;
-        const double th0 = dev_dot(p, x, u, n);
-        CK(launch_axpy(-th0, x, u, n, st));
-        CK(launch_lz_mdot(W.K.as<double>(), W.ld, r1.m, n, u, W.part.as<double>(), W.sh, W.ctl() + 4, W.g(), st));
-        std::vector<double> g(r1.m);
-        CK(cudaMemcpyAsync(g.data(), W.g(), (size_t)r1.m * 8, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        double model = 0;
-        std::vector<double> z = krylov_correction(r1.alpha, r1.beta, th0, r1.y, g, &model);
-        double zn = 0;
-        for (double t : z) zn += t * t;
-        if (model < 0 && std::sqrt(zn) < 0.5) {
-            std::vector<double> yz(r1.y);
-            for (size_t i = 0; i < yz.size(); ++i) yz[i] += z[i];
-            lz_ritz(p, W, yz, x);
+        // Probe: FP64 Lanczos whose first iteration gives the start vector's
+        // FP64 residual.  A start vector already within a few times the split
+        // operator's noise of an eigenvector (late sweeps) gains nothing from
+        // split HxVs, which cannot resolve it further; the FP64 run goes on and
+        // its first HxV is not wasted.  Otherwise the split path starts over.
+        LzResult r0 = lz_run(p, W, VMPS_PREC_FP64, max_iter, tol_eigval, tol_state, kSplitProbeRel);
+        account(r0, VMPS_PREC_FP64);
+        if (!r0.aborted) {
+            split_phase = false;
+            s.iterations = r0.m;
+            s.energy_first = r0.theta;
+            lz_ritz(p, W, r0.y, x);
+            e = r0.theta;
+            res = r0.res;
+        } else {
+            CK(cudaMemcpyAsync(W.q.p, K0, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
         }
-        CK(cudaMemcpyAsync(K0, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-        CK(cudaMemcpyAsync(W.q.p, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-        LzResult r2 = lz_run(p, W, VMPS_PREC_FP64, std::max(1, refine_iters - 1), tol_eigval, tol_state);
-        s.refine_iterations = r2.m;
-        s.hxv_fp64 += r2.launched;
-        s.ms_wait += r2.ms_wait;
-        s.ms_host += r2.ms_host;
-        lz_ritz(p, W, r2.y, x);
-        e = r2.theta;
-        res = r2.res;
+    }
+    if (split_phase) {
+        LzResult r1 = lz_run(p, W, prec, max_iter, tol_eigval, tol_state);
+        account(r1, prec);
+        s.iterations = r1.m;
+        s.energy_first = r1.theta;
+        e = r1.theta;
+        res = r1.res;
+        lz_ritz(p, W, r1.y, x);
+        if (refine) {
+            // FP64 residual of the split-precision Ritz vector, corrected inside
+            // the split Krylov space where its error lies (the low-lying part of
+            // the spectrum), then closing FP64 Lanczos steps from the result
+            double* u = W.u.as<double>();
+            pivot_hxv_dev(p, VMPS_PREC_FP64, x, u);
+            s.hxv_fp64++;
+            const double th0 = dev_dot(p, x, u, n);
+            CK(launch_axpy(-th0, x, u, n, st));
+            CK(launch_lz_mdot(W.K.as<double>(), W.ld, r1.m, n, u, W.part.as<double>(), W.sh, W.ctl() + 4, W.g(),
+                              st));
+            std::vector<double> g(r1.m);
+            CK(cudaMemcpyAsync(g.data(), W.g(), (size_t)r1.m * 8, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            double model = 0;
+            std::vector<double> z = krylov_correction(r1.alpha, r1.beta, th0, r1.y, g, &model);
+            double zn = 0;
+            for (double t : z) zn += t * t;
+            if (model < 0 && std::sqrt(zn) < 0.5) {
+                std::vector<double> yz(r1.y);
+                for (size_t i = 0; i < yz.size(); ++i) yz[i] += z[i];
+                lz_ritz(p, W, yz, x);
+            }
+            CK(cudaMemcpyAsync(K0, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(W.q.p, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+            LzResult r2 = lz_run(p, W, VMPS_PREC_FP64, std::max(1, refine_iters - 1), tol_eigval, tol_state);
+            account(r2, VMPS_PREC_FP64);
+            s.refine_iterations = r2.m;
+            lz_ritz(p, W, r2.y, x);
+            e = r2.theta;
+            res = r2.res;
+        }
     }
     s.residual = res;
     pack_out(p->ctx, p->dPack, p->npack, x, p->Vt.total, p->stage_out, v, st);

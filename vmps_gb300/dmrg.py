@@ -74,7 +74,7 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
             right = step < L
             t = clock()
             H = PivotMatrix1(ctx, sym, envL[l], envR[l + 1], model.W[l], mps.A[l])
-            H.prepare(precision, refine_iters > 0)
+            H.prepare("fp64" if refine_iters > 0 else precision)   # the split plan is built if the split phase runs
             t1 = clock()
             E, v, st = H.lanczos(mps.A[l].data, precision, max_iter=max_iter, tol_eigval=tol_eigval,
                                  tol_state=tol_state, refine_iters=refine_iters)
