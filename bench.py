@@ -151,14 +151,16 @@ def sweep_bench(ctx, args, with_cpu=True):
     """Single-site DMRG sweep times.
 
     * Heisenberg L=32, D=64: GPU FP64 and the CPU oracle, 2 sweeps each.
-    * Hubbard L=64, D=1024 (U(1)xU(1), half filling):
+    * Hubbard L=64, D=1024 (U(1)xU(1), half filling), single-site:
       - from the same random MPS, 2 sweeps in FP64 and 2 in split precision
         (BF16x3 + FP64 refinement).  Far from convergence the sweep is a chaotic
         map, so the two trajectories reach different intermediate energies;
       - after 4 more split sweeps (near convergence), one more sweep in each
         precision from the same MPS: there the energies agree to the
         tolerance, which is the |dE/E| the metric asks for.
-    HxV, Lanczos and contract_L/R run on the GPU; the QR gauge step on the
+    * the same chain with two-site DMRG at Dmax=1024 (SVD truncation on the host
+      cores), one sweep in each precision from the same random MPS.
+    HxV, Lanczos and contract_L/R run on the GPU; the QR / SVD gauge steps on the
     host.  Per-sweep timers split lanczos / precalc / gauge / lr."""
     import copy
 
@@ -201,6 +203,15 @@ def sweep_bench(ctx, args, with_cpu=True):
         hub["converged_split"] = summary(rsp)
         hub["converged_rel_diff"] = abs(rsp["energies"][-1] - r64["energies"][-1]) / abs(r64["energies"][-1])
         out["hubbard_L64_D1024"] = hub
+        # two-site DMRG (the sweep of the metric's configuration) at D=1024: one sweep in
+        # each precision from the same random MPS, bond bases truncated by the SVD
+        from vmps_gb300.dmrg import dmrg2
+        two = {"tolerances": dict(refine_iters=3, **tol), "Dmax": 1024}
+        for tag, prec, kw in (("split", args.precision, dict(refine_iters=3)), ("fp64", "fp64", {})):
+            r = dmrg2(ctx, model, copy.deepcopy(mps0), n_sweeps=1, Dmax=1024, precision=prec, **tol, **kw)
+            two[tag] = dict(summary(r), truncation=r["truncation"], max_bond_dim=r["max_bond_dim"])
+        two["sweep_speedup"] = two["fp64"]["s_per_sweep"][0] / two["split"]["s_per_sweep"][0]
+        out["hubbard_L64_D1024_two_site"] = two
     return out
 
 

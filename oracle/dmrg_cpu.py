@@ -81,3 +81,47 @@ def dmrg1_cpu(model, mps, n_sweeps=2, max_iter=100, tol_eigval=1e-12, tol_state=
         times.append(time.perf_counter() - ts)
         energies.append(E)
     return {"energies": energies, "sweep_times": times}
+
+
+def dmrg2_cpu(model, mps, n_sweeps=2, Dmax=None, max_iter=100, tol_eigval=1e-12, tol_state=1e-8, eps_svd=1e-14):
+    """Two-site DMRG on the oracle: the sweep of vmps_gb300.dmrg.dmrg2 (bond order, split_AA2
+    truncation, environment updates) with the oracle's two-site HxV and contract_L/R."""
+    from vmps_gb300.mps import contract_two_sites, split_two_site
+    from vmps_gb300.pivot import left_vacuum, right_target
+    sym, L, nq = model.sym, model.L, model.sym.nq
+    Dmax = Dmax if Dmax is not None else max(mps.bond_dim(l) for l in range(L + 1))
+    qloc = model.qloc
+
+    def env(side, E, A, W):
+        return OracleEnv(side, nq, E, A, W, A).run(E, A, A)
+
+    envL = [None] * (L + 1)
+    envR = [None] * (L + 1)
+    envL[0] = left_vacuum(sym)
+    envR[L] = right_target(sym, mps.Qtot)
+    for l in range(L - 1, 1, -1):
+        envR[l] = env("R", envR[l + 1], mps.A[l], model.W[l])
+    energies, times = [], []
+    E = None
+    for sweep in range(n_sweeps):
+        ts = time.perf_counter()
+        for move, bonds in (("right", range(L - 1)), ("left", range(L - 2, -1, -1))):
+            for l in bonds:
+                A1, A2 = mps.A[l], mps.A[l + 1]
+                din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
+                dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
+                V, comb = contract_two_sites(sym, A1, A2, qloc, qloc, nq, return_basis=True)
+                op = OraclePivot(2, nq, envL[l], envR[l + 2], V, model.W[l], model.W[l + 1])
+                E, v, _ = lanczos_np(op.hxv, V.data.copy(), max_iter, tol_eigval, tol_state)
+                V.data[:] = v
+                A1, A2, _, dmid = split_two_site(V, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
+                                                 eps_svd=eps_svd)
+                mps.A[l], mps.A[l + 1] = A1, A2
+                mps.dims[l + 1] = dmid
+                if move == "right":
+                    envL[l + 1] = env("L", envL[l], A1, model.W[l])
+                else:
+                    envR[l + 1] = env("R", envR[l + 2], A2, model.W[l + 1])
+        times.append(time.perf_counter() - ts)
+        energies.append(E)
+    return {"energies": energies, "sweep_times": times}

@@ -194,3 +194,57 @@ def test_oracle_dmrg1_heisenberg_matches_ed():
     M = np.array([sum(1 if ((s >> (L - 1 - j)) & 1) == 0 else -1 for j in range(L)) for s in range(2 ** L)])
     e_ed = ed.ground_energy(H, M == 0)
     assert abs(res["energies"][-1] - e_ed) < 1e-10 * abs(e_ed)
+
+
+def _hubbard_sector(L, N, M):
+    nm = 2 * L
+    mask = []
+    for s in range(2 ** nm):
+        bits = [(s >> (nm - 1 - j)) & 1 for j in range(nm)]
+        mask.append(sum(bits) == N and sum(bits[0::2]) - sum(bits[1::2]) == M)
+    return np.array(mask)
+
+
+def test_two_site_split_is_exact_and_orthonormal():
+    """split_AA2 without truncation reproduces the two-site tensor; the
+    orthonormal site is orthonormal; truncation reports the discarded weight"""
+    from vmps_gb300.mps import RandomMPS, contract_two_sites, split_two_site
+    m = models.hubbard_u1xu1(8)
+    mps = RandomMPS(m, (8, 0), 16, seed=3).canonicalize(3, 4)
+    A, B = mps.A[3], mps.A[4]
+    V, comb = contract_two_sites(m.sym, A, B, m.qloc, m.qloc, 2, return_basis=True)
+    din = {tuple(A.qin[i]): int(A.rows[i]) for i in range(A.n)}
+    dout = {tuple(B.qout[i]): int(B.cols[i]) for i in range(B.n)}
+    nrm = V.norm()
+    for move in ("right", "left"):
+        A1, A2, disc, dmid = split_two_site(V, comb, m.qloc, m.qloc, din, dout, 2, Dmax=10 ** 6, move=move)
+        assert disc < 1e-28
+        V2 = contract_two_sites(m.sym, A1, A2, m.qloc, m.qloc, 2)
+        assert np.linalg.norm(V2.data * nrm - V.data) < 1e-13 * nrm
+        O = A1 if move == "right" else A2
+        G = {}
+        for i in range(O.n):
+            q = tuple(O.qout[i]) if move == "right" else tuple(O.qin[i])
+            b = O.block(i)
+            g = b.T @ b if move == "right" else b @ b.T
+            G[q] = G.get(q, 0) + g
+        assert max(np.abs(g - np.eye(g.shape[0])).max() for g in G.values()) < 1e-13
+    A1, A2, disc, dmid = split_two_site(V, comb, m.qloc, m.qloc, din, dout, 2, Dmax=8, move="right")
+    assert sum(dmid.values()) == 8 and 0 < disc < 1
+    V2 = contract_two_sites(m.sym, A1, A2, m.qloc, m.qloc, 2)
+    assert abs(np.linalg.norm(V2.data) - 1) < 1e-13
+
+
+def test_oracle_dmrg2_hubbard_matches_ed():
+    """two-site DMRG on the oracle grows the bond bases from D=4 to the exact
+    state of the L=6 Hubbard chain (DMRG vs ED, programs/test_Hubbard/test_Hubbard.cc:227-300)"""
+    from oracle.dmrg_cpu import dmrg2_cpu
+    from vmps_gb300.mps import RandomMPS
+    L = 6
+    model = models.hubbard_u1xu1(L, t=1.0, U=4.0)
+    mps = RandomMPS(model, (L, 0), 4, seed=5).canonicalize(0, 0)
+    res = dmrg2_cpu(model, mps, n_sweeps=3, Dmax=64)
+    # ED of the MPO (pinned against the fermionic dense Hamiltonian by test_mpo_matches_dense_hubbard)
+    H = ed.permute_to_reference(ed.mpo_to_dense(model), model)
+    e_ed = ed.ground_energy(H, _hubbard_sector(L, L, 0))
+    assert abs(res["energies"][-1] - e_ed) < 1e-10 * abs(e_ed), (res, e_ed)

@@ -212,18 +212,25 @@ __global__ void prep_kernel(const PrepBlock* __restrict__ pbs, int nb, const dou
     }
 }
 
-// column pieces of a column-major FP64 source into panels: column c of the
-// piece is panel row c, its element r is K index r; four loads in flight
-__global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np, const double* __restrict__ src,
+// column pieces of a column-major FP64 or FP32 source into panels: column c of
+// the piece is panel row c, its element r is K index r; four loads in flight
+__device__ __forceinline__ float piece_value(double x, bool unit, double scale) {
+    return f64_to_f32_rn(unit ? x : scale * x);
+}
+__device__ __forceinline__ float piece_value(float x, bool unit, double scale) {
+    return unit ? x : f64_to_f32_rn(scale) * x;
+}
+template <typename T>
+__global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np, const T* __restrict__ src,
                                    __nv_bfloat16* __restrict__ dst) {
     for (int b = blockIdx.x; b < np; b += gridDim.x) {
         const PanelPiece pc = pieces[b];
         const int rows = pc.rows, n = pc.rows * pc.cols;
-        const double* s = src + pc.src_off;
+        const T* s = src + pc.src_off;
         __nv_bfloat16* d = dst + pc.dst_off;
         const bool unit = pc.scale == 1.0;
         for (int e0 = threadIdx.x; e0 < n; e0 += 4 * blockDim.x) {
-            double x[4];
+            T x[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int e = e0 + u * blockDim.x;
@@ -231,7 +238,7 @@ __global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np
                     const int c = e / rows, r = e - c * rows;
                     x[u] = s[r + c * pc.src_ld];
                 } else {
-                    x[u] = 0.0;
+                    x[u] = T(0);
                 }
             }
 #pragma unroll
@@ -239,7 +246,7 @@ __global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np
                 const int e = e0 + u * blockDim.x;
                 if (e >= n) break;
                 const int c = e / rows, r = e - c * rows;
-                split_store(d + (int64_t)c * pc.dst_pitch, r, f64_to_f32_rn(unit ? x[u] : pc.scale * x[u]));
+                split_store(d + (int64_t)c * pc.dst_pitch, r, piece_value(x[u], unit, pc.scale));
             }
         }
     }
@@ -442,7 +449,13 @@ cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* ds
 cudaError_t launch_panel_split(const PanelPiece* pieces, int np, const double* src, void* dst, cudaStream_t st) {
     if (np <= 0) return cudaSuccess;
     if (!pieces || !src || !dst) return cudaErrorInvalidValue;
-    panel_split_kernel<<<min(np, 4096), 256, 0, st>>>(pieces, np, src, (__nv_bfloat16*)dst);
+    panel_split_kernel<double><<<min(np, 4096), 256, 0, st>>>(pieces, np, src, (__nv_bfloat16*)dst);
+    return cudaGetLastError();
+}
+cudaError_t launch_panel_split_f32(const PanelPiece* pieces, int np, const float* src, void* dst, cudaStream_t st) {
+    if (np <= 0) return cudaSuccess;
+    if (!pieces || !src || !dst) return cudaErrorInvalidValue;
+    panel_split_kernel<float><<<min(np, 4096), 256, 0, st>>>(pieces, np, src, (__nv_bfloat16*)dst);
     return cudaGetLastError();
 }
 

@@ -43,10 +43,12 @@ cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st);
 // TMA-fed, tiles up to 128 x 256; out_split = 1: C is a bf16 [hi|lo] panel arena,
 // 0: C is double
 cudaError_t umma_init();
-cudaError_t launch_gg_umma(int out_split, const GGArgs& a, const TmaMaps& maps, cudaStream_t st);
+// out_mode: 0 FP64 output, 1 bf16 [hi|lo] panel rows (split intermediates), 2 FP32 output
+cudaError_t launch_gg_umma(int out_mode, const GGArgs& a, const TmaMaps& maps, cudaStream_t st);
 // split operands: FP64 blocks -> bf16 [hi|lo] panels
 cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* dst, cudaStream_t st);
 cudaError_t launch_panel_split(const PanelPiece* pieces, int np, const double* src, void* dst, cudaStream_t st);
+cudaError_t launch_panel_split_f32(const PanelPiece* pieces, int np, const float* src, void* dst, cudaStream_t st);
 cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, double* dst, int to_padded,
                         cudaStream_t st);
 int64_t dot_chunk(int64_t n);
@@ -71,10 +73,10 @@ cudaError_t launch_transfer_combine(const CombineBlock* cb, int n, const double*
 constexpr int kLzMaxIter = 1024;       // Krylov dimension limit of the device step
 constexpr int kLzMaxPerThread = 16;    // vector elements per thread of one block chunk
 struct LzArgs {
-    double* K;          // basis, row i at K + i * ld; kmax + 1 rows
+    void* K;            // basis (double or float), row i at K + i * ld; kmax + 1 rows
     int64_t ld;
-    double* w;          // HxV output, orthogonalised in place
-    double* q;          // HxV input: copy of the newest basis vector
+    void* w;            // HxV output, orthogonalised in place
+    void* q;            // HxV input: copy of the newest basis vector
     double* part;       // per-chunk partial sums [max(kmax, 2)][nchunk]
     double* cl;         // [2]: <K_{j-1}, w>, <K_j, w>
     double* coef;       // [kmax]: full-pass coefficients
@@ -84,14 +86,16 @@ struct LzArgs {
     int64_t n;          // vector length (padded layout)
     int kmax;           // iterations the buffers hold
     int nchunk;         // blocks per launch (chunks of per_thread * 256 elements)
+    int fp32;           // vectors are float (split-precision phase), else double
 };
 struct LzShape { int per_thread = 1, chunk = 256, nchunk = 1; };
 LzShape lz_shape(int64_t n, int num_sms);
 cudaError_t lz_init();
 cudaError_t launch_lz_step(const LzArgs& a, int per_thread, cudaStream_t st);
-cudaError_t launch_lz_combine(const double* K, int64_t ld, int m, int64_t n, const double* c, double* y,
+cudaError_t launch_lz_combine(const void* K, int fp32, int64_t ld, int m, int64_t n, const double* c, double* y,
                               cudaStream_t st);
-cudaError_t launch_lz_mdot(const double* K, int64_t ld, int m, int64_t n, const double* r, double* part,
+cudaError_t launch_lz_mdot(const void* K, int fp32, int64_t ld, int m, int64_t n, const double* r, double* part,
                            const LzShape& sh, unsigned* counter, double* out, cudaStream_t st);
+cudaError_t launch_lz_to_f32(const double* x, float* y, int64_t n, cudaStream_t st);
 
 }  // namespace vmps

@@ -16,6 +16,11 @@
 // one pass cost 2(j+1)+5 FP64 FMAs per element against 4(j+1) for two full
 // passes; on GB300 the FP64 rate, not HBM, bounds these loops).
 //
+// The Krylov vectors are FP64, or FP32 for the split-precision phase (whose
+// operator carries 4e-6 relative rounding noise, far above FP32's): FP32 halves
+// the bytes and moves the FMAs off GB300's slow FP64 pipe.  Chunk partial sums,
+// alpha, beta and the coefficients are FP64 either way.
+//
 // The iteration index lives in device memory, so the HxV plan and these
 // kernels form one CUDA graph that the host replays per iteration.  Reductions
 // are deterministic: each block writes the partial sums of its element chunk,
@@ -23,6 +28,7 @@
 // fence) adds the partials in chunk order.  No block waits on another.
 #include <algorithm>
 
+#include "convert.hpp"
 #include "kernels.hpp"
 
 namespace vmps {
@@ -54,129 +60,135 @@ __device__ __forceinline__ double lz_row_sum(const double* part, int row, int nc
     return lz_warp_sum(s);
 }
 
-template <int E>
+// partial dot of basis row `ki` (chunk-relative) with the chunk of w staged in
+// shared memory: one warp, len valid elements, four independent accumulators
+// in the vector type, FP64 from the warp sum on
+template <typename V, int E>
+__device__ __forceinline__ double lz_chunk_dot(const V* __restrict__ ki, const V* wsh, int len, int lane) {
+    V s[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int t = 0; t < E * 8; ++t) {
+        const int x = lane + 32 * t;
+        if (x < len) s[t & 3] = fma(ki[x], wsh[x], s[t & 3]);
+    }
+    return lz_warp_sum((double)((s[0] + s[1]) + (s[2] + s[3])));
+}
+
+template <typename V, int E>
 __global__ void __launch_bounds__(kLzThreads) lz_local_kernel(LzArgs a) {
     const int j = (int)a.ctl[0];
     if (j >= a.kmax) return;
     __shared__ double red[2][kLzWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t e0 = (int64_t)blockIdx.x * (E * kLzThreads) + threadIdx.x;
-    const double* kj = a.K + (int64_t)j * a.ld;
-    const double* km = j > 0 ? a.K + (int64_t)(j - 1) * a.ld : nullptr;
-    double s0 = 0, s1 = 0;
+    const V* K = (const V*)a.K;
+    const V* w = (const V*)a.w;
+    const V* kj = K + (int64_t)j * a.ld;
+    const V* km = j > 0 ? K + (int64_t)(j - 1) * a.ld : nullptr;
+    V s0 = 0, s1 = 0;
 #pragma unroll
     for (int u = 0; u < E; ++u) {
         const int64_t e = e0 + u * kLzThreads;
         if (e < a.n) {
-            const double w = a.w[e];
-            s1 = fma(kj[e], w, s1);
-            if (km) s0 = fma(km[e], w, s0);
+            const V x = w[e];
+            s1 = fma(kj[e], x, s1);
+            if (km) s0 = fma(km[e], x, s0);
         }
     }
-    s0 = lz_warp_sum(s0);
-    s1 = lz_warp_sum(s1);
-    if (lane == 0) { red[0][warp] = s0; red[1][warp] = s1; }
+    const double d0 = lz_warp_sum((double)s0), d1 = lz_warp_sum((double)s1);
+    if (lane == 0) { red[0][warp] = d0; red[1][warp] = d1; }
     __syncthreads();
     if (threadIdx.x < 2) {
-        double s = 0;
-        for (int w = 0; w < kLzWarps; ++w) s += red[threadIdx.x][w];
-        a.part[(int64_t)threadIdx.x * a.nchunk + blockIdx.x] = s;
+        double t = 0;
+        for (int q = 0; q < kLzWarps; ++q) t += red[threadIdx.x][q];
+        a.part[(int64_t)threadIdx.x * a.nchunk + blockIdx.x] = t;
     }
     if (!lz_last_block(a.ctl + 1)) return;
     if (warp < 2) {
-        const double s = lz_row_sum(a.part, warp, a.nchunk, lane);
-        if (lane == 0) a.cl[warp] = s;
+        const double t = lz_row_sum(a.part, warp, a.nchunk, lane);
+        if (lane == 0) a.cl[warp] = t;
     }
     if (threadIdx.x == 0) a.ctl[1] = 0;
 }
 
-// partial dot of basis row `ki` (chunk-relative) with the chunk of w staged in
-// shared memory: one warp, len valid elements, four independent accumulators
-template <int E>
-__device__ __forceinline__ double lz_chunk_dot(const double* __restrict__ ki, const double* wsh, int len, int lane) {
-    double s[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int t = 0; t < E * 8; ++t) {
-        const int x = lane + 32 * t;
-        if (x < len) s[t & 3] = fma(ki[x], wsh[x], s[t & 3]);
-    }
-    return lz_warp_sum((s[0] + s[1]) + (s[2] + s[3]));
-}
-
-template <int E>
+template <typename V, int E>
 __global__ void __launch_bounds__(kLzThreads) lz_proj_kernel(LzArgs a) {
-    __shared__ double wsh[E * kLzThreads];   // this block's chunk of w after the local step
+    __shared__ V wsh[E * kLzThreads];   // this block's chunk of w after the local step
     const int j = (int)a.ctl[0];
     if (j >= a.kmax) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t cb = (int64_t)blockIdx.x * (E * kLzThreads);
     const int len = (int)(a.n - cb < E * kLzThreads ? a.n - cb : E * kLzThreads);
-    const double c0 = a.cl[0], c1 = a.cl[1];
-    const double* kj = a.K + (int64_t)j * a.ld + cb;
-    const double* km = j > 0 ? a.K + (int64_t)(j - 1) * a.ld + cb : nullptr;
+    const V c0 = (V)a.cl[0], c1 = (V)a.cl[1];
+    const V* K = (const V*)a.K;
+    V* w = (V*)a.w;
+    const V* kj = K + (int64_t)j * a.ld + cb;
+    const V* km = j > 0 ? K + (int64_t)(j - 1) * a.ld + cb : nullptr;
 #pragma unroll
     for (int u = 0; u < E; ++u) {
         const int x = threadIdx.x + u * kLzThreads;
-        double v = 0;
+        V v = 0;
         if (x < len) {
-            v = fma(-c1, kj[x], a.w[cb + x]);
+            v = fma(-c1, kj[x], w[cb + x]);
             if (km) v = fma(-c0, km[x], v);
-            a.w[cb + x] = v;
+            w[cb + x] = v;
         }
         wsh[x] = v;
     }
     __syncthreads();
     // one warp per basis row: d_i partial over this chunk
     for (int i = warp; i <= j; i += kLzWarps) {
-        const double s = lz_chunk_dot<E>(a.K + (int64_t)i * a.ld + cb, wsh, len, lane);
-        if (lane == 0) a.part[(int64_t)i * a.nchunk + blockIdx.x] = s;
+        const double t = lz_chunk_dot<V, E>(K + (int64_t)i * a.ld + cb, wsh, len, lane);
+        if (lane == 0) a.part[(int64_t)i * a.nchunk + blockIdx.x] = t;
     }
     if (!lz_last_block(a.ctl + 2)) return;
     for (int i = warp; i <= j; i += kLzWarps) {
-        const double s = lz_row_sum(a.part, i, a.nchunk, lane);
-        if (lane == 0) a.coef[i] = s;
+        const double t = lz_row_sum(a.part, i, a.nchunk, lane);
+        if (lane == 0) a.coef[i] = t;
     }
     if (threadIdx.x == 0) a.ctl[2] = 0;
 }
 
-template <int E>
+template <typename V, int E>
 __global__ void __launch_bounds__(kLzThreads) lz_orth_kernel(LzArgs a) {
     const int j = (int)a.ctl[0];
     if (j >= a.kmax) return;
     __shared__ double red[kLzWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t e0 = (int64_t)blockIdx.x * (E * kLzThreads) + threadIdx.x;
-    double wr[E];
+    const V* K = (const V*)a.K;
+    V* w = (V*)a.w;
+    V wr[E];
 #pragma unroll
     for (int u = 0; u < E; ++u) {
         const int64_t e = e0 + u * kLzThreads;
-        wr[u] = e < a.n ? a.w[e] : 0.0;
+        wr[u] = e < a.n ? w[e] : V(0);
     }
 #pragma unroll 4
     for (int i = 0; i <= j; ++i) {
-        const double* ki = a.K + (int64_t)i * a.ld;
-        const double d = a.coef[i];
+        const V* ki = K + (int64_t)i * a.ld;
+        const V d = (V)a.coef[i];
 #pragma unroll
         for (int u = 0; u < E; ++u) {
             const int64_t e = e0 + u * kLzThreads;
             if (e < a.n) wr[u] = fma(-d, ki[e], wr[u]);
         }
     }
-    double s = 0;
+    V s = 0;
 #pragma unroll
     for (int u = 0; u < E; ++u) {
         const int64_t e = e0 + u * kLzThreads;
         if (e < a.n) {
-            a.w[e] = wr[u];
+            w[e] = wr[u];
             s = fma(wr[u], wr[u], s);
         }
     }
-    s = lz_warp_sum(s);
-    if (lane == 0) red[warp] = s;
+    const double ds = lz_warp_sum((double)s);
+    if (lane == 0) red[warp] = ds;
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0;
-        for (int w = 0; w < kLzWarps; ++w) t += red[w];
+        for (int q = 0; q < kLzWarps; ++q) t += red[q];
         a.part[blockIdx.x] = t;
     }
     if (!lz_last_block(a.ctl + 3)) return;
@@ -199,54 +211,70 @@ __global__ void __launch_bounds__(kLzThreads) lz_orth_kernel(LzArgs a) {
     }
 }
 
+template <typename V>
 __global__ void lz_next_kernel(LzArgs a) {
     const int jn = (int)a.ctl[0];
     if (jn < 1 || jn > a.kmax) return;
-    const double s = a.ab[2 * a.kmax + jn - 1];
-    double* k = a.K + (int64_t)jn * a.ld;
+    const V s = (V)a.ab[2 * a.kmax + jn - 1];
+    V* k = (V*)a.K + (int64_t)jn * a.ld;
+    const V* w = (const V*)a.w;
+    V* q = (V*)a.q;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double v = a.w[i] * s;
+        const V v = w[i] * s;
         k[i] = v;
-        a.q[i] = v;
+        q[i] = v;
     }
 }
 
-// y[e] = sum_{i < m} c[i] K_i[e] + (y0 ? y0[e] : 0)   (Ritz vectors and corrections)
-__global__ void lz_combine_kernel(const double* __restrict__ K, int64_t ld, int m, int64_t n,
+__device__ __forceinline__ double lz_f64(double x) { return x; }
+__device__ __forceinline__ double lz_f64(float x) { return f32_to_f64(x); }   // exact, integer pipe
+
+// y[e] = sum_{i < m} c[i] K_i[e] in FP64 (Ritz vectors and corrections)
+template <typename V>
+__global__ void lz_combine_kernel(const V* __restrict__ K, int64_t ld, int m, int64_t n,
                                   const double* __restrict__ c, double* __restrict__ y) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
         double s = 0;
-        for (int i = 0; i < m; ++i) s = fma(c[i], K[(int64_t)i * ld + e], s);
+        for (int i = 0; i < m; ++i) s = fma(c[i], lz_f64(K[(int64_t)i * ld + e]), s);
         y[e] = s;
     }
 }
 
-// out[i] = <K_i, r> for i < m, deterministic (partials per chunk, last block sums)
-template <int E>
-__global__ void __launch_bounds__(kLzThreads) lz_mdot_kernel(const double* __restrict__ K, int64_t ld, int m,
-                                                              int64_t n, const double* __restrict__ r,
+__device__ __forceinline__ void lz_stage(double* d, double x) { *d = x; }
+__device__ __forceinline__ void lz_stage(float* d, double x) { *d = f64_to_f32_rn(x); }
+
+// out[i] = <K_i, r> for i < m, deterministic (partials per chunk, last block
+// sums); r is FP64 and is rounded to the basis type when staged
+template <typename V, int E>
+__global__ void __launch_bounds__(kLzThreads) lz_mdot_kernel(const V* __restrict__ K, int64_t ld, int m, int64_t n,
+                                                              const double* __restrict__ r,
                                                               double* __restrict__ part, int nchunk,
                                                               unsigned* counter, double* __restrict__ out) {
-    __shared__ double rsh[E * kLzThreads];
+    __shared__ V rsh[E * kLzThreads];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t cb = (int64_t)blockIdx.x * (E * kLzThreads);
     const int len = (int)(n - cb < E * kLzThreads ? n - cb : E * kLzThreads);
 #pragma unroll
     for (int u = 0; u < E; ++u) {
         const int x = threadIdx.x + u * kLzThreads;
-        rsh[x] = x < len ? r[cb + x] : 0.0;
+        lz_stage(rsh + x, x < len ? r[cb + x] : 0.0);
     }
     __syncthreads();
     for (int i = warp; i < m; i += kLzWarps) {
-        const double s = lz_chunk_dot<E>(K + (int64_t)i * ld + cb, rsh, len, lane);
-        if (lane == 0) part[(int64_t)i * nchunk + blockIdx.x] = s;
+        const double t = lz_chunk_dot<V, E>(K + (int64_t)i * ld + cb, rsh, len, lane);
+        if (lane == 0) part[(int64_t)i * nchunk + blockIdx.x] = t;
     }
     if (!lz_last_block(counter)) return;
     for (int i = warp; i < m; i += kLzWarps) {
-        const double s = lz_row_sum(part, i, nchunk, lane);
-        if (lane == 0) out[i] = s;
+        const double t = lz_row_sum(part, i, nchunk, lane);
+        if (lane == 0) out[i] = t;
     }
     if (threadIdx.x == 0) *counter = 0;
+}
+
+__global__ void lz_to_f32_kernel(const double* __restrict__ x, float* __restrict__ y, int64_t n) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        y[e] = f64_to_f32_rn(x[e]);
 }
 }  // namespace
 
@@ -266,49 +294,66 @@ LzShape lz_shape(int64_t n, int num_sms) {
 
 cudaError_t lz_init() { return cudaSuccess; }
 
-#define LZ_DISPATCH(PER, CALL)        \
-    switch (PER) {                    \
-        case 1: CALL(1); break;       \
-        case 2: CALL(2); break;       \
-        case 4: CALL(4); break;       \
-        case 8: CALL(8); break;       \
-        case 16: CALL(16); break;     \
+#define LZ_DISPATCH(PER, CALL)                 \
+    switch (PER) {                             \
+        case 1: CALL(1); break;                \
+        case 2: CALL(2); break;                \
+        case 4: CALL(4); break;                \
+        case 8: CALL(8); break;                \
+        case 16: CALL(16); break;              \
         default: return cudaErrorInvalidValue; \
     }
+
+template <typename V>
+static cudaError_t lz_step(const LzArgs& a, int per_thread, cudaStream_t st) {
+#define LZ_CALL(EE)                                                   \
+    lz_local_kernel<V, EE><<<a.nchunk, kLzThreads, 0, st>>>(a);       \
+    lz_proj_kernel<V, EE><<<a.nchunk, kLzThreads, 0, st>>>(a);        \
+    lz_orth_kernel<V, EE><<<a.nchunk, kLzThreads, 0, st>>>(a);
+    LZ_DISPATCH(per_thread, LZ_CALL)
+#undef LZ_CALL
+    const int g = (int)std::min<int64_t>((a.n + 255) / 256, 152 * 8);
+    lz_next_kernel<V><<<g, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_lz_step(const LzArgs& a, int per_thread, cudaStream_t st) {
     if (a.kmax < 1 || a.kmax > kLzMaxIter || a.n <= 0 || a.nchunk < 1 || !a.K || !a.w || !a.q || !a.part ||
         !a.coef || !a.cl || !a.ab || !a.ctl)
         return cudaErrorInvalidValue;
     if ((int64_t)a.nchunk * per_thread * kLzThreads < a.n) return cudaErrorInvalidValue;
-#define LZ_CALL(EE)                                                     \
-    lz_local_kernel<EE><<<a.nchunk, kLzThreads, 0, st>>>(a);            \
-    lz_proj_kernel<EE><<<a.nchunk, kLzThreads, 0, st>>>(a);             \
-    lz_orth_kernel<EE><<<a.nchunk, kLzThreads, 0, st>>>(a);
-    LZ_DISPATCH(per_thread, LZ_CALL)
-#undef LZ_CALL
-    int g = (int)std::min<int64_t>((a.n + 255) / 256, 152 * 8);
-    lz_next_kernel<<<g, 256, 0, st>>>(a);
-    return cudaGetLastError();
+    return a.fp32 ? lz_step<float>(a, per_thread, st) : lz_step<double>(a, per_thread, st);
 }
 
-cudaError_t launch_lz_combine(const double* K, int64_t ld, int m, int64_t n, const double* c, double* y,
+cudaError_t launch_lz_combine(const void* K, int fp32, int64_t ld, int m, int64_t n, const double* c, double* y,
                               cudaStream_t st) {
     if (m < 1 || n <= 0 || !K || !c || !y) return cudaErrorInvalidValue;
-    int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
-    lz_combine_kernel<<<g, 256, 0, st>>>(K, ld, m, n, c, y);
+    const int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    if (fp32) lz_combine_kernel<float><<<g, 256, 0, st>>>((const float*)K, ld, m, n, c, y);
+    else lz_combine_kernel<double><<<g, 256, 0, st>>>((const double*)K, ld, m, n, c, y);
     return cudaGetLastError();
 }
 
-cudaError_t launch_lz_mdot(const double* K, int64_t ld, int m, int64_t n, const double* r, double* part,
+cudaError_t launch_lz_mdot(const void* K, int fp32, int64_t ld, int m, int64_t n, const double* r, double* part,
                            const LzShape& sh, unsigned* counter, double* out, cudaStream_t st) {
     if (m < 1 || m > kLzMaxIter || n <= 0 || !K || !r || !part || !counter || !out) return cudaErrorInvalidValue;
     if ((int64_t)sh.nchunk * sh.chunk < n) return cudaErrorInvalidValue;
-#define LZ_CALL(EE) lz_mdot_kernel<EE><<<sh.nchunk, kLzThreads, 0, st>>>(K, ld, m, n, r, part, sh.nchunk, counter, out);
+#define LZ_CALL(EE)                                                                                        \
+    if (fp32) lz_mdot_kernel<float, EE><<<sh.nchunk, kLzThreads, 0, st>>>((const float*)K, ld, m, n, r, part, \
+                                                                          sh.nchunk, counter, out);         \
+    else lz_mdot_kernel<double, EE><<<sh.nchunk, kLzThreads, 0, st>>>((const double*)K, ld, m, n, r, part,   \
+                                                                        sh.nchunk, counter, out);
     LZ_DISPATCH(sh.per_thread, LZ_CALL)
 #undef LZ_CALL
     return cudaGetLastError();
 }
 #undef LZ_DISPATCH
+
+cudaError_t launch_lz_to_f32(const double* x, float* y, int64_t n, cudaStream_t st) {
+    if (n <= 0 || !x || !y) return cudaErrorInvalidValue;
+    const int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    lz_to_f32_kernel<<<g, 256, 0, st>>>(x, y, n);
+    return cudaGetLastError();
+}
 
 }  // namespace vmps

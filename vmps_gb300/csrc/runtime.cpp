@@ -93,6 +93,7 @@ template <typename T> static void upload_vec(DBuf& d, const std::vector<T>& v, c
 // for later Lanczos runs (a DMRG sweep runs one per site).
 struct LzWork {
     DBuf K, w, q, x, u, part, small;
+    DBuf K32, w32, q32;           // FP32 basis and vectors of split-precision runs (allocated on first use)
     double* host = nullptr;       // pinned, mapped: alpha [cap] | beta [cap]
     double* host_dev = nullptr;   // its device address
     int cap = 0;                  // iterations the buffers hold (cap + 1 basis rows)
@@ -366,6 +367,9 @@ struct Operands {
     const double* Z = nullptr;
     double* O = nullptr;
     int* err = nullptr;
+    // split plans only: FP32 vectors in place of Y and O (same padded layout)
+    const float* Yf = nullptr;
+    float* Of = nullptr;
 };
 
 // Invariants the tcgen05 engine relies on, checked on the host once per plan:
@@ -501,13 +505,13 @@ static void run_phase_on(const DevPlan& dp, int ph, const DevPhase& d, const Pha
     }
     a.A = ph == 1 ? dp.X2.p : dp.T.p;
     a.B = ph == 1 ? dp.Y2.p : dp.Z2.p;
-    a.C = ph == 1 ? dp.T.p : ops.O;
+    a.C = ph == 1 ? dp.T.p : (ops.Of ? (void*)ops.Of : (void*)ops.O);
     a.steps = d.steps.as<TStep>();
     a.cta_tiles = d.cta_tiles.as<int32_t>();
     a.ncta = d.ncta;
     if (d.ntiles > 0 && (!a.A || !a.B || !a.C || !a.tiles || !a.steps || !a.cta_tiles || !d.maps))
         throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
-    if (d.ntiles > 0) CK(launch_gg_umma(ph == 1 ? 1 : 0, a, *d.maps, st));
+    if (d.ntiles > 0) CK(launch_gg_umma(ph == 1 ? 1 : (ops.Of ? 2 : 0), a, *d.maps, st));
 }
 
 static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream_t st) {
@@ -517,7 +521,11 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
 
 // one application of a planned contraction: (split plans) split Y, phase 1, phase 2
 static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
-    if (dp.plan.split) CK(launch_panel_split(dp.ypieces.as<PanelPiece>(), dp.nypieces, ops.Y, dp.Y2.p, st));
+    if ((ops.Yf || ops.Of) && !dp.plan.split) throw std::invalid_argument("FP32 vectors need a split plan");
+    if (dp.plan.split) {
+        if (ops.Yf) CK(launch_panel_split_f32(dp.ypieces.as<PanelPiece>(), dp.nypieces, ops.Yf, dp.Y2.p, st));
+        else CK(launch_panel_split(dp.ypieces.as<PanelPiece>(), dp.nypieces, ops.Y, dp.Y2.p, st));
+    }
     run_phase(dp, 1, ops, st);
     run_phase(dp, 2, ops, st);
 }
@@ -1265,6 +1273,17 @@ LzWork& lz_work(vmps_ctx* c, int64_t n, int cap) {
 // operator's rounding noise (4e-6 relative) leaves on an exact eigenvector.
 constexpr double kSplitProbeRel = 1e-5;
 
+// FP32 start of a split-precision run: K32_0 = q32 = (float) K_0, padding zero
+void lz_start_f32(LzWork& W, cudaStream_t st) {
+    // (DBuf::alloc keeps a buffer that is already large enough)
+    W.K32.alloc((size_t)(W.cap + 1) * W.ld * 4, st, false);
+    W.w32.alloc((size_t)W.ld * 4, st, false);
+    W.q32.alloc((size_t)W.ld * 4, st, false);
+    CK(cudaMemsetAsync(W.w32.p, 0, (size_t)W.ld * 4, st));
+    CK(launch_lz_to_f32(W.K.as<double>(), W.K32.as<float>(), W.ld, st));
+    CK(cudaMemcpyAsync(W.q32.p, W.K32.p, (size_t)W.ld * 4, cudaMemcpyDeviceToDevice, st));
+}
+
 // one Lanczos run from K_0 (= q, normalised), at most kmax iterations
 struct LzResult {
     int m = 0;          // basis vectors of the Ritz space
@@ -1282,11 +1301,13 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
                 double probe_rel = 0) {
     cudaStream_t st = p->st();
     DevPlan& dp = get_plan(p, prec);
+    const bool f32 = prec != VMPS_PREC_FP64;   // split-precision runs keep FP32 Krylov vectors
     LzArgs a{};
-    a.K = W.K.as<double>();
+    a.fp32 = f32;
+    a.K = f32 ? W.K32.p : W.K.p;
     a.ld = W.ld;
-    a.w = W.w.as<double>();
-    a.q = W.q.as<double>();
+    a.w = f32 ? W.w32.p : W.w.p;
+    a.q = f32 ? W.q32.p : W.q.p;
     a.part = W.part.as<double>();
     a.cl = W.cl();
     a.coef = W.coef();
@@ -1300,8 +1321,13 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
     Operands ops;
     ops.X = p->dL.as<double>();
     ops.Z = p->dR.as<double>();
-    ops.Y = W.q.as<double>();
-    ops.O = W.w.as<double>();
+    if (f32) {
+        ops.Yf = W.q32.as<float>();
+        ops.Of = W.w32.as<float>();
+    } else {
+        ops.Y = W.q.as<double>();
+        ops.O = W.w.as<double>();
+    }
     ops.err = p->ctx->err;
     // one iteration = the HxV plan + the four step kernels, captured once
     cudaGraph_t g = nullptr;
@@ -1377,10 +1403,10 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
 }
 
 // x = K y / |K y| for the Ritz coefficients of a run
-void lz_ritz(vmps_pivot* p, LzWork& W, const std::vector<double>& y, double* x) {
+void lz_ritz(vmps_pivot* p, LzWork& W, const std::vector<double>& y, double* x, bool f32) {
     cudaStream_t st = p->st();
     CK(cudaMemcpyAsync(W.g(), y.data(), y.size() * 8, cudaMemcpyHostToDevice, st));
-    CK(launch_lz_combine(W.K.as<double>(), W.ld, (int)y.size(), W.n, W.g(), x, st));
+    CK(launch_lz_combine(f32 ? W.K32.p : W.K.p, f32, W.ld, (int)y.size(), W.n, W.g(), x, st));
     const double nx = std::sqrt(dev_dot(p, x, x, W.n));
     if (!(nx > 0) || !std::isfinite(nx)) throw CudaFail("Ritz vector is zero or not finite");
     CK(launch_scale(1.0 / nx, x, W.n, st));
@@ -1493,7 +1519,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
             split_phase = false;
             s.iterations = r0.m;
             s.energy_first = r0.theta;
-            lz_ritz(p, W, r0.y, x);
+            lz_ritz(p, W, r0.y, x, false);
             e = r0.theta;
             res = r0.res;
         } else {
@@ -1501,13 +1527,15 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
         }
     }
     if (split_phase) {
+        const bool f32 = prec != VMPS_PREC_FP64;
+        if (f32) lz_start_f32(W, st);
         LzResult r1 = lz_run(p, W, prec, max_iter, tol_eigval, tol_state);
         account(r1, prec);
         s.iterations = r1.m;
         s.energy_first = r1.theta;
         e = r1.theta;
         res = r1.res;
-        lz_ritz(p, W, r1.y, x);
+        lz_ritz(p, W, r1.y, x, f32);
         if (refine) {
             // FP64 residual of the split-precision Ritz vector, corrected inside
             // the split Krylov space where its error lies (the low-lying part of
@@ -1517,8 +1545,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
             s.hxv_fp64++;
             const double th0 = dev_dot(p, x, u, n);
             CK(launch_axpy(-th0, x, u, n, st));
-            CK(launch_lz_mdot(W.K.as<double>(), W.ld, r1.m, n, u, W.part.as<double>(), W.sh, W.ctl() + 4, W.g(),
-                              st));
+            CK(launch_lz_mdot(W.K32.p, 1, W.ld, r1.m, n, u, W.part.as<double>(), W.sh, W.ctl() + 4, W.g(), st));
             std::vector<double> g(r1.m);
             CK(cudaMemcpyAsync(g.data(), W.g(), (size_t)r1.m * 8, cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
@@ -1529,14 +1556,14 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
             if (model < 0 && std::sqrt(zn) < 0.5) {
                 std::vector<double> yz(r1.y);
                 for (size_t i = 0; i < yz.size(); ++i) yz[i] += z[i];
-                lz_ritz(p, W, yz, x);
+                lz_ritz(p, W, yz, x, true);
             }
             CK(cudaMemcpyAsync(K0, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(W.q.p, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
             LzResult r2 = lz_run(p, W, VMPS_PREC_FP64, std::max(1, refine_iters - 1), tol_eigval, tol_state);
             account(r2, VMPS_PREC_FP64);
             s.refine_iterations = r2.m;
-            lz_ritz(p, W, r2.y, x);
+            lz_ritz(p, W, r2.y, x, false);
             e = r2.theta;
             res = r2.res;
         }

@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                     if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
                 }
                 const int tn = ncols - c0 < 64 ? ncols - c0 : 64;   // columns of this chunk
-                if (OUT_SPLIT) {
+                if (OUT_SPLIT == 1) {
                     // T panel rows: columns col0+c0 .. +63 are two 32-wide K steps, i.e. the
                     // 256-byte row segment [hi 0-31 | lo 0-31 | hi 32-63 | lo 32-63] (16-byte
                     // units u = 8q + 4h + g: K step q, half h, columns 8g..8g+7).  Columns past
@@ -346,6 +346,21 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                         }
                     }
                     __syncwarp();   // the staging area is rewritten by the next chunk
+                } else if (OUT_SPLIT == 2) {
+                    // FP32 output: the accumulator as it is
+                    float* C = (float*)g.C;
+                    if (rl < tile.tm) {
+                        const int64_t gr = tile.row0 + rl;
+                        const int col0 = tile.col0 + c0;
+#pragma unroll
+                        for (int j = 0; j < 64; ++j) {
+                            if (j < tn) {
+                                const int64_t gc = col0 + j;
+                                C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] =
+                                    __uint_as_float(v[j]);
+                            }
+                        }
+                    }
                 } else {
                     double* C = (double*)g.C;
                     if (rl < tile.tm) {
@@ -373,15 +388,19 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
 cudaError_t umma_init() {
     cudaError_t e = cudaFuncSetAttribute(gg_umma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(gg_umma_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(gg_umma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
 }
 
-cudaError_t launch_gg_umma(int out_split, const GGArgs& a, const TmaMaps& maps, cudaStream_t st) {
+cudaError_t launch_gg_umma(int out_mode, const GGArgs& a, const TmaMaps& maps, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
     if (!a.steps || !a.cta_tiles || a.ncta <= 0 || !a.C) return cudaErrorInvalidValue;
-    if (out_split && !a.transC) return cudaErrorInvalidValue;   // the staged epilogue writes panel rows
-    if (out_split) gg_umma_kernel<1><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-    else gg_umma_kernel<0><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    if (out_mode == 1 && !a.transC) return cudaErrorInvalidValue;   // the staged epilogue writes panel rows
+    if (out_mode == 1) gg_umma_kernel<1><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 2) gg_umma_kernel<2><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 0) gg_umma_kernel<0><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 

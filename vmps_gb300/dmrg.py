@@ -24,8 +24,8 @@ import time
 
 import numpy as np
 
-from .mps import left_normalize, right_normalize
-from .pivot import EnvUpdate, PivotMatrix1, left_vacuum, right_target
+from .mps import contract_two_sites, left_normalize, right_normalize, split_two_site
+from .pivot import EnvUpdate, PivotMatrix1, PivotMatrix2, left_vacuum, right_target
 
 
 class SweepResult(dict):
@@ -109,3 +109,94 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
         if verbose:
             print(f"sweep {sweep}: E = {E:.14f}  ({sweep_times[-1]:.2f} s)", flush=True)
     return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv)
+
+
+def _env(ctx, sym, side, E, A, W):
+    e = EnvUpdate(ctx, sym, side, E, A, W, A)
+    out = e.run(E, A, A)
+    e.close()
+    return out
+
+
+def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100, tol_eigval=1e-12,
+          tol_state=1e-8, refine_iters=0, eps_svd=1e-14, pool=None, verbose=False):
+    """Two-site DMRG sweeps (DmrgSolver::iteration_two, solvers/DmrgSolver.h:1399-1522): per bond
+    (l, l+1) the two-site tensor A[l] A[l+1] (contract_AA2) is the start vector of the Lanczos
+    ground state of PivotMatrix2(L[l], R[l+2], W[l], W[l+1]); split_AA2 with a truncated SVD
+    (at most Dmax states over all sectors of the middle bond) returns the two sites, the
+    orthonormal one feeds contract_L (left-to-right) or contract_R (right-to-left).  Bond
+    bases grow and shrink with the SVD.  Abelian symmetries.
+
+    `mps` must be right-canonical with the gauge centre on site 0.  A sweep is a
+    left-to-right pass over bonds 0..L-2 followed by a right-to-left pass over L-2..0.
+    Timers per sweep as in dmrg1; "gauge" holds the two-site contraction and the SVD,
+    whose sectors run on the host cores (`pool`, a hostla.SectorPool; one is made if
+    none is given)."""
+    sym, L, nq = model.sym, model.L, model.sym.nq
+    if sym.nonabelian:
+        raise ValueError("dmrg2 supports abelian symmetries")
+    Dmax = Dmax if Dmax is not None else max(mps.bond_dim(l) for l in range(L + 1))
+    qloc = model.qloc
+    own_pool = pool is None
+    if own_pool:
+        from .hostla import SectorPool
+        pool = SectorPool()
+    envL = [None] * (L + 1)
+    envR = [None] * (L + 1)
+    envL[0] = left_vacuum(sym)
+    envR[L] = right_target(sym, mps.Qtot)
+    t0 = time.perf_counter()
+    for l in range(L - 1, 1, -1):
+        envR[l] = _env(ctx, sym, "R", envR[l + 1], mps.A[l], model.W[l])
+    t_init = time.perf_counter() - t0
+    energies, sweep_times, timers, trunc, dims, hxv = [], [], [], [], [], 0
+    E = None
+    clock = time.perf_counter
+    for sweep in range(n_sweeps):
+        ts = clock()
+        tm = dict(lanczos=0.0, precalc=0.0, gauge=0.0, lr=0.0)
+        disc_max = 0.0
+        for move, bonds in (("right", range(L - 1)), ("left", range(L - 2, -1, -1))):
+            for l in bonds:
+                t = clock()
+                A1, A2 = mps.A[l], mps.A[l + 1]
+                din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
+                dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
+                V, comb = contract_two_sites(sym, A1, A2, qloc, qloc, nq, return_basis=True)
+                t1 = clock()
+                H = PivotMatrix2(ctx, sym, envL[l], envR[l + 2], model.W[l], model.W[l + 1], V)
+                H.prepare("fp64" if refine_iters > 0 else precision)
+                t2 = clock()
+                E, v, st = H.lanczos(V.data, precision, max_iter=max_iter, tol_eigval=tol_eigval,
+                                     tol_state=tol_state, refine_iters=refine_iters)
+                hxv += st["hxv_fp64"] + st["hxv_split"]
+                H.close()
+                t3 = clock()
+                V.data[:] = v
+                A1, A2, disc, dmid = split_two_site(V, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
+                                                    eps_svd=eps_svd, pool=pool)
+                mps.A[l], mps.A[l + 1] = A1, A2
+                mps.dims[l + 1] = dmid
+                disc_max = max(disc_max, disc)
+                t4 = clock()
+                if move == "right":
+                    envL[l + 1] = _env(ctx, sym, "L", envL[l], A1, model.W[l])
+                else:
+                    envR[l + 1] = _env(ctx, sym, "R", envR[l + 2], A2, model.W[l + 1])
+                t5 = clock()
+                tm["gauge"] += (t1 - t) + (t4 - t3)
+                tm["precalc"] += t2 - t1
+                tm["lanczos"] += t3 - t2
+                tm["lr"] += t5 - t4
+        sweep_times.append(clock() - ts)
+        timers.append(tm)
+        energies.append(E)
+        trunc.append(disc_max)
+        dims.append(max(sum(mps.dims[l].values()) for l in range(1, L)))
+        if verbose:
+            print(f"sweep {sweep}: E = {E:.14f}  D = {dims[-1]}  trunc = {disc_max:.2e}  ({sweep_times[-1]:.2f} s)",
+                  flush=True)
+    if own_pool:
+        pool.close()
+    return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv,
+                       truncation=trunc, max_bond_dim=dims)

@@ -147,9 +147,10 @@ def random_site(qloc, din, dout, nq, rng, sym=None):
     return A
 
 
-def left_normalize(A, nq, carry=None, sym=None):
+def left_normalize(A, nq, carry=None, sym=None, pool=None):
     """QR per outgoing sector: A -> Q (left-orthonormal), returns (Q, R dict qout->R).
-    `carry` (dict qin -> matrix) multiplies the incoming bond first."""
+    `carry` (dict qin -> matrix) multiplies the incoming bond first.  `pool`
+    (hostla.SectorPool) runs the sector QRs in parallel."""
     A = A.like(A.data.copy())
     if carry is not None:
         for i in range(A.n):
@@ -158,10 +159,10 @@ def left_normalize(A, nq, carry=None, sym=None):
     groups = {}
     for i in range(A.n):
         groups.setdefault(tuple(A.qout[i]), []).append(i)
+    mats = [np.vstack([A.block(i) for i in idx]) for idx in groups.values()]
+    qrs = pool.map(np.linalg.qr, mats) if pool is not None else [np.linalg.qr(M) for M in mats]
     Rs = {}
-    for qout, idx in groups.items():
-        M = np.vstack([A.block(i) for i in idx])
-        Q, R = np.linalg.qr(M)
+    for (qout, idx), (Q, R) in zip(groups.items(), qrs):
         r0 = 0
         for i in idx:
             r = A.block(i).shape[0]
@@ -171,10 +172,11 @@ def left_normalize(A, nq, carry=None, sym=None):
     return A, Rs
 
 
-def right_normalize(A, nq, carry=None, sym=None):
+def right_normalize(A, nq, carry=None, sym=None, pool=None):
     """LQ per incoming sector: A -> Q (right-orthonormal), returns (Q, Lfac dict qin->L).
     `carry` (dict qout -> matrix) multiplies the outgoing bond first (A @ carry).
-    SU(2) blocks carry the weight sqrt(q_out/q_in) through the LQ."""
+    SU(2) blocks carry the weight sqrt(q_out/q_in) through the LQ.  `pool`
+    (hostla.SectorPool) runs the sector QRs in parallel."""
     A = A.like(A.data.copy())
     if carry is not None:
         for i in range(A.n):
@@ -184,11 +186,12 @@ def right_normalize(A, nq, carry=None, sym=None):
     groups = {}
     for i in range(A.n):
         groups.setdefault(tuple(A.qin[i]), []).append(i)
+    weights = {qin: [_ortho_weight(sym, qin, tuple(A.qout[i])) for i in idx] for qin, idx in groups.items()}
+    mats = [np.hstack([A.block(i) * wi for i, wi in zip(idx, weights[qin])]).T for qin, idx in groups.items()]
+    qrs = pool.map(np.linalg.qr, mats) if pool is not None else [np.linalg.qr(M) for M in mats]
     Ls = {}
-    for qin, idx in groups.items():
-        w = [_ortho_weight(sym, qin, tuple(A.qout[i])) for i in idx]
-        M = np.hstack([A.block(i) * wi for i, wi in zip(idx, w)])
-        Q, R = np.linalg.qr(M.T)
+    for (qin, idx), (Q, R) in zip(groups.items(), qrs):
+        w = weights[qin]
         Qt = Q.T
         c0 = 0
         for i, wi in zip(idx, w):
@@ -298,24 +301,127 @@ def combined_basis(sym, q12, q34):
     return {"q_of": q_of, "index": index, "n": cur}
 
 
-def contract_two_sites(sym, A1, A2, qloc12, qloc34, nq):
+def contract_two_sites(sym, A1, A2, qloc12, qloc34, nq, return_basis=False, pool=None):
     """Two-site tensor AA[s1s3](qin, qout) = sum_qmid A1[s1](qin,qmid) A2[s3](qmid,qout)
-    (abelian case of contract_AA2, tensors/DmrgContractions.h:1870-1927)."""
+    (abelian case of contract_AA2, tensors/DmrgContractions.h:1870-1927).  With
+    abelian QNs every (s1, s3) is one combined state and every A2 block is fixed
+    by (s3, qmid), so each two-site block is one product.  return_basis: also
+    return the combined basis (for split_two_site); `pool` (hostla.SectorPool)
+    runs the block products in parallel."""
     din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
     dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
     V, comb = two_site_layout(sym, qloc12, qloc34, din, dout, nq)
-    for (s1, s3), lst in comb["index"].items():
-        for qm, s13 in lst:
-            for i in range(A1.n):
-                if A1.leg[i] != s1:
-                    continue
-                qin = tuple(A1.qin[i])
-                qmid = tuple(A1.qout[i])
-                for j in range(A2.n):
-                    if A2.leg[j] != s3 or tuple(A2.qin[j]) != qmid:
-                        continue
-                    qout = tuple(A2.qout[j])
+    a2 = {}
+    for j in range(A2.n):
+        a2.setdefault((int(A2.leg[j]), tuple(A2.qin[j])), []).append(j)
+    prods = []
+    for i in range(A1.n):
+        s1, qin, qmid = int(A1.leg[i]), tuple(A1.qin[i]), tuple(A1.qout[i])
+        for s3 in range(len(qloc34)):
+            for j in a2.get((s3, qmid), ()):
+                qout = tuple(A2.qout[j])
+                for _, s13 in comb["index"][(s1, s3)]:
                     k = V.find(s13, qin, qout)
                     if k >= 0:
-                        V.block(k)[...] += A1.block(i) @ A2.block(j)
-    return V
+                        prods.append((k, i, j))
+    if pool is not None:
+        # each two-site block receives one product in the abelian case
+        outs = pool.map(lambda t: A1.block(t[1]) @ A2.block(t[2]), prods)
+        for (k, _, _), b in zip(prods, outs):
+            V.block(k)[...] += b
+    else:
+        for k, i, j in prods:
+            V.block(k)[...] += A1.block(i) @ A2.block(j)
+    return (V, comb) if return_basis else V
+
+
+def _sector_svd(M):
+    U, S, Vt = np.linalg.svd(M, full_matrices=False)
+    return U, S, Vt
+
+
+def split_two_site(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move="right", eps_svd=1e-14, pool=None):
+    """Truncated SVD of a two-site tensor back into two site tensors (abelian QNs):
+    split_AA2 with Biped::truncateSVD (tensors/DmrgContractions.h:2461-2631,
+    tensors/Biped.h:744-932).  For every middle QN qmid the matrix
+    Psi[(s1, qin), (s3, qout)] = V[s13(s1, s3)](qin, qout), qin + q(s1) = qmid, is
+    decomposed; the Dmax largest singular values over all sectors are kept (none
+    below eps_svd times the largest) and renormalised.
+    move="right": A1 = U (left-orthonormal), A2 = S Vt (the new centre);
+    move="left":  A1 = U S (the new centre), A2 = Vt (right-orthonormal).
+    Returns A1, A2, the discarded weight and the middle bond basis {qmid: dim}.
+    `pool` (hostla.SectorPool) runs the sector SVDs in parallel."""
+    pair = {}
+    for (s1, s3), lst in comb["index"].items():
+        pair[(s1, s3)] = lst[0][1]
+    rows, cols = {}, {}
+    for s1, q1 in enumerate(qloc12):
+        for qin in sorted(din):
+            qm = _add(qin, q1)
+            rows.setdefault(qm, []).append((s1, qin))
+    for s3, q3 in enumerate(qloc34):
+        for qout in sorted(dout):
+            qm = _sub(qout, q3)
+            cols.setdefault(qm, []).append((s3, qout))
+    sectors = []
+    for qm in sorted(set(rows) & set(cols)):
+        r_off, c_off, r0, c0 = [], [], 0, 0
+        for s1, qin in rows[qm]:
+            r_off.append((s1, qin, r0))
+            r0 += din[qin]
+        for s3, qout in cols[qm]:
+            c_off.append((s3, qout, c0))
+            c0 += dout[qout]
+        M = np.zeros((r0, c0))
+        any_block = False
+        for s1, qin, ra in r_off:
+            for s3, qout, ca in c_off:
+                k = V.find(pair[(s1, s3)], qin, qout)
+                if k >= 0:
+                    M[ra:ra + din[qin], ca:ca + dout[qout]] = V.block(k)
+                    any_block = True
+        if any_block:
+            sectors.append((qm, r_off, c_off, M))
+    mats = [t[3] for t in sectors]
+    svds = pool.map(_sector_svd, mats) if pool is not None else [_sector_svd(M) for M in mats]
+    allsv = np.concatenate([sv[1] for sv in svds]) if svds else np.zeros(0)
+    smax = float(allsv.max()) if allsv.size else 0.0
+    keep_vals = np.sort(allsv[allsv > eps_svd * smax])[::-1][:Dmax]
+    thresh = keep_vals[-1] if keep_vals.size else np.inf
+    kept, disc = {}, 0.0
+    # ties at the threshold: keep in sector order until Dmax is reached
+    budget = keep_vals.size
+    for (qm, _, _, _), (U, S, Vt) in zip(sectors, svds):
+        k = int(np.sum(S > thresh))
+        kept[qm] = k
+        budget -= k
+    for (qm, _, _, _), (U, S, Vt) in zip(sectors, svds):
+        if budget <= 0:
+            break
+        extra = int(np.sum(S == thresh))
+        take = min(extra, budget)
+        kept[qm] += take
+        budget -= take
+    norm2 = sum(float(np.sum(S[:kept[qm]] ** 2)) for (qm, _, _, _), (_, S, _) in zip(sectors, svds))
+    tot2 = float(np.sum(allsv ** 2))
+    disc = max(0.0, tot2 - norm2) / tot2 if tot2 > 0 else 0.0
+    scale = 1.0 / np.sqrt(norm2) if norm2 > 0 else 1.0
+    dmid = {qm: kept[qm] for qm in kept if kept[qm] > 0}
+    A1 = site_layout(qloc12, din, dmid, nq)
+    A2 = site_layout(qloc34, dmid, dout, nq)
+    for (qm, r_off, c_off, _), (U, S, Vt) in zip(sectors, svds):
+        k = kept[qm]
+        if k == 0:
+            continue
+        Sk = S[:k] * scale
+        Uk = U[:, :k] * Sk[None, :] if move == "left" else U[:, :k]
+        Vk = Vt[:k] * Sk[:, None] if move == "right" else Vt[:k]
+        for s1, qin, ra in r_off:
+            i = A1.find(s1, qin, qm)
+            if i >= 0:
+                A1.block(i)[...] = Uk[ra:ra + din[qin]]
+        for s3, qout, ca in c_off:
+            j = A2.find(s3, qm, qout)
+            if j >= 0:
+                A2.block(j)[...] = Vk[:, ca:ca + dout[qout]]
+    return A1, A2, disc, dmid
