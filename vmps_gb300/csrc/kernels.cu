@@ -125,14 +125,19 @@ __global__ void __launch_bounds__(f64k::NT, 3) gg_fp64_kernel(GGArgs g) {
     };
 
     int seg = tile.seg_begin, k0 = 0;
-    // warps whose 32x32 sub-tile is entirely outside the tile skip the MMAs
-    const bool warp_live = wm < mrem && wn < nrem;
+    // DMMA work is skipped, warp-uniformly, for 8x8 fragments wholly outside the
+    // tile and for k-quads past the end of the segment: GB300's FP64 MMA rate is
+    // fixed, so MMAs on zero padding of small blocks cost full time
+    const int mi_live = mrem > wm ? min(4, (mrem - wm + 7) >> 3) : 0;
+    const int ni_live = nrem > wn ? min(4, (nrem - wn + 7) >> 3) : 0;
+    const bool warp_live = mi_live > 0 && ni_live > 0;
     if (seg < tile.seg_end) {
         stage(seg, k0);
         int buf = 0;
         while (true) {
             commit(buf);
             __syncthreads();
+            const int kcur = min(BK, g.segs[seg].K - k0);   // valid k of the step in `buf`
             int ns = seg, nk = k0 + BK;
             if (nk >= g.segs[seg].K) { nk = 0; ++ns; }
             const bool more = ns < tile.seg_end;
@@ -141,6 +146,7 @@ __global__ void __launch_bounds__(f64k::NT, 3) gg_fp64_kernel(GGArgs g) {
                 const int g4 = lane >> 2, t4 = lane & 3;
 #pragma unroll
                 for (int kq = 0; kq < BK; kq += 4) {
+                    if (kq >= kcur) break;
                     double af[4], bf[4];
 #pragma unroll
                     for (int mi = 0; mi < 4; ++mi) {
@@ -155,7 +161,8 @@ __global__ void __launch_bounds__(f64k::NT, 3) gg_fp64_kernel(GGArgs g) {
 #pragma unroll
                     for (int mi = 0; mi < 4; ++mi)
 #pragma unroll
-                        for (int ni = 0; ni < 4; ++ni) dmma(acc[mi][ni][0], acc[mi][ni][1], af[mi], bf[ni]);
+                        for (int ni = 0; ni < 4; ++ni)
+                            if (mi < mi_live && ni < ni_live) dmma(acc[mi][ni][0], acc[mi][ni][1], af[mi], bf[ni]);
                 }
             }
             if (!more) break;
