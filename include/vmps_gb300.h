@@ -220,6 +220,33 @@ int vmps_lanczos_ground(vmps_pivot* p, double* v, int precision, int max_iter,
                         double tol_eigval, double tol_state, int refine_iters,
                         double* energy, vmps_lanczos_stats* stats);
 
+/* ---- many right-hand sides --------------------------------------------------------
+ * Vout_k = H Vin_k for k < nrhs (compact layouts, vector k at element k * dim).
+ * Split precision runs all right-hand sides in one grouped HxV (one vector split,
+ * phase 1 with the vectors side by side, phase 2 with every vector's segments);
+ * FP64 applies the plain HxV per vector.  Each right-hand side's result equals the
+ * single-vector HxV bit for bit.                                                  */
+int vmps_hxv_multi(vmps_pivot* p, const double* vin, double* vout, int nrhs, int precision);
+/* extreme Ritz values of H after `iters` FP64 Lanczos steps from v (compact): inner
+ * bounds of the spectrum for the rescaling of a polynomial expansion             */
+int vmps_spectral_bounds(vmps_pivot* p, const double* v, int iters, double* emin, double* emax);
+/* Chebyshev moments mu_k[n] = <v0_k| T_n((H - b)/a) |v0_k>, n < nmom, of nrhs start
+ * vectors v0 (compact, vector k at k * dim) advanced together: the recursion
+ * t_{n+1} = 2 H~ t_n - t_{n-1} of polyIter / MpsCompressor::polyCompress
+ * (DmrgLinearAlgebra.h:550-566, solvers/MpsCompressor.h:1372-1564) on the pivot,
+ * with FP64 vectors and FP64 moments; the HxVs in `precision` (split: one grouped
+ * launch for all right-hand sides).  ceil(nmom/2) HxVs per vector through
+ * mu_{2n} = 2<t_n,t_n> - mu_0, mu_{2n+1} = 2<t_{n+1},t_n> - mu_1.  mu: nrhs x nmom. */
+typedef struct {
+    int32_t steps;        /* recursion steps (HxV applications per vector)     */
+    int32_t hxv;          /* steps * nrhs                                       */
+    double  ms_device;    /* CUDA-event time of the steps                        */
+    double  ms_per_step;
+    double  ms_total;     /* the whole call, plans and copies included           */
+} vmps_cheb_stats;
+int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs, int nmom, double a, double b,
+                           int precision, double* mu, vmps_cheb_stats* stats);
+
 /* ---- environment updates (contract_L / contract_R, FULL mode) -----------------
  * Step 1 builds the task list and the output Tripod layout; the caller reads the
  * layout, allocates the output data, and step 2 runs the contraction.

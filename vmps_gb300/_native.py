@@ -68,6 +68,14 @@ class vmps_lanczos_stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class vmps_cheb_stats(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("hxv", C.c_int32), ("ms_device", C.c_double), ("ms_per_step", C.c_double),
+                ("ms_total", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # (name, restype, argtypes)
 _PROTOS = [
     ("vmps_last_error", C.c_char_p, []),
@@ -87,6 +95,10 @@ _PROTOS = [
     ("vmps_pivot_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),
     ("vmps_pivot_dim", C.c_int, [C.c_void_p, i64p]),
     ("vmps_hxv", C.c_int, [C.c_void_p, f64p, f64p, C.c_int]),
+    ("vmps_hxv_multi", C.c_int, [C.c_void_p, f64p, f64p, C.c_int, C.c_int]),
+    ("vmps_spectral_bounds", C.c_int, [C.c_void_p, f64p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("vmps_chebyshev_moments", C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, f64p,
+                                         C.POINTER(vmps_cheb_stats)]),
     ("vmps_dvec_create", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("vmps_dvec_destroy", C.c_int, [C.c_void_p]),
     ("vmps_dvec_upload", C.c_int, [C.c_void_p, f64p]),

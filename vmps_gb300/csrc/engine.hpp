@@ -134,7 +134,9 @@ DevLayout make_dev_layout(const std::vector<int64_t>& rows, const std::vector<in
 
 // GPU work items (POD, copied verbatim to the device)
 struct GTerm { int64_t off; double coef; };
-struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, K, pad; };
+// (split plans: akoff = K offset of the A operand inside its panel rows, a multiple of
+// 32; nonzero for the right-hand sides after the first of a multi-RHS plan)
+struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, K, akoff; };
 // one output tile: rows [row0, row0+tm) x cols [col0, col0+tn) of a block
 // (split plans: step0 / nsteps index its K steps in PhasePlan::steps)
 struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, step0, nsteps, pad0, pad1; };
@@ -169,9 +171,10 @@ struct PanelArena {
 struct OpBlock { int64_t off; int32_t outer, K, cls, row, pitch, pad; };
 
 // one K step of the tcgen05 engine: TMA descriptors (indices into the phase's
-// descriptor lists) of A and B, x = 2*k0 (column of the [hi|lo] panel), the
-// panel rows the A and B boxes start at, and the box heights
-struct TStep { int32_t amap, bmap, x, ay, by, arows, brows, pad; };
+// descriptor lists) of A and B, x = 2*k0 (column of the B operand's [hi|lo]
+// panel), the panel rows the A and B boxes start at, the box heights, and
+// xa = 2*(akoff + k0), the column of the A operand's panel
+struct TStep { int32_t amap, bmap, x, ay, by, arows, brows, xa; };
 // a TMA descriptor of a phase: box of `rows` rows over the panel matrix of class `cls`
 struct MapKey { int32_t cls, rows; };
 constexpr int kMaxMapsA = 64, kMaxMapsB = 128;
@@ -213,6 +216,11 @@ struct Plan {
     PanelArena ax, ay, at, az;                    // panels of op(X), Y, T = op(X)Y, c*op(Z)
     std::vector<PrepBlock> prepX, prepZ;          // X blocks, and c*op(Z) copies
     std::vector<OpBlock> opX, opY, opZ, opT;      // blocks of each panel arena
+    // multi-RHS split plans: nrhs vectors Y_k (and outputs O_k) at element stride
+    // Y.total (O.total); V block y's panel holds rhs k's columns from panel row
+    // k * ycolsP[y] on (ycolsP = cols rounded up to 32 when nrhs > 1)
+    int nrhs = 1;
+    std::vector<int32_t> ycolsP;
 };
 // FP64 plan: two phases, the second sums first-stage products on the fly
 Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
@@ -220,8 +228,11 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // Split-precision plan for the tcgen05 engine: op(X), Y and the chain-scaled
 // copies c*op(Z) in panels; phase 1 computes the intermediates T = op(X)Y into
 // panels, phase 2 the outputs as K-concatenations over chains.
+// nrhs > 1: the same contraction applied to nrhs vectors at once (phase 1 one
+// GEMM per V block with the right-hand sides side by side in N; phase 2 the
+// single-vector segments once per right-hand side, reading its K range of T).
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ);
+                     const DevLayout& O, bool transX, bool transZ, int nrhs = 1);
 // Static schedule of a split phase for the persistent tcgen05 engine on ncta
 // CTAs: K steps of kUmmaBK per segment with their TMA boxes, tiles assigned
 // longest-first to the least-loaded CTA and stored CTA by CTA.

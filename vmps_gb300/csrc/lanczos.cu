@@ -276,6 +276,71 @@ __global__ void lz_to_f32_kernel(const double* __restrict__ x, float* __restrict
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
         y[e] = f64_to_f32_rn(x[e]);
 }
+
+// One step of the Chebyshev recursion for nrhs vectors at once (grid: chunks x
+// right-hand sides).  Step n makes t_{n+1} = c_a (H t_n - b t_n) - c_p t_{n-1}
+// with (c_a, c_p) = (1/a, 0) for n = 0 and (2/a, 1) after, and accumulates in
+// FP64 the two inner products of the moment doubling relations
+//   mu_{2n} = 2 <t_n, t_n> - mu_0,  mu_{2n+1} = 2 <t_{n+1}, t_n> - mu_1
+// (mu_0 = <t_0, t_0>, mu_1 = <t_1, t_0> at n = 0).  The last block to finish
+// writes the moments and advances n.
+template <int E>
+__global__ void __launch_bounds__(kLzThreads) cheb_step_kernel(ChebArgs a) {
+    const int step = (int)a.ctl[0];
+    const double ca = step == 0 ? a.inv_a : 2.0 * a.inv_a, cp = step == 0 ? 0.0 : 1.0;
+    const int k = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = (int64_t)k * a.vs;
+    const int64_t e0 = (int64_t)blockIdx.x * (E * kLzThreads) + threadIdx.x;
+    __shared__ double red[2][kLzWarps];
+    double s0 = 0, s1 = 0;
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+        const int64_t e = e0 + u * kLzThreads;
+        if (e < a.n) {
+            const double x = a.tn[base + e];
+            const double v = fma(ca, fma(-a.b, x, a.w[base + e]), -cp * a.tprev[base + e]);
+            a.tnext[base + e] = v;
+            s0 = fma(x, x, s0);
+            s1 = fma(v, x, s1);
+        }
+    }
+    s0 = lz_warp_sum(s0);
+    s1 = lz_warp_sum(s1);
+    if (lane == 0) { red[0][warp] = s0; red[1][warp] = s1; }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double t = 0;
+        for (int q = 0; q < kLzWarps; ++q) t += red[threadIdx.x][q];
+        a.part[((int64_t)k * 2 + threadIdx.x) * a.nchunk + blockIdx.x] = t;
+    }
+    // last block of the whole grid (both dimensions)
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(a.ctl + 1, 1u) == gridDim.x * gridDim.y - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int r = warp; r < a.nrhs; r += kLzWarps) {
+        const double d0 = lz_row_sum(a.part, 2 * r, a.nchunk, lane);
+        const double d1 = lz_row_sum(a.part, 2 * r + 1, a.nchunk, lane);
+        if (lane == 0) {
+            double* mu = a.mu + (int64_t)r * a.nmom;
+            if (step == 0) {
+                mu[0] = d0;
+                if (a.nmom > 1) mu[1] = d1;
+            } else {
+                const int i = 2 * step;
+                if (i < a.nmom) mu[i] = 2.0 * d0 - mu[0];
+                if (i + 1 < a.nmom) mu[i + 1] = 2.0 * d1 - mu[1];
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        a.ctl[1] = 0;
+        a.ctl[0] = (unsigned)(step + 1);
+    }
+}
 }  // namespace
 
 // elements per thread (E) and chunk count for a vector length: the smallest
@@ -353,6 +418,25 @@ cudaError_t launch_lz_to_f32(const double* x, float* y, int64_t n, cudaStream_t 
     if (n <= 0 || !x || !y) return cudaErrorInvalidValue;
     const int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
     lz_to_f32_kernel<<<g, 256, 0, st>>>(x, y, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cheb_step(const ChebArgs& a, int per_thread, cudaStream_t st) {
+    if (a.nrhs < 1 || a.nrhs > 65535 || a.n <= 0 || a.nchunk < 1 || a.nmom < 1 || !a.w || !a.tn || !a.tprev ||
+        !a.tnext || !a.part || !a.mu || !a.ctl)
+        return cudaErrorInvalidValue;
+    if ((int64_t)a.nchunk * per_thread * kLzThreads < a.n || a.vs < a.n) return cudaErrorInvalidValue;
+    const dim3 grid(a.nchunk, a.nrhs);
+#define LZ_CALL(EE) cheb_step_kernel<EE><<<grid, kLzThreads, 0, st>>>(a);
+    switch (per_thread) {
+        case 1: LZ_CALL(1); break;
+        case 2: LZ_CALL(2); break;
+        case 4: LZ_CALL(4); break;
+        case 8: LZ_CALL(8); break;
+        case 16: LZ_CALL(16); break;
+        default: return cudaErrorInvalidValue;
+    }
+#undef LZ_CALL
     return cudaGetLastError();
 }
 

@@ -314,6 +314,29 @@ static std::vector<PanelPiece> panel_pieces(const std::vector<int64_t>& off, con
     return v;
 }
 
+// pieces of the vector split of a split plan: right-hand side k's block y (at
+// k * Y.total + Y.off[y]) into panel rows from k * ycolsP[y] of the block's panel;
+// with one right-hand side exactly the pieces of panel_pieces
+static std::vector<PanelPiece> vector_panel_pieces(const DevLayout& Y, const Plan& plan) {
+    std::vector<PanelPiece> v;
+    for (int k = 0; k < plan.nrhs; ++k)
+        for (size_t i = 0; i < Y.rows.size(); ++i) {
+            const int64_t rows = Y.rows[i], cols = Y.cols[i];
+            if (rows <= 0 || cols <= 0) continue;
+            const OpBlock& op = plan.opY[i];
+            if (op.K != rows || op.outer != (int64_t)plan.nrhs * plan.ycolsP[i] || plan.ycolsP[i] < cols)
+                throw std::logic_error("vector panel does not match its block");
+            const int64_t per = std::max<int64_t>(1, kPackPiece / rows);
+            for (int64_t c0 = 0; c0 < cols; c0 += per) {
+                const int64_t nc = std::min(per, cols - c0);
+                v.push_back(PanelPiece{(int64_t)k * Y.total + Y.off[i] + c0 * Y.ld[i],
+                                       op.off + ((int64_t)k * plan.ycolsP[i] + c0) * op.pitch, (int32_t)rows,
+                                       (int32_t)nc, (int32_t)Y.ld[i], op.pitch, 1.0});
+            }
+        }
+    return v;
+}
+
 // A pointer the device may dereference for a caller's host buffer, or null when
 // the buffer must be staged with a copy: page-locked (registered) memory has a
 // device mapping; pageable memory is read in place when the device walks the
@@ -384,7 +407,9 @@ static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A
         const int32_t a = ph.seg_amap[s], b = ph.seg_bmap[s];
         if (a < 0 || a >= (int32_t)A.size() || b < 0 || b >= (int32_t)B.size())
             throw std::logic_error("tcgen05 plan: operand block index out of range");
-        if (A[a].K != ph.segs[s].K || B[b].K != ph.segs[s].K || ph.segs[s].K <= 0)
+        const int32_t ko = ph.segs[s].akoff;
+        // the A operand may be a K range of wider panel rows (multi-RHS intermediates)
+        if (B[b].K != ph.segs[s].K || ph.segs[s].K <= 0 || ko < 0 || ko % 32 != 0 || ko + ph.segs[s].K > A[a].K)
             throw std::logic_error("tcgen05 plan: contraction length mismatch");
     }
     for (const GTile& t : ph.tiles) {
@@ -425,8 +450,9 @@ static void validate_tma_schedule(const PhasePlan& ph, const PanelArena& A, cons
             if (ka.rows != s.arows || kb.rows != s.brows || s.arows < t.tm || s.brows < ((t.tn + 15) / 16) * 16 ||
                 s.arows > kUmmaTileM || s.brows > kUmmaTileN)
                 throw std::logic_error("tcgen05 plan: TMA box does not cover its tile");
-            if (s.x % 64 != 0 || s.x < 0 || s.x >= 2 * A.cls[ka.cls].kpad || s.x >= 2 * B.cls[kb.cls].kpad ||
-                s.ay < 0 || s.by < 0 || s.ay >= A.cls[ka.cls].rows || s.by >= B.cls[kb.cls].rows)
+            if (s.x % 64 != 0 || s.x < 0 || s.xa % 64 != 0 || s.xa < 0 || s.xa >= 2 * A.cls[ka.cls].kpad ||
+                s.x >= 2 * B.cls[kb.cls].kpad || s.ay < 0 || s.by < 0 || s.ay >= A.cls[ka.cls].rows ||
+                s.by >= B.cls[kb.cls].rows)
                 throw std::logic_error("tcgen05 plan: TMA coordinate outside its panel");
         }
     }
@@ -460,7 +486,7 @@ static void plan_to_device(DevPlan& dp, const DevLayout& Y, cudaStream_t st) {
     upload_vec(dp.prepZ, dp.plan.prepZ, st);
     dp.nprepX = (int)dp.plan.prepX.size();
     dp.nprepZ = (int)dp.plan.prepZ.size();
-    const auto yp = panel_pieces(Y.off, Y.rows, Y.cols, Y.ld, dp.plan.opY, nullptr);
+    const auto yp = vector_panel_pieces(Y, dp.plan);
     upload_vec(dp.ypieces, yp, st);
     dp.nypieces = (int)yp.size();
     dp.p1.maps = build_phase_maps(dp.plan.p1, dp.plan.ax, dp.X2, dp.plan.ay, dp.Y2);
@@ -584,6 +610,8 @@ struct vmps_pivot_s {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     const void* graph_in[2] = {nullptr, nullptr};
     const void* graph_out[2] = {nullptr, nullptr};
+    std::map<int, std::unique_ptr<DevPlan>> multi;   // split plans for nrhs > 1 vectors, by nrhs
+    DBuf mvin, mvout;                                // nrhs padded vectors for host-buffer multi-RHS HxV
     ~vmps_pivot_s() {
         for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
     }
@@ -623,6 +651,23 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
     plan_to_device(dp, p->Vd, p->st());
     split_prepare(dp, p->dL.as<double>(), p->dR.as<double>(), p->st());
     if (prec == VMPS_PREC_BF16X3) make_chunks(p, dp);
+    CK(cudaStreamSynchronize(p->st()));
+    dp.ready = true;
+    return dp;
+}
+
+// the split plan of a pivot for nrhs vectors at once (built on first use)
+static DevPlan& get_multi_plan(vmps_pivot* p, int nrhs) {
+    if (nrhs == 1) return get_plan(p, VMPS_PREC_BF16X3);
+    auto& slot = p->multi[nrhs];
+    if (slot && slot->ready) return *slot;
+    slot.reset(new DevPlan());
+    DevPlan& dp = *slot;
+    dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, nrhs);
+    schedule_and_validate(dp.plan, p->ctx->num_sms);
+    if (p->ctx->device < 0) { dp.ready = true; return dp; }
+    plan_to_device(dp, p->Vd, p->st());
+    split_prepare(dp, p->dL.as<double>(), p->dR.as<double>(), p->st());
     CK(cudaStreamSynchronize(p->st()));
     dp.ready = true;
     return dp;
@@ -998,6 +1043,39 @@ int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int prec) {
     pack_in(p->ctx, p->dPack, p->npack, vin, p->Vt.total, p->stage_in, p->vin.as<double>(), st);
     pivot_hxv_dev(p, prec, p->vin.as<double>(), p->vout.as<double>());
     pack_out(p->ctx, p->dPack, p->npack, p->vout.as<double>(), p->Vt.total, p->stage_out, vout, st);
+    CK(cudaStreamSynchronize(st));
+    check_device_error(p->ctx);
+    API_END
+}
+
+int vmps_hxv_multi(vmps_pivot* p, const double* vin, double* vout, int nrhs, int prec) {
+    API_BEGIN
+    if (!p || !vin || !vout || nrhs < 1) return set_err(VMPS_E_ARG, "bad argument");
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
+    require_device(p->ctx);
+    cudaStream_t st = p->st();
+    ensure_staging(p);
+    const int64_t dim = p->Vt.total, n = p->Vd.total;
+    p->mvin.alloc((size_t)nrhs * n * 8, st, true);
+    p->mvout.alloc((size_t)nrhs * n * 8, st, true);
+    double* din = p->mvin.as<double>();
+    double* dout = p->mvout.as<double>();
+    for (int k = 0; k < nrhs; ++k)
+        pack_in(p->ctx, p->dPack, p->npack, vin + (int64_t)k * dim, dim, p->stage_in, din + (int64_t)k * n, st);
+    if (prec == VMPS_PREC_BF16X3) {
+        DevPlan& dp = get_multi_plan(p, nrhs);
+        Operands ops;
+        ops.X = p->dL.as<double>();
+        ops.Z = p->dR.as<double>();
+        ops.Y = din;
+        ops.O = dout;
+        ops.err = p->ctx->err;
+        run_plan(dp, ops, st);
+    } else {
+        for (int k = 0; k < nrhs; ++k) pivot_hxv_dev(p, prec, din + (int64_t)k * n, dout + (int64_t)k * n);
+    }
+    for (int k = 0; k < nrhs; ++k)
+        pack_out(p->ctx, p->dPack, p->npack, dout + (int64_t)k * n, dim, p->stage_out, vout + (int64_t)k * dim, st);
     CK(cudaStreamSynchronize(st));
     check_device_error(p->ctx);
     API_END
@@ -1575,6 +1653,137 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     *energy = e;
     s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = s;
+    API_END
+}
+
+extern "C" int vmps_spectral_bounds(vmps_pivot* p, const double* v, int iters, double* emin, double* emax) {
+    API_BEGIN
+    if (!p || !v || !emin || !emax || iters < 1 || iters >= kLzMaxIter) return set_err(VMPS_E_ARG, "bad argument");
+    require_device(p->ctx);
+    std::lock_guard<std::mutex> lock(p->ctx->lz_mu);
+    cudaStream_t st = p->st();
+    get_plan(p, VMPS_PREC_FP64);
+    const int64_t n = p->Vd.total;
+    LzWork& W = lz_work(p->ctx, n, iters);
+    for (double* b : {W.K.as<double>(), W.w.as<double>(), W.q.as<double>()})
+        CK(cudaMemsetAsync(b, 0, (size_t)W.ld * 8, st));
+    double* K0 = W.K.as<double>();
+    ensure_staging(p);
+    pack_in(p->ctx, p->dPack, p->npack, v, p->Vt.total, p->stage_in, K0, st);
+    const double n0 = std::sqrt(dev_dot(p, K0, K0, n));
+    if (!(n0 > 0) || !std::isfinite(n0)) return set_err(VMPS_E_NONFINITE, "start vector is zero or not finite");
+    CK(launch_scale(1.0 / n0, K0, n, st));
+    CK(cudaMemcpyAsync(W.q.p, K0, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+    // no convergence test: `iters` steps (or fewer at an invariant subspace)
+    LzResult r = lz_run(p, W, VMPS_PREC_FP64, iters, 0.0, -1.0);
+    CK(cudaStreamSynchronize(st));
+    check_device_error(p->ctx);
+    std::vector<double> a(r.alpha), b(r.beta), y;
+    b.resize(a.size() > 0 ? a.size() - 1 : 0);
+    double lo = 0, hi = 0;
+    tridiag_lowest(a, b, lo, y);
+    for (double& x : a) x = -x;
+    tridiag_lowest(a, b, hi, y);
+    *emin = lo;
+    *emax = -hi;
+    API_END
+}
+
+// Chebyshev moments of nrhs start vectors advanced together: the recursion
+// t_{n+1} = 2 H~ t_n - t_{n-1} of the reference's polyIter / polyCompress
+// (DmrgLinearAlgebra.h:550-566, solvers/MpsCompressor.h:1372-1564) on the
+// pivot, with H~ = (H - b)/a.  One step is one CUDA graph: the HxV of all
+// right-hand sides (split precision: one grouped multi-RHS launch pair; FP64:
+// the plain HxV per vector) and cheb_step_kernel (update and FP64 moments).
+// The three vector buffers rotate, so three graphs cover every step.
+extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs, int nmom, double a, double b,
+                                      int prec, double* mu, vmps_cheb_stats* stats) {
+    API_BEGIN
+    if (!p || !v0 || !mu || nrhs < 1 || nrhs > 65535 || nmom < 1) return set_err(VMPS_E_ARG, "bad argument");
+    if (!(a > 0) || !std::isfinite(a) || !std::isfinite(b)) return set_err(VMPS_E_ARG, "scale a must be > 0");
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
+    require_device(p->ctx);
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t st = p->st();
+    DevPlan& dp = prec == VMPS_PREC_BF16X3 ? get_multi_plan(p, nrhs) : get_plan(p, VMPS_PREC_FP64);
+    const int64_t dim = p->Vt.total, n = p->Vd.total;
+    const size_t vbytes = (size_t)nrhs * n * 8;
+    DBuf B[3], Wb, part, mud, ctl;
+    for (DBuf& x : B) x.alloc(vbytes, st, true);
+    Wb.alloc(vbytes, st, true);
+    const LzShape sh = lz_shape(n, p->ctx->num_sms);
+    part.alloc((size_t)nrhs * 2 * sh.nchunk * 8, st, false);
+    mud.alloc((size_t)nrhs * nmom * 8, st, true);
+    ctl.alloc(64, st, true);
+    ensure_staging(p);
+    for (int k = 0; k < nrhs; ++k)
+        pack_in(p->ctx, p->dPack, p->npack, v0 + (int64_t)k * dim, dim, p->stage_in, B[0].as<double>() + (int64_t)k * n,
+                st);
+    cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};
+    struct Guard {
+        cudaGraphExec_t* g;
+        ~Guard() { for (int i = 0; i < 3; ++i) if (g[i]) cudaGraphExecDestroy(g[i]); }
+    } guard{g};
+    for (int r = 0; r < 3; ++r) {
+        ChebArgs c{};
+        c.w = Wb.as<double>();
+        c.tn = B[r].as<double>();
+        c.tprev = B[(r + 2) % 3].as<double>();
+        c.tnext = B[(r + 1) % 3].as<double>();
+        c.part = part.as<double>();
+        c.mu = mud.as<double>();
+        c.ctl = ctl.as<unsigned>();
+        c.n = n;
+        c.vs = n;
+        c.nrhs = nrhs;
+        c.nmom = nmom;
+        c.nchunk = sh.nchunk;
+        c.inv_a = 1.0 / a;
+        c.b = b;
+        Operands ops;
+        ops.X = p->dL.as<double>();
+        ops.Z = p->dR.as<double>();
+        ops.err = p->ctx->err;
+        cudaGraph_t gr = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            if (prec == VMPS_PREC_BF16X3) {
+                ops.Y = c.tn;
+                ops.O = Wb.as<double>();
+                run_plan(dp, ops, st);
+            } else {
+                for (int k = 0; k < nrhs; ++k) {
+                    ops.Y = c.tn + (int64_t)k * n;
+                    ops.O = Wb.as<double>() + (int64_t)k * n;
+                    run_plan(dp, ops, st);
+                }
+            }
+            CK(launch_cheb_step(c, sh.per_thread, st));
+        } catch (...) {
+            if (cudaStreamEndCapture(st, &gr) == cudaSuccess && gr) cudaGraphDestroy(gr);
+            throw;
+        }
+        CK(cudaStreamEndCapture(st, &gr));
+        const cudaError_t ie = cudaGraphInstantiate(&g[r], gr, 0);
+        cudaGraphDestroy(gr);
+        CK(ie);
+    }
+    const int steps = (nmom + 1) / 2;
+    CK(cudaEventRecord(p->ctx->ev0, st));
+    for (int i = 0; i < steps; ++i) CK(cudaGraphLaunch(g[i % 3], st));
+    CK(cudaEventRecord(p->ctx->ev1, st));
+    CK(cudaMemcpyAsync(mu, mud.p, (size_t)nrhs * nmom * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    check_device_error(p->ctx);
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, p->ctx->ev0, p->ctx->ev1));
+    if (stats) {
+        stats->steps = steps;
+        stats->hxv = steps * nrhs;
+        stats->ms_device = ms;
+        stats->ms_per_step = ms / steps;
+        stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
     API_END
 }
 

@@ -735,6 +735,7 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const 
                     st.amap = am;
                     st.bmap = bm;
                     st.x = 2 * k0;
+                    st.xa = 2 * (ph.segs[s].akoff + k0);
                     st.ay = oa.row + t.row0;
                     st.by = ob.row + t.col0;
                     st.arows = ha;
@@ -963,10 +964,16 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // split-precision planner
 // ===========================================================================
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ) {
+                     const DevLayout& O, bool transX, bool transZ, int nrhs) {
+    if (nrhs < 1) throw std::invalid_argument("nrhs must be at least 1");
     Plan P;
     P.split = true;
     P.association = 0;
+    P.nrhs = nrhs;
+    P.ycolsP.resize(Y.rows.size());
+    for (size_t y = 0; y < Y.rows.size(); ++y)
+        P.ycolsP[y] = (int32_t)(nrhs > 1 ? (Y.cols[y] + 31) / 32 * 32 : Y.cols[y]);
+    auto ywide = [&](size_t y) { return (int64_t)nrhs * P.ycolsP[y]; };   // N of phase 1, K extent of T
     auto xm = [&](int64_t x) { return transX ? X.cols[x] : X.rows[x]; };
     auto xk = [&](int64_t x) { return transX ? X.rows[x] : X.cols[x]; };
     auto zn = [&](int64_t z) { return transZ ? Z.cols[z] : Z.rows[z]; };
@@ -997,11 +1004,12 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
             if (!uz[c.z]) { uz[c.z] = 1; bytes += 8.0 * Z.rows[c.z] * Z.cols[c.z]; }
             uo[c.out] = 1;
         }
-        for (size_t i = 0; i < Y.rows.size(); ++i) bytes += 8.0 * Y.rows[i] * Y.cols[i];
+        for (size_t i = 0; i < Y.rows.size(); ++i) bytes += 8.0 * nrhs * Y.rows[i] * Y.cols[i];
         int64_t no = 0;
-        for (size_t i = 0; i < O.rows.size(); ++i) if (uo[i]) { bytes += 8.0 * O.rows[i] * O.cols[i]; ++no; }
+        for (size_t i = 0; i < O.rows.size(); ++i) if (uo[i]) { bytes += 8.0 * nrhs * O.rows[i] * O.cols[i]; ++no; }
         P.bytes_alg = bytes;
         P.n_out_blocks = no;
+        P.flops_merged *= nrhs;
     }
 
     // panel arenas: blocks are added first (class and row), the class matrices
@@ -1126,7 +1134,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
     PanelBuilder pt{{}, {}, &tstacks};
     std::vector<int32_t> tstack(Y.rows.size(), -1);
     for (size_t y = 0; y < Y.rows.size(); ++y)
-        if (!by_y[y].empty()) tstack[y] = pt.add(stack_rows[y], Y.cols[y]);
+        if (!by_y[y].empty()) tstack[y] = pt.add(stack_rows[y], ywide(y));
     pt.finish();
     P.at = pt.a;
     P.opT.resize(ipairs.size());
@@ -1141,7 +1149,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
 
     // the vector Y in panels: panel rows are its columns, K = its rows
     PanelBuilder py{{}, {}, &P.opY};
-    for (size_t y = 0; y < Y.rows.size(); ++y) py.add(Y.cols[y], Y.rows[y]);
+    for (size_t y = 0; y < Y.rows.size(); ++y) py.add(ywide(y), Y.rows[y]);
     py.finish();
     P.ay = py.a;
 
@@ -1163,7 +1171,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         p1.segs.push_back(s);
         p1.seg_amap.push_back(xstack[y]);
         p1.seg_bmap.push_back((int32_t)y);
-        p1.flops += 2.0 * st.outer * st.K * s.K;
+        p1.flops += 2.0 * st.outer * nrhs * Y.cols[y] * s.K;
         // column tiles start on panel K steps (multiples of 32): the epilogue writes whole row segments
         add_tiles(p1, st.off, st.pitch, st.outer, st.K, sb, sb + 1, kUmmaTileM, kUmmaTileN, 32);
     }
@@ -1180,34 +1188,44 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         if (ch[a].z != ch[b].z) return ch[a].z < ch[b].z;
         return chain_t[a] < chain_t[b];
     });
+    // (multi-RHS: the same segments once per right-hand side k, whose T columns start
+    // at K offset k * ycolsP[y] and whose output is vector k)
     std::vector<char> seen(O.rows.size(), 0);
-    size_t i = 0;
-    while (i < order.size()) {
-        const int64_t o = ch[order[i]].out;
-        seen[o] = 1;
-        const int32_t sb = (int32_t)p2.segs.size();
-        double kk = 0;
-        while (i < order.size() && ch[order[i]].out == o) {
-            const size_t c = order[i];
-            const int64_t t = chain_t[c], zq = chain_zp[c];
-            GSeg s{};
-            s.term_begin = (int32_t)p2.terms.size();
-            s.term_count = 1;
-            p2.terms.push_back(GTerm{P.opT[t].off, 1.0});
-            s.K = P.opT[t].K;
-            kk += s.K;
-            p2.segs.push_back(s);
-            p2.seg_amap.push_back((int32_t)t);
-            p2.seg_bmap.push_back((int32_t)zq);
-            ++i;
+    for (int k = 0; k < nrhs; ++k) {
+        size_t i = 0;
+        while (i < order.size()) {
+            const int64_t o = ch[order[i]].out;
+            seen[o] = 1;
+            const int32_t sb = (int32_t)p2.segs.size();
+            double kk = 0;
+            while (i < order.size() && ch[order[i]].out == o) {
+                const size_t c = order[i];
+                const int64_t t = chain_t[c], zq = chain_zp[c];
+                const int64_t y = ipairs[t].second;
+                GSeg s{};
+                s.term_begin = (int32_t)p2.terms.size();
+                s.term_count = 1;
+                p2.terms.push_back(GTerm{P.opT[t].off, 1.0});
+                s.K = (int32_t)Y.cols[y];
+                s.akoff = k * P.ycolsP[y];
+                kk += s.K;
+                p2.segs.push_back(s);
+                p2.seg_amap.push_back((int32_t)t);
+                p2.seg_bmap.push_back((int32_t)zq);
+                ++i;
+            }
+            p2.flops += 2.0 * O.rows[o] * O.cols[o] * kk;
+            add_tiles(p2, O.off[o] + (int64_t)k * O.total, O.ld[o], O.rows[o], O.cols[o], sb,
+                      (int32_t)p2.segs.size(), kUmmaTileM, kUmmaTileN);
         }
-        p2.flops += 2.0 * O.rows[o] * O.cols[o] * kk;
-        add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, (int32_t)p2.segs.size(), kUmmaTileM, kUmmaTileN);
     }
     P.flops_p2_unsummed = p2.flops;
     const int32_t sb = (int32_t)p2.segs.size();
-    for (size_t o = 0; o < O.rows.size(); ++o)
-        if (!seen[o]) add_tiles(p2, O.off[o], O.ld[o], O.rows[o], O.cols[o], sb, sb, kUmmaTileM, kUmmaTileN);
+    for (int k = 0; k < nrhs; ++k)
+        for (size_t o = 0; o < O.rows.size(); ++o)
+            if (!seen[o])
+                add_tiles(p2, O.off[o] + (int64_t)k * O.total, O.ld[o], O.rows[o], O.cols[o], sb, sb, kUmmaTileM,
+                          kUmmaTileN);
     sort_tiles(p2);
     return P;
 }

@@ -212,6 +212,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
             const int amap = __shfl_sync(0xffffffffu, cur.amap, src);
             const int bmap = __shfl_sync(0xffffffffu, cur.bmap, src);
             const int x = __shfl_sync(0xffffffffu, cur.x, src);
+            const int xa = __shfl_sync(0xffffffffu, cur.xa, src);
             const int ay = __shfl_sync(0xffffffffu, cur.ay, src);
             const int by = __shfl_sync(0xffffffffu, cur.by, src);
             const int rows = __shfl_sync(0xffffffffu, cur.arows + cur.brows, src);
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                 } else {
                     const uint32_t sb = ring + st * STAGE_BYTES;
                     mbar_expect_tx(bar(st), (uint32_t)(rows * ROW_BYTES));
-                    tma_load_2d(sb, &maps.a[amap], x, ay, bar(st));
+                    tma_load_2d(sb, &maps.a[amap], xa, ay, bar(st));
                     tma_load_2d(sb + A_BYTES, &maps.b[bmap], x, by, bar(st));
                 }
             }

@@ -94,6 +94,37 @@ class _Pivot:
         N.check(N.lib().vmps_hxv(self._h, vin.ctypes.data_as(N.f64p), out.ctypes.data_as(N.f64p), _prec(precision)))
         return out
 
+    def apply_multi(self, vin: np.ndarray, precision="fp64") -> np.ndarray:
+        """H applied to the rows of vin (nrhs x dim) in one call; split precision runs
+        all right-hand sides in one grouped HxV."""
+        vin = np.ascontiguousarray(np.atleast_2d(vin), dtype=np.float64)
+        if vin.shape[1] != self.dim:
+            raise ValueError(f"vectors have {vin.shape[1]} elements, layout needs {self.dim}")
+        out = np.empty_like(vin)
+        N.check(N.lib().vmps_hxv_multi(self._h, vin.ctypes.data_as(N.f64p), out.ctypes.data_as(N.f64p),
+                                       vin.shape[0], _prec(precision)))
+        return out
+
+    def spectral_bounds(self, v0: np.ndarray, iters=80):
+        """(E_min, E_max): extreme Ritz values after `iters` FP64 Lanczos steps."""
+        v = np.ascontiguousarray(v0, dtype=np.float64)
+        lo, hi = C.c_double(), C.c_double()
+        N.check(N.lib().vmps_spectral_bounds(self._h, v.ctypes.data_as(N.f64p), iters, C.byref(lo), C.byref(hi)))
+        return lo.value, hi.value
+
+    def chebyshev_moments(self, v0: np.ndarray, nmom: int, a: float, b: float, precision="fp64"):
+        """Moments mu[k, n] = <v0_k| T_n((H - b)/a) |v0_k> of the rows of v0 (nrhs x dim),
+        advanced together on the device; returns (mu, stats)."""
+        v0 = np.ascontiguousarray(np.atleast_2d(v0), dtype=np.float64)
+        if v0.shape[1] != self.dim:
+            raise ValueError(f"vectors have {v0.shape[1]} elements, layout needs {self.dim}")
+        mu = np.empty((v0.shape[0], nmom))
+        st = N.vmps_cheb_stats()
+        N.check(N.lib().vmps_chebyshev_moments(self._h, v0.ctypes.data_as(N.f64p), v0.shape[0], nmom, float(a),
+                                               float(b), _prec(precision), mu.ctypes.data_as(N.f64p),
+                                               C.byref(st)))
+        return mu, st.as_dict()
+
     def lanczos(self, v0: np.ndarray, precision="fp64", max_iter=200, tol_eigval=1e-12, tol_state=1e-8,
                 refine_iters=0):
         """Ground state by full-reorthogonalisation Lanczos on the device."""
