@@ -215,6 +215,43 @@ def sweep_bench(ctx, args, with_cpu=True):
     return out
 
 
+def chebyshev_bench(ctx, args):
+    """Config C5 on a frozen pivot: Hubbard L=64, U=4, U(1)xU(1), D=512, the two-site
+    pivot of the middle in the sector of c_k|0> (N-1 electrons, 2Sz = -1); 32 seeded
+    start vectors (stand-ins for the momentum-resolved c_k|0> projected on the
+    pivot, one QN layout) advanced together for N=1000 Chebyshev moments of the
+    rescaled H in [-1, 1] (2 % margin).  Split precision runs all 32 right-hand
+    sides in one grouped HxV per step; moments accumulate in FP64 and each
+    moment's error is taken against the FP64 run."""
+    from vmps_gb300.pivot import PivotMatrix2
+    from vmps_gb300.workloads import hubbard_two_site
+    model, mps, Lenv, Renv, W1, W2, V, info = hubbard_two_site(ctx, L=64, D=512, seed=5, Qtot=(63, -1))
+    H = PivotMatrix2(ctx, model.sym, Lenv, Renv, W1, W2, V)
+    n, nrhs, nmom = H.dim, 32, 1000
+    rng = np.random.default_rng(5)
+    V0 = rng.standard_normal((nrhs, n))
+    V0 /= np.linalg.norm(V0, axis=1, keepdims=True)
+    lo, hi = H.spectral_bounds(V0[0], iters=120)
+    a, b = (hi - lo) / (2 * 0.98), (hi + lo) / 2
+    mu64, s64 = H.chebyshev_moments(V0, nmom, a, b, "fp64")
+    mus, ss = H.chebyshev_moments(V0, nmom, a, b, args.precision)
+    _, s1 = H.chebyshev_moments(V0[:1], nmom, a, b, args.precision)   # one right-hand side alone
+    err = np.max(np.abs(mus - mu64), axis=0)                           # per moment, over the 32 vectors (mu_0 = 1)
+    H.close()
+    per_vec_multi = ss["ms_per_step"] / nrhs
+    return {"workload": "hubbard_u1xu1_L64_D512_two_site_middle_N63_2Sz-1", "dim_V": n, "nrhs": nrhs, "nmom": nmom,
+            "spectrum": [lo, hi], "a": a, "b": b, "steps": ss["steps"],
+            "split": {"ms_total_device": ss["ms_device"], "ms_per_step": ss["ms_per_step"],
+                      "hxv_per_s": ss["hxv"] / (ss["ms_device"] * 1e-3)},
+            "fp64": {"ms_total_device": s64["ms_device"], "ms_per_step": s64["ms_per_step"],
+                     "hxv_per_s": s64["hxv"] / (s64["ms_device"] * 1e-3)},
+            "split_speedup": s64["ms_device"] / ss["ms_device"],
+            "single_rhs_split_ms_per_step": s1["ms_per_step"],
+            "batching_gain_per_vector": s1["ms_per_step"] / per_vec_multi,
+            "moment_abs_err_vs_fp64": {"max": float(err.max()), "n=1": float(err[1]), "n=10": float(err[10]),
+                                       "n=100": float(err[100]), "n=500": float(err[500]), "n=999": float(err[999])}}
+
+
 def run_reference(args):
     """CPU restatement of the reference path (the oracle), all host threads."""
     rank = int(os.environ.get("RANK", "0"))
@@ -266,6 +303,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-energy", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-chebyshev", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -378,6 +416,9 @@ def main():
     sweep = None
     if not args.no_sweep and rank == 0:
         sweep = sweep_bench(ctx, args, with_cpu=not args.no_cpu and world == 1)
+    cheb = None
+    if not args.no_chebyshev and rank == 0:
+        cheb = chebyshev_bench(ctx, args)
 
     cpu = None
     if not args.no_cpu and world == 1 and rank == 0:
@@ -412,6 +453,7 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "dmrg_sweep": sweep,
+            "chebyshev": cheb,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

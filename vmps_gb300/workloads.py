@@ -31,12 +31,14 @@ def build_envs(ctx, model, mps, lo, hi, precision="fp64"):
     return Lenv, Renv
 
 
-def hubbard_two_site(ctx, L=64, D=4096, U=4.0, seed=2, sigma=2.5, verbose=False):
-    """Hubbard U(1)xU(1) chain at half filling, Sz = 0; two-site pivot at the middle."""
+def hubbard_two_site(ctx, L=64, D=4096, U=4.0, seed=2, sigma=2.5, verbose=False, Qtot=None):
+    """Hubbard U(1)xU(1) chain, two-site pivot at the middle; total (N, 2Sz) = Qtot,
+    half filling with Sz = 0 by default."""
     t0 = time.time()
     model = models.hubbard_u1xu1(L, t=1.0, U=U)
     site = L // 2 - 1
-    mps = RandomMPS(model, (L, 0), D, seed=seed, profile="gaussian", sigma=[sigma, sigma])
+    Qtot = (L, 0) if Qtot is None else tuple(Qtot)
+    mps = RandomMPS(model, Qtot, D, seed=seed, profile="gaussian", sigma=[sigma, sigma])
     mps.canonicalize(site, site + 1)
     t1 = time.time()
     Lenv, Renv = build_envs(ctx, model, mps, site, site + 1)
