@@ -75,3 +75,39 @@ def test_su2_dmrg_matches_u1_ed(gpu_ctx, precision):
     res = dmrg1(gpu_ctx, m, mps, n_sweeps=2, precision=precision, **kw)
     e_ed = _heisenberg_ed(L)
     assert abs(res["energies"][-1] - e_ed) < 1e-10 * abs(e_ed), (res["energies"], e_ed)
+
+
+def _hubbard_ed(model_u1, L, N):
+    H = ed.permute_to_reference(ed.mpo_to_dense(model_u1), model_u1)
+    nm = 2 * L
+    mask = []
+    for s in range(2 ** nm):
+        bits = [(s >> (nm - 1 - j)) & 1 for j in range(nm)]
+        mask.append(sum(bits) == N and sum(bits[0::2]) - sum(bits[1::2]) == 0)
+    return ed.ground_energy(H, np.array(mask))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "bf16x3"])
+def test_su2xu1_hubbard_chain_matches_u1_ed(gpu_ctx, precision):
+    """SU(2)xU(1) Hubbard (reduced fermion operators, sign strings) against the U(1)xU(1) ED"""
+    from vmps_gb300.dmrg import dmrg1
+    L = 4
+    m = models.hubbard_su2xu1(L, t=1.0, U=4.0)
+    mps = RandomMPS(m, (1, L), 64, seed=7).canonicalize(0, 0)
+    kw = dict(tol_eigval=1e-10, tol_state=1e-7, refine_iters=10) if precision == "bf16x3" else {}
+    res = dmrg1(gpu_ctx, m, mps, n_sweeps=3, precision=precision, **kw)
+    e_ed = _hubbard_ed(models.hubbard_u1xu1(L, 1.0, 4.0), L, L)
+    assert abs(res["energies"][-1] - e_ed) < 1e-10 * abs(e_ed), (res["energies"], e_ed)
+
+
+def test_su2xu1_hubbard_ladder_matches_u1_ed(gpu_ctx):
+    """the width-2 ladder (range-2 hoppings through a sign string) with SU(2)xU(1); Dmax=128
+    so that the even split over the 10 middle sectors keeps every multiplet (8 at most)"""
+    from vmps_gb300.dmrg import dmrg1
+    L = 6
+    bonds = models.cylinder_bonds(3, 2)
+    m = models.hubbard_su2xu1_lattice(L, bonds, U=8.0)
+    mps = RandomMPS(m, (1, L), 128, seed=8).canonicalize(0, 0)
+    res = dmrg1(gpu_ctx, m, mps, n_sweeps=4, precision="fp64")
+    e_ed = _hubbard_ed(models.hubbard_u1xu1_lattice(L, bonds, U=8.0), L, L)
+    assert abs(res["energies"][-1] - e_ed) < 1e-10 * abs(e_ed), (res["energies"], e_ed)

@@ -248,3 +248,15 @@ def test_oracle_dmrg2_hubbard_matches_ed():
     H = ed.permute_to_reference(ed.mpo_to_dense(model), model)
     e_ed = ed.ground_energy(H, _hubbard_sector(L, L, 0))
     assert abs(res["energies"][-1] - e_ed) < 1e-10 * abs(e_ed), (res, e_ed)
+
+
+def test_lattice_mpo_matches_dense_hubbard_cylinder():
+    """the long-range lattice MPO (sign strings through intermediate sites) equals the
+    second-quantised Hubbard Hamiltonian on a 2x2 cylinder and on the open chain"""
+    bonds = models.cylinder_bonds(2, 2)
+    m = models.hubbard_u1xu1_lattice(4, bonds, U=8.0)
+    H = ed.permute_to_reference(ed.mpo_to_dense(m), m)
+    assert np.abs(H - models.dense_hubbard(4, U=8.0, bonds=bonds)).max() < 1e-12
+    chain = models.hubbard_u1xu1_lattice(4, [(i, i + 1, 1.0) for i in range(3)], U=4.0)
+    assert np.abs(ed.mpo_to_dense(chain) - ed.mpo_to_dense(models.hubbard_u1xu1(4, 1.0, 4.0))).max() < 1e-14
+    assert models.hubbard_su2xu1_lattice(64, models.cylinder_bonds(16, 4)).wdim == 10

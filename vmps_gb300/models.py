@@ -206,6 +206,162 @@ def heisenberg_su2(L, J=1.0):
     return SU2ChainModel(sym, L, qloc, ops, terms, [], name=f"HeisenbergSU2(L={L},J={J})")
 
 
+def cylinder_bonds(Lx, W, t=1.0):
+    """Bonds (i, j, t) of a width-W cylinder of Lx rings mapped to a snake: site x*W + y,
+    hoppings around each ring (periodic in y) and between neighbouring rings (range W)."""
+    bonds = set()
+    for x in range(Lx):
+        for y in range(W):
+            i = x * W + y
+            if W > 1:
+                j = x * W + (y + 1) % W
+                if j != i:
+                    bonds.add((min(i, j), max(i, j)))
+            if x + 1 < Lx:
+                bonds.add((i, i + W))
+    return [(i, j, t) for i, j in sorted(bonds)]
+
+
+class LatticeModel(ChainModel):
+    """MPO of a lattice Hamiltonian on a chain ordering (a two-dimensional lattice mapped to
+    a snake): for every bond (i < j, t_ij) and every term (A, B, c) the product
+    c t_ij A_i S_{i+1} ... S_{j-1} B_j, with the string operator S (the fermionic sign,
+    a singlet), plus on-site terms.  This is the finite-state machine that the reference's
+    MpoTerms builds from push_full / push_tight pushlists (MpoTerms.h, models/HubbardSU2xU1.h:
+    188-233): auxiliary states IDLE, DONE and OPEN(term, k) = "A applied k sites to the
+    left", present only on bonds that a lattice bond crosses (w = 2 + #terms x range in the
+    bulk).  `reduced`: operators are SU(2)-reduced (matrix, operator multiplet) pairs and W
+    holds reduced elements, as in SU2ChainModel; otherwise operator QNs follow from the
+    local basis as in ChainModel."""
+
+    def __init__(self, sym, L, qloc, ops, terms, bonds, onsite, string, reduced=False, name=""):
+        self.bonds = {}
+        for i, j, tij in bonds:
+            if not (0 <= i < j < L):
+                raise ValueError(f"bond ({i}, {j}) outside the chain")
+            self.bonds[(i, j)] = self.bonds.get((i, j), 0.0) + tij
+        self.string = string
+        self.reduced = reduced
+        super().__init__(sym, L, qloc, ops, terms, onsite, name=name)
+
+    def _build(self):
+        vac = self.sym.vacuum()
+        need = [set() for _ in range(self.L + 1)]   # (term, k) open at bond l
+        for (i, j) in self.bonds:
+            for l in range(i + 1, j + 1):
+                for t in range(len(self.terms)):
+                    need[l].add((t, l - i))
+        self.aux = []
+        for l in range(self.L + 1):
+            if l == 0:
+                self.aux.append([("IDLE", vac)])
+            elif l == self.L:
+                self.aux.append([("DONE", vac)])
+            else:
+                opened = [(f"OPEN{t}_{k}", self.ops[self.terms[t][0]][1]) for t, k in sorted(need[l])]
+                self.aux.append([("IDLE", vac)] + opened + [("DONE", vac)])
+        self.W = [self._site(l) for l in range(self.L)]
+        self.wdim = max(len(a) for a in self.aux)
+
+    def _site(self, l):
+        d = self.d
+        ain, aout = self._sector_index(self.aux[l]), self._sector_index(self.aux[l + 1])
+        vac = self.sym.vacuum()
+        I = np.eye(d)
+        S, qS = self.ops[self.string] if self.string else (I, vac)
+        entries = []   # (state_in, state_out, matrix, operator QN)
+        if "IDLE" in ain and "IDLE" in aout:
+            entries.append(("IDLE", "IDLE", I, vac))
+        if "DONE" in ain and "DONE" in aout:
+            entries.append(("DONE", "DONE", I, vac))
+        if "IDLE" in ain and "DONE" in aout and self.onsite:
+            entries.append(("IDLE", "DONE", sum(c * self.ops[o][0] for o, c in self.onsite), vac))
+        for t, (a, b, c) in enumerate(self.terms):
+            if "IDLE" in ain and f"OPEN{t}_1" in aout:
+                entries.append(("IDLE", f"OPEN{t}_1", self.ops[a][0], self.ops[a][1]))
+            for k in range(1, l + 1):
+                src = f"OPEN{t}_{k}"
+                if src not in ain:
+                    continue
+                if f"OPEN{t}_{k + 1}" in aout:
+                    entries.append((src, f"OPEN{t}_{k + 1}", S, qS))
+                tij = self.bonds.get((l - k, l))
+                if tij is not None and "DONE" in aout:
+                    entries.append((src, "DONE", c * tij * self.ops[b][0], self.ops[b][1]))
+        nz = []
+        for sin, sout, M, qop in entries:
+            for s1 in range(d):
+                for s2 in range(d):
+                    v = M[s1, s2]
+                    if abs(v) < 1e-15:
+                        continue
+                    q = tuple(qop) if self.reduced else tuple(x - y for x, y in zip(self.qloc[s1], self.qloc[s2]))
+                    nz.append((s1, s2, q, ain[sin], aout[sout], v))
+        qop_list = sorted({e[2] for e in nz})
+        kidx = {q: i for i, q in enumerate(qop_list)}
+        site = MpoSite(nq=self.sym.nq, qloc=list(self.qloc), qop=qop_list)
+        for s1, s2, q, (qi, ri), (qo, co), v in nz:
+            if self.reduced:
+                assert tuple(qo) in self.sym.fuse(tuple(qi), q), (qi, q, qo)
+            else:
+                assert tuple(x + y for x, y in zip(qi, q)) == tuple(qo), (qi, q, qo)
+            site.add(s1, s2, kidx[q], qi, qo, ri, co, v)
+        return site
+
+
+def _hubbard_u1xu1_ops(U):
+    qloc = [(0, 0), (1, 1), (1, -1), (2, 0)]
+    cdu = np.zeros((4, 4)); cdu[1, 0] = 1.0; cdu[3, 2] = 1.0
+    cdd = np.zeros((4, 4)); cdd[2, 0] = 1.0; cdd[3, 1] = -1.0
+    F = np.diag([1.0, -1.0, -1.0, 1.0])
+    cu, cd = cdu.T.copy(), cdd.T.copy()
+    ops = {"cdu_F": (cdu @ F, (1, 1)), "cdd_F": (cdd @ F, (1, -1)), "F_cu": (F @ cu, (-1, -1)),
+           "F_cd": (F @ cd, (-1, 1)), "cu": (cu, (-1, -1)), "cd": (cd, (-1, 1)), "cdu": (cdu, (1, 1)),
+           "cdd": (cdd, (1, -1)), "nupdn": (np.diag([0.0, 0.0, 0.0, 1.0]), (0, 0)), "F": (F, (0, 0))}
+    terms = [("cdu_F", "cu", -1.0), ("cdd_F", "cd", -1.0), ("F_cu", "cdu", -1.0), ("F_cd", "cdd", -1.0)]
+    onsite = [("nupdn", U)] if U != 0 else []
+    return qloc, ops, terms, onsite
+
+
+def hubbard_u1xu1_lattice(L, bonds, U=4.0):
+    """Hubbard model with U(1)xU(1) (N, 2Sz) on the bonds [(i, j, t_ij)] of a chain ordering."""
+    qloc, ops, terms, onsite = _hubbard_u1xu1_ops(U)
+    return LatticeModel(Symmetry(("U1", "U1")), L, qloc, ops, terms, bonds, onsite, "F", reduced=False,
+                        name=f"HubbardU1xU1(L={L},bonds={len(bonds)},U={U})")
+
+
+def _hubbard_su2xu1_ops(U):
+    """SU(2)xU(1) local multiplets (2S+1, N): empty (1,0), single (2,1), double (1,2); reduced
+    elements of FermionSite<SU2xU1> (sites/FermionSiteSU2xU1.h:100-123): <empty||c||single> =
+    sqrt(2), <single||c||double> = 1; c^dagger = c.adjoint() with coeff_adjoint
+    (tensors/SiteOperatorQ.h:292-305, symmetry/SU2.h:335-341), so <single||c^dag||empty> = 1,
+    <double||c^dag||single> = -sqrt(2); the sign F = diag(1, -1, 1); products with the
+    singlet F are plain matrix products (coeff_prod with a scalar factor is 1)."""
+    qloc = [(1, 0), (2, 1), (1, 2)]
+    c = np.zeros((3, 3)); c[0, 1] = np.sqrt(2.0); c[1, 2] = 1.0
+    cdag = np.zeros((3, 3)); cdag[1, 0] = 1.0; cdag[2, 1] = -np.sqrt(2.0)
+    F = np.diag([1.0, -1.0, 1.0])
+    ops = {"cdagF": (cdag @ F, (2, 1)), "cF": (c @ F, (2, -1)), "c": (c, (2, -1)), "cdag": (cdag, (2, 1)),
+           "d": (np.diag([0.0, 0.0, 1.0]), (1, 0)), "F": (F, (1, 0))}
+    # hopping of HubbardSU2xU1 (models/HubbardSU2xU1.h:429-430): -sqrt(2) t [(c^dag F)_i c_j + (c F)_i c^dag_j]
+    terms = [("cdagF", "c", -np.sqrt(2.0)), ("cF", "cdag", -np.sqrt(2.0))]
+    onsite = [("d", U)] if U != 0 else []
+    return qloc, ops, terms, onsite
+
+
+def hubbard_su2xu1_lattice(L, bonds, U=8.0):
+    """Hubbard model with SU(2)xU(1) (spin multiplet, N) on the bonds [(i, j, t_ij)] of a chain
+    ordering, as the reference's HubbardSU2xU1 builds it."""
+    qloc, ops, terms, onsite = _hubbard_su2xu1_ops(U)
+    return LatticeModel(Symmetry(("SU2", "U1")), L, qloc, ops, terms, bonds, onsite, "F", reduced=True,
+                        name=f"HubbardSU2xU1(L={L},bonds={len(bonds)},U={U})")
+
+
+def hubbard_su2xu1(L, t=1.0, U=4.0):
+    """Hubbard chain with SU(2)xU(1) symmetry (open, nearest-neighbour hopping)."""
+    return hubbard_su2xu1_lattice(L, [(i, i + 1, t) for i in range(L - 1)], U=U)
+
+
 # ---------------------------------------------------------------------------
 # exact dense Hamiltonians (independent of the MPO), for the oracle's pins
 # ---------------------------------------------------------------------------
@@ -225,9 +381,10 @@ def dense_heisenberg(L, J=1.0):
     return H
 
 
-def dense_hubbard(L, t=1.0, U=4.0):
+def dense_hubbard(L, t=1.0, U=4.0, bonds=None):
     """Full 4^L Hubbard Hamiltonian built from fermion modes (i,up),(i,dn) in order
-    (0,up),(0,dn),(1,up),... with explicit Jordan-Wigner strings over all modes."""
+    (0,up),(0,dn),(1,up),... with explicit Jordan-Wigner strings over all modes.
+    `bonds` [(i, j, t_ij)] replaces the open chain's nearest-neighbour hoppings."""
     nm = 2 * L
     a = np.array([[0.0, 1.0], [0.0, 0.0]])   # annihilator on one mode (|0>,|1>)
     Z = np.diag([1.0, -1.0])
@@ -240,11 +397,11 @@ def dense_hubbard(L, t=1.0, U=4.0):
         return o
     c = [ann(m) for m in range(nm)]
     H = np.zeros((2 ** nm, 2 ** nm))
-    for i in range(L - 1):
+    for i, j, tij in (bonds if bonds is not None else [(i, i + 1, t) for i in range(L - 1)]):
         for s in range(2):
-            m1, m2 = 2 * i + s, 2 * (i + 1) + s
+            m1, m2 = 2 * i + s, 2 * j + s
             hop = c[m1].T @ c[m2]
-            H += -t * (hop + hop.T)
+            H += -tij * (hop + hop.T)
     for i in range(L):
         H += U * (c[2 * i].T @ c[2 * i]) @ (c[2 * i + 1].T @ c[2 * i + 1])
     return H
