@@ -215,6 +215,41 @@ def sweep_bench(ctx, args, with_cpu=True):
     return out
 
 
+def su2_cylinder_bench(ctx, args):
+    """Config C3: Hubbard SU(2)xU(1), width-4 cylinder as a 64-site snake, U/t=8, 1/8 hole
+    doping (N=56, S=0), MPO w=10, D=2000 multiplets (~5,800 states); the two-site pivot of
+    the middle.  Device-resident HxV (CUDA graph, events) in FP64 and split precision, the
+    split error, and the Lanczos ground state of the pivot in both precisions."""
+    from vmps_gb300.pivot import DeviceVector, PivotMatrix2, time_hxv
+    from vmps_gb300.workloads import hubbard_su2xu1_cylinder_two_site
+    model, mps, Lenv, Renv, W1, W2, V, info = hubbard_su2xu1_cylinder_two_site(ctx)
+    H = PivotMatrix2(ctx, model.sym, Lenv, Renv, W1, W2, V)
+    st64, sts = H.stats("fp64"), H.stats(args.precision)
+    a, b = DeviceVector(H, V.data), DeviceVector(H)
+    for p in ("fp64", args.precision):
+        time_hxv(H, a, b, p, n_iter=3)
+    ms64, _ = time_hxv(H, a, b, "fp64", n_iter=10)
+    mss, _ = time_hxv(H, a, b, args.precision, n_iter=50)
+    a.close()
+    b.close()
+    h64, hs = H.apply(V.data, "fp64"), H.apply(V.data, args.precision)
+    err = float(np.linalg.norm(hs - h64) / np.linalg.norm(h64))
+    v0 = np.random.default_rng(7).standard_normal(H.dim)
+    tol = dict(tol_eigval=1e-10, tol_state=1e-6)
+    e64, _, l64 = H.lanczos(v0, "fp64", max_iter=300, **tol)
+    es, _, ls = H.lanczos(v0, args.precision, max_iter=300, refine_iters=4, **tol)
+    H.close()
+    return dict(info, n_tasks=st64["n_tasks"], flops_per_hxv=st64["flops_merged"],
+                hxv_fp64={"ms": ms64, "per_s": 1e3 / ms64, "tflops": st64["flops_merged"] / ms64 * 1e-9},
+                hxv_split={"ms": mss, "per_s": 1e3 / mss, "tflops_useful": sts["flops_merged"] / mss * 1e-9,
+                           "tensor_tflops_issued": (sts["tensor_flops_phase1"] + sts["tensor_flops_phase2"]) /
+                           mss * 1e-9},
+                split_over_fp64=ms64 / mss, hxv_split_rel_err=err,
+                lanczos={"E_fp64": e64, "E_split": es, "rel_diff": abs(es - e64) / abs(e64),
+                         "ms_fp64": l64["ms_total"], "ms_split": ls["ms_total"],
+                         "hxv_fp64": l64["hxv_fp64"], "split_hxv": [ls["hxv_split"], ls["hxv_fp64"]]})
+
+
 def chebyshev_bench(ctx, args):
     """Config C5 on a frozen pivot: Hubbard L=64, U=4, U(1)xU(1), D=512, the two-site
     pivot of the middle in the sector of c_k|0> (N-1 electrons, 2Sz = -1); 32 seeded
@@ -304,6 +339,7 @@ def main():
     ap.add_argument("--no-energy", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-chebyshev", action="store_true")
+    ap.add_argument("--no-su2", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -419,6 +455,9 @@ def main():
     cheb = None
     if not args.no_chebyshev and rank == 0:
         cheb = chebyshev_bench(ctx, args)
+    su2 = None
+    if not args.no_su2 and rank == 0:
+        su2 = su2_cylinder_bench(ctx, args)
 
     cpu = None
     if not args.no_cpu and world == 1 and rank == 0:
@@ -454,6 +493,7 @@ def main():
             "cpu_baseline": cpu,
             "dmrg_sweep": sweep,
             "chebyshev": cheb,
+            "su2xu1_cylinder": su2,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -11,7 +11,9 @@ from __future__ import annotations
 import time
 
 from . import models
-from .mps import RandomMPS, contract_two_sites
+import numpy as np
+
+from .mps import RandomMPS, contract_two_sites, two_site_layout
 from .pivot import EnvUpdate, left_vacuum, right_target
 
 
@@ -60,3 +62,31 @@ def heisenberg_one_site(ctx, L=32, D=64, seed=1, site=None):
     mps = RandomMPS(model, (0,), D, seed=seed, profile="gaussian", sigma=[4.0]).canonicalize(site, site)
     Lenv, Renv = build_envs(ctx, model, mps, site, site)
     return model, mps, Lenv, Renv, model.W[site], mps.A[site]
+
+
+def hubbard_su2xu1_cylinder_two_site(ctx, Lx=16, W=4, D=2000, U=8.0, N=None, seed=3, sigma=(3.0, 3.0), verbose=False):
+    """Config C3: Hubbard SU(2)xU(1) on a width-W cylinder of Lx rings mapped to an
+    L = Lx*W snake (hoppings around the rings and between rings, MPO w = 2W+2), U/t = U,
+    N electrons (default 1/8 hole doping), total spin 0; D multiplets per bond from a
+    Gaussian sector profile; two-site pivot at the middle.  The pivot vector is seeded
+    N(0,1) data in the SU(2) two-site layout (its values do not enter the timings)."""
+    t0 = time.time()
+    L = Lx * W
+    N = int(round(L * 7 / 8)) if N is None else N
+    model = models.hubbard_su2xu1_lattice(L, models.cylinder_bonds(Lx, W), U=U)
+    site = L // 2 - 1
+    mps = RandomMPS(model, (1, N), D, seed=seed, profile="gaussian", sigma=list(sigma))
+    mps.canonicalize(site, site + 1)
+    t1 = time.time()
+    Lenv, Renv = build_envs(ctx, model, mps, site, site + 1)
+    t2 = time.time()
+    V, _ = two_site_layout(model.sym, model.qloc, model.qloc, mps.dims[site], mps.dims[site + 2], model.sym.nq)
+    V.data[:] = np.random.default_rng(seed).standard_normal(V.data.size)
+    mid = mps.dims[site + 1]
+    info = dict(model=model.name, L=L, width=W, N=N, D_multiplets=sum(mid.values()),
+                D_states=sum(q[0] * n for q, n in mid.items()), sectors=len(mid), mpo_w=model.wdim,
+                max_sector=max(mid.values()), dim_V=int(V.data.size), seed=seed,
+                setup_mps_s=round(t1 - t0, 2), setup_env_s=round(t2 - t1, 2))
+    if verbose:
+        print("workload", info, flush=True)
+    return model, mps, Lenv, Renv, model.W[site], model.W[site + 1], V, info
