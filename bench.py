@@ -250,6 +250,81 @@ def su2_cylinder_bench(ctx, args):
                          "hxv_fp64": l64["hxv_fp64"], "split_hxv": [ls["hxv_split"], ls["hxv_fp64"]]})
 
 
+def vumps_bench(ctx, args):
+    """Config C4 pieces on a frozen cell: spin-1/2 Heisenberg with SU(2), ~470 multiplets
+    (7,000 states, D=512 requested) at the middle of a 60-site chain, the two-site cell
+    of sites 29-30 whose outer bonds carry the same basis.  Times the MpoTransferMatrix
+    application (the cell chain of contract_L plans), the GMRES environment solve
+    (FP64, and split precision with FP64 iterative refinement), and the HAC / HC
+    pivot HxVs (PivotMatrix1 / PivotMatrix0) of the cell in both precisions."""
+    from vmps_gb300 import models
+    from vmps_gb300.blocks import Blocks
+    from vmps_gb300.mps import RandomMPS
+    from vmps_gb300.pivot import DeviceVector, EnvUpdate, PivotMatrix0, PivotMatrix1, time_hxv
+    from vmps_gb300.vumps import MpoTransferMatrix
+    from vmps_gb300.workloads import build_envs
+    m = models.heisenberg_su2(60)
+    c = 29
+    # the cell sites left-normalised (the transfer operator of a left-canonical uniform
+    # MPS has spectral radius 1); the gauge centre sits at c + 2
+    mps = RandomMPS(m, (1,), 512, seed=4).canonicalize(c + 2, c + 2)
+    Lenv, Renv = build_envs(ctx, m, mps, c, c + 1)
+    rng = np.random.default_rng(5)
+    ent = [(0, q, q, rng.standard_normal((d, d))) for q, d in sorted(mps.dims[c].items())]
+    LR = Blocks.from_entries(m.sym.nq, ent)
+    order = m.basis_order_map(c)
+    vac = m.sym.vacuum()
+    ab = sorted(v for (q, i), v in order.items() if tuple(q) == vac)[0]
+    A, W = [mps.A[c], mps.A[c + 1]], [m.W[c], m.W[c + 1]]
+    T = MpoTransferMatrix(ctx, m.sym, "L", A, A, W, LR, ab, order, Lenv)
+    out = {"multiplets": sum(mps.dims[c].values()), "states": sum(q[0] * n for q, n in mps.dims[c].items()),
+           "dim_transfer_vector": int(Lenv.data.size)}
+    v = rng.standard_normal(Lenv.data.size)
+    for p in ("fp64", "bf16x3"):
+        T.hxv(v, p)
+        t0 = time.perf_counter()
+        for _ in range(5):
+            T.hxv(v, p)
+        out[f"transfer_hxv_ms_{p}"] = (time.perf_counter() - t0) / 5 * 1e3
+    b = T.rhs(rng.standard_normal(Lenv.data.size), 0.3) * T.slot_mask()
+    t0 = time.perf_counter()
+    x64, i64 = T.solve_linear(b, tol=1e-10, dimK=100)
+    t1 = time.perf_counter()
+    xs, isp = T.solve_linear_refined(b, tol=1e-10, inner_tol=1e-4, dimK=100)
+    t2 = time.perf_counter()
+    out["gmres_fp64"] = {"s": t1 - t0, "iterations": i64["iterations"], "residual": i64["residual"]}
+    out["gmres_split_refined"] = dict(isp, s=t2 - t1)
+    out["gmres_solution_rel_diff"] = float(np.sqrt(T.dot(xs - x64, xs - x64) / T.dot(x64, x64)))
+    T.close()
+    # HAC: one-site pivot of site c; HC: zero-site pivot of bond c+1
+    Rc1 = _right_env(ctx, m, mps, Renv, c)      # sites >= c + 1
+    HAC = PivotMatrix1(ctx, m.sym, Lenv, Rc1, m.W[c], mps.A[c])
+    e = EnvUpdate(ctx, m.sym, "L", Lenv, mps.A[c], m.W[c], mps.A[c])
+    Lc1 = e.run(Lenv, mps.A[c], mps.A[c])       # sites <= c
+    e.close()
+    C = Blocks.from_entries(m.sym.nq, [(0, q, q, rng.standard_normal((d, d))) for q, d in sorted(mps.dims[c + 1].items())])
+    HC = PivotMatrix0(ctx, m.sym, Lc1, Rc1, C)
+    for name, H, vec in (("hac", HAC, mps.A[c].data), ("hc", HC, C.data)):
+        a, bb = DeviceVector(H, vec), DeviceVector(H)
+        for p in ("fp64", "bf16x3"):
+            time_hxv(H, a, bb, p, n_iter=3)
+            out[f"{name}_hxv_ms_{p}"] = time_hxv(H, a, bb, p, n_iter=20)[0]
+        out[f"{name}_dim"] = H.dim
+        a.close()
+        bb.close()
+        H.close()
+    return out
+
+
+def _right_env(ctx, m, mps, Renv, site):
+    """R environment of sites >= site + 1 from the one of sites >= site + 2 (Renv)"""
+    from vmps_gb300.pivot import EnvUpdate
+    e = EnvUpdate(ctx, m.sym, "R", Renv, mps.A[site + 1], m.W[site + 1], mps.A[site + 1])
+    R = e.run(Renv, mps.A[site + 1], mps.A[site + 1])
+    e.close()
+    return R
+
+
 def chebyshev_bench(ctx, args):
     """Config C5 on a frozen pivot: Hubbard L=64, U=4, U(1)xU(1), D=512, the two-site
     pivot of the middle in the sector of c_k|0> (N-1 electrons, 2Sz = -1); 32 seeded
@@ -340,6 +415,7 @@ def main():
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-chebyshev", action="store_true")
     ap.add_argument("--no-su2", action="store_true")
+    ap.add_argument("--no-vumps", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -458,6 +534,9 @@ def main():
     su2 = None
     if not args.no_su2 and rank == 0:
         su2 = su2_cylinder_bench(ctx, args)
+    vum = None
+    if not args.no_vumps and rank == 0:
+        vum = vumps_bench(ctx, args)
 
     cpu = None
     if not args.no_cpu and world == 1 and rank == 0:
@@ -494,6 +573,7 @@ def main():
             "dmrg_sweep": sweep,
             "chebyshev": cheb,
             "su2xu1_cylinder": su2,
+            "vumps_cell": vum,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

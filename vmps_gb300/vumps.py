@@ -59,20 +59,24 @@ class MpoTransferMatrix:
 
     # ---- the transfer-vector space: blocks of mid QN ab.first at slot ab.second
     def slot_mask(self) -> np.ndarray:
-        V, (q, a) = self.V, self.ab_key
-        m = np.zeros(V.data.size, dtype=bool)
-        for i in range(V.n):
-            if tuple(V.qmid[i]) == tuple(q) and V.leg[i] == a:
-                m[V.offset[i]:V.offset[i] + V.rows[i] * V.cols[i]] = True
-        return m
+        if getattr(self, "_mask", None) is None:
+            V, (q, a) = self.V, self.ab_key
+            m = np.zeros(V.data.size, dtype=bool)
+            for i in range(V.n):
+                if tuple(V.qmid[i]) == tuple(q) and V.leg[i] == a:
+                    m[V.offset[i]:V.offset[i] + V.rows[i] * V.cols[i]] = True
+            self._mask = m
+        return self._mask
 
     def weights(self) -> np.ndarray:
         """coeff_dot(out) per element (VumpsMpoTransferMatrix.h:258-275)"""
-        V = self.V
-        w = np.zeros(V.data.size)
-        for i in range(V.n):
-            w[V.offset[i]:V.offset[i] + V.rows[i] * V.cols[i]] = self.sym.dot_weight(tuple(V.qout[i]))
-        return w
+        if getattr(self, "_w", None) is None:
+            V = self.V
+            w = np.zeros(V.data.size)
+            for i in range(V.n):
+                w[V.offset[i]:V.offset[i] + V.rows[i] * V.cols[i]] = self.sym.dot_weight(tuple(V.qout[i]))
+            self._w = w
+        return self._w
 
     def dot(self, a: np.ndarray, b: np.ndarray) -> float:
         m = self.slot_mask()
@@ -113,6 +117,8 @@ class MpoTransferMatrix:
                     Hh[j, k] = self.dot(Q[j], w)
                     w = w - Hh[j, k] * Q[j]
                 Hh[k + 1, k] = np.sqrt(self.dot(w, w))
+                if not np.all(np.isfinite(Hh[:k + 2, k])):
+                    raise FloatingPointError("GMRES: the operator produced non-finite values")
                 e1 = np.zeros(k + 2); e1[0] = beta
                 y, *_ = np.linalg.lstsq(Hh[:k + 2, :k + 1], e1, rcond=None)
                 res = np.linalg.norm(Hh[:k + 2, :k + 1] @ y - e1)
@@ -122,6 +128,30 @@ class MpoTransferMatrix:
             x = x + sum(yi * qi for yi, qi in zip(y, Q))
         r = (b - self.hxv(x, precision)) * m
         return x, {"iterations": its, "residual": np.sqrt(self.dot(r, r)) / nb}
+
+    def solve_linear_refined(self, b: np.ndarray, tol=1e-10, inner_tol=1e-4, dimK=200, max_outer=10):
+        """Mixed-precision iterative refinement: the residual r = b - H x with the FP64
+        operator, the correction H d = r by GMRES with the split-precision operator to
+        inner_tol, x += d; each round gains about the split operator's accuracy.
+        Returns (x, info) with the FP64 residual."""
+        m = self.slot_mask()
+        x = np.zeros_like(b)
+        nb = np.sqrt(self.dot(b, b))
+        info = {"outer": 0, "split_iterations": 0, "fp64_hxv": 0, "residual": 0.0}
+        if nb == 0:
+            return x, info
+        for outer in range(max_outer):
+            r = (b - self.hxv(x, "fp64")) * m
+            info["fp64_hxv"] += 1
+            res = np.sqrt(self.dot(r, r)) / nb
+            info["residual"] = res
+            if res <= tol:
+                break
+            d, inner = self.solve_linear(r, tol=inner_tol, dimK=dimK, max_restarts=2, precision="bf16x3")
+            info["split_iterations"] += inner["iterations"]
+            info["outer"] = outer + 1
+            x = x + d
+        return x, info
 
     def close(self):
         if getattr(self, "_h", None):
