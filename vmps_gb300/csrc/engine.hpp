@@ -172,7 +172,8 @@ struct OpBlock { int64_t off; int32_t outer, K, cls, row, pitch, pad; };
 
 // one K step of the tcgen05 engine: TMA descriptors (indices into the phase's
 // descriptor lists) of A and B, x = 2*k0 (column of the B operand's [hi|lo]
-// panel), the panel rows the A and B boxes start at, the box heights, and
+// panel; bit 0 set when only the step's first 16 K columns lie inside the
+// segment), the panel rows the A and B boxes start at, the box heights, and
 // xa = 2*(akoff + k0), the column of the A operand's panel
 struct TStep { int32_t amap, bmap, x, ay, by, arows, brows, xa; };
 // a TMA descriptor of a phase: box of `rows` rows over the panel matrix of class `cls`

@@ -450,8 +450,9 @@ static void validate_tma_schedule(const PhasePlan& ph, const PanelArena& A, cons
             if (ka.rows != s.arows || kb.rows != s.brows || s.arows < t.tm || s.brows < ((t.tn + 15) / 16) * 16 ||
                 s.arows > kUmmaTileM || s.brows > kUmmaTileN)
                 throw std::logic_error("tcgen05 plan: TMA box does not cover its tile");
-            if (s.x % 64 != 0 || s.x < 0 || s.xa % 64 != 0 || s.xa < 0 || s.xa >= 2 * A.cls[ka.cls].kpad ||
-                s.x >= 2 * B.cls[kb.cls].kpad || s.ay < 0 || s.by < 0 || s.ay >= A.cls[ka.cls].rows ||
+            const int32_t xb = s.x & ~1;   // bit 0 flags a padding second K16 slice
+            if (xb % 64 != 0 || xb < 0 || s.xa % 64 != 0 || s.xa < 0 || s.xa >= 2 * A.cls[ka.cls].kpad ||
+                xb >= 2 * B.cls[kb.cls].kpad || s.ay < 0 || s.by < 0 || s.ay >= A.cls[ka.cls].rows ||
                 s.by >= B.cls[kb.cls].rows)
                 throw std::logic_error("tcgen05 plan: TMA coordinate outside its panel");
         }
@@ -578,9 +579,17 @@ static void fill_stats(const ChainSet& cs, const Plan& p, int prec, vmps_plan_st
     s->flops_phase2_unsummed = p.flops_p2_unsummed;
     s->association = p.association;
     if (p.split) {
+        // bf16 MMA work issued: 3 products of M=128 x N=round16(tn) x K per step,
+        // K = 16 for steps whose second K16 slice is padding (skipped), else 32
         auto tensor = [](const PhasePlan& ph) {
             double f = 0;
-            for (const GTile& t : ph.tiles) f += (double)t.nsteps * 3.0 * 2.0 * kUmmaTileM * ((t.tn + 15) / 16 * 16) * kUmmaBK;
+            for (const GTile& t : ph.tiles) {
+                double k = 0;
+                for (int j = t.step0; j < t.step0 + t.nsteps && j < (int)ph.steps.size(); ++j)
+                    k += (ph.steps[j].x & 1) ? 16 : kUmmaBK;
+                if (ph.steps.empty()) k = (double)t.nsteps * kUmmaBK;
+                f += k * 3.0 * 2.0 * kUmmaTileM * ((t.tn + 15) / 16 * 16);
+            }
             return f;
         };
         s->tensor_flops_phase1 = tensor(p.p1);

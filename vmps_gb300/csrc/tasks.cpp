@@ -734,7 +734,8 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const 
                     TStep st{};
                     st.amap = am;
                     st.bmap = bm;
-                    st.x = 2 * k0;
+                    // bit 0 of x: only the first 16 of the 32 K columns lie inside the segment
+                    st.x = 2 * k0 | (ph.segs[s].K - k0 <= 16 ? 1 : 0);
                     st.xa = 2 * (ph.segs[s].akoff + k0);
                     st.ay = oa.row + t.row0;
                     st.by = ob.row + t.col0;

@@ -34,6 +34,7 @@ constexpr int B_BYTES = BN * ROW_BYTES;                    // B region, at most:
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;             // 48 KB
 constexpr int STAGE_OUT_BYTES = 4 * 8192;                  // split-output epilogue: 32 rows x 256 B per warp
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGE_OUT_BYTES + 1024 + 256;
+static_assert((2 * STAGES + 5) * 8 + 4 * (2 + STAGES) <= 256, "barrier area overflow");
 constexpr uint32_t ACC_COLS = BN;                          // one FP32 accumulator: 128 lanes x 256 columns
 constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two (all of TMEM), so an epilogue overlaps the next tile
 // kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1),
@@ -165,6 +166,10 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
     // [2S+4] drain of the MMAs issued
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
     volatile int* s_fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    // per stage: 1 when only the first K16 slice of its 32-wide K step lies inside
+    // the segment (written by the producer before the stage's expect-tx arrive,
+    // read by the MMA thread after the stage's full barrier)
+    volatile int* s_half = reinterpret_cast<volatile int*>(tmem_slot + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     auto bar = [&](int i) { return su32(&bars[i]); };
 
@@ -211,7 +216,8 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
             const int src = j - B;   // < 32
             const int amap = __shfl_sync(0xffffffffu, cur.amap, src);
             const int bmap = __shfl_sync(0xffffffffu, cur.bmap, src);
-            const int x = __shfl_sync(0xffffffffu, cur.x, src);
+            const int xf = __shfl_sync(0xffffffffu, cur.x, src);
+            const int x = xf & ~1;   // bit 0: the step's second K16 slice is padding
             const int xa = __shfl_sync(0xffffffffu, cur.xa, src);
             const int ay = __shfl_sync(0xffffffffu, cur.ay, src);
             const int by = __shfl_sync(0xffffffffu, cur.by, src);
@@ -223,6 +229,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                     go = 0;
                 } else {
                     const uint32_t sb = ring + st * STAGE_BYTES;
+                    s_half[st] = xf & 1;
                     mbar_expect_tx(bar(st), (uint32_t)(rows * ROW_BYTES));
                     tma_load_2d(sb, &maps.a[amap], xa, ay, bar(st));
                     tma_load_2d(sb + A_BYTES, &maps.b[bmap], x, by, bar(st));
@@ -254,8 +261,11 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                 tc_fence_after();
                 const uint32_t sb = ring + st * STAGE_BYTES;
                 const uint64_t a = sw128_desc(sb), b = sw128_desc(sb + A_BYTES);
+                // a padding half (zeros in A and B) adds nothing: its three MMAs are skipped
+                const int nk16 = s_half[st] ? 1 : BK / 16;
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
+                    if (kk >= nk16) break;
                     // 16 bf16 = 32 bytes along K; the lo halves sit 64 bytes after the hi halves
                     const uint64_t hi = (uint64_t)(kk * 32) >> 4, lo = (uint64_t)(64 + kk * 32) >> 4;
                     umma_bf16(dacc, a + lo, b + hi, idesc, (k | kk) != 0 ? 1u : 0u);
