@@ -220,6 +220,14 @@ int vmps_lanczos_ground(vmps_pivot* p, double* v, int precision, int max_iter,
                         double tol_eigval, double tol_state, int refine_iters,
                         double* energy, vmps_lanczos_stats* stats);
 
+/* ---- two-site tensor ---------------------------------------------------------------
+ * contract_AA2 (tensors/DmrgContractions.h:1870-1927, abelian QNs): V[k] = sum over the
+ * given (k, i, j) triples of A1[i] * A2[j] (block products), as one FP64 grouped GEMM on
+ * the device; prods holds nprod triples, V's blocks without a product are zero.   */
+int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* sym, const vmps_blocks* A1, const double* a1,
+                           const vmps_blocks* A2, const double* a2, const vmps_blocks* V, double* v,
+                           int64_t nprod, const int64_t* prods);
+
 /* ---- many right-hand sides --------------------------------------------------------
  * Vout_k = H Vin_k for k < nrhs (compact layouts, vector k at element k * dim).
  * Split precision runs all right-hand sides in one grouped HxV (one vector split,

@@ -49,3 +49,13 @@ def test_dmrg2_heisenberg_gpu_matches_oracle_sweep(gpu_ctx):
     c = dmrg2_cpu(model, mps_cpu, n_sweeps=4, Dmax=16)
     assert abs(g["energies"][-1] - c["energies"][-1]) < 1e-10 * abs(c["energies"][-1]), (g, c)
     assert g["max_bond_dim"][-1] == 16 and g["truncation"][-1] > 0
+
+
+def test_two_site_contraction_on_gpu_matches_host(gpu_ctx):
+    """contract_AA2 as one FP64 grouped GEMM (vmps_two_site_contract) against the host products"""
+    from vmps_gb300.mps import contract_two_sites
+    m = models.hubbard_u1xu1(12)
+    mps = RandomMPS(m, (12, 0), 96, seed=9).canonicalize(5, 6)
+    Vh, _ = contract_two_sites(m.sym, mps.A[5], mps.A[6], m.qloc, m.qloc, 2, return_basis=True)
+    Vg, _ = contract_two_sites(m.sym, mps.A[5], mps.A[6], m.qloc, m.qloc, 2, return_basis=True, ctx=gpu_ctx)
+    assert np.linalg.norm(Vg.data - Vh.data) <= 1e-14 * np.linalg.norm(Vh.data)

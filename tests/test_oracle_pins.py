@@ -218,7 +218,7 @@ def test_two_site_split_is_exact_and_orthonormal():
     nrm = V.norm()
     for move in ("right", "left"):
         A1, A2, disc, dmid = split_two_site(V, comb, m.qloc, m.qloc, din, dout, 2, Dmax=10 ** 6, move=move)
-        assert disc < 1e-28
+        assert disc < 1e-14   # eigenvalue round-off of the Gram matrix
         V2 = contract_two_sites(m.sym, A1, A2, m.qloc, m.qloc, 2)
         assert np.linalg.norm(V2.data * nrm - V.data) < 1e-13 * nrm
         O = A1 if move == "right" else A2

@@ -96,6 +96,9 @@ _PROTOS = [
     ("vmps_pivot_dim", C.c_int, [C.c_void_p, i64p]),
     ("vmps_hxv", C.c_int, [C.c_void_p, f64p, f64p, C.c_int]),
     ("vmps_hxv_multi", C.c_int, [C.c_void_p, f64p, f64p, C.c_int, C.c_int]),
+    ("vmps_two_site_contract", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
+                                         C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks), f64p, C.c_int64,
+                                         i64p]),
     ("vmps_spectral_bounds", C.c_int, [C.c_void_p, f64p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("vmps_chebyshev_moments", C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, f64p,
                                          C.POINTER(vmps_cheb_stats)]),

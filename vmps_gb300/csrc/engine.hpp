@@ -1,6 +1,7 @@
 // Internal interfaces shared by the host task-list builder (tasks.cpp), the
 // device runtime / C ABI (runtime.cpp) and the kernels (kernels.cu).
 #pragma once
+#include <array>
 #include <cstdint>
 #include <string>
 #include <unordered_map>
@@ -234,6 +235,12 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // single-vector segments once per right-hand side, reading its K range of T).
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
                      const DevLayout& O, bool transX, bool transZ, int nrhs = 1);
+// One FP64 grouped-GEMM phase of plain block products C[k] = sum A[i] * B[j] over
+// the (k, i, j) triples (contract_AA2's two-site tensor): one tile range per
+// output block, one segment per product; output blocks without a product are
+// written with zeros.
+PhasePlan make_product_plan(const DevLayout& A, const DevLayout& B, const DevLayout& C,
+                            const std::vector<std::array<int64_t, 3>>& prods);
 // Static schedule of a split phase for the persistent tcgen05 engine on ncta
 // CTAs: K steps of kUmmaBK per segment with their TMA boxes, tiles assigned
 // longest-first to the least-loaded CTA and stored CTA by CTA.

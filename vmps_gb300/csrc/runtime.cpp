@@ -1796,6 +1796,51 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
     API_END
 }
 
+// contract_AA2 (tensors/DmrgContractions.h:1870-1927, abelian): the two-site
+// tensor V[k] = sum A1[i] * A2[j] over the (k, i, j) products, as one FP64
+// grouped-GEMM launch on padded device copies of the three block tables
+extern "C" int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* A1,
+                                      const double* a1, const vmps_blocks* A2, const double* a2,
+                                      const vmps_blocks* V, double* v, int64_t nprod, const int64_t* prods) {
+    API_BEGIN
+    if (!ctx || !a1 || !a2 || !v || nprod < 0 || (nprod > 0 && !prods)) return set_err(VMPS_E_ARG, "bad argument");
+    require_device(ctx);
+    const Symmetry sym = make_sym(symd);
+    const BlockTable t1 = parse_blocks(sym, A1, false), t2 = parse_blocks(sym, A2, false),
+                     tv = parse_blocks(sym, V, false);
+    const DevLayout d1 = make_dev_layout(t1.rows, t1.cols), d2 = make_dev_layout(t2.rows, t2.cols),
+                    dv = make_dev_layout(tv.rows, tv.cols);
+    std::vector<std::array<int64_t, 3>> pr((size_t)nprod);
+    for (int64_t q = 0; q < nprod; ++q) pr[q] = {prods[3 * q], prods[3 * q + 1], prods[3 * q + 2]};
+    PhasePlan ph = make_product_plan(d1, d2, dv, pr);
+    cudaStream_t st = ctx->stream;
+    DBuf g1, g2, gv, stage;
+    upload_blocks_padded(ctx, t1, d1, a1, g1, st);
+    upload_blocks_padded(ctx, t2, d2, a2, g2, st);
+    gv.alloc((size_t)std::max<int64_t>(dv.total, 1) * 8, st, true);
+    DevPhase dph;
+    dph.upload(ph, st);
+    GGArgs g{};
+    g.A = g1.p;
+    g.B = g2.p;
+    g.C = gv.p;
+    g.err = ctx->err;
+    g.tiles = dph.tiles.as<GTile>();
+    g.segs = dph.segs.as<GSeg>();
+    g.terms = dph.terms.as<GTerm>();
+    g.ntiles = dph.ntiles;
+    CK(launch_gg64(g, st));
+    if (tv.n > 0) {
+        DBuf pk;
+        const auto pb = pack_blocks(tv, dv, nullptr);
+        upload_vec(pk, pb, st);
+        pack_out(ctx, pk, (int)pb.size(), gv.as<double>(), tv.total, stage, v, st);
+    }
+    CK(cudaStreamSynchronize(st));
+    check_device_error(ctx);
+    API_END
+}
+
 // ---------------------------------------------------------------------------
 // environment updates
 // ---------------------------------------------------------------------------

@@ -752,6 +752,41 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const 
     ph.ncta = ncta;
 }
 
+PhasePlan make_product_plan(const DevLayout& A, const DevLayout& B, const DevLayout& C,
+                            const std::vector<std::array<int64_t, 3>>& prods) {
+    PhasePlan ph;
+    ph.transA = false; ph.transB = false; ph.transC = false;
+    std::vector<std::vector<size_t>> by_out(C.rows.size());
+    for (size_t q = 0; q < prods.size(); ++q) {
+        const int64_t k = prods[q][0], i = prods[q][1], j = prods[q][2];
+        if (k < 0 || k >= (int64_t)C.rows.size() || i < 0 || i >= (int64_t)A.rows.size() || j < 0 ||
+            j >= (int64_t)B.rows.size())
+            throw std::invalid_argument("product references a block outside its table");
+        if (A.cols[i] != B.rows[j] || C.rows[k] != A.rows[i] || C.cols[k] != B.cols[j])
+            throw std::domain_error("block shapes do not chain in product " + std::to_string(q));
+        by_out[k].push_back(q);
+    }
+    for (size_t k = 0; k < C.rows.size(); ++k) {
+        const int32_t sb = (int32_t)ph.segs.size();
+        for (size_t q : by_out[k]) {
+            const int64_t i = prods[q][1], j = prods[q][2];
+            GSeg s{};
+            s.b_off = B.off[j];
+            s.term_begin = (int32_t)ph.terms.size();
+            s.term_count = 1;
+            ph.terms.push_back(GTerm{A.off[i], 1.0});
+            s.lda = (int32_t)A.ld[i];
+            s.ldb = (int32_t)B.ld[j];
+            s.K = (int32_t)A.cols[i];
+            ph.segs.push_back(s);
+            ph.flops += 2.0 * A.rows[i] * A.cols[i] * B.cols[j];
+        }
+        add_tiles(ph, C.off[k], C.ld[k], C.rows[k], C.cols[k], sb, (int32_t)ph.segs.size(), kTileMax, kTileMax);
+    }
+    sort_tiles(ph);
+    return ph;
+}
+
 Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z, const DevLayout& O,
                bool transX, bool transZ, int tile_m, int tile_n) {
     Plan P;

@@ -119,7 +119,7 @@ def _env(ctx, sym, side, E, A, W):
 
 
 def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100, tol_eigval=1e-12,
-          tol_state=1e-8, refine_iters=0, eps_svd=1e-14, pool=None, verbose=False):
+          tol_state=1e-8, refine_iters=0, eps_svd=1e-14, pool=None, factor="eigh", verbose=False):
     """Two-site DMRG sweeps (DmrgSolver::iteration_two, solvers/DmrgSolver.h:1399-1522): per bond
     (l, l+1) the two-site tensor A[l] A[l+1] (contract_AA2) is the start vector of the Lanczos
     ground state of PivotMatrix2(L[l], R[l+2], W[l], W[l+1]); split_AA2 with a truncated SVD
@@ -162,7 +162,7 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
                 A1, A2 = mps.A[l], mps.A[l + 1]
                 din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
                 dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
-                V, comb = contract_two_sites(sym, A1, A2, qloc, qloc, nq, return_basis=True)
+                V, comb = contract_two_sites(sym, A1, A2, qloc, qloc, nq, return_basis=True, ctx=ctx)
                 t1 = clock()
                 H = PivotMatrix2(ctx, sym, envL[l], envR[l + 2], model.W[l], model.W[l + 1], V)
                 H.prepare("fp64" if refine_iters > 0 else precision)
@@ -174,7 +174,7 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
                 t3 = clock()
                 V.data[:] = v
                 A1, A2, disc, dmid = split_two_site(V, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
-                                                    eps_svd=eps_svd, pool=pool)
+                                                    eps_svd=eps_svd, pool=pool, factor=factor)
                 mps.A[l], mps.A[l + 1] = A1, A2
                 mps.dims[l + 1] = dmid
                 disc_max = max(disc_max, disc)

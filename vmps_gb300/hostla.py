@@ -47,32 +47,40 @@ def _openblas_controls():
 
 
 class SectorPool:
-    """Thread pool for independent per-sector LAPACK calls (map(f, items))."""
+    """Thread pool for independent per-sector LAPACK calls (map(f, items)).  While
+    the pool is open, numpy's OpenBLAS runs one thread per call (set once: changing
+    OpenBLAS's thread count is not free); close() restores the previous count."""
 
     def __init__(self, threads: int | None = None):
         self.threads = max(1, threads or min(16, os.cpu_count() or 1))
         self._ex = ThreadPoolExecutor(self.threads) if self.threads > 1 else None
+        self._ctl = _openblas_controls() if self._ex is not None else None
+        self._prev = None
+        if self._ctl:
+            self._prev = self._ctl[1]()
+            self._ctl[0](1)
 
     def map(self, f, items):
         items = list(items)
         if self._ex is None or len(items) < 2:
             return [f(x) for x in items]
-        ctl = _openblas_controls()
-        prev = ctl[1]() if ctl else None
-        if ctl:
-            ctl[0](1)
-        try:
-            # largest sectors first so the pool drains evenly
-            order = sorted(range(len(items)), key=lambda i: -getattr(items[i], "size", 0))
-            out = [None] * len(items)
-            for i, r in zip(order, self._ex.map(lambda i: f(items[i]), order)):
-                out[i] = r
-            return out
-        finally:
-            if ctl:
-                ctl[0](prev)
+        # largest sectors first so the pool drains evenly
+        order = sorted(range(len(items)), key=lambda i: -getattr(items[i], "size", 0))
+        out = [None] * len(items)
+        for i, r in zip(order, self._ex.map(lambda i: f(items[i]), order)):
+            out[i] = r
+        return out
 
     def close(self):
         if self._ex is not None:
             self._ex.shutdown()
             self._ex = None
+        if self._ctl and self._prev is not None:
+            self._ctl[0](self._prev)
+            self._prev = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

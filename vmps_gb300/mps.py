@@ -301,13 +301,14 @@ def combined_basis(sym, q12, q34):
     return {"q_of": q_of, "index": index, "n": cur}
 
 
-def contract_two_sites(sym, A1, A2, qloc12, qloc34, nq, return_basis=False, pool=None):
+def contract_two_sites(sym, A1, A2, qloc12, qloc34, nq, return_basis=False, pool=None, ctx=None):
     """Two-site tensor AA[s1s3](qin, qout) = sum_qmid A1[s1](qin,qmid) A2[s3](qmid,qout)
     (abelian case of contract_AA2, tensors/DmrgContractions.h:1870-1927).  With
     abelian QNs every (s1, s3) is one combined state and every A2 block is fixed
     by (s3, qmid), so each two-site block is one product.  return_basis: also
     return the combined basis (for split_two_site); `pool` (hostla.SectorPool)
-    runs the block products in parallel."""
+    runs the block products in parallel on the host; `ctx` (a device Context)
+    runs them as one grouped GEMM on the GPU (vmps_two_site_contract)."""
     din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
     dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
     V, comb = two_site_layout(sym, qloc12, qloc34, din, dout, nq)
@@ -324,6 +325,15 @@ def contract_two_sites(sym, A1, A2, qloc12, qloc34, nq, return_basis=False, pool
                     k = V.find(s13, qin, qout)
                     if k >= 0:
                         prods.append((k, i, j))
+    if ctx is not None and getattr(ctx, "device", -1) >= 0 and prods:
+        from . import _native as N
+        import ctypes as C
+        tri = np.ascontiguousarray(np.array(prods, dtype=np.int64).reshape(-1, 3))
+        s_, b1, b2, bv = sym.c_struct(), A1.c_struct(), A2.c_struct(), V.c_struct()
+        N.check(N.lib().vmps_two_site_contract(ctx._h, C.byref(s_), C.byref(b1), A1.data_ptr(), C.byref(b2),
+                                               A2.data_ptr(), C.byref(bv), V.data_ptr(), len(prods),
+                                               tri.ctypes.data_as(N.i64p)))
+        return (V, comb) if return_basis else V
     if pool is not None:
         # each two-site block receives one product in the abelian case
         outs = pool.map(lambda t: A1.block(t[1]) @ A2.block(t[2]), prods)
@@ -335,12 +345,28 @@ def contract_two_sites(sym, A1, A2, qloc12, qloc34, nq, return_basis=False, pool
     return (V, comb) if return_basis else V
 
 
-def _sector_svd(M):
+def _sector_factor_svd(M, move):
+    """_sector_factor through LAPACK's SVD (gesdd)"""
     U, S, Vt = np.linalg.svd(M, full_matrices=False)
-    return U, S, Vt
+    return S, (U if move == "right" else Vt.T)
 
 
-def split_two_site(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move="right", eps_svd=1e-14, pool=None):
+def _sector_factor(M, move):
+    """Singular values (descending) and the orthonormal factor of a sector matrix M
+    that the sweep direction keeps: the left singular vectors U (move="right") or
+    the right singular vectors V (move="left"), from the eigendecomposition of the
+    Gram matrix M M^T (M^T M): the density-matrix form of the truncated SVD.  The
+    factor is orthonormal to working precision; singular values below ~1e-8 of the
+    largest lose accuracy, which touches only states of negligible weight."""
+    G = M @ M.T if move == "right" else M.T @ M
+    w, Q = np.linalg.eigh(G)
+    k = min(M.shape)
+    order = np.argsort(w)[::-1][:k]
+    return np.sqrt(np.maximum(w[order], 0.0)), Q[:, order]
+
+
+def split_two_site(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move="right", eps_svd=1e-14, pool=None,
+                   factor="eigh"):
     """Truncated SVD of a two-site tensor back into two site tensors (abelian QNs):
     split_AA2 with Biped::truncateSVD (tensors/DmrgContractions.h:2461-2631,
     tensors/Biped.h:744-932).  For every middle QN qmid the matrix
@@ -350,72 +376,89 @@ def split_two_site(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move="right", e
     move="right": A1 = U (left-orthonormal), A2 = S Vt (the new centre);
     move="left":  A1 = U S (the new centre), A2 = Vt (right-orthonormal).
     Returns A1, A2, the discarded weight and the middle bond basis {qmid: dim}.
-    `pool` (hostla.SectorPool) runs the sector SVDs in parallel."""
-    pair = {}
+    `pool` (hostla.SectorPool) runs the sector factorisations in parallel; `factor`:
+    "eigh" (Gram matrix, default) or "svd".  Either way the orthonormal factor's
+    columns are the singular vectors for the sweep direction."""
+    # each two-site block (s13, qin, qout) is one (s1, s3) pair (abelian): scatter the
+    # blocks into their middle-QN sector matrices in one pass over the blocks
+    pair_of = {}
     for (s1, s3), lst in comb["index"].items():
-        pair[(s1, s3)] = lst[0][1]
+        pair_of[lst[0][1]] = (s1, s3)
     rows, cols = {}, {}
     for s1, q1 in enumerate(qloc12):
         for qin in sorted(din):
-            qm = _add(qin, q1)
-            rows.setdefault(qm, []).append((s1, qin))
+            rows.setdefault(_add(qin, q1), []).append((s1, qin))
     for s3, q3 in enumerate(qloc34):
         for qout in sorted(dout):
-            qm = _sub(qout, q3)
-            cols.setdefault(qm, []).append((s3, qout))
-    sectors = []
-    for qm in sorted(set(rows) & set(cols)):
-        r_off, c_off, r0, c0 = [], [], 0, 0
+            cols.setdefault(_sub(qout, q3), []).append((s3, qout))
+    roff, coff, shape = {}, {}, {}
+    for qm in set(rows) & set(cols):
+        r0 = 0
         for s1, qin in rows[qm]:
-            r_off.append((s1, qin, r0))
+            roff[(s1, qin)] = (qm, r0)
             r0 += din[qin]
+        c0 = 0
         for s3, qout in cols[qm]:
-            c_off.append((s3, qout, c0))
+            coff[(s3, qout)] = (qm, c0)
             c0 += dout[qout]
-        M = np.zeros((r0, c0))
-        any_block = False
-        for s1, qin, ra in r_off:
-            for s3, qout, ca in c_off:
-                k = V.find(pair[(s1, s3)], qin, qout)
-                if k >= 0:
-                    M[ra:ra + din[qin], ca:ca + dout[qout]] = V.block(k)
-                    any_block = True
-        if any_block:
-            sectors.append((qm, r_off, c_off, M))
+        shape[qm] = (r0, c0)
+    mats_by_q = {}
+    qins, qouts, legs = [tuple(x) for x in V.qin.tolist()], [tuple(x) for x in V.qout.tolist()], V.leg.tolist()
+    for k in range(V.n):
+        s1, s3 = pair_of[legs[k]]
+        ro, co = roff.get((s1, qins[k])), coff.get((s3, qouts[k]))
+        if ro is None or co is None or ro[0] != co[0]:
+            continue
+        qm = ro[0]
+        M = mats_by_q.get(qm)
+        if M is None:
+            M = mats_by_q[qm] = np.zeros(shape[qm])
+        r, c = int(V.rows[k]), int(V.cols[k])
+        M[ro[1]:ro[1] + r, co[1]:co[1] + c] = V.block(k)
+    sectors = []
+    for qm in sorted(mats_by_q):
+        r_off = [(s1, qin, roff[(s1, qin)][1]) for s1, qin in rows[qm]]
+        c_off = [(s3, qout, coff[(s3, qout)][1]) for s3, qout in cols[qm]]
+        sectors.append((qm, r_off, c_off, mats_by_q[qm]))
     mats = [t[3] for t in sectors]
-    svds = pool.map(_sector_svd, mats) if pool is not None else [_sector_svd(M) for M in mats]
-    allsv = np.concatenate([sv[1] for sv in svds]) if svds else np.zeros(0)
+    f = _sector_factor if factor == "eigh" else _sector_factor_svd
+    fac = (lambda M: f(M, move))
+    svds = pool.map(fac, mats) if pool is not None else [fac(M) for M in mats]
+    allsv = np.concatenate([sv[0] for sv in svds]) if svds else np.zeros(0)
     smax = float(allsv.max()) if allsv.size else 0.0
     keep_vals = np.sort(allsv[allsv > eps_svd * smax])[::-1][:Dmax]
     thresh = keep_vals[-1] if keep_vals.size else np.inf
     kept, disc = {}, 0.0
     # ties at the threshold: keep in sector order until Dmax is reached
     budget = keep_vals.size
-    for (qm, _, _, _), (U, S, Vt) in zip(sectors, svds):
+    for (qm, _, _, _), (S, _) in zip(sectors, svds):
         k = int(np.sum(S > thresh))
         kept[qm] = k
         budget -= k
-    for (qm, _, _, _), (U, S, Vt) in zip(sectors, svds):
+    for (qm, _, _, _), (S, _) in zip(sectors, svds):
         if budget <= 0:
             break
         extra = int(np.sum(S == thresh))
         take = min(extra, budget)
         kept[qm] += take
         budget -= take
-    norm2 = sum(float(np.sum(S[:kept[qm]] ** 2)) for (qm, _, _, _), (_, S, _) in zip(sectors, svds))
+    norm2 = sum(float(np.sum(S[:kept[qm]] ** 2)) for (qm, _, _, _), (S, _) in zip(sectors, svds))
     tot2 = float(np.sum(allsv ** 2))
     disc = max(0.0, tot2 - norm2) / tot2 if tot2 > 0 else 0.0
     scale = 1.0 / np.sqrt(norm2) if norm2 > 0 else 1.0
     dmid = {qm: kept[qm] for qm in kept if kept[qm] > 0}
     A1 = site_layout(qloc12, din, dmid, nq)
     A2 = site_layout(qloc34, dmid, dout, nq)
-    for (qm, r_off, c_off, _), (U, S, Vt) in zip(sectors, svds):
+    for (qm, r_off, c_off, M), (S, Q) in zip(sectors, svds):
         k = kept[qm]
         if k == 0:
             continue
-        Sk = S[:k] * scale
-        Uk = U[:, :k] * Sk[None, :] if move == "left" else U[:, :k]
-        Vk = Vt[:k] * Sk[:, None] if move == "right" else Vt[:k]
+        if move == "right":       # A1 = U (orthonormal), A2 = S V^T = U^T M
+            Uk = Q[:, :k]
+            Vk = (Uk.T @ M) * scale
+        else:                     # A2 = V^T (orthonormal), A1 = U S = M V
+            Vk = Q[:, :k].T
+            Uk = (M @ Q[:, :k]) * scale
         for s1, qin, ra in r_off:
             i = A1.find(s1, qin, qm)
             if i >= 0:

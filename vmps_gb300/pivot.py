@@ -34,6 +34,7 @@ class Context:
 
     def __init__(self, device=0):
         self._h = C.c_void_p()
+        self.device = device
         N.check(N.lib().vmps_ctx_create(device, C.byref(self._h)))
 
     def close(self):
