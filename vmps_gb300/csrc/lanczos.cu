@@ -60,16 +60,58 @@ __device__ __forceinline__ double lz_row_sum(const double* part, int row, int nc
     return lz_warp_sum(s);
 }
 
+// 16-byte groups of vector elements (float4 / double2): the step kernels issue
+// one load per group, not per element (per element and basis row the work is a
+// load, a shared load and an FMA, so instruction issue, not HBM, bounded the
+// scalar form)
+template <typename V>
+struct LzPack {
+    static constexpr int W = 16 / (int)sizeof(V);
+    V v[W];
+};
+template <typename V>
+__device__ __forceinline__ LzPack<V> lz_ld16(const V* p) {
+    LzPack<V> r;
+    *reinterpret_cast<uint4*>(&r) = *reinterpret_cast<const uint4*>(p);
+    return r;
+}
+template <typename V>
+__device__ __forceinline__ void lz_st16(V* p, const LzPack<V>& r) {
+    *reinterpret_cast<uint4*>(p) = *reinterpret_cast<const uint4*>(&r);
+}
+// whole 16-byte groups per thread in a chunk of E * 256 elements
+template <typename V, int E>
+struct LzVecOk {
+    static constexpr bool value = E % LzPack<V>::W == 0;
+};
+
 // partial dot of basis row `ki` (chunk-relative) with the chunk of w staged in
 // shared memory: one warp, len valid elements, four independent accumulators
-// in the vector type, FP64 from the warp sum on
+// in the vector type, FP64 from the warp sum on.  Full chunks go by 16-byte
+// groups; the partial last chunk element by element.
 template <typename V, int E>
 __device__ __forceinline__ double lz_chunk_dot(const V* __restrict__ ki, const V* wsh, int len, int lane) {
     V s[4] = {0, 0, 0, 0};
+    constexpr int W = LzPack<V>::W;
+    bool done = false;
+    if constexpr (LzVecOk<V, E>::value) {
+        if (len == E * 256) {
 #pragma unroll
-    for (int t = 0; t < E * 8; ++t) {
-        const int x = lane + 32 * t;
-        if (x < len) s[t & 3] = fma(ki[x], wsh[x], s[t & 3]);
+            for (int t = 0; t < E * 8 / W; ++t) {
+                const int x = (lane + 32 * t) * W;
+                const LzPack<V> a = lz_ld16(ki + x), b = lz_ld16(wsh + x);
+#pragma unroll
+                for (int q = 0; q < W; ++q) s[t & 3] = fma(a.v[q], b.v[q], s[t & 3]);
+            }
+            done = true;
+        }
+    }
+    if (!done) {
+#pragma unroll
+        for (int t = 0; t < E * 8; ++t) {
+            const int x = lane + 32 * t;
+            if (x < len) s[t & 3] = fma(ki[x], wsh[x], s[t & 3]);
+        }
     }
     return lz_warp_sum((double)((s[0] + s[1]) + (s[2] + s[3])));
 }
@@ -113,7 +155,7 @@ __global__ void __launch_bounds__(kLzThreads) lz_local_kernel(LzArgs a) {
 
 template <typename V, int E>
 __global__ void __launch_bounds__(kLzThreads) lz_proj_kernel(LzArgs a) {
-    __shared__ V wsh[E * kLzThreads];   // this block's chunk of w after the local step
+    __shared__ __align__(16) V wsh[E * kLzThreads];   // this block's chunk of w after the local step
     const int j = (int)a.ctl[0];
     if (j >= a.kmax) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -124,16 +166,40 @@ __global__ void __launch_bounds__(kLzThreads) lz_proj_kernel(LzArgs a) {
     V* w = (V*)a.w;
     const V* kj = K + (int64_t)j * a.ld + cb;
     const V* km = j > 0 ? K + (int64_t)(j - 1) * a.ld + cb : nullptr;
+    bool done = false;
+    if constexpr (LzVecOk<V, E>::value) {
+        constexpr int W = LzPack<V>::W;
+        if (len == E * kLzThreads) {
 #pragma unroll
-    for (int u = 0; u < E; ++u) {
-        const int x = threadIdx.x + u * kLzThreads;
-        V v = 0;
-        if (x < len) {
-            v = fma(-c1, kj[x], w[cb + x]);
-            if (km) v = fma(-c0, km[x], v);
-            w[cb + x] = v;
+            for (int u = 0; u < E / W; ++u) {
+                const int x = (threadIdx.x + u * kLzThreads) * W;
+                LzPack<V> v = lz_ld16(w + cb + x);
+                const LzPack<V> b = lz_ld16(kj + x);
+#pragma unroll
+                for (int q = 0; q < W; ++q) v.v[q] = fma(-c1, b.v[q], v.v[q]);
+                if (km) {
+                    const LzPack<V> m = lz_ld16(km + x);
+#pragma unroll
+                    for (int q = 0; q < W; ++q) v.v[q] = fma(-c0, m.v[q], v.v[q]);
+                }
+                lz_st16(w + cb + x, v);
+                lz_st16(wsh + x, v);
+            }
+            done = true;
         }
-        wsh[x] = v;
+    }
+    if (!done) {
+#pragma unroll
+        for (int u = 0; u < E; ++u) {
+            const int x = threadIdx.x + u * kLzThreads;
+            V v = 0;
+            if (x < len) {
+                v = fma(-c1, kj[x], w[cb + x]);
+                if (km) v = fma(-c0, km[x], v);
+                w[cb + x] = v;
+            }
+            wsh[x] = v;
+        }
     }
     __syncthreads();
     // one warp per basis row: d_i partial over this chunk
@@ -158,29 +224,60 @@ __global__ void __launch_bounds__(kLzThreads) lz_orth_kernel(LzArgs a) {
     const int64_t e0 = (int64_t)blockIdx.x * (E * kLzThreads) + threadIdx.x;
     const V* K = (const V*)a.K;
     V* w = (V*)a.w;
-    V wr[E];
+    V s = 0;
+    const int64_t cb = (int64_t)blockIdx.x * (E * kLzThreads);
+    bool done = false;
+    if constexpr (LzVecOk<V, E>::value) {
+      constexpr int W = LzPack<V>::W;
+      if (cb + E * kLzThreads <= a.n) {
+        // full chunk: each thread owns E / W 16-byte groups
+        LzPack<V> wr[E / W];
 #pragma unroll
-    for (int u = 0; u < E; ++u) {
-        const int64_t e = e0 + u * kLzThreads;
-        wr[u] = e < a.n ? w[e] : V(0);
+        for (int u = 0; u < E / W; ++u) wr[u] = lz_ld16(w + cb + (threadIdx.x + u * kLzThreads) * W);
+#pragma unroll 2
+        for (int i = 0; i <= j; ++i) {
+            const V* ki = K + (int64_t)i * a.ld + cb;
+            const V d = (V)a.coef[i];
+#pragma unroll
+            for (int u = 0; u < E / W; ++u) {
+                const LzPack<V> kv = lz_ld16(ki + (threadIdx.x + u * kLzThreads) * W);
+#pragma unroll
+                for (int q = 0; q < W; ++q) wr[u].v[q] = fma(-d, kv.v[q], wr[u].v[q]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < E / W; ++u) {
+            lz_st16(w + cb + (threadIdx.x + u * kLzThreads) * W, wr[u]);
+#pragma unroll
+            for (int q = 0; q < W; ++q) s = fma(wr[u].v[q], wr[u].v[q], s);
+        }
+        done = true;
+      }
     }
-#pragma unroll 4
-    for (int i = 0; i <= j; ++i) {
-        const V* ki = K + (int64_t)i * a.ld;
-        const V d = (V)a.coef[i];
+    if (!done) {
+        V wr[E];
 #pragma unroll
         for (int u = 0; u < E; ++u) {
             const int64_t e = e0 + u * kLzThreads;
-            if (e < a.n) wr[u] = fma(-d, ki[e], wr[u]);
+            wr[u] = e < a.n ? w[e] : V(0);
         }
-    }
-    V s = 0;
+#pragma unroll 4
+        for (int i = 0; i <= j; ++i) {
+            const V* ki = K + (int64_t)i * a.ld;
+            const V d = (V)a.coef[i];
 #pragma unroll
-    for (int u = 0; u < E; ++u) {
-        const int64_t e = e0 + u * kLzThreads;
-        if (e < a.n) {
-            w[e] = wr[u];
-            s = fma(wr[u], wr[u], s);
+            for (int u = 0; u < E; ++u) {
+                const int64_t e = e0 + u * kLzThreads;
+                if (e < a.n) wr[u] = fma(-d, ki[e], wr[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < E; ++u) {
+            const int64_t e = e0 + u * kLzThreads;
+            if (e < a.n) {
+                w[e] = wr[u];
+                s = fma(wr[u], wr[u], s);
+            }
         }
     }
     const double ds = lz_warp_sum((double)s);
@@ -250,7 +347,7 @@ __global__ void __launch_bounds__(kLzThreads) lz_mdot_kernel(const V* __restrict
                                                               const double* __restrict__ r,
                                                               double* __restrict__ part, int nchunk,
                                                               unsigned* counter, double* __restrict__ out) {
-    __shared__ V rsh[E * kLzThreads];
+    __shared__ __align__(16) V rsh[E * kLzThreads];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t cb = (int64_t)blockIdx.x * (E * kLzThreads);
     const int len = (int)(n - cb < E * kLzThreads ? n - cb : E * kLzThreads);
