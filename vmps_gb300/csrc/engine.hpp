@@ -140,7 +140,10 @@ struct GTerm { int64_t off; double coef; };
 struct GSeg  { int64_t b_off; int32_t term_begin, term_count; int32_t lda, ldb, K, akoff; };
 // one output tile: rows [row0, row0+tm) x cols [col0, col0+tn) of a block
 // (split plans: step0 / nsteps index its K steps in PhasePlan::steps)
-struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, step0, nsteps, pad0, pad1; };
+// (multi-RHS split plans: rstride = the per-right-hand-side column stride ycolsP of a
+// phase-1 tile, nrhs = R on every tile of the plan; the intermediates' panel rows and
+// the phase-2 tile rows are interleaved, row R*i + k = row i of right-hand side k)
+struct GTile { int64_t c_off; int32_t ldc, row0, col0, tm, tn, seg_begin, seg_end, step0, nsteps, rstride, nrhs; };
 // at most this many A terms per segment (the FP64 kernel stages them in shared memory)
 constexpr int kMaxTerms = 16;
 // FP64 engine tiles are at most 64 x 64 (rows split on multiples of 16, columns
@@ -219,9 +222,12 @@ struct Plan {
     std::vector<PrepBlock> prepX, prepZ;          // X blocks, and c*op(Z) copies
     std::vector<OpBlock> opX, opY, opZ, opT;      // blocks of each panel arena
     // multi-RHS split plans: nrhs vectors Y_k (and outputs O_k) at element stride
-    // Y.total (O.total); V block y's panel holds rhs k's columns from panel row
-    // k * ycolsP[y] on (ycolsP = cols rounded up to 32 when nrhs > 1)
+    // Y.total (O.total = vstride); V block y's panel holds rhs k's columns from
+    // panel row k * ycolsP[y] on (ycolsP = cols rounded up to 32 when nrhs > 1);
+    // phase 1 writes the intermediate of rhs k to the interleaved panel rows R*i + k,
+    // so one phase-2 tile (R*m rows) serves every right-hand side of its rows
     int nrhs = 1;
+    int64_t vstride = 0;
     std::vector<int32_t> ycolsP;
 };
 // FP64 plan: two phases, the second sums first-stage products on the fly

@@ -21,6 +21,7 @@ struct GGArgs {
     const GTerm* terms;
     int ntiles;
     int transA, transB, transC;
+    int64_t vstride;   // multi-RHS phase 2: element stride between the output vectors
 };
 
 // tcgen05 engine: TMA descriptors of a phase, passed by value as a grid-constant
@@ -44,7 +45,8 @@ cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st);
 // 0: C is double
 cudaError_t umma_init();
 // out_mode: 0 FP64 output, 1 bf16 [hi|lo] panel rows (split intermediates), 2 FP32 output
-cudaError_t launch_gg_umma(int out_mode, const GGArgs& a, const TmaMaps& maps, cudaStream_t st);
+// multi: tiles of a multi-RHS plan (interleaved right-hand sides)
+cudaError_t launch_gg_umma(int out_mode, bool multi, const GGArgs& a, const TmaMaps& maps, cudaStream_t st);
 // split operands: FP64 blocks -> bf16 [hi|lo] panels
 cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* dst, cudaStream_t st);
 cudaError_t launch_panel_split(const PanelPiece* pieces, int np, const double* src, void* dst, cudaStream_t st);

@@ -422,6 +422,9 @@ static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A
                 throw std::logic_error("tcgen05 plan: tile outside its operand blocks");
         if (split_out && (!ph.transC || t.col0 % 32 != 0 || t.ldc % 64 != 0 || t.c_off % 64 != 0))
             throw std::logic_error("tcgen05 plan: split-output tile not on whole panel K steps");
+        if (t.nrhs > 1 && ((split_out && (t.rstride <= 0 || t.rstride % 32 != 0 || t.col0 + t.tn > t.nrhs * t.rstride)) ||
+                           (!split_out && ph.transC)))
+            throw std::logic_error("tcgen05 plan: multi-RHS tile with a bad right-hand-side stride");
     }
 }
 
@@ -536,9 +539,10 @@ static void run_phase_on(const DevPlan& dp, int ph, const DevPhase& d, const Pha
     a.steps = d.steps.as<TStep>();
     a.cta_tiles = d.cta_tiles.as<int32_t>();
     a.ncta = d.ncta;
+    a.vstride = dp.plan.vstride;
     if (d.ntiles > 0 && (!a.A || !a.B || !a.C || !a.tiles || !a.steps || !a.cta_tiles || !d.maps))
         throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
-    if (d.ntiles > 0) CK(launch_gg_umma(ph == 1 ? 1 : (ops.Of ? 2 : 0), a, *d.maps, st));
+    if (d.ntiles > 0) CK(launch_gg_umma(ph == 1 ? 1 : (ops.Of ? 2 : 0), dp.plan.nrhs > 1, a, *d.maps, st));
 }
 
 static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream_t st) {

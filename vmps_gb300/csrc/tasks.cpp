@@ -1006,6 +1006,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
     P.split = true;
     P.association = 0;
     P.nrhs = nrhs;
+    P.vstride = O.total;
     P.ycolsP.resize(Y.rows.size());
     for (size_t y = 0; y < Y.rows.size(); ++y)
         P.ycolsP[y] = (int32_t)(nrhs > 1 ? (Y.cols[y] + 31) / 32 * 32 : Y.cols[y]);
@@ -1169,17 +1170,18 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
     std::vector<OpBlock> tstacks;
     PanelBuilder pt{{}, {}, &tstacks};
     std::vector<int32_t> tstack(Y.rows.size(), -1);
+    // (multi-RHS: R*stack rows of K = ycolsP, the rows of rhs k interleaved at R*i + k)
     for (size_t y = 0; y < Y.rows.size(); ++y)
-        if (!by_y[y].empty()) tstack[y] = pt.add(stack_rows[y], ywide(y));
+        if (!by_y[y].empty()) tstack[y] = pt.add((int64_t)nrhs * stack_rows[y], P.ycolsP[y]);
     pt.finish();
     P.at = pt.a;
     P.opT.resize(ipairs.size());
     for (size_t j = 0; j < ipairs.size(); ++j) {
         const OpBlock& sk = tstacks[tstack[ipairs[j].second]];
         OpBlock b = sk;
-        b.outer = (int32_t)xm(ipairs[j].first);
-        b.row = sk.row + (int32_t)row_in_stack[j];
-        b.off = sk.off + row_in_stack[j] * sk.pitch;
+        b.outer = (int32_t)(nrhs * xm(ipairs[j].first));
+        b.row = sk.row + (int32_t)(nrhs * row_in_stack[j]);
+        b.off = sk.off + (int64_t)nrhs * row_in_stack[j] * sk.pitch;
         P.opT[j] = b;
     }
 
@@ -1207,9 +1209,14 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         p1.segs.push_back(s);
         p1.seg_amap.push_back(xstack[y]);
         p1.seg_bmap.push_back((int32_t)y);
-        p1.flops += 2.0 * st.outer * nrhs * Y.cols[y] * s.K;
+        p1.flops += 2.0 * stack_rows[y] * nrhs * Y.cols[y] * s.K;
         // column tiles start on panel K steps (multiples of 32): the epilogue writes whole row segments
-        add_tiles(p1, st.off, st.pitch, st.outer, st.K, sb, sb + 1, kUmmaTileM, kUmmaTileN, 32);
+        const size_t t0 = p1.tiles.size();
+        add_tiles(p1, st.off, st.pitch, stack_rows[y], ywide(y), sb, sb + 1, kUmmaTileM, kUmmaTileN, 32);
+        for (size_t t = t0; t < p1.tiles.size(); ++t) {
+            p1.tiles[t].rstride = P.ycolsP[y];
+            p1.tiles[t].nrhs = nrhs;
+        }
     }
     sort_tiles(p1);
 
@@ -1224,44 +1231,47 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         if (ch[a].z != ch[b].z) return ch[a].z < ch[b].z;
         return chain_t[a] < chain_t[b];
     });
-    // (multi-RHS: the same segments once per right-hand side k, whose T columns start
-    // at K offset k * ycolsP[y] and whose output is vector k)
+    // (multi-RHS: the tiles span R*m interleaved rows, row R*i + k of output block o
+    // being row i of vector k's block o; one tile serves every right-hand side)
     std::vector<char> seen(O.rows.size(), 0);
-    for (int k = 0; k < nrhs; ++k) {
-        size_t i = 0;
-        while (i < order.size()) {
-            const int64_t o = ch[order[i]].out;
-            seen[o] = 1;
-            const int32_t sb = (int32_t)p2.segs.size();
-            double kk = 0;
-            while (i < order.size() && ch[order[i]].out == o) {
-                const size_t c = order[i];
-                const int64_t t = chain_t[c], zq = chain_zp[c];
-                const int64_t y = ipairs[t].second;
-                GSeg s{};
-                s.term_begin = (int32_t)p2.terms.size();
-                s.term_count = 1;
-                p2.terms.push_back(GTerm{P.opT[t].off, 1.0});
-                s.K = (int32_t)Y.cols[y];
-                s.akoff = k * P.ycolsP[y];
-                kk += s.K;
-                p2.segs.push_back(s);
-                p2.seg_amap.push_back((int32_t)t);
-                p2.seg_bmap.push_back((int32_t)zq);
-                ++i;
-            }
-            p2.flops += 2.0 * O.rows[o] * O.cols[o] * kk;
-            add_tiles(p2, O.off[o] + (int64_t)k * O.total, O.ld[o], O.rows[o], O.cols[o], sb,
-                      (int32_t)p2.segs.size(), kUmmaTileM, kUmmaTileN);
+    auto mark = [&](size_t t0) {
+        for (size_t t = t0; t < p2.tiles.size(); ++t) p2.tiles[t].nrhs = nrhs;
+    };
+    size_t i = 0;
+    while (i < order.size()) {
+        const int64_t o = ch[order[i]].out;
+        seen[o] = 1;
+        const int32_t sb = (int32_t)p2.segs.size();
+        double kk = 0;
+        while (i < order.size() && ch[order[i]].out == o) {
+            const size_t c = order[i];
+            const int64_t t = chain_t[c], zq = chain_zp[c];
+            const int64_t y = ipairs[t].second;
+            GSeg s{};
+            s.term_begin = (int32_t)p2.terms.size();
+            s.term_count = 1;
+            p2.terms.push_back(GTerm{P.opT[t].off, 1.0});
+            s.K = (int32_t)Y.cols[y];
+            kk += s.K;
+            p2.segs.push_back(s);
+            p2.seg_amap.push_back((int32_t)t);
+            p2.seg_bmap.push_back((int32_t)zq);
+            ++i;
         }
+        p2.flops += 2.0 * nrhs * O.rows[o] * O.cols[o] * kk;
+        const size_t t0 = p2.tiles.size();
+        add_tiles(p2, O.off[o], O.ld[o], (int64_t)nrhs * O.rows[o], O.cols[o], sb, (int32_t)p2.segs.size(),
+                  kUmmaTileM, kUmmaTileN);
+        mark(t0);
     }
     P.flops_p2_unsummed = p2.flops;
     const int32_t sb = (int32_t)p2.segs.size();
-    for (int k = 0; k < nrhs; ++k)
-        for (size_t o = 0; o < O.rows.size(); ++o)
-            if (!seen[o])
-                add_tiles(p2, O.off[o] + (int64_t)k * O.total, O.ld[o], O.rows[o], O.cols[o], sb, sb, kUmmaTileM,
-                          kUmmaTileN);
+    for (size_t o = 0; o < O.rows.size(); ++o)
+        if (!seen[o]) {
+            const size_t t0 = p2.tiles.size();
+            add_tiles(p2, O.off[o], O.ld[o], (int64_t)nrhs * O.rows[o], O.cols[o], sb, sb, kUmmaTileM, kUmmaTileN);
+            mark(t0);
+        }
     sort_tiles(p2);
     return P;
 }

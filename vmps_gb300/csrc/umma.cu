@@ -153,7 +153,7 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
 //     overlapping the next tile's main loop.  A split output (T panels) is
 //     staged through swizzled shared memory so that each panel row segment is
 //     one 256-byte store.
-template <int OUT_SPLIT>
+template <int OUT_SPLIT, bool MULTI>
 __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, const __grid_constant__ TmaMaps maps) {
     using namespace um;
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -351,38 +351,39 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                         const uint4 val = *reinterpret_cast<const uint4*>(so + row * 256 + ((u ^ (row & 15)) << 4));
                         if (sp * 32 + row < tile.tm && ucol < tn) {
                             // (col0 + c0) is a multiple of 32: the chunk starts a panel K step
-                            const int64_t e = tile.c_off + (int64_t)(tile.row0 + sp * 32 + row) * tile.ldc +
-                                              (int64_t)((tile.col0 + c0) >> 5) * 64 + u * 8;
+                            int64_t e;
+                            if (MULTI) {
+                                // multi-RHS: column n = k * rstride + c goes to panel row R*i + k, K step c/32
+                                const int n = tile.col0 + c0 + (u >> 3) * 32;
+                                const int k = n / tile.rstride, c = n - k * tile.rstride;
+                                e = tile.c_off + ((int64_t)(tile.row0 + sp * 32 + row) * tile.nrhs + k) * tile.ldc +
+                                    (int64_t)(c >> 5) * 64 + (u & 7) * 8;
+                            } else {
+                                e = tile.c_off + (int64_t)(tile.row0 + sp * 32 + row) * tile.ldc +
+                                    (int64_t)((tile.col0 + c0) >> 5) * 64 + u * 8;
+                            }
                             *reinterpret_cast<uint4*>(C + e) = val;
                         }
                     }
                     __syncwarp();   // the staging area is rewritten by the next chunk
-                } else if (OUT_SPLIT == 2) {
-                    // FP32 output: the accumulator as it is
-                    float* C = (float*)g.C;
-                    if (rl < tile.tm) {
-                        const int64_t gr = tile.row0 + rl;
-                        const int col0 = tile.col0 + c0;
-#pragma unroll
-                        for (int j = 0; j < 64; ++j) {
-                            if (j < tn) {
-                                const int64_t gc = col0 + j;
-                                C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] =
-                                    __uint_as_float(v[j]);
-                            }
-                        }
-                    }
                 } else {
-                    double* C = (double*)g.C;
+                    // FP32 (OUT_SPLIT 2) or FP64 output, column-major (transC = 0) or row-major;
+                    // multi-RHS tiles: tile row R*i + k is row i of vector k (at k * vstride)
                     if (rl < tile.tm) {
-                        const int64_t gr = tile.row0 + rl;
+                        int64_t gr = tile.row0 + rl, base = tile.c_off;
+                        if (MULTI) {
+                            const int64_t i = gr / tile.nrhs;
+                            base += (gr - i * tile.nrhs) * g.vstride;
+                            gr = i;
+                        }
                         const int col0 = tile.col0 + c0;
 #pragma unroll
                         for (int j = 0; j < 64; ++j) {
                             if (j < tn) {
                                 const int64_t gc = col0 + j;
-                                C[tile.c_off + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc))] =
-                                    f32_to_f64(__uint_as_float(v[j]));
+                                const int64_t e = base + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc));
+                                if (OUT_SPLIT == 2) ((float*)g.C)[e] = __uint_as_float(v[j]);
+                                else ((double*)g.C)[e] = f32_to_f64(__uint_as_float(v[j]));
                             }
                         }
                     }
@@ -397,20 +398,28 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
 }
 
 cudaError_t umma_init() {
-    cudaError_t e = cudaFuncSetAttribute(gg_umma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(gg_umma_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(gg_umma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, um::SMEM_BYTES);
+    cudaError_t e;
+#define UMMA_ATTR(O, M)                                                                                     \
+    if ((e = cudaFuncSetAttribute(gg_umma_kernel<O, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                                  um::SMEM_BYTES)) != cudaSuccess)                                          \
+        return e;
+    UMMA_ATTR(0, false) UMMA_ATTR(1, false) UMMA_ATTR(2, false) UMMA_ATTR(0, true) UMMA_ATTR(1, true)
+#undef UMMA_ATTR
+    return cudaSuccess;
 }
 
-cudaError_t launch_gg_umma(int out_mode, const GGArgs& a, const TmaMaps& maps, cudaStream_t st) {
+// multi: the plan's tiles interleave nrhs right-hand sides (separate instances, so
+// that the single-vector epilogues keep their register budget)
+cudaError_t launch_gg_umma(int out_mode, bool multi, const GGArgs& a, const TmaMaps& maps, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
     if (!a.steps || !a.cta_tiles || a.ncta <= 0 || !a.C) return cudaErrorInvalidValue;
     if (out_mode == 1 && !a.transC) return cudaErrorInvalidValue;   // the staged epilogue writes panel rows
-    if (out_mode == 1) gg_umma_kernel<1><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-    else if (out_mode == 2) gg_umma_kernel<2><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-    else if (out_mode == 0) gg_umma_kernel<0><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    if (multi && (out_mode == 2 || (out_mode == 0 && a.vstride <= 0))) return cudaErrorInvalidValue;
+    if (out_mode == 1 && !multi) gg_umma_kernel<1, false><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 1) gg_umma_kernel<1, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 2) gg_umma_kernel<2, false><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 0 && !multi) gg_umma_kernel<0, false><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 0) gg_umma_kernel<0, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
