@@ -88,3 +88,21 @@ def test_spectral_bounds_and_chebyshev_moments(gpu_ctx):
         # split precision: each moment within 1e-4 of the FP64 one (relative to mu_0)
         assert np.max(np.abs(mus[k] - mu64[k])) < 1e-4 * scale, np.max(np.abs(mus[k] - mu64[k]))
     H.close()
+
+
+def test_hxv_multi_su2_pivot(gpu_ctx):
+    """multi-RHS on an SU(2)xU(1) two-site pivot (CG prefactors in the chain scalars)"""
+    from vmps_gb300 import models
+    from vmps_gb300.mps import RandomMPS, two_site_layout
+    from vmps_gb300.workloads import build_envs
+    m = models.hubbard_su2xu1_lattice(8, models.cylinder_bonds(4, 2), U=8.0)
+    mps = RandomMPS(m, (1, 8), 48, seed=21).canonicalize(3, 4)
+    Lenv, Renv = build_envs(gpu_ctx, m, mps, 3, 4)
+    V, _ = two_site_layout(m.sym, m.qloc, m.qloc, mps.dims[3], mps.dims[5], m.sym.nq)
+    H = PivotMatrix2(gpu_ctx, m.sym, Lenv, Renv, m.W[3], m.W[4], V)
+    X = np.random.default_rng(5).standard_normal((9, H.dim))
+    ms = H.apply_multi(X, "bf16x3")
+    for k in range(9):
+        assert np.array_equal(ms[k], H.apply(X[k], "bf16x3")), k
+        assert rel_err(ms[k], H.apply(X[k], "fp64")) < 2e-4
+    H.close()
