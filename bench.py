@@ -492,8 +492,8 @@ def main():
     energy = None
     if not args.no_energy and rank == 0:
         # Lanczos ground state of this pivot from the same start vector: a tight
-        # FP64 reference, then FP64 and split precision (+ Krylov-space
-        # correction and closing FP64 steps) at the sweep tolerances
+        # FP64 reference, then FP64 and split precision (+ refinement rounds:
+        # FP64 residual, split Lanczos from it) at the sweep tolerances
         keys = ("iterations", "refine_iterations", "hxv_split", "hxv_fp64", "residual", "ms_total", "ms_wait")
         e_ref, _, s_ref = H.lanczos(v0, "fp64", max_iter=300, tol_eigval=1e-14, tol_state=1e-9)
         e64, _, s64 = H.lanczos(v0, "fp64", max_iter=300, tol_eigval=1e-10, tol_state=1e-6)

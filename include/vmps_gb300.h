@@ -195,23 +195,26 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
  * precision VMPS_PREC_BF16X3 first applies FP64 HxV once to the start vector: if its
  * residual is below 1e-5 of its energy (a converged neighbourhood the split
  * operator cannot resolve) the solve continues as FP64 Lanczos.  Otherwise it runs
- * the Krylov phase with split-precision HxV, then corrects the Ritz vector with one
- * FP64 HxV: its FP64 residual, projected on the split Krylov space, drives the
- * Jacobi-Davidson correction equation solved in that space; closing FP64 Lanczos
- * steps (at most refine_iters - 1) start from the corrected vector.  refine_iters
- * counts the FP64 HxVs of that refinement (the probe is one more).
+ * the Krylov phase with split-precision HxV and refines its Ritz vector x in
+ * rounds: one FP64 HxV gives x's Rayleigh quotient E and residual r = Hx - Ex;
+ * a split-precision Lanczos run from the pair (x, r/|r|), whose first tridiagonal
+ * row (E, |r|) is FP64-exact, solves the correction equation and gives the next x.
+ * It stops when |r| <= tol_state and |r|^2 / gap <= tol_eigval |E| (gap from the
+ * last run's Ritz values); a round that does not halve |r| hands the rest of the
+ * budget to FP64 Lanczos steps.  refine_iters counts the FP64 HxVs after the
+ * Krylov phase (the probe is one more).
  * Krylov vectors, dots and the tridiagonal solve are FP64 throughout.  v (compact
  * layout) is the start vector on entry and the ground state on exit.
  * max_iter and refine_iters are below 1024.                                     */
 typedef struct {
     int32_t iterations;        /* Krylov steps in the first phase            */
-    int32_t refine_iterations; /* closing FP64 Lanczos steps                  */
+    int32_t refine_iterations; /* refinement rounds (+ closing FP64 steps)    */
     int32_t hxv_fp64;
     int32_t hxv_split;
     double  energy_first;      /* eigenvalue after the first phase            */
-    double  residual;          /* |beta_m y_m| of the last Lanczos phase: the
-                                  residual ||H v - E v|| of the returned vector
-                                  for that phase's operator (FP64 when refined) */
+    double  residual;          /* ||H v - E v|| of the returned vector: the
+                                  FP64 residual when refined, else |beta_m y_m|
+                                  of the Lanczos run for its operator           */
     double  ms_total;
     double  ms_wait;           /* host time blocked on the device's iterations */
     double  ms_host;           /* host time in the tridiagonal solves          */

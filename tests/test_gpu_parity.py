@@ -220,15 +220,24 @@ def test_lanczos_energy(gpu_ctx, case):
     assert abs(e64 - e_ref) < 1e-10 * abs(e_ref), (e64, e_ref, st64)
     es, vs, sts = H.lanczos(v0, "bf16x3", max_iter=300, tol_eigval=1e-9, tol_state=1e-5, refine_iters=30)
     assert abs(es - e_ref) < 1e-10 * abs(e_ref), (es, e_ref, sts)
-    assert sts["hxv_split"] > 0 and sts["refine_iterations"] > 0
+    # the probe and the FP64 residual of the split Ritz vector at least
+    assert sts["hxv_split"] > 0 and sts["hxv_fp64"] >= 2
+    # a state tolerance below the split operator's noise takes refinement rounds
+    # (split runs from the FP64 residual, one FP64 HxV each)
+    et, vt, stt = H.lanczos(v0, "bf16x3", max_iter=300, tol_eigval=1e-12, tol_state=1e-9, refine_iters=8)
+    assert abs(et - e_ref) < 1e-10 * abs(e_ref), (et, e_ref, stt)
+    assert stt["refine_iterations"] >= 1 and stt["residual"] <= 1e-9 and stt["hxv_fp64"] <= 1 + 8, stt
+    true_res = np.linalg.norm(H.apply(vt / np.linalg.norm(vt), "fp64") - et * vt / np.linalg.norm(vt))
+    assert true_res <= 2e-9, (true_res, stt)
 
 
 def test_lanczos_residual_estimate_and_determinism(gpu_ctx):
     """The device Lanczos reports |beta_m y_m| as the residual: it equals the
     explicit FP64 residual ||H v - E v|| of the returned vector.  Its
     reductions are deterministic, so two runs agree bit for bit.  The split
-    run with the Krylov-space correction reaches the FP64 energy within
-    1e-10 relative using at most refine_iters FP64 HxVs after the probe.
+    run with its refinement rounds reaches the FP64 energy within 1e-10
+    relative using at most refine_iters FP64 HxVs after the probe, and reports
+    the FP64 residual of the returned vector.
     From a start vector that is already an eigenvector the split run is the
     FP64 run."""
     model, mps, Lenv, Renv, W, V = pivot1_case("hubb", L=10, D=32, site=4, seed=41)

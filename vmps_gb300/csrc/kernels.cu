@@ -220,40 +220,68 @@ __global__ void prep_kernel(const PrepBlock* __restrict__ pbs, int nb, const dou
 }
 
 // column pieces of a column-major FP64 or FP32 source into panels: column c of
-// the piece is panel row c, its element r is K index r; four loads in flight
+// the piece is panel row c, its element r is K index r.  A thread converts four
+// consecutive elements of one column (one 16-byte load per four floats, two per
+// four doubles) into four hi and four lo values of the same 32-element panel
+// group (two 8-byte stores).  Columns start at multiples of 8 elements in the
+// padded vector layout, so the group's loads stay inside the column's padded
+// extent; pieces whose offsets or strides break that alignment (or the stores')
+// take the element-wise path.
 __device__ __forceinline__ float piece_value(double x, bool unit, double scale) {
     return f64_to_f32_rn(unit ? x : scale * x);
 }
 __device__ __forceinline__ float piece_value(float x, bool unit, double scale) {
     return unit ? x : f64_to_f32_rn(scale) * x;
 }
+__device__ __forceinline__ void piece_load4(const float* p, float (&x)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ void piece_load4(const double* p, double (&x)[4]) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y;
+}
+__device__ __forceinline__ uint32_t bf16_pair(__nv_bfloat16 a, __nv_bfloat16 b) {
+    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
 template <typename T>
 __global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np, const T* __restrict__ src,
                                    __nv_bfloat16* __restrict__ dst) {
     for (int b = blockIdx.x; b < np; b += gridDim.x) {
         const PanelPiece pc = pieces[b];
-        const int rows = pc.rows, n = pc.rows * pc.cols;
+        const int rows = pc.rows, nr4 = (rows + 3) >> 2, ng = nr4 * pc.cols;
         const T* s = src + pc.src_off;
         __nv_bfloat16* d = dst + pc.dst_off;
         const bool unit = pc.scale == 1.0;
-        for (int e0 = threadIdx.x; e0 < n; e0 += 4 * blockDim.x) {
+        const bool vload = ((reinterpret_cast<uintptr_t>(s) | (uintptr_t)pc.src_ld * sizeof(T)) & 15) == 0 &&
+                           pc.src_ld >= 4 * nr4;
+        const bool vstore = ((reinterpret_cast<uintptr_t>(d) | (uintptr_t)pc.dst_pitch * 2) & 7) == 0;
+        for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+            const int c = g / nr4, r0 = (g - c * nr4) << 2;
+            const T* sc = s + (int64_t)c * pc.src_ld + r0;
             T x[4];
+            if (vload) {
+                piece_load4(sc, x);
+            } else {
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int e = e0 + u * blockDim.x;
-                if (e < n) {
-                    const int c = e / rows, r = e - c * rows;
-                    x[u] = s[r + c * pc.src_ld];
-                } else {
-                    x[u] = T(0);
-                }
+                for (int q = 0; q < 4; ++q) x[q] = r0 + q < rows ? sc[q] : T(0);
             }
+            __nv_bfloat16* row = d + (int64_t)c * pc.dst_pitch;
+            if (vstore && r0 + 4 <= rows) {
+                __nv_bfloat16 h[4], l[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int e = e0 + u * blockDim.x;
-                if (e >= n) break;
-                const int c = e / rows, r = e - c * rows;
-                split_store(d + (int64_t)c * pc.dst_pitch, r, piece_value(x[u], unit, pc.scale));
+                for (int q = 0; q < 4; ++q) {
+                    const float v = piece_value(x[q], unit, pc.scale);
+                    h[q] = __float2bfloat16_rn(v);
+                    l[q] = __float2bfloat16_rn(v - __bfloat162float(h[q]));
+                }
+                const int p = panel_pos(r0);   // r0 % 4 == 0: the four stay in one 32-group
+                *reinterpret_cast<uint2*>(row + p) = make_uint2(bf16_pair(h[0], h[1]), bf16_pair(h[2], h[3]));
+                *reinterpret_cast<uint2*>(row + p + 32) = make_uint2(bf16_pair(l[0], l[1]), bf16_pair(l[2], l[3]));
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (r0 + q < rows) split_store(row, r0 + q, piece_value(x[q], unit, pc.scale));
             }
         }
     }

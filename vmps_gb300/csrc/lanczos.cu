@@ -326,7 +326,7 @@ __global__ void lz_next_kernel(LzArgs a) {
 __device__ __forceinline__ double lz_f64(double x) { return x; }
 __device__ __forceinline__ double lz_f64(float x) { return f32_to_f64(x); }   // exact, integer pipe
 
-// y[e] = sum_{i < m} c[i] K_i[e] in FP64 (Ritz vectors and corrections)
+// y[e] = sum_{i < m} c[i] K_i[e] in FP64 (Ritz vectors)
 template <typename V>
 __global__ void lz_combine_kernel(const V* __restrict__ K, int64_t ld, int m, int64_t n,
                                   const double* __restrict__ c, double* __restrict__ y) {
@@ -335,38 +335,6 @@ __global__ void lz_combine_kernel(const V* __restrict__ K, int64_t ld, int m, in
         for (int i = 0; i < m; ++i) s = fma(c[i], lz_f64(K[(int64_t)i * ld + e]), s);
         y[e] = s;
     }
-}
-
-__device__ __forceinline__ void lz_stage(double* d, double x) { *d = x; }
-__device__ __forceinline__ void lz_stage(float* d, double x) { *d = f64_to_f32_rn(x); }
-
-// out[i] = <K_i, r> for i < m, deterministic (partials per chunk, last block
-// sums); r is FP64 and is rounded to the basis type when staged
-template <typename V, int E>
-__global__ void __launch_bounds__(kLzThreads) lz_mdot_kernel(const V* __restrict__ K, int64_t ld, int m, int64_t n,
-                                                              const double* __restrict__ r,
-                                                              double* __restrict__ part, int nchunk,
-                                                              unsigned* counter, double* __restrict__ out) {
-    __shared__ __align__(16) V rsh[E * kLzThreads];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t cb = (int64_t)blockIdx.x * (E * kLzThreads);
-    const int len = (int)(n - cb < E * kLzThreads ? n - cb : E * kLzThreads);
-#pragma unroll
-    for (int u = 0; u < E; ++u) {
-        const int x = threadIdx.x + u * kLzThreads;
-        lz_stage(rsh + x, x < len ? r[cb + x] : 0.0);
-    }
-    __syncthreads();
-    for (int i = warp; i < m; i += kLzWarps) {
-        const double t = lz_chunk_dot<V, E>(K + (int64_t)i * ld + cb, rsh, len, lane);
-        if (lane == 0) part[(int64_t)i * nchunk + blockIdx.x] = t;
-    }
-    if (!lz_last_block(counter)) return;
-    for (int i = warp; i < m; i += kLzWarps) {
-        const double t = lz_row_sum(part, i, nchunk, lane);
-        if (lane == 0) out[i] = t;
-    }
-    if (threadIdx.x == 0) *counter = 0;
 }
 
 __global__ void lz_to_f32_kernel(const double* __restrict__ x, float* __restrict__ y, int64_t n) {
@@ -496,19 +464,6 @@ cudaError_t launch_lz_combine(const void* K, int fp32, int64_t ld, int m, int64_
     return cudaGetLastError();
 }
 
-cudaError_t launch_lz_mdot(const void* K, int fp32, int64_t ld, int m, int64_t n, const double* r, double* part,
-                           const LzShape& sh, unsigned* counter, double* out, cudaStream_t st) {
-    if (m < 1 || m > kLzMaxIter || n <= 0 || !K || !r || !part || !counter || !out) return cudaErrorInvalidValue;
-    if ((int64_t)sh.nchunk * sh.chunk < n) return cudaErrorInvalidValue;
-#define LZ_CALL(EE)                                                                                        \
-    if (fp32) lz_mdot_kernel<float, EE><<<sh.nchunk, kLzThreads, 0, st>>>((const float*)K, ld, m, n, r, part, \
-                                                                          sh.nchunk, counter, out);         \
-    else lz_mdot_kernel<double, EE><<<sh.nchunk, kLzThreads, 0, st>>>((const double*)K, ld, m, n, r, part,   \
-                                                                        sh.nchunk, counter, out);
-    LZ_DISPATCH(sh.per_thread, LZ_CALL)
-#undef LZ_CALL
-    return cudaGetLastError();
-}
 #undef LZ_DISPATCH
 
 cudaError_t launch_lz_to_f32(const double* x, float* y, int64_t n, cudaStream_t st) {

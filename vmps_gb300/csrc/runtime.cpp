@@ -1322,6 +1322,26 @@ void tridiag_lowest(const std::vector<double>& a, const std::vector<double>& b, 
     if (rq >= lo - 1e-9 * scale && rq <= hi + 1e-9 * scale) theta = rq;
 }
 
+// second-lowest eigenvalue of the tridiagonal (Sturm bisection to 1e-9 of the
+// spectral scale); +inf for a 1 x 1 matrix
+double tridiag_second(const std::vector<double>& a, const std::vector<double>& b) {
+    const size_t n = a.size();
+    if (n < 2) return HUGE_VAL;
+    double lo = a[0], hi = a[0];
+    for (size_t i = 0; i < n; ++i) {
+        const double r = (i ? std::abs(b[i - 1]) : 0.0) + (i + 1 < n ? std::abs(b[i]) : 0.0);
+        lo = std::min(lo, a[i] - r);
+        hi = std::max(hi, a[i] + r);
+    }
+    const double scale = std::max(std::abs(lo), std::abs(hi)) + 1e-300;
+    for (int it = 0; it < 80 && hi - lo > 1e-9 * scale; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (sturm_count_below(a, b, mid) >= 2) hi = mid; else lo = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
 double dev_dot(vmps_pivot* p, const double* x, const double* y, int64_t n) {
     CK(launch_dot(x, y, n, p->part.as<double>(), p->scal.as<double>(), p->st()));
     double r;
@@ -1387,9 +1407,11 @@ struct LzResult {
 
 // probe_rel > 0: iteration 0 runs alone first, and the run stops after it
 // (aborted = true) when beta_0 > probe_rel * max(1, |alpha_0|), i.e. when the
-// start vector's residual is above that fraction of its energy
+// start vector's residual is above that fraction of its energy.
+// first_row = {alpha_0, beta_0}: the caller has set K_0, K_1 (and q = K_1) and
+// knows the first row of the tridiagonal exactly; the run starts at iteration 1.
 LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval, double tol_state,
-                double probe_rel = 0) {
+                double probe_rel = 0, const double* first_row = nullptr) {
     cudaStream_t st = p->st();
     DevPlan& dp = get_plan(p, prec);
     const bool f32 = prec != VMPS_PREC_FP64;   // split-precision runs keep FP32 Krylov vectors
@@ -1408,7 +1430,12 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
     a.n = W.n;
     a.kmax = W.cap;
     a.nchunk = W.sh.nchunk;
+    const int j0 = first_row ? 1 : 0;
     CK(cudaMemsetAsync(W.ctl(), 0, 8 * sizeof(unsigned), st));
+    if (j0) {
+        static const unsigned kStartOne = 1;
+        CK(cudaMemcpyAsync(W.ctl(), &kStartOne, sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    }
     Operands ops;
     ops.X = p->dL.as<double>();
     ops.Z = p->dR.as<double>();
@@ -1447,17 +1474,21 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
     volatile const double* hab = W.host;
     double theta = 0, theta_prev = 1e300, res = 0;
     std::vector<double> y;
+    if (j0) {
+        r.alpha.push_back(first_row[0]);
+        r.beta.push_back(first_row[1]);
+    }
     auto launch = [&]() {
         CK(cudaGraphLaunch(ge, st));
         CK(cudaEventRecord(W.ev[r.launched & 1], st));
         ++r.launched;
     };
     launch();
-    int j = 0;
-    for (j = 0; j < kmax; ++j) {
-        if (r.launched < kmax && !(probe_rel > 0 && j == 0)) launch();
+    int j = j0;
+    for (j = j0; j < kmax; ++j) {
+        if (r.launched < kmax - j0 && !(probe_rel > 0 && j == 0)) launch();
         const auto tw = std::chrono::steady_clock::now();
-        CK(cudaEventSynchronize(W.ev[j & 1]));
+        CK(cudaEventSynchronize(W.ev[(j - j0) & 1]));
         const auto th = std::chrono::steady_clock::now();
         r.ms_wait += std::chrono::duration<double, std::milli>(th - tw).count();
         struct HostTimer {
@@ -1503,63 +1534,29 @@ void lz_ritz(vmps_pivot* p, LzWork& W, const std::vector<double>& y, double* x, 
     CK(launch_scale(1.0 / nx, x, W.n, st));
 }
 
-// Correction of a Ritz vector y (unit norm, lowest eigenvector of the
-// tridiagonal T = tridiag(beta, alpha, beta)) inside the Krylov space: the
-// Jacobi-Davidson correction equation restricted to span(K),
-//     P (T - th) P z = -P g,   P = 1 - y y^T,   z orthogonal to y,
-// with g = K^T r the projection of the residual r = H x - th x.  Solved by
-// conjugate gradients on the m-dimensional system (positive definite on y's
-// complement while th lies below the second Ritz value; the iteration stops
-// at the first direction of non-positive curvature).  `model` returns the
-// second-order energy change 2 g.z + z.(T - th) z of the step.
-std::vector<double> krylov_correction(const std::vector<double>& a, const std::vector<double>& b, double th,
-                                      const std::vector<double>& y, const std::vector<double>& g, double* model) {
-    const size_t m = a.size();
-    auto Tv = [&](const std::vector<double>& v, std::vector<double>& out) {
-        for (size_t i = 0; i < m; ++i) {
-            double s = (a[i] - th) * v[i];
-            if (i > 0) s += b[i - 1] * v[i - 1];
-            if (i + 1 < m) s += b[i] * v[i + 1];
-            out[i] = s;
-        }
-    };
-    auto proj = [&](std::vector<double>& v) {
-        double d = 0;
-        for (size_t i = 0; i < m; ++i) d += y[i] * v[i];
-        for (size_t i = 0; i < m; ++i) v[i] -= d * y[i];
-    };
-    auto dot = [&](const std::vector<double>& u, const std::vector<double>& v) {
-        double s = 0;
-        for (size_t i = 0; i < m; ++i) s += u[i] * v[i];
-        return s;
-    };
-    std::vector<double> z(m, 0.0), r(g), p, Ap(m);
-    for (double& v : r) v = -v;
-    proj(r);
-    p = r;
-    double rr = dot(r, r);
-    const double r0 = std::sqrt(rr);
-    for (size_t it = 0; it < 2 * m + 10 && rr > 0 && std::sqrt(rr) > 1e-14 * r0; ++it) {
-        Tv(p, Ap);
-        proj(Ap);
-        const double pAp = dot(p, Ap);
-        if (!(pAp > 0)) break;
-        const double al = rr / pAp;
-        for (size_t i = 0; i < m; ++i) {
-            z[i] += al * p[i];
-            r[i] -= al * Ap[i];
-        }
-        proj(r);
-        const double rr2 = dot(r, r);
-        for (size_t i = 0; i < m; ++i) p[i] = r[i] + (rr2 / rr) * p[i];
-        rr = rr2;
+// Ritz vector of a run started from first_row: out = y_0 x0 + sum_{i>=1} y_i K_i,
+// normalised.  K_0 of that run is the FP32 copy of x0; the FP64 x0 itself enters
+// here so that the result keeps FP64 accuracy along it.
+void lz_ritz_mixed(vmps_pivot* p, LzWork& W, const std::vector<double>& y, const double* x0, double* out) {
+    cudaStream_t st = p->st();
+    const int m = (int)y.size();
+    if (m < 1) throw std::logic_error("empty Ritz coefficients");
+    if (m > 1) {
+        CK(cudaMemcpyAsync(W.g(), y.data() + 1, (size_t)(m - 1) * 8, cudaMemcpyHostToDevice, st));
+        CK(launch_lz_combine(W.K32.as<float>() + W.ld, 1, W.ld, m - 1, W.n, W.g(), out, st));
+    } else {
+        CK(cudaMemsetAsync(out, 0, (size_t)W.n * 8, st));
     }
-    proj(z);
-    std::vector<double> Tz(m);
-    Tv(z, Tz);
-    *model = 2 * dot(g, z) + dot(z, Tz);
-    return z;
+    CK(launch_axpy(y[0], x0, out, W.n, st));
+    const double nx = std::sqrt(dev_dot(p, out, out, W.n));
+    if (!(nx > 0) || !std::isfinite(nx)) throw CudaFail("Ritz vector is zero or not finite");
+    CK(launch_scale(1.0 / nx, out, W.n, st));
 }
+
+// Model residual, relative to the residual a refinement round starts from, at
+// which its split-precision run stops: below the reduction the split operator's
+// noise allows in one round.
+constexpr double kRoundReduce = 1e-3;
 }  // namespace
 
 extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_iter, double tol_eigval,
@@ -1628,35 +1625,73 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
         res = r1.res;
         lz_ritz(p, W, r1.y, x, f32);
         if (refine) {
-            // FP64 residual of the split-precision Ritz vector, corrected inside
-            // the split Krylov space where its error lies (the low-lying part of
-            // the spectrum), then closing FP64 Lanczos steps from the result
+            // Refinement rounds.  Each round knows x (FP64, unit norm), its FP64
+            // Rayleigh quotient th and residual r = H x - th x.  A split-precision
+            // Lanczos run starts from the pair K_0 = x, K_1 = r / |r|: the first row
+            // of its tridiagonal (th, |r|) is FP64-exact, the rows after it come
+            // from split HxVs.  Its Ritz vector solves the correction equation for
+            // x to the split operator's noise, which enters only through the
+            // correction (second order); one FP64 HxV then gives the new x's
+            // Rayleigh quotient and residual.  A round that does not halve the
+            // residual hands the rest of the budget to FP64 Lanczos steps.
             double* u = W.u.as<double>();
-            pivot_hxv_dev(p, VMPS_PREC_FP64, x, u);
-            s.hxv_fp64++;
-            const double th0 = dev_dot(p, x, u, n);
-            CK(launch_axpy(-th0, x, u, n, st));
-            CK(launch_lz_mdot(W.K32.p, 1, W.ld, r1.m, n, u, W.part.as<double>(), W.sh, W.ctl() + 4, W.g(), st));
-            std::vector<double> g(r1.m);
-            CK(cudaMemcpyAsync(g.data(), W.g(), (size_t)r1.m * 8, cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            double model = 0;
-            std::vector<double> z = krylov_correction(r1.alpha, r1.beta, th0, r1.y, g, &model);
-            double zn = 0;
-            for (double t : z) zn += t * t;
-            if (model < 0 && std::sqrt(zn) < 0.5) {
-                std::vector<double> yz(r1.y);
-                for (size_t i = 0; i < yz.size(); ++i) yz[i] += z[i];
-                lz_ritz(p, W, yz, x, true);
+            double* xn = W.w.as<double>();   // a round's candidate (the FP64 w buffer is idle in split runs)
+            int budget = refine_iters;        // FP64 HxVs of the refinement
+            auto residual = [&](const double* xv, double& th, double& rn) {
+                pivot_hxv_dev(p, VMPS_PREC_FP64, xv, u);
+                s.hxv_fp64++;
+                --budget;
+                th = dev_dot(p, xv, u, n);
+                CK(launch_axpy(-th, xv, u, n, st));
+                rn = std::sqrt(dev_dot(p, u, u, n));
+            };
+            // converged: residual within tol_state, and the energy error bound
+            // |r|^2 / gap (gap = second Ritz value - first, of the last run's
+            // tridiagonal) within tol_eigval
+            auto converged = [&](double th, double rn, double gap) {
+                return rn <= tol_state && rn * rn <= tol_eigval * std::max(1.0, std::abs(th)) * gap;
+            };
+            double th = 0, rn = 0;
+            residual(x, th, rn);
+            double gap = std::max(0.0, tridiag_second(r1.alpha, r1.beta) - r1.theta);
+            bool stalled = false;
+            float* K32 = W.K32.as<float>();
+            while (!converged(th, rn, gap) && budget > 0 && rn > 0) {
+                CK(launch_scale(1.0 / rn, u, n, st));
+                CK(launch_lz_to_f32(x, K32, W.ld, st));
+                CK(launch_lz_to_f32(u, K32 + W.ld, W.ld, st));
+                CK(cudaMemcpyAsync(W.q32.p, K32 + W.ld, (size_t)W.ld * 4, cudaMemcpyDeviceToDevice, st));
+                const double row0[2] = {th, rn};
+                LzResult ri = lz_run(p, W, prec, std::max(2, max_iter), HUGE_VAL,
+                                     std::max(0.1 * tol_state, kRoundReduce * rn), 0, row0);
+                account(ri, prec);
+                lz_ritz_mixed(p, W, ri.y, x, xn);
+                double th2 = 0, rn2 = 0;
+                residual(xn, th2, rn2);
+                s.refine_iterations++;
+                if (!(rn2 < rn)) {
+                    stalled = true;
+                    break;
+                }
+                CK(cudaMemcpyAsync(x, xn, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+                stalled = rn2 > 0.5 * rn;
+                th = th2;
+                rn = rn2;
+                gap = std::max(0.0, tridiag_second(ri.alpha, ri.beta) - ri.theta);
+                if (stalled) break;
             }
-            CK(cudaMemcpyAsync(K0, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-            CK(cudaMemcpyAsync(W.q.p, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-            LzResult r2 = lz_run(p, W, VMPS_PREC_FP64, std::max(1, refine_iters - 1), tol_eigval, tol_state);
-            account(r2, VMPS_PREC_FP64);
-            s.refine_iterations = r2.m;
-            lz_ritz(p, W, r2.y, x, false);
-            e = r2.theta;
-            res = r2.res;
+            e = th;
+            res = rn;
+            if (stalled && budget > 0) {
+                CK(cudaMemcpyAsync(K0, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+                CK(cudaMemcpyAsync(W.q.p, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+                LzResult r2 = lz_run(p, W, VMPS_PREC_FP64, std::max(1, budget), tol_eigval, tol_state);
+                account(r2, VMPS_PREC_FP64);
+                s.refine_iterations += r2.m;
+                lz_ritz(p, W, r2.y, x, false);
+                e = r2.theta;
+                res = r2.res;
+            }
         }
     }
     s.residual = res;
