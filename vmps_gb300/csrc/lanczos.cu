@@ -35,6 +35,7 @@ namespace vmps {
 
 namespace {
 constexpr int kLzThreads = 256, kLzWarps = kLzThreads / 32;
+constexpr int kLzCoefBlocks = 152;   // rows of d summed in parallel (one per block, strided)
 
 __device__ __forceinline__ double lz_warp_sum(double s) {
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -58,6 +59,25 @@ __device__ __forceinline__ double lz_row_sum(const double* part, int row, int nc
     double s = 0;
     for (int c = lane; c < nchunk; c += 32) s += __ldcg(part + (int64_t)row * nchunk + c);
     return lz_warp_sum(s);
+}
+
+// the same sum by the whole block (every thread returns it): a few independent
+// loads per thread instead of nchunk / 32 dependent rounds of one warp, which
+// left a single block reducing long after the others had finished
+__device__ __forceinline__ double lz_block_row_sum(const double* part, int row, int nchunk) {
+    __shared__ double red[kLzWarps];
+    const double* p = part + (int64_t)row * nchunk;
+    double s = 0;
+#pragma unroll 8
+    for (int c = threadIdx.x; c < nchunk; c += kLzThreads) s += __ldcg(p + c);
+    s = lz_warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double t = 0;
+#pragma unroll
+    for (int q = 0; q < kLzWarps; ++q) t += red[q];
+    __syncthreads();   // red is reused by the next call
+    return t;
 }
 
 // 16-byte groups of vector elements (float4 / double2): the step kernels issue
@@ -146,11 +166,12 @@ __global__ void __launch_bounds__(kLzThreads) lz_local_kernel(LzArgs a) {
         a.part[(int64_t)threadIdx.x * a.nchunk + blockIdx.x] = t;
     }
     if (!lz_last_block(a.ctl + 1)) return;
-    if (warp < 2) {
-        const double t = lz_row_sum(a.part, warp, a.nchunk, lane);
-        if (lane == 0) a.cl[warp] = t;
+    const double t0 = lz_block_row_sum(a.part, 0, a.nchunk), t1 = lz_block_row_sum(a.part, 1, a.nchunk);
+    if (threadIdx.x == 0) {
+        a.cl[0] = t0;
+        a.cl[1] = t1;
+        a.ctl[1] = 0;
     }
-    if (threadIdx.x == 0) a.ctl[1] = 0;
 }
 
 template <typename V, int E>
@@ -202,17 +223,21 @@ __global__ void __launch_bounds__(kLzThreads) lz_proj_kernel(LzArgs a) {
         }
     }
     __syncthreads();
-    // one warp per basis row: d_i partial over this chunk
+    // one warp per basis row: d_i partial over this chunk (summed by lz_coef)
     for (int i = warp; i <= j; i += kLzWarps) {
         const double t = lz_chunk_dot<V, E>(K + (int64_t)i * a.ld + cb, wsh, len, lane);
         if (lane == 0) a.part[(int64_t)i * a.nchunk + blockIdx.x] = t;
     }
-    if (!lz_last_block(a.ctl + 2)) return;
-    for (int i = warp; i <= j; i += kLzWarps) {
-        const double t = lz_row_sum(a.part, i, a.nchunk, lane);
-        if (lane == 0) a.coef[i] = t;
+}
+
+// d_i = sum over chunks of lz_proj's partials, one block per basis row
+__global__ void __launch_bounds__(kLzThreads) lz_coef_kernel(LzArgs a) {
+    const int j = (int)a.ctl[0];
+    if (j >= a.kmax) return;
+    for (int i = blockIdx.x; i <= j; i += gridDim.x) {
+        const double t = lz_block_row_sum(a.part, i, a.nchunk);
+        if (threadIdx.x == 0) a.coef[i] = t;
     }
-    if (threadIdx.x == 0) a.ctl[2] = 0;
 }
 
 template <typename V, int E>
@@ -289,22 +314,20 @@ __global__ void __launch_bounds__(kLzThreads) lz_orth_kernel(LzArgs a) {
         a.part[blockIdx.x] = t;
     }
     if (!lz_last_block(a.ctl + 3)) return;
-    if (warp == 0) {
-        const double ww = lz_row_sum(a.part, 0, a.nchunk, lane);
-        if (lane == 0) {
-            const double alpha = a.cl[1] + a.coef[j];
-            const double beta = sqrt(ww);
-            a.ab[j] = alpha;
-            a.ab[a.kmax + j] = beta;
-            a.ab[2 * a.kmax + j] = beta > 1e-300 ? 1.0 / beta : 0.0;
-            if (a.host_ab) {
-                volatile double* h = a.host_ab;
-                h[j] = alpha;
-                h[a.kmax + j] = beta;
-            }
-            a.ctl[3] = 0;
-            a.ctl[0] = (unsigned)(j + 1);
+    const double ww = lz_block_row_sum(a.part, 0, a.nchunk);
+    if (threadIdx.x == 0) {
+        const double alpha = a.cl[1] + a.coef[j];
+        const double beta = sqrt(ww);
+        a.ab[j] = alpha;
+        a.ab[a.kmax + j] = beta;
+        a.ab[2 * a.kmax + j] = beta > 1e-300 ? 1.0 / beta : 0.0;
+        if (a.host_ab) {
+            volatile double* h = a.host_ab;
+            h[j] = alpha;
+            h[a.kmax + j] = beta;
         }
+        a.ctl[3] = 0;
+        a.ctl[0] = (unsigned)(j + 1);
     }
 }
 
@@ -439,6 +462,7 @@ static cudaError_t lz_step(const LzArgs& a, int per_thread, cudaStream_t st) {
 #define LZ_CALL(EE)                                                   \
     lz_local_kernel<V, EE><<<a.nchunk, kLzThreads, 0, st>>>(a);       \
     lz_proj_kernel<V, EE><<<a.nchunk, kLzThreads, 0, st>>>(a);        \
+    lz_coef_kernel<<<kLzCoefBlocks, kLzThreads, 0, st>>>(a);           \
     lz_orth_kernel<V, EE><<<a.nchunk, kLzThreads, 0, st>>>(a);
     LZ_DISPATCH(per_thread, LZ_CALL)
 #undef LZ_CALL
