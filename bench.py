@@ -188,7 +188,8 @@ def sweep_bench(ctx, args, with_cpu=True):
 
         def summary(r):
             return {"s_per_sweep": r["sweep_times"], "E": r["energies"], "hxv": r["hxv"],
-                    "timers_s": [{k: round(v, 4) for k, v in t.items()} for t in r["timers"]]}
+                    "timers_s": [{k: round(v, 4) for k, v in t.items()} for t in r["timers"]],
+                    "lanczos": r["solves"]}
 
         hub = {"tolerances": dict(refine_iters=10, **tol)}
         mps = copy.deepcopy(mps0)

@@ -231,6 +231,48 @@ int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* sym, const vmps_b
                            const vmps_blocks* A2, const double* a2, const vmps_blocks* V, double* v,
                            int64_t nprod, const int64_t* prods);
 
+/* ---- two-site split on the host cores ----------------------------------------------
+ * split_AA2 with Biped::truncateSVD (tensors/DmrgContractions.h:2461-2631,
+ * tensors/Biped.h:744-932), abelian QNs.  For every middle QN qmid the blocks of the
+ * two-site tensor V (leg = combined index s13 = (pair1[s13], pair3[s13])) form the
+ * sector matrix Psi[(s1, qin), (s3, qout)], qin + qloc1[s1] = qmid = qout - qloc3[s3],
+ * rows in (s1, sorted qin) order and columns in (s3, sorted qout) order.  Its singular
+ * values and the orthonormal factor of the sweep direction come from the eigensystem
+ * of the Gram matrix (Psi Psi^T for move_right, Psi^T Psi otherwise; LAPACK dsyevd).
+ * The dmax largest values over all sectors are kept (none at or below eps_svd times
+ * the largest; ties at the threshold in sector order), renormalised; move_right: A1 = U,
+ * A2 = S V^T, else A1 = U S, A2 = V^T.  A1 and A2 come in site-layout block order
+ * (for s, for qin in sorted order, qout = qin + qloc[s] when present), compact
+ * column-major data.  Sectors run on `threads` host threads (one LAPACK call each:
+ * the caller keeps that LAPACK single-threaded meanwhile).
+ * vmps_hostla_load binds the ILP64 LAPACK / BLAS (dsyevd, dsyrk, dgemm, optionally
+ * with a scipy_ prefix) of the shared library at `path` (numpy's bundled OpenBLAS).
+ * Results: vmps_split_info gives the counts, vmps_split_get copies out
+ * (qmid: nmid * nq, dmid: nmid; then A1's and A2's tables and data).              */
+typedef struct {
+    int32_t nq;
+    int32_t n1, n3, n13;                        /* local dims; combined dim        */
+    const int32_t* qloc1;                       /* [n1 * nq]                       */
+    const int32_t* qloc3;                       /* [n3 * nq]                       */
+    const int32_t* pair1;                       /* [n13]: s1 of combined index     */
+    const int32_t* pair3;                       /* [n13]: s3 of combined index     */
+    int32_t nin;  const int32_t* qin;  const int64_t* din;    /* left bond basis  */
+    int32_t nout; const int32_t* qout; const int64_t* dout;   /* right bond basis */
+    int64_t dmax;
+    double  eps_svd;
+    int32_t move_right;
+    int32_t threads;
+} vmps_split_args;
+typedef struct vmps_split_s vmps_split;
+int  vmps_hostla_load(const char* path);
+int  vmps_two_site_split(const vmps_split_args* args, const vmps_blocks* V, const double* v, vmps_split** out);
+int  vmps_split_info(const vmps_split* s, int* nmid, double* disc, int64_t* nblocks1, int64_t* size1,
+                     int64_t* nblocks2, int64_t* size2);
+int  vmps_split_get(const vmps_split* s, int32_t* qmid, int64_t* dmid,
+                    int32_t* leg1, int32_t* qin1, int32_t* qout1, int64_t* rows1, int64_t* cols1, double* a1,
+                    int32_t* leg2, int32_t* qin2, int32_t* qout2, int64_t* rows2, int64_t* cols2, double* a2);
+void vmps_split_destroy(vmps_split* s);
+
 /* ---- many right-hand sides --------------------------------------------------------
  * Vout_k = H Vin_k for k < nrhs (compact layouts, vector k at element k * dim).
  * Split precision runs all right-hand sides in one grouped HxV (one vector split,

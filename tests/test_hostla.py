@@ -1,0 +1,73 @@
+"""Native two-site split (vmps_two_site_split) against the numpy restatement of
+split_AA2 / Biped::truncateSVD (tensors/DmrgContractions.h:2461-2631,
+tensors/Biped.h:744-932): same middle bond basis, same block layout, the same
+two-site tensor after truncation, orthonormal factors.  Host code only."""
+import numpy as np
+import pytest
+
+from vmps_gb300 import models
+from vmps_gb300.hostla import SectorPool, native_lapack
+from vmps_gb300.mps import RandomMPS, contract_two_sites, split_two_site
+
+
+def _case(L, D, l, seed):
+    model = models.hubbard_u1xu1(L, t=1.0, U=4.0)
+    mps = RandomMPS(model, (L, 0), D, seed=seed, profile="gaussian", sigma=[2.5, 2.5]).canonicalize(l, l)
+    A1, A2 = mps.A[l], mps.A[l + 1]
+    din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
+    dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
+    V, comb = contract_two_sites(model.sym, A1, A2, model.qloc, model.qloc, model.sym.nq, return_basis=True)
+    return model, V, comb, din, dout
+
+
+def _product(A1, A2):
+    out = {}
+    for i in range(A1.n):
+        for j in range(A2.n):
+            if tuple(A1.qout[i]) == tuple(A2.qin[j]):
+                k = (int(A1.leg[i]), int(A2.leg[j]), tuple(A1.qin[i]), tuple(A2.qout[j]))
+                out[k] = out.get(k, 0) + A1.block(i) @ A2.block(j)
+    return out
+
+
+@pytest.mark.parametrize("move", ["right", "left"])
+@pytest.mark.parametrize("dmax", [24, 64])
+@pytest.mark.parametrize("threads", [1, 4])
+def test_native_split_matches_numpy(move, dmax, threads):
+    if not native_lapack():
+        pytest.skip("numpy's bundled OpenBLAS exports no ILP64 LAPACK")
+    model, V, comb, din, dout = _case(10, 64, 4, seed=5)
+    pool = SectorPool(threads)
+    try:
+        a = split_two_site(V, comb, model.qloc, model.qloc, din, dout, 2, dmax, move=move, pool=pool, native=False)
+        b = split_two_site(V, comb, model.qloc, model.qloc, din, dout, 2, dmax, move=move, pool=pool, native=True)
+    finally:
+        pool.close()
+    assert a[3] == b[3] and sum(b[3].values()) <= dmax
+    assert abs(a[2] - b[2]) < 1e-13
+    for X, Y in ((a[0], b[0]), (a[1], b[1])):
+        for f in ("leg", "qin", "qout", "rows", "cols", "offset"):
+            assert np.array_equal(getattr(X, f), getattr(Y, f)), f
+    pa, pb = _product(a[0], a[1]), _product(b[0], b[1])
+    assert pa.keys() == pb.keys()
+    assert max(np.abs(pa[k] - pb[k]).max() for k in pa) < 1e-12
+    # the orthonormal factor of the sweep direction
+    Q = b[0] if move == "right" else b[1]
+    for qm in b[3]:
+        blks = [Q.block(i) for i in range(Q.n) if tuple((Q.qout if move == "right" else Q.qin)[i]) == qm]
+        M = np.vstack(blks) if move == "right" else np.hstack(blks)
+        G = M.T @ M if move == "right" else M @ M.T
+        assert np.abs(G - np.eye(len(G))).max() < 1e-12
+
+
+def test_native_split_rejects_bad_leg():
+    if not native_lapack():
+        pytest.skip("numpy's bundled OpenBLAS exports no ILP64 LAPACK")
+    from vmps_gb300 import _native as N
+    model, V, comb, din, dout = _case(6, 16, 2, seed=1)
+    bad = dict(comb)
+    bad["n"] = 1
+    bad["index"] = {k: [(q, 0) for q, _ in v] for k, v in comb["index"].items()}
+    V.leg[:] = 3
+    with pytest.raises(N.VmpsError):
+        split_two_site(V, bad, model.qloc, model.qloc, din, dout, 2, 16, native=True)

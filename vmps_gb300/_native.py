@@ -76,6 +76,14 @@ class vmps_cheb_stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class vmps_split_args(C.Structure):
+    _fields_ = [("nq", C.c_int32), ("n1", C.c_int32), ("n3", C.c_int32), ("n13", C.c_int32),
+                ("qloc1", i32p), ("qloc3", i32p), ("pair1", i32p), ("pair3", i32p),
+                ("nin", C.c_int32), ("qin", i32p), ("din", i64p), ("nout", C.c_int32), ("qout", i32p),
+                ("dout", i64p), ("dmax", C.c_int64), ("eps_svd", C.c_double), ("move_right", C.c_int32),
+                ("threads", C.c_int32)]
+
+
 # (name, restype, argtypes)
 _PROTOS = [
     ("vmps_last_error", C.c_char_p, []),
@@ -99,6 +107,13 @@ _PROTOS = [
     ("vmps_two_site_contract", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
                                          C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks), f64p, C.c_int64,
                                          i64p]),
+    ("vmps_hostla_load", C.c_int, [C.c_char_p]),
+    ("vmps_two_site_split", C.c_int, [C.POINTER(vmps_split_args), C.POINTER(vmps_blocks), f64p,
+                                      C.POINTER(C.c_void_p)]),
+    ("vmps_split_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), i64p, i64p, i64p, i64p]),
+    ("vmps_split_get", C.c_int, [C.c_void_p, i32p, i64p, i32p, i32p, i32p, i64p, i64p, f64p, i32p, i32p, i32p,
+                                 i64p, i64p, f64p]),
+    ("vmps_split_destroy", None, [C.c_void_p]),
     ("vmps_spectral_bounds", C.c_int, [C.c_void_p, f64p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("vmps_chebyshev_moments", C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, f64p,
                                          C.POINTER(vmps_cheb_stats)]),

@@ -1,0 +1,489 @@
+// Host dense linear algebra of the two-site sweep: the truncated SVD of
+// split_AA2 (tensors/DmrgContractions.h:2461-2631, with Biped::truncateSVD,
+// tensors/Biped.h:744-932), abelian quantum numbers.
+//
+// For every middle QN qmid the two-site tensor's blocks form one sector matrix
+//     Psi[(s1, qin), (s3, qout)] = V[s13(s1, s3)](qin, qout),  qin + q(s1) = qmid;
+// its singular values and the orthonormal factor the sweep direction keeps come
+// from the eigendecomposition of the Gram matrix (Psi Psi^T for a move to the
+// right, Psi^T Psi to the left).  The Dmax largest singular values over all
+// sectors are kept (none below eps_svd times the largest), renormalised, and the
+// two site tensors are assembled in the block order of a site layout
+// (for s, for qin in sorted order, qout = qin + q(s) if present).
+//
+// GB300's FP64 rate makes these small dense problems (sectors of tens to a few
+// hundred rows) cheaper on the Grace cores than on the GPU.  The LAPACK / BLAS
+// routines are the ILP64 ones of the OpenBLAS that numpy bundles, bound at run
+// time from the path the caller passes; the sectors run on a pool of host
+// threads, largest first, one sector per thread.
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <array>
+#include <unordered_map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "vmps_gb300.h"
+
+namespace vmps {
+void set_last_error_message(const std::string& msg);   // runtime.cpp
+}
+
+namespace {
+
+int set_err(int code, const std::string& msg) {
+    vmps::set_last_error_message(msg);
+    return code;
+}
+
+using lint = int64_t;   // ILP64 LAPACK integers
+typedef void (*dsyevd_fn)(const char*, const char*, const lint*, double*, const lint*, double*, double*, const lint*,
+                          lint*, const lint*, lint*, size_t, size_t);
+typedef void (*dsyev_fn)(const char*, const char*, const lint*, double*, const lint*, double*, double*, const lint*,
+                         lint*, size_t, size_t);
+typedef void (*dsyrk_fn)(const char*, const char*, const lint*, const lint*, const double*, const double*, const lint*,
+                         const double*, double*, const lint*, size_t, size_t);
+typedef void (*dgemm_fn)(const char*, const char*, const lint*, const lint*, const lint*, const double*, const double*,
+                         const lint*, const double*, const lint*, const double*, double*, const lint*, size_t, size_t);
+
+struct Lapack {
+    dsyevd_fn syevd = nullptr;
+    dsyev_fn syev = nullptr;
+    dsyrk_fn syrk = nullptr;
+    dgemm_fn gemm = nullptr;
+    bool ok() const { return syevd && syev && syrk && gemm; }
+};
+
+// Gram matrices of at least this order go to dsyevd (divide and conquer), smaller
+// ones to dsyev (QR iteration).  On the 16 Grace cores concurrent dsyevd calls
+// contend inside OpenBLAS's level-3 kernels: an order-64 call took 0.28 ms alone
+// and 2.1 ms with 16 threads busy, where dsyev went from 0.40 to 1.0 ms; at order
+// 178 dsyevd still gives the higher throughput.
+constexpr int64_t kSyevdMin = 128;
+Lapack g_lapack;
+std::mutex g_lapack_mu;
+
+void* find_symbol(void* h, const char* base) {
+    for (const char* pre : {"scipy_", ""}) {
+        for (const char* suf : {"_64_", "64_"}) {
+            const std::string name = std::string(pre) + base + suf;
+            if (void* p = dlsym(h, name.c_str())) return p;
+        }
+    }
+    return nullptr;
+}
+
+// quantum numbers (at most 4 components) packed into one key whose integer order
+// is the lexicographic order of the components (first component most significant)
+using QN = std::array<int32_t, 4>;
+using QKey = uint64_t;
+QKey qkey(const QN& q, int nq) {
+    QKey k = 0;
+    for (int i = 0; i < nq; ++i) {
+        if (q[(size_t)i] <= -32768 || q[(size_t)i] >= 32768) throw std::invalid_argument("quantum number out of range");
+        k = (k << 16) | (QKey)(uint16_t)(q[(size_t)i] + 32768);
+    }
+    return k;
+}
+QN qload(const int32_t* p, int nq) {
+    QN q{0, 0, 0, 0};
+    for (int i = 0; i < nq; ++i) q[(size_t)i] = p[i];
+    return q;
+}
+
+struct Sector {
+    QN q;
+    uint64_t key = 0;
+    int64_t rows = 0, cols = 0;
+    std::vector<double> M;        // rows x cols, column-major
+    std::vector<double> S;        // singular values, descending (min(rows, cols))
+    std::vector<double> Q;        // eigenvectors of the Gram matrix, columns in S's order (n x n)
+    int64_t n = 0;                // Gram matrix order
+    int64_t kept = 0;
+    std::string err;
+};
+
+// eigendecomposition of the sector's Gram matrix (move right: rows x rows, else cols x cols)
+void factor(Sector& s, bool right) {
+    const Lapack& L = g_lapack;
+    const lint r = s.rows, c = s.cols;
+    const lint n = right ? r : c, k = right ? c : r;
+    s.n = n;
+    std::vector<double> G((size_t)n * n, 0.0);
+    const double one = 1.0, zero = 0.0;
+    // lower triangle of M M^T ('N') or M^T M ('T')
+    L.syrk("L", right ? "N" : "T", &n, &k, &one, s.M.data(), &r, &zero, G.data(), &n, 1, 1);
+    std::vector<double> w((size_t)n);
+    lint info = 0;
+    if (n >= kSyevdMin) {
+        const lint lwork = 1 + 6 * n + 2 * n * n, liwork = 3 + 5 * n;
+        std::vector<double> work((size_t)lwork);
+        std::vector<lint> iwork((size_t)liwork);
+        L.syevd("V", "L", &n, G.data(), &n, w.data(), work.data(), &lwork, iwork.data(), &liwork, &info, 1, 1);
+    } else {
+        const lint lwork = std::max<lint>(1, 66 * n);   // (block size + 2) n
+        std::vector<double> work((size_t)lwork);
+        L.syev("V", "L", &n, G.data(), &n, w.data(), work.data(), &lwork, &info, 1, 1);
+    }
+    if (info != 0) {
+        s.err = "symmetric eigensolver failed (info " + std::to_string(info) + ")";
+        return;
+    }
+    // descending order, min(rows, cols) values
+    const int64_t m = std::min(r, c);
+    s.S.resize((size_t)m);
+    s.Q.resize((size_t)n * n);
+    for (int64_t j = 0; j < n; ++j) {
+        const int64_t src = n - 1 - j;
+        std::memcpy(s.Q.data() + (size_t)j * n, G.data() + (size_t)src * n, sizeof(double) * (size_t)n);
+        if (j < m) s.S[(size_t)j] = std::sqrt(std::max(w[(size_t)src], 0.0));
+    }
+}
+
+}  // namespace
+
+struct vmps_split_s {
+    int nq = 1;
+    std::vector<QN> qmid;
+    std::vector<int64_t> dmid;
+    double disc = 0;
+    // site tensors in site-layout block order
+    std::vector<int32_t> leg1, qin1, qout1, leg2, qin2, qout2;
+    std::vector<int64_t> rows1, cols1, rows2, cols2;
+    std::vector<double> data1, data2;
+};
+
+namespace {
+
+QN qadd(const QN& a, const int32_t* b, int nq, int sign) {
+    QN r = a;
+    for (int i = 0; i < nq; ++i) r[(size_t)i] += sign * b[i];
+    return r;
+}
+
+void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd, vmps_split_s& out) {
+    const int nq = a->nq;
+    out.nq = nq;
+    const bool right = a->move_right != 0;
+    // bond bases in sorted QN order
+    struct Basis { QKey k; QN q; int64_t d; };
+    auto load_basis = [nq](int m, const int32_t* qs, const int64_t* ds) {
+        std::vector<Basis> b((size_t)m);
+        for (int i = 0; i < m; ++i) {
+            b[(size_t)i].q = qload(qs + (size_t)i * nq, nq);
+            b[(size_t)i].k = qkey(b[(size_t)i].q, nq);
+            b[(size_t)i].d = ds[i];
+        }
+        std::sort(b.begin(), b.end(), [](const Basis& x, const Basis& y) { return x.k < y.k; });
+        return b;
+    };
+    const std::vector<Basis> bin = load_basis(a->nin, a->qin, a->din);
+    const std::vector<Basis> bout = load_basis(a->nout, a->qout, a->dout);
+    std::unordered_map<QKey, int64_t> dout;
+    for (const Basis& b : bout) dout[b.k] = b.d;
+    // sector rows: (s1, qin) in (s1, sorted qin) order; columns: (s3, qout)
+    struct Pos { QKey qm; int64_t off; };
+    std::unordered_map<QKey, int64_t> nrows, ncols;
+    std::unordered_map<QKey, QN> qn_of;
+    std::vector<std::unordered_map<QKey, Pos>> roff((size_t)a->n1), coff((size_t)a->n3);
+    for (int s1 = 0; s1 < a->n1; ++s1)
+        for (const Basis& b : bin) {
+            const QN qm = qadd(b.q, a->qloc1 + (size_t)s1 * nq, nq, +1);
+            const QKey km = qkey(qm, nq);
+            qn_of[km] = qm;
+            int64_t& nr = nrows[km];
+            roff[(size_t)s1][b.k] = Pos{km, nr};
+            nr += b.d;
+        }
+    for (int s3 = 0; s3 < a->n3; ++s3)
+        for (const Basis& b : bout) {
+            const QN qm = qadd(b.q, a->qloc3 + (size_t)s3 * nq, nq, -1);
+            const QKey km = qkey(qm, nq);
+            int64_t& nc = ncols[km];
+            coff[(size_t)s3][b.k] = Pos{km, nc};
+            nc += b.d;
+        }
+    // scatter the two-site blocks into their sectors (sectors without blocks are dropped)
+    std::unordered_map<QKey, size_t> sidx;
+    std::vector<std::unique_ptr<Sector>> sec;
+    for (int64_t k = 0; k < V->nblocks; ++k) {
+        const int s13 = V->leg[k];
+        if (s13 < 0 || s13 >= a->n13) throw std::invalid_argument("two-site block leg outside the combined basis");
+        const int s1 = a->pair1[s13], s3 = a->pair3[s13];
+        const QKey ki = qkey(qload(V->qin + (size_t)k * nq, nq), nq), ko = qkey(qload(V->qout + (size_t)k * nq, nq), nq);
+        auto ri = roff[(size_t)s1].find(ki);
+        auto ci = coff[(size_t)s3].find(ko);
+        if (ri == roff[(size_t)s1].end() || ci == coff[(size_t)s3].end() || ri->second.qm != ci->second.qm) continue;
+        const QKey km = ri->second.qm;
+        auto it = sidx.find(km);
+        if (it == sidx.end()) {
+            std::unique_ptr<Sector> S(new Sector());
+            S->q = qn_of[km];
+            S->key = km;
+            S->rows = nrows[km];
+            S->cols = ncols[km];
+            S->M.assign((size_t)(S->rows * S->cols), 0.0);
+            it = sidx.emplace(km, sec.size()).first;
+            sec.push_back(std::move(S));
+        }
+        Sector& S = *sec[it->second];
+        const int64_t r = V->rows[k], c = V->cols[k];
+        if (ri->second.off + r > S.rows || ci->second.off + c > S.cols)
+            throw std::invalid_argument("two-site block does not fit its sector");
+        const double* src = Vd + V->offset[k];
+        for (int64_t j = 0; j < c; ++j)
+            std::memcpy(S.M.data() + (size_t)((ci->second.off + j) * S.rows + ri->second.off), src + (size_t)(j * r),
+                        sizeof(double) * (size_t)r);
+    }
+    std::vector<Sector*> order;   // sorted by middle QN
+    for (auto& p : sec) order.push_back(p.get());
+    std::sort(order.begin(), order.end(), [](const Sector* x, const Sector* y) { return x->key < y->key; });
+    // factorisations on the host threads, largest first
+    std::vector<Sector*> work(order);
+    std::sort(work.begin(), work.end(), [right](const Sector* x, const Sector* y) {
+        const int64_t nx = right ? x->rows : x->cols, ny = right ? y->rows : y->cols;
+        return nx * nx * (right ? x->cols : x->rows) > ny * ny * (right ? y->cols : y->rows);
+    });
+    const int nt = std::max(1, std::min<int>(a->threads, (int)work.size()));
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t i = next++; i < work.size(); i = next++) factor(*work[i], right);
+    };
+    if (nt == 1) {
+        worker();
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t) th.emplace_back(worker);
+        for (auto& t : th) t.join();
+    }
+    for (Sector* s : order)
+        if (!s->err.empty()) throw std::runtime_error(s->err);
+    // global truncation: the Dmax largest values above eps_svd * max; ties at the
+    // threshold are kept in sector order until Dmax is reached
+    std::vector<double> all;
+    for (Sector* s : order) all.insert(all.end(), s->S.begin(), s->S.end());
+    double smax = 0, tot2 = 0;
+    for (double v : all) {
+        smax = std::max(smax, v);
+        tot2 += v * v;
+    }
+    std::vector<double> keep;
+    for (double v : all)
+        if (v > a->eps_svd * smax) keep.push_back(v);
+    std::sort(keep.begin(), keep.end(), [](double x, double y) { return x > y; });
+    if ((int64_t)keep.size() > a->dmax) keep.resize((size_t)std::max<int64_t>(a->dmax, 0));
+    const double thresh = keep.empty() ? std::numeric_limits<double>::infinity() : keep.back();
+    int64_t budget = (int64_t)keep.size();
+    for (Sector* s : order) {
+        s->kept = 0;
+        for (double v : s->S) s->kept += v > thresh;
+        budget -= s->kept;
+    }
+    for (Sector* s : order) {
+        if (budget <= 0) break;
+        int64_t extra = 0;
+        for (double v : s->S) extra += v == thresh;
+        const int64_t take = std::min(extra, budget);
+        s->kept += take;
+        budget -= take;
+    }
+    double norm2 = 0;
+    for (Sector* s : order)
+        for (int64_t i = 0; i < s->kept; ++i) norm2 += s->S[(size_t)i] * s->S[(size_t)i];
+    out.disc = tot2 > 0 ? std::max(0.0, tot2 - norm2) / tot2 : 0.0;
+    const double scale = norm2 > 0 ? 1.0 / std::sqrt(norm2) : 1.0;
+    std::vector<Sector*> ks;   // kept sectors, in QN order
+    std::unordered_map<QKey, size_t> kidx;
+    for (Sector* s : order)
+        if (s->kept > 0) {
+            kidx[s->key] = ks.size();
+            ks.push_back(s);
+            out.qmid.push_back(s->q);
+            out.dmid.push_back(s->kept);
+        }
+    // the non-orthonormal factor: A2 = scale U_k^T Psi (right) or A1 = scale Psi V_k (left)
+    const Lapack& L = g_lapack;
+    std::atomic<size_t> next2{0};
+    std::vector<std::vector<double>> Fk(ks.size());
+    auto worker2 = [&]() {
+        for (size_t i = next2++; i < ks.size(); i = next2++) {
+            Sector& s = *ks[i];
+            const lint r = s.rows, c = s.cols, k = s.kept, n = s.n;
+            const double zero = 0.0;
+            if (right) {
+                Fk[i].assign((size_t)(k * c), 0.0);   // k x c
+                L.gemm("T", "N", &k, &c, &r, &scale, s.Q.data(), &n, s.M.data(), &r, &zero, Fk[i].data(), &k, 1, 1);
+            } else {
+                Fk[i].assign((size_t)(r * k), 0.0);   // r x k
+                L.gemm("N", "N", &r, &k, &c, &scale, s.M.data(), &r, s.Q.data(), &n, &zero, Fk[i].data(), &r, 1, 1);
+            }
+        }
+    };
+    const int nt2 = std::max(1, std::min<int>(a->threads, (int)ks.size()));
+    if (nt2 == 1) {
+        worker2();
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt2; ++t) th.emplace_back(worker2);
+        for (auto& t : th) t.join();
+    }
+    // output sizes first (one allocation per table)
+    {
+        size_t nb1 = 0, sz1 = 0, nb2 = 0, sz2 = 0;
+        for (int s1 = 0; s1 < a->n1; ++s1)
+            for (const Basis& b : bin) {
+                auto it = kidx.find(qkey(qadd(b.q, a->qloc1 + (size_t)s1 * nq, nq, +1), nq));
+                if (it == kidx.end()) continue;
+                ++nb1;
+                sz1 += (size_t)(b.d * ks[it->second]->kept);
+            }
+        for (int s3 = 0; s3 < a->n3; ++s3)
+            for (const Sector* s : ks) {
+                auto di = dout.find(qkey(qadd(s->q, a->qloc3 + (size_t)s3 * nq, nq, +1), nq));
+                if (di == dout.end()) continue;
+                ++nb2;
+                sz2 += (size_t)(s->kept * di->second);
+            }
+        out.leg1.reserve(nb1); out.rows1.reserve(nb1); out.cols1.reserve(nb1);
+        out.qin1.reserve(nb1 * (size_t)nq); out.qout1.reserve(nb1 * (size_t)nq);
+        out.leg2.reserve(nb2); out.rows2.reserve(nb2); out.cols2.reserve(nb2);
+        out.qin2.reserve(nb2 * (size_t)nq); out.qout2.reserve(nb2 * (size_t)nq);
+        out.data1.reserve(sz1);
+        out.data2.reserve(sz2);
+    }
+    // A1 = site layout (qloc1, din, dmid): rows of the sector at (s1, qin)
+    for (int s1 = 0; s1 < a->n1; ++s1)
+        for (const Basis& b : bin) {
+            const QN qm = qadd(b.q, a->qloc1 + (size_t)s1 * nq, nq, +1);
+            auto it = kidx.find(qkey(qm, nq));
+            if (it == kidx.end()) continue;
+            const Sector& s = *ks[it->second];
+            const int64_t r = b.d, c = s.kept, ra = roff[(size_t)s1][b.k].off;
+            out.leg1.push_back(s1);
+            out.qin1.insert(out.qin1.end(), b.q.begin(), b.q.begin() + nq);
+            out.qout1.insert(out.qout1.end(), qm.begin(), qm.begin() + nq);
+            out.rows1.push_back(r);
+            out.cols1.push_back(c);
+            const size_t base = out.data1.size();
+            out.data1.resize(base + (size_t)(r * c));
+            double* dst = out.data1.data() + base;
+            if (right) {   // U_k rows ra.. of the eigenvectors
+                for (int64_t j = 0; j < c; ++j)
+                    std::memcpy(dst + (size_t)(j * r), s.Q.data() + (size_t)(j * s.n + ra), sizeof(double) * (size_t)r);
+            } else {       // scale Psi V_k, rows ra..
+                const std::vector<double>& f = Fk[it->second];
+                for (int64_t j = 0; j < c; ++j)
+                    std::memcpy(dst + (size_t)(j * r), f.data() + (size_t)(j * s.rows + ra), sizeof(double) * (size_t)r);
+            }
+        }
+    // A2 = site layout (qloc3, dmid, dout): columns of the sector at (s3, qout)
+    for (int s3 = 0; s3 < a->n3; ++s3)
+        for (size_t i = 0; i < ks.size(); ++i) {
+            const Sector& s = *ks[i];
+            const QN qo = qadd(s.q, a->qloc3 + (size_t)s3 * nq, nq, +1);
+            const QKey ko = qkey(qo, nq);
+            auto di = dout.find(ko);
+            if (di == dout.end()) continue;
+            const int64_t r = s.kept, c = di->second, ca = coff[(size_t)s3][ko].off;
+            out.leg2.push_back(s3);
+            out.qin2.insert(out.qin2.end(), s.q.begin(), s.q.begin() + nq);
+            out.qout2.insert(out.qout2.end(), qo.begin(), qo.begin() + nq);
+            out.rows2.push_back(r);
+            out.cols2.push_back(c);
+            const size_t base = out.data2.size();
+            out.data2.resize(base + (size_t)(r * c));
+            double* dst = out.data2.data() + base;
+            if (right) {   // scale U_k^T Psi, columns ca..
+                std::memcpy(dst, Fk[i].data() + (size_t)(ca * r), sizeof(double) * (size_t)(r * c));
+            } else {       // V_k^T: row i = eigenvector i at entries ca..
+                for (int64_t j = 0; j < c; ++j)
+                    for (int64_t q = 0; q < r; ++q) dst[j * r + q] = s.Q[(size_t)(q * s.n + ca + j)];
+            }
+        }
+}
+
+}  // namespace
+
+extern "C" int vmps_hostla_load(const char* path) {
+    std::lock_guard<std::mutex> lock(g_lapack_mu);
+    if (g_lapack.ok()) return VMPS_OK;
+    if (!path) return set_err(VMPS_E_ARG, "no library path");
+    void* h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+    if (!h) return set_err(VMPS_E_ARG, std::string("cannot open ") + path);
+    Lapack L;
+    L.syevd = (dsyevd_fn)find_symbol(h, "dsyevd");
+    L.syev = (dsyev_fn)find_symbol(h, "dsyev");
+    L.syrk = (dsyrk_fn)find_symbol(h, "dsyrk");
+    L.gemm = (dgemm_fn)find_symbol(h, "dgemm");
+    if (!L.ok()) return set_err(VMPS_E_ARG, std::string("no ILP64 dsyevd/dsyev/dsyrk/dgemm in ") + path);
+    g_lapack = L;
+    return VMPS_OK;
+}
+
+extern "C" int vmps_two_site_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vdata,
+                                   vmps_split** out) {
+    if (!a || !V || !out || (V->nblocks > 0 && !Vdata)) return set_err(VMPS_E_ARG, "bad argument");
+    if (a->nq < 1 || a->nq > 4 || a->n1 < 1 || a->n3 < 1 || a->n13 < 1 || !a->pair1 || !a->pair3 ||
+        !a->qloc1 || !a->qloc3 || a->nin < 0 || a->nout < 0 || a->dmax < 0)
+        return set_err(VMPS_E_ARG, "bad split arguments");
+    for (int i = 0; i < a->n13; ++i)
+        if (a->pair1[i] < 0 || a->pair1[i] >= a->n1 || a->pair3[i] < 0 || a->pair3[i] >= a->n3)
+            return set_err(VMPS_E_ARG, "combined index outside the local bases");
+    if (!g_lapack.ok()) return set_err(VMPS_E_ARG, "host LAPACK not bound (vmps_hostla_load)");
+    try {
+        std::unique_ptr<vmps_split_s> s(new vmps_split_s());
+        run_split(a, V, Vdata, *s);
+        *out = s.release();
+    } catch (const std::bad_alloc& e) {
+        return set_err(VMPS_E_NOMEM, e.what());
+    } catch (const std::exception& e) {
+        return set_err(VMPS_E_ARG, e.what());
+    }
+    return VMPS_OK;
+}
+
+extern "C" int vmps_split_info(const vmps_split* s, int* nmid, double* disc, int64_t* nblocks1, int64_t* size1,
+                               int64_t* nblocks2, int64_t* size2) {
+    if (!s || !nmid || !disc || !nblocks1 || !size1 || !nblocks2 || !size2)
+        return set_err(VMPS_E_ARG, "bad argument");
+    *nmid = (int)s->qmid.size();
+    *disc = s->disc;
+    *nblocks1 = (int64_t)s->leg1.size();
+    *size1 = (int64_t)s->data1.size();
+    *nblocks2 = (int64_t)s->leg2.size();
+    *size2 = (int64_t)s->data2.size();
+    return VMPS_OK;
+}
+
+extern "C" int vmps_split_get(const vmps_split* s, int32_t* qmid, int64_t* dmid, int32_t* leg1, int32_t* qin1,
+                              int32_t* qout1, int64_t* rows1, int64_t* cols1, double* data1, int32_t* leg2,
+                              int32_t* qin2, int32_t* qout2, int64_t* rows2, int64_t* cols2, double* data2) {
+    if (!s) return set_err(VMPS_E_ARG, "bad argument");
+    auto put = [](auto* dst, const auto& v) {
+        if (!v.empty()) std::memcpy(dst, v.data(), sizeof(v[0]) * v.size());
+    };
+    if (!qmid || !dmid || !leg1 || !qin1 || !qout1 || !rows1 || !cols1 || !data1 || !leg2 || !qin2 || !qout2 ||
+        !rows2 || !cols2 || !data2)
+        return set_err(VMPS_E_ARG, "bad argument");
+    for (size_t i = 0; i < s->qmid.size(); ++i)
+        for (int c = 0; c < s->nq; ++c) qmid[i * (size_t)s->nq + (size_t)c] = s->qmid[i][(size_t)c];
+    put(dmid, s->dmid);
+    put(leg1, s->leg1); put(qin1, s->qin1); put(qout1, s->qout1); put(rows1, s->rows1); put(cols1, s->cols1);
+    put(data1, s->data1);
+    put(leg2, s->leg2); put(qin2, s->qin2); put(qout2, s->qout2); put(rows2, s->rows2); put(cols2, s->cols2);
+    put(data2, s->data2);
+    return VMPS_OK;
+}
+
+extern "C" void vmps_split_destroy(vmps_split* s) { delete s; }

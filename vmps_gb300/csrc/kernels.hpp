@@ -96,6 +96,9 @@ cudaError_t lz_init();
 cudaError_t launch_lz_step(const LzArgs& a, int per_thread, cudaStream_t st);
 cudaError_t launch_lz_combine(const void* K, int fp32, int64_t ld, int m, int64_t n, const double* c, double* y,
                               cudaStream_t st);
+// out[i] = <K_i, r>, i < m (deterministic; part holds m * sh.nchunk doubles)
+cudaError_t launch_lz_mdot(const void* K, int fp32, int64_t ld, int m, int64_t n, const double* r, double* part,
+                           const LzShape& sh, double* out, cudaStream_t st);
 cudaError_t launch_lz_to_f32(const double* x, float* y, int64_t n, cudaStream_t st);
 
 // ---- Chebyshev recursion over many right-hand sides (lanczos.cu) -------------------

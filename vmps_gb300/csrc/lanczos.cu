@@ -349,7 +349,7 @@ __global__ void lz_next_kernel(LzArgs a) {
 __device__ __forceinline__ double lz_f64(double x) { return x; }
 __device__ __forceinline__ double lz_f64(float x) { return f32_to_f64(x); }   // exact, integer pipe
 
-// y[e] = sum_{i < m} c[i] K_i[e] in FP64 (Ritz vectors)
+// y[e] = sum_{i < m} c[i] K_i[e] in FP64 (Ritz vectors and corrections)
 template <typename V>
 __global__ void lz_combine_kernel(const V* __restrict__ K, int64_t ld, int m, int64_t n,
                                   const double* __restrict__ c, double* __restrict__ y) {
@@ -357,6 +357,37 @@ __global__ void lz_combine_kernel(const V* __restrict__ K, int64_t ld, int m, in
         double s = 0;
         for (int i = 0; i < m; ++i) s = fma(c[i], lz_f64(K[(int64_t)i * ld + e]), s);
         y[e] = s;
+    }
+}
+
+// out[i] = <K_i, r> for i < m, deterministic: per-chunk partials here (r is
+// FP64, rounded to the basis type when staged), summed by lz_rowsum_kernel
+template <typename V, int E>
+__global__ void __launch_bounds__(kLzThreads) lz_mdot_kernel(const V* __restrict__ K, int64_t ld, int m, int64_t n,
+                                                              const double* __restrict__ r,
+                                                              double* __restrict__ part, int nchunk) {
+    __shared__ __align__(16) V rsh[E * kLzThreads];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t cb = (int64_t)blockIdx.x * (E * kLzThreads);
+    const int len = (int)(n - cb < E * kLzThreads ? n - cb : E * kLzThreads);
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+        const int x = threadIdx.x + u * kLzThreads;
+        rsh[x] = (V)(x < len ? r[cb + x] : 0.0);
+    }
+    __syncthreads();
+    for (int i = warp; i < m; i += kLzWarps) {
+        const double t = lz_chunk_dot<V, E>(K + (int64_t)i * ld + cb, rsh, len, lane);
+        if (lane == 0) part[(int64_t)i * nchunk + blockIdx.x] = t;
+    }
+}
+
+// out[i] = sum over chunks of part[i], i < rows, one block per row
+__global__ void __launch_bounds__(kLzThreads) lz_rowsum_kernel(const double* part, int nchunk, int rows,
+                                                                double* out) {
+    for (int i = blockIdx.x; i < rows; i += gridDim.x) {
+        const double t = lz_block_row_sum(part, i, nchunk);
+        if (threadIdx.x == 0) out[i] = t;
     }
 }
 
@@ -488,6 +519,20 @@ cudaError_t launch_lz_combine(const void* K, int fp32, int64_t ld, int m, int64_
     return cudaGetLastError();
 }
 
+cudaError_t launch_lz_mdot(const void* K, int fp32, int64_t ld, int m, int64_t n, const double* r, double* part,
+                           const LzShape& sh, double* out, cudaStream_t st) {
+    if (m < 1 || m > kLzMaxIter || n <= 0 || !K || !r || !part || !out) return cudaErrorInvalidValue;
+    if ((int64_t)sh.nchunk * sh.chunk < n) return cudaErrorInvalidValue;
+#define LZ_CALL(EE)                                                                                        \
+    if (fp32) lz_mdot_kernel<float, EE><<<sh.nchunk, kLzThreads, 0, st>>>((const float*)K, ld, m, n, r, part, \
+                                                                          sh.nchunk);                       \
+    else lz_mdot_kernel<double, EE><<<sh.nchunk, kLzThreads, 0, st>>>((const double*)K, ld, m, n, r, part,   \
+                                                                        sh.nchunk);
+    LZ_DISPATCH(sh.per_thread, LZ_CALL)
+#undef LZ_CALL
+    lz_rowsum_kernel<<<m < kLzCoefBlocks ? m : kLzCoefBlocks, kLzThreads, 0, st>>>(part, sh.nchunk, m, out);
+    return cudaGetLastError();
+}
 #undef LZ_DISPATCH
 
 cudaError_t launch_lz_to_f32(const double* x, float* y, int64_t n, cudaStream_t st) {

@@ -1383,6 +1383,11 @@ LzWork& lz_work(vmps_ctx* c, int64_t n, int cap) {
 // solve runs as FP64 Lanczos: about twice the residual that the BF16x3
 // operator's rounding noise (4e-6 relative) leaves on an exact eigenvector.
 constexpr double kSplitProbeRel = 1e-5;
+// Model residual (relative to the energy) at which a refined split-precision
+// phase stops: a tenth of the FP64 residual the operator's noise leaves on its
+// Ritz vector; iterations past it only resolve that noise, and the refinement
+// rounds start from the FP64 residual in any case.
+constexpr double kSplitStateRel = 5e-7;
 
 // FP32 start of a split-precision run: K32_0 = q32 = (float) K_0, padding zero
 void lz_start_f32(LzWork& W, cudaStream_t st) {
@@ -1410,8 +1415,9 @@ struct LzResult {
 // start vector's residual is above that fraction of its energy.
 // first_row = {alpha_0, beta_0}: the caller has set K_0, K_1 (and q = K_1) and
 // knows the first row of the tridiagonal exactly; the run starts at iteration 1.
+// state_rel > 0: the residual test is |r| <= max(tol_state, state_rel * max(1, |theta|)).
 LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval, double tol_state,
-                double probe_rel = 0, const double* first_row = nullptr) {
+                double probe_rel = 0, const double* first_row = nullptr, double state_rel = 0) {
     cudaStream_t st = p->st();
     DevPlan& dp = get_plan(p, prec);
     const bool f32 = prec != VMPS_PREC_FP64;   // split-precision runs keep FP32 Krylov vectors
@@ -1511,7 +1517,8 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
         res = std::abs(b_j * y.back());
         const bool conv_e = std::abs(theta - theta_prev) <= tol_eigval * std::max(1.0, std::abs(theta));
         theta_prev = theta;
-        if ((conv_e && res <= tol_state) || b_j <= 1e-14 * std::max(1.0, std::abs(theta)) || j + 1 == kmax) {
+        const double tol_res = std::max(tol_state, state_rel * std::max(1.0, std::abs(theta)));
+        if ((conv_e && res <= tol_res) || b_j <= 1e-14 * std::max(1.0, std::abs(theta)) || j + 1 == kmax) {
             ++j;
             break;
         }
@@ -1534,6 +1541,63 @@ void lz_ritz(vmps_pivot* p, LzWork& W, const std::vector<double>& y, double* x, 
     CK(launch_scale(1.0 / nx, x, W.n, st));
 }
 
+// Correction of a Ritz vector y (unit norm, lowest eigenvector of the
+// tridiagonal T = tridiag(beta, alpha, beta)) inside the Krylov space: the
+// Jacobi-Davidson correction equation restricted to span(K),
+//     P (T - th) P z = -P g,   P = 1 - y y^T,   z orthogonal to y,
+// with g = K^T r the projection of the residual r = H x - th x.  Solved by
+// conjugate gradients on the m-dimensional system (positive definite on y's
+// complement while th lies below the second Ritz value; the iteration stops
+// at the first direction of non-positive curvature).  `model` returns the
+// second-order energy change 2 g.z + z.(T - th) z of the step.
+std::vector<double> krylov_correction(const std::vector<double>& a, const std::vector<double>& b, double th,
+                                      const std::vector<double>& y, const std::vector<double>& g, double* model) {
+    const size_t m = a.size();
+    auto Tv = [&](const std::vector<double>& v, std::vector<double>& out) {
+        for (size_t i = 0; i < m; ++i) {
+            double s = (a[i] - th) * v[i];
+            if (i > 0) s += b[i - 1] * v[i - 1];
+            if (i + 1 < m) s += b[i] * v[i + 1];
+            out[i] = s;
+        }
+    };
+    auto proj = [&](std::vector<double>& v) {
+        double d = 0;
+        for (size_t i = 0; i < m; ++i) d += y[i] * v[i];
+        for (size_t i = 0; i < m; ++i) v[i] -= d * y[i];
+    };
+    auto dot = [&](const std::vector<double>& u, const std::vector<double>& v) {
+        double s = 0;
+        for (size_t i = 0; i < m; ++i) s += u[i] * v[i];
+        return s;
+    };
+    std::vector<double> z(m, 0.0), r(g), p, Ap(m);
+    for (double& v : r) v = -v;
+    proj(r);
+    p = r;
+    double rr = dot(r, r);
+    const double r0 = std::sqrt(rr);
+    for (size_t it = 0; it < 2 * m + 10 && rr > 0 && std::sqrt(rr) > 1e-14 * r0; ++it) {
+        Tv(p, Ap);
+        proj(Ap);
+        const double pAp = dot(p, Ap);
+        if (!(pAp > 0)) break;
+        const double al = rr / pAp;
+        for (size_t i = 0; i < m; ++i) {
+            z[i] += al * p[i];
+            r[i] -= al * Ap[i];
+        }
+        proj(r);
+        const double rr2 = dot(r, r);
+        for (size_t i = 0; i < m; ++i) p[i] = r[i] + (rr2 / rr) * p[i];
+        rr = rr2;
+    }
+    proj(z);
+    std::vector<double> Tz(m);
+    Tv(z, Tz);
+    *model = 2 * dot(g, z) + dot(z, Tz);
+    return z;
+}
 // Ritz vector of a run started from first_row: out = y_0 x0 + sum_{i>=1} y_i K_i,
 // normalised.  K_0 of that run is the FP32 copy of x0; the FP64 x0 itself enters
 // here so that the result keeps FP64 accuracy along it.
@@ -1557,6 +1621,20 @@ void lz_ritz_mixed(vmps_pivot* p, LzWork& W, const std::vector<double>& y, const
 // which its split-precision run stops: below the reduction the split operator's
 // noise allows in one round.
 constexpr double kRoundReduce = 1e-3;
+// Refinement rounds replace closing FP64 Lanczos steps when an FP64 HxV costs at
+// least this many split-precision Lanczos steps: a round spends a few tens of
+// split steps and one FP64 HxV where the FP64 steps need several FP64 HxVs.
+constexpr double kRoundMinRatio = 10;
+
+// VMPS_LANCZOS_REFINE = rounds | polish pins the refinement; unset or auto
+// chooses by the measured cost ratio
+int refine_mode() {
+    const char* v = std::getenv("VMPS_LANCZOS_REFINE");
+    if (!v || !*v || !std::strcmp(v, "auto")) return 0;
+    if (!std::strcmp(v, "rounds")) return 1;
+    if (!std::strcmp(v, "polish")) return 2;
+    throw std::invalid_argument("VMPS_LANCZOS_REFINE must be auto, rounds or polish");
+}
 }  // namespace
 
 extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_iter, double tol_eigval,
@@ -1571,8 +1649,10 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t st = p->st();
     const bool refine = prec != VMPS_PREC_FP64 && refine_iters > 0;
-    get_plan(p, prec);
-    if (refine) get_plan(p, VMPS_PREC_FP64);
+    const int mode = refine_mode();
+    // a refined solve may end in the FP64 probe: the split plan is built when
+    // the split phase starts
+    get_plan(p, refine ? VMPS_PREC_FP64 : prec);
     const int64_t n = p->Vd.total;
     LzWork& W = lz_work(p->ctx, n, std::max(max_iter, refine_iters));
     // padding positions of the layout stay zero in every vector
@@ -1617,7 +1697,10 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     if (split_phase) {
         const bool f32 = prec != VMPS_PREC_FP64;
         if (f32) lz_start_f32(W, st);
-        LzResult r1 = lz_run(p, W, prec, max_iter, tol_eigval, tol_state);
+        const auto ts0 = std::chrono::steady_clock::now();
+        LzResult r1 = lz_run(p, W, prec, max_iter, tol_eigval, tol_state, 0, nullptr, refine ? kSplitStateRel : 0);
+        const double ms_split_step = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ts0)
+                                         .count() / std::max(1, r1.launched);
         account(r1, prec);
         s.iterations = r1.m;
         s.energy_first = r1.theta;
@@ -1625,15 +1708,22 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
         res = r1.res;
         lz_ritz(p, W, r1.y, x, f32);
         if (refine) {
-            // Refinement rounds.  Each round knows x (FP64, unit norm), its FP64
-            // Rayleigh quotient th and residual r = H x - th x.  A split-precision
-            // Lanczos run starts from the pair K_0 = x, K_1 = r / |r|: the first row
-            // of its tridiagonal (th, |r|) is FP64-exact, the rows after it come
-            // from split HxVs.  Its Ritz vector solves the correction equation for
-            // x to the split operator's noise, which enters only through the
-            // correction (second order); one FP64 HxV then gives the new x's
-            // Rayleigh quotient and residual.  A round that does not halve the
-            // residual hands the rest of the budget to FP64 Lanczos steps.
+            // FP64 residual of the split-precision Ritz vector x, then one of two
+            // refinements, whichever the measured cost ratio favours:
+            //
+            // * Rounds (an FP64 HxV costs many split steps).  A round holds x
+            //   (FP64, unit norm), its Rayleigh quotient th and residual
+            //   r = H x - th x.  A split-precision Lanczos run starts from the pair
+            //   K_0 = x, K_1 = r / |r|: the first row of its tridiagonal (th, |r|) is
+            //   FP64-exact, the later rows come from split HxVs.  Its Ritz vector
+            //   solves the correction equation for x; the split operator's noise
+            //   enters only through the correction (second order).  One FP64 HxV
+            //   gives the new x's th and r.  A round that does not halve |r| hands
+            //   the rest of the budget to FP64 Lanczos steps.
+            // * Correction and polish (FP64 HxVs are cheap).  The residual,
+            //   projected on the split Krylov space, drives the Jacobi-Davidson
+            //   correction equation solved in that space; closing FP64 Lanczos
+            //   steps start from the corrected vector.
             double* u = W.u.as<double>();
             double* xn = W.w.as<double>();   // a round's candidate (the FP64 w buffer is idle in split runs)
             int budget = refine_iters;        // FP64 HxVs of the refinement
@@ -1652,37 +1742,60 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
                 return rn <= tol_state && rn * rn <= tol_eigval * std::max(1.0, std::abs(th)) * gap;
             };
             double th = 0, rn = 0;
+            const auto tr0 = std::chrono::steady_clock::now();
             residual(x, th, rn);
+            const double ms_fp64 =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tr0).count();
             double gap = std::max(0.0, tridiag_second(r1.alpha, r1.beta) - r1.theta);
-            bool stalled = false;
-            float* K32 = W.K32.as<float>();
-            while (!converged(th, rn, gap) && budget > 0 && rn > 0) {
-                CK(launch_scale(1.0 / rn, u, n, st));
-                CK(launch_lz_to_f32(x, K32, W.ld, st));
-                CK(launch_lz_to_f32(u, K32 + W.ld, W.ld, st));
-                CK(cudaMemcpyAsync(W.q32.p, K32 + W.ld, (size_t)W.ld * 4, cudaMemcpyDeviceToDevice, st));
-                const double row0[2] = {th, rn};
-                LzResult ri = lz_run(p, W, prec, std::max(2, max_iter), HUGE_VAL,
-                                     std::max(0.1 * tol_state, kRoundReduce * rn), 0, row0);
-                account(ri, prec);
-                lz_ritz_mixed(p, W, ri.y, x, xn);
-                double th2 = 0, rn2 = 0;
-                residual(xn, th2, rn2);
-                s.refine_iterations++;
-                if (!(rn2 < rn)) {
-                    stalled = true;
-                    break;
-                }
-                CK(cudaMemcpyAsync(x, xn, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
-                stalled = rn2 > 0.5 * rn;
-                th = th2;
-                rn = rn2;
-                gap = std::max(0.0, tridiag_second(ri.alpha, ri.beta) - ri.theta);
-                if (stalled) break;
-            }
+            bool polish = false;
             e = th;
             res = rn;
-            if (stalled && budget > 0) {
+            if (converged(th, rn, gap) || budget <= 0) {
+            } else if (mode == 1 || (mode == 0 && ms_fp64 >= kRoundMinRatio * ms_split_step)) {
+                float* K32 = W.K32.as<float>();
+                while (!converged(th, rn, gap) && budget > 0 && rn > 0) {
+                    CK(launch_scale(1.0 / rn, u, n, st));
+                    CK(launch_lz_to_f32(x, K32, W.ld, st));
+                    CK(launch_lz_to_f32(u, K32 + W.ld, W.ld, st));
+                    CK(cudaMemcpyAsync(W.q32.p, K32 + W.ld, (size_t)W.ld * 4, cudaMemcpyDeviceToDevice, st));
+                    const double row0[2] = {th, rn};
+                    LzResult ri = lz_run(p, W, prec, std::max(2, max_iter), HUGE_VAL,
+                                         std::max(0.1 * tol_state, kRoundReduce * rn), 0, row0);
+                    account(ri, prec);
+                    lz_ritz_mixed(p, W, ri.y, x, xn);
+                    double th2 = 0, rn2 = 0;
+                    residual(xn, th2, rn2);
+                    s.refine_iterations++;
+                    if (!(rn2 < rn)) {
+                        polish = true;
+                        break;
+                    }
+                    CK(cudaMemcpyAsync(x, xn, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+                    polish = rn2 > 0.5 * rn;
+                    th = th2;
+                    rn = rn2;
+                    gap = std::max(0.0, tridiag_second(ri.alpha, ri.beta) - ri.theta);
+                    if (polish) break;
+                }
+                e = th;
+                res = rn;
+            } else {
+                CK(launch_lz_mdot(W.K32.p, 1, W.ld, r1.m, n, u, W.part.as<double>(), W.sh, W.g(), st));
+                std::vector<double> g(r1.m);
+                CK(cudaMemcpyAsync(g.data(), W.g(), (size_t)r1.m * 8, cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                double model = 0;
+                std::vector<double> z = krylov_correction(r1.alpha, r1.beta, th, r1.y, g, &model);
+                double zn = 0;
+                for (double t : z) zn += t * t;
+                if (model < 0 && std::sqrt(zn) < 0.5) {
+                    std::vector<double> yz(r1.y);
+                    for (size_t i = 0; i < yz.size(); ++i) yz[i] += z[i];
+                    lz_ritz(p, W, yz, x, true);
+                }
+                polish = true;
+            }
+            if (polish && budget > 0) {
                 CK(cudaMemcpyAsync(K0, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
                 CK(cudaMemcpyAsync(W.q.p, x, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
                 LzResult r2 = lz_run(p, W, VMPS_PREC_FP64, std::max(1, budget), tol_eigval, tol_state);

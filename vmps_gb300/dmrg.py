@@ -32,6 +32,13 @@ class SweepResult(dict):
     pass
 
 
+def _count(counts, st):
+    """add one Lanczos call's statistics to the running totals"""
+    counts["solves"] = counts.get("solves", 0) + 1
+    for k in ("hxv_split", "hxv_fp64", "refine_iterations"):
+        counts[k] = counts.get(k, 0) + int(st[k])
+
+
 def _push_right(A_next, Rfac):
     """A_next[s](qin, qout) <- R[qin] @ A_next[s](qin, qout)"""
     for i in range(A_next.n):
@@ -63,12 +70,13 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
         envR[l] = e.run(envR[l + 1], mps.A[l], mps.A[l])
         e.close()
     t_init = time.perf_counter() - t0
-    energies, sweep_times, timers, hxv = [], [], [], 0
+    energies, sweep_times, timers, solves, hxv = [], [], [], [], 0
     E = None
     clock = time.perf_counter
     for sweep in range(n_sweeps):
         ts = clock()
         tm = dict(lanczos=0.0, precalc=0.0, gauge=0.0, lr=0.0)
+        counts = {}
         order = list(range(L)) + list(range(L - 1, -1, -1))
         for step, l in enumerate(order):
             right = step < L
@@ -79,6 +87,7 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
             E, v, st = H.lanczos(mps.A[l].data, precision, max_iter=max_iter, tol_eigval=tol_eigval,
                                  tol_state=tol_state, refine_iters=refine_iters)
             hxv += st["hxv_fp64"] + st["hxv_split"]
+            _count(counts, st)
             H.close()
             t2 = clock()
             tm["precalc"] += t1 - t
@@ -105,10 +114,12 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
             tm["lr"] += t4 - t3
         sweep_times.append(clock() - ts)
         timers.append(tm)
+        solves.append(counts)
         energies.append(E)
         if verbose:
             print(f"sweep {sweep}: E = {E:.14f}  ({sweep_times[-1]:.2f} s)", flush=True)
-    return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv)
+    return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv,
+                       solves=solves)
 
 
 def _env(ctx, sym, side, E, A, W):
@@ -149,12 +160,13 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     for l in range(L - 1, 1, -1):
         envR[l] = _env(ctx, sym, "R", envR[l + 1], mps.A[l], model.W[l])
     t_init = time.perf_counter() - t0
-    energies, sweep_times, timers, trunc, dims, hxv = [], [], [], [], [], 0
+    energies, sweep_times, timers, solves, trunc, dims, hxv = [], [], [], [], [], [], 0
     E = None
     clock = time.perf_counter
     for sweep in range(n_sweeps):
         ts = clock()
         tm = dict(lanczos=0.0, precalc=0.0, gauge=0.0, lr=0.0)
+        counts = {}
         disc_max = 0.0
         for move, bonds in (("right", range(L - 1)), ("left", range(L - 2, -1, -1))):
             for l in bonds:
@@ -170,6 +182,7 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
                 E, v, st = H.lanczos(V.data, precision, max_iter=max_iter, tol_eigval=tol_eigval,
                                      tol_state=tol_state, refine_iters=refine_iters)
                 hxv += st["hxv_fp64"] + st["hxv_split"]
+                _count(counts, st)
                 H.close()
                 t3 = clock()
                 V.data[:] = v
@@ -190,6 +203,7 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
                 tm["lr"] += t5 - t4
         sweep_times.append(clock() - ts)
         timers.append(tm)
+        solves.append(counts)
         energies.append(E)
         trunc.append(disc_max)
         dims.append(max(sum(mps.dims[l].values()) for l in range(1, L)))
@@ -199,4 +213,4 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     if own_pool:
         pool.close()
     return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv,
-                       truncation=trunc, max_bond_dim=dims)
+                       solves=solves, truncation=trunc, max_bond_dim=dims)

@@ -19,15 +19,37 @@ import numpy as np
 _blas = None
 
 
+def _openblas_paths():
+    """Shared-library files of numpy's bundled OpenBLAS."""
+    d = os.path.dirname(np.__file__)
+    return sorted(glob.glob(os.path.join(d, "..", "numpy.libs", "*openblas*.so*")) +
+                  glob.glob(os.path.join(d, ".libs", "*openblas*.so*")))
+
+
+_native_lapack = None
+
+
+def native_lapack() -> bool:
+    """Bind numpy's ILP64 LAPACK to the native library's host routines (the
+    two-site split); False when no bundled OpenBLAS exports them."""
+    global _native_lapack
+    if _native_lapack is None:
+        from . import _native as N
+        _native_lapack = False
+        for path in _openblas_paths():
+            if N.lib().vmps_hostla_load(os.path.abspath(path).encode()) == 0:
+                _native_lapack = True
+                break
+    return _native_lapack
+
+
 def _openblas_controls():
     """(set_num_threads, get_num_threads) of numpy's bundled OpenBLAS, or None."""
     global _blas
     if _blas is not None:
         return _blas or None
     _blas = False
-    d = os.path.dirname(np.__file__)
-    for path in sorted(glob.glob(os.path.join(d, "..", "numpy.libs", "*openblas*.so*")) +
-                       glob.glob(os.path.join(d, ".libs", "*openblas*.so*"))):
+    for path in _openblas_paths():
         try:
             lib = C.CDLL(path)
         except OSError:

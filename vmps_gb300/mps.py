@@ -365,8 +365,71 @@ def _sector_factor(M, move):
     return np.sqrt(np.maximum(w[order], 0.0)), Q[:, order]
 
 
+def _split_native(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move, eps_svd, threads):
+    """split_two_site through the native host routine (vmps_two_site_split): the
+    same sectors, Gram-matrix eigensystems (LAPACK dsyevd), truncation and block
+    order, without per-block Python work; the sectors run on `threads` threads."""
+    import ctypes as C
+    from . import _native as N
+    n13 = int(comb["n"])
+    pair1 = np.full(n13, -1, dtype=np.int32)
+    pair3 = np.full(n13, -1, dtype=np.int32)
+    for (s1, s3), lst in comb["index"].items():
+        for _, s13 in lst:
+            pair1[s13], pair3[s13] = s1, s3
+    qin = sorted(din)
+    qout = sorted(dout)
+    arr = dict(qloc1=np.ascontiguousarray(np.reshape(qloc12, (-1, nq)), dtype=np.int32),
+               qloc3=np.ascontiguousarray(np.reshape(qloc34, (-1, nq)), dtype=np.int32),
+               qin=np.ascontiguousarray(np.reshape(qin, (-1, nq)), dtype=np.int32),
+               din=np.array([din[q] for q in qin], dtype=np.int64),
+               qout=np.ascontiguousarray(np.reshape(qout, (-1, nq)), dtype=np.int32),
+               dout=np.array([dout[q] for q in qout], dtype=np.int64))
+    a = N.vmps_split_args()
+    a.nq, a.n1, a.n3, a.n13 = nq, len(qloc12), len(qloc34), n13
+    a.qloc1 = arr["qloc1"].ctypes.data_as(N.i32p)
+    a.qloc3 = arr["qloc3"].ctypes.data_as(N.i32p)
+    a.pair1 = pair1.ctypes.data_as(N.i32p)
+    a.pair3 = pair3.ctypes.data_as(N.i32p)
+    a.nin, a.qin, a.din = len(qin), arr["qin"].ctypes.data_as(N.i32p), arr["din"].ctypes.data_as(N.i64p)
+    a.nout, a.qout, a.dout = len(qout), arr["qout"].ctypes.data_as(N.i32p), arr["dout"].ctypes.data_as(N.i64p)
+    a.dmax, a.eps_svd, a.move_right, a.threads = int(Dmax), float(eps_svd), int(move == "right"), int(threads)
+    vb = V.c_struct()
+    h = C.c_void_p()
+    lib = N.lib()
+    N.check(lib.vmps_two_site_split(C.byref(a), C.byref(vb), V.data_ptr(), C.byref(h)))
+    try:
+        nmid, disc = C.c_int(), C.c_double()
+        nb1, sz1, nb2, sz2 = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        N.check(lib.vmps_split_info(h, C.byref(nmid), C.byref(disc), C.byref(nb1), C.byref(sz1), C.byref(nb2),
+                                    C.byref(sz2)))
+        m, b1, b2 = nmid.value, nb1.value, nb2.value
+        qmid = np.zeros((max(m, 1), nq), np.int32)
+        dm = np.zeros(max(m, 1), np.int64)
+        t1 = dict(leg=np.zeros(max(b1, 1), np.int32), qin=np.zeros((max(b1, 1), nq), np.int32),
+                  qout=np.zeros((max(b1, 1), nq), np.int32), rows=np.zeros(max(b1, 1), np.int64),
+                  cols=np.zeros(max(b1, 1), np.int64), data=np.zeros(max(sz1.value, 1)))
+        t2 = dict(leg=np.zeros(max(b2, 1), np.int32), qin=np.zeros((max(b2, 1), nq), np.int32),
+                  qout=np.zeros((max(b2, 1), nq), np.int32), rows=np.zeros(max(b2, 1), np.int64),
+                  cols=np.zeros(max(b2, 1), np.int64), data=np.zeros(max(sz2.value, 1)))
+        ptr = lambda x, t: x.ctypes.data_as(t)
+        N.check(lib.vmps_split_get(h, ptr(qmid, N.i32p), ptr(dm, N.i64p),
+                                   *[ptr(t1[k], N.i32p) for k in ("leg", "qin", "qout")],
+                                   ptr(t1["rows"], N.i64p), ptr(t1["cols"], N.i64p), ptr(t1["data"], N.f64p),
+                                   *[ptr(t2[k], N.i32p) for k in ("leg", "qin", "qout")],
+                                   ptr(t2["rows"], N.i64p), ptr(t2["cols"], N.i64p), ptr(t2["data"], N.f64p)))
+    finally:
+        lib.vmps_split_destroy(h)
+    dmid = {tuple(int(x) for x in qmid[i]): int(dm[i]) for i in range(m)}
+
+    def blocks(t, n, size):
+        return Blocks(nq, t["qin"][:n], t["qout"][:n], t["leg"][:n], t["rows"][:n], t["cols"][:n],
+                      data=t["data"][:size])
+    return blocks(t1, b1, sz1.value), blocks(t2, b2, sz2.value), disc.value, dmid
+
+
 def split_two_site(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move="right", eps_svd=1e-14, pool=None,
-                   factor="eigh"):
+                   factor="eigh", native=True):
     """Truncated SVD of a two-site tensor back into two site tensors (abelian QNs):
     split_AA2 with Biped::truncateSVD (tensors/DmrgContractions.h:2461-2631,
     tensors/Biped.h:744-932).  For every middle QN qmid the matrix
@@ -378,7 +441,14 @@ def split_two_site(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move="right", e
     Returns A1, A2, the discarded weight and the middle bond basis {qmid: dim}.
     `pool` (hostla.SectorPool) runs the sector factorisations in parallel; `factor`:
     "eigh" (Gram matrix, default) or "svd".  Either way the orthonormal factor's
-    columns are the singular vectors for the sweep direction."""
+    columns are the singular vectors for the sweep direction.  native=True (with
+    "eigh") runs the whole split in the native library (vmps_two_site_split) on
+    the pool's thread count when numpy's LAPACK can be bound to it."""
+    if native and factor == "eigh":
+        from .hostla import native_lapack
+        if native_lapack():
+            return _split_native(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move, eps_svd,
+                                 pool.threads if pool is not None else 1)
     # each two-site block (s13, qin, qout) is one (s1, s3) pair (abelian): scatter the
     # blocks into their middle-QN sector matrices in one pass over the blocks
     pair_of = {}
