@@ -213,6 +213,24 @@ def sweep_bench(ctx, args, with_cpu=True):
             two[tag] = dict(summary(r), truncation=r["truncation"], max_bond_dim=r["max_bond_dim"])
         two["sweep_speedup"] = two["fp64"]["s_per_sweep"][0] / two["split"]["s_per_sweep"][0]
         out["hubbard_L64_D1024_two_site"] = two
+    if args.D >= 4096 and not args.no_window:
+        # two-site DMRG at D=4096: a window of bonds around the middle of the chain
+        # (4 bonds to the right and back, 8 two-site steps), in each precision from
+        # the same seeded MPS; a full sweep at this D is 126 such steps
+        from vmps_gb300.dmrg import dmrg2
+        model = models.hubbard_u1xu1(64, t=1.0, U=4.0)
+        lo, width = 31, 4
+        mps0 = RandomMPS(model, (64, 0), 4096, seed=args.seed, profile="gaussian",
+                         sigma=[2.5, 2.5]).canonicalize(lo, lo + 1)
+        win = {"window": [lo, lo + width], "steps": 2 * width, "Dmax": 4096,
+               "tolerances": dict(refine_iters=3, tol_eigval=1e-10, tol_state=1e-6)}
+        for tag, prec, kw in (("split", args.precision, dict(refine_iters=3)), ("fp64", "fp64", {})):
+            r = dmrg2(ctx, model, copy.deepcopy(mps0), n_sweeps=1, Dmax=4096, precision=prec,
+                      tol_eigval=1e-10, tol_state=1e-6, window=(lo, lo + width), **kw)
+            win[tag] = dict(summary(r), s_per_step=r["sweep_times"][0] / (2 * width), truncation=r["truncation"])
+        win["E_rel_diff"] = abs(win["split"]["E"][-1] - win["fp64"]["E"][-1]) / abs(win["fp64"]["E"][-1])
+        win["step_speedup"] = win["fp64"]["s_per_step"] / win["split"]["s_per_step"]
+        out["hubbard_L64_D4096_two_site_window"] = win
     return out
 
 
@@ -417,6 +435,7 @@ def main():
     ap.add_argument("--no-chebyshev", action="store_true")
     ap.add_argument("--no-su2", action="store_true")
     ap.add_argument("--no-vumps", action="store_true")
+    ap.add_argument("--no-window", action="store_true", help="skip the D=4096 two-site window")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 

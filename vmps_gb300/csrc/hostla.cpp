@@ -52,6 +52,14 @@ typedef void (*dsyevd_fn)(const char*, const char*, const lint*, double*, const 
                           lint*, const lint*, lint*, size_t, size_t);
 typedef void (*dsyev_fn)(const char*, const char*, const lint*, double*, const lint*, double*, double*, const lint*,
                          lint*, size_t, size_t);
+typedef void (*dsytrd_fn)(const char*, const lint*, double*, const lint*, double*, double*, double*, double*,
+                          const lint*, lint*, size_t);
+typedef void (*dsterf_fn)(const lint*, double*, double*, lint*);
+typedef void (*dstemr_fn)(const char*, const char*, const lint*, double*, double*, const double*, const double*,
+                          const lint*, const lint*, lint*, double*, double*, const lint*, const lint*, lint*, lint*,
+                          double*, const lint*, lint*, const lint*, lint*, size_t, size_t);
+typedef void (*dormtr_fn)(const char*, const char*, const char*, const lint*, const lint*, const double*, const lint*,
+                          const double*, double*, const lint*, double*, const lint*, lint*, size_t, size_t, size_t);
 typedef void (*dsyrk_fn)(const char*, const char*, const lint*, const lint*, const double*, const double*, const lint*,
                          const double*, double*, const lint*, size_t, size_t);
 typedef void (*dgemm_fn)(const char*, const char*, const lint*, const lint*, const lint*, const double*, const double*,
@@ -60,17 +68,26 @@ typedef void (*dgemm_fn)(const char*, const char*, const lint*, const lint*, con
 struct Lapack {
     dsyevd_fn syevd = nullptr;
     dsyev_fn syev = nullptr;
+    dsytrd_fn sytrd = nullptr;
+    dsterf_fn sterf = nullptr;
+    dstemr_fn stemr = nullptr;
+    dormtr_fn ormtr = nullptr;
     dsyrk_fn syrk = nullptr;
     dgemm_fn gemm = nullptr;
-    bool ok() const { return syevd && syev && syrk && gemm; }
+    bool ok() const { return syevd && syev && sytrd && sterf && stemr && ormtr && syrk && gemm; }
 };
 
-// Gram matrices of at least this order go to dsyevd (divide and conquer), smaller
-// ones to dsyev (QR iteration).  On the 16 Grace cores concurrent dsyevd calls
-// contend inside OpenBLAS's level-3 kernels: an order-64 call took 0.28 ms alone
-// and 2.1 ms with 16 threads busy, where dsyev went from 0.40 to 1.0 ms; at order
-// 178 dsyevd still gives the higher throughput.
-constexpr int64_t kSyevdMin = 128;
+// Gram matrices below order kSelectMin get their full eigensystem at once: QR
+// iteration (dsyev) below kSyevdMin, divide and conquer (dsyevd) above.  Larger
+// ones are reduced to tridiagonal form first; after the truncation only the kept
+// eigenvectors are computed (dstemr) and back-transformed (dormtr).  In the
+// two-site split about a quarter of each large sector is kept (rank of the middle
+// bond), and on the 16 Grace cores concurrent dsyevd calls contend inside
+// OpenBLAS's level-3 kernels: an order-64 dsyevd took 0.28 ms alone and 2.1 ms
+// with 16 threads busy, where dsyev went from 0.40 to 1.0 ms.  Measured per
+// D=1024 bond (sectors up to order 178): 7.8 ms with full eigensystems against
+// 9.0 ms selected; per D=4096 bond (up to 772): 0.114 s against 0.106 s.
+constexpr int64_t kSyevdMin = 128, kSelectMin = 256;
 Lapack g_lapack;
 std::mutex g_lapack_mu;
 
@@ -107,48 +124,128 @@ struct Sector {
     uint64_t key = 0;
     int64_t rows = 0, cols = 0;
     std::vector<double> M;        // rows x cols, column-major
-    std::vector<double> S;        // singular values, descending (min(rows, cols))
-    std::vector<double> Q;        // eigenvectors of the Gram matrix, columns in S's order (n x n)
     int64_t n = 0;                // Gram matrix order
+    std::vector<double> G;        // Householder reflectors of the tridiagonal reduction (n x n)
+    std::vector<double> tau, d, e;
+    std::vector<double> S;        // singular values, descending (min(rows, cols))
+    std::vector<double> Q;        // eigenvectors of the Gram matrix, descending (n x n, then n x kept)
+    bool full = false;            // Q holds the full eigensystem (small sectors)
     int64_t kept = 0;
     std::string err;
 };
 
-// eigendecomposition of the sector's Gram matrix (move right: rows x rows, else cols x cols)
-void factor(Sector& s, bool right) {
-    const Lapack& L = g_lapack;
-    const lint r = s.rows, c = s.cols;
-    const lint n = right ? r : c, k = right ? c : r;
-    s.n = n;
-    std::vector<double> G((size_t)n * n, 0.0);
+// Gram matrix of a sector (move right: M M^T, rows x rows; else M^T M), lower triangle
+void gram(Sector& s, bool right, std::vector<double>& G) {
+    const lint r = s.rows, n = s.n, k = right ? s.cols : s.rows;
     const double one = 1.0, zero = 0.0;
-    // lower triangle of M M^T ('N') or M^T M ('T')
-    L.syrk("L", right ? "N" : "T", &n, &k, &one, s.M.data(), &r, &zero, G.data(), &n, 1, 1);
-    std::vector<double> w((size_t)n);
-    lint info = 0;
-    if (n >= kSyevdMin) {
-        const lint lwork = 1 + 6 * n + 2 * n * n, liwork = 3 + 5 * n;
-        std::vector<double> work((size_t)lwork);
-        std::vector<lint> iwork((size_t)liwork);
-        L.syevd("V", "L", &n, G.data(), &n, w.data(), work.data(), &lwork, iwork.data(), &liwork, &info, 1, 1);
-    } else {
-        const lint lwork = std::max<lint>(1, 66 * n);   // (block size + 2) n
-        std::vector<double> work((size_t)lwork);
-        L.syev("V", "L", &n, G.data(), &n, w.data(), work.data(), &lwork, &info, 1, 1);
-    }
-    if (info != 0) {
-        s.err = "symmetric eigensolver failed (info " + std::to_string(info) + ")";
+    G.assign((size_t)(n * n), 0.0);
+    g_lapack.syrk("L", right ? "N" : "T", &n, &k, &one, s.M.data(), &r, &zero, G.data(), &n, 1, 1);
+}
+
+// values pass: tridiagonal reduction of the Gram matrix (kept for the vectors
+// pass) and all its eigenvalues; S = their square roots, descending
+void factor_values(Sector& s, bool right) {
+    const Lapack& L = g_lapack;
+    const lint n = right ? s.rows : s.cols;
+    s.n = n;
+    gram(s, right, s.G);
+    if (n < kSelectMin) {   // the full eigensystem now
+        std::vector<double> w((size_t)n);
+        lint info = 0;
+        if (n >= kSyevdMin) {
+            const lint lwork = 1 + 6 * n + 2 * n * n, liwork = 3 + 5 * n;
+            std::vector<double> work((size_t)lwork);
+            std::vector<lint> iwork((size_t)liwork);
+            L.syevd("V", "L", &n, s.G.data(), &n, w.data(), work.data(), &lwork, iwork.data(), &liwork, &info, 1, 1);
+        } else {
+            const lint lwork = std::max<lint>(1, 66 * n);   // (block size + 2) n
+            std::vector<double> work((size_t)lwork);
+            L.syev("V", "L", &n, s.G.data(), &n, w.data(), work.data(), &lwork, &info, 1, 1);
+        }
+        if (info != 0) {
+            s.err = "symmetric eigensolver failed (info " + std::to_string(info) + ")";
+            return;
+        }
+        const int64_t m = std::min(s.rows, s.cols);
+        s.S.resize((size_t)m);
+        s.Q.resize((size_t)(n * n));
+        for (int64_t j = 0; j < n; ++j) {
+            const int64_t src = n - 1 - j;
+            std::memcpy(s.Q.data() + (size_t)(j * n), s.G.data() + (size_t)(src * n), sizeof(double) * (size_t)n);
+            if (j < m) s.S[(size_t)j] = std::sqrt(std::max(w[(size_t)src], 0.0));
+        }
+        std::vector<double>().swap(s.G);
+        s.full = true;
         return;
     }
-    // descending order, min(rows, cols) values
-    const int64_t m = std::min(r, c);
-    s.S.resize((size_t)m);
-    s.Q.resize((size_t)n * n);
-    for (int64_t j = 0; j < n; ++j) {
-        const int64_t src = n - 1 - j;
-        std::memcpy(s.Q.data() + (size_t)j * n, G.data() + (size_t)src * n, sizeof(double) * (size_t)n);
-        if (j < m) s.S[(size_t)j] = std::sqrt(std::max(w[(size_t)src], 0.0));
+    s.d.resize((size_t)n);
+    s.e.resize((size_t)std::max<lint>(n, 1));
+    s.tau.resize((size_t)std::max<lint>(n, 1));
+    const lint lwork = 64 * std::max<lint>(n, 1);
+    std::vector<double> work((size_t)lwork);
+    lint info = 0;
+    L.sytrd("L", &n, s.G.data(), &n, s.d.data(), s.e.data(), s.tau.data(), work.data(), &lwork, &info, 1);
+    if (info != 0) {
+        s.err = "dsytrd failed (info " + std::to_string(info) + ")";
+        return;
     }
+    std::vector<double> w(s.d), e2(s.e);
+    L.sterf(&n, w.data(), e2.data(), &info);
+    if (info != 0) {
+        s.err = "dsterf failed (info " + std::to_string(info) + ")";
+        return;
+    }
+    const int64_t m = std::min(s.rows, s.cols);
+    s.S.resize((size_t)m);
+    for (int64_t j = 0; j < m; ++j) s.S[(size_t)j] = std::sqrt(std::max(w[(size_t)(n - 1 - j)], 0.0));
+}
+
+// vectors pass: eigenvectors of the kept (largest) eigenvalues only, from the
+// tridiagonal form (dstemr) and back-transformed with the stored reflectors
+// (dormtr); a dstemr failure falls back to the full eigensystem (dsyevd)
+void factor_vectors(Sector& s, bool right) {
+    const Lapack& L = g_lapack;
+    const lint n = s.n, k = s.kept;
+    if (k <= 0) return;
+    if (s.full) {   // the leading k columns of the full eigensystem
+        s.Q.resize((size_t)(n * k));
+        return;
+    }
+    std::vector<double> d(s.d), e(s.e), w((size_t)n), Z((size_t)(n * k));
+    std::vector<lint> isuppz((size_t)(2 * k));
+    const lint il = n - k + 1, iu = n, lwork = 18 * n, liwork = 10 * n;
+    std::vector<double> work((size_t)lwork);
+    std::vector<lint> iwork((size_t)liwork);
+    lint m = 0, info = 0, tryrac = 1;
+    const double vl = 0, vu = 0;
+    L.stemr("V", "I", &n, d.data(), e.data(), &vl, &vu, &il, &iu, &m, w.data(), Z.data(), &n, &k, isuppz.data(),
+            &tryrac, work.data(), &lwork, iwork.data(), &liwork, &info, 1, 1);
+    if (info == 0 && m == k) {
+        const lint lw2 = 64 * std::max<lint>(k, 1) + 4096;
+        std::vector<double> work2((size_t)lw2);
+        L.ormtr("L", "L", "N", &n, &k, s.G.data(), &n, s.tau.data(), Z.data(), &n, work2.data(), &lw2, &info, 1, 1, 1);
+        if (info != 0) {
+            s.err = "dormtr failed (info " + std::to_string(info) + ")";
+            return;
+        }
+        s.Q.resize((size_t)(n * k));
+        for (lint j = 0; j < k; ++j)   // ascending -> descending
+            std::memcpy(s.Q.data() + (size_t)(j * n), Z.data() + (size_t)((k - 1 - j) * n), sizeof(double) * (size_t)n);
+        return;
+    }
+    std::vector<double> G;
+    gram(s, right, G);
+    const lint lw = 1 + 6 * n + 2 * n * n, liw = 3 + 5 * n;
+    std::vector<double> wk((size_t)lw), wv((size_t)n);
+    std::vector<lint> iwk((size_t)liw);
+    L.syevd("V", "L", &n, G.data(), &n, wv.data(), wk.data(), &lw, iwk.data(), &liw, &info, 1, 1);
+    if (info != 0) {
+        s.err = "dsyevd failed (info " + std::to_string(info) + ")";
+        return;
+    }
+    s.Q.resize((size_t)(n * k));
+    for (lint j = 0; j < k; ++j)
+        std::memcpy(s.Q.data() + (size_t)(j * n), G.data() + (size_t)((n - 1 - j) * n), sizeof(double) * (size_t)n);
 }
 
 }  // namespace
@@ -165,6 +262,24 @@ struct vmps_split_s {
 };
 
 namespace {
+
+// fn(0 .. count-1) on up to `threads` host threads (dynamic: the next index to
+// the next free thread)
+template <typename F>
+void parallel_for(size_t count, int threads, F fn) {
+    const int nt = std::max(1, std::min<int>(threads, (int)count));
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t i = next++; i < count; i = next++) fn(i);
+    };
+    if (nt == 1) {
+        worker();
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) th.emplace_back(worker);
+    for (auto& t : th) t.join();
+}
 
 QN qadd(const QN& a, const int32_t* b, int nq, int sign) {
     QN r = a;
@@ -255,18 +370,7 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
         const int64_t nx = right ? x->rows : x->cols, ny = right ? y->rows : y->cols;
         return nx * nx * (right ? x->cols : x->rows) > ny * ny * (right ? y->cols : y->rows);
     });
-    const int nt = std::max(1, std::min<int>(a->threads, (int)work.size()));
-    std::atomic<size_t> next{0};
-    auto worker = [&]() {
-        for (size_t i = next++; i < work.size(); i = next++) factor(*work[i], right);
-    };
-    if (nt == 1) {
-        worker();
-    } else {
-        std::vector<std::thread> th;
-        for (int t = 0; t < nt; ++t) th.emplace_back(worker);
-        for (auto& t : th) t.join();
-    }
+    parallel_for(work.size(), a->threads, [&](size_t i) { factor_values(*work[i], right); });
     for (Sector* s : order)
         if (!s->err.empty()) throw std::runtime_error(s->err);
     // global truncation: the Dmax largest values above eps_svd * max; ties at the
@@ -306,38 +410,44 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
     std::vector<Sector*> ks;   // kept sectors, in QN order
     std::unordered_map<QKey, size_t> kidx;
     for (Sector* s : order)
+        if (s->kept == 0) {   // nothing of this sector is kept
+            std::vector<double>().swap(s->G);
+            std::vector<double>().swap(s->Q);
+            std::vector<double>().swap(s->M);
+        }
+    for (Sector* s : order)
         if (s->kept > 0) {
             kidx[s->key] = ks.size();
             ks.push_back(s);
             out.qmid.push_back(s->q);
             out.dmid.push_back(s->kept);
         }
-    // the non-orthonormal factor: A2 = scale U_k^T Psi (right) or A1 = scale Psi V_k (left)
+    // the kept eigenvectors, then the non-orthonormal factor: A2 = scale U_k^T Psi
+    // (right) or A1 = scale Psi V_k (left), largest sectors first
     const Lapack& L = g_lapack;
-    std::atomic<size_t> next2{0};
+    std::vector<size_t> vorder(ks.size());
+    for (size_t i = 0; i < ks.size(); ++i) vorder[i] = i;
+    std::sort(vorder.begin(), vorder.end(), [&](size_t x, size_t y) {
+        return ks[x]->n * ks[x]->n * ks[x]->kept > ks[y]->n * ks[y]->n * ks[y]->kept;
+    });
     std::vector<std::vector<double>> Fk(ks.size());
-    auto worker2 = [&]() {
-        for (size_t i = next2++; i < ks.size(); i = next2++) {
-            Sector& s = *ks[i];
-            const lint r = s.rows, c = s.cols, k = s.kept, n = s.n;
-            const double zero = 0.0;
-            if (right) {
-                Fk[i].assign((size_t)(k * c), 0.0);   // k x c
-                L.gemm("T", "N", &k, &c, &r, &scale, s.Q.data(), &n, s.M.data(), &r, &zero, Fk[i].data(), &k, 1, 1);
-            } else {
-                Fk[i].assign((size_t)(r * k), 0.0);   // r x k
-                L.gemm("N", "N", &r, &k, &c, &scale, s.M.data(), &r, s.Q.data(), &n, &zero, Fk[i].data(), &r, 1, 1);
-            }
+    parallel_for(ks.size(), a->threads, [&](size_t t) {
+        const size_t i = vorder[t];
+        Sector& s = *ks[i];
+        factor_vectors(s, right);
+        if (!s.err.empty()) return;
+        const lint r = s.rows, c = s.cols, k = s.kept, n = s.n;
+        const double zero = 0.0;
+        if (right) {
+            Fk[i].assign((size_t)(k * c), 0.0);   // k x c
+            L.gemm("T", "N", &k, &c, &r, &scale, s.Q.data(), &n, s.M.data(), &r, &zero, Fk[i].data(), &k, 1, 1);
+        } else {
+            Fk[i].assign((size_t)(r * k), 0.0);   // r x k
+            L.gemm("N", "N", &r, &k, &c, &scale, s.M.data(), &r, s.Q.data(), &n, &zero, Fk[i].data(), &r, 1, 1);
         }
-    };
-    const int nt2 = std::max(1, std::min<int>(a->threads, (int)ks.size()));
-    if (nt2 == 1) {
-        worker2();
-    } else {
-        std::vector<std::thread> th;
-        for (int t = 0; t < nt2; ++t) th.emplace_back(worker2);
-        for (auto& t : th) t.join();
-    }
+    });
+    for (Sector* s : ks)
+        if (!s->err.empty()) throw std::runtime_error(s->err);
     // output sizes first (one allocation per table)
     {
         size_t nb1 = 0, sz1 = 0, nb2 = 0, sz2 = 0;
@@ -424,9 +534,13 @@ extern "C" int vmps_hostla_load(const char* path) {
     Lapack L;
     L.syevd = (dsyevd_fn)find_symbol(h, "dsyevd");
     L.syev = (dsyev_fn)find_symbol(h, "dsyev");
+    L.sytrd = (dsytrd_fn)find_symbol(h, "dsytrd");
+    L.sterf = (dsterf_fn)find_symbol(h, "dsterf");
+    L.stemr = (dstemr_fn)find_symbol(h, "dstemr");
+    L.ormtr = (dormtr_fn)find_symbol(h, "dormtr");
     L.syrk = (dsyrk_fn)find_symbol(h, "dsyrk");
     L.gemm = (dgemm_fn)find_symbol(h, "dgemm");
-    if (!L.ok()) return set_err(VMPS_E_ARG, std::string("no ILP64 dsyevd/dsyev/dsyrk/dgemm in ") + path);
+    if (!L.ok()) return set_err(VMPS_E_ARG, std::string("no ILP64 dsyevd/dsyev/dsytrd/dsterf/dstemr/dormtr/dsyrk/dgemm in ") + path);
     g_lapack = L;
     return VMPS_OK;
 }

@@ -130,7 +130,7 @@ def _env(ctx, sym, side, E, A, W):
 
 
 def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100, tol_eigval=1e-12,
-          tol_state=1e-8, refine_iters=0, eps_svd=1e-14, pool=None, factor="eigh", verbose=False):
+          tol_state=1e-8, refine_iters=0, eps_svd=1e-14, pool=None, factor="eigh", verbose=False, window=None):
     """Two-site DMRG sweeps (DmrgSolver::iteration_two, solvers/DmrgSolver.h:1399-1522): per bond
     (l, l+1) the two-site tensor A[l] A[l+1] (contract_AA2) is the start vector of the Lanczos
     ground state of PivotMatrix2(L[l], R[l+2], W[l], W[l+1]); split_AA2 with a truncated SVD
@@ -140,8 +140,10 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
 
     `mps` must be right-canonical with the gauge centre on site 0.  A sweep is a
     left-to-right pass over bonds 0..L-2 followed by a right-to-left pass over L-2..0.
-    Timers per sweep as in dmrg1; "gauge" holds the two-site contraction and the SVD,
-    whose sectors run on the host cores (`pool`, a hostla.SectorPool; one is made if
+    window=(lo, hi) sweeps bonds lo..hi-1 and back instead (sites < lo left-canonical,
+    sites > lo+1 right-canonical), the steps of a full sweep in that part of the chain.
+    Timers per sweep as in dmrg1; "gauge" holds the two-site contraction ("contract") and
+    the SVD ("split"), whose sectors run on the host cores (`pool`, a hostla.SectorPool; one is made if
     none is given)."""
     sym, L, nq = model.sym, model.L, model.sym.nq
     if sym.nonabelian:
@@ -156,8 +158,13 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     envR = [None] * (L + 1)
     envL[0] = left_vacuum(sym)
     envR[L] = right_target(sym, mps.Qtot)
+    lo, hi = (0, L - 1) if window is None else (int(window[0]), int(window[1]))
+    if not 0 <= lo < hi <= L - 1:
+        raise ValueError("window must satisfy 0 <= lo < hi <= L-1")
     t0 = time.perf_counter()
-    for l in range(L - 1, 1, -1):
+    for l in range(lo):
+        envL[l + 1] = _env(ctx, sym, "L", envL[l], mps.A[l], model.W[l])
+    for l in range(L - 1, lo + 1, -1):
         envR[l] = _env(ctx, sym, "R", envR[l + 1], mps.A[l], model.W[l])
     t_init = time.perf_counter() - t0
     energies, sweep_times, timers, solves, trunc, dims, hxv = [], [], [], [], [], [], 0
@@ -165,10 +172,10 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     clock = time.perf_counter
     for sweep in range(n_sweeps):
         ts = clock()
-        tm = dict(lanczos=0.0, precalc=0.0, gauge=0.0, lr=0.0)
+        tm = dict(lanczos=0.0, precalc=0.0, gauge=0.0, lr=0.0, contract=0.0, split=0.0)
         counts = {}
         disc_max = 0.0
-        for move, bonds in (("right", range(L - 1)), ("left", range(L - 2, -1, -1))):
+        for move, bonds in (("right", range(lo, hi)), ("left", range(hi - 1, lo - 1, -1))):
             for l in bonds:
                 t = clock()
                 A1, A2 = mps.A[l], mps.A[l + 1]
@@ -198,6 +205,8 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
                     envR[l + 1] = _env(ctx, sym, "R", envR[l + 2], A2, model.W[l + 1])
                 t5 = clock()
                 tm["gauge"] += (t1 - t) + (t4 - t3)
+                tm["contract"] += t1 - t
+                tm["split"] += t4 - t3
                 tm["precalc"] += t2 - t1
                 tm["lanczos"] += t3 - t2
                 tm["lr"] += t5 - t4
