@@ -309,12 +309,88 @@ CombinedBasis combine_bases(const Symmetry& sym, const std::vector<QN>& q12, con
 // ===========================================================================
 // 2-site effective Hamiltonian (PivotMatrix2)
 // ===========================================================================
+// Abelian symmetries: every reduction has exactly one result and all coupling
+// coefficients are 1.  The loop nest of build_pivot2 below then visits, for the
+// combined index s1s3, only the L keys whose incoming QN has a two-site block
+// (s1s3, Lin, Lin + q(s1s3)) -- an ordered list made once -- so it produces the
+// same chains in the same order while skipping the keys that produce none.
+static ChainSet build_pivot2_abelian(const Symmetry& sym, const BlockTable& L, const BlockTable& R,
+                                     const MpoView& W12, const MpoView& W34, const BlockTable& V,
+                                     const TripodView& Lv, const TripodView& Rv, const CombinedBasis& cb,
+                                     const BipedsView& Vv) {
+    ChainSet cs;
+    auto add = [&](const QN& a, const QN& b) {
+        QN r = a;
+        for (int i = 0; i < sym.nq; ++i) r.v[i] += b.v[i];
+        return r;
+    };
+    const int nkeys = (int)Lv.keys.size();
+    // per combined index c: (qL, q13) for the keys with a block (c, Lin, Lin + q(c)),
+    // and q24 of (c, Lout, Lout + q(c)) for every key
+    std::vector<std::vector<std::pair<int, int64_t>>> in13((size_t)cb.n);
+    std::vector<std::vector<int64_t>> at24((size_t)cb.n, std::vector<int64_t>((size_t)nkeys, -1));
+    for (int c = 0; c < cb.n; ++c)
+        for (int qL = 0; qL < nkeys; ++qL) {
+            const QN& Lin = Lv.keys[qL].q[0];
+            const QN& Lout = Lv.keys[qL].q[1];
+            const int64_t q13 = Vv.find(c, Lin, add(Lin, cb.q_of[c]));
+            if (q13 >= 0) in13[(size_t)c].push_back({qL, q13});
+            at24[(size_t)c][(size_t)qL] = Vv.find(c, Lout, add(Lout, cb.q_of[c]));
+        }
+    const int n12 = W12.nloc, n34 = W34.nloc;
+    for (int s1 = 0; s1 < n12; ++s1)
+    for (int s2 = 0; s2 < n12; ++s2)
+    for (int k12 = 0; k12 < W12.nop; ++k12) {
+        if (!sym.triangle(W12.qloc[s2], W12.qop[k12], W12.qloc[s1])) continue;
+        for (int s3 = 0; s3 < n34; ++s3)
+        for (int s4 = 0; s4 < n34; ++s4)
+        for (int k34 = 0; k34 < W34.nop; ++k34) {
+            if (!sym.triangle(W34.qloc[s4], W34.qop[k34], W34.qloc[s3])) continue;
+            for (const auto& m13 : cb.index[s1 * n34 + s3])
+            for (const auto& m24 : cb.index[s2 * n34 + s4]) {
+                const int s1s3 = m13.second, s2s4 = m24.second;
+                const auto& t24 = at24[(size_t)s2s4];
+                for (const auto& e13 : in13[(size_t)s1s3]) {
+                    const int qL = e13.first;
+                    const int64_t q13 = e13.second, q24 = t24[(size_t)qL];
+                    if (q24 < 0) continue;
+                    const QN& Lmid = Lv.keys[qL].q[2];
+                    const QN qRout = V.qout[q13], qRin = V.qout[q24];
+                    const QN qW = add(Lmid, W12.qop[k12]);
+                    const auto* nz12 = W12.find(s1, s2, k12, Lmid, qW);
+                    if (!nz12) continue;
+                    const QN qRmid = add(qW, W34.qop[k34]);
+                    const auto* nz34 = W34.find(s3, s4, k34, qW, qRmid);
+                    if (!nz34) continue;
+                    if (!sym.triangle(qRin, qRmid, qRout)) continue;
+                    auto itR = Rv.dict.find(QN3{{qRin, qRout, qRmid}});
+                    if (itR == Rv.dict.end()) continue;
+                    const int qR = itR->second;
+                    cs.n_tasks++;
+                    for (const auto& e12 : *nz12)
+                        for (const auto& e34 : *nz34) {
+                            if (e12.col != e34.row) continue;
+                            const int64_t la = Lv.at(qL, e12.row), rb = Rv.at(qR, e34.col);
+                            if (la < 0 || rb < 0) continue;
+                            cs.n_chains_raw++;
+                            cs.flops_reference += chain_flops((double)L.rows[la], (double)L.cols[la],
+                                                              (double)V.cols[q24], (double)R.cols[rb]);
+                            cs.chains.push_back(Chain{q13, la, q24, rb, e12.val * e34.val});
+                        }
+                }
+            }
+        }
+    }
+    return cs;
+}
+
 ChainSet build_pivot2(const Symmetry& sym, const BlockTable& L, const BlockTable& R, const MpoView& W12,
                       const MpoView& W34, const BlockTable& V) {
     ChainSet cs;
     TripodView Lv = make_tripod_view(L), Rv = make_tripod_view(R);
     CombinedBasis cb = combine_bases(sym, W12.qloc, W34.qloc);
     BipedsView Vv = make_bipeds_view(V, cb.n);
+    if (!sym.nonabelian()) return build_pivot2_abelian(sym, L, R, W12, W34, V, Lv, Rv, cb, Vv);
     const double eps = 2.220446049250313e-16;
     const int n12 = W12.nloc, n34 = W34.nloc;
     for (int s1 = 0; s1 < n12; ++s1)
