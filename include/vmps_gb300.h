@@ -230,6 +230,12 @@ int vmps_lanczos_ground(vmps_pivot* p, double* v, int precision, int max_iter,
 int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* sym, const vmps_blocks* A1, const double* a1,
                            const vmps_blocks* A2, const double* a2, const vmps_blocks* V, double* v,
                            int64_t nprod, const int64_t* prods);
+/* The same with the products found here: for every A1 block (s1, qin, qmid) and A2
+ * block (s3, qmid, qout), the V block (s13_of_pair[s1 * n3 + s3], qin, qout) if V has
+ * it (abelian QNs: each pair of local states is one combined state).            */
+int vmps_two_site_contract_pairs(vmps_ctx* ctx, const vmps_symmetry* sym, const vmps_blocks* A1, const double* a1,
+                                 const vmps_blocks* A2, const double* a2, const vmps_blocks* V, double* v,
+                                 int n1, int n3, const int32_t* s13_of_pair);
 
 /* ---- two-site split on the host cores ----------------------------------------------
  * split_AA2 with Biped::truncateSVD (tensors/DmrgContractions.h:2461-2631,

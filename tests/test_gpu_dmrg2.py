@@ -52,10 +52,32 @@ def test_dmrg2_heisenberg_gpu_matches_oracle_sweep(gpu_ctx):
 
 
 def test_two_site_contraction_on_gpu_matches_host(gpu_ctx):
-    """contract_AA2 as one FP64 grouped GEMM (vmps_two_site_contract) against the host products"""
+    """contract_AA2 as one FP64 grouped GEMM against the host products: with the
+    products found in the library (vmps_two_site_contract_pairs, the path
+    contract_two_sites takes) and with an explicit product list
+    (vmps_two_site_contract); both give the same bits."""
+    import ctypes as C
+    from vmps_gb300 import _native as N
     from vmps_gb300.mps import contract_two_sites
     m = models.hubbard_u1xu1(12)
     mps = RandomMPS(m, (12, 0), 96, seed=9).canonicalize(5, 6)
-    Vh, _ = contract_two_sites(m.sym, mps.A[5], mps.A[6], m.qloc, m.qloc, 2, return_basis=True)
-    Vg, _ = contract_two_sites(m.sym, mps.A[5], mps.A[6], m.qloc, m.qloc, 2, return_basis=True, ctx=gpu_ctx)
+    A1, A2 = mps.A[5], mps.A[6]
+    Vh, comb = contract_two_sites(m.sym, A1, A2, m.qloc, m.qloc, 2, return_basis=True)
+    Vg, _ = contract_two_sites(m.sym, A1, A2, m.qloc, m.qloc, 2, return_basis=True, ctx=gpu_ctx)
     assert np.linalg.norm(Vg.data - Vh.data) <= 1e-14 * np.linalg.norm(Vh.data)
+    prods = []
+    for i in range(A1.n):
+        for j in range(A2.n):
+            if tuple(A1.qout[i]) != tuple(A2.qin[j]):
+                continue
+            s13 = comb["index"][(int(A1.leg[i]), int(A2.leg[j]))][0][1]
+            k = Vh.find(s13, tuple(A1.qin[i]), tuple(A2.qout[j]))
+            if k >= 0:
+                prods.append((k, i, j))
+    tri = np.ascontiguousarray(np.array(prods, dtype=np.int64).reshape(-1, 3))
+    Ve = Vh.like()
+    s_, b1, b2, bv = m.sym.c_struct(), A1.c_struct(), A2.c_struct(), Ve.c_struct()
+    N.check(N.lib().vmps_two_site_contract(gpu_ctx._h, C.byref(s_), C.byref(b1), A1.data_ptr(), C.byref(b2),
+                                           A2.data_ptr(), C.byref(bv), Ve.data_ptr(), len(prods),
+                                           tri.ctypes.data_as(N.i64p)))
+    assert np.array_equal(Ve.data, Vg.data)

@@ -107,6 +107,9 @@ _PROTOS = [
     ("vmps_two_site_contract", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
                                          C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks), f64p, C.c_int64,
                                          i64p]),
+    ("vmps_two_site_contract_pairs", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
+                                               C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks), f64p, C.c_int,
+                                               C.c_int, i32p]),
     ("vmps_hostla_load", C.c_int, [C.c_char_p]),
     ("vmps_two_site_split", C.c_int, [C.POINTER(vmps_split_args), C.POINTER(vmps_blocks), f64p,
                                       C.POINTER(C.c_void_p)]),

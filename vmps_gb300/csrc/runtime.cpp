@@ -116,8 +116,11 @@ struct LzWork {
     unsigned* ctl() const { return (unsigned*)(g() + cap); }
 };
 
+struct TwoSiteScratch;   // device buffers of vmps_two_site_contract*
+
 struct vmps_ctx_s {
     std::unique_ptr<LzWork> lz;   // Lanczos workspace (vmps_lanczos_ground)
+    std::unique_ptr<TwoSiteScratch> two_site;
     std::mutex lz_mu;             // one Lanczos run at a time per context
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -159,6 +162,11 @@ struct DevPhase {
             upload_vec(cta_tiles, ph.cta_tiles, st);
         }
     }
+};
+
+struct TwoSiteScratch {
+    DBuf a1, a2, v, stage, pack;
+    DevPhase phase;
 };
 
 // Host-buffer HxV pipeline: the vector's blocks in contiguous chunks, and each
@@ -1951,26 +1959,25 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
 // contract_AA2 (tensors/DmrgContractions.h:1870-1927, abelian): the two-site
 // tensor V[k] = sum A1[i] * A2[j] over the (k, i, j) products, as one FP64
 // grouped-GEMM launch on padded device copies of the three block tables
-extern "C" int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* A1,
-                                      const double* a1, const vmps_blocks* A2, const double* a2,
-                                      const vmps_blocks* V, double* v, int64_t nprod, const int64_t* prods) {
-    API_BEGIN
-    if (!ctx || !a1 || !a2 || !v || nprod < 0 || (nprod > 0 && !prods)) return set_err(VMPS_E_ARG, "bad argument");
-    require_device(ctx);
-    const Symmetry sym = make_sym(symd);
-    const BlockTable t1 = parse_blocks(sym, A1, false), t2 = parse_blocks(sym, A2, false),
-                     tv = parse_blocks(sym, V, false);
+// V[k] = sum of A1[i] A2[j] over the (k, i, j) products, one FP64 grouped GEMM
+static void two_site_contract(vmps_ctx* ctx, const BlockTable& t1, const double* a1, const BlockTable& t2,
+                              const double* a2, const BlockTable& tv, double* v,
+                              const std::vector<std::array<int64_t, 3>>& pr) {
     const DevLayout d1 = make_dev_layout(t1.rows, t1.cols), d2 = make_dev_layout(t2.rows, t2.cols),
                     dv = make_dev_layout(tv.rows, tv.cols);
-    std::vector<std::array<int64_t, 3>> pr((size_t)nprod);
-    for (int64_t q = 0; q < nprod; ++q) pr[q] = {prods[3 * q], prods[3 * q + 1], prods[3 * q + 2]};
+    for (const auto& t : pr)
+        if (t[0] < 0 || t[0] >= tv.n || t[1] < 0 || t[1] >= t1.n || t[2] < 0 || t[2] >= t2.n)
+            throw std::invalid_argument("product index outside its block table");
     PhasePlan ph = make_product_plan(d1, d2, dv, pr);
     cudaStream_t st = ctx->stream;
-    DBuf g1, g2, gv, stage;
+    // device buffers kept in the context between calls (a sweep makes one call per bond)
+    if (!ctx->two_site) ctx->two_site.reset(new TwoSiteScratch());
+    TwoSiteScratch& S = *ctx->two_site;
+    DBuf &g1 = S.a1, &g2 = S.a2, &gv = S.v, &stage = S.stage;
     upload_blocks_padded(ctx, t1, d1, a1, g1, st);
     upload_blocks_padded(ctx, t2, d2, a2, g2, st);
     gv.alloc((size_t)std::max<int64_t>(dv.total, 1) * 8, st, true);
-    DevPhase dph;
+    DevPhase& dph = S.phase;
     dph.upload(ph, st);
     GGArgs g{};
     g.A = g1.p;
@@ -1983,13 +1990,73 @@ extern "C" int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* symd, 
     g.ntiles = dph.ntiles;
     CK(launch_gg64(g, st));
     if (tv.n > 0) {
-        DBuf pk;
         const auto pb = pack_blocks(tv, dv, nullptr);
-        upload_vec(pk, pb, st);
-        pack_out(ctx, pk, (int)pb.size(), gv.as<double>(), tv.total, stage, v, st);
+        upload_vec(S.pack, pb, st);
+        pack_out(ctx, S.pack, (int)pb.size(), gv.as<double>(), tv.total, stage, v, st);
     }
     CK(cudaStreamSynchronize(st));
+    dph.host = nullptr;
     check_device_error(ctx);
+}
+
+extern "C" int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* A1,
+                                      const double* a1, const vmps_blocks* A2, const double* a2,
+                                      const vmps_blocks* V, double* v, int64_t nprod, const int64_t* prods) {
+    API_BEGIN
+    if (!ctx || !a1 || !a2 || !v || nprod < 0 || (nprod > 0 && !prods)) return set_err(VMPS_E_ARG, "bad argument");
+    require_device(ctx);
+    const Symmetry sym = make_sym(symd);
+    const BlockTable t1 = parse_blocks(sym, A1, false), t2 = parse_blocks(sym, A2, false),
+                     tv = parse_blocks(sym, V, false);
+    std::vector<std::array<int64_t, 3>> pr((size_t)nprod);
+    for (int64_t q = 0; q < nprod; ++q) pr[q] = {prods[3 * q], prods[3 * q + 1], prods[3 * q + 2]};
+    two_site_contract(ctx, t1, a1, t2, a2, tv, v, pr);
+    API_END
+}
+
+extern "C" int vmps_two_site_contract_pairs(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* A1,
+                                            const double* a1, const vmps_blocks* A2, const double* a2,
+                                            const vmps_blocks* V, double* v, int n1, int n3,
+                                            const int32_t* s13_of_pair) {
+    API_BEGIN
+    if (!ctx || !a1 || !a2 || !v || n1 < 1 || n3 < 1 || !s13_of_pair) return set_err(VMPS_E_ARG, "bad argument");
+    require_device(ctx);
+    const Symmetry sym = make_sym(symd);
+    if (sym.nonabelian()) return set_err(VMPS_E_ARG, "the pair form needs abelian quantum numbers");
+    const BlockTable t1 = parse_blocks(sym, A1, false), t2 = parse_blocks(sym, A2, false),
+                     tv = parse_blocks(sym, V, false);
+    // V blocks by (s13, qin, qout); A2 blocks by (s3, qin) in table order
+    std::unordered_map<QN3, int64_t, QNTupleHash<3>> vfind;
+    for (int64_t k = 0; k < tv.n; ++k) {
+        QN leg{};
+        leg.v[0] = tv.leg[k];
+        vfind.emplace(QN3{{leg, tv.qin[k], tv.qout[k]}}, k);
+    }
+    std::unordered_map<QN2, std::vector<int64_t>, QNTupleHash<2>> a2by;
+    for (int64_t j = 0; j < t2.n; ++j) {
+        if (t2.leg[j] >= n3) throw std::invalid_argument("A2 block leg outside the local basis");
+        QN leg{};
+        leg.v[0] = t2.leg[j];
+        a2by[QN2{{leg, t2.qin[j]}}].push_back(j);
+    }
+    std::vector<std::array<int64_t, 3>> pr;
+    for (int64_t i = 0; i < t1.n; ++i) {
+        const int s1 = t1.leg[i];
+        if (s1 >= n1) throw std::invalid_argument("A1 block leg outside the local basis");
+        for (int s3 = 0; s3 < n3; ++s3) {
+            QN leg{};
+            leg.v[0] = s3;
+            auto it = a2by.find(QN2{{leg, t1.qout[i]}});
+            if (it == a2by.end()) continue;
+            QN l13{};
+            l13.v[0] = s13_of_pair[s1 * n3 + s3];
+            for (int64_t j : it->second) {
+                auto kv = vfind.find(QN3{{l13, t1.qin[i], t2.qout[j]}});
+                if (kv != vfind.end()) pr.push_back({kv->second, i, j});
+            }
+        }
+    }
+    two_site_contract(ctx, t1, a1, t2, a2, tv, v, pr);
     API_END
 }
 

@@ -312,6 +312,19 @@ def contract_two_sites(sym, A1, A2, qloc12, qloc34, nq, return_basis=False, pool
     din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
     dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
     V, comb = two_site_layout(sym, qloc12, qloc34, din, dout, nq)
+    if ctx is not None and getattr(ctx, "device", -1) >= 0 and not sym.nonabelian:
+        # the products are found in the native library (vmps_two_site_contract_pairs)
+        from . import _native as N
+        import ctypes as C
+        n1, n3 = len(qloc12), len(qloc34)
+        pair = np.full(n1 * n3, -1, dtype=np.int32)
+        for (s1, s3), lst in comb["index"].items():
+            pair[s1 * n3 + s3] = lst[0][1]
+        s_, b1, b2, bv = sym.c_struct(), A1.c_struct(), A2.c_struct(), V.c_struct()
+        N.check(N.lib().vmps_two_site_contract_pairs(ctx._h, C.byref(s_), C.byref(b1), A1.data_ptr(), C.byref(b2),
+                                                     A2.data_ptr(), C.byref(bv), V.data_ptr(), n1, n3,
+                                                     pair.ctypes.data_as(N.i32p)))
+        return (V, comb) if return_basis else V
     a2 = {}
     for j in range(A2.n):
         a2.setdefault((int(A2.leg[j]), tuple(A2.qin[j])), []).append(j)
