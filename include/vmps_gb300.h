@@ -270,6 +270,16 @@ typedef struct {
     int32_t threads;
 } vmps_split_args;
 typedef struct vmps_split_s vmps_split;
+/* Gauge step of a single-site sweep (Mps::sweepStep with QR, Mps.h; Biped::QR,
+ * tensors/Biped.h): move_right: for every outgoing QN the blocks of A (stacked by
+ * rows in table order) are replaced by Q of their reduced QR, and the blocks of the
+ * right neighbour N with that incoming QN are multiplied by R from the left; otherwise
+ * the LQ form for every incoming QN (blocks side by side, scaled by w[i] when w is not
+ * NULL, the SU(2) weights sqrt(q_out / q_in)), and N's blocks with that outgoing QN
+ * are multiplied by L from the right.  A and N are updated in place; sectors run on
+ * `threads` host threads.  Needs vmps_hostla_load.                                  */
+int  vmps_gauge_step(int nq, int move_right, const vmps_blocks* A, double* a, const double* w,
+                     const vmps_blocks* N, double* n, int threads);
 int  vmps_hostla_load(const char* path);
 int  vmps_two_site_split(const vmps_split_args* args, const vmps_blocks* V, const double* v, vmps_split** out);
 int  vmps_split_info(const vmps_split* s, int* nmid, double* disc, int64_t* nblocks1, int64_t* size1,

@@ -111,3 +111,39 @@ def test_native_split_rejects_bad_leg():
     V.leg[:] = 3
     with pytest.raises(N.VmpsError):
         split_two_site(V, bad, model.qloc, model.qloc, din, dout, 2, 16, native=True)
+
+
+@pytest.mark.parametrize("move", ["right", "left"])
+@pytest.mark.parametrize("kind", ["hubbard", "su2"])
+def test_native_gauge_step_matches_numpy(move, kind):
+    """vmps_gauge_step (QR / LQ per sector and the neighbour's factor) against
+    left/right_normalize with the factor pushed by numpy"""
+    import copy
+    from vmps_gb300.dmrg import _push_left, _push_right
+    from vmps_gb300.mps import gauge_step, left_normalize, right_normalize
+    if not native_lapack():
+        pytest.skip("numpy's bundled OpenBLAS exports no ILP64 LAPACK")
+    if kind == "hubbard":
+        model = models.hubbard_u1xu1(10, t=1.0, U=4.0)
+        mps = RandomMPS(model, (10, 0), 64, seed=4, profile="gaussian", sigma=[2.5, 2.5]).canonicalize(4, 4)
+    else:
+        model = models.heisenberg_su2(10)
+        mps = RandomMPS(model, (1,), 24, seed=4).canonicalize(4, 4)
+    nq, sym = model.sym.nq, mps.sym
+    l = 4
+    nb = l + 1 if move == "right" else l - 1
+    A, N = copy.deepcopy(mps.A[l]), copy.deepcopy(mps.A[nb])
+    if move == "right":
+        Q, R = left_normalize(A, nq, sym=sym)
+        _push_right(N, R)
+    else:
+        Q, Lf = right_normalize(A, nq, sym=sym)
+        _push_left(N, Lf)
+    A2, N2 = copy.deepcopy(mps.A[l]), copy.deepcopy(mps.A[nb])
+    pool = SectorPool(4)
+    try:
+        gauge_step(A2, N2, nq, move, sym=sym, pool=pool)
+    finally:
+        pool.close()
+    assert np.abs(Q.data - A2.data).max() < 1e-13
+    assert np.abs(N.data - N2.data).max() < 1e-12 * np.abs(N.data).max()

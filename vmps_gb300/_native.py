@@ -117,6 +117,8 @@ _PROTOS = [
     ("vmps_split_get", C.c_int, [C.c_void_p, i32p, i64p, i32p, i32p, i32p, i64p, i64p, f64p, i32p, i32p, i32p,
                                  i64p, i64p, f64p]),
     ("vmps_split_destroy", None, [C.c_void_p]),
+    ("vmps_gauge_step", C.c_int, [C.c_int, C.c_int, C.POINTER(vmps_blocks), f64p, f64p, C.POINTER(vmps_blocks),
+                                  f64p, C.c_int]),
     ("vmps_spectral_bounds", C.c_int, [C.c_void_p, f64p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("vmps_chebyshev_moments", C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, f64p,
                                          C.POINTER(vmps_cheb_stats)]),

@@ -60,6 +60,9 @@ typedef void (*dstemr_fn)(const char*, const char*, const lint*, double*, double
                           double*, const lint*, lint*, const lint*, lint*, size_t, size_t);
 typedef void (*dormtr_fn)(const char*, const char*, const char*, const lint*, const lint*, const double*, const lint*,
                           const double*, double*, const lint*, double*, const lint*, lint*, size_t, size_t, size_t);
+typedef void (*dgeqrf_fn)(const lint*, const lint*, double*, const lint*, double*, double*, const lint*, lint*);
+typedef void (*dorgqr_fn)(const lint*, const lint*, const lint*, double*, const lint*, const double*, double*,
+                          const lint*, lint*);
 typedef void (*dsyrk_fn)(const char*, const char*, const lint*, const lint*, const double*, const double*, const lint*,
                          const double*, double*, const lint*, size_t, size_t);
 typedef void (*dgemm_fn)(const char*, const char*, const lint*, const lint*, const lint*, const double*, const double*,
@@ -74,7 +77,9 @@ struct Lapack {
     dormtr_fn ormtr = nullptr;
     dsyrk_fn syrk = nullptr;
     dgemm_fn gemm = nullptr;
-    bool ok() const { return syevd && syev && sytrd && sterf && stemr && ormtr && syrk && gemm; }
+    dgeqrf_fn geqrf = nullptr;   // the QR gauge step
+    dorgqr_fn orgqr = nullptr;
+    bool ok() const { return syevd && syev && sytrd && sterf && stemr && ormtr && syrk && gemm && geqrf && orgqr; }
 };
 
 // Gram matrices below order kSelectMin get their full eigensystem at once: QR
@@ -263,6 +268,10 @@ struct vmps_split_s {
 
 namespace {
 
+// Below this many floating-point operations a call runs on the calling thread:
+// starting host threads costs more than such small sectors (a D=64 sweep).
+constexpr double kParallelMinFlops = 4e6;
+
 // fn(0 .. count-1) on up to `threads` host threads (dynamic: the next index to
 // the next free thread)
 template <typename F>
@@ -370,7 +379,13 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
         const int64_t nx = right ? x->rows : x->cols, ny = right ? y->rows : y->cols;
         return nx * nx * (right ? x->cols : x->rows) > ny * ny * (right ? y->cols : y->rows);
     });
-    parallel_for(work.size(), a->threads, [&](size_t i) { factor_values(*work[i], right); });
+    double work_flops = 0;
+    for (const Sector* s : work) {
+        const double n = (double)(right ? s->rows : s->cols);
+        work_flops += 10.0 * n * n * n;
+    }
+    const int threads = work_flops < kParallelMinFlops ? 1 : a->threads;
+    parallel_for(work.size(), threads, [&](size_t i) { factor_values(*work[i], right); });
     for (Sector* s : order)
         if (!s->err.empty()) throw std::runtime_error(s->err);
     // global truncation: the Dmax largest values above eps_svd * max; ties at the
@@ -431,7 +446,7 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
         return ks[x]->n * ks[x]->n * ks[x]->kept > ks[y]->n * ks[y]->n * ks[y]->kept;
     });
     std::vector<std::vector<double>> Fk(ks.size());
-    parallel_for(ks.size(), a->threads, [&](size_t t) {
+    parallel_for(ks.size(), threads, [&](size_t t) {
         const size_t i = vorder[t];
         Sector& s = *ks[i];
         factor_vectors(s, right);
@@ -525,6 +540,153 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
 
 }  // namespace
 
+namespace {
+
+// Q R of an m x n column-major matrix (m >= n), reduced: a <- Q (m x n), R (n x n, upper)
+void qr_reduced(double* a, lint m, lint n, double* R) {
+    const Lapack& L = g_lapack;
+    std::vector<double> tau((size_t)std::max<lint>(n, 1));
+    lint info = 0, lwork = -1;
+    double wq = 0;
+    L.geqrf(&m, &n, a, &m, tau.data(), &wq, &lwork, &info);   // workspace query
+    lwork = std::max<lint>((lint)wq, std::max<lint>(n, 1));
+    std::vector<double> work((size_t)lwork);
+    L.geqrf(&m, &n, a, &m, tau.data(), work.data(), &lwork, &info);
+    if (info != 0) throw std::runtime_error("dgeqrf failed (info " + std::to_string(info) + ")");
+    for (lint j = 0; j < n; ++j)
+        for (lint i = 0; i < n; ++i) R[j * n + i] = i <= j ? a[j * m + i] : 0.0;
+    lwork = -1;
+    L.orgqr(&m, &n, &n, a, &m, tau.data(), &wq, &lwork, &info);
+    lwork = std::max<lint>((lint)wq, std::max<lint>(n, 1));
+    work.assign((size_t)lwork, 0.0);
+    L.orgqr(&m, &n, &n, a, &m, tau.data(), work.data(), &lwork, &info);
+    if (info != 0) throw std::runtime_error("dorgqr failed (info " + std::to_string(info) + ")");
+}
+
+void run_gauge(int nq, bool right, const vmps_blocks* A, double* a, const double* w, const vmps_blocks* Nb,
+               double* nb, int threads) {
+    const Lapack& L = g_lapack;
+    // sectors of A: blocks sharing qout (right) or qin (left), in order of first appearance
+    std::unordered_map<QKey, size_t> sidx;
+    std::vector<std::vector<int64_t>> members;
+    std::vector<QKey> skey;
+    for (int64_t i = 0; i < A->nblocks; ++i) {
+        const QKey k = qkey(qload((right ? A->qout : A->qin) + (size_t)i * nq, nq), nq);
+        auto it = sidx.find(k);
+        if (it == sidx.end()) {
+            it = sidx.emplace(k, members.size()).first;
+            members.emplace_back();
+            skey.push_back(k);
+        }
+        members[it->second].push_back(i);
+    }
+    const size_t ns = members.size();
+    double work_flops = 0;
+    for (const auto& mb : members) {
+        double m = 0;
+        for (int64_t i : mb) m += (double)(right ? A->rows[i] : A->cols[i]);
+        const double n = (double)(right ? A->cols[mb[0]] : A->rows[mb[0]]);
+        work_flops += 4.0 * m * n * n;
+    }
+    if (work_flops < kParallelMinFlops) threads = 1;
+    std::vector<std::vector<double>> Rf(ns);
+    std::vector<int64_t> rdim(ns, 0);
+    std::vector<std::string> err(ns);
+    parallel_for(ns, threads, [&](size_t q) {
+        const auto& mb = members[q];
+        // right: M = vstack(A_i), m x n with n = the common column count
+        // left:  M^T = vstack((w_i A_i)^T), the LQ of hstack(w_i A_i)
+        int64_t m = 0, n = right ? A->cols[mb[0]] : A->rows[mb[0]];
+        for (int64_t i : mb) {
+            if ((right ? A->cols[i] : A->rows[i]) != n) { err[q] = "blocks of one sector differ in their shared extent"; return; }
+            m += right ? A->rows[i] : A->cols[i];
+        }
+        if (m < n) { err[q] = "sector has fewer rows than columns (no reduced QR of this shape)"; return; }
+        std::vector<double> M((size_t)(m * n));
+        int64_t r0 = 0;
+        for (int64_t i : mb) {
+            const double* src = a + A->offset[i];
+            const int64_t br = A->rows[i], bc = A->cols[i];
+            if (right) {
+                for (int64_t j = 0; j < bc; ++j)
+                    std::memcpy(M.data() + (size_t)(j * m + r0), src + (size_t)(j * br), sizeof(double) * (size_t)br);
+                r0 += br;
+            } else {
+                const double wi = w ? w[i] : 1.0;
+                for (int64_t j = 0; j < bc; ++j)          // row r0 + j of M^T = column j of the block
+                    for (int64_t t = 0; t < br; ++t) M[(size_t)(t * m + r0 + j)] = wi * src[(size_t)(j * br + t)];
+                r0 += bc;
+            }
+        }
+        Rf[q].assign((size_t)(n * n), 0.0);
+        try {
+            qr_reduced(M.data(), m, n, Rf[q].data());
+        } catch (const std::exception& e) {
+            err[q] = e.what();
+            return;
+        }
+        rdim[q] = n;
+        r0 = 0;
+        for (int64_t i : mb) {
+            double* dst = a + A->offset[i];
+            const int64_t br = A->rows[i], bc = A->cols[i];
+            if (right) {
+                for (int64_t j = 0; j < bc; ++j)
+                    std::memcpy(dst + (size_t)(j * br), M.data() + (size_t)(j * m + r0), sizeof(double) * (size_t)br);
+                r0 += br;
+            } else {   // A_i = (Q^T)[:, r0:r0+bc] / w_i
+                const double wi = w ? w[i] : 1.0;
+                for (int64_t j = 0; j < bc; ++j)
+                    for (int64_t t = 0; t < br; ++t) dst[(size_t)(j * br + t)] = M[(size_t)(t * m + r0 + j)] / wi;
+                r0 += bc;
+            }
+        }
+    });
+    for (const auto& e : err)
+        if (!e.empty()) throw std::invalid_argument(e);
+    // the neighbour: right: N_i <- R[qin] N_i;  left: N_i <- N_i L[qout], L = R^T
+    std::vector<int64_t> nwork;
+    std::vector<size_t> nsec;
+    for (int64_t i = 0; i < Nb->nblocks; ++i) {
+        const QKey k = qkey(qload((right ? Nb->qin : Nb->qout) + (size_t)i * nq, nq), nq);
+        auto it = sidx.find(k);
+        if (it == sidx.end()) continue;
+        if ((right ? Nb->rows[i] : Nb->cols[i]) != rdim[it->second])
+            throw std::invalid_argument("neighbour block does not match the gauge factor");
+        nwork.push_back(i);
+        nsec.push_back(it->second);
+    }
+    parallel_for(nwork.size(), threads, [&](size_t t) {
+        const int64_t i = nwork[t];
+        const std::vector<double>& R = Rf[nsec[t]];
+        double* blk = nb + Nb->offset[i];
+        const lint br = Nb->rows[i], bc = Nb->cols[i];
+        std::vector<double> in(blk, blk + (size_t)(br * bc));
+        const double one = 1.0, zero = 0.0;
+        if (right)
+            L.gemm("N", "N", &br, &bc, &br, &one, R.data(), &br, in.data(), &br, &zero, blk, &br, 1, 1);
+        else   // N L with L = R^T
+            L.gemm("N", "T", &br, &bc, &bc, &one, in.data(), &br, R.data(), &bc, &zero, blk, &br, 1, 1);
+    });
+}
+
+}  // namespace
+
+extern "C" int vmps_gauge_step(int nq, int move_right, const vmps_blocks* A, double* a, const double* w,
+                               const vmps_blocks* N, double* n, int threads) {
+    if (nq < 1 || nq > 4 || !A || !N || (A->nblocks > 0 && !a) || (N->nblocks > 0 && !n))
+        return set_err(VMPS_E_ARG, "bad argument");
+    if (!g_lapack.ok()) return set_err(VMPS_E_ARG, "host LAPACK not bound (vmps_hostla_load)");
+    try {
+        run_gauge(nq, move_right != 0, A, a, w, N, n, threads);
+    } catch (const std::bad_alloc& e) {
+        return set_err(VMPS_E_NOMEM, e.what());
+    } catch (const std::exception& e) {
+        return set_err(VMPS_E_ARG, e.what());
+    }
+    return VMPS_OK;
+}
+
 extern "C" int vmps_hostla_load(const char* path) {
     std::lock_guard<std::mutex> lock(g_lapack_mu);
     if (g_lapack.ok()) return VMPS_OK;
@@ -538,9 +700,11 @@ extern "C" int vmps_hostla_load(const char* path) {
     L.sterf = (dsterf_fn)find_symbol(h, "dsterf");
     L.stemr = (dstemr_fn)find_symbol(h, "dstemr");
     L.ormtr = (dormtr_fn)find_symbol(h, "dormtr");
+    L.geqrf = (dgeqrf_fn)find_symbol(h, "dgeqrf");
+    L.orgqr = (dorgqr_fn)find_symbol(h, "dorgqr");
     L.syrk = (dsyrk_fn)find_symbol(h, "dsyrk");
     L.gemm = (dgemm_fn)find_symbol(h, "dgemm");
-    if (!L.ok()) return set_err(VMPS_E_ARG, std::string("no ILP64 dsyevd/dsyev/dsytrd/dsterf/dstemr/dormtr/dsyrk/dgemm in ") + path);
+    if (!L.ok()) return set_err(VMPS_E_ARG, std::string("no ILP64 dsyevd/dsyev/dsytrd/dsterf/dstemr/dormtr/dsyrk/dgemm/dgeqrf/dorgqr in ") + path);
     g_lapack = L;
     return VMPS_OK;
 }

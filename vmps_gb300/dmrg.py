@@ -24,7 +24,7 @@ import time
 
 import numpy as np
 
-from .mps import contract_two_sites, left_normalize, right_normalize, split_two_site
+from .mps import contract_two_sites, gauge_step, split_two_site
 from .pivot import EnvUpdate, PivotMatrix1, PivotMatrix2, left_vacuum, right_target
 
 
@@ -55,11 +55,17 @@ def _push_left(A_prev, Lfac):
 
 
 def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigval=1e-12, tol_state=1e-8,
-          refine_iters=0, verbose=False):
+          refine_iters=0, verbose=False, pool=None):
     """Run n_sweeps full sweeps of single-site DMRG; returns energies and timings.
-    `mps` must be right-canonical with the gauge centre on site 0."""
+    `mps` must be right-canonical with the gauge centre on site 0.  The QR / LQ gauge
+    steps run on the host cores (`pool`, a hostla.SectorPool; one is made if none is
+    given)."""
     sym, L = model.sym, model.L
     nq = sym.nq
+    own_pool = pool is None
+    if own_pool:
+        from .hostla import SectorPool
+        pool = SectorPool()
     envL = [None] * (L + 1)
     envR = [None] * (L + 1)
     envL[0] = left_vacuum(sym)
@@ -94,15 +100,13 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
             tm["lanczos"] += t2 - t1
             mps.A[l].data[:] = v
             if right and l < L - 1:
-                mps.A[l], Rf = left_normalize(mps.A[l], nq, sym=mps.sym)
-                _push_right(mps.A[l + 1], Rf)
+                gauge_step(mps.A[l], mps.A[l + 1], nq, "right", sym=mps.sym, pool=pool)
                 t3 = clock()
                 e = EnvUpdate(ctx, sym, "L", envL[l], mps.A[l], model.W[l], mps.A[l])
                 envL[l + 1] = e.run(envL[l], mps.A[l], mps.A[l])
                 e.close()
             elif not right and l > 0:
-                mps.A[l], Lf = right_normalize(mps.A[l], nq, sym=mps.sym)
-                _push_left(mps.A[l - 1], Lf)
+                gauge_step(mps.A[l], mps.A[l - 1], nq, "left", sym=mps.sym, pool=pool)
                 t3 = clock()
                 e = EnvUpdate(ctx, sym, "R", envR[l + 1], mps.A[l], model.W[l], mps.A[l])
                 envR[l] = e.run(envR[l + 1], mps.A[l], mps.A[l])
@@ -118,6 +122,8 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
         energies.append(E)
         if verbose:
             print(f"sweep {sweep}: E = {E:.14f}  ({sweep_times[-1]:.2f} s)", flush=True)
+    if own_pool:
+        pool.close()
     return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv,
                        solves=solves)
 

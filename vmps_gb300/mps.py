@@ -172,6 +172,40 @@ def left_normalize(A, nq, carry=None, sym=None, pool=None):
     return A, Rs
 
 
+def gauge_step(A, N, nq, move, sym=None, pool=None):
+    """One gauge step of a single-site sweep: move="right" makes A left-orthonormal
+    (QR per outgoing sector) and multiplies the right neighbour N by R; move="left"
+    makes A right-orthonormal (LQ per incoming sector, SU(2) weights as in
+    right_normalize) and multiplies the left neighbour N by L.  A and N are updated
+    in place, in the native library (vmps_gauge_step, sectors on the pool's threads)
+    when numpy's LAPACK can be bound to it, else by left/right_normalize."""
+    from .hostla import native_lapack
+    if native_lapack():
+        import ctypes as C
+        from . import _native as N_
+        w = None
+        if move == "left" and sym is not None and sym.nonabelian:
+            w = np.array([_ortho_weight(sym, tuple(A.qin[i]), tuple(A.qout[i])) for i in range(A.n)])
+        ab, nb = A.c_struct(), N.c_struct()
+        N_.check(N_.lib().vmps_gauge_step(nq, int(move == "right"), C.byref(ab), A.data_ptr(),
+                                          w.ctypes.data_as(N_.f64p) if w is not None else C.cast(None, N_.f64p),
+                                          C.byref(nb), N.data_ptr(), pool.threads if pool is not None else 1))
+        return
+    if move == "right":
+        Q, Rf = left_normalize(A, nq, sym=sym)
+        for i in range(N.n):
+            q = tuple(N.qin[i])
+            if q in Rf:
+                N.block(i)[...] = Rf[q] @ N.block(i)
+    else:
+        Q, Lf = right_normalize(A, nq, sym=sym)
+        for i in range(N.n):
+            q = tuple(N.qout[i])
+            if q in Lf:
+                N.block(i)[...] = N.block(i) @ Lf[q]
+    A.data[:] = Q.data
+
+
 def right_normalize(A, nq, carry=None, sym=None, pool=None):
     """LQ per incoming sector: A -> Q (right-orthonormal), returns (Q, Lfac dict qin->L).
     `carry` (dict qout -> matrix) multiplies the outgoing bond first (A @ carry).
