@@ -201,8 +201,12 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
  * row (E, |r|) is FP64-exact, solves the correction equation and gives the next x.
  * It stops when |r| <= tol_state and |r|^2 / gap <= tol_eigval |E| (gap from the
  * last run's Ritz values); a round that does not halve |r| hands the rest of the
- * budget to FP64 Lanczos steps.  refine_iters counts the FP64 HxVs after the
- * Krylov phase (the probe is one more).
+ * budget to FP64 Lanczos steps.  Where an FP64 HxV costs fewer than ten split
+ * Lanczos steps (a cost model of the two plans, so the choice is the same in every
+ * run) the residual instead drives a Jacobi-Davidson correction inside the split
+ * Krylov space, followed by FP64 Lanczos steps; the environment variable
+ * VMPS_LANCZOS_REFINE = rounds | polish | auto overrides the choice.  refine_iters
+ * counts the FP64 HxVs after the Krylov phase (the probe is one more).
  * Krylov vectors, dots and the tridiagonal solve are FP64 throughout.  v (compact
  * layout) is the start vector on entry and the ground state on exit.
  * max_iter and refine_iters are below 1024.                                     */

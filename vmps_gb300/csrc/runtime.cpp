@@ -569,6 +569,20 @@ static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
     run_phase(dp, 2, ops, st);
 }
 
+// bf16 MMA work a split phase issues: 3 products of M=128 x N=round16(tn) x K per
+// step, K = 16 for steps whose second K16 slice is padding (skipped), else 32
+static double phase_tensor_flops(const PhasePlan& ph) {
+    double f = 0;
+    for (const GTile& t : ph.tiles) {
+        double k = 0;
+        for (int j = t.step0; j < t.step0 + t.nsteps && j < (int)ph.steps.size(); ++j)
+            k += (ph.steps[j].x & 1) ? 16 : kUmmaBK;
+        if (ph.steps.empty()) k = (double)t.nsteps * kUmmaBK;
+        f += k * 3.0 * 2.0 * kUmmaTileM * ((t.tn + 15) / 16 * 16);
+    }
+    return f;
+}
+
 static void fill_stats(const ChainSet& cs, const Plan& p, int prec, vmps_plan_stats* s) {
     std::memset(s, 0, sizeof(*s));
     s->n_tasks = cs.n_tasks;
@@ -591,21 +605,8 @@ static void fill_stats(const ChainSet& cs, const Plan& p, int prec, vmps_plan_st
     s->flops_phase2_unsummed = p.flops_p2_unsummed;
     s->association = p.association;
     if (p.split) {
-        // bf16 MMA work issued: 3 products of M=128 x N=round16(tn) x K per step,
-        // K = 16 for steps whose second K16 slice is padding (skipped), else 32
-        auto tensor = [](const PhasePlan& ph) {
-            double f = 0;
-            for (const GTile& t : ph.tiles) {
-                double k = 0;
-                for (int j = t.step0; j < t.step0 + t.nsteps && j < (int)ph.steps.size(); ++j)
-                    k += (ph.steps[j].x & 1) ? 16 : kUmmaBK;
-                if (ph.steps.empty()) k = (double)t.nsteps * kUmmaBK;
-                f += k * 3.0 * 2.0 * kUmmaTileM * ((t.tn + 15) / 16 * 16);
-            }
-            return f;
-        };
-        s->tensor_flops_phase1 = tensor(p.p1);
-        s->tensor_flops_phase2 = tensor(p.p2);
+        s->tensor_flops_phase1 = phase_tensor_flops(p.p1);
+        s->tensor_flops_phase2 = phase_tensor_flops(p.p2);
     }
 }
 
@@ -1634,8 +1635,23 @@ constexpr double kRoundReduce = 1e-3;
 // split steps and one FP64 HxV where the FP64 steps need several FP64 HxVs.
 constexpr double kRoundMinRatio = 10;
 
+// The ratio comes from a cost model of the plans (not from timings, so that the
+// choice, and with it every result bit, does not depend on the run): GEMM work at
+// the rates the engines reach on GB300 (FP64 DMMA 0.87 TFLOP/s, bf16 tensor work
+// as issued 530 TFLOP/s), the Lanczos step's vector reads and writes at 5 TB/s,
+// and 3 us per launch.
+constexpr double kFp64FlopsPerMs = 0.87e9, kTensorFlopsPerMs = 5.3e11, kStepBytesPerMs = 5.0e9,
+                 kLaunchMs = 0.003;
+double est_ms_fp64_hxv(const Plan& p) { return (p.p1.flops + p.p2.flops) / kFp64FlopsPerMs + 2 * kLaunchMs; }
+// one split Lanczos iteration with a basis of j rows (FP32 vectors): HxV + step kernels
+double est_ms_split_step(const Plan& p, int64_t n, int j) {
+    const double tensor = phase_tensor_flops(p.p1) + phase_tensor_flops(p.p2);
+    const double bytes = 4.0 * (double)n * (2.0 * (j + 1) + 8.0);
+    return tensor / kTensorFlopsPerMs + bytes / kStepBytesPerMs + 8 * kLaunchMs;
+}
+
 // VMPS_LANCZOS_REFINE = rounds | polish pins the refinement; unset or auto
-// chooses by the measured cost ratio
+// chooses by the modelled cost ratio
 int refine_mode() {
     const char* v = std::getenv("VMPS_LANCZOS_REFINE");
     if (!v || !*v || !std::strcmp(v, "auto")) return 0;
@@ -1705,10 +1721,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     if (split_phase) {
         const bool f32 = prec != VMPS_PREC_FP64;
         if (f32) lz_start_f32(W, st);
-        const auto ts0 = std::chrono::steady_clock::now();
         LzResult r1 = lz_run(p, W, prec, max_iter, tol_eigval, tol_state, 0, nullptr, refine ? kSplitStateRel : 0);
-        const double ms_split_step = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ts0)
-                                         .count() / std::max(1, r1.launched);
         account(r1, prec);
         s.iterations = r1.m;
         s.energy_first = r1.theta;
@@ -1717,7 +1730,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
         lz_ritz(p, W, r1.y, x, f32);
         if (refine) {
             // FP64 residual of the split-precision Ritz vector x, then one of two
-            // refinements, whichever the measured cost ratio favours:
+            // refinements, whichever the modelled cost ratio favours:
             //
             // * Rounds (an FP64 HxV costs many split steps).  A round holds x
             //   (FP64, unit norm), its Rayleigh quotient th and residual
@@ -1750,10 +1763,9 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
                 return rn <= tol_state && rn * rn <= tol_eigval * std::max(1.0, std::abs(th)) * gap;
             };
             double th = 0, rn = 0;
-            const auto tr0 = std::chrono::steady_clock::now();
             residual(x, th, rn);
-            const double ms_fp64 =
-                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tr0).count();
+            const double ms_fp64 = est_ms_fp64_hxv(get_plan(p, VMPS_PREC_FP64).plan);
+            const double ms_split_step = est_ms_split_step(get_plan(p, prec).plan, n, std::max(1, r1.m / 2));
             double gap = std::max(0.0, tridiag_second(r1.alpha, r1.beta) - r1.theta);
             bool polish = false;
             e = th;
