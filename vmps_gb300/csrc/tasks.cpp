@@ -544,11 +544,40 @@ ChainSet build_env(const Symmetry& sym, int side, const BlockTable& E, const Blo
         }
         return v[a];
     };
+    // Abelian symmetries: every reduction has one result, so for each s1 only the
+    // E keys with a bra block (s1, ...) can produce chains; they are listed once, in
+    // key order, and the loop below visits those alone (same chains, same order)
+    const bool abelian = !sym.nonabelian();
+    const int nkeys = (int)Ev.keys.size();
+    std::vector<std::vector<int>> bra_keys;   // per s1: E keys with a bra block
+    std::vector<std::vector<int64_t>> ket_at; // per s2 and E key: the ket block or -1
+    if (abelian) {
+        auto add = [&](const QN& a, const QN& b, int sign) {
+            QN r = a;
+            for (int i = 0; i < sym.nq; ++i) r.v[i] += sign * b.v[i];
+            return r;
+        };
+        bra_keys.resize(W.nloc);
+        ket_at.assign(W.nloc, std::vector<int64_t>((size_t)nkeys, -1));
+        for (int s = 0; s < W.nloc; ++s)
+            for (int qE = 0; qE < nkeys; ++qE) {
+                const QN& Ein = Ev.keys[qE].q[0];
+                const QN& Eout = Ev.keys[qE].q[1];
+                const int64_t b = side == VMPS_ENV_LEFT ? Bv.find(s, Ein, add(Ein, W.qloc[s], 1))
+                                                        : Bv.find(s, add(Eout, W.qloc[s], -1), Eout);
+                if (b >= 0) bra_keys[s].push_back(qE);
+                ket_at[s][qE] = side == VMPS_ENV_LEFT ? Kv.find(s, Eout, add(Eout, W.qloc[s], 1))
+                                                      : Kv.find(s, add(Ein, W.qloc[s], -1), Ein);
+            }
+    }
+    std::vector<int> all_keys((size_t)nkeys);
+    for (int q = 0; q < nkeys; ++q) all_keys[(size_t)q] = q;
     for (int s1 = 0; s1 < W.nloc; ++s1)
     for (int s2 = 0; s2 < W.nloc; ++s2)
     for (int k = 0; k < W.nop; ++k) {
         if (!sym.triangle(W.qloc[s2], W.qop[k], W.qloc[s1])) continue;
-        for (int qE = 0; qE < (int)Ev.keys.size(); ++qE) {
+        for (int qE : abelian ? bra_keys[s1] : all_keys) {
+            if (abelian && ket_at[s2][qE] < 0) continue;
             const QN& Ein = Ev.keys[qE].q[0];
             const QN& Eout = Ev.keys[qE].q[1];
             const QN& Emid = Ev.keys[qE].q[2];
