@@ -81,3 +81,28 @@ def test_two_site_contraction_on_gpu_matches_host(gpu_ctx):
                                            A2.data_ptr(), C.byref(bv), Ve.data_ptr(), len(prods),
                                            tri.ctypes.data_as(N.i64p)))
     assert np.array_equal(Ve.data, Vg.data)
+
+
+def test_dmrg2_window(gpu_ctx):
+    """dmrg2(window=(lo, hi)): the window (0, L-1) is the full sweep (same bits), and
+    a window sweep in the middle of a converged MPS (re-centred there) keeps the ED
+    energy; bonds outside the window keep their bases"""
+    L = 6
+    model = models.hubbard_u1xu1(L, t=1.0, U=4.0)
+    mps = RandomMPS(model, (L, 0), 4, seed=5).canonicalize(0, 0)
+    full = dmrg2(gpu_ctx, model, copy.deepcopy(mps), n_sweeps=1, Dmax=64, precision="fp64")
+    win = dmrg2(gpu_ctx, model, copy.deepcopy(mps), n_sweeps=1, Dmax=64, precision="fp64", window=(0, L - 1))
+    assert full["energies"] == win["energies"]
+    with pytest.raises(ValueError):
+        dmrg2(gpu_ctx, model, copy.deepcopy(mps), n_sweeps=1, Dmax=64, window=(3, 3))
+    conv = copy.deepcopy(mps)
+    dmrg2(gpu_ctx, model, conv, n_sweeps=3, Dmax=64, precision="fp64")
+    # after full sweeps the centre is on site 0 (right-canonical); move it to sites (2, 3)
+    centred = copy.deepcopy(conv).canonicalize(2, 3)
+    dims_before = [dict(centred.dims[b]) for b in (1, 5)]
+    r = dmrg2(gpu_ctx, model, centred, n_sweeps=1, Dmax=64, precision="bf16x3", tol_eigval=1e-10,
+              tol_state=1e-7, refine_iters=10, window=(2, 4))
+    H = ed.permute_to_reference(ed.mpo_to_dense(model), model)
+    e_ed = ed.ground_energy(H, _hubbard_sector(L, L, 0))
+    assert abs(r["energies"][-1] - e_ed) < 1e-10 * abs(e_ed), (r, e_ed)
+    assert [dict(centred.dims[b]) for b in (1, 5)] == dims_before
