@@ -147,3 +147,23 @@ def test_native_gauge_step_matches_numpy(move, kind):
         pool.close()
     assert np.abs(Q.data - A2.data).max() < 1e-13
     assert np.abs(N.data - N2.data).max() < 1e-12 * np.abs(N.data).max()
+
+
+def test_native_split_edge_cases():
+    """Dmax = 0 keeps nothing; a two-site tensor without blocks gives empty sites;
+    a sector with a quantum number out of the packed range is refused (host
+    threads report the error to the caller instead of ending the process)"""
+    from vmps_gb300 import _native as N
+    if not native_lapack():
+        pytest.skip("numpy's bundled OpenBLAS exports no ILP64 LAPACK")
+    model, V, comb, din, dout = _case(8, 32, 3, seed=2)
+    a = split_two_site(V, comb, model.qloc, model.qloc, din, dout, 2, 0, native=False)
+    b = split_two_site(V, comb, model.qloc, model.qloc, din, dout, 2, 0, native=True)
+    assert a[3] == b[3] == {} and b[0].n == 0 and b[1].n == 0
+    empty = V.like()
+    empty.data[:] = 0
+    e = split_two_site(empty, comb, model.qloc, model.qloc, din, dout, 2, 16, native=True)
+    assert e[3] == {} and e[2] == 0.0
+    big = {(q[0] + 40000, q[1]): d for q, d in din.items()}
+    with pytest.raises(N.VmpsError):
+        split_two_site(V, comb, model.qloc, model.qloc, big, dout, 2, 16, native=True)

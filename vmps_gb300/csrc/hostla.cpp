@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <exception>
 #include <limits>
 #include <map>
 #include <array>
@@ -274,20 +275,37 @@ constexpr double kParallelMinFlops = 4e6;
 
 // fn(0 .. count-1) on up to `threads` host threads (dynamic: the next index to
 // the next free thread)
+// An exception in fn (an allocation failure, a malformed table) stops the
+// remaining work and is rethrown on the calling thread after all threads joined.
 template <typename F>
 void parallel_for(size_t count, int threads, F fn) {
     const int nt = std::max(1, std::min<int>(threads, (int)count));
     std::atomic<size_t> next{0};
+    std::exception_ptr first;
+    std::mutex mu;
     auto worker = [&]() {
-        for (size_t i = next++; i < count; i = next++) fn(i);
+        try {
+            for (size_t i = next++; i < count; i = next++) fn(i);
+        } catch (...) {
+            std::lock_guard<std::mutex> lock(mu);
+            if (!first) first = std::current_exception();
+            next = count;
+        }
     };
     if (nt == 1) {
         worker();
-        return;
+    } else {
+        std::vector<std::thread> th;
+        try {
+            for (int t = 0; t < nt; ++t) th.emplace_back(worker);
+        } catch (...) {   // no thread could be started: stop the ones that run, report
+            next = count;
+            for (auto& t : th) t.join();
+            throw;
+        }
+        for (auto& t : th) t.join();
     }
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; ++t) th.emplace_back(worker);
-    for (auto& t : th) t.join();
+    if (first) std::rethrow_exception(first);
 }
 
 QN qadd(const QN& a, const int32_t* b, int nq, int sign) {
