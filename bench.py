@@ -238,7 +238,8 @@ def su2_cylinder_bench(ctx, args):
     """Config C3: Hubbard SU(2)xU(1), width-4 cylinder as a 64-site snake, U/t=8, 1/8 hole
     doping (N=56, S=0), MPO w=10, D=2000 multiplets (~5,800 states); the two-site pivot of
     the middle.  Device-resident HxV (CUDA graph, events) in FP64 and split precision, the
-    split error, and the Lanczos ground state of the pivot in both precisions."""
+    split error, the Lanczos ground state of the pivot in both precisions, and one
+    single-site DMRG sweep of the cylinder in each precision."""
     from vmps_gb300.pivot import DeviceVector, PivotMatrix2, time_hxv
     from vmps_gb300.workloads import hubbard_su2xu1_cylinder_two_site
     model, mps, Lenv, Renv, W1, W2, V, info = hubbard_su2xu1_cylinder_two_site(ctx)
@@ -258,7 +259,20 @@ def su2_cylinder_bench(ctx, args):
     e64, _, l64 = H.lanczos(v0, "fp64", max_iter=300, **tol)
     es, _, ls = H.lanczos(v0, args.precision, max_iter=300, refine_iters=4, **tol)
     H.close()
-    return dict(info, n_tasks=st64["n_tasks"], flops_per_hxv=st64["flops_merged"],
+    # single-site DMRG sweep of the cylinder: one sweep in each precision from the same
+    # seeded MPS (D=2000 multiplets, centre on site 0)
+    import copy
+
+    from vmps_gb300.dmrg import dmrg1
+    from vmps_gb300.mps import RandomMPS
+    mps0 = RandomMPS(model, (1, info["N"]), 2000, seed=3, profile="gaussian", sigma=[3.0, 3.0]).canonicalize(0, 0)
+    sweep = {}
+    for tag, prec, kw in (("split", args.precision, dict(refine_iters=10)), ("fp64", "fp64", {})):
+        r = dmrg1(ctx, model, copy.deepcopy(mps0), n_sweeps=1, precision=prec, **tol, **kw)
+        sweep[tag] = {"s_per_sweep": r["sweep_times"], "E": r["energies"], "lanczos": r["solves"],
+                      "timers_s": [{k: round(v, 4) for k, v in t.items()} for t in r["timers"]]}
+    sweep["sweep_speedup"] = sweep["fp64"]["s_per_sweep"][0] / sweep["split"]["s_per_sweep"][0]
+    return dict(info, n_tasks=st64["n_tasks"], flops_per_hxv=st64["flops_merged"], single_site_sweep=sweep,
                 hxv_fp64={"ms": ms64, "per_s": 1e3 / ms64, "tflops": st64["flops_merged"] / ms64 * 1e-9},
                 hxv_split={"ms": mss, "per_s": 1e3 / mss, "tflops_useful": sts["flops_merged"] / mss * 1e-9,
                            "tensor_tflops_issued": (sts["tensor_flops_phase1"] + sts["tensor_flops_phase2"]) /
