@@ -50,7 +50,49 @@ long double log_delta(int a, int b, int c) {   // 2j arguments, triangle already
 }
 }  // namespace
 
+// Memoised per thread: the builders ask for the same few symbols once per task
+// (thousands of times per pivot), and each evaluation is an exp/log-factorial sum
+// (three 6j per term of a 9j).  Arguments (2j) up to 127 pack into one key.
+namespace {
+template <int N>
+bool pack_key(const int (&a)[N], uint64_t& key) {
+    key = 0;
+    for (int i = 0; i < N; ++i) {
+        if (a[i] < 0 || a[i] > 127) return false;
+        key = (key << 7) | (uint64_t)a[i];
+    }
+    return true;
+}
+double coupling_6j_eval(int j1, int j2, int j3, int j4, int j5, int j6);
+double coupling_9j_eval(int j1, int j2, int j3, int j4, int j5, int j6, int j7, int j8, int j9);
+}  // namespace
+
 double coupling_6j(int j1, int j2, int j3, int j4, int j5, int j6) {
+    thread_local std::unordered_map<uint64_t, double> memo;
+    const int a[6] = {j1, j2, j3, j4, j5, j6};
+    uint64_t key;
+    if (!pack_key(a, key)) return coupling_6j_eval(j1, j2, j3, j4, j5, j6);
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+    const double v = coupling_6j_eval(j1, j2, j3, j4, j5, j6);
+    memo.emplace(key, v);
+    return v;
+}
+
+double coupling_9j(int j1, int j2, int j3, int j4, int j5, int j6, int j7, int j8, int j9) {
+    thread_local std::unordered_map<uint64_t, double> memo;
+    const int a[9] = {j1, j2, j3, j4, j5, j6, j7, j8, j9};
+    uint64_t key;
+    if (!pack_key(a, key)) return coupling_9j_eval(j1, j2, j3, j4, j5, j6, j7, j8, j9);
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+    const double v = coupling_9j_eval(j1, j2, j3, j4, j5, j6, j7, j8, j9);
+    memo.emplace(key, v);
+    return v;
+}
+
+namespace {
+double coupling_6j_eval(int j1, int j2, int j3, int j4, int j5, int j6) {
     if (!tri2(j1, j2, j3) || !tri2(j1, j5, j6) || !tri2(j4, j2, j6) || !tri2(j4, j5, j3)) return 0.0;
     const auto& f = facts().lf;
     const int a1 = (j1 + j2 + j3) / 2, a2 = (j1 + j5 + j6) / 2, a3 = (j4 + j2 + j6) / 2, a4 = (j4 + j5 + j3) / 2;
@@ -67,7 +109,7 @@ double coupling_6j(int j1, int j2, int j3, int j4, int j5, int j6) {
     return (double)sum;
 }
 
-double coupling_9j(int j1, int j2, int j3, int j4, int j5, int j6, int j7, int j8, int j9) {
+double coupling_9j_eval(int j1, int j2, int j3, int j4, int j5, int j6, int j7, int j8, int j9) {
     // {j1 j2 j3; j4 j5 j6; j7 j8 j9} = sum_x (-1)^{2x} (2x+1) {j1 j4 j7; j8 j9 x}{j2 j5 j8; j4 x j6}{j3 j6 j9; x j1 j2}
     if (!tri2(j1, j2, j3) || !tri2(j4, j5, j6) || !tri2(j7, j8, j9) || !tri2(j1, j4, j7) || !tri2(j2, j5, j8) ||
         !tri2(j3, j6, j9))
@@ -82,6 +124,7 @@ double coupling_9j(int j1, int j2, int j3, int j4, int j5, int j6, int j7, int j
     }
     return (double)sum;
 }
+}  // namespace
 
 // ===========================================================================
 // parsing
