@@ -9,6 +9,8 @@ from vmps_gb300 import models
 from vmps_gb300.hostla import SectorPool, native_lapack
 from vmps_gb300.mps import RandomMPS, contract_two_sites, split_two_site
 
+VMPS_E_ARG = -1   # include/vmps_gb300.h
+
 
 def _case(L, D, l, seed, kind="hubbard", sigma=1.5):
     if kind == "hubbard":
@@ -167,3 +169,34 @@ def test_native_split_edge_cases():
     big = {(q[0] + 40000, q[1]): d for q, d in din.items()}
     with pytest.raises(N.VmpsError):
         split_two_site(V, comb, model.qloc, model.qloc, big, dout, 2, 16, native=True)
+
+
+def test_host_routines_refuse_bad_tables():
+    """malformed tables or arguments come back as VMPS_E_ARG (-1), nothing is read"""
+    import ctypes as C
+    from vmps_gb300 import _native as N
+    from vmps_gb300.blocks import Blocks
+    if not native_lapack():
+        pytest.skip("numpy's bundled OpenBLAS exports no ILP64 LAPACK")
+    lib = N.lib()
+    A = Blocks(1, [[0]], [[1]], [0], [3], [2])
+    bad = Blocks(1, [[0]], [[1]], [0], [3], [2])
+    bad.rows[0] = 0                      # non-positive shape
+    ab, bb = A.c_struct(), bad.c_struct()
+    rc = lib.vmps_gauge_step(1, 1, C.byref(bb), bad.data_ptr(), C.cast(None, N.f64p), C.byref(ab), A.data_ptr(), 1)
+    assert rc == VMPS_E_ARG
+    nul = N.vmps_blocks()
+    nul.nblocks = 1                       # arrays left null
+    rc = lib.vmps_gauge_step(1, 1, C.byref(nul), A.data_ptr(), C.cast(None, N.f64p), C.byref(ab), A.data_ptr(), 1)
+    assert rc == VMPS_E_ARG
+    args = N.vmps_split_args()
+    q = np.zeros(1, np.int32)
+    pair = np.zeros(1, np.int32)
+    args.nq, args.n1, args.n3, args.n13 = 1, 1, 1, 1
+    args.qloc1 = args.qloc3 = q.ctypes.data_as(N.i32p)
+    args.pair1 = args.pair3 = pair.ctypes.data_as(N.i32p)
+    args.nin = 1                          # a left basis without its arrays
+    args.dmax, args.threads = 4, 1
+    h = C.c_void_p()
+    rc = lib.vmps_two_site_split(C.byref(args), C.byref(ab), A.data_ptr(), C.byref(h))
+    assert rc == VMPS_E_ARG and not h.value

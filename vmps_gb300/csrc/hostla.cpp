@@ -48,6 +48,16 @@ int set_err(int code, const std::string& msg) {
     return code;
 }
 
+// a block table the host routines may read: arrays present, shapes positive, offsets non-negative
+bool table_ok(const vmps_blocks* t) {
+    if (t->nblocks < 0) return false;
+    if (t->nblocks == 0) return true;
+    if (!t->qin || !t->qout || !t->leg || !t->rows || !t->cols || !t->offset) return false;
+    for (int64_t i = 0; i < t->nblocks; ++i)
+        if (t->rows[i] <= 0 || t->cols[i] <= 0 || t->offset[i] < 0 || t->leg[i] < 0) return false;
+    return true;
+}
+
 using lint = int64_t;   // ILP64 LAPACK integers
 typedef void (*dsyevd_fn)(const char*, const char*, const lint*, double*, const lint*, double*, double*, const lint*,
                           lint*, const lint*, lint*, size_t, size_t);
@@ -694,6 +704,7 @@ extern "C" int vmps_gauge_step(int nq, int move_right, const vmps_blocks* A, dou
                                const vmps_blocks* N, double* n, int threads) {
     if (nq < 1 || nq > 4 || !A || !N || (A->nblocks > 0 && !a) || (N->nblocks > 0 && !n))
         return set_err(VMPS_E_ARG, "bad argument");
+    if (!table_ok(A) || !table_ok(N)) return set_err(VMPS_E_ARG, "block table with null arrays or non-positive shapes");
     if (!g_lapack.ok()) return set_err(VMPS_E_ARG, "host LAPACK not bound (vmps_hostla_load)");
     try {
         run_gauge(nq, move_right != 0, A, a, w, N, n, threads);
@@ -731,8 +742,14 @@ extern "C" int vmps_two_site_split(const vmps_split_args* a, const vmps_blocks* 
                                    vmps_split** out) {
     if (!a || !V || !out || (V->nblocks > 0 && !Vdata)) return set_err(VMPS_E_ARG, "bad argument");
     if (a->nq < 1 || a->nq > 4 || a->n1 < 1 || a->n3 < 1 || a->n13 < 1 || !a->pair1 || !a->pair3 ||
-        !a->qloc1 || !a->qloc3 || a->nin < 0 || a->nout < 0 || a->dmax < 0)
+        !a->qloc1 || !a->qloc3 || a->nin < 0 || a->nout < 0 || a->dmax < 0 ||
+        (a->nin > 0 && (!a->qin || !a->din)) || (a->nout > 0 && (!a->qout || !a->dout)))
         return set_err(VMPS_E_ARG, "bad split arguments");
+    if (!table_ok(V)) return set_err(VMPS_E_ARG, "two-site table with null arrays or non-positive shapes");
+    for (int i = 0; i < a->nin; ++i)
+        if (a->din[i] < 0) return set_err(VMPS_E_ARG, "negative bond dimension");
+    for (int i = 0; i < a->nout; ++i)
+        if (a->dout[i] < 0) return set_err(VMPS_E_ARG, "negative bond dimension");
     for (int i = 0; i < a->n13; ++i)
         if (a->pair1[i] < 0 || a->pair1[i] >= a->n1 || a->pair3[i] < 0 || a->pair3[i] >= a->n3)
             return set_err(VMPS_E_ARG, "combined index outside the local bases");
