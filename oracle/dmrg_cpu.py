@@ -114,8 +114,9 @@ def dmrg2_cpu(model, mps, n_sweeps=2, Dmax=None, max_iter=100, tol_eigval=1e-12,
                 op = OraclePivot(2, nq, envL[l], envR[l + 2], V, model.W[l], model.W[l + 1])
                 E, v, _ = lanczos_np(op.hxv, V.data.copy(), max_iter, tol_eigval, tol_state)
                 V.data[:] = v
+                # the numpy restatement of the split (not the native library's routine)
                 A1, A2, _, dmid = split_two_site(V, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
-                                                 eps_svd=eps_svd)
+                                                 eps_svd=eps_svd, native=False)
                 mps.A[l], mps.A[l + 1] = A1, A2
                 mps.dims[l + 1] = dmid
                 if move == "right":
