@@ -4,7 +4,8 @@ A frozen site is the middle of a chain: a random MPS (N(0,1) blocks, QR/LQ
 normalised towards the pivot), its left and right environments built with the
 engine's own contract_L / contract_R on the GPU, the MPO tensors of the pivot
 sites, and the pivot vector layout.  The reference publishes no benchmark data;
-these inputs stand in for the BASELINE configurations with their shapes.
+these inputs stand in for its benchmark configurations (Heisenberg chain, Hubbard
+chain at D=1024 / 4096, SU(2)xU(1) Hubbard cylinder, ...) with their shapes.
 """
 from __future__ import annotations
 
