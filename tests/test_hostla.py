@@ -200,3 +200,30 @@ def test_host_routines_refuse_bad_tables():
     h = C.c_void_p()
     rc = lib.vmps_two_site_split(C.byref(args), C.byref(ab), A.data_ptr(), C.byref(h))
     assert rc == VMPS_E_ARG and not h.value
+
+
+@pytest.mark.parametrize("kind,D,l", [("hubbard", 256, 5), ("heisenberg", 64, 6), ("su2", 32, 6)])
+def test_two_site_layout_matches_direct_loop(kind, D, l):
+    """two_site_layout (pairs made once per merged QN) gives the table of the direct
+    loop over (s1s3, sorted qin, fused qout), block for block"""
+    from vmps_gb300.mps import combined_basis, two_site_layout
+    if kind == "hubbard":
+        model, Q = models.hubbard_u1xu1(12, t=1.0, U=4.0), (12, 0)
+    elif kind == "heisenberg":
+        model, Q = models.heisenberg_u1(14), (0,)
+    else:
+        model, Q = models.heisenberg_su2(14), (1,)
+    mps = RandomMPS(model, Q, D, seed=2)
+    din, dout = mps.dims[l], mps.dims[l + 2]
+    V, comb = two_site_layout(model.sym, model.qloc, model.qloc, din, dout, model.sym.nq)
+    assert comb == combined_basis(model.sym, model.qloc, model.qloc)
+    ent = []
+    for s13, qm in enumerate(comb["q_of"]):
+        for qin in sorted(din):
+            for qout in model.sym.fuse(qin, qm):
+                if qout in dout:
+                    ent.append((s13, qin, qout, din[qin], dout[qout]))
+    assert V.n == len(ent) > 0
+    for i, (s13, qin, qout, r, c) in enumerate(ent):
+        assert (int(V.leg[i]), tuple(V.qin[i]), tuple(V.qout[i]), int(V.rows[i]), int(V.cols[i])) == \
+            (s13, qin, qout, r, c)

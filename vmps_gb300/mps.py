@@ -281,14 +281,29 @@ def two_site_layout(sym, qloc12, qloc34, din, dout, nq):
     Qbasis::combine (tensors/Qbasis.h:685-798); QNs of combined states in the
     order the combined basis lists them."""
     comb = combined_basis(sym, qloc12, qloc34)
-    ent = []
-    for s13, qm in enumerate(comb["q_of"]):
-        for qin in sorted(din):
-            for qout in sym.fuse(qin, qm):
+    qins = sorted(din)
+    abelian = not sym.nonabelian
+    # the (qin, qout) pairs depend only on the merged QN: made once per distinct one
+    pairs = {}
+    for qm in comb["q_of"]:
+        if qm in pairs:
+            continue
+        lst = []
+        for qin in qins:
+            # abelian: the one fused QN is the sum (Symmetry.fuse gives the same)
+            for qout in ((tuple(a + b for a, b in zip(qin, qm)),) if abelian else sym.fuse(qin, qm)):
                 if qout in dout:
-                    ent.append((s13, qin, qout, din[qin], dout[qout]))
-    return Blocks(nq, [e[1] for e in ent], [e[2] for e in ent], [e[0] for e in ent],
-                  [e[3] for e in ent], [e[4] for e in ent]), comb
+                    lst.append((qin, qout, din[qin], dout[qout]))
+        pairs[qm] = lst
+    qi, qo, leg, rows, cols = [], [], [], [], []
+    for s13, qm in enumerate(comb["q_of"]):
+        for qin, qout, r, c in pairs[qm]:
+            qi.append(qin)
+            qo.append(qout)
+            leg.append(s13)
+            rows.append(r)
+            cols.append(c)
+    return Blocks(nq, qi, qo, leg, rows, cols), comb
 
 
 def combined_basis(sym, q12, q34):
