@@ -147,6 +147,32 @@ def cpu_oracle_hxv_rate(L, R, V, W1, W2, threads, n_hxv, warm=1):
     return n_hxv / dt, dt, oracle.blas_kind()
 
 
+def oracle_check(L, R, V, W1, W2, v0, h64, hsp, e_ref, e64, es, x64, xs):
+    """The engine's results at the bench pivot against the FP64 oracle (CPU
+    restatement of OxV, all host threads): both HxVs of v0, the ground-state energy
+    from the oracle's own Lanczos (numpy three-term recurrence on the oracle's
+    HxV), and the Rayleigh quotient and residual of the engine's returned vectors
+    under the oracle's operator."""
+    import oracle
+    oracle.set_threads(os.cpu_count() or 1)
+    op = oracle.OraclePivot(2, 2, L, R, V, W1, W2)
+    t0 = time.perf_counter()
+    ref = op.hxv(v0)
+    out = {"hxv_fp64_rel_err": float(np.linalg.norm(h64 - ref) / np.linalg.norm(ref)),
+           "hxv_split_rel_err": float(np.linalg.norm(hsp - ref) / np.linalg.norm(ref))}
+    e_or, steps = oracle.lanczos_ground(op.hxv, v0, tol=1e-14)
+    out.update({"E_oracle": e_or, "oracle_lanczos_steps": steps, "oracle_s": round(time.perf_counter() - t0, 1),
+                "E_ref_fp64_rel_err": abs(e_ref - e_or) / abs(e_or),
+                "E_fp64_rel_err": abs(e64 - e_or) / abs(e_or), "E_split_rel_err": abs(es - e_or) / abs(e_or)})
+    for tag, x in (("fp64", x64), ("split", xs)):
+        x = x / np.linalg.norm(x)
+        hx = op.hxv(x)
+        rq = float(x @ hx)
+        out[f"{tag}_vector"] = {"rayleigh_rel_err": abs(rq - e_or) / abs(e_or),
+                                "residual": float(np.linalg.norm(hx - rq * x))}
+    return out
+
+
 def sweep_bench(ctx, args, with_cpu=True):
     """Single-site DMRG sweep times.
 
@@ -395,19 +421,93 @@ def chebyshev_bench(ctx, args):
                                        "n=100": float(err[100]), "n=500": float(err[500]), "n=999": float(err[999])}}
 
 
+def cpu_model():
+    """CPU model string of the host (lscpu's "Model name", else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                             timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def loaded_native_libs():
+    """shared libraries of this repository mapped into the process (from /proc/self/maps)"""
+    libs = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for ln in f:
+                path = ln.split()[-1] if ln.strip() else ""
+                if path.endswith(".so") and path.startswith(ROOT):
+                    libs.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(libs)
+
+
+def workload_config(args, info, world):
+    """The `config` object of the bench line; both arms print the same one.  `l2` says
+    how the timed region avoids L2 reuse: the two-site vectors (in + out) and the
+    environments alone are larger than the 129 MB L2."""
+    n = info["dim_V"]
+    io_bytes = 2 * 8 * n + 8 * (info["env_elems"])
+    return {"workload": f"hubbard_u1xu1_L{args.L}_D{args.D}_two_site_middle", "L": args.L, "D": args.D,
+            "U": 4.0, "seed": args.seed, "D_left": info["D_left"], "sectors": info["sectors_left"], "dim_V": n,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2" if io_bytes > L2_BYTES else "inputs fit L2"}
+
+
+def oracle_two_site_workload(L, D, seed, U=4.0, sigma=2.5):
+    """The frozen two-site pivot of the bench built on the host only: the same seeded
+    MPS (numpy QR/LQ normalisation), environments from the oracle's contract_L /
+    contract_R, the two-site tensor from numpy block products.  No GPU and no
+    engine library is touched."""
+    import oracle
+    from vmps_gb300 import models
+    from vmps_gb300.mps import RandomMPS, contract_two_sites
+    from vmps_gb300.blocks import Blocks
+    model = models.hubbard_u1xu1(L, t=1.0, U=U)
+    site = L // 2 - 1
+    mps = RandomMPS(model, (L, 0), D, seed=seed, profile="gaussian", sigma=[sigma, sigma])
+    mps.canonicalize(site, site + 1)
+    sym, nq = model.sym, model.sym.nq
+    v = sym.vacuum()
+    Lenv = Blocks.from_entries(nq, [(0, v, v, v, np.ones((1, 1)))], tripod=True)
+    for l in range(site):
+        Lenv = oracle.contract_L(nq, Lenv, mps.A[l], model.W[l], mps.A[l])
+    Renv = Blocks.from_entries(nq, [(0, (L, 0), (L, 0), v, np.ones((1, 1)))], tripod=True)
+    for l in range(L - 1, site + 1, -1):
+        Renv = oracle.contract_R(nq, Renv, mps.A[l], model.W[l], mps.A[l])
+    V = contract_two_sites(sym, mps.A[site], mps.A[site + 1], model.qloc, model.qloc, nq)
+    info = dict(D_left=mps.bond_dim(site), sectors_left=len(mps.dims[site]), dim_V=int(V.data.size),
+                env_elems=int(Lenv.data.size + Renv.data.size))
+    return model, Lenv, Renv, model.W[site], model.W[site + 1], V, info
+
+
 def run_reference(args):
-    """CPU restatement of the reference path (the oracle), all host threads."""
+    """CPU restatement of the reference path (the oracle), all host threads.  The
+    inputs are made on the host with numpy and the oracle: this arm loads no GPU
+    code and no engine library."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
     import oracle
-    from vmps_gb300.pivot import Context
-    from vmps_gb300.workloads import hubbard_two_site
     oracle.build()
-    # environments need the engine once (setup, untimed); the timed work is CPU only
-    ctx = Context(0)
-    model, mps, L, R, W1, W2, V, info = hubbard_two_site(ctx, L=args.L, D=args.D, seed=args.seed)
-    ctx.close()
+    t0 = time.perf_counter()
+    model, L, R, W1, W2, V, info = oracle_two_site_workload(args.L, args.D, args.seed)
+    setup_s = time.perf_counter() - t0
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
     op = oracle.OraclePivot(2, 2, L, R, V, W1, W2)
@@ -419,15 +519,16 @@ def run_reference(args):
         op.hxv(v)
     dt = time.perf_counter() - t0
     rate = args.steps / dt
-    line = {"metric": METRIC, "value": rate, "unit": "HxV/s", "n_gpus": 1, "steps": args.steps,
+    line = {"metric": METRIC, "value": rate, "unit": "HxV/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": f"hubbard_u1xu1_L{args.L}_D{args.D}_two_site_middle", "L": args.L, "D": args.D,
-                       "seed": args.seed, "D_left": info["D_left"], "dim_V": info["dim_V"]},
+            "config": workload_config(args, info, world),
             "cpu_baseline": {"value": rate, "unit": "HxV/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} full HxV of the workload", "gemm": oracle.blas_kind()},
-            "e2e": {"value": rate, "unit": "HxV/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "cpu": cpu_model(), "sample": f"{args.steps} full HxV of the workload",
+                             "gemm": oracle.blas_kind()},
+            "e2e": {"value": rate, "unit": "HxV/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "setup_s": round(setup_s, 2), "native_libs_loaded": loaded_native_libs()}
     print(json.dumps(line), flush=True)
 
 
@@ -443,6 +544,8 @@ def main():
     ap.add_argument("--precision", default="bf16x3")
     ap.add_argument("--cpu-hxv", type=int, default=250,
                     help="HxV applications in the CPU-baseline sample (about 13 s on 16 cores)")
+    ap.add_argument("--cpu-hxv-1t", type=int, default=12,
+                    help="HxV applications in the single-thread CPU sample (about 10 s)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-energy", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
@@ -530,13 +633,15 @@ def main():
         # FP64 residual, split Lanczos from it) at the sweep tolerances
         keys = ("iterations", "refine_iterations", "hxv_split", "hxv_fp64", "residual", "ms_total", "ms_wait")
         e_ref, _, s_ref = H.lanczos(v0, "fp64", max_iter=300, tol_eigval=1e-14, tol_state=1e-9)
-        e64, _, s64 = H.lanczos(v0, "fp64", max_iter=300, tol_eigval=1e-10, tol_state=1e-6)
-        es, _, ss = H.lanczos(v0, args.precision, max_iter=300, tol_eigval=1e-10, tol_state=1e-6, refine_iters=10)
+        e64, x64, s64 = H.lanczos(v0, "fp64", max_iter=300, tol_eigval=1e-10, tol_state=1e-6)
+        es, xs, ss = H.lanczos(v0, args.precision, max_iter=300, tol_eigval=1e-10, tol_state=1e-6, refine_iters=10)
         energy = {"E_ref_fp64": e_ref, "tolerances": {"tol_eigval": 1e-10, "tol_state": 1e-6, "refine_iters": 10},
                   "fp64": dict({k: s64[k] for k in keys}, rel_err=abs(e64 - e_ref) / abs(e_ref)),
                   "split": dict({k: ss[k] for k in keys}, rel_err=abs(es - e_ref) / abs(e_ref),
                                 energy_first_rel_err=abs(ss["energy_first"] - e_ref) / abs(e_ref)),
                   "split_speedup": s64["ms_total"] / ss["ms_total"]}
+        if not args.no_cpu and world == 1:
+            energy["oracle"] = oracle_check(Lenv, Renv, V, W1, W2, v0, h64, hsp, e_ref, e64, es, x64, xs)
 
     # ---- roofline of the dominant kernel (the larger of the two grouped-GEMM phases)
     hbm, bf16, peak_kind = load_peaks()
@@ -576,19 +681,20 @@ def main():
     if not args.no_cpu and world == 1 and rank == 0:
         threads = os.cpu_count() or 1
         rate, dt, gemm = cpu_oracle_hxv_rate(Lenv, Renv, V, W1, W2, threads, args.cpu_hxv)
-        cpu = {"value": rate, "unit": "HxV/s", "cores": threads, "kind": "port",
+        rate1, dt1, _ = cpu_oracle_hxv_rate(Lenv, Renv, V, W1, W2, 1, args.cpu_hxv_1t)
+        cpu = {"value": rate, "unit": "HxV/s", "cores": threads, "kind": "port", "cpu": cpu_model(),
                "sample": f"{args.cpu_hxv} full HxV of the workload ({dt:.1f} s)", "gemm": gemm,
-               "flops_per_hxv": st_split["flops_reference"]}
+               "flops_per_hxv": st_split["flops_reference"],
+               "single_thread": {"value": rate1, "unit": "HxV/s", "cores": 1,
+                                 "sample": f"{args.cpu_hxv_1t} full HxV ({dt1:.1f} s)"}}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "HxV/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16x3->f32 (f64 vectors)", "data": "synthetic",
-            "config": {"workload": f"hubbard_u1xu1_L{args.L}_D{args.D}_two_site_middle", "L": args.L, "D": args.D,
-                       "U": 4.0, "seed": args.seed, "D_left": info["D_left"], "sectors": info["sectors_left"],
-                       "dim_V": n, "parallelism": "replicas" if world > 1 else "single",
-                       "l2": l2_note, "working_set_MB": round(working_set / 2 ** 20, 1),
+            "config": workload_config(args, info, world),
+            "timing": {"working_set_MB": round(working_set / 2 ** 20, 1), "l2_note": l2_note,
                        "graph": "CUDA graph per HxV (vector split + 2 grouped-GEMM launches)"},
             "e2e": {"value": e2e, "unit": "HxV/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
             "gpu_launches": (3 if args.precision == "bf16x3" else 2) * args.steps,

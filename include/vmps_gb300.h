@@ -394,8 +394,10 @@ int vmps_transfer_destroy(vmps_transfer* t);
  * point -- a framework that has given all device memory to its own pool, or a
  * loop that cannot afford the device synchronisation of cudaMalloc/cudaFree.
  * m * n above 2^20 returns VMPS_E_ARG.  All calls on a device share that array:
- * calls that overlap on the GPU race.  The first call on a device looks up the
- * array's address; make it outside any stream capture.  `stream` is a
+ * calls that overlap on the GPU race.  Every call looks the array's device
+ * address up in the current context (no allocation), so it stays valid across
+ * cudaDeviceReset; the first call on a device may load the library's device
+ * code, so make that first call outside any stream capture.  `stream` is a
  * cudaStream_t (NULL = default stream); the work is asynchronous on it. */
 int vmps_chain_fp64_noalloc(const double* X, int64_t x_rows, int64_t x_cols, int32_t transX,
                             const double* Y, int64_t y_rows, int64_t y_cols,

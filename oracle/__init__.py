@@ -185,3 +185,40 @@ def contract_L(nq, Lold, Abra, W, Aket):
 
 def contract_R(nq, Rold, Abra, W, Aket):
     return OracleEnv("R", nq, Rold, Abra, W, Aket).run(Rold, Abra, Aket)
+
+
+def lanczos_ground(hxv, v0, tol=1e-14, max_iter=600, patience=4):
+    """Lowest eigenvalue of the symmetric operator `hxv` (a function on flat FP64
+    vectors) by plain three-term Lanczos from v0, in numpy.  Without
+    reorthogonalisation the basis loses orthogonality once a Ritz value converges,
+    which only adds copies of converged values; the lowest Ritz value itself is
+    accurate to rounding.  Stops when it changes by less than tol * |E| for
+    `patience` consecutive steps.  Returns (E, steps).  Three vectors of memory,
+    so it runs at any pivot size the oracle handles; the tridiagonal problem is
+    solved with numpy.linalg.eigvalsh."""
+    q = np.array(v0, dtype=np.float64, copy=True)
+    q /= np.linalg.norm(q)
+    q_prev = np.zeros_like(q)
+    alpha, beta = [], []
+    b = 0.0
+    e_old, calm = None, 0
+    for j in range(max_iter):
+        w = hxv(q)
+        a = float(q @ w)
+        w -= a * q + b * q_prev
+        alpha.append(a)
+        b = float(np.linalg.norm(w))
+        T = np.diag(alpha) + np.diag(beta, 1) + np.diag(beta, -1)
+        e = float(np.linalg.eigvalsh(T)[0])
+        if e_old is not None and abs(e - e_old) <= tol * abs(e):
+            calm += 1
+            if calm >= patience:
+                return e, j + 1
+        else:
+            calm = 0
+        e_old = e
+        if b == 0.0:
+            return e, j + 1
+        beta.append(b)
+        q_prev, q = q, w / b
+    return e_old, max_iter

@@ -286,3 +286,39 @@ def test_env_mode_parity(gpu_ctx, side, mode, ab):
     e = EnvUpdate(gpu_ctx, model.sym, side, E, A, model.W[l], A, mode=mode, fixed_ab=ab, order=order)
     assert compare_tripods(e.run(E, A, A, "fp64"), ref) < TOL_FP64
     assert compare_tripods(e.run(E, A, A, "bf16x3"), ref) < TOL_SPLIT
+
+
+def test_hxv2_parity_hubbard_L64_D1024_middle(gpu_ctx):
+    """The C2 configuration's D=1024 stage: the two-site pivot in the middle of the
+    L=64 Hubbard chain (U/t=4, half filling, Sz=0, seeded Gaussian-profile MPS, the
+    bench's inputs at D=1024) with environments from the oracle.  One FP64 and one
+    split HxV against the oracle's HxV, then the ground-state energy of the pivot
+    from the engine's Lanczos (FP64, and split precision + FP64 refinement) against
+    the oracle's own FP64 Lanczos energy.  Blocks here reach 140-190 rows (two
+    M=128 MMA tiles) and the K-class panels of the large sectors appear."""
+    from vmps_gb300.mps import RandomMPS, contract_two_sites
+    model, Q = make_model("hubb", 64)
+    site = 31
+    mps = RandomMPS(model, Q, 1024, seed=2, profile="gaussian", sigma=[2.5, 2.5]).canonicalize(site, site + 1)
+    Lenv, Renv = oracle_envs(model, mps, site, site + 1)
+    V = contract_two_sites(model.sym, mps.A[site], mps.A[site + 1], model.qloc, model.qloc, model.sym.nq)
+    H = PivotMatrix2(gpu_ctx, model.sym, Lenv, Renv, model.W[site], model.W[site + 1], V)
+    op = oracle.OraclePivot(2, model.sym.nq, Lenv, Renv, V, model.W[site], model.W[site + 1])
+    v = np.random.default_rng(8).standard_normal(V.data.size)
+    ref = op.hxv(v)
+    assert rel_err(H.apply(v, "fp64"), ref) < TOL_FP64
+    assert rel_err(H.apply(v, "bf16x3"), ref) < TOL_SPLIT
+    e_or, _ = oracle.lanczos_ground(op.hxv, v, tol=1e-14)
+    tol = dict(max_iter=300, tol_eigval=1e-12, tol_state=1e-7)
+    e64, x64, _ = H.lanczos(v, "fp64", **tol)
+    es, xs, st = H.lanczos(v, "bf16x3", refine_iters=10, **tol)
+    assert st["hxv_split"] > 0
+    assert abs(e64 - e_or) <= 1e-10 * abs(e_or), (e64, e_or)
+    assert abs(es - e_or) <= 1e-10 * abs(e_or), (es, e_or)
+    # the split solve's vector, checked with the oracle's operator: Rayleigh quotient and residual
+    xs = xs / np.linalg.norm(xs)
+    hx = op.hxv(xs)
+    rq = float(xs @ hx)
+    assert abs(rq - e_or) <= 1e-10 * abs(e_or), (rq, e_or)
+    assert np.linalg.norm(hx - rq * xs) <= 1e-6 * abs(e_or)
+    H.close()

@@ -260,3 +260,16 @@ def test_lattice_mpo_matches_dense_hubbard_cylinder():
     chain = models.hubbard_u1xu1_lattice(4, [(i, i + 1, 1.0) for i in range(3)], U=4.0)
     assert np.abs(ed.mpo_to_dense(chain) - ed.mpo_to_dense(models.hubbard_u1xu1(4, 1.0, 4.0))).max() < 1e-14
     assert models.hubbard_su2xu1_lattice(64, models.cylinder_bonds(16, 4)).wdim == 10
+
+
+def test_oracle_lanczos_ground_matches_dense_eigh():
+    """the numpy three-term Lanczos of the oracle finds the lowest eigenvalue of a
+    dense symmetric matrix to rounding (it is the energy reference of the GPU
+    solves at sizes where no dense matrix can be built)"""
+    rng = np.random.default_rng(3)
+    n = 400
+    A = rng.standard_normal((n, n))
+    A = (A + A.T) / 2
+    e_ref = np.linalg.eigvalsh(A)[0]
+    e, steps = oracle.lanczos_ground(lambda v: A @ v, rng.standard_normal(n))
+    assert abs(e - e_ref) <= 1e-12 * abs(e_ref), (e, e_ref, steps)

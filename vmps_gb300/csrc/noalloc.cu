@@ -19,12 +19,13 @@
 // * the scratch keeps whatever the last call left there; nothing in it needs to
 //   start at zero because every element of the intermediate is written before
 //   it is read;
-// * the first call on each device looks up the array's device address (a
-//   runtime query, no allocation); make that first call outside any stream
+// * every call looks up the array's device address in the current context (a
+//   runtime query, no allocation), so the address stays valid across
+//   cudaDeviceReset; the first call on a device may also load the library's
+//   device code into the context, so make that first call outside any stream
 //   capture.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/vmps_gb300.h"
@@ -38,20 +39,16 @@ constexpr long long kScratchDoubles = 1LL << 20;   // 8 MiB
 // address up with cudaGetSymbolAddress instead (chain_scratch_ptr below).
 static __device__ __align__(256) double g_chain_scratch[kScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_scratch_ptr[kMaxDevices] = {nullptr};
-
-// device address of the scratch array on the current device (looked up once per device)
-cudaError_t chain_scratch_ptr(int dev, double** out) {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_chain_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_ptr[dev] = static_cast<double*>(p);
-    }
-    *out = g_scratch_ptr[dev];
+// Device address of the scratch array in the current context.  Looked up on
+// every call (a runtime query; it allocates nothing): an address cached across
+// calls would dangle once the context it came from is gone (cudaDeviceReset, or
+// a primary context released and created again), and the next call would then
+// write through it.
+cudaError_t chain_scratch_ptr(double** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_chain_scratch);
+    if (e != cudaSuccess) return e;
+    *out = static_cast<double*>(p);
     return cudaSuccess;
 }
 
@@ -150,12 +147,8 @@ extern "C" int vmps_chain_fp64_noalloc(const double* X, int64_t x_rows, int64_t 
     if (m * n > kScratchDoubles)
         return fail(VMPS_E_ARG, "vmps_chain_fp64_noalloc: intermediate op(X)*Y has " + std::to_string(m * n) +
                                     " elements, the fixed scratch holds " + std::to_string(kScratchDoubles));
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(VMPS_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(VMPS_E_ARG, "vmps_chain_fp64_noalloc: device index out of range");
     double* T = nullptr;
-    e = chain_scratch_ptr(dev, &T);
+    cudaError_t e = chain_scratch_ptr(&T);
     if (e != cudaSuccess) return fail(VMPS_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // T (m x n, ld = m) = op(X) * Y

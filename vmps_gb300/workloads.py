@@ -50,7 +50,7 @@ def hubbard_two_site(ctx, L=64, D=4096, U=4.0, seed=2, sigma=2.5, verbose=False,
     info = dict(model=model.name, L=L, D=D, site=site, seed=seed, sigma=sigma,
                 D_left=mps.bond_dim(site), D_right=mps.bond_dim(site + 2),
                 sectors_left=len(mps.dims[site]), dim_V=int(V.data.size),
-                setup_mps_s=round(t1 - t0, 2), setup_env_s=round(t2 - t1, 2))
+                env_elems=int(Lenv.data.size + Renv.data.size), setup_mps_s=round(t1 - t0, 2), setup_env_s=round(t2 - t1, 2))
     if verbose:
         print("workload", info, flush=True)
     return model, mps, Lenv, Renv, model.W[site], model.W[site + 1], V, info
