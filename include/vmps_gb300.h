@@ -159,6 +159,32 @@ int vmps_pivot0_create(vmps_ctx* ctx, const vmps_symmetry* sym,
                        const vmps_blocks* L, const double* Ldata,
                        const vmps_blocks* R, const double* Rdata,
                        const vmps_blocks* V, vmps_pivot** out);
+/* Pivots with several terms: PivotMatrix1::Terms / PivotMatrix2::Terms
+ * (pivot/DmrgPivotMatrix1.h:56, the sum over terms at :273-287; the same in
+ * pivot/DmrgPivotMatrix2.h).  Term t has its own environments L[t], R[t] and MPO
+ * tensors W[t] (two-site: W12[t], W34[t]); all terms share the PivotVector layout
+ * V.  HxV returns the sum over terms, computed as one grouped HxV.  nterms = 1 is
+ * the same as vmps_pivot1_create / vmps_pivot2_create.                         */
+int vmps_pivot1_create_terms(vmps_ctx* ctx, const vmps_symmetry* sym, int nterms,
+                             const vmps_blocks* const* L, const double* const* Ldata,
+                             const vmps_blocks* const* R, const double* const* Rdata,
+                             const vmps_mpo_site* const* W, const vmps_blocks* V,
+                             vmps_pivot** out);
+int vmps_pivot2_create_terms(vmps_ctx* ctx, const vmps_symmetry* sym, int nterms,
+                             const vmps_blocks* const* L, const double* const* Ldata,
+                             const vmps_blocks* const* R, const double* const* Rdata,
+                             const vmps_mpo_site* const* W12, const vmps_mpo_site* const* W34,
+                             const vmps_blocks* V, vmps_pivot** out);
+/* Excited-state projector of PivotMatrix1/2 (A0proj, Epenalty;
+ * pivot/DmrgPivotMatrix1.h:64-68, applied at :304-331): after every HxV of the
+ * pivot, for n < nproj, Vout += Epenalty * <A0_n|Vin> * A0_n, the overlap being the
+ * plain sum over blocks of tr(A0_n^dagger Vin) as the reference takes it (no SU(2)
+ * weight).  A0 holds nproj vectors in the compact layout of V (vector n at
+ * n * dim); blocks of A0proj that V's layout lacks drop out, as they do in the
+ * reference.  Applies to vmps_hxv, vmps_hxv_device, vmps_hxv_multi (at most 64
+ * right-hand sides), the Lanczos solves and the Chebyshev moments.  nproj = 0
+ * removes the projector.                                                       */
+int vmps_pivot_set_penalty(vmps_pivot* p, int nproj, const double* A0, double Epenalty);
 int vmps_pivot_destroy(vmps_pivot* p);
 int vmps_pivot_stats(const vmps_pivot* p, int precision, vmps_plan_stats* out);
 /* number of doubles of a PivotVector in the compact layout of V */

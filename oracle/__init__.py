@@ -222,3 +222,25 @@ def lanczos_ground(hxv, v0, tol=1e-14, max_iter=600, patience=4):
         beta.append(b)
         q_prev, q = q, w / b
     return e_old, max_iter
+
+
+class OracleTerms:
+    """PivotMatrix1/2 with several terms and the excited-state projector, as
+    HxV(PivotMatrix1) evaluates them (pivot/DmrgPivotMatrix1.h:273-287 and
+    :304-331): the sum of the terms' OxV, then for every projector vector A0_n
+    Vout += Epenalty * overlap * A0_n with overlap = sum over blocks of
+    tr(A0_n^dagger Vin), the plain Frobenius product of the compact arrays.
+    terms: list of (L, R, W) for kind 1 or (L, R, W12, W34) for kind 2."""
+
+    def __init__(self, kind, nq, terms, V, A0proj=(), Epenalty=0.0):
+        self.ops = [OraclePivot(kind, nq, t[0], t[1], V, *t[2:]) for t in terms]
+        self.A0 = [np.asarray(a, dtype=np.float64) for a in A0proj]
+        self.E = float(Epenalty)
+
+    def hxv(self, vin):
+        out = self.ops[0].hxv(vin)
+        for op in self.ops[1:]:
+            out += op.hxv(vin)
+        for a in self.A0:
+            out += self.E * float(a @ vin) * a
+        return out

@@ -99,6 +99,17 @@ _PROTOS = [
     ("vmps_pivot0_create", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
                                      C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks),
                                      C.POINTER(C.c_void_p)]),
+    ("vmps_pivot1_create_terms", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.c_int,
+                                           C.POINTER(C.POINTER(vmps_blocks)), C.POINTER(f64p),
+                                           C.POINTER(C.POINTER(vmps_blocks)), C.POINTER(f64p),
+                                           C.POINTER(C.POINTER(vmps_mpo_site)), C.POINTER(vmps_blocks),
+                                           C.POINTER(C.c_void_p)]),
+    ("vmps_pivot2_create_terms", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.c_int,
+                                           C.POINTER(C.POINTER(vmps_blocks)), C.POINTER(f64p),
+                                           C.POINTER(C.POINTER(vmps_blocks)), C.POINTER(f64p),
+                                           C.POINTER(C.POINTER(vmps_mpo_site)), C.POINTER(C.POINTER(vmps_mpo_site)),
+                                           C.POINTER(vmps_blocks), C.POINTER(C.c_void_p)]),
+    ("vmps_pivot_set_penalty", C.c_int, [C.c_void_p, C.c_int, f64p, C.c_double]),
     ("vmps_pivot_destroy", C.c_int, [C.c_void_p]),
     ("vmps_pivot_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),
     ("vmps_pivot_dim", C.c_int, [C.c_void_p, i64p]),

@@ -412,6 +412,55 @@ __global__ void finite_kernel(const double* __restrict__ x, int64_t n, int* __re
 }
 
 // ---------------------------------------------------------------------------
+// Excited-state projector of an HxV (pivot/DmrgPivotMatrix1.h:304-331):
+// out_r += sum_p E <d_p, y_r> a_p for right-hand sides r < nrhs (stride n) and
+// projectors p < npen; d_p and a_p are the projector vector in the padded layout
+// with the SU(2) dot weights folded in.  Fixed chunks and a fixed summation
+// order: the same bits in every run.
+// ---------------------------------------------------------------------------
+template <typename TY>
+__global__ void pen_dot_kernel(PenaltyArgs a, const TY* __restrict__ y) {
+    __shared__ double red[kDotThreads];
+    const int pr = blockIdx.y, p = pr / a.nrhs, r = pr - p * a.nrhs;
+    const int64_t b0 = blockIdx.x * a.chunk, b1 = min(a.n, b0 + a.chunk);
+    const double* d = a.dvec + (int64_t)p * a.n;
+    const TY* v = y + (int64_t)r * a.n;
+    double s = 0;
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += kDotThreads) s = fma(d[i], (double)v[i], s);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kDotThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.part[(int64_t)pr * a.nchunk + blockIdx.x] = red[0];
+}
+// coef[p * nrhs + r] = E * (sum of the chunk partials), one block per (p, r)
+__global__ void pen_sum_kernel(PenaltyArgs a) {
+    __shared__ double red[kDotThreads];
+    const int pr = blockIdx.x;
+    double s = 0;
+    for (int i = threadIdx.x; i < a.nchunk; i += kDotThreads) s += a.part[(int64_t)pr * a.nchunk + i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kDotThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.coef[pr] = a.E * red[0];
+}
+template <typename TO>
+__global__ void pen_add_kernel(PenaltyArgs a, TO* __restrict__ out) {
+    const int r = blockIdx.y;
+    TO* o = out + (int64_t)r * a.n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
+        double s = (double)o[i];
+        for (int p = 0; p < a.npen; ++p) s = fma(a.coef[p * a.nrhs + r], a.avec[(int64_t)p * a.n + i], s);
+        o[i] = (TO)s;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // VUMPS transfer operator pieces
 // ---------------------------------------------------------------------------
 // part[b] = w_b * sum_ij V[i + j*v_ld] * LR[j + i*lr_ld]  (the trace of a block product)
@@ -556,6 +605,21 @@ cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t st) {
 }
 cudaError_t launch_combine(const double* V, int nv, int64_t n, const double* c, double* y, cudaStream_t st) {
     combine_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>(V, nv, n, c, y);
+    return cudaGetLastError();
+}
+cudaError_t launch_penalty(const PenaltyArgs& a, const double* y, const float* yf, double* o, float* of,
+                           cudaStream_t st) {
+    if (a.npen <= 0 || a.nrhs <= 0) return cudaSuccess;
+    if (!a.dvec || !a.avec || !a.part || !a.coef || (!y && !yf) || (!o && !of) || a.chunk <= 0 ||
+        (int64_t)a.nchunk * a.chunk < a.n)
+        return cudaErrorInvalidValue;
+    const dim3 gd(a.nchunk, a.npen * a.nrhs);
+    if (yf) pen_dot_kernel<float><<<gd, kDotThreads, 0, st>>>(a, yf);
+    else pen_dot_kernel<double><<<gd, kDotThreads, 0, st>>>(a, y);
+    pen_sum_kernel<<<a.npen * a.nrhs, kDotThreads, 0, st>>>(a);
+    const dim3 ga(grid_for(a.n, 256, 152 * 4), a.nrhs);
+    if (of) pen_add_kernel<float><<<ga, 256, 0, st>>>(a, of);
+    else pen_add_kernel<double><<<ga, 256, 0, st>>>(a, o);
     return cudaGetLastError();
 }
 cudaError_t launch_finite(const double* x, int64_t n, int* bad, cudaStream_t st) {

@@ -63,6 +63,19 @@ cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStr
 cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t st);
 cudaError_t launch_combine(const double* V, int nv, int64_t n, const double* c, double* y, cudaStream_t st);
 cudaError_t launch_finite(const double* x, int64_t n, int* bad, cudaStream_t st);
+// excited-state projector after an HxV: out_r += sum_p E <dvec_p, y_r> avec_p (r < nrhs, vectors
+// at stride n; y and out double or float, the other pointer null); deterministic
+struct PenaltyArgs {
+    const double* dvec;   // [npen][n]: projector vectors for the overlap
+    const double* avec;   // [npen][n]: projector vectors added to the output
+    double* part;         // [npen * nrhs][nchunk] chunk partials
+    double* coef;         // [npen * nrhs]: E * overlap
+    int64_t n, chunk;
+    int npen, nrhs, nchunk;
+    double E;
+};
+cudaError_t launch_penalty(const PenaltyArgs& a, const double* y, const float* yf, double* o, float* of,
+                           cudaStream_t st);
 // VUMPS transfer operator: out = sum_b w_b tr(V_b LR_b) (deterministic); out[V block] = V - T + s * 1
 struct TracePair { int64_t v_off, lr_off; int32_t rows, cols, v_ld, lr_ld; double weight; };
 struct CombineBlock { int64_t v_off, t_off; int32_t rows, cols, v_ld, t_ld; };

@@ -401,6 +401,8 @@ struct Operands {
     // split plans only: FP32 vectors in place of Y and O (same padded layout)
     const float* Yf = nullptr;
     float* Of = nullptr;
+    // pivots with an excited-state projector: applied after the second phase
+    const PenaltyArgs* pen = nullptr;
 };
 
 // Invariants the tcgen05 engine relies on, checked on the host once per plan:
@@ -567,6 +569,11 @@ static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
     }
     run_phase(dp, 1, ops, st);
     run_phase(dp, 2, ops, st);
+    if (ops.pen && ops.pen->npen > 0) {
+        PenaltyArgs a = *ops.pen;
+        a.nrhs = dp.plan.nrhs;
+        CK(launch_penalty(a, ops.Y, ops.Yf, ops.O, ops.Of, st));
+    }
 }
 
 // bf16 MMA work a split phase issues: 3 products of M=128 x N=round16(tn) x K per
@@ -634,6 +641,10 @@ struct vmps_pivot_s {
     const void* graph_out[2] = {nullptr, nullptr};
     std::map<int, std::unique_ptr<DevPlan>> multi;   // split plans for nrhs > 1 vectors, by nrhs
     DBuf mvin, mvout;                                // nrhs padded vectors for host-buffer multi-RHS HxV
+    // excited-state projector (A0proj, Epenalty): projector vectors in the padded layout
+    // with the SU(2) dot weights folded in, chunk partials and coefficients
+    DBuf pen_d, pen_a, pen_part, pen_coef;
+    PenaltyArgs pen{};
     ~vmps_pivot_s() {
         for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
     }
@@ -856,12 +867,21 @@ static void require_device(const vmps_ctx* c) {
     if (!c || c->device < 0) throw std::invalid_argument("operation needs a device context (this one is host-only)");
 }
 
-static void pivot_hxv_dev(vmps_pivot* p, int prec, const double* vin, double* vout) {
-    require_device(p->ctx);
-    DevPlan& dp = get_plan(p, prec);
+// the operands every HxV of a pivot shares: L and R arenas, the error word and
+// the excited-state projector when one is set
+static Operands pivot_ops(const vmps_pivot* p) {
     Operands ops;
     ops.X = p->dL.as<double>();
     ops.Z = p->dR.as<double>();
+    ops.err = p->ctx->err;
+    if (p->pen.npen > 0) ops.pen = &p->pen;
+    return ops;
+}
+
+static void pivot_hxv_dev(vmps_pivot* p, int prec, const double* vin, double* vout) {
+    require_device(p->ctx);
+    DevPlan& dp = get_plan(p, prec);
+    Operands ops = pivot_ops(p);
     ops.Y = vin;
     ops.O = vout;
     ops.err = p->ctx->err;
@@ -1026,6 +1046,149 @@ int vmps_pivot0_create(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_bloc
     API_END
 }
 
+// ---- pivots with several terms (PivotMatrix1/2::Terms) ------------------------
+// The reference sums the HxV of every term (pivot/DmrgPivotMatrix1.h:273-287,
+// pivot/DmrgPivotMatrix2.h the same).  Here the terms' L and R tables are laid
+// end to end in one arena each, every term's chains are built against its own
+// tables and shifted to its blocks' place in the arenas, and all chains go into
+// one plan: one grouped HxV for the sum, output tiles owned as before.
+static void append_table(BlockTable& all, const BlockTable& t, int64_t data_base) {
+    for (int64_t i = 0; i < t.n; ++i) {
+        all.qin.push_back(t.qin[i]);
+        all.qout.push_back(t.qout[i]);
+        all.qmid.push_back(t.qmid[i]);
+        all.leg.push_back(t.leg[i]);
+        all.rows.push_back(t.rows[i]);
+        all.cols.push_back(t.cols[i]);
+        all.off.push_back(data_base + t.off[i]);
+    }
+    all.n += t.n;
+    all.has_mid = true;
+    all.total = data_base + t.total;
+}
+
+static int pivot_create_terms(vmps_ctx* ctx, const vmps_symmetry* symd, int kind, int nterms,
+                              const vmps_blocks* const* L, const double* const* Ldata, const vmps_blocks* const* R,
+                              const double* const* Rdata, const vmps_mpo_site* const* W,
+                              const vmps_mpo_site* const* W34, const vmps_blocks* V, vmps_pivot** out) {
+    if (!out) return set_err(VMPS_E_ARG, "null out");
+    if (!ctx) return set_err(VMPS_E_ARG, "null context");
+    if (nterms < 1 || !L || !Ldata || !R || !Rdata || !W || (kind == 2 && !W34))
+        return set_err(VMPS_E_ARG, "a pivot needs at least one term and non-null term arrays");
+    Symmetry sym = make_sym(symd);
+    std::unique_ptr<vmps_pivot> p(new vmps_pivot_s());
+    p->ctx = ctx;
+    p->sym = sym;
+    p->Vt = parse_blocks(sym, V, false);
+    std::vector<double> lcat, rcat;
+    for (int t = 0; t < nterms; ++t) {
+        if (!Ldata[t] || !Rdata[t] || !W[t] || (kind == 2 && !W34[t]))
+            throw std::invalid_argument("term " + std::to_string(t) + ": null data or MPO");
+        BlockTable Lt = parse_blocks(sym, L[t], true), Rt = parse_blocks(sym, R[t], true);
+        ChainSet cs;
+        if (kind == 1) cs = build_pivot1(sym, Lt, Rt, parse_mpo(sym, W[t]), p->Vt);
+        else cs = build_pivot2(sym, Lt, Rt, parse_mpo(sym, W[t]), parse_mpo(sym, W34[t]), p->Vt);
+        const int64_t xb = p->Lt.n, zb = p->Rt.n;
+        for (auto& c : cs.chains) {
+            c.x += xb;
+            c.z += zb;
+            p->cs.chains.push_back(c);
+        }
+        p->cs.n_tasks += cs.n_tasks;
+        p->cs.n_chains_raw += cs.n_chains_raw;
+        p->cs.flops_reference += cs.flops_reference;
+        const int64_t lb = (int64_t)lcat.size(), rb = (int64_t)rcat.size();
+        append_table(p->Lt, Lt, lb);
+        append_table(p->Rt, Rt, rb);
+        lcat.insert(lcat.end(), Ldata[t], Ldata[t] + Lt.total);
+        rcat.insert(rcat.end(), Rdata[t], Rdata[t] + Rt.total);
+    }
+    p->Ld = make_dev_layout(p->Lt.rows, p->Lt.cols);
+    p->Rd = make_dev_layout(p->Rt.rows, p->Rt.cols);
+    p->Vd = make_dev_layout(p->Vt.rows, p->Vt.cols);
+    pivot_finish(p.get(), lcat.data(), rcat.data());
+    *out = p.release();
+    return VMPS_OK;
+}
+
+int vmps_pivot1_create_terms(vmps_ctx* ctx, const vmps_symmetry* sym, int nterms, const vmps_blocks* const* L,
+                             const double* const* Ldata, const vmps_blocks* const* R, const double* const* Rdata,
+                             const vmps_mpo_site* const* W, const vmps_blocks* V, vmps_pivot** out) {
+    API_BEGIN
+    return pivot_create_terms(ctx, sym, 1, nterms, L, Ldata, R, Rdata, W, nullptr, V, out);
+    API_END
+}
+
+int vmps_pivot2_create_terms(vmps_ctx* ctx, const vmps_symmetry* sym, int nterms, const vmps_blocks* const* L,
+                             const double* const* Ldata, const vmps_blocks* const* R, const double* const* Rdata,
+                             const vmps_mpo_site* const* W12, const vmps_mpo_site* const* W34,
+                             const vmps_blocks* V, vmps_pivot** out) {
+    API_BEGIN
+    return pivot_create_terms(ctx, sym, 2, nterms, L, Ldata, R, Rdata, W12, W34, V, out);
+    API_END
+}
+
+// ---- excited-state projector (A0proj, Epenalty) ---------------------------------
+// pivot/DmrgPivotMatrix1.h:64-68 and :304-331: after the HxV, for every projector
+// vector A0_n: overlap = sum over blocks of tr(A0_n^dagger Vin) (no SU(2) weight),
+// Vout += Epenalty * overlap * A0_n.  The device vectors carry sqrt(coeff_dot) per
+// block (v_dev = s v), so the overlap uses A0 / s and the update adds s A0.
+constexpr int kPenMaxRhs = 64;   // right-hand sides one projected HxV may carry
+
+int vmps_pivot_set_penalty(vmps_pivot* p, int nproj, const double* A0, double Epenalty) {
+    API_BEGIN
+    if (!p) return set_err(VMPS_E_ARG, "null pivot");
+    if (nproj < 0 || (nproj > 0 && !A0)) return set_err(VMPS_E_ARG, "bad projector arguments");
+    if (!std::isfinite(Epenalty)) return set_err(VMPS_E_NONFINITE, "Epenalty is not finite");
+    const int64_t dim = p->Vt.total;
+    for (int64_t i = 0; i < (int64_t)nproj * dim; ++i)
+        if (!std::isfinite(A0[i])) return set_err(VMPS_E_NONFINITE, "projector vector has NaN/Inf");
+    // cached HxV graphs were captured without (or with another) projector
+    for (auto& g : p->graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    p->graph_in[0] = p->graph_in[1] = p->graph_out[0] = p->graph_out[1] = nullptr;
+    p->pen = PenaltyArgs{};
+    if (nproj == 0) return VMPS_OK;
+    require_device(p->ctx);
+    cudaStream_t st = p->st();
+    const int64_t n = p->Vd.total;
+    std::vector<double> dh((size_t)nproj * dim), ah((size_t)nproj * dim);
+    for (int k = 0; k < nproj; ++k)
+        for (int64_t b = 0; b < p->Vt.n; ++b) {
+            const double sc = p->vscale[b];
+            const int64_t o = (int64_t)k * dim + p->Vt.off[b], e = p->Vt.rows[b] * p->Vt.cols[b];
+            for (int64_t i = 0; i < e; ++i) {
+                dh[o + i] = A0[o + i] / sc;
+                ah[o + i] = A0[o + i] * sc;
+            }
+        }
+    auto pb = pack_blocks(p->Vt, p->Vd, nullptr);
+    DBuf pk, tmp;
+    upload_vec(pk, pb, st);
+    p->pen_d.alloc((size_t)nproj * n * 8, st, true);
+    p->pen_a.alloc((size_t)nproj * n * 8, st, true);
+    for (int k = 0; k < nproj; ++k) {
+        pack_in(p->ctx, pk, (int)pb.size(), dh.data() + (int64_t)k * dim, dim, tmp, p->pen_d.as<double>() + k * n, st);
+        pack_in(p->ctx, pk, (int)pb.size(), ah.data() + (int64_t)k * dim, dim, tmp, p->pen_a.as<double>() + k * n, st);
+        CK(cudaStreamSynchronize(st));   // the staging buffer is reused by the next vector
+    }
+    PenaltyArgs a{};
+    a.n = n;
+    a.chunk = dot_chunk(n);
+    a.nchunk = dot_nchunk(n);
+    a.npen = nproj;
+    a.nrhs = 1;
+    a.E = Epenalty;
+    p->pen_part.alloc((size_t)nproj * kPenMaxRhs * a.nchunk * 8, st, true);
+    p->pen_coef.alloc((size_t)nproj * kPenMaxRhs * 8, st, true);
+    a.dvec = p->pen_d.as<double>();
+    a.avec = p->pen_a.as<double>();
+    a.part = p->pen_part.as<double>();
+    a.coef = p->pen_coef.as<double>();
+    CK(cudaStreamSynchronize(st));
+    p->pen = a;
+    API_END
+}
+
 // Destroy functions never touch the owning context or pivot: callers (and
 // garbage collectors) may release objects in any order.  cudaFree waits for
 // the device work that still uses the memory.
@@ -1057,7 +1220,7 @@ int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int prec) {
     ensure_staging(p);
     ensure_io(p);
     DevPlan& dp = get_plan(p, prec);
-    if (dp.chunks) {
+    if (dp.chunks && p->pen.npen == 0) {   // the projector needs the whole output: no pipeline
         hxv_host_pipelined(p, dp, vin, vout);
         check_device_error(p->ctx);
         return VMPS_OK;
@@ -1074,6 +1237,8 @@ int vmps_hxv_multi(vmps_pivot* p, const double* vin, double* vout, int nrhs, int
     API_BEGIN
     if (!p || !vin || !vout || nrhs < 1) return set_err(VMPS_E_ARG, "bad argument");
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
+    if (p->pen.npen > 0 && nrhs > kPenMaxRhs)
+        return set_err(VMPS_E_UNSUPPORTED, "a pivot with a projector takes at most 64 right-hand sides");
     require_device(p->ctx);
     cudaStream_t st = p->st();
     ensure_staging(p);
@@ -1086,12 +1251,9 @@ int vmps_hxv_multi(vmps_pivot* p, const double* vin, double* vout, int nrhs, int
         pack_in(p->ctx, p->dPack, p->npack, vin + (int64_t)k * dim, dim, p->stage_in, din + (int64_t)k * n, st);
     if (prec == VMPS_PREC_BF16X3) {
         DevPlan& dp = get_multi_plan(p, nrhs);
-        Operands ops;
-        ops.X = p->dL.as<double>();
-        ops.Z = p->dR.as<double>();
+        Operands ops = pivot_ops(p);
         ops.Y = din;
         ops.O = dout;
-        ops.err = p->ctx->err;
         run_plan(dp, ops, st);
     } else {
         for (int k = 0; k < nrhs; ++k) pivot_hxv_dev(p, prec, din + (int64_t)k * n, dout + (int64_t)k * n);
@@ -1187,12 +1349,9 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
     DevPlan& dp = get_plan(p, prec);
     const double* vi = vin->d.as<double>();
     double* vo = vout->d.as<double>();
-    Operands ops;
-    ops.X = p->dL.as<double>();
-    ops.Z = p->dR.as<double>();
+    Operands ops = pivot_ops(p);
     ops.Y = vi;
     ops.O = vo;
-    ops.err = p->ctx->err;
     if (use_graph) {
         if (!p->graph[prec] || p->graph_in[prec] != vi || p->graph_out[prec] != vo) {
             if (p->graph[prec]) { cudaGraphExecDestroy(p->graph[prec]); p->graph[prec] = nullptr; }
@@ -1451,9 +1610,7 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
         static const unsigned kStartOne = 1;
         CK(cudaMemcpyAsync(W.ctl(), &kStartOne, sizeof(unsigned), cudaMemcpyHostToDevice, st));
     }
-    Operands ops;
-    ops.X = p->dL.as<double>();
-    ops.Z = p->dR.as<double>();
+    Operands ops = pivot_ops(p);
     if (f32) {
         ops.Yf = W.q32.as<float>();
         ops.Of = W.w32.as<float>();
@@ -1461,7 +1618,6 @@ LzResult lz_run(vmps_pivot* p, LzWork& W, int prec, int kmax, double tol_eigval,
         ops.Y = W.q.as<double>();
         ops.O = W.w.as<double>();
     }
-    ops.err = p->ctx->err;
     // one iteration = the HxV plan + the four step kernels, captured once
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1883,6 +2039,8 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
     if (!p || !v0 || !mu || nrhs < 1 || nrhs > 65535 || nmom < 1) return set_err(VMPS_E_ARG, "bad argument");
     if (!(a > 0) || !std::isfinite(a) || !std::isfinite(b)) return set_err(VMPS_E_ARG, "scale a must be > 0");
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
+    if (p->pen.npen > 0 && nrhs > kPenMaxRhs)
+        return set_err(VMPS_E_UNSUPPORTED, "a pivot with a projector takes at most 64 right-hand sides");
     require_device(p->ctx);
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t st = p->st();
@@ -1921,10 +2079,7 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
         c.nchunk = sh.nchunk;
         c.inv_a = 1.0 / a;
         c.b = b;
-        Operands ops;
-        ops.X = p->dL.as<double>();
-        ops.Z = p->dR.as<double>();
-        ops.err = p->ctx->err;
+        Operands ops = pivot_ops(p);
         cudaGraph_t gr = nullptr;
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         try {

@@ -29,7 +29,7 @@ from .blocks import MpoSite, Symmetry
 class ChainModel:
     """MPO of a chain: sites W[l], aux bases aux[l] (l = 0..L), local bases."""
 
-    def __init__(self, sym, L, qloc, ops, terms, onsite, name=""):
+    def __init__(self, sym, L, qloc, ops, terms, onsite, name="", site_coef=None):
         self.sym = sym
         self.L = L
         self.qloc = qloc            # list of QN tuples (same on every site)
@@ -37,6 +37,7 @@ class ChainModel:
         self.ops = ops              # name -> (matrix, QN)
         self.terms = terms          # list of (opA, opB, coef)
         self.onsite = onsite        # list of (op, coef)
+        self.site_coef = site_coef  # per-site factor of the on-site terms (None: 1 everywhere)
         self._build()
 
     @property
@@ -77,6 +78,8 @@ class ChainModel:
             entries.append(("DONE", "DONE", I))
         if "IDLE" in ain and "DONE" in aout and self.onsite:
             h = sum(c * self.ops[o][0] for o, c in self.onsite)
+            if self.site_coef is not None:
+                h = self.site_coef[l] * h
             entries.append(("IDLE", "DONE", h))
         for t, (a, b, c) in enumerate(self.terms):
             if "IDLE" in ain and f"OPEN{t}" in aout:
@@ -121,16 +124,31 @@ class ChainModel:
         return self.W[l].dense(self.aux_qns(l), self.aux_qns(l + 1))
 
 
-def heisenberg_u1(L, J=1.0):
-    """Spin-1/2 XXX chain, H = J sum (Sz Sz + (S+S- + S-S+)/2), U(1) M = 2 S^z."""
-    sym = Symmetry(("U1",))
-    qloc = [(1,), (-1,)]
+def _spin_half_ops():
     Sz = np.diag([0.5, -0.5])
     Sp = np.array([[0.0, 1.0], [0.0, 0.0]])   # |up><dn|
     Sm = Sp.T.copy()
-    ops = {"Sz": (Sz, (0,)), "Sp": (Sp, (2,)), "Sm": (Sm, (-2,))}
-    terms = [("Sp", "Sm", 0.5 * J), ("Sm", "Sp", 0.5 * J), ("Sz", "Sz", J)]
-    return ChainModel(sym, L, qloc, ops, terms, [], name=f"HeisenbergU1(L={L},J={J})")
+    return {"Sz": (Sz, (0,)), "Sp": (Sp, (2,)), "Sm": (Sm, (-2,))}
+
+
+def heisenberg_u1(L, J=1.0, Jxy=None, Jz=None):
+    """Spin-1/2 XXZ chain, H = sum (Jz Sz Sz + Jxy (S+S- + S-S+)/2), U(1) M = 2 S^z;
+    Jxy = Jz = J by default (XXX).  The couplings follow models/HeisenbergU1.h, which
+    places 0.5*Jxy on S+S- and S-S+ and Jz on SzSz."""
+    Jxy = J if Jxy is None else Jxy
+    Jz = J if Jz is None else Jz
+    sym = Symmetry(("U1",))
+    qloc = [(1,), (-1,)]
+    terms = [("Sp", "Sm", 0.5 * Jxy), ("Sm", "Sp", 0.5 * Jxy), ("Sz", "Sz", Jz)]
+    return ChainModel(sym, L, qloc, _spin_half_ops(), terms, [], name=f"HeisenbergU1(L={L},Jxy={Jxy},Jz={Jz})")
+
+
+def spin_half_local_sum(L, coef, op="Sz"):
+    """MPO of the one-site observable sum_l coef[l] op_l on a spin-1/2 U(1) chain (bond
+    dimension 2), e.g. the staggered magnetisation with coef[l] = (-1)^l / L."""
+    sym = Symmetry(("U1",))
+    return ChainModel(sym, L, [(1,), (-1,)], _spin_half_ops(), [], [(op, 1.0)], name=f"sum_l c_l {op}_l (L={L})",
+                      site_coef=list(coef))
 
 
 def hubbard_u1xu1(L, t=1.0, U=4.0):

@@ -126,6 +126,14 @@ class _Pivot:
                                                C.byref(st)))
         return mu, st.as_dict()
 
+    def set_projector(self, A0proj, Epenalty: float):
+        """Excited-state projector (PivotMatrix1/2::A0proj, Epenalty): every later HxV
+        adds Epenalty * <A0_n|Vin> * A0_n for each vector A0_n (compact layout of this
+        pivot; a list of vectors or an nproj x dim array).  An empty list removes it."""
+        A0 = np.ascontiguousarray(np.reshape(np.asarray(A0proj, dtype=np.float64), (-1, self.dim)))
+        self._A0 = A0
+        N.check(N.lib().vmps_pivot_set_penalty(self._h, A0.shape[0], A0.ctypes.data_as(N.f64p), float(Epenalty)))
+
     def lanczos(self, v0: np.ndarray, precision="fp64", max_iter=200, tol_eigval=1e-12, tol_state=1e-8,
                 refine_iters=0):
         """Ground state by full-reorthogonalisation Lanczos on the device."""
@@ -137,25 +145,67 @@ class _Pivot:
         return e.value, v, st.as_dict()
 
 
+def _term_arrays(terms, nmpo):
+    """ctypes arrays of the per-term tables of a multi-term pivot"""
+    n = len(terms)
+    keep = []
+    Lt, Ld = (C.POINTER(N.vmps_blocks) * n)(), (N.f64p * n)()
+    Rt, Rd = (C.POINTER(N.vmps_blocks) * n)(), (N.f64p * n)()
+    Ws = [(C.POINTER(N.vmps_mpo_site) * n)() for _ in range(nmpo)]
+    for t, term in enumerate(terms):
+        L, R, mpos = term[0], term[1], term[2:]
+        lb, rb = L.c_struct(), R.c_struct()
+        ws = [W.c_struct() for W in mpos]
+        keep += [lb, rb] + ws
+        Lt[t], Ld[t] = C.pointer(lb), L.data_ptr()
+        Rt[t], Rd[t] = C.pointer(rb), R.data_ptr()
+        for i in range(nmpo):
+            Ws[i][t] = C.pointer(ws[i])
+    return Lt, Ld, Rt, Rd, Ws, keep
+
+
 class PivotMatrix1(_Pivot):
     """1-site effective Hamiltonian (pivot/DmrgPivotMatrix1.h:46-121)."""
 
-    def __init__(self, ctx, sym, L: Blocks, R: Blocks, W: MpoSite, V: Blocks):
+    def __init__(self, ctx, sym, L: Blocks, R: Blocks, W: MpoSite, V: Blocks, _terms=None):
         super().__init__(ctx, sym, V)
-        s, lb, rb, wb, vb = sym.c_struct(), L.c_struct(), R.c_struct(), W.c_struct(), V.c_struct()
+        s, vb = sym.c_struct(), V.c_struct()
+        if _terms is not None:
+            Lt, Ld, Rt, Rd, (Wt,), keep = _term_arrays(_terms, 1)
+            N.check(N.lib().vmps_pivot1_create_terms(ctx._h, C.byref(s), len(_terms), Lt, Ld, Rt, Rd, Wt,
+                                                     C.byref(vb), C.byref(self._h)))
+            return
+        lb, rb, wb = L.c_struct(), R.c_struct(), W.c_struct()
         N.check(N.lib().vmps_pivot1_create(ctx._h, C.byref(s), C.byref(lb), L.data_ptr(), C.byref(rb), R.data_ptr(),
                                            C.byref(wb), C.byref(vb), C.byref(self._h)))
+
+    @classmethod
+    def from_terms(cls, ctx, sym, terms, V: Blocks):
+        """PivotMatrix1 with several terms (PivotMatrix1::Terms): `terms` is a list of
+        (L, R, W); HxV returns the sum over the terms."""
+        return cls(ctx, sym, None, None, None, V, _terms=list(terms))
 
 
 class PivotMatrix2(_Pivot):
     """2-site effective Hamiltonian (pivot/DmrgPivotMatrix2.h:29-76)."""
 
-    def __init__(self, ctx, sym, L: Blocks, R: Blocks, W12: MpoSite, W34: MpoSite, V: Blocks):
+    def __init__(self, ctx, sym, L: Blocks, R: Blocks, W12: MpoSite, W34: MpoSite, V: Blocks, _terms=None):
         super().__init__(ctx, sym, V)
-        s, lb, rb, vb = sym.c_struct(), L.c_struct(), R.c_struct(), V.c_struct()
+        s, vb = sym.c_struct(), V.c_struct()
+        if _terms is not None:
+            Lt, Ld, Rt, Rd, (W1t, W2t), keep = _term_arrays(_terms, 2)
+            N.check(N.lib().vmps_pivot2_create_terms(ctx._h, C.byref(s), len(_terms), Lt, Ld, Rt, Rd, W1t, W2t,
+                                                     C.byref(vb), C.byref(self._h)))
+            return
+        lb, rb = L.c_struct(), R.c_struct()
         w1, w2 = W12.c_struct(), W34.c_struct()
         N.check(N.lib().vmps_pivot2_create(ctx._h, C.byref(s), C.byref(lb), L.data_ptr(), C.byref(rb), R.data_ptr(),
                                            C.byref(w1), C.byref(w2), C.byref(vb), C.byref(self._h)))
+
+    @classmethod
+    def from_terms(cls, ctx, sym, terms, V: Blocks):
+        """PivotMatrix2 with several terms: `terms` is a list of (L, R, W12, W34)."""
+        return cls(ctx, sym, None, None, None, None, V, _terms=list(terms))
 
 
 class PivotMatrix0(_Pivot):
