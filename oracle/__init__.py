@@ -5,6 +5,8 @@ dense exact-diagonalisation pins (ed.py).  Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use this
 package, as the checker.  The GPU engine never imports it.
 
+Symmetries: U(1) and SU(2) components and their products (set_symmetry).
+
 Parity status: the reference (header-only C++ over Eigen, Boost, GSL and the
 TNWorkers TOOLS/ALGS headers) cannot be compiled in this environment, and it
 ships no numeric golden vectors for this path.  The restatement is therefore
@@ -69,6 +71,11 @@ def lib(use_blas=True):
             getattr(_lib, f).argtypes = None
         _lib.oracle_set_blas.argtypes = [C.c_char_p]
         _lib.oracle_set_threads.argtypes = [C.c_int]
+        _lib.oracle_set_symmetry.argtypes = [C.c_int, C.POINTER(C.c_int32)]
+        _lib.oracle_coupling_6j.restype = C.c_double
+        _lib.oracle_coupling_6j.argtypes = [C.c_int] * 6
+        _lib.oracle_coupling_9j.restype = C.c_double
+        _lib.oracle_coupling_9j.argtypes = [C.c_int] * 9
         if use_blas:
             p = find_openblas()
             if p and _lib.oracle_set_blas(p.encode()) > 0:
@@ -87,6 +94,27 @@ def set_threads(n):
 
 def max_threads():
     return lib().oracle_max_threads()
+
+
+def set_symmetry(nq, kinds=None):
+    """QN component kinds of the oracle objects created next: a sequence of "U1" /
+    "SU2" (or a vmps_gb300 Symmetry); None means U(1) for every component."""
+    if kinds is not None and hasattr(kinds, "kinds"):
+        kinds = kinds.kinds
+    k = np.zeros(4, dtype=np.int32)
+    for i, name in enumerate(kinds or ()):
+        k[i] = 1 if name == "SU2" else 0
+    lib().oracle_set_symmetry(int(nq), k.ctypes.data_as(C.POINTER(C.c_int32)))
+
+
+def coupling_6j(*two_j):
+    """the oracle's 6j symbol; arguments are 2j"""
+    return lib().oracle_coupling_6j(*[int(x) for x in two_j])
+
+
+def coupling_9j(*two_j):
+    """the oracle's 9j symbol; arguments are 2j"""
+    return lib().oracle_coupling_9j(*[int(x) for x in two_j])
 
 
 def _p(a, t=C.c_int32):
@@ -113,9 +141,10 @@ def _mpo(W):
 class OraclePivot:
     """kind 1: PivotMatrix1 (W), kind 2: PivotMatrix2 (W, W34), kind 0: PivotMatrix0."""
 
-    def __init__(self, kind, nq, L, R, V, W=None, W34=None):
+    def __init__(self, kind, nq, L, R, V, W=None, W34=None, sym=None):
         self.V = V
         self._keep = (L, R, V, W, W34)
+        set_symmetry(nq, sym)
         args = [C.c_int(kind), C.c_int(nq)] + _tab(L) + [_p(L.data, C.c_double)] + _tab(R) + \
                [_p(R.data, C.c_double)] + _tab(V, mid=False) + _mpo(W) + _mpo(W34)
         self._h = C.c_void_p(lib().oracle_pivot_create(*args))
@@ -151,8 +180,9 @@ MODES = {"FULL": 0, "TRIANGULAR": 1, "FIXED_ROWS": 2, "FIXED_COLS": 3}
 class OracleEnv:
     """contract_L (side 'L') / contract_R (side 'R'), with CONTRACT_LR_MODE."""
 
-    def __init__(self, side, nq, E, B, W, K, mode="FULL", fixed_ab=0, order=None):
+    def __init__(self, side, nq, E, B, W, K, mode="FULL", fixed_ab=0, order=None, sym=None):
         from vmps_gb300.blocks import Blocks
+        set_symmetry(nq, sym)
         qn, idx, val = order_arrays(nq, order or {})
         self._keep = (E, B, W, K, qn, idx, val)
         args = [C.c_int(0 if side == "L" else 1), C.c_int(nq)] + _tab(E) + _tab(B, mid=False) + \
@@ -179,12 +209,12 @@ class OracleEnv:
             self._h = None
 
 
-def contract_L(nq, Lold, Abra, W, Aket):
-    return OracleEnv("L", nq, Lold, Abra, W, Aket).run(Lold, Abra, Aket)
+def contract_L(nq, Lold, Abra, W, Aket, sym=None):
+    return OracleEnv("L", nq, Lold, Abra, W, Aket, sym=sym).run(Lold, Abra, Aket)
 
 
-def contract_R(nq, Rold, Abra, W, Aket):
-    return OracleEnv("R", nq, Rold, Abra, W, Aket).run(Rold, Abra, Aket)
+def contract_R(nq, Rold, Abra, W, Aket, sym=None):
+    return OracleEnv("R", nq, Rold, Abra, W, Aket, sym=sym).run(Rold, Abra, Aket)
 
 
 def lanczos_ground(hxv, v0, tol=1e-14, max_iter=600, patience=4):
@@ -232,8 +262,8 @@ class OracleTerms:
     tr(A0_n^dagger Vin), the plain Frobenius product of the compact arrays.
     terms: list of (L, R, W) for kind 1 or (L, R, W12, W34) for kind 2."""
 
-    def __init__(self, kind, nq, terms, V, A0proj=(), Epenalty=0.0):
-        self.ops = [OraclePivot(kind, nq, t[0], t[1], V, *t[2:]) for t in terms]
+    def __init__(self, kind, nq, terms, V, A0proj=(), Epenalty=0.0, sym=None):
+        self.ops = [OraclePivot(kind, nq, t[0], t[1], V, *t[2:], sym=sym) for t in terms]
         self.A0 = [np.asarray(a, dtype=np.float64) for a in A0proj]
         self.E = float(Epenalty)
 

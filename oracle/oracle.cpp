@@ -20,7 +20,17 @@
 //
 // GEMM: the OpenBLAS library bundled with numpy when its path is handed in
 // (oracle_set_blas), else a plain cache-blocked triple loop.
-// Only SU(2)-free (abelian) symmetries are restated here.
+//
+// Symmetries: products of U(1) and SU(2) components (oracle_set_symmetry), as
+// Sym::S1xS2 composes them (symmetry/S1xS2.h).  SU(2) quantum numbers are
+// q = 2S+1; fusion |q1-q2|+1 .. q1+q2-1 step 2 (SU2::reduceSilent,
+// symmetry/SU2.h:174-183); the prefactors are the reference's coefficient
+// families (symmetry/SU2.h:388-519) evaluated per SU(2) component and
+// multiplied (U(1) components contribute 1):
+//   coeff_HPsi / coeff_buildL / coeff_tensorProd = 9j * sqrt(q7 q8 q3 q6)
+//   coeff_buildR = 9j * sqrt(q7 q8 q3 q6) * q9 / q7
+//   coeff_Apair  = 6j * sqrt(q3 q6) * (-1)^((q1+q2+q4+q5-4)/2)
+// with the 6j / 9j symbols of SU2Wrappers.h:72-120 (GSL's arguments are 2j = q-1).
 #include <dlfcn.h>
 #include <omp.h>
 
@@ -67,9 +77,111 @@ Tab read_tab(int nq, int64_t n, const int32_t* qin, const int32_t* qout, const i
     return t;
 }
 
-// unused QN components are zero everywhere, so the arithmetic runs over all four
-Q addq(const Q& a, const Q& b) { Q r{0, 0, 0, 0}; for (int k = 0; k < 4; ++k) r[k] = a[k] + b[k]; return r; }
-Q subq(const Q& a, const Q& b) { Q r{0, 0, 0, 0}; for (int k = 0; k < 4; ++k) r[k] = a[k] - b[k]; return r; }
+// unused QN components are zero everywhere
+
+// ---- symmetry: component kinds (0 = U(1), 1 = SU(2)) ----------------------------
+int g_nq = 1;
+int g_kind[4] = {0, 0, 0, 0};
+bool g_nonabelian = false;
+
+// Symmetry::reduceSilent(a, b): all fusion outcomes, components varied from the
+// first (outermost) to the last
+std::vector<Q> fuse(const Q& a, const Q& b) {
+    std::vector<Q> out{Q{0, 0, 0, 0}};
+    for (int k = 0; k < g_nq; ++k) {
+        std::vector<Q> nxt;
+        for (const Q& p : out) {
+            if (g_kind[k] == 0) {
+                Q r = p; r[k] = a[k] + b[k]; nxt.push_back(r);
+            } else {
+                for (int q = std::abs(a[k] - b[k]) + 1; q <= a[k] + b[k] - 1; q += 2) { Q r = p; r[k] = q; nxt.push_back(r); }
+            }
+        }
+        out.swap(nxt);
+    }
+    return out;
+}
+// Symmetry::flip: U(1) -q, SU(2) q
+Q flipq(const Q& a) { Q r = a; for (int k = 0; k < g_nq; ++k) if (g_kind[k] == 0) r[k] = -a[k]; return r; }
+// Symmetry::validate({a, b, c}): c is among the fusion outcomes of a and b
+bool tri(const Q& a, const Q& b, const Q& c) {
+    for (int k = 0; k < g_nq; ++k) {
+        if (g_kind[k] == 0) { if (a[k] + b[k] != c[k]) return false; }
+        else if (c[k] < std::abs(a[k] - b[k]) + 1 || c[k] > a[k] + b[k] - 1 || ((a[k] + b[k] + c[k]) % 2) == 0) return false;
+    }
+    for (int k = g_nq; k < 4; ++k) if (a[k] + b[k] != c[k]) return false;
+    return true;
+}
+
+// ---- 6j and 9j symbols (arguments 2j) ---------------------------------------------
+// Racah's single-sum formula with the factorials themselves in long double (the
+// arguments stay small: a sum of four 2j values below ~60), 9j as the sum over x of
+// (2x+1) times three 6j (the standard reduction).
+long double fact(int n) {
+    static std::vector<long double> f;
+    if (f.empty()) { f.resize(171); f[0] = 1; for (int i = 1; i < 171; ++i) f[i] = f[i - 1] * i; }
+    return f[n];
+}
+bool tri2(int a, int b, int c) {
+    return a >= 0 && b >= 0 && c >= 0 && ((a + b + c) % 2 == 0) && c >= std::abs(a - b) && c <= a + b;
+}
+long double delta2(int a, int b, int c) {
+    return std::sqrt(fact((a + b - c) / 2) * fact((a - b + c) / 2) * fact((-a + b + c) / 2) / fact((a + b + c) / 2 + 1));
+}
+double sixj(int a, int b, int c, int d, int e, int f) {   // {a/2 b/2 c/2; d/2 e/2 f/2}
+    if (!tri2(a, b, c) || !tri2(a, e, f) || !tri2(d, b, f) || !tri2(d, e, c)) return 0.0;
+    const int t1 = (a + b + c) / 2, t2 = (a + e + f) / 2, t3 = (d + b + f) / 2, t4 = (d + e + c) / 2;
+    const int u1 = (a + b + d + e) / 2, u2 = (b + c + e + f) / 2, u3 = (c + a + f + d) / 2;
+    const int zmin = std::max(std::max(t1, t2), std::max(t3, t4)), zmax = std::min(u1, std::min(u2, u3));
+    long double sum = 0;
+    for (int z = zmin; z <= zmax; ++z) {
+        long double term = fact(z + 1) / (fact(z - t1) * fact(z - t2) * fact(z - t3) * fact(z - t4) * fact(u1 - z) *
+                                          fact(u2 - z) * fact(u3 - z));
+        sum += (z % 2) ? -term : term;
+    }
+    return (double)(sum * delta2(a, b, c) * delta2(a, e, f) * delta2(d, b, f) * delta2(d, e, c));
+}
+double ninej(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
+    if (!tri2(a, b, c) || !tri2(d, e, f) || !tri2(g, h, i) || !tri2(a, d, g) || !tri2(b, e, h) || !tri2(c, f, i))
+        return 0.0;
+    const int xmin = std::max(std::abs(a - i), std::max(std::abs(d - h), std::abs(b - f)));
+    const int xmax = std::min(a + i, std::min(d + h, b + f));
+    long double sum = 0;
+    for (int x = xmin; x <= xmax; x += 2) {
+        long double t = (long double)(x + 1) * sixj(a, d, g, h, i, x) * sixj(b, e, h, d, x, f) * sixj(c, f, i, x, a, b);
+        sum += (x % 2) ? -t : t;
+    }
+    return (double)sum;
+}
+// the coefficient families, product over the SU(2) components (q = 2S+1)
+double c9(const Q* q, int form) {   // form 0: HPsi / buildL / tensorProd, 1: buildR
+    double out = 1.0;
+    for (int k = 0; k < g_nq; ++k) {
+        if (g_kind[k] != 1) continue;
+        double v = ninej(q[0][k] - 1, q[1][k] - 1, q[2][k] - 1, q[3][k] - 1, q[4][k] - 1, q[5][k] - 1, q[6][k] - 1,
+                         q[7][k] - 1, q[8][k] - 1) *
+                   std::sqrt((double)q[6][k] * q[7][k] * q[2][k] * q[5][k]);
+        if (form == 1) v *= (double)q[8][k] / (double)q[6][k];
+        out *= v;
+    }
+    return out;
+}
+double c9(const Q& q1, const Q& q2, const Q& q3, const Q& q4, const Q& q5, const Q& q6, const Q& q7, const Q& q8,
+          const Q& q9, int form = 0) {
+    const Q q[9] = {q1, q2, q3, q4, q5, q6, q7, q8, q9};
+    return c9(q, form);
+}
+double capair(const Q& q1, const Q& q2, const Q& q3, const Q& q4, const Q& q5, const Q& q6) {
+    double out = 1.0;
+    for (int k = 0; k < g_nq; ++k) {
+        if (g_kind[k] != 1) continue;
+        const int ph = (q1[k] + q2[k] + q4[k] + q5[k] - 4) / 2;
+        out *= sixj(q1[k] - 1, q2[k] - 1, q3[k] - 1, q4[k] - 1, q5[k] - 1, q6[k] - 1) * std::sqrt((double)q3[k] * q6[k]) *
+               ((ph % 2) ? -1.0 : 1.0);
+    }
+    return out;
+}
+constexpr double kCgcEps = 2.220446049250313e-16;   // mynumeric_limits<double>::epsilon()
 
 // ---- GEMM ------------------------------------------------------------------
 typedef void (*dgemm_t)(const char*, const char*, const int64_t*, const int64_t*, const int64_t*, const double*,
@@ -200,11 +312,6 @@ Mpo read_mpo(int nq, int64_t nnz, const int32_t* s1, const int32_t* s2, const in
         m.W[((size_t)s1[i] * nloc + s2[i]) * nop + k[i]][Q2{rd(qin, i), rd(qout, i)}].push_back(Nz{row[i], col[i], val[i]});
     return m;
 }
-// U(1) validate({a,b,c}) (symmetry/U1.h:476-482, S1xS2.h:729-743)
-bool tri(const Q& a, const Q& b, const Q& c) {
-    for (int k = 0; k < 4; ++k) if (a[k] + b[k] != c[k]) return false;
-    return true;
-}
 
 // ---- precalc results (the reference's qlhs / qrhs / factor_cgcs) ---------------
 struct Task1 { int s2; int64_t q2; int qL, qR, k; Q2 qW; double cgc; };
@@ -224,6 +331,7 @@ struct Pivot {
     int64_t n_tasks = 0;
 };
 
+// precalc_blockStructure, 1-site (tensors/DmrgIndexGymnastics.h:487-590) with LAWA (:32-77)
 void precalc1(Pivot& P) {
     const Mpo& W = P.W12;
     BipedVec Vb = bipeds(P.V, W.nloc);
@@ -234,23 +342,29 @@ void precalc1(Pivot& P) {
         if (!tri(W.qloc[s2], W.qop[k], W.qloc[s1])) continue;
         for (int qL = 0; qL < (int)P.Lt.keys.size(); ++qL) {
             const Q Lin = P.Lt.keys[qL][0], Lout = P.Lt.keys[qL][1], Lmid = P.Lt.keys[qL][2];
-            // LAWA, U(1) fusion has a single outcome
-            const Q Rout = addq(Lin, W.qloc[s1]);
-            int64_t qAbra = bfind(Vb, s1, Lin, Rout);
-            if (qAbra < 0) continue;
-            const Q Rin = addq(Lout, W.qloc[s2]);
-            int64_t qAket = bfind(Vb, s2, Lout, Rin);
-            if (qAket < 0) continue;
-            const Q Rmid = addq(Lmid, W.qop[k]);
-            const auto* nz = W.find(s1, s2, k, Lmid, Rmid);
-            if (!nz || !tri(Rin, Rmid, Rout)) continue;
-            auto itR = P.Rt.dict.find(Q3{Rin, Rout, Rmid});
-            if (itR == P.Rt.dict.end()) continue;
-            bool empty = true;
-            for (const auto& e : *nz)
-                if (aux_at(P.Lt, qL, e.row) >= 0 && aux_at(P.Rt, itR->second, e.col) >= 0) empty = false;
-            if (empty) continue;
-            lookup[qAbra].push_back(Task1{s2, qAket, qL, itR->second, k, Q2{Lmid, Rmid}, 1.0});
+            for (const Q& Rout : fuse(Lin, W.qloc[s1])) {
+                int64_t qAbra = bfind(Vb, s1, Lin, Rout);
+                if (qAbra < 0) continue;
+                for (const Q& Rin : fuse(Lout, W.qloc[s2])) {
+                    int64_t qAket = bfind(Vb, s2, Lout, Rin);
+                    if (qAket < 0) continue;
+                    for (const Q& Rmid : fuse(Lmid, W.qop[k])) {
+                        const auto* nz = W.find(s1, s2, k, Lmid, Rmid);
+                        if (!nz || !tri(Rin, Rmid, Rout)) continue;
+                        auto itR = P.Rt.dict.find(Q3{Rin, Rout, Rmid});
+                        if (itR == P.Rt.dict.end()) continue;
+                        bool empty = true;
+                        for (const auto& e : *nz)
+                            if (aux_at(P.Lt, qL, e.row) >= 0 && aux_at(P.Rt, itR->second, e.col) >= 0) empty = false;
+                        if (empty) continue;
+                        const double cgc = g_nonabelian ? c9(Lout, W.qloc[s2], Rin, Lmid, W.qop[k], Rmid, Lin,
+                                                             W.qloc[s1], Rout)
+                                                        : 1.0;
+                        if (std::abs(cgc) < kCgcEps) continue;
+                        lookup[qAbra].push_back(Task1{s2, qAket, qL, itR->second, k, Q2{Lmid, Rmid}, cgc});
+                    }
+                }
+            }
         }
     }
     for (auto& kv : lookup) {
@@ -260,8 +374,9 @@ void precalc1(Pivot& P) {
     }
 }
 
-// combined two-site index (Qbasis::combine + leftOffset), abelian
-std::map<std::pair<int, int>, int> combine_index(const std::vector<Q>& q12, const std::vector<Q>& q34) {
+// combined two-site index of Qbasis::combine + outer_num + leftOffset
+// (tensors/Qbasis.h:438-463, :685-798): key (s1, s3, merged QN) -> combined index
+std::map<std::tuple<int, int, Q>, int> combine_index(const std::vector<Q>& q12, const std::vector<Q>& q34) {
     // distinct QNs and inner indices in order of appearance (Qbasis::pullData)
     auto pull = [](const std::vector<Q>& qs, std::vector<Q>& dq, std::vector<int>& dd, std::vector<int>& inner) {
         for (const Q& q : qs) {
@@ -275,9 +390,11 @@ std::map<std::pair<int, int>, int> combine_index(const std::vector<Q>& q12, cons
     std::vector<int> n1, n2, i1, i2;
     pull(q12, d1, n1, i1);
     pull(q34, d2, n2, i2);
+    // history per merged QN: the source pairs (q1, q2), sorted; merged QNs in sorted order
     std::map<Q, std::vector<std::tuple<Q, Q, int, int>>> hist;
     for (size_t a = 0; a < d1.size(); ++a)
-        for (size_t b = 0; b < d2.size(); ++b) hist[addq(d1[a], d2[b])].push_back({d1[a], d2[b], n1[a], n2[b]});
+        for (size_t b = 0; b < d2.size(); ++b)
+            for (const Q& qm : fuse(d1[a], d2[b])) hist[qm].push_back({d1[a], d2[b], n1[a], n2[b]});
     for (auto& kv : hist) std::sort(kv.second.begin(), kv.second.end());
     std::map<Q, int> start;
     int cur = 0;
@@ -285,20 +402,21 @@ std::map<std::pair<int, int>, int> combine_index(const std::vector<Q>& q12, cons
         start[kv.first] = cur;
         for (auto& e : kv.second) cur += std::get<2>(e) * std::get<3>(e);
     }
-    std::map<std::pair<int, int>, int> idx;
+    std::map<std::tuple<int, int, Q>, int> idx;
     for (size_t s1 = 0; s1 < q12.size(); ++s1)
-        for (size_t s3 = 0; s3 < q34.size(); ++s3) {
-            Q qm = addq(q12[s1], q34[s3]);
-            int off = 0;
-            for (auto& e : hist[qm]) {
-                if (std::get<0>(e) == q12[s1] && std::get<1>(e) == q34[s3]) { off += i1[s1] + std::get<2>(e) * i2[s3]; break; }
-                off += std::get<2>(e) * std::get<3>(e);
+        for (size_t s3 = 0; s3 < q34.size(); ++s3)
+            for (const Q& qm : fuse(q12[s1], q34[s3])) {
+                int off = 0;
+                for (auto& e : hist[qm]) {
+                    if (std::get<0>(e) == q12[s1] && std::get<1>(e) == q34[s3]) { off += i1[s1] + std::get<2>(e) * i2[s3]; break; }
+                    off += std::get<2>(e) * std::get<3>(e);
+                }
+                idx[{(int)s1, (int)s3, qm}] = start[qm] + off;
             }
-            idx[{(int)s1, (int)s3}] = start[qm] + off;
-        }
     return idx;
 }
 
+// precalc_blockStructure, 2-site (tensors/DmrgIndexGymnastics.h:699-856) with AAWWAA (:198-262)
 void precalc2(Pivot& P) {
     const Mpo &W12 = P.W12, &W34 = P.W34;
     auto cidx = combine_index(W12.qloc, W34.qloc);
@@ -314,26 +432,41 @@ void precalc2(Pivot& P) {
         for (int s4 = 0; s4 < W34.nloc; ++s4)
         for (int k34 = 0; k34 < W34.nop; ++k34) {
             if (!tri(W34.qloc[s4], W34.qop[k34], W34.qloc[s3])) continue;
-            const Q qm13 = addq(W12.qloc[s1], W34.qloc[s3]), qm24 = addq(W12.qloc[s2], W34.qloc[s4]);
-            const int s1s3 = cidx[{s1, s3}], s2s4 = cidx[{s2, s4}];
-            for (int qL = 0; qL < (int)P.Lt.keys.size(); ++qL) {
-                const Q Lin = P.Lt.keys[qL][0], Lout = P.Lt.keys[qL][1], Lmid = P.Lt.keys[qL][2];
-                // AAWWAA
-                const Q qRout = addq(Lin, qm13);
-                int64_t q13 = bfind(Vb, s1s3, Lin, qRout);
-                if (q13 < 0) continue;
-                const Q qRin = addq(Lout, qm24);
-                int64_t q24 = bfind(Vb, s2s4, Lout, qRin);
-                if (q24 < 0) continue;
-                const Q qW = addq(Lmid, W12.qop[k12]);
-                if (!W12.find(s1, s2, k12, Lmid, qW)) continue;
-                const Q qRmid = addq(qW, W34.qop[k34]);
-                if (!W34.find(s3, s4, k34, qW, qRmid)) continue;
-                if (!tri(qRin, qRmid, qRout)) continue;
-                auto itR = P.Rt.dict.find(Q3{qRin, qRout, qRmid});
-                if (itR == P.Rt.dict.end()) continue;
-                lookup[q13].push_back(Task2{q24, qL, itR->second, s1, s2, k12, Q2{Lmid, qW}, s3, s4, k34,
-                                            Q2{qW, qRmid}, 1.0});
+            for (const Q& qOp : fuse(W12.qop[k12], W34.qop[k34]))
+            for (const Q& qm13 : fuse(W12.qloc[s1], W34.qloc[s3]))
+            for (const Q& qm24 : fuse(W12.qloc[s2], W34.qloc[s4])) {
+                const int s1s3 = cidx[{s1, s3, qm13}], s2s4 = cidx[{s2, s4, qm24}];
+                const double cgc9 = g_nonabelian ? c9(W12.qloc[s2], W34.qloc[s4], qm24, W12.qop[k12], W34.qop[k34], qOp,
+                                                      W12.qloc[s1], W34.qloc[s3], qm13)
+                                                 : 1.0;
+                if (std::abs(cgc9) < kCgcEps) continue;
+                for (int qL = 0; qL < (int)P.Lt.keys.size(); ++qL) {
+                    const Q Lin = P.Lt.keys[qL][0], Lout = P.Lt.keys[qL][1], Lmid = P.Lt.keys[qL][2];
+                    for (const Q& qRout : fuse(Lin, qm13)) {
+                        int64_t q13 = bfind(Vb, s1s3, Lin, qRout);
+                        if (q13 < 0) continue;
+                        for (const Q& qRin : fuse(Lout, qm24)) {
+                            int64_t q24 = bfind(Vb, s2s4, Lout, qRin);
+                            if (q24 < 0) continue;
+                            for (const Q& qW : fuse(Lmid, W12.qop[k12])) {
+                                if (!W12.find(s1, s2, k12, Lmid, qW)) continue;
+                                for (const Q& qRmid : fuse(qW, W34.qop[k34])) {
+                                    if (!W34.find(s3, s4, k34, qW, qRmid)) continue;
+                                    if (!tri(qRin, qRmid, qRout)) continue;
+                                    const double cgc6 =
+                                        g_nonabelian ? capair(Lmid, W12.qop[k12], qW, W34.qop[k34], qRmid, qOp) : 1.0;
+                                    if (std::abs(cgc6) < kCgcEps) continue;
+                                    auto itR = P.Rt.dict.find(Q3{qRin, qRout, qRmid});
+                                    if (itR == P.Rt.dict.end()) continue;
+                                    const double cgcH =
+                                        g_nonabelian ? c9(Lout, qm24, qRin, Lmid, qOp, qRmid, Lin, qm13, qRout) : 1.0;
+                                    lookup[q13].push_back(Task2{q24, qL, itR->second, s1, s2, k12, Q2{Lmid, qW}, s3, s4,
+                                                                k34, Q2{qW, qRmid}, cgc6 * cgc9 * cgcH});
+                                }
+                            }
+                        }
+                    }
+                }
             }
         }
     }
@@ -450,35 +583,60 @@ void env_plan(Env& V) {
         for (int qE = 0; qE < (int)Et.keys.size(); ++qE) {
             const Q Ein = Et.keys[qE][0], Eout = Et.keys[qE][1], Emid = Et.keys[qE][2];
             if (V.side == 0) {
-                const Q Rout = addq(Ein, W.qloc[s1]), Rin = addq(Eout, W.qloc[s2]), Rmid = addq(Emid, W.qop[k]);
-                int64_t qb = bfind(Bb, s1, Ein, Rout), qk = bfind(Kb, s2, Eout, Rin);
-                if (qb < 0 || qk < 0) continue;
-                const auto* nz = W.find(s1, s2, k, Emid, Rmid);
-                if (!nz || !tri(Rin, Rmid, Rout)) continue;
-                for (const auto& e : *nz) {
-                    if (V.mode == 1 && !(V.at(Emid, e.row) > V.fixed_ab)) continue;
-                    if (V.mode == 3 && V.at(Rmid, e.col) != V.fixed_ab) continue;
-                    if (V.mode == 2 && V.at(Emid, e.row) != V.fixed_ab) continue;
-                    int64_t la = aux_at(Et, qE, e.row);
-                    if (la < 0) continue;
-                    int64_t o = oblock(Q3{Rout, Rin, Rmid}, e.col, V.B.cols[qb], V.K.cols[qk]);
-                    items.push_back(Env::Item{o, qb, la, qk, e.val});
+                // contract_L (tensors/DmrgContractions.h:34-158): LAWA, then the key {Rout, Rin, Rmid}
+                for (const Q& Rout : fuse(Ein, W.qloc[s1])) {
+                    int64_t qb = bfind(Bb, s1, Ein, Rout);
+                    if (qb < 0) continue;
+                    for (const Q& Rin : fuse(Eout, W.qloc[s2])) {
+                        int64_t qk = bfind(Kb, s2, Eout, Rin);
+                        if (qk < 0) continue;
+                        for (const Q& Rmid : fuse(Emid, W.qop[k])) {
+                            const auto* nz = W.find(s1, s2, k, Emid, Rmid);
+                            if (!nz || !tri(Rin, Rmid, Rout)) continue;
+                            const double cgc = g_nonabelian ? c9(Eout, W.qloc[s2], Rin, Emid, W.qop[k], Rmid, Ein,
+                                                                 W.qloc[s1], Rout)
+                                                            : 1.0;
+                            if (std::abs(cgc) < kCgcEps) continue;
+                            for (const auto& e : *nz) {
+                                if (V.mode == 1 && !(V.at(Emid, e.row) > V.fixed_ab)) continue;
+                                if (V.mode == 3 && V.at(Rmid, e.col) != V.fixed_ab) continue;
+                                if (V.mode == 2 && V.at(Emid, e.row) != V.fixed_ab) continue;
+                                int64_t la = aux_at(Et, qE, e.row);
+                                if (la < 0) continue;
+                                int64_t o = oblock(Q3{Rout, Rin, Rmid}, e.col, V.B.cols[qb], V.K.cols[qk]);
+                                items.push_back(Env::Item{o, qb, la, qk, cgc * e.val});
+                            }
+                        }
+                    }
                 }
             } else {
+                // contract_R (tensors/DmrgContractions.h:179-311): AWAR (DmrgIndexGymnastics.h:79-124),
+                // then the key {Lout, Lin, Lmid}
                 const Q Rin = Ein, Rout = Eout, Rmid = Emid;
-                const Q Lin = subq(Rout, W.qloc[s1]), Lout = subq(Rin, W.qloc[s2]), Lmid = subq(Rmid, W.qop[k]);
-                int64_t qb = bfind(Bb, s1, Lin, Rout), qk = bfind(Kb, s2, Lout, Rin);
-                if (qb < 0 || qk < 0) continue;
-                const auto* nz = W.find(s1, s2, k, Lmid, Rmid);
-                if (!nz || !tri(Lout, Lmid, Lin)) continue;
-                for (const auto& e : *nz) {
-                    if (V.mode == 1 && !(V.fixed_ab > V.at(Rmid, e.col))) continue;
-                    if (V.mode == 2 && V.at(Lmid, e.row) != V.fixed_ab) continue;
-                    if (V.mode == 3 && V.at(Rmid, e.col) != V.fixed_ab) continue;
-                    int64_t rb = aux_at(Et, qE, e.col);
-                    if (rb < 0) continue;
-                    int64_t o = oblock(Q3{Lout, Lin, Lmid}, e.row, V.K.rows[qk], V.B.rows[qb]);
-                    items.push_back(Env::Item{o, qk, rb, qb, e.val});
+                for (const Q& Lin : fuse(Rout, flipq(W.qloc[s1]))) {
+                    int64_t qb = bfind(Bb, s1, Lin, Rout);
+                    if (qb < 0) continue;
+                    for (const Q& Lout : fuse(Rin, flipq(W.qloc[s2]))) {
+                        int64_t qk = bfind(Kb, s2, Lout, Rin);
+                        if (qk < 0) continue;
+                        for (const Q& Lmid : fuse(Rmid, flipq(W.qop[k]))) {
+                            const auto* nz = W.find(s1, s2, k, Lmid, Rmid);
+                            if (!nz || !tri(Lout, Lmid, Lin)) continue;
+                            const double cgc = g_nonabelian ? c9(Lout, W.qloc[s2], Rin, Lmid, W.qop[k], Rmid, Lin,
+                                                                 W.qloc[s1], Rout, 1)
+                                                            : 1.0;
+                            if (std::abs(cgc) < kCgcEps) continue;
+                            for (const auto& e : *nz) {
+                                if (V.mode == 1 && !(V.fixed_ab > V.at(Rmid, e.col))) continue;
+                                if (V.mode == 2 && V.at(Lmid, e.row) != V.fixed_ab) continue;
+                                if (V.mode == 3 && V.at(Rmid, e.col) != V.fixed_ab) continue;
+                                int64_t rb = aux_at(Et, qE, e.col);
+                                if (rb < 0) continue;
+                                int64_t o = oblock(Q3{Lout, Lin, Lmid}, e.row, V.K.rows[qk], V.B.rows[qb]);
+                                items.push_back(Env::Item{o, qk, rb, qb, cgc * e.val});
+                            }
+                        }
+                    }
                 }
             }
         }
@@ -528,6 +686,20 @@ int oracle_set_blas(const char* path) {
         }
     }
     return -2;
+}
+
+// QN component kinds of the objects created next: 0 = U(1), 1 = SU(2)
+void oracle_set_symmetry(int nq, const int32_t* kinds) {
+    g_nq = std::max(1, std::min(nq, 4));
+    g_nonabelian = false;
+    for (int k = 0; k < 4; ++k) {
+        g_kind[k] = (k < g_nq && kinds) ? kinds[k] : 0;
+        if (g_kind[k] == 1) g_nonabelian = true;
+    }
+}
+double oracle_coupling_6j(int a, int b, int c, int d, int e, int f) { return sixj(a, b, c, d, e, f); }
+double oracle_coupling_9j(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
+    return ninej(a, b, c, d, e, f, g, h, i);
 }
 
 void oracle_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
