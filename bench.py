@@ -285,6 +285,21 @@ def su2_cylinder_bench(ctx, args):
     e64, _, l64 = H.lanczos(v0, "fp64", max_iter=300, **tol)
     es, _, ls = H.lanczos(v0, args.precision, max_iter=300, refine_iters=4, **tol)
     H.close()
+    orc = None
+    if not args.no_cpu:
+        # the same pivot on the oracle's SU(2) restatement: both HxVs of V, and the
+        # ground-state energy from the oracle's Lanczos on the dot-weighted operator
+        import oracle
+        oracle.set_threads(os.cpu_count() or 1)
+        op = oracle.OraclePivot(2, model.sym.nq, Lenv, Renv, V, W1, W2, sym=model.sym)
+        t0 = time.perf_counter()
+        ref = op.hxv(V.data)
+        w = oracle.dot_weights(V, model.sym)
+        e_or, steps = oracle.lanczos_ground(lambda x: w * op.hxv(x / w), w * v0, tol=1e-14)
+        orc = {"hxv_fp64_rel_err": float(np.linalg.norm(h64 - ref) / np.linalg.norm(ref)),
+               "hxv_split_rel_err": float(np.linalg.norm(hs - ref) / np.linalg.norm(ref)),
+               "E_oracle": e_or, "oracle_lanczos_steps": steps, "oracle_s": round(time.perf_counter() - t0, 1),
+               "E_fp64_rel_err": abs(e64 - e_or) / abs(e_or), "E_split_rel_err": abs(es - e_or) / abs(e_or)}
     # single-site DMRG sweep of the cylinder: one sweep in each precision from the same
     # seeded MPS (D=2000 multiplets, centre on site 0)
     import copy
@@ -304,6 +319,7 @@ def su2_cylinder_bench(ctx, args):
                            "tensor_tflops_issued": (sts["tensor_flops_phase1"] + sts["tensor_flops_phase2"]) /
                            mss * 1e-9},
                 split_over_fp64=ms64 / mss, hxv_split_rel_err=err,
+                oracle=orc,
                 lanczos={"E_fp64": e64, "E_split": es, "rel_diff": abs(es - e64) / abs(e64),
                          "ms_fp64": l64["ms_total"], "ms_split": ls["ms_total"],
                          "hxv_fp64": l64["hxv_fp64"], "split_hxv": [ls["hxv_split"], ls["hxv_fp64"]]})

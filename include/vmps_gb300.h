@@ -133,6 +133,15 @@ typedef struct vmps_dvec_s  vmps_dvec;
 /* ---- context ----------------------------------------------------------------*/
 int         vmps_ctx_create(int device, vmps_ctx** out);
 int         vmps_ctx_destroy(vmps_ctx* ctx);
+/* Clock-cycle budget of every main-loop barrier wait in the split-precision
+ * (tcgen05) engine of this context; 0 restores the default (about 2 s).  When a
+ * wait runs out the kernel stops issuing work, lets the copies and tensor-core
+ * operations already in flight finish (those drain waits keep the full budget),
+ * releases its tensor memory and returns; the call then fails with
+ * VMPS_E_TIMEOUT and the context stays usable.  A budget shorter than the
+ * engine's normal wait times makes that path run on purpose (failure tests).
+ * The reference has no device waits; this has no counterpart there.           */
+int         vmps_ctx_set_wait_budget(vmps_ctx* ctx, int64_t cycles);
 const char* vmps_last_error(void);
 const char* vmps_version(void);
 
@@ -231,7 +240,8 @@ int vmps_hxv_time(vmps_pivot* p, const vmps_dvec* vin, vmps_dvec* vout, int prec
  * Lanczos steps (a cost model of the two plans, so the choice is the same in every
  * run) the residual instead drives a Jacobi-Davidson correction inside the split
  * Krylov space, followed by FP64 Lanczos steps; the environment variable
- * VMPS_LANCZOS_REFINE = rounds | polish | auto overrides the choice.  refine_iters
+ * VMPS_LANCZOS_REFINE = rounds | polish | auto overrides the choice, and
+ * VMPS_LANCZOS_PROBE = off skips the FP64 probe (the split phase always runs).  refine_iters
  * counts the FP64 HxVs after the Krylov phase (the probe is one more).
  * Krylov vectors, dots and the tridiagonal solve are FP64 throughout.  v (compact
  * layout) is the start vector on entry and the ground state on exit.

@@ -274,3 +274,20 @@ class OracleTerms:
         for a in self.A0:
             out += self.E * float(a @ vin) * a
         return out
+
+
+def dot_weights(V, sym):
+    """sqrt(coeff_dot(qout)) per element of a PivotVector layout (SU(2) components: the
+    multiplet dimension q; pivot/DmrgPivotVector.h:296-339 weights every block's
+    Frobenius product by it).  Scaling a vector by these turns the weighted dot into
+    a plain one, which makes the SU(2) HxV symmetric for a plain Lanczos."""
+    kinds = getattr(sym, "kinds", ())
+    w = np.ones(V.data.size)
+    for i in range(V.n):
+        q = 1.0
+        for k, name in enumerate(kinds):
+            if name == "SU2":
+                q *= float(V.qout[i][k])
+        o, n = int(V.offset[i]), int(V.rows[i] * V.cols[i])
+        w[o:o + n] = np.sqrt(q)
+    return w

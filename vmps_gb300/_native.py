@@ -90,6 +90,7 @@ _PROTOS = [
     ("vmps_version", C.c_char_p, []),
     ("vmps_ctx_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     ("vmps_ctx_destroy", C.c_int, [C.c_void_p]),
+    ("vmps_ctx_set_wait_budget", C.c_int, [C.c_void_p, C.c_int64]),
     ("vmps_pivot1_create", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
                                      C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_mpo_site),
                                      C.POINTER(vmps_blocks), C.POINTER(C.c_void_p)]),

@@ -22,6 +22,7 @@ struct GGArgs {
     int ntiles;
     int transA, transB, transC;
     int64_t vstride;   // multi-RHS phase 2: element stride between the output vectors
+    long long wait_budget;   // tcgen05 engine: clock cycles a main-loop barrier wait may take (0: ~2 s)
 };
 
 // tcgen05 engine: TMA descriptors of a phase, passed by value as a grid-constant

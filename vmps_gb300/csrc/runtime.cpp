@@ -44,6 +44,10 @@ void set_last_error_message(const std::string& msg) { g_last_error = msg; }
 struct CudaFail : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
+// a bounded device wait gave up (the device error word was set)
+struct WaitTimeout : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
 #define CK(call)                                                                                         \
     do {                                                                                                 \
         cudaError_t e_ = (call);                                                                         \
@@ -55,6 +59,7 @@ struct CudaFail : std::runtime_error {
 #define API_BEGIN try {
 #define API_END                                                                 \
     }                                                                           \
+    catch (const WaitTimeout& e) { return set_err(VMPS_E_TIMEOUT, e.what()); }  \
     catch (const CudaFail& e) { return set_err(VMPS_E_CUDA, e.what()); }        \
     catch (const std::bad_alloc& e) { return set_err(VMPS_E_NOMEM, e.what()); } \
     catch (const std::domain_error& e) { return set_err(VMPS_E_SHAPE, e.what()); } \
@@ -129,6 +134,7 @@ struct vmps_ctx_s {
     int* err = nullptr;   // device error word written by the tcgen05 engine
     bool pageable_access = false;   // the device reads pageable host memory in place
     int num_sms = 152;              // CTAs of the persistent tcgen05 engine (host-only: GB300's count)
+    long long wait_budget = 0;      // main-loop wait budget of the tcgen05 engine in cycles (0: ~2 s)
 };
 
 // read and clear the device error word (after the stream has been synchronised)
@@ -139,7 +145,7 @@ static void check_device_error(vmps_ctx* c) {
     CK(cudaStreamSynchronize(c->stream));
     if (h) {
         CK(cudaMemsetAsync(c->err, 0, 4, c->stream));
-        throw CudaFail("a bounded device wait in the tcgen05 engine ran out (error word " + std::to_string(h) + ")");
+        throw WaitTimeout("a bounded device wait in the tcgen05 engine ran out (error word " + std::to_string(h) + ")");
     }
 }
 
@@ -403,6 +409,7 @@ struct Operands {
     float* Of = nullptr;
     // pivots with an excited-state projector: applied after the second phase
     const PenaltyArgs* pen = nullptr;
+    long long wait_budget = 0;   // tcgen05 engine main-loop wait budget (cycles, 0: default)
 };
 
 // Invariants the tcgen05 engine relies on, checked on the host once per plan:
@@ -523,6 +530,7 @@ static void run_phase_on(const DevPlan& dp, int ph, const DevPhase& d, const Pha
     a.ntiles = d.ntiles;
     a.transA = h.transA; a.transB = h.transB; a.transC = h.transC;
     a.err = ops.err;
+    a.wait_budget = ops.wait_budget;
     if (!dp.plan.split) {
         auto slot = [&](int s) -> const void* {
             switch (s) {
@@ -832,6 +840,7 @@ static void hxv_host_pipelined(vmps_pivot* p, DevPlan& dp, const double* vin, do
     ops.Y = din;
     ops.O = ch.compact_out ? sout : dout;
     ops.err = p->ctx->err;
+    ops.wait_budget = p->ctx->wait_budget;
     const int kin = (int)ch.in.size(), kout = (int)ch.out.size();
     // the copy stream starts after everything already queued on the compute stream
     CK(cudaEventRecord(ch.ev_start, cs));
@@ -874,6 +883,7 @@ static Operands pivot_ops(const vmps_pivot* p) {
     ops.X = p->dL.as<double>();
     ops.Z = p->dR.as<double>();
     ops.err = p->ctx->err;
+    ops.wait_budget = p->ctx->wait_budget;
     if (p->pen.npen > 0) ops.pen = &p->pen;
     return ops;
 }
@@ -986,6 +996,13 @@ int vmps_ctx_create(int device, vmps_ctx** out) {
     CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
     *out = c;
     API_END
+}
+
+int vmps_ctx_set_wait_budget(vmps_ctx* ctx, int64_t cycles) {
+    if (!ctx) return set_err(VMPS_E_ARG, "null context");
+    if (cycles < 0) return set_err(VMPS_E_ARG, "negative wait budget");
+    ctx->wait_budget = (long long)cycles;
+    return VMPS_OK;
 }
 
 int vmps_ctx_destroy(vmps_ctx* ctx) {
@@ -1815,6 +1832,15 @@ int refine_mode() {
     if (!std::strcmp(v, "polish")) return 2;
     throw std::invalid_argument("VMPS_LANCZOS_REFINE must be auto, rounds or polish");
 }
+// VMPS_LANCZOS_PROBE = off: split-precision solves skip the FP64 probe, so the
+// split phase runs even from a start vector that is already an eigenvector to
+// the split operator's noise level; unset or on keeps the probe
+bool probe_enabled() {
+    const char* v = std::getenv("VMPS_LANCZOS_PROBE");
+    if (!v || !*v || !std::strcmp(v, "on")) return true;
+    if (!std::strcmp(v, "off")) return false;
+    throw std::invalid_argument("VMPS_LANCZOS_PROBE must be on or off");
+}
 }  // namespace
 
 extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_iter, double tol_eigval,
@@ -1855,7 +1881,7 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
         s.ms_host += r.ms_host;
     };
     bool split_phase = true;
-    if (refine) {
+    if (refine && probe_enabled()) {
         // Probe: FP64 Lanczos whose first iteration gives the start vector's
         // FP64 residual.  A start vector already within a few times the split
         // operator's noise of an eigenvector (late sweeps) gains nothing from

@@ -76,12 +76,13 @@ __device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity, volati
         if (clock64() - t0 > um::WAIT_BUDGET) { *fail = 1; return; }
 }
 // bounded wait on the phase of the given parity; false when the clock budget ran
-// out or another role has already given up (the failure word is then set)
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* fail) {
+// out or another role has already given up (the failure word is then set).
+// budget: clock cycles (the main loops pass the kernel's budget; drains use WAIT_BUDGET)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* fail, long long budget) {
     const long long t0 = clock64();
     while (!mbar_test(bar, parity)) {
         if (*fail) return false;
-        if (clock64() - t0 > um::WAIT_BUDGET) { *fail = 1; return false; }
+        if (clock64() - t0 > budget) { *fail = 1; return false; }
     }
     return true;
 }
@@ -189,6 +190,8 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     const int t0 = g.cta_tiles[blockIdx.x], t1 = g.cta_tiles[blockIdx.x + 1];
+    // main-loop waits give up after wb cycles; the drains before exit keep the full budget
+    const long long wb = g.wait_budget > 0 ? g.wait_budget : WAIT_BUDGET;
 
     if (warp == 0) {
         // ---------------- TMA producer
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
             int go = 1;
             if (lane == 0) {
                 const int st = it % STAGES, use = it / STAGES;
-                if (*s_fail || (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), s_fail))) {
+                if (*s_fail || (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), s_fail, wb))) {
                     go = 0;
                 } else {
                     const uint32_t sb = ring + st * STAGE_BYTES;
@@ -252,12 +255,12 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
             const int nsteps = tile.nsteps;
             const uint32_t idesc = IDESC_BASE | ((uint32_t)(((tile.tn + 15) & ~15) >> 3) << 17);   // N = round16(tn)
             const int buf = lt & 1, buse = lt >> 1;
-            if (buse >= 1 && !mbar_wait(bar(2 * STAGES + 2 + buf), (uint32_t)((buse - 1) & 1), s_fail)) break;
+            if (buse >= 1 && !mbar_wait(bar(2 * STAGES + 2 + buf), (uint32_t)((buse - 1) & 1), s_fail, wb)) break;
             tc_fence_after();
             const uint32_t dacc = tmem + (uint32_t)buf * ACC_COLS;
             for (int k = 0; k < nsteps; ++k, ++it) {
                 const int st = it % STAGES, use = it / STAGES;
-                if (!mbar_wait(bar(st), (uint32_t)(use & 1), s_fail)) break;
+                if (!mbar_wait(bar(st), (uint32_t)(use & 1), s_fail, wb)) break;
                 tc_fence_after();
                 const uint32_t sb = ring + st * STAGE_BYTES;
                 const uint64_t a = sw128_desc(sb), b = sw128_desc(sb + A_BYTES);
@@ -289,7 +292,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
             const GTile tile = g.tiles[t];
             const int buf = lt & 1, buse = lt >> 1;
             // warp-uniform outcome: the tensor-memory loads below are warp-collective
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(bar(2 * STAGES + buf), (uint32_t)(buse & 1), s_fail));
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(bar(2 * STAGES + buf), (uint32_t)(buse & 1), s_fail, wb));
             if (!ok) break;
             tc_fence_after();
             const int ncols = tile.tn;

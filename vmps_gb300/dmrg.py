@@ -20,6 +20,8 @@ site) and "lr" (contract_L / contract_R).
 """
 from __future__ import annotations
 
+import contextlib
+import os
 import time
 
 import numpy as np
@@ -39,6 +41,24 @@ def _count(counts, st):
         counts[k] = counts.get(k, 0) + int(st[k])
 
 
+@contextlib.contextmanager
+def _probe_setting(probe):
+    """probe=False: split-precision solves skip the FP64 probe (VMPS_LANCZOS_PROBE=off)
+    for the duration of the sweeps"""
+    if probe:
+        yield
+        return
+    old = os.environ.get("VMPS_LANCZOS_PROBE")
+    os.environ["VMPS_LANCZOS_PROBE"] = "off"
+    try:
+        yield
+    finally:
+        if old is None:
+            del os.environ["VMPS_LANCZOS_PROBE"]
+        else:
+            os.environ["VMPS_LANCZOS_PROBE"] = old
+
+
 def _push_right(A_next, Rfac):
     """A_next[s](qin, qout) <- R[qin] @ A_next[s](qin, qout)"""
     for i in range(A_next.n):
@@ -55,11 +75,18 @@ def _push_left(A_prev, Lfac):
 
 
 def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigval=1e-12, tol_state=1e-8,
-          refine_iters=0, verbose=False, pool=None):
+          refine_iters=0, verbose=False, pool=None, probe=True):
     """Run n_sweeps full sweeps of single-site DMRG; returns energies and timings.
     `mps` must be right-canonical with the gauge centre on site 0.  The QR / LQ gauge
     steps run on the host cores (`pool`, a hostla.SectorPool; one is made if none is
-    given)."""
+    given).  The result's `steps` lists every local solve: its energy and its HxV
+    counts per precision.  probe=False makes split-precision solves skip the FP64 probe."""
+    with _probe_setting(probe):
+        return _dmrg1(ctx, model, mps, n_sweeps, precision, max_iter, tol_eigval, tol_state, refine_iters, verbose,
+                      pool)
+
+
+def _dmrg1(ctx, model, mps, n_sweeps, precision, max_iter, tol_eigval, tol_state, refine_iters, verbose, pool):
     sym, L = model.sym, model.L
     nq = sym.nq
     own_pool = pool is None
@@ -76,7 +103,7 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
         envR[l] = e.run(envR[l + 1], mps.A[l], mps.A[l])
         e.close()
     t_init = time.perf_counter() - t0
-    energies, sweep_times, timers, solves, hxv = [], [], [], [], 0
+    energies, sweep_times, timers, solves, hxv, steps = [], [], [], [], 0, []
     E = None
     clock = time.perf_counter
     for sweep in range(n_sweeps):
@@ -94,6 +121,7 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
                                  tol_state=tol_state, refine_iters=refine_iters)
             hxv += st["hxv_fp64"] + st["hxv_split"]
             _count(counts, st)
+            steps.append((sweep, l, E, st["hxv_split"], st["hxv_fp64"]))
             H.close()
             t2 = clock()
             tm["precalc"] += t1 - t
@@ -125,7 +153,7 @@ def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigva
     if own_pool:
         pool.close()
     return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv,
-                       solves=solves)
+                       solves=solves, steps=steps)
 
 
 def _env(ctx, sym, side, E, A, W):
@@ -136,7 +164,8 @@ def _env(ctx, sym, side, E, A, W):
 
 
 def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100, tol_eigval=1e-12,
-          tol_state=1e-8, refine_iters=0, eps_svd=1e-14, pool=None, factor="eigh", verbose=False, window=None):
+          tol_state=1e-8, refine_iters=0, eps_svd=1e-14, pool=None, factor="eigh", verbose=False, window=None,
+          probe=True):
     """Two-site DMRG sweeps (DmrgSolver::iteration_two, solvers/DmrgSolver.h:1399-1522): per bond
     (l, l+1) the two-site tensor A[l] A[l+1] (contract_AA2) is the start vector of the Lanczos
     ground state of PivotMatrix2(L[l], R[l+2], W[l], W[l+1]); split_AA2 with a truncated SVD
@@ -150,7 +179,15 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     sites > lo+1 right-canonical), the steps of a full sweep in that part of the chain.
     Timers per sweep as in dmrg1; "gauge" holds the two-site contraction ("contract") and
     the SVD ("split"), whose sectors run on the host cores (`pool`, a hostla.SectorPool; one is made if
-    none is given)."""
+    none is given).  `steps` lists every local solve (energy, HxV counts per precision);
+    probe=False makes split-precision solves skip the FP64 probe."""
+    with _probe_setting(probe):
+        return _dmrg2(ctx, model, mps, n_sweeps, Dmax, precision, max_iter, tol_eigval, tol_state, refine_iters,
+                      eps_svd, pool, factor, verbose, window)
+
+
+def _dmrg2(ctx, model, mps, n_sweeps, Dmax, precision, max_iter, tol_eigval, tol_state, refine_iters, eps_svd,
+           pool, factor, verbose, window):
     sym, L, nq = model.sym, model.L, model.sym.nq
     if sym.nonabelian:
         raise ValueError("dmrg2 supports abelian symmetries")
@@ -173,7 +210,7 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     for l in range(L - 1, lo + 1, -1):
         envR[l] = _env(ctx, sym, "R", envR[l + 1], mps.A[l], model.W[l])
     t_init = time.perf_counter() - t0
-    energies, sweep_times, timers, solves, trunc, dims, hxv = [], [], [], [], [], [], 0
+    energies, sweep_times, timers, solves, trunc, dims, hxv, steps = [], [], [], [], [], [], 0, []
     E = None
     clock = time.perf_counter
     for sweep in range(n_sweeps):
@@ -196,6 +233,7 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
                                      tol_state=tol_state, refine_iters=refine_iters)
                 hxv += st["hxv_fp64"] + st["hxv_split"]
                 _count(counts, st)
+                steps.append((sweep, l, E, st["hxv_split"], st["hxv_fp64"]))
                 H.close()
                 t3 = clock()
                 V.data[:] = v
@@ -228,4 +266,4 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     if own_pool:
         pool.close()
     return SweepResult(energies=energies, sweep_times=sweep_times, timers=timers, init_time=t_init, hxv=hxv,
-                       solves=solves, truncation=trunc, max_bond_dim=dims)
+                       solves=solves, truncation=trunc, max_bond_dim=dims, steps=steps)
