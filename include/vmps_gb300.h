@@ -322,6 +322,15 @@ int  vmps_gauge_step(int nq, int move_right, const vmps_blocks* A, double* a, co
                      const vmps_blocks* N, double* n, int threads);
 int  vmps_hostla_load(const char* path);
 int  vmps_two_site_split(const vmps_split_args* args, const vmps_blocks* V, const double* v, vmps_split** out);
+/* The same split with the large sectors on the GPU in FP64: sectors whose Gram
+ * matrix has order >= VMPS_SPLIT_GPU_MIN (environment variable, 512 by default)
+ * form it with cuBLAS dsyrk, take its full eigensystem with cuSOLVER dsyevd and
+ * the non-orthonormal factor with cuBLAS dgemm, on the context's stream and a
+ * host thread of their own, while the host threads factor the smaller sectors
+ * as above.  The truncation rule and the output layout are the host routine's.
+ * Still needs vmps_hostla_load for the small sectors.                          */
+int  vmps_two_site_split_device(vmps_ctx* ctx, const vmps_split_args* args, const vmps_blocks* V, const double* v,
+                                vmps_split** out);
 int  vmps_split_info(const vmps_split* s, int* nmid, double* disc, int64_t* nblocks1, int64_t* size1,
                      int64_t* nblocks2, int64_t* size2);
 int  vmps_split_get(const vmps_split* s, int32_t* qmid, int64_t* dmid,

@@ -125,6 +125,8 @@ _PROTOS = [
     ("vmps_hostla_load", C.c_int, [C.c_char_p]),
     ("vmps_two_site_split", C.c_int, [C.POINTER(vmps_split_args), C.POINTER(vmps_blocks), f64p,
                                       C.POINTER(C.c_void_p)]),
+    ("vmps_two_site_split_device", C.c_int, [C.c_void_p, C.POINTER(vmps_split_args), C.POINTER(vmps_blocks), f64p,
+                                             C.POINTER(C.c_void_p)]),
     ("vmps_split_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), i64p, i64p, i64p, i64p]),
     ("vmps_split_get", C.c_int, [C.c_void_p, i32p, i64p, i32p, i32p, i32p, i64p, i64p, f64p, i32p, i32p, i32p,
                                  i64p, i64p, f64p]),

@@ -76,7 +76,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         for fut in [ex.submit(_run, j) for j in jobs]:
             fut.result()
     tmp = LIB + ".tmp"
-    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-ldl", "-lpthread"])
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcublas", "-lcusolver", "-ldl", "-lpthread"])
     os.replace(tmp, LIB)
     if verbose:
         print("built", LIB)

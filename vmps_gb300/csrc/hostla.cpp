@@ -11,11 +11,18 @@
 // two site tensors are assembled in the block order of a site layout
 // (for s, for qin in sorted order, qout = qin + q(s) if present).
 //
-// GB300's FP64 rate makes these small dense problems (sectors of tens to a few
-// hundred rows) cheaper on the Grace cores than on the GPU.  The LAPACK / BLAS
-// routines are the ILP64 ones of the OpenBLAS that numpy bundles, bound at run
-// time from the path the caller passes; the sectors run on a pool of host
-// threads, largest first, one sector per thread.
+// Small sectors (tens to a few hundred rows) are cheaper on the Grace cores than
+// on the GPU at GB300's FP64 rate: LAPACK / BLAS, the ILP64 routines of the
+// OpenBLAS that numpy bundles (bound at run time from the path the caller
+// passes), one sector per host thread, largest first.  With a device context
+// (vmps_two_site_split_device) the sectors whose Gram matrix has order >=
+// VMPS_SPLIT_GPU_MIN (512 by default) run on the GPU in FP64 instead -- the
+// Gram matrix (cuBLAS dsyrk, DMMA), its eigensystem (cuSOLVER dsyevd) and the
+// non-orthonormal factor (cuBLAS dgemm) -- on a thread of their own while the
+// host threads factor the rest.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
 #include <dlfcn.h>
 
 #include <algorithm>
@@ -39,6 +46,9 @@
 
 namespace vmps {
 void set_last_error_message(const std::string& msg);   // runtime.cpp
+cudaStream_t ctx_stream(vmps_ctx* c);                 // runtime.cpp: the context's compute stream
+int ctx_device(const vmps_ctx* c);
+std::shared_ptr<void>& ctx_la_slot(vmps_ctx* c);      // per-context state of this file
 }
 
 namespace {
@@ -146,9 +156,137 @@ struct Sector {
     std::vector<double> S;        // singular values, descending (min(rows, cols))
     std::vector<double> Q;        // eigenvectors of the Gram matrix, descending (n x n, then n x kept)
     bool full = false;            // Q holds the full eigensystem (small sectors)
+    bool gpu = false;             // factorised on the device
     int64_t kept = 0;
     std::string err;
 };
+
+// ---- device path of the large sectors ------------------------------------------
+// One per context: cuBLAS and cuSOLVER handles on the context's stream and device
+// buffers grown to the largest sector seen.  Used by one thread at a time (the
+// split's device thread).
+struct GpuLa {
+    int device = -1;
+    cudaStream_t st = nullptr;
+    cublasHandle_t blas = nullptr;
+    cusolverDnHandle_t sol = nullptr;
+    double *M = nullptr, *G = nullptr, *W = nullptr, *Q = nullptr, *F = nullptr, *work = nullptr;
+    int* info = nullptr;
+    size_t cM = 0, cG = 0, cW = 0, cQ = 0, cF = 0, cwork = 0;
+    std::mutex mu;
+    ~GpuLa() {
+        for (double* p : {M, G, W, Q, F, work}) if (p) cudaFree(p);
+        if (info) cudaFree(info);
+        if (sol) cusolverDnDestroy(sol);
+        if (blas) cublasDestroy(blas);
+    }
+};
+void cu_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+void blas_check(cublasStatus_t e, const char* what) {
+    if (e != CUBLAS_STATUS_SUCCESS) throw std::runtime_error(std::string(what) + ": cuBLAS status " + std::to_string((int)e));
+}
+void sol_check(cusolverStatus_t e, const char* what) {
+    if (e != CUSOLVER_STATUS_SUCCESS)
+        throw std::runtime_error(std::string(what) + ": cuSOLVER status " + std::to_string((int)e));
+}
+// grow a device buffer to n doubles (contents are not kept)
+void dgrow(double*& p, size_t& cap, size_t n) {
+    if (cap >= n && p) return;
+    if (p) { cudaFree(p); p = nullptr; cap = 0; }
+    cu_check(cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(double)), "cudaMalloc (split)");
+    cap = std::max<size_t>(n, 1);
+}
+
+GpuLa& gpu_la(vmps_ctx* ctx) {
+    std::shared_ptr<void>& slot = vmps::ctx_la_slot(ctx);
+    if (!slot) {
+        auto g = std::make_shared<GpuLa>();
+        g->device = vmps::ctx_device(ctx);
+        g->st = vmps::ctx_stream(ctx);
+        cu_check(cudaSetDevice(g->device), "cudaSetDevice");
+        blas_check(cublasCreate(&g->blas), "cublasCreate");
+        blas_check(cublasSetStream(g->blas, g->st), "cublasSetStream");
+        sol_check(cusolverDnCreate(&g->sol), "cusolverDnCreate");
+        sol_check(cusolverDnSetStream(g->sol, g->st), "cusolverDnSetStream");
+        cu_check(cudaMalloc((void**)&g->info, sizeof(int)), "cudaMalloc (split)");
+        slot = g;
+    }
+    return *static_cast<GpuLa*>(slot.get());
+}
+
+// values pass of a sector on the device: Gram matrix (dsyrk), full eigensystem
+// (dsyevd, ascending), copied back as S (descending square roots) and Q (all
+// eigenvectors, descending)
+void gpu_factor_values(GpuLa& g, Sector& s, bool right) {
+    const int64_t r = s.rows, c = s.cols, n = right ? r : c, k = right ? c : r;
+    s.n = n;
+    dgrow(g.M, g.cM, (size_t)(r * c));
+    dgrow(g.G, g.cG, (size_t)(n * n));
+    dgrow(g.W, g.cW, (size_t)n);
+    cu_check(cudaMemcpyAsync(g.M, s.M.data(), sizeof(double) * (size_t)(r * c), cudaMemcpyHostToDevice, g.st),
+             "upload sector");
+    const double one = 1.0, zero = 0.0;
+    blas_check(cublasDsyrk(g.blas, CUBLAS_FILL_MODE_LOWER, right ? CUBLAS_OP_N : CUBLAS_OP_T, (int)n, (int)k, &one,
+                           g.M, (int)r, &zero, g.G, (int)n),
+               "cublasDsyrk");
+    int lwork = 0;
+    sol_check(cusolverDnDsyevd_bufferSize(g.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, g.G, (int)n,
+                                          g.W, &lwork),
+              "cusolverDnDsyevd_bufferSize");
+    dgrow(g.work, g.cwork, (size_t)lwork);
+    sol_check(cusolverDnDsyevd(g.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)n, g.G, (int)n, g.W,
+                               g.work, lwork, g.info),
+              "cusolverDnDsyevd");
+    std::vector<double> w((size_t)n), Z((size_t)(n * n));
+    int info = 0;
+    cu_check(cudaMemcpyAsync(w.data(), g.W, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, g.st), "download");
+    cu_check(cudaMemcpyAsync(Z.data(), g.G, sizeof(double) * (size_t)(n * n), cudaMemcpyDeviceToHost, g.st),
+             "download");
+    cu_check(cudaMemcpyAsync(&info, g.info, sizeof(int), cudaMemcpyDeviceToHost, g.st), "download");
+    cu_check(cudaStreamSynchronize(g.st), "split stream");
+    if (info != 0) {
+        s.err = "device eigensolver failed (info " + std::to_string(info) + ")";
+        return;
+    }
+    const int64_t m = std::min(r, c);
+    s.S.resize((size_t)m);
+    s.Q.resize((size_t)(n * n));
+    for (int64_t j = 0; j < n; ++j) {
+        const int64_t src = n - 1 - j;
+        std::memcpy(s.Q.data() + (size_t)(j * n), Z.data() + (size_t)(src * n), sizeof(double) * (size_t)n);
+        if (j < m) s.S[(size_t)j] = std::sqrt(std::max(w[(size_t)src], 0.0));
+    }
+    s.full = true;
+    s.gpu = true;
+}
+
+// the non-orthonormal factor of a device sector: scale U_k^T Psi (right, k x c) or
+// scale Psi V_k (left, r x k) by dgemm on the device
+void gpu_factor_product(GpuLa& g, Sector& s, bool right, double scale, std::vector<double>& F) {
+    const int64_t r = s.rows, c = s.cols, n = s.n, k = s.kept;
+    dgrow(g.M, g.cM, (size_t)(r * c));
+    dgrow(g.Q, g.cQ, (size_t)(n * k));
+    const size_t fsz = (size_t)(right ? k * c : r * k);
+    dgrow(g.F, g.cF, fsz);
+    cu_check(cudaMemcpyAsync(g.M, s.M.data(), sizeof(double) * (size_t)(r * c), cudaMemcpyHostToDevice, g.st),
+             "upload sector");
+    cu_check(cudaMemcpyAsync(g.Q, s.Q.data(), sizeof(double) * (size_t)(n * k), cudaMemcpyHostToDevice, g.st),
+             "upload eigenvectors");
+    const double zero = 0.0;
+    if (right)
+        blas_check(cublasDgemm(g.blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)k, (int)c, (int)r, &scale, g.Q, (int)n, g.M,
+                               (int)r, &zero, g.F, (int)k),
+                   "cublasDgemm");
+    else
+        blas_check(cublasDgemm(g.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)r, (int)k, (int)c, &scale, g.M, (int)r, g.Q,
+                               (int)n, &zero, g.F, (int)r),
+                   "cublasDgemm");
+    F.assign(fsz, 0.0);
+    cu_check(cudaMemcpyAsync(F.data(), g.F, sizeof(double) * fsz, cudaMemcpyDeviceToHost, g.st), "download");
+    cu_check(cudaStreamSynchronize(g.st), "split stream");
+}
 
 // Gram matrix of a sector (move right: M M^T, rows x rows; else M^T M), lower triangle
 void gram(Sector& s, bool right, std::vector<double>& G) {
@@ -324,7 +462,17 @@ QN qadd(const QN& a, const int32_t* b, int nq, int sign) {
     return r;
 }
 
-void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd, vmps_split_s& out) {
+// order of the Gram matrices that go to the device (VMPS_SPLIT_GPU_MIN overrides)
+int64_t split_gpu_min() {
+    const char* v = std::getenv("VMPS_SPLIT_GPU_MIN");
+    if (!v || !*v) return 512;
+    const long long x = std::atoll(v);
+    if (x < 1) throw std::invalid_argument("VMPS_SPLIT_GPU_MIN must be a positive integer");
+    return (int64_t)x;
+}
+
+// gpu: device state of a context, or null (host only)
+void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd, vmps_split_s& out, GpuLa* gpu) {
     const int nq = a->nq;
     out.nq = nq;
     const bool right = a->move_right != 0;
@@ -413,7 +561,41 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
         work_flops += 10.0 * n * n * n;
     }
     const int threads = work_flops < kParallelMinFlops ? 1 : a->threads;
-    parallel_for(work.size(), threads, [&](size_t i) { factor_values(*work[i], right); });
+    // the large sectors (Gram order >= the device threshold) on the device thread,
+    // the others on the host threads meanwhile
+    std::vector<Sector*> gwork, hwork;
+    const int64_t gmin = gpu ? split_gpu_min() : 0;
+    for (Sector* s : work) ((gpu && (right ? s->rows : s->cols) >= gmin) ? gwork : hwork).push_back(s);
+    auto on_device = [&](const std::vector<Sector*>& list, auto fn) {
+        if (list.empty()) return std::thread();
+        return std::thread([&, fn]() {
+            std::lock_guard<std::mutex> lock(gpu->mu);
+            try {
+                cu_check(cudaSetDevice(gpu->device), "cudaSetDevice");
+            } catch (const std::exception& e) {
+                for (Sector* s : list) s->err = e.what();
+                return;
+            }
+            for (Sector* s : list) {
+                try {
+                    fn(*s);
+                } catch (const std::exception& e) {
+                    s->err = e.what();
+                    return;
+                }
+            }
+        });
+    };
+    {
+        std::thread gt = on_device(gwork, [&](Sector& s) { gpu_factor_values(*gpu, s, right); });
+        try {
+            parallel_for(hwork.size(), threads, [&](size_t i) { factor_values(*hwork[i], right); });
+        } catch (...) {
+            if (gt.joinable()) gt.join();
+            throw;
+        }
+        if (gt.joinable()) gt.join();
+    }
     for (Sector* s : order)
         if (!s->err.empty()) throw std::runtime_error(s->err);
     // global truncation: the Dmax largest values above eps_svd * max; ties at the
@@ -474,8 +656,19 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
         return ks[x]->n * ks[x]->n * ks[x]->kept > ks[y]->n * ks[y]->n * ks[y]->kept;
     });
     std::vector<std::vector<double>> Fk(ks.size());
-    parallel_for(ks.size(), threads, [&](size_t t) {
-        const size_t i = vorder[t];
+    std::vector<size_t> gvec, hvec;
+    for (size_t t = 0; t < vorder.size(); ++t) (ks[vorder[t]]->gpu ? gvec : hvec).push_back(vorder[t]);
+    std::vector<Sector*> gks;
+    for (size_t i : gvec) gks.push_back(ks[i]);
+    std::unordered_map<const Sector*, size_t> kpos;
+    for (size_t i = 0; i < ks.size(); ++i) kpos[ks[i]] = i;
+    std::thread gt = on_device(gks, [&](Sector& s) {
+        s.Q.resize((size_t)(s.n * s.kept));   // the leading kept eigenvectors (descending)
+        gpu_factor_product(*gpu, s, right, scale, Fk[kpos[&s]]);
+    });
+    try {
+    parallel_for(hvec.size(), threads, [&](size_t t) {
+        const size_t i = hvec[t];
         Sector& s = *ks[i];
         factor_vectors(s, right);
         if (!s.err.empty()) return;
@@ -489,6 +682,11 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
             L.gemm("N", "N", &r, &k, &c, &scale, s.M.data(), &r, s.Q.data(), &n, &zero, Fk[i].data(), &r, 1, 1);
         }
     });
+    } catch (...) {
+        if (gt.joinable()) gt.join();
+        throw;
+    }
+    if (gt.joinable()) gt.join();
     for (Sector* s : ks)
         if (!s->err.empty()) throw std::runtime_error(s->err);
     // output sizes first (one allocation per table)
@@ -738,8 +936,9 @@ extern "C" int vmps_hostla_load(const char* path) {
     return VMPS_OK;
 }
 
-extern "C" int vmps_two_site_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vdata,
-                                   vmps_split** out) {
+namespace {
+int split_entry(vmps_ctx* ctx, const vmps_split_args* a, const vmps_blocks* V, const double* Vdata,
+                vmps_split** out) {
     if (!a || !V || !out || (V->nblocks > 0 && !Vdata)) return set_err(VMPS_E_ARG, "bad argument");
     if (a->nq < 1 || a->nq > 4 || a->n1 < 1 || a->n3 < 1 || a->n13 < 1 || !a->pair1 || !a->pair3 ||
         !a->qloc1 || !a->qloc3 || a->nin < 0 || a->nout < 0 || a->dmax < 0 ||
@@ -755,8 +954,13 @@ extern "C" int vmps_two_site_split(const vmps_split_args* a, const vmps_blocks* 
             return set_err(VMPS_E_ARG, "combined index outside the local bases");
     if (!g_lapack.ok()) return set_err(VMPS_E_ARG, "host LAPACK not bound (vmps_hostla_load)");
     try {
+        GpuLa* g = nullptr;
+        if (ctx) {
+            if (vmps::ctx_device(ctx) < 0) return set_err(VMPS_E_ARG, "device split needs a device context");
+            g = &gpu_la(ctx);
+        }
         std::unique_ptr<vmps_split_s> s(new vmps_split_s());
-        run_split(a, V, Vdata, *s);
+        run_split(a, V, Vdata, *s, g);
         *out = s.release();
     } catch (const std::bad_alloc& e) {
         return set_err(VMPS_E_NOMEM, e.what());
@@ -764,6 +968,18 @@ extern "C" int vmps_two_site_split(const vmps_split_args* a, const vmps_blocks* 
         return set_err(VMPS_E_ARG, e.what());
     }
     return VMPS_OK;
+}
+}  // namespace
+
+extern "C" int vmps_two_site_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vdata,
+                                   vmps_split** out) {
+    return split_entry(nullptr, a, V, Vdata, out);
+}
+
+extern "C" int vmps_two_site_split_device(vmps_ctx* ctx, const vmps_split_args* a, const vmps_blocks* V,
+                                          const double* Vdata, vmps_split** out) {
+    if (!ctx) return set_err(VMPS_E_ARG, "null context");
+    return split_entry(ctx, a, V, Vdata, out);
 }
 
 extern "C" int vmps_split_info(const vmps_split* s, int* nmid, double* disc, int64_t* nblocks1, int64_t* size1,

@@ -135,6 +135,7 @@ struct vmps_ctx_s {
     bool pageable_access = false;   // the device reads pageable host memory in place
     int num_sms = 152;              // CTAs of the persistent tcgen05 engine (host-only: GB300's count)
     long long wait_budget = 0;      // main-loop wait budget of the tcgen05 engine in cycles (0: ~2 s)
+    std::shared_ptr<void> la;       // device state of the two-site split (hostla.cpp)
 };
 
 // read and clear the device error word (after the stream has been synchronised)
@@ -148,6 +149,12 @@ static void check_device_error(vmps_ctx* c) {
         throw WaitTimeout("a bounded device wait in the tcgen05 engine ran out (error word " + std::to_string(h) + ")");
     }
 }
+
+namespace vmps {
+cudaStream_t ctx_stream(vmps_ctx* c) { return c->stream; }
+int ctx_device(const vmps_ctx* c) { return c->device; }
+std::shared_ptr<void>& ctx_la_slot(vmps_ctx* c) { return c->la; }
+}  // namespace vmps
 
 // device copy of one phase's work lists
 struct DevPhase {
@@ -1009,6 +1016,7 @@ int vmps_ctx_destroy(vmps_ctx* ctx) {
     if (!ctx) return VMPS_OK;
     if (ctx->device < 0) { delete ctx; return VMPS_OK; }
     cudaStreamSynchronize(ctx->stream);
+    ctx->la.reset();   // library handles bound to the stream go first
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
     cudaEventDestroy(ctx->ev2);

@@ -165,7 +165,7 @@ def _env(ctx, sym, side, E, A, W):
 
 def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100, tol_eigval=1e-12,
           tol_state=1e-8, refine_iters=0, eps_svd=1e-14, pool=None, factor="eigh", verbose=False, window=None,
-          probe=True):
+          probe=True, split_device=True):
     """Two-site DMRG sweeps (DmrgSolver::iteration_two, solvers/DmrgSolver.h:1399-1522): per bond
     (l, l+1) the two-site tensor A[l] A[l+1] (contract_AA2) is the start vector of the Lanczos
     ground state of PivotMatrix2(L[l], R[l+2], W[l], W[l+1]); split_AA2 with a truncated SVD
@@ -179,15 +179,17 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     sites > lo+1 right-canonical), the steps of a full sweep in that part of the chain.
     Timers per sweep as in dmrg1; "gauge" holds the two-site contraction ("contract") and
     the SVD ("split"), whose sectors run on the host cores (`pool`, a hostla.SectorPool; one is made if
-    none is given).  `steps` lists every local solve (energy, HxV counts per precision);
-    probe=False makes split-precision solves skip the FP64 probe."""
+    none is given); with split_device (default) the sectors whose Gram matrix has order
+    >= 512 run on the GPU in FP64 (vmps_two_site_split_device).  `steps` lists every
+    local solve (energy, HxV counts per precision); probe=False makes split-precision
+    solves skip the FP64 probe."""
     with _probe_setting(probe):
         return _dmrg2(ctx, model, mps, n_sweeps, Dmax, precision, max_iter, tol_eigval, tol_state, refine_iters,
-                      eps_svd, pool, factor, verbose, window)
+                      eps_svd, pool, factor, verbose, window, split_device)
 
 
 def _dmrg2(ctx, model, mps, n_sweeps, Dmax, precision, max_iter, tol_eigval, tol_state, refine_iters, eps_svd,
-           pool, factor, verbose, window):
+           pool, factor, verbose, window, split_device):
     sym, L, nq = model.sym, model.L, model.sym.nq
     if sym.nonabelian:
         raise ValueError("dmrg2 supports abelian symmetries")
@@ -238,7 +240,8 @@ def _dmrg2(ctx, model, mps, n_sweeps, Dmax, precision, max_iter, tol_eigval, tol
                 t3 = clock()
                 V.data[:] = v
                 A1, A2, disc, dmid = split_two_site(V, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
-                                                    eps_svd=eps_svd, pool=pool, factor=factor)
+                                                    eps_svd=eps_svd, pool=pool, factor=factor,
+                                                    ctx=ctx if split_device else None)
                 mps.A[l], mps.A[l + 1] = A1, A2
                 mps.dims[l + 1] = dmid
                 disc_max = max(disc_max, disc)

@@ -427,10 +427,12 @@ def _sector_factor(M, move):
     return np.sqrt(np.maximum(w[order], 0.0)), Q[:, order]
 
 
-def _split_native(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move, eps_svd, threads):
-    """split_two_site through the native host routine (vmps_two_site_split): the
-    same sectors, Gram-matrix eigensystems (LAPACK dsyevd), truncation and block
-    order, without per-block Python work; the sectors run on `threads` threads."""
+def _split_native(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move, eps_svd, threads, ctx=None):
+    """split_two_site through the native routine (vmps_two_site_split): the same
+    sectors, Gram-matrix eigensystems (LAPACK dsyevd), truncation and block order,
+    without per-block Python work; the sectors run on `threads` threads.  With a
+    device context `ctx` the large sectors run on the GPU in FP64
+    (vmps_two_site_split_device)."""
     import ctypes as C
     from . import _native as N
     n13 = int(comb["n"])
@@ -459,7 +461,10 @@ def _split_native(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move, eps_svd, t
     vb = V.c_struct()
     h = C.c_void_p()
     lib = N.lib()
-    N.check(lib.vmps_two_site_split(C.byref(a), C.byref(vb), V.data_ptr(), C.byref(h)))
+    if ctx is not None and getattr(ctx, "device", -1) >= 0:
+        N.check(lib.vmps_two_site_split_device(ctx._h, C.byref(a), C.byref(vb), V.data_ptr(), C.byref(h)))
+    else:
+        N.check(lib.vmps_two_site_split(C.byref(a), C.byref(vb), V.data_ptr(), C.byref(h)))
     try:
         nmid, disc = C.c_int(), C.c_double()
         nb1, sz1, nb2, sz2 = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
@@ -491,7 +496,7 @@ def _split_native(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move, eps_svd, t
 
 
 def split_two_site(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move="right", eps_svd=1e-14, pool=None,
-                   factor="eigh", native=True):
+                   factor="eigh", native=True, ctx=None):
     """Truncated SVD of a two-site tensor back into two site tensors (abelian QNs):
     split_AA2 with Biped::truncateSVD (tensors/DmrgContractions.h:2461-2631,
     tensors/Biped.h:744-932).  For every middle QN qmid the matrix
@@ -505,12 +510,13 @@ def split_two_site(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move="right", e
     "eigh" (Gram matrix, default) or "svd".  Either way the orthonormal factor's
     columns are the singular vectors for the sweep direction.  native=True (with
     "eigh") runs the whole split in the native library (vmps_two_site_split) on
-    the pool's thread count when numpy's LAPACK can be bound to it."""
+    the pool's thread count when numpy's LAPACK can be bound to it; with a device
+    context `ctx` its large sectors run on the GPU in FP64."""
     if native and factor == "eigh":
         from .hostla import native_lapack
         if native_lapack():
             return _split_native(V, comb, qloc12, qloc34, din, dout, nq, Dmax, move, eps_svd,
-                                 pool.threads if pool is not None else 1)
+                                 pool.threads if pool is not None else 1, ctx=ctx)
     # each two-site block (s13, qin, qout) is one (s1, s3) pair (abelian): scatter the
     # blocks into their middle-QN sector matrices in one pass over the blocks
     pair_of = {}
