@@ -199,7 +199,33 @@ int vmps_pivot_stats(const vmps_pivot* p, int precision, vmps_plan_stats* out);
 /* number of doubles of a PivotVector in the compact layout of V */
 int vmps_pivot_dim(const vmps_pivot* p, int64_t* out);
 
-/* HxV with host buffers in the compact layout of V: Vout = H * Vin.
+/* Autotuner of the split-precision grouped GEMM (the reference picks a product
+ * order per chain, DmrgExternal.h:141-215; here the tile shape of the whole
+ * grouped launch is chosen).  Candidates: tile N caps of 256 or 128 columns for
+ * each of the two phases and a split-K of 1, 2 or 4 for the second phase (more
+ * than 1 only when that phase has fewer tiles than twice the SM count; the parts
+ * are summed in a fixed order, so results stay deterministic).  Each candidate is
+ * timed on this pivot (`trials` HxVs, CUDA events) and the fastest kept, ties to
+ * the default (256, 256, 1).  The choice is cached for the process under the
+ * pivot's sector-layout key (the histogram of its chains' block sizes); a pivot
+ * whose key is cached takes the cached choice without timing, and with the
+ * environment variable VMPS_AUTOTUNE=1 every new layout is tuned (3 trials) when
+ * its first split plan is built.  The FP64 plan is not affected.               */
+typedef struct {
+    int32_t ncap1, ncap2, splitk;  /* the chosen tiling                               */
+    int32_t candidates;            /* plans timed (0 when the choice came from the cache) */
+    int32_t from_cache;
+    int32_t reserved;
+    double  ms_default, ms_best;   /* ms per HxV of the default and the chosen plan    */
+    uint64_t layout_key;
+} vmps_tune_info;
+int vmps_pivot_autotune(vmps_pivot* p, int trials, vmps_tune_info* out);
+int vmps_tune_cache_clear(void);
+/* Set the split-precision tiling of a pivot directly (N caps multiples of 32 up to
+ * 256, split-K 1..8), bypassing the tuner; the plan is rebuilt on next use.    */
+int vmps_pivot_set_tiling(vmps_pivot* p, int ncap1, int ncap2, int splitk);
+
+/* HxV with host buffers in the compact layout of V: Vout = H * Vin./* HxV with host buffers in the compact layout of V: Vout = H * Vin.
  * Host->device copy, the product and the device->host copy all happen here.
  * Replaces HxV(PivotMatrixN, Vin, Vout), pivot/DmrgPivotMatrix1.h:124-129.  */
 int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int precision);

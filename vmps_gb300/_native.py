@@ -76,6 +76,15 @@ class vmps_cheb_stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class vmps_tune_info(C.Structure):
+    _fields_ = [("ncap1", C.c_int32), ("ncap2", C.c_int32), ("splitk", C.c_int32), ("candidates", C.c_int32),
+                ("from_cache", C.c_int32), ("reserved", C.c_int32), ("ms_default", C.c_double),
+                ("ms_best", C.c_double), ("layout_key", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class vmps_split_args(C.Structure):
     _fields_ = [("nq", C.c_int32), ("n1", C.c_int32), ("n3", C.c_int32), ("n13", C.c_int32),
                 ("qloc1", i32p), ("qloc3", i32p), ("pair1", i32p), ("pair3", i32p),
@@ -111,6 +120,9 @@ _PROTOS = [
                                            C.POINTER(C.POINTER(vmps_mpo_site)), C.POINTER(C.POINTER(vmps_mpo_site)),
                                            C.POINTER(vmps_blocks), C.POINTER(C.c_void_p)]),
     ("vmps_pivot_set_penalty", C.c_int, [C.c_void_p, C.c_int, f64p, C.c_double]),
+    ("vmps_pivot_autotune", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_tune_info)]),
+    ("vmps_tune_cache_clear", C.c_int, []),
+    ("vmps_pivot_set_tiling", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     ("vmps_pivot_destroy", C.c_int, [C.c_void_p]),
     ("vmps_pivot_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),
     ("vmps_pivot_dim", C.c_int, [C.c_void_p, i64p]),

@@ -229,6 +229,17 @@ struct Plan {
     int nrhs = 1;
     int64_t vstride = 0;
     std::vector<int32_t> ycolsP;
+    // split-K of phase 2 (single right-hand side): part j of every output block's
+    // K concatenation writes the whole block at element offset j * vstride of a
+    // partial buffer; a reduction sums the parts in order into the output
+    int splitk = 1;
+};
+// Tile options of a split-precision plan (chosen by the autotuner): the N caps of
+// the phase-1 and phase-2 tiles (multiples of 32, at most kUmmaTileN) and the
+// split-K factor of phase 2.
+struct SplitTiling {
+    int ncap1 = 256, ncap2 = 256, splitk = 1;
+    bool operator==(const SplitTiling& o) const { return ncap1 == o.ncap1 && ncap2 == o.ncap2 && splitk == o.splitk; }
 };
 // FP64 plan: two phases, the second sums first-stage products on the fly
 Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
@@ -240,7 +251,8 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // GEMM per V block with the right-hand sides side by side in N; phase 2 the
 // single-vector segments once per right-hand side, reading its K range of T).
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ, int nrhs = 1);
+                     const DevLayout& O, bool transX, bool transZ, int nrhs = 1,
+                     const SplitTiling& tiling = SplitTiling());
 // One FP64 grouped-GEMM phase of plain block products C[k] = sum A[i] * B[j] over
 // the (k, i, j) triples (contract_AA2's two-site tensor): one tile range per
 // output block, one segment per product; output blocks without a product are

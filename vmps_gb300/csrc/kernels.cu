@@ -411,6 +411,16 @@ __global__ void finite_kernel(const double* __restrict__ x, int64_t n, int* __re
         if (!isfinite(x[i])) { atomicOr(bad, 1); return; }
 }
 
+// split-K of the grouped GEMM: out[e] = sum_j part[j * n + e], parts in order
+template <typename T>
+__global__ void splitk_reduce_kernel(const T* __restrict__ part, int nparts, int64_t n, T* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double s = (double)part[i];
+        for (int j = 1; j < nparts; ++j) s += (double)part[(int64_t)j * n + i];
+        out[i] = (T)s;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Excited-state projector of an HxV (pivot/DmrgPivotMatrix1.h:304-331):
 // out_r += sum_p E <d_p, y_r> a_p for right-hand sides r < nrhs (stride n) and
@@ -605,6 +615,13 @@ cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t st) {
 }
 cudaError_t launch_combine(const double* V, int nv, int64_t n, const double* c, double* y, cudaStream_t st) {
     combine_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>(V, nv, n, c, y);
+    return cudaGetLastError();
+}
+cudaError_t launch_splitk_reduce(const void* part, int nparts, int64_t n, void* out, int f32, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (!part || !out || nparts < 1) return cudaErrorInvalidValue;
+    if (f32) splitk_reduce_kernel<float><<<grid_for(n, 256, 152 * 8), 256, 0, st>>>((const float*)part, nparts, n, (float*)out);
+    else splitk_reduce_kernel<double><<<grid_for(n, 256, 152 * 8), 256, 0, st>>>((const double*)part, nparts, n, (double*)out);
     return cudaGetLastError();
 }
 cudaError_t launch_penalty(const PenaltyArgs& a, const double* y, const float* yf, double* o, float* of,

@@ -64,6 +64,8 @@ cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStr
 cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t st);
 cudaError_t launch_combine(const double* V, int nv, int64_t n, const double* c, double* y, cudaStream_t st);
 cudaError_t launch_finite(const double* x, int64_t n, int* bad, cudaStream_t st);
+// split-K partials of a grouped GEMM summed in order: out[e] = sum_j part[j * n + e] (double or float)
+cudaError_t launch_splitk_reduce(const void* part, int nparts, int64_t n, void* out, int f32, cudaStream_t st);
 // excited-state projector after an HxV: out_r += sum_p E <dvec_p, y_r> avec_p (r < nrhs, vectors
 // at stride n; y and out double or float, the other pointer null); deterministic
 struct PenaltyArgs {

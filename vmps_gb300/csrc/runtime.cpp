@@ -76,6 +76,15 @@ struct DBuf {
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) {
+            if (p) cudaFree(p);
+            p = o.p; bytes = o.bytes;
+            o.p = nullptr; o.bytes = 0;
+        }
+        return *this;
+    }
     ~DBuf() { if (p) cudaFree(p); }
     void alloc(size_t b, cudaStream_t st = 0, bool zero = true) {
         if (p && bytes >= b) { if (zero) CK(cudaMemsetAsync(p, 0, b, st)); return; }
@@ -220,6 +229,9 @@ struct DevPlan {
     DBuf ypieces;                  // PanelPiece list: the FP64 Y arena -> Y2
     int nprepX = 0, nprepZ = 0, nypieces = 0;
     std::unique_ptr<DevChunked> chunks;   // host-buffer pipeline (split plans of pivots)
+    // split-K partial outputs (plan.splitk parts of vstride elements), one buffer per
+    // output type so that the zero padding of each stays zero
+    DBuf part_d, part_f;
     bool ready = false;
 };
 
@@ -519,6 +531,11 @@ static void plan_to_device(DevPlan& dp, const DevLayout& Y, cudaStream_t st) {
     dp.nypieces = (int)yp.size();
     dp.p1.maps = build_phase_maps(dp.plan.p1, dp.plan.ax, dp.X2, dp.plan.ay, dp.Y2);
     dp.p2.maps = build_phase_maps(dp.plan.p2, dp.plan.at, dp.T, dp.plan.az, dp.Z2);
+    if (dp.plan.splitk > 1) {
+        const size_t n = (size_t)dp.plan.splitk * (size_t)dp.plan.vstride;
+        dp.part_d.alloc(n * 8, st, true);
+        dp.part_f.alloc(n * 4, st, true);
+    }
 }
 
 // split plans: the bf16 panels of the X and scaled Z operands
@@ -561,6 +578,13 @@ static void run_phase_on(const DevPlan& dp, int ph, const DevPhase& d, const Pha
     a.A = ph == 1 ? dp.X2.p : dp.T.p;
     a.B = ph == 1 ? dp.Y2.p : dp.Z2.p;
     a.C = ph == 1 ? dp.T.p : (ops.Of ? (void*)ops.Of : (void*)ops.O);
+    if (ph == 2 && dp.plan.splitk > 1) {
+        // split-K: the parts go to a partial buffer (zeroed once: padding stays zero)
+        const DBuf& pb = ops.Of ? dp.part_f : dp.part_d;
+        const size_t bytes = (size_t)dp.plan.splitk * (size_t)dp.plan.vstride * (ops.Of ? 4 : 8);
+        if (!pb.p || pb.bytes < bytes) throw std::invalid_argument("split-K plan without its partial buffer");
+        a.C = pb.p;
+    }
     a.steps = d.steps.as<TStep>();
     a.cta_tiles = d.cta_tiles.as<int32_t>();
     a.ncta = d.ncta;
@@ -584,6 +608,9 @@ static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
     }
     run_phase(dp, 1, ops, st);
     run_phase(dp, 2, ops, st);
+    if (dp.plan.split && dp.plan.splitk > 1)
+        CK(launch_splitk_reduce(ops.Of ? dp.part_f.p : dp.part_d.p, dp.plan.splitk, dp.plan.vstride,
+                                ops.Of ? (void*)ops.Of : (void*)ops.O, ops.Of ? 1 : 0, st));
     if (ops.pen && ops.pen->npen > 0) {
         PenaltyArgs a = *ops.pen;
         a.nrhs = dp.plan.nrhs;
@@ -660,6 +687,11 @@ struct vmps_pivot_s {
     // with the SU(2) dot weights folded in, chunk partials and coefficients
     DBuf pen_d, pen_a, pen_part, pen_coef;
     PenaltyArgs pen{};
+    // tiling of the split-precision plan (autotuner or its cache), and the key of
+    // the pivot's block-size histogram in that cache (0 = not computed yet)
+    SplitTiling tiling;
+    bool tiling_set = false;
+    uint64_t layout_key = 0;
     ~vmps_pivot_s() {
         for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
     }
@@ -685,6 +717,7 @@ static void ensure_io(vmps_pivot* p) {
 }
 
 static void make_chunks(vmps_pivot* p, DevPlan& dp);
+static SplitTiling pivot_tiling(vmps_pivot* p);
 
 static DevPlan& get_plan(vmps_pivot* p, int prec) {
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
@@ -692,13 +725,13 @@ static DevPlan& get_plan(vmps_pivot* p, int prec) {
     if (dp.ready) return dp;
     if (prec == VMPS_PREC_FP64) dp.plan = make_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 64, 64);
     else {
-        dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false);
+        dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 1, pivot_tiling(p));
         schedule_and_validate(dp.plan, p->ctx->num_sms);
     }
     if (p->ctx->device < 0) { dp.ready = true; return dp; }   // host-only: plan without device copies
     plan_to_device(dp, p->Vd, p->st());
     split_prepare(dp, p->dL.as<double>(), p->dR.as<double>(), p->st());
-    if (prec == VMPS_PREC_BF16X3) make_chunks(p, dp);
+    if (prec == VMPS_PREC_BF16X3 && dp.plan.splitk == 1) make_chunks(p, dp);
     CK(cudaStreamSynchronize(p->st()));
     dp.ready = true;
     return dp;
@@ -903,6 +936,129 @@ static void pivot_hxv_dev(vmps_pivot* p, int prec, const double* vin, double* vo
     ops.O = vout;
     ops.err = p->ctx->err;
     run_plan(dp, ops, p->st());
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner of the split-precision tiling.  The candidates are the phase-1 and
+// phase-2 tile N caps (256 or 128 columns) and the split-K factor of phase 2
+// (1, 2, 4; more than 1 only while phase 2 has fewer tiles than twice the SM
+// count, where it is the only source of parallelism).  Each candidate plan is
+// built and timed on the pivot itself (CUDA events, `trials` HxVs after one
+// warm-up); the fastest wins, ties to the default.  The choice is cached per
+// sector layout: the key is the block-size histogram of the pivot's chains
+// ((m, k, n, p) of op(X) m x k, Y k x n, Z n x p, with counts), so the pivots of
+// later sweeps over the same bond bases reuse it without timing.
+// ---------------------------------------------------------------------------
+static std::mutex g_tune_mu;
+static std::unordered_map<uint64_t, SplitTiling> g_tune_cache;
+
+static uint64_t pivot_layout_key(vmps_pivot* p) {
+    if (p->layout_key) return p->layout_key;
+    std::map<std::array<int64_t, 4>, int64_t> hist;
+    for (const Chain& c : p->cs.chains)
+        ++hist[{p->Lt.rows[c.x], p->Lt.cols[c.x], p->Vt.cols[c.y], p->Rt.cols[c.z]}];
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) {
+        for (int i = 0; i < 8; ++i) { h ^= (v >> (8 * i)) & 0xffu; h *= 1099511628211ull; }
+    };
+    mix((uint64_t)p->Vt.n);
+    mix((uint64_t)p->Vt.total);
+    for (const auto& kv : hist) {
+        for (int64_t v : kv.first) mix((uint64_t)v);
+        mix((uint64_t)kv.second);
+    }
+    p->layout_key = h ? h : 1;
+    return p->layout_key;
+}
+
+// VMPS_AUTOTUNE = 1: the first split plan of a pivot whose layout is not in the
+// cache is tuned (3 timed HxVs per candidate)
+static bool autotune_on_first_plan() {
+    const char* v = std::getenv("VMPS_AUTOTUNE");
+    return v && !std::strcmp(v, "1");
+}
+
+static SplitTiling tune_pivot(vmps_pivot* p, int trials, double* ms_default, double* ms_best, int* ncand);
+
+static SplitTiling pivot_tiling(vmps_pivot* p) {
+    if (p->tiling_set) return p->tiling;
+    const uint64_t key = pivot_layout_key(p);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            p->tiling = it->second;
+            p->tiling_set = true;
+            return p->tiling;
+        }
+    }
+    if (p->ctx->device >= 0 && autotune_on_first_plan()) {
+        double a = 0, b = 0;
+        int n = 0;
+        p->tiling = tune_pivot(p, 3, &a, &b, &n);
+        p->tiling_set = true;
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = p->tiling;
+        return p->tiling;
+    }
+    return SplitTiling();
+}
+
+static double time_split_plan(vmps_pivot* p, const SplitTiling& tl, int trials, int64_t* tiles2) {
+    cudaStream_t st = p->st();
+    DevPlan dp;
+    dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 1, tl);
+    schedule_and_validate(dp.plan, p->ctx->num_sms);
+    if (tiles2) *tiles2 = (int64_t)dp.plan.p2.tiles.size();
+    plan_to_device(dp, p->Vd, st);
+    split_prepare(dp, p->dL.as<double>(), p->dR.as<double>(), st);
+    Operands ops = pivot_ops(p);
+    ops.Y = p->vin.as<double>();
+    ops.O = p->vout.as<double>();
+    run_plan(dp, ops, st);   // warm-up
+    CK(cudaStreamSynchronize(st));
+    CK(cudaEventRecord(p->ctx->ev0, st));
+    for (int i = 0; i < trials; ++i) run_plan(dp, ops, st);
+    CK(cudaEventRecord(p->ctx->ev1, st));
+    CK(cudaEventSynchronize(p->ctx->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, p->ctx->ev0, p->ctx->ev1));
+    check_device_error(p->ctx);
+    return (double)ms / trials;
+}
+
+static SplitTiling tune_pivot(vmps_pivot* p, int trials, double* ms_default, double* ms_best, int* ncand) {
+    require_device(p->ctx);
+    ensure_staging(p);
+    ensure_io(p);
+    // a nonzero input (the timing does not depend on the values)
+    std::vector<double> ones((size_t)std::max<int64_t>(p->Vt.total, 1), 1.0);
+    pack_in(p->ctx, p->dPack, p->npack, ones.data(), p->Vt.total, p->stage_in, p->vin.as<double>(), p->st());
+    CK(cudaStreamSynchronize(p->st()));
+    const SplitTiling def;
+    int64_t tiles2 = 0;
+    double best = time_split_plan(p, def, trials, &tiles2);
+    *ms_default = best;
+    SplitTiling pick = def;
+    int n = 1;
+    std::vector<SplitTiling> cand;
+    for (int c1 : {256, 128})
+        for (int c2 : {256, 128})
+            for (int sk : {1, 2, 4}) {
+                SplitTiling t;
+                t.ncap1 = c1; t.ncap2 = c2; t.splitk = sk;
+                if (t == def) continue;
+                if (sk > 1 && tiles2 >= 2LL * p->ctx->num_sms) continue;
+                cand.push_back(t);
+            }
+    for (const SplitTiling& t : cand) {
+        const double ms = time_split_plan(p, t, trials, nullptr);
+        ++n;
+        if (ms < best) { best = ms; pick = t; }
+    }
+    *ms_best = best;
+    *ncand = n;
+    return pick;
 }
 
 static void upload_blocks_padded(const vmps_ctx* c, const BlockTable& t, const DevLayout& d, const double* host, DBuf& dst,
@@ -1151,6 +1307,80 @@ int vmps_pivot2_create_terms(vmps_ctx* ctx, const vmps_symmetry* sym, int nterms
     API_BEGIN
     return pivot_create_terms(ctx, sym, 2, nterms, L, Ldata, R, Rdata, W12, W34, V, out);
     API_END
+}
+
+// ---- autotuner entry points -------------------------------------------------------
+int vmps_pivot_autotune(vmps_pivot* p, int trials, vmps_tune_info* out) {
+    API_BEGIN
+    if (!p || trials < 1 || trials > 1000) return set_err(VMPS_E_ARG, "bad argument");
+    require_device(p->ctx);
+    vmps_tune_info info{};
+    const uint64_t key = pivot_layout_key(p);
+    bool cached = false;
+    SplitTiling t;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) { t = it->second; cached = true; }
+    }
+    if (!cached) {
+        double a = 0, b = 0;
+        int n = 0;
+        t = tune_pivot(p, trials, &a, &b, &n);
+        info.ms_default = a;
+        info.ms_best = b;
+        info.candidates = n;
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = t;
+    }
+    if (!p->tiling_set || !(p->tiling == t)) {
+        // the split plan is rebuilt with the chosen tiling on next use
+        p->tiling = t;
+        p->tiling_set = true;
+        DevPlan& dp = p->plans[VMPS_PREC_BF16X3];
+        dp.~DevPlan();
+        new (&dp) DevPlan();
+        if (p->graph[VMPS_PREC_BF16X3]) {
+            cudaGraphExecDestroy(p->graph[VMPS_PREC_BF16X3]);
+            p->graph[VMPS_PREC_BF16X3] = nullptr;
+        }
+        p->graph_in[VMPS_PREC_BF16X3] = p->graph_out[VMPS_PREC_BF16X3] = nullptr;
+    }
+    info.ncap1 = t.ncap1;
+    info.ncap2 = t.ncap2;
+    info.splitk = t.splitk;
+    info.from_cache = cached ? 1 : 0;
+    info.layout_key = key;
+    if (out) *out = info;
+    API_END
+}
+
+int vmps_pivot_set_tiling(vmps_pivot* p, int ncap1, int ncap2, int splitk) {
+    API_BEGIN
+    if (!p) return set_err(VMPS_E_ARG, "null pivot");
+    for (int cap : {ncap1, ncap2})
+        if (cap < 32 || cap > kUmmaTileN || cap % 32 != 0)
+            return set_err(VMPS_E_ARG, "tile N caps must be multiples of 32 up to 256");
+    if (splitk < 1 || splitk > 8) return set_err(VMPS_E_ARG, "split-K must be 1..8");
+    SplitTiling t;
+    t.ncap1 = ncap1; t.ncap2 = ncap2; t.splitk = splitk;
+    p->tiling = t;
+    p->tiling_set = true;
+    DevPlan& dp = p->plans[VMPS_PREC_BF16X3];
+    dp.~DevPlan();
+    new (&dp) DevPlan();
+    if (p->graph[VMPS_PREC_BF16X3]) {
+        cudaGraphExecDestroy(p->graph[VMPS_PREC_BF16X3]);
+        p->graph[VMPS_PREC_BF16X3] = nullptr;
+    }
+    p->graph_in[VMPS_PREC_BF16X3] = p->graph_out[VMPS_PREC_BF16X3] = nullptr;
+    API_END
+}
+
+int vmps_tune_cache_clear(void) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache.clear();
+    return VMPS_OK;
 }
 
 // ---- excited-state projector (A0proj, Epenalty) ---------------------------------

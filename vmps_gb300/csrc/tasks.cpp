@@ -1148,9 +1148,15 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // split-precision planner
 // ===========================================================================
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ, int nrhs) {
+                     const DevLayout& O, bool transX, bool transZ, int nrhs, const SplitTiling& tiling) {
     if (nrhs < 1) throw std::invalid_argument("nrhs must be at least 1");
+    for (int cap : {tiling.ncap1, tiling.ncap2})
+        if (cap < 32 || cap > kUmmaTileN || cap % 32 != 0)
+            throw std::invalid_argument("tile N caps must be multiples of 32 up to 256");
+    if (tiling.splitk < 1 || tiling.splitk > 8 || (tiling.splitk > 1 && nrhs > 1))
+        throw std::invalid_argument("split-K of 1..8, single right-hand side only");
     Plan P;
+    P.splitk = tiling.splitk;
     P.split = true;
     P.association = 0;
     P.nrhs = nrhs;
@@ -1360,7 +1366,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
         p1.flops += 2.0 * stack_rows[y] * nrhs * Y.cols[y] * s.K;
         // column tiles start on panel K steps (multiples of 32): the epilogue writes whole row segments
         const size_t t0 = p1.tiles.size();
-        add_tiles(p1, st.off, st.pitch, stack_rows[y], ywide(y), sb, sb + 1, kUmmaTileM, kUmmaTileN, 32);
+        add_tiles(p1, st.off, st.pitch, stack_rows[y], ywide(y), sb, sb + 1, kUmmaTileM, tiling.ncap1, 32);
         for (size_t t = t0; t < p1.tiles.size(); ++t) {
             p1.tiles[t].rstride = P.ycolsP[y];
             p1.tiles[t].nrhs = nrhs;
@@ -1385,6 +1391,30 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
     auto mark = [&](size_t t0) {
         for (size_t t = t0; t < p2.tiles.size(); ++t) p2.tiles[t].nrhs = nrhs;
     };
+    const int nsk = tiling.splitk;
+    // tiles of output block o for segments [sb, se): split-K cuts the segment list
+    // into nsk parts of about equal K (part j -> element offset j * vstride of the
+    // partial buffer); parts without segments write zeros
+    auto block_tiles = [&](int64_t o, int32_t sb, int32_t se) {
+        const size_t t0 = p2.tiles.size();
+        if (nsk == 1) {
+            add_tiles(p2, O.off[o], O.ld[o], (int64_t)nrhs * O.rows[o], O.cols[o], sb, se, kUmmaTileM, tiling.ncap2);
+        } else {
+            double ktot = 0;
+            for (int32_t q = sb; q < se; ++q) ktot += p2.segs[q].K;
+            int32_t a = sb;
+            double acc = 0;
+            for (int j = 0; j < nsk; ++j) {
+                int32_t b = a;
+                const double goal = ktot * (j + 1) / nsk;
+                while (b < se && (j == nsk - 1 || acc + 0.5 * p2.segs[b].K <= goal)) acc += p2.segs[b++].K;
+                add_tiles(p2, O.off[o] + (int64_t)j * P.vstride, O.ld[o], O.rows[o], O.cols[o], a, b, kUmmaTileM,
+                          tiling.ncap2);
+                a = b;
+            }
+        }
+        mark(t0);
+    };
     size_t i = 0;
     while (i < order.size()) {
         const int64_t o = ch[order[i]].out;
@@ -1407,19 +1437,12 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
             ++i;
         }
         p2.flops += 2.0 * nrhs * O.rows[o] * O.cols[o] * kk;
-        const size_t t0 = p2.tiles.size();
-        add_tiles(p2, O.off[o], O.ld[o], (int64_t)nrhs * O.rows[o], O.cols[o], sb, (int32_t)p2.segs.size(),
-                  kUmmaTileM, kUmmaTileN);
-        mark(t0);
+        block_tiles(o, sb, (int32_t)p2.segs.size());
     }
     P.flops_p2_unsummed = p2.flops;
     const int32_t sb = (int32_t)p2.segs.size();
     for (size_t o = 0; o < O.rows.size(); ++o)
-        if (!seen[o]) {
-            const size_t t0 = p2.tiles.size();
-            add_tiles(p2, O.off[o], O.ld[o], (int64_t)nrhs * O.rows[o], O.cols[o], sb, sb, kUmmaTileM, kUmmaTileN);
-            mark(t0);
-        }
+        if (!seen[o]) block_tiles((int64_t)o, sb, sb);
     sort_tiles(p2);
     return P;
 }

@@ -126,6 +126,18 @@ class _Pivot:
                                                C.byref(st)))
         return mu, st.as_dict()
 
+    def autotune(self, trials=5) -> dict:
+        """Choose the split-precision tiling (tile N caps, split-K) of this pivot by
+        timing the candidates on it (vmps_pivot_autotune); cached per sector layout."""
+        info = N.vmps_tune_info()
+        N.check(N.lib().vmps_pivot_autotune(self._h, int(trials), C.byref(info)))
+        return info.as_dict()
+
+    def set_tiling(self, ncap1=256, ncap2=256, splitk=1):
+        """Fix the split-precision tiling (tile N caps of the two phases, split-K of
+        phase 2) without tuning."""
+        N.check(N.lib().vmps_pivot_set_tiling(self._h, int(ncap1), int(ncap2), int(splitk)))
+
     def set_projector(self, A0proj, Epenalty: float):
         """Excited-state projector (PivotMatrix1/2::A0proj, Epenalty): every later HxV
         adds Epenalty * <A0_n|Vin> * A0_n for each vector A0_n (compact layout of this
