@@ -173,6 +173,44 @@ def oracle_check(L, R, V, W1, W2, v0, h64, hsp, e_ref, e64, es, x64, xs):
     return out
 
 
+def autotune_small(ctx):
+    """The autotuner on the small and middle pivots of the configurations: the
+    two-site middle pivots of the Heisenberg chain L=32 D=64 (C1's model and size),
+    the Hubbard chain at D=256 and D=1024 (C2's first stage), and the C5 pivot
+    (Hubbard D=512, N=63): tuned against default ms per split HxV (CUDA events)."""
+    from vmps_gb300.pivot import PivotMatrix2
+    from vmps_gb300.workloads import hubbard_two_site, heisenberg_two_site
+    out = {}
+    cases = [("heisenberg_L32_D64", lambda: heisenberg_two_site(ctx, L=32, D=64, seed=1)),
+             ("hubbard_L64_D256", lambda: hubbard_two_site(ctx, L=64, D=256, seed=2)),
+             ("hubbard_L64_D512_N63", lambda: hubbard_two_site(ctx, L=64, D=512, seed=5, Qtot=(63, -1))),
+             ("hubbard_L64_D1024", lambda: hubbard_two_site(ctx, L=64, D=1024, seed=2))]
+    for name, make in cases:
+        model, mps, Lenv, Renv, W1, W2, V, info = make()
+        H = PivotMatrix2(ctx, model.sym, Lenv, Renv, W1, W2, V)
+        t = H.autotune(trials=10)
+        t["speedup"] = t["ms_default"] / t["ms_best"] if t["ms_best"] > 0 else None
+        t["dim_V"] = H.dim
+        out[name] = t
+        H.close()
+    return out
+
+
+def step_trace(a, b):
+    """per-step comparison of two sweeps run from the same MPS: relative energy
+    difference of every local solve, the first step where it exceeds 1e-10 (-1: none)
+    and the split-precision HxVs of run a"""
+    ea = np.array([s[2] for s in a["steps"]])
+    eb = np.array([s[2] for s in b["steps"]])
+    d = np.abs(ea - eb) / np.abs(eb)
+    first = int(np.argmax(d > 1e-10)) if np.any(d > 1e-10) else -1
+    return {"steps": int(d.size), "max_rel_diff": float(d.max()), "first_step_above_1e-10": first,
+            "site_of_first": int(a["steps"][first][1]) if first >= 0 else None,
+            "max_rel_diff_before_first": float(d[:first].max()) if first > 0 else (float(d.max()) if first < 0 else None),
+            "rel_diff_first_12": [float(x) for x in d[:12]], "split_hxv": int(sum(s[3] for s in a["steps"])),
+            "fp64_hxv": int(sum(s[4] for s in a["steps"]))}
+
+
 def sweep_bench(ctx, args, with_cpu=True):
     """Single-site DMRG sweep times.
 
@@ -209,7 +247,8 @@ def sweep_bench(ctx, args, with_cpu=True):
     if args.D >= 1024:
         model = models.hubbard_u1xu1(64, t=1.0, U=4.0)
         mps0 = RandomMPS(model, (64, 0), 1024, seed=2, profile="gaussian", sigma=[2.5, 2.5]).canonicalize(0, 0)
-        tol = dict(tol_eigval=1e-10, tol_state=1e-6)
+        tol = dict(tol_eigval=1e-10, tol_state=1e-6)        # sweep tolerances
+        tight = dict(tol_eigval=1e-13, tol_state=1e-10)     # converged comparisons
         split_kw = dict(precision=args.precision, refine_iters=10, **tol)
 
         def summary(r):
@@ -217,27 +256,55 @@ def sweep_bench(ctx, args, with_cpu=True):
                     "timers_s": [{k: round(v, 4) for k, v in t.items()} for t in r["timers"]],
                     "lanczos": r["solves"]}
 
-        hub = {"tolerances": dict(refine_iters=10, **tol)}
+        hub = {"tolerances": dict(refine_iters=10, **tol), "tight": tight}
         mps = copy.deepcopy(mps0)
-        hub["from_random_split"] = summary(dmrg1(ctx, model, mps, n_sweeps=2, **split_kw))
-        hub["from_random_fp64"] = summary(dmrg1(ctx, model, copy.deepcopy(mps0), n_sweeps=2, precision="fp64",
-                                                **tol))
+        rs = dmrg1(ctx, model, mps, n_sweeps=2, **split_kw)
+        r6 = dmrg1(ctx, model, copy.deepcopy(mps0), n_sweeps=2, precision="fp64", **tol)
+        hub["from_random_split"] = summary(rs)
+        hub["from_random_fp64"] = summary(r6)
+        hub["from_random_trace"] = step_trace(rs, r6)
         w = dmrg1(ctx, model, mps, n_sweeps=4, **split_kw)
         hub["warm_split_sweeps"] = summary(w)
-        r64 = dmrg1(ctx, model, copy.deepcopy(mps), n_sweeps=1, precision="fp64", **tol)
-        rsp = dmrg1(ctx, model, copy.deepcopy(mps), n_sweeps=1, **split_kw)
+        # near convergence, one sweep in each precision with tight tolerances; the split
+        # run skips the FP64 probe, so that its local solves do run split-precision HxVs
+        r64 = dmrg1(ctx, model, copy.deepcopy(mps), n_sweeps=1, precision="fp64", **tight)
+        rsp = dmrg1(ctx, model, copy.deepcopy(mps), n_sweeps=1, precision=args.precision, refine_iters=10,
+                    probe=False, **tight)
         hub["converged_fp64"] = summary(r64)
-        hub["converged_split"] = summary(rsp)
+        hub["converged_split_no_probe"] = summary(rsp)
+        hub["converged_trace"] = step_trace(rsp, r64)
         hub["converged_rel_diff"] = abs(rsp["energies"][-1] - r64["energies"][-1]) / abs(r64["energies"][-1])
         out["hubbard_L64_D1024"] = hub
-        # two-site DMRG (the sweep of the metric's configuration) at D=1024: one sweep in
-        # each precision from the same random MPS, bond bases truncated by the SVD
+        # two-site DMRG (the sweep of the metric's configuration) at Dmax=1024 from the same
+        # random MPS: one sweep in each precision (timings and the per-step trace), an FP64
+        # control from the MPS perturbed by 1e-12 (where FP64 parts from FP64), then three
+        # more split sweeps to convergence and one more sweep in each precision with tight
+        # tolerances (split HxVs forced: no FP64 probe)
         from vmps_gb300.dmrg import dmrg2
         two = {"tolerances": dict(refine_iters=3, **tol), "Dmax": 1024}
-        for tag, prec, kw in (("split", args.precision, dict(refine_iters=3)), ("fp64", "fp64", {})):
-            r = dmrg2(ctx, model, copy.deepcopy(mps0), n_sweeps=1, Dmax=1024, precision=prec, **tol, **kw)
+        mps_s = copy.deepcopy(mps0)
+        rs = dmrg2(ctx, model, mps_s, n_sweeps=1, Dmax=1024, precision=args.precision, refine_iters=3, **tol)
+        r6 = dmrg2(ctx, model, copy.deepcopy(mps0), n_sweeps=1, Dmax=1024, precision="fp64", **tol)
+        mps_p = copy.deepcopy(mps0)
+        noise = np.random.default_rng(99)
+        for A in mps_p.A:
+            A.data *= 1.0 + 1e-12 * noise.standard_normal(A.data.size)
+        rc = dmrg2(ctx, model, mps_p, n_sweeps=1, Dmax=1024, precision="fp64", **tol)
+        for tag, r in (("split", rs), ("fp64", r6)):
             two[tag] = dict(summary(r), truncation=r["truncation"], max_bond_dim=r["max_bond_dim"])
         two["sweep_speedup"] = two["fp64"]["s_per_sweep"][0] / two["split"]["s_per_sweep"][0]
+        two["trace_split_vs_fp64"] = step_trace(rs, r6)
+        two["trace_fp64_vs_perturbed_fp64"] = step_trace(rc, r6)
+        conv = dmrg2(ctx, model, mps_s, n_sweeps=3, Dmax=1024, precision=args.precision, refine_iters=10,
+                     tol_eigval=1e-12, tol_state=1e-8)
+        c64 = dmrg2(ctx, model, copy.deepcopy(mps_s), n_sweeps=1, Dmax=1024, precision="fp64", **tight)
+        csp = dmrg2(ctx, model, copy.deepcopy(mps_s), n_sweeps=1, Dmax=1024, precision=args.precision,
+                    refine_iters=10, probe=False, **tight)
+        two["converging_split_E"] = conv["energies"]
+        two["converged"] = {"fp64": dict(summary(c64), truncation=c64["truncation"]),
+                            "split_no_probe": dict(summary(csp), truncation=csp["truncation"]),
+                            "trace": step_trace(csp, c64),
+                            "E_rel_diff": abs(csp["energies"][-1] - c64["energies"][-1]) / abs(c64["energies"][-1])}
         out["hubbard_L64_D1024_two_site"] = two
     if args.D >= 4096 and not args.no_window:
         # two-site DMRG at D=4096: a window of bonds around the middle of the chain
@@ -250,11 +317,14 @@ def sweep_bench(ctx, args, with_cpu=True):
                          sigma=[2.5, 2.5]).canonicalize(lo, lo + 1)
         win = {"window": [lo, lo + width], "steps": 2 * width, "Dmax": 4096,
                "tolerances": dict(refine_iters=3, tol_eigval=1e-10, tol_state=1e-6)}
+        runs = {}
         for tag, prec, kw in (("split", args.precision, dict(refine_iters=3)), ("fp64", "fp64", {})):
             r = dmrg2(ctx, model, copy.deepcopy(mps0), n_sweeps=1, Dmax=4096, precision=prec,
                       tol_eigval=1e-10, tol_state=1e-6, window=(lo, lo + width), **kw)
+            runs[tag] = r
             win[tag] = dict(summary(r), s_per_step=r["sweep_times"][0] / (2 * width), truncation=r["truncation"])
         win["E_rel_diff"] = abs(win["split"]["E"][-1] - win["fp64"]["E"][-1]) / abs(win["fp64"]["E"][-1])
+        win["trace"] = step_trace(runs["split"], runs["fp64"])
         win["step_speedup"] = win["fp64"]["s_per_step"] / win["split"]["s_per_step"]
         out["hubbard_L64_D4096_two_site_window"] = win
     return out
@@ -307,11 +377,13 @@ def su2_cylinder_bench(ctx, args):
     from vmps_gb300.dmrg import dmrg1
     from vmps_gb300.mps import RandomMPS
     mps0 = RandomMPS(model, (1, info["N"]), 2000, seed=3, profile="gaussian", sigma=[3.0, 3.0]).canonicalize(0, 0)
-    sweep = {}
+    sweep, runs = {}, {}
     for tag, prec, kw in (("split", args.precision, dict(refine_iters=10)), ("fp64", "fp64", {})):
         r = dmrg1(ctx, model, copy.deepcopy(mps0), n_sweeps=1, precision=prec, **tol, **kw)
+        runs[tag] = r
         sweep[tag] = {"s_per_sweep": r["sweep_times"], "E": r["energies"], "lanczos": r["solves"],
                       "timers_s": [{k: round(v, 4) for k, v in t.items()} for t in r["timers"]]}
+    sweep["trace"] = step_trace(runs["split"], runs["fp64"])
     sweep["sweep_speedup"] = sweep["fp64"]["s_per_sweep"][0] / sweep["split"]["s_per_sweep"][0]
     return dict(info, n_tasks=st64["n_tasks"], flops_per_hxv=st64["flops_merged"], single_site_sweep=sweep,
                 hxv_fp64={"ms": ms64, "per_s": 1e3 / ms64, "tflops": st64["flops_merged"] / ms64 * 1e-9},
@@ -569,6 +641,7 @@ def main():
     ap.add_argument("--no-su2", action="store_true")
     ap.add_argument("--no-vumps", action="store_true")
     ap.add_argument("--no-window", action="store_true", help="skip the D=4096 two-site window")
+    ap.add_argument("--no-tune-small", action="store_true", help="skip the autotuner on the smaller pivots")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -588,6 +661,8 @@ def main():
     ctx = Context(local)
     model, mps, Lenv, Renv, W1, W2, V, info = hubbard_two_site(ctx, L=args.L, D=args.D, seed=args.seed)
     H = PivotMatrix2(ctx, model.sym, Lenv, Renv, W1, W2, V)
+    # tile shape and split-K of the split plan: timed candidates on this pivot (autotuner)
+    tune = H.autotune(trials=5) if args.precision == "bf16x3" else None
     st_split = H.stats(args.precision)
     st64 = H.stats("fp64")
     n = H.dim
@@ -693,6 +768,10 @@ def main():
     if not args.no_vumps and rank == 0:
         vum = vumps_bench(ctx, args)
 
+    tune_small = None
+    if rank == 0 and args.precision == "bf16x3" and not args.no_tune_small:
+        tune_small = autotune_small(ctx)
+
     cpu = None
     if not args.no_cpu and world == 1 and rank == 0:
         threads = os.cpu_count() or 1
@@ -713,7 +792,9 @@ def main():
             "timing": {"working_set_MB": round(working_set / 2 ** 20, 1), "l2_note": l2_note,
                        "graph": "CUDA graph per HxV (vector split + 2 grouped-GEMM launches)"},
             "e2e": {"value": e2e, "unit": "HxV/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
-            "gpu_launches": (3 if args.precision == "bf16x3" else 2) * args.steps,
+            "gpu_launches": ((3 + (1 if tune and tune["splitk"] > 1 else 0)) if args.precision == "bf16x3" else 2)
+                            * args.steps,
+            "autotune": {"headline_pivot": tune, "small_pivots": tune_small},
             "fp64": {"value": world * 1000.0 / ms64, "unit": "HxV/s", "ms_per_step": ms64,
                      "phase2_ms": ms64_2, "flops_executed": st64["flops_executed"]},
             "split_over_fp64": ms64 / ms,

@@ -106,3 +106,26 @@ def test_dmrg2_window(gpu_ctx):
     e_ed = ed.ground_energy(H, _hubbard_sector(L, L, 0))
     assert abs(r["energies"][-1] - e_ed) < 1e-10 * abs(e_ed), (r, e_ed)
     assert [dict(centred.dims[b]) for b in (1, 5)] == dims_before
+
+
+def test_converged_sweep_split_equals_fp64_step_by_step(gpu_ctx):
+    """A converged two-site sweep (Hubbard L=24, Dmax=256) in both precisions with
+    tight tolerances from the same MPS; the split-precision run skips the FP64 probe,
+    so every local solve runs split HxVs before its FP64 refinement.  Every one of
+    the sweep's local ground-state energies agrees with the FP64 sweep to 1e-10
+    relative (the |dE/E| of the metric), and so does the final energy."""
+    L = 24
+    model = models.hubbard_u1xu1(L, t=1.0, U=4.0)
+    mps = RandomMPS(model, (L, 0), 256, seed=2, profile="gaussian", sigma=[2.5, 2.5]).canonicalize(0, 0)
+    dmrg2(gpu_ctx, model, mps, n_sweeps=4, Dmax=256, precision="bf16x3", refine_iters=10, tol_eigval=1e-12,
+          tol_state=1e-8)
+    tight = dict(tol_eigval=1e-13, tol_state=1e-10)
+    r64 = dmrg2(gpu_ctx, model, copy.deepcopy(mps), n_sweeps=1, Dmax=256, precision="fp64", **tight)
+    rsp = dmrg2(gpu_ctx, model, copy.deepcopy(mps), n_sweeps=1, Dmax=256, precision="bf16x3", refine_iters=10,
+                probe=False, **tight)
+    e64 = np.array([s[2] for s in r64["steps"]])
+    esp = np.array([s[2] for s in rsp["steps"]])
+    assert sum(s[3] for s in rsp["steps"]) > 0            # split HxVs ran
+    assert all(s[3] > 0 for s in rsp["steps"])            # in every local solve
+    assert np.max(np.abs(esp - e64) / np.abs(e64)) < 1e-10
+    assert abs(rsp["energies"][-1] - r64["energies"][-1]) < 1e-10 * abs(r64["energies"][-1])

@@ -56,6 +56,20 @@ def hubbard_two_site(ctx, L=64, D=4096, U=4.0, seed=2, sigma=2.5, verbose=False,
     return model, mps, Lenv, Renv, model.W[site], model.W[site + 1], V, info
 
 
+def heisenberg_two_site(ctx, L=32, D=64, seed=1):
+    """Heisenberg U(1) chain, Sz = 0; two-site pivot in the middle (the same return
+    values as hubbard_two_site)."""
+    model = models.heisenberg_u1(L)
+    site = L // 2 - 1
+    mps = RandomMPS(model, (0,), D, seed=seed, profile="gaussian", sigma=[4.0]).canonicalize(site, site + 1)
+    Lenv, Renv = build_envs(ctx, model, mps, site, site + 1)
+    V = contract_two_sites(model.sym, mps.A[site], mps.A[site + 1], model.qloc, model.qloc, model.sym.nq)
+    info = dict(model=model.name, L=L, D=D, site=site, seed=seed, D_left=mps.bond_dim(site),
+                sectors_left=len(mps.dims[site]), dim_V=int(V.data.size),
+                env_elems=int(Lenv.data.size + Renv.data.size))
+    return model, mps, Lenv, Renv, model.W[site], model.W[site + 1], V, info
+
+
 def heisenberg_one_site(ctx, L=32, D=64, seed=1, site=None):
     """Heisenberg U(1) chain, Sz = 0; one-site pivot (default: the middle)."""
     model = models.heisenberg_u1(L)
