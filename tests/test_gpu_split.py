@@ -5,7 +5,10 @@ routine (LAPACK) on the same two-site tensors: the same middle bond basis and
 block layout, the kept singular spectrum and discarded weight to 1e-12, the same
 truncated two-site tensor to 1e-12 (eigenvector signs may differ), orthonormal
 factors.  The device threshold is lowered so that most sectors take the device
-path, and left at its default for the D=1024 case."""
+path, and left at its default for the D=1024 case.  The cuts keep singular values
+well above the Gram matrices' resolution (about 1e-8 of the largest value: the
+Gram matrix squares them), with a gap at the cut: states below that resolution
+are determined by rounding alone, in either routine."""
 import numpy as np
 import pytest
 
@@ -37,7 +40,7 @@ def _compare(a, b, move, dmax):
 
 @pytest.mark.parametrize("move", ["right", "left"])
 @pytest.mark.parametrize("kind,L,D,l,gmin,dmax", [("hubbard", 12, 256, 5, "16", 200),
-                                                  ("heisenberg", 24, 1024, 11, "512", 700)])
+                                                  ("heisenberg", 24, 1024, 11, "512", 301)])
 def test_device_split_matches_host(gpu_ctx, monkeypatch, move, kind, L, D, l, gmin, dmax):
     if not native_lapack():
         pytest.skip("numpy's bundled OpenBLAS exports no ILP64 LAPACK")
