@@ -749,6 +749,7 @@ def main():
             prof = json.load(f)
     roofline = {"bound": "tensor", "achieved": tensor_flops, "peak": bf16, "unit": "TFLOP/s",
                 "frac": tensor_flops / bf16, "traffic": (prof or {}).get(f"traffic_{phase}"),
+                "traffic_commit": (prof or {}).get("commit"),
                 "kernel": f"{engine} ({phase})", "peak_source": f"bf16_tflops of {peak_kind}",
                 "useful_tflops": flops_phase / (t_phase * 1e-3) / 1e12,
                 "issued_tflops": st_split[f"tensor_flops_{phase}"] / (t_phase * 1e-3) / 1e12,

@@ -205,8 +205,8 @@ int vmps_pivot_dim(const vmps_pivot* p, int64_t* out);
  * each of the two phases and a split-K of 1, 2 or 4 for the second phase (more
  * than 1 only when that phase has fewer tiles than twice the SM count; the parts
  * are summed in a fixed order, so results stay deterministic).  Each candidate is
- * timed on this pivot (`trials` HxVs, CUDA events) and the fastest kept, ties to
- * the default (256, 256, 1).  The choice is cached for the process under the
+ * timed on this pivot (the median of `trials` HxVs, CUDA events, after a warm-up)
+ * and the fastest kept if it beats the default (256, 256, 1) by 2 %.  The choice is cached for the process under the
  * pivot's sector-layout key (the histogram of its chains' block sizes); a pivot
  * whose key is cached takes the cached choice without timing, and with the
  * environment variable VMPS_AUTOTUNE=1 every new layout is tuned (3 trials) when
@@ -348,13 +348,16 @@ int  vmps_gauge_step(int nq, int move_right, const vmps_blocks* A, double* a, co
                      const vmps_blocks* N, double* n, int threads);
 int  vmps_hostla_load(const char* path);
 int  vmps_two_site_split(const vmps_split_args* args, const vmps_blocks* V, const double* v, vmps_split** out);
-/* The same split with the large sectors on the GPU in FP64: sectors whose Gram
+/* The same split with the largest sectors on the GPU in FP64: a sector whose Gram
  * matrix has order >= VMPS_SPLIT_GPU_MIN (environment variable, 512 by default)
- * form it with cuBLAS dsyrk, take its full eigensystem with cuSOLVER dsyevd and
- * the non-orthonormal factor with cuBLAS dgemm, on the context's stream and a
- * host thread of their own, while the host threads factor the smaller sectors
- * as above.  The truncation rule and the output layout are the host routine's.
- * Still needs vmps_hostla_load for the small sectors.                          */
+ * may form it with cuBLAS dsyrk, take its full eigensystem with cuSOLVER dsyevd and
+ * the non-orthonormal factor with cuBLAS dgemm, on the context's stream and a host
+ * thread of their own, while the host threads factor the other sectors as above.
+ * Largest first, a sector goes to the device when the estimated end of the split
+ * (the later of the device queue and the host threads' makespan) comes earlier;
+ * VMPS_SPLIT_DEVICE=all sends every sector of order >= VMPS_SPLIT_GPU_MIN.  The
+ * truncation rule and the output layout are the host routine's.  Still needs
+ * vmps_hostla_load for the host sectors.                                       */
 int  vmps_two_site_split_device(vmps_ctx* ctx, const vmps_split_args* args, const vmps_blocks* V, const double* v,
                                 vmps_split** out);
 int  vmps_split_info(const vmps_split* s, int* nmid, double* disc, int64_t* nblocks1, int64_t* size1,

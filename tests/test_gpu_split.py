@@ -46,6 +46,7 @@ def test_device_split_matches_host(gpu_ctx, monkeypatch, move, kind, L, D, l, gm
         pytest.skip("numpy's bundled OpenBLAS exports no ILP64 LAPACK")
     model, V, comb, din, dout = _case(L, D, l, seed=3, kind=kind, sigma=1.0)
     monkeypatch.setenv("VMPS_SPLIT_GPU_MIN", gmin)
+    monkeypatch.setenv("VMPS_SPLIT_DEVICE", "all")   # every sector of order >= gmin on the device
     pool = SectorPool(4)
     try:
         nq = model.sym.nq

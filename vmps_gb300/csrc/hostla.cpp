@@ -16,10 +16,11 @@
 // OpenBLAS that numpy bundles (bound at run time from the path the caller
 // passes), one sector per host thread, largest first.  With a device context
 // (vmps_two_site_split_device) the sectors whose Gram matrix has order >=
-// VMPS_SPLIT_GPU_MIN (512 by default) run on the GPU in FP64 instead -- the
+// VMPS_SPLIT_GPU_MIN (512 by default) may run on the GPU in FP64 instead -- the
 // Gram matrix (cuBLAS dsyrk, DMMA), its eigensystem (cuSOLVER dsyevd) and the
 // non-orthonormal factor (cuBLAS dgemm) -- on a thread of their own while the
-// host threads factor the rest.
+// host threads factor the rest; which of them do is decided by estimated costs
+// (assign_device_sectors), or VMPS_SPLIT_DEVICE=all sends every one of them.
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
@@ -471,6 +472,43 @@ int64_t split_gpu_min() {
     return (int64_t)x;
 }
 
+// Which sectors go to the device.  The device thread factors its sectors one after
+// another while `threads` host threads share the rest, so the split ends with the
+// later of the two.  Largest first, a sector (of Gram order >= gmin) goes to the
+// device when that makes the estimated end earlier; the estimates are fitted to
+// GB300 + Grace measurements of the split at a D=4096 bond (Gram orders up to 772:
+// 0.115 s on 16 host threads; every sector of order >= 512 on the device: 0.183 s;
+// the largest one only: 0.095 s): a host sector of order n and k columns takes
+// about 1.3e-10 s * n^2 (n + k), a device sector about 8 ms + 2.5e-11 s * n^2 (n + k)
+// (the device's FP64 eigensolver runs its tridiagonal stage at a low rate, and each
+// sector pays for its transfers and its own sequence of launches).
+void assign_device_sectors(const std::vector<Sector*>& work, bool right, int64_t gmin, int threads,
+                           std::vector<Sector*>& gwork, std::vector<Sector*>& hwork) {
+    const int nt = std::max(1, threads);
+    const char* pol = std::getenv("VMPS_SPLIT_DEVICE");   // "all": every sector of order >= gmin
+    if (pol && !std::strcmp(pol, "all")) {
+        for (Sector* s : work) ((right ? s->rows : s->cols) >= gmin ? gwork : hwork).push_back(s);
+        return;
+    }
+    std::vector<double> bins((size_t)nt, 0.0);   // host threads' estimated loads (largest-first list scheduling)
+    double tdev = 0;
+    auto host_cost = [](double n, double k) { return 1.3e-10 * n * n * (n + k); };
+    auto dev_cost = [](double n, double k) { return 8e-3 + 2.5e-11 * n * n * (n + k); };
+    for (Sector* s : work) {   // work is sorted largest first
+        const double n = (double)(right ? s->rows : s->cols), k = (double)(right ? s->cols : s->rows);
+        auto lo = std::min_element(bins.begin(), bins.end());
+        const double host_end = std::max(*std::max_element(bins.begin(), bins.end()), *lo + host_cost(n, k));
+        const double dev_end = std::max(tdev + dev_cost(n, k), *std::max_element(bins.begin(), bins.end()));
+        if (n >= (double)gmin && std::max(dev_end, tdev + dev_cost(n, k)) < std::max(host_end, tdev)) {
+            tdev += dev_cost(n, k);
+            gwork.push_back(s);
+        } else {
+            *lo += host_cost(n, k);
+            hwork.push_back(s);
+        }
+    }
+}
+
 // gpu: device state of a context, or null (host only)
 void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd, vmps_split_s& out, GpuLa* gpu) {
     const int nq = a->nq;
@@ -564,8 +602,8 @@ void run_split(const vmps_split_args* a, const vmps_blocks* V, const double* Vd,
     // the large sectors (Gram order >= the device threshold) on the device thread,
     // the others on the host threads meanwhile
     std::vector<Sector*> gwork, hwork;
-    const int64_t gmin = gpu ? split_gpu_min() : 0;
-    for (Sector* s : work) ((gpu && (right ? s->rows : s->cols) >= gmin) ? gwork : hwork).push_back(s);
+    if (gpu) assign_device_sectors(work, right, split_gpu_min(), threads, gwork, hwork);
+    else hwork = work;
     auto on_device = [&](const std::vector<Sector*>& list, auto fn) {
         if (list.empty()) return std::thread();
         return std::thread([&, fn]() {

@@ -1017,14 +1017,31 @@ static double time_split_plan(vmps_pivot* p, const SplitTiling& tl, int trials, 
     ops.O = p->vout.as<double>();
     run_plan(dp, ops, st);   // warm-up
     CK(cudaStreamSynchronize(st));
-    CK(cudaEventRecord(p->ctx->ev0, st));
-    for (int i = 0; i < trials; ++i) run_plan(dp, ops, st);
-    CK(cudaEventRecord(p->ctx->ev1, st));
-    CK(cudaEventSynchronize(p->ctx->ev1));
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, p->ctx->ev0, p->ctx->ev1));
+    // one event between consecutive HxVs; the median per-HxV time is robust to a
+    // slow outlier (a first launch under a profiler, a clock change)
+    std::vector<cudaEvent_t> ev((size_t)trials + 1, nullptr);
+    std::vector<double> t((size_t)trials);
+    try {
+        for (auto& e : ev) CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(ev[0], st));
+        for (int i = 0; i < trials; ++i) {
+            run_plan(dp, ops, st);
+            CK(cudaEventRecord(ev[(size_t)i + 1], st));
+        }
+        CK(cudaEventSynchronize(ev[(size_t)trials]));
+        for (int i = 0; i < trials; ++i) {
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, ev[(size_t)i], ev[(size_t)i + 1]));
+            t[(size_t)i] = ms;
+        }
+    } catch (...) {
+        for (auto e : ev) if (e) cudaEventDestroy(e);
+        throw;
+    }
+    for (auto e : ev) cudaEventDestroy(e);
     check_device_error(p->ctx);
-    return (double)ms / trials;
+    std::sort(t.begin(), t.end());
+    return t[t.size() / 2];
 }
 
 static SplitTiling tune_pivot(vmps_pivot* p, int trials, double* ms_default, double* ms_best, int* ncand) {
@@ -1037,8 +1054,10 @@ static SplitTiling tune_pivot(vmps_pivot* p, int trials, double* ms_default, dou
     CK(cudaStreamSynchronize(p->st()));
     const SplitTiling def;
     int64_t tiles2 = 0;
+    time_split_plan(p, def, 1, nullptr);   // module and descriptor warm-up before anything is compared
     double best = time_split_plan(p, def, trials, &tiles2);
     *ms_default = best;
+    const double margin = 0.98;   // a candidate must beat the default by 2 % (timing noise)
     SplitTiling pick = def;
     int n = 1;
     std::vector<SplitTiling> cand;
@@ -1054,7 +1073,7 @@ static SplitTiling tune_pivot(vmps_pivot* p, int trials, double* ms_default, dou
     for (const SplitTiling& t : cand) {
         const double ms = time_split_plan(p, t, trials, nullptr);
         ++n;
-        if (ms < best) { best = ms; pick = t; }
+        if (ms < best && ms < margin * *ms_default) { best = ms; pick = t; }
     }
     *ms_best = best;
     *ncand = n;
