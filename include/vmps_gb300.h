@@ -48,6 +48,10 @@ extern "C" {
 /* ---- arithmetic of the block products --------------------------------------*/
 #define VMPS_PREC_FP64       0   /* plain FP64 (DMMA), parity with the Eigen path */
 #define VMPS_PREC_BF16X3     1   /* hi*hi + hi*lo + lo*hi bf16 products, FP32 accumulate */
+#define VMPS_PREC_TF32X3     2   /* the same three products with TF32 hi/lo operands (3xTF32): about
+                                    2^-21 relative per product against 2^-16, at half the bf16 tensor
+                                    rate; pivot HxVs and Lanczos solves (not the multi-RHS, Chebyshev,
+                                    environment and transfer-operator entry points)         */
 
 /* ---- symmetry descriptor ----------------------------------------------------
  * A quantum number is nq int32 values.  kind[i] says how component i fuses:

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(_HERE, "libvmps_gb300.so")
 VMPS_OK = 0
 PREC_FP64 = 0
 PREC_BF16X3 = 1
+PREC_TF32X3 = 2
 SYM_U1 = 0
 SYM_SU2 = 1
 ENV_LEFT = 0

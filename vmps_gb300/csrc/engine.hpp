@@ -233,6 +233,11 @@ struct Plan {
     // K concatenation writes the whole block at element offset j * vstride of a
     // partial buffer; a reduction sums the parts in order into the output
     int splitk = 1;
+    // panel element: bf16 (elt 2; a 128-byte row segment is [32 hi | 32 lo], one K
+    // step of 32) or tf32 in FP32 storage (elt 4; [16 hi | 16 lo], one K step of 16).
+    // Offsets, pitches and TMA x coordinates are in elements either way (x = 2 * k0).
+    int elt = 2;
+    int kstep = kUmmaBK;
 };
 // Tile options of a split-precision plan (chosen by the autotuner): the N caps of
 // the phase-1 and phase-2 tiles (multiples of 32, at most kUmmaTileN) and the
@@ -252,7 +257,7 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // single-vector segments once per right-hand side, reading its K range of T).
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
                      const DevLayout& O, bool transX, bool transZ, int nrhs = 1,
-                     const SplitTiling& tiling = SplitTiling());
+                     const SplitTiling& tiling = SplitTiling(), bool tf32 = false);
 // One FP64 grouped-GEMM phase of plain block products C[k] = sum A[i] * B[j] over
 // the (k, i, j) triples (contract_AA2's two-site tensor): one tile range per
 // output block, one segment per product; output blocks without a product are
@@ -262,7 +267,8 @@ PhasePlan make_product_plan(const DevLayout& A, const DevLayout& B, const DevLay
 // Static schedule of a split phase for the persistent tcgen05 engine on ncta
 // CTAs: K steps of kUmmaBK per segment with their TMA boxes, tiles assigned
 // longest-first to the least-loaded CTA and stored CTA by CTA.
-void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B);
+void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B,
+                  int kstep = kUmmaBK);
 // TMA box heights: A boxes 16/32/64/128 rows, B boxes a multiple of 32 up to
 // 256 (16 for the narrowest), the smallest that covers the tile
 int32_t box_rows_a(int32_t tm);

@@ -287,6 +287,55 @@ __global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np
     }
 }
 
+// ---------------------------------------------------------------------------
+// 3xTF32 panels: FP32 storage, element k of panel row i at i*pitch + (k/16)*32 +
+// k%16 (hi) and + 16 (lo); hi = tf32(v), lo = tf32(v - hi), both with their low
+// 13 mantissa bits zero (the tensor cores read TF32 from the upper 19 bits)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int panel_pos_tf32(int k) { return ((k >> 4) << 5) | (k & 15); }
+__device__ __forceinline__ float to_tf32(float v) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
+__device__ __forceinline__ void split_store_tf32(float* row, int k, float v) {
+    const float h = to_tf32(v);
+    const int p = panel_pos_tf32(k);
+    row[p] = h;
+    row[p + 16] = to_tf32(v - h);
+}
+__global__ void prep_tf32_kernel(const PrepBlock* __restrict__ pbs, int nb, const double* __restrict__ src,
+                                 float* __restrict__ dst) {
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        const PrepBlock pb = pbs[b];
+        const int rows = pb.rows, n = pb.rows * pb.cols;
+        const bool unit = pb.scale == 1.0;
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int j = e / rows, i = e - j * rows;
+            const double x = src[pb.src_off + i + (int64_t)j * pb.src_ld];
+            const float v = f64_to_f32_rn(unit ? x : pb.scale * x);
+            const int r = pb.trans ? i : j, k = pb.trans ? j : i;
+            split_store_tf32(dst + pb.dst_off + (int64_t)r * pb.dst_ld, k, v);
+        }
+    }
+}
+// vector pieces -> 3xTF32 panels: one element per thread (column c of the piece is
+// panel row c, its element r is K index r)
+template <typename T>
+__global__ void panel_split_tf32_kernel(const PanelPiece* __restrict__ pieces, int np, const T* __restrict__ src,
+                                        float* __restrict__ dst) {
+    for (int b = blockIdx.x; b < np; b += gridDim.x) {
+        const PanelPiece pc = pieces[b];
+        const int rows = pc.rows, n = rows * pc.cols;
+        const bool unit = pc.scale == 1.0;
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int c = e / rows, r = e - c * rows;
+            const T x = src[pc.src_off + (int64_t)c * pc.src_ld + r];
+            split_store_tf32(dst + pc.dst_off + (int64_t)c * pc.dst_pitch, r, piece_value(x, unit, pc.scale));
+        }
+    }
+}
+
 // ===========================================================================
 // layout conversion, vector algebra
 // ===========================================================================
@@ -544,6 +593,20 @@ cudaError_t launch_panel_split(const PanelPiece* pieces, int np, const double* s
     if (np <= 0) return cudaSuccess;
     if (!pieces || !src || !dst) return cudaErrorInvalidValue;
     panel_split_kernel<double><<<min(np, 4096), 256, 0, st>>>(pieces, np, src, (__nv_bfloat16*)dst);
+    return cudaGetLastError();
+}
+cudaError_t launch_prep_tf32(const PrepBlock* pb, int nb, const double* src, void* dst, cudaStream_t st) {
+    if (nb <= 0) return cudaSuccess;
+    if (!pb || !src || !dst) return cudaErrorInvalidValue;
+    prep_tf32_kernel<<<min(nb, 8192), 256, 0, st>>>(pb, nb, src, (float*)dst);
+    return cudaGetLastError();
+}
+cudaError_t launch_panel_split_tf32(const PanelPiece* pieces, int np, const double* src, const float* srcf, void* dst,
+                                    cudaStream_t st) {
+    if (np <= 0) return cudaSuccess;
+    if (!pieces || (!src && !srcf) || !dst) return cudaErrorInvalidValue;
+    if (srcf) panel_split_tf32_kernel<float><<<min(np, 4096), 256, 0, st>>>(pieces, np, srcf, (float*)dst);
+    else panel_split_tf32_kernel<double><<<min(np, 4096), 256, 0, st>>>(pieces, np, src, (float*)dst);
     return cudaGetLastError();
 }
 cudaError_t launch_panel_split_f32(const PanelPiece* pieces, int np, const float* src, void* dst, cudaStream_t st) {

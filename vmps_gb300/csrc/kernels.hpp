@@ -47,11 +47,17 @@ cudaError_t launch_gg64(const GGArgs& a, cudaStream_t st);
 cudaError_t umma_init();
 // out_mode: 0 FP64 output, 1 bf16 [hi|lo] panel rows (split intermediates), 2 FP32 output
 // multi: tiles of a multi-RHS plan (interleaved right-hand sides)
-cudaError_t launch_gg_umma(int out_mode, bool multi, const GGArgs& a, const TmaMaps& maps, cudaStream_t st);
+// tf32: the operands are 3xTF32 panels (kind::tf32 MMAs, K steps of 16); single right-hand side
+cudaError_t launch_gg_umma(int out_mode, bool multi, const GGArgs& a, const TmaMaps& maps, cudaStream_t st,
+                           bool tf32 = false);
 // split operands: FP64 blocks -> bf16 [hi|lo] panels
 cudaError_t launch_prep(const PrepBlock* pb, int nb, const double* src, void* dst, cudaStream_t st);
 cudaError_t launch_panel_split(const PanelPiece* pieces, int np, const double* src, void* dst, cudaStream_t st);
 cudaError_t launch_panel_split_f32(const PanelPiece* pieces, int np, const float* src, void* dst, cudaStream_t st);
+// 3xTF32 operands: FP64 blocks (or FP64 / FP32 vector pieces) -> FP32 [16 hi | 16 lo] panels
+cudaError_t launch_prep_tf32(const PrepBlock* pb, int nb, const double* src, void* dst, cudaStream_t st);
+cudaError_t launch_panel_split_tf32(const PanelPiece* pieces, int np, const double* src, const float* srcf, void* dst,
+                                    cudaStream_t st);
 cudaError_t launch_pack(const PackBlock* blocks, int nb, const double* src, double* dst, int to_padded,
                         cudaStream_t st);
 int64_t dot_chunk(int64_t n);

@@ -258,17 +258,21 @@ static EncodeTiledFn encode_tiled() {
 // a 2-d tensor over the class matrix (2*kpad bf16 columns, its stacked rows) with
 // boxes of 64 columns (one 32-wide K step, hi and lo) x the key's rows, 128-byte
 // swizzle and zero fill below the last row.
-static void encode_panel_map(CUtensorMap* m, const PanelArena& ar, const DBuf& arena, const MapKey& k) {
+// (elt 2: bf16 panels, boxes of 64 elements; elt 4: 3xTF32 panels in FP32 storage, boxes of
+// 32 elements -- 128 bytes either way)
+static void encode_panel_map(CUtensorMap* m, const PanelArena& ar, const DBuf& arena, const MapKey& k, int elt) {
     if (k.cls < 0 || k.cls >= (int)ar.cls.size()) throw std::logic_error("TMA descriptor of an unknown panel class");
+    if (elt != 2 && elt != 4) throw std::logic_error("panel element must be 2 or 4 bytes");
     const PanelClass& c = ar.cls[k.cls];
     if (k.rows < 16 || k.rows > 256 || k.rows % 16 != 0) throw std::logic_error("TMA box rows out of range");
     if (c.base % 64 != 0 || c.kpad % 32 != 0) throw std::logic_error("panel class not 128-byte aligned");
     const cuuint64_t dims[2] = {(cuuint64_t)2 * c.kpad, (cuuint64_t)std::max<int64_t>(c.rows, 1)};
-    const cuuint64_t strides[1] = {(cuuint64_t)4 * c.kpad};
-    const cuuint32_t box[2] = {64, (cuuint32_t)k.rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)2 * c.kpad * elt};
+    const cuuint32_t box[2] = {(cuuint32_t)(128 / elt), (cuuint32_t)k.rows};
     const cuuint32_t estr[2] = {1, 1};
-    void* base = arena.as<uint16_t>() + c.base;
-    CUresult res = encode_tiled()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+    void* base = static_cast<unsigned char*>(arena.p) + (size_t)c.base * elt;
+    CUresult res = encode_tiled()(m, elt == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                  base, dims, strides, box, estr,
                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (res != CUDA_SUCCESS)
@@ -277,13 +281,13 @@ static void encode_panel_map(CUtensorMap* m, const PanelArena& ar, const DBuf& a
 }
 
 static std::unique_ptr<TmaMaps> build_phase_maps(const PhasePlan& ph, const PanelArena& A, const DBuf& Aarena,
-                                                 const PanelArena& B, const DBuf& Barena) {
+                                                 const PanelArena& B, const DBuf& Barena, int elt) {
     if ((int)ph.amaps.size() > kMaxMapsA || (int)ph.bmaps.size() > kMaxMapsB)
         throw std::logic_error("tcgen05 plan: too many TMA descriptors in one phase");
     auto m = std::make_unique<TmaMaps>();
     std::memset(m.get(), 0, sizeof(TmaMaps));
-    for (size_t i = 0; i < ph.amaps.size(); ++i) encode_panel_map(&m->a[i], A, Aarena, ph.amaps[i]);
-    for (size_t i = 0; i < ph.bmaps.size(); ++i) encode_panel_map(&m->b[i], B, Barena, ph.bmaps[i]);
+    for (size_t i = 0; i < ph.amaps.size(); ++i) encode_panel_map(&m->a[i], A, Aarena, ph.amaps[i], elt);
+    for (size_t i = 0; i < ph.bmaps.size(); ++i) encode_panel_map(&m->b[i], B, Barena, ph.bmaps[i], elt);
     return m;
 }
 
@@ -467,7 +471,8 @@ static void validate_tma_plan(const PhasePlan& ph, const std::vector<OpBlock>& A
 // the schedule: CTA tile ranges partition the tiles, every tile's steps lie in
 // the step list, TMA coordinates are 128-byte aligned and inside their panel
 // classes' columns, boxes cover the tiles, descriptors exist
-static void validate_tma_schedule(const PhasePlan& ph, const PanelArena& A, const PanelArena& B) {
+static void validate_tma_schedule(const PhasePlan& ph, const PanelArena& A, const PanelArena& B, int elt = 2) {
+    const int32_t box = 128 / elt;   // elements of one 128-byte TMA box row
     if (ph.tiles.empty()) return;
     if (ph.ncta <= 0 || (int)ph.cta_tiles.size() != ph.ncta + 1 || ph.cta_tiles.front() != 0 ||
         ph.cta_tiles.back() != (int32_t)ph.tiles.size())
@@ -490,7 +495,7 @@ static void validate_tma_schedule(const PhasePlan& ph, const PanelArena& A, cons
                 s.arows > kUmmaTileM || s.brows > kUmmaTileN)
                 throw std::logic_error("tcgen05 plan: TMA box does not cover its tile");
             const int32_t xb = s.x & ~1;   // bit 0 flags a padding second K16 slice
-            if (xb % 64 != 0 || xb < 0 || s.xa % 64 != 0 || s.xa < 0 || s.xa >= 2 * A.cls[ka.cls].kpad ||
+            if (xb % box != 0 || xb < 0 || s.xa % box != 0 || s.xa < 0 || s.xa >= 2 * A.cls[ka.cls].kpad ||
                 xb >= 2 * B.cls[kb.cls].kpad || s.ay < 0 || s.by < 0 || s.ay >= A.cls[ka.cls].rows ||
                 s.by >= B.cls[kb.cls].rows)
                 throw std::logic_error("tcgen05 plan: TMA coordinate outside its panel");
@@ -502,10 +507,10 @@ static void validate_tma_schedule(const PhasePlan& ph, const PanelArena& A, cons
 static void schedule_and_validate(Plan& p, int ncta) {
     validate_tma_plan(p.p1, p.opX, p.opY, true);
     validate_tma_plan(p.p2, p.opT, p.opZ, false);
-    schedule_tma(p.p1, ncta, p.opX, p.opY);
-    schedule_tma(p.p2, ncta, p.opT, p.opZ);
-    validate_tma_schedule(p.p1, p.ax, p.ay);
-    validate_tma_schedule(p.p2, p.at, p.az);
+    schedule_tma(p.p1, ncta, p.opX, p.opY, p.kstep);
+    schedule_tma(p.p2, ncta, p.opT, p.opZ, p.kstep);
+    validate_tma_schedule(p.p1, p.ax, p.ay, p.elt);
+    validate_tma_schedule(p.p2, p.at, p.az, p.elt);
 }
 
 // device buffers and work lists of a freshly made plan; Y is the FP64 layout
@@ -518,10 +523,11 @@ static void plan_to_device(DevPlan& dp, const DevLayout& Y, cudaStream_t st) {
         return;
     }
     // zero-filled: panel padding stays zero
-    dp.T.alloc((size_t)dp.plan.at.total * 2, st, true);
-    dp.X2.alloc((size_t)dp.plan.ax.total * 2, st, true);
-    dp.Z2.alloc((size_t)dp.plan.az.total * 2, st, true);
-    dp.Y2.alloc((size_t)dp.plan.ay.total * 2, st, true);
+    const size_t elt = (size_t)dp.plan.elt;
+    dp.T.alloc((size_t)dp.plan.at.total * elt, st, true);
+    dp.X2.alloc((size_t)dp.plan.ax.total * elt, st, true);
+    dp.Z2.alloc((size_t)dp.plan.az.total * elt, st, true);
+    dp.Y2.alloc((size_t)dp.plan.ay.total * elt, st, true);
     upload_vec(dp.prepX, dp.plan.prepX, st);
     upload_vec(dp.prepZ, dp.plan.prepZ, st);
     dp.nprepX = (int)dp.plan.prepX.size();
@@ -529,8 +535,8 @@ static void plan_to_device(DevPlan& dp, const DevLayout& Y, cudaStream_t st) {
     const auto yp = vector_panel_pieces(Y, dp.plan);
     upload_vec(dp.ypieces, yp, st);
     dp.nypieces = (int)yp.size();
-    dp.p1.maps = build_phase_maps(dp.plan.p1, dp.plan.ax, dp.X2, dp.plan.ay, dp.Y2);
-    dp.p2.maps = build_phase_maps(dp.plan.p2, dp.plan.at, dp.T, dp.plan.az, dp.Z2);
+    dp.p1.maps = build_phase_maps(dp.plan.p1, dp.plan.ax, dp.X2, dp.plan.ay, dp.Y2, dp.plan.elt);
+    dp.p2.maps = build_phase_maps(dp.plan.p2, dp.plan.at, dp.T, dp.plan.az, dp.Z2, dp.plan.elt);
     if (dp.plan.splitk > 1) {
         const size_t n = (size_t)dp.plan.splitk * (size_t)dp.plan.vstride;
         dp.part_d.alloc(n * 8, st, true);
@@ -541,6 +547,11 @@ static void plan_to_device(DevPlan& dp, const DevLayout& Y, cudaStream_t st) {
 // split plans: the bf16 panels of the X and scaled Z operands
 static void split_prepare(DevPlan& dp, const double* X, const double* Z, cudaStream_t st) {
     if (!dp.plan.split) return;
+    if (dp.plan.elt == 4) {
+        CK(launch_prep_tf32(dp.prepX.as<PrepBlock>(), dp.nprepX, X, dp.X2.p, st));
+        CK(launch_prep_tf32(dp.prepZ.as<PrepBlock>(), dp.nprepZ, Z, dp.Z2.p, st));
+        return;
+    }
     CK(launch_prep(dp.prepX.as<PrepBlock>(), dp.nprepX, X, dp.X2.p, st));
     CK(launch_prep(dp.prepZ.as<PrepBlock>(), dp.nprepZ, Z, dp.Z2.p, st));
 }
@@ -591,7 +602,8 @@ static void run_phase_on(const DevPlan& dp, int ph, const DevPhase& d, const Pha
     a.vstride = dp.plan.vstride;
     if (d.ntiles > 0 && (!a.A || !a.B || !a.C || !a.tiles || !a.steps || !a.cta_tiles || !d.maps))
         throw std::invalid_argument("grouped GEMM launched with an unallocated operand");
-    if (d.ntiles > 0) CK(launch_gg_umma(ph == 1 ? 1 : (ops.Of ? 2 : 0), dp.plan.nrhs > 1, a, *d.maps, st));
+    if (d.ntiles > 0)
+        CK(launch_gg_umma(ph == 1 ? 1 : (ops.Of ? 2 : 0), dp.plan.nrhs > 1, a, *d.maps, st, dp.plan.elt == 4));
 }
 
 static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream_t st) {
@@ -602,7 +614,10 @@ static void run_phase(const DevPlan& dp, int ph, const Operands& ops, cudaStream
 // one application of a planned contraction: (split plans) split Y, phase 1, phase 2
 static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
     if ((ops.Yf || ops.Of) && !dp.plan.split) throw std::invalid_argument("FP32 vectors need a split plan");
-    if (dp.plan.split) {
+    if (dp.plan.split && dp.plan.elt == 4) {
+        CK(launch_panel_split_tf32(dp.ypieces.as<PanelPiece>(), dp.nypieces, ops.Yf ? nullptr : ops.Y, ops.Yf, dp.Y2.p,
+                                   st));
+    } else if (dp.plan.split) {
         if (ops.Yf) CK(launch_panel_split_f32(dp.ypieces.as<PanelPiece>(), dp.nypieces, ops.Yf, dp.Y2.p, st));
         else CK(launch_panel_split(dp.ypieces.as<PanelPiece>(), dp.nypieces, ops.Y, dp.Y2.p, st));
     }
@@ -618,15 +633,15 @@ static void run_plan(const DevPlan& dp, const Operands& ops, cudaStream_t st) {
     }
 }
 
-// bf16 MMA work a split phase issues: 3 products of M=128 x N=round16(tn) x K per
-// step, K = 16 for steps whose second K16 slice is padding (skipped), else 32
-static double phase_tensor_flops(const PhasePlan& ph) {
+// tensor work a split phase issues: 3 products of M=128 x N=round16(tn) x K per
+// step, K = kstep/2 for steps whose second K slice is padding (skipped), else kstep
+static double phase_tensor_flops(const PhasePlan& ph, int kstep = kUmmaBK) {
     double f = 0;
     for (const GTile& t : ph.tiles) {
         double k = 0;
         for (int j = t.step0; j < t.step0 + t.nsteps && j < (int)ph.steps.size(); ++j)
-            k += (ph.steps[j].x & 1) ? 16 : kUmmaBK;
-        if (ph.steps.empty()) k = (double)t.nsteps * kUmmaBK;
+            k += (ph.steps[j].x & 1) ? kstep / 2 : kstep;
+        if (ph.steps.empty()) k = (double)t.nsteps * kstep;
         f += k * 3.0 * 2.0 * kUmmaTileM * ((t.tn + 15) / 16 * 16);
     }
     return f;
@@ -647,15 +662,15 @@ static void fill_stats(const ChainSet& cs, const Plan& p, int prec, vmps_plan_st
     s->flops_phase2 = p.p2.flops;
     s->flops_executed = p.p1.flops + p.p2.flops;
     s->bytes_algorithmic = p.bytes_alg;
-    s->bytes_intermediate = p.split ? 2.0 * (double)p.at.total : 8.0 * (double)p.T.total;
+    s->bytes_intermediate = p.split ? (double)p.elt * (double)p.at.total : 8.0 * (double)p.T.total;
     (void)prec;
     s->n_segments_phase2 = (int64_t)p.p2.segs.size();
     s->n_terms_phase2 = (int64_t)p.p2.terms.size();
     s->flops_phase2_unsummed = p.flops_p2_unsummed;
     s->association = p.association;
     if (p.split) {
-        s->tensor_flops_phase1 = phase_tensor_flops(p.p1);
-        s->tensor_flops_phase2 = phase_tensor_flops(p.p2);
+        s->tensor_flops_phase1 = phase_tensor_flops(p.p1, p.kstep);
+        s->tensor_flops_phase2 = phase_tensor_flops(p.p2, p.kstep);
     }
 }
 
@@ -669,7 +684,7 @@ struct vmps_pivot_s {
     BlockTable Lt, Rt, Vt;
     DevLayout Ld, Rd, Vd;
     ChainSet cs;
-    DevPlan plans[2];
+    DevPlan plans[3];   // by precision: FP64, BF16x3, 3xTF32
     DBuf dL, dR;
     DBuf dPack;                 // PackBlock[] of the vector layout
     int npack = 0;
@@ -678,9 +693,9 @@ struct vmps_pivot_s {
     DBuf vin, vout;             // padded vectors for host-buffer HxV
     DBuf part, scal;            // reduction scratch
     DBuf flag;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    const void* graph_in[2] = {nullptr, nullptr};
-    const void* graph_out[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    const void* graph_in[3] = {nullptr, nullptr, nullptr};
+    const void* graph_out[3] = {nullptr, nullptr, nullptr};
     std::map<int, std::unique_ptr<DevPlan>> multi;   // split plans for nrhs > 1 vectors, by nrhs
     DBuf mvin, mvout;                                // nrhs padded vectors for host-buffer multi-RHS HxV
     // excited-state projector (A0proj, Epenalty): projector vectors in the padded layout
@@ -720,11 +735,15 @@ static void make_chunks(vmps_pivot* p, DevPlan& dp);
 static SplitTiling pivot_tiling(vmps_pivot* p);
 
 static DevPlan& get_plan(vmps_pivot* p, int prec) {
-    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3 && prec != VMPS_PREC_TF32X3)
+        throw std::invalid_argument("unknown precision");
     DevPlan& dp = p->plans[prec];
     if (dp.ready) return dp;
     if (prec == VMPS_PREC_FP64) dp.plan = make_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 64, 64);
-    else {
+    else if (prec == VMPS_PREC_TF32X3) {
+        dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 1, SplitTiling(), true);
+        schedule_and_validate(dp.plan, p->ctx->num_sms);
+    } else {
         dp.plan = make_split_plan(p->cs, p->Ld, p->Vd, p->Rd, p->Vd, false, false, 1, pivot_tiling(p));
         schedule_and_validate(dp.plan, p->ctx->num_sms);
     }
@@ -835,16 +854,16 @@ static void make_chunks(vmps_pivot* p, DevPlan& dp) {
             sp.slotA = full.slotA; sp.slotB = full.slotB; sp.slotC = full.slotC;
             sp.tiles = std::move(per[c]);
             if (ph == 1) {
-                schedule_tma(sp, p->ctx->num_sms, dp.plan.opX, dp.plan.opY);
-                validate_tma_schedule(sp, dp.plan.ax, dp.plan.ay);
+                schedule_tma(sp, p->ctx->num_sms, dp.plan.opX, dp.plan.opY, dp.plan.kstep);
+                validate_tma_schedule(sp, dp.plan.ax, dp.plan.ay, dp.plan.elt);
             } else {
-                schedule_tma(sp, p->ctx->num_sms, dp.plan.opT, dp.plan.opZ);
-                validate_tma_schedule(sp, dp.plan.at, dp.plan.az);
+                schedule_tma(sp, p->ctx->num_sms, dp.plan.opT, dp.plan.opZ, dp.plan.kstep);
+                validate_tma_schedule(sp, dp.plan.at, dp.plan.az, dp.plan.elt);
             }
             ds.emplace_back();
             ds.back().upload(sp, p->st());
-            ds.back().maps = ph == 1 ? build_phase_maps(sp, dp.plan.ax, dp.X2, dp.plan.ay, dp.Y2)
-                                     : build_phase_maps(sp, dp.plan.at, dp.T, dp.plan.az, dp.Z2);
+            ds.back().maps = ph == 1 ? build_phase_maps(sp, dp.plan.ax, dp.X2, dp.plan.ay, dp.Y2, dp.plan.elt)
+                                     : build_phase_maps(sp, dp.plan.at, dp.T, dp.plan.az, dp.Z2, dp.plan.elt);
         }
     };
     cut(dp.plan.p1, 1, ch->p1h, ch->p1);
@@ -1419,7 +1438,7 @@ int vmps_pivot_set_penalty(vmps_pivot* p, int nproj, const double* A0, double Ep
         if (!std::isfinite(A0[i])) return set_err(VMPS_E_NONFINITE, "projector vector has NaN/Inf");
     // cached HxV graphs were captured without (or with another) projector
     for (auto& g : p->graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
-    p->graph_in[0] = p->graph_in[1] = p->graph_out[0] = p->graph_out[1] = nullptr;
+    for (int i = 0; i < 3; ++i) p->graph_in[i] = p->graph_out[i] = nullptr;
     p->pen = PenaltyArgs{};
     if (nproj == 0) return VMPS_OK;
     require_device(p->ctx);
@@ -1510,6 +1529,7 @@ int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int prec) {
 int vmps_hxv_multi(vmps_pivot* p, const double* vin, double* vout, int nrhs, int prec) {
     API_BEGIN
     if (!p || !vin || !vout || nrhs < 1) return set_err(VMPS_E_ARG, "bad argument");
+    if (prec == VMPS_PREC_TF32X3) return set_err(VMPS_E_UNSUPPORTED, "3xTF32 runs single-vector HxVs");
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
     if (p->pen.npen > 0 && nrhs > kPenMaxRhs)
         return set_err(VMPS_E_UNSUPPORTED, "a pivot with a projector takes at most 64 right-hand sides");
@@ -2075,7 +2095,8 @@ constexpr double kFp64FlopsPerMs = 0.87e9, kTensorFlopsPerMs = 5.3e11, kStepByte
 double est_ms_fp64_hxv(const Plan& p) { return (p.p1.flops + p.p2.flops) / kFp64FlopsPerMs + 2 * kLaunchMs; }
 // one split Lanczos iteration with a basis of j rows (FP32 vectors): HxV + step kernels
 double est_ms_split_step(const Plan& p, int64_t n, int j) {
-    const double tensor = phase_tensor_flops(p.p1) + phase_tensor_flops(p.p2);
+    // TF32 MMAs run at half the bf16 rate
+    const double tensor = (phase_tensor_flops(p.p1, p.kstep) + phase_tensor_flops(p.p2, p.kstep)) * (p.elt == 4 ? 2 : 1);
     const double bytes = 4.0 * (double)n * (2.0 * (j + 1) + 8.0);
     return tensor / kTensorFlopsPerMs + bytes / kStepBytesPerMs + 8 * kLaunchMs;
 }
@@ -2106,7 +2127,8 @@ extern "C" int vmps_lanczos_ground(vmps_pivot* p, double* v, int prec, int max_i
     if (!p || !v || !energy || max_iter <= 0 || refine_iters < 0) return set_err(VMPS_E_ARG, "bad argument");
     if (max_iter >= kLzMaxIter || refine_iters >= kLzMaxIter)
         return set_err(VMPS_E_ARG, "max_iter and refine_iters must be below " + std::to_string(kLzMaxIter));
-    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3 && prec != VMPS_PREC_TF32X3)
+        return set_err(VMPS_E_ARG, "unknown precision");
     require_device(p->ctx);
     std::lock_guard<std::mutex> lock(p->ctx->lz_mu);
     auto t0 = std::chrono::steady_clock::now();
@@ -2321,6 +2343,7 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
     API_BEGIN
     if (!p || !v0 || !mu || nrhs < 1 || nrhs > 65535 || nmom < 1) return set_err(VMPS_E_ARG, "bad argument");
     if (!(a > 0) || !std::isfinite(a) || !std::isfinite(b)) return set_err(VMPS_E_ARG, "scale a must be > 0");
+    if (prec == VMPS_PREC_TF32X3) return set_err(VMPS_E_UNSUPPORTED, "3xTF32 runs single-vector HxVs");
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
     if (p->pen.npen > 0 && nrhs > kPenMaxRhs)
         return set_err(VMPS_E_UNSUPPORTED, "a pivot with a projector takes at most 64 right-hand sides");
@@ -2527,6 +2550,7 @@ struct vmps_env_s {
 };
 
 static DevPlan& env_plan(vmps_env* e, int prec) {
+    if (prec == VMPS_PREC_TF32X3) throw std::invalid_argument("3xTF32 runs pivot HxVs only");
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) throw std::invalid_argument("unknown precision");
     DevPlan& dp = e->plans[prec];
     if (dp.ready) return dp;
@@ -2830,6 +2854,7 @@ int vmps_transfer_create(vmps_ctx* ctx, const vmps_symmetry* symd, int dir, int 
 int vmps_transfer_hxv(vmps_transfer* t, const double* vin, double* vout, int prec) {
     API_BEGIN
     if (!t || !vin || !vout) return set_err(VMPS_E_ARG, "null argument");
+    if (prec == VMPS_PREC_TF32X3) return set_err(VMPS_E_UNSUPPORTED, "3xTF32 runs pivot HxVs only");
     if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
     CK(cudaSetDevice(t->ctx->device));
     cudaStream_t st = t->st();

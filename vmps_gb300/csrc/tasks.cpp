@@ -821,7 +821,9 @@ int32_t box_rows_b(int32_t tn) {
     return std::min<int32_t>(256, (tn + 31) / 32 * 32);
 }
 
-void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B) {
+void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B,
+                  int kstep) {
+    if (kstep != 32 && kstep != 16) throw std::invalid_argument("K step of a split plan must be 32 or 16");
     const size_t nt = ph.tiles.size();
     ph.steps.clear();
     ph.amaps.clear();
@@ -836,7 +838,7 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const 
     for (size_t i = 0; i < nt; ++i) {
         const GTile& t = ph.tiles[i];
         int32_t n = 0;
-        for (int s = t.seg_begin; s < t.seg_end; ++s) n += (ph.segs[s].K + kUmmaBK - 1) / kUmmaBK;
+        for (int s = t.seg_begin; s < t.seg_end; ++s) n += (ph.segs[s].K + kstep - 1) / kstep;
         nsteps[i] = n;
         cost[i] = n + 1.0;
     }
@@ -878,12 +880,12 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const 
                 const OpBlock& oa = A[ph.seg_amap[s]];
                 const OpBlock& ob = B[ph.seg_bmap[s]];
                 const int32_t am = map_of(aidx, ph.amaps, oa.cls, ha), bm = map_of(bidx, ph.bmaps, ob.cls, hb);
-                for (int32_t k0 = 0; k0 < ph.segs[s].K; k0 += kUmmaBK) {
+                for (int32_t k0 = 0; k0 < ph.segs[s].K; k0 += kstep) {
                     TStep st{};
                     st.amap = am;
                     st.bmap = bm;
-                    // bit 0 of x: only the first 16 of the 32 K columns lie inside the segment
-                    st.x = 2 * k0 | (ph.segs[s].K - k0 <= 16 ? 1 : 0);
+                    // bit 0 of x: only the first half of the step's K columns lies inside the segment
+                    st.x = 2 * k0 | (ph.segs[s].K - k0 <= kstep / 2 ? 1 : 0);
                     st.xa = 2 * (ph.segs[s].akoff + k0);
                     st.ay = oa.row + t.row0;
                     st.by = ob.row + t.col0;
@@ -1148,15 +1150,18 @@ Plan make_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const
 // split-precision planner
 // ===========================================================================
 Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y, const DevLayout& Z,
-                     const DevLayout& O, bool transX, bool transZ, int nrhs, const SplitTiling& tiling) {
+                     const DevLayout& O, bool transX, bool transZ, int nrhs, const SplitTiling& tiling, bool tf32) {
     if (nrhs < 1) throw std::invalid_argument("nrhs must be at least 1");
     for (int cap : {tiling.ncap1, tiling.ncap2})
         if (cap < 32 || cap > kUmmaTileN || cap % 32 != 0)
             throw std::invalid_argument("tile N caps must be multiples of 32 up to 256");
     if (tiling.splitk < 1 || tiling.splitk > 8 || (tiling.splitk > 1 && nrhs > 1))
         throw std::invalid_argument("split-K of 1..8, single right-hand side only");
+    if (tf32 && nrhs > 1) throw std::invalid_argument("3xTF32 plans take one right-hand side");
     Plan P;
     P.splitk = tiling.splitk;
+    P.elt = tf32 ? 4 : 2;
+    P.kstep = tf32 ? 16 : kUmmaBK;
     P.split = true;
     P.association = 0;
     P.nrhs = nrhs;

@@ -40,6 +40,8 @@ constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;               // two (all of TMEM),
 // kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1),
 // both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22 (per tile), M >> 4 in bits 24-28
 constexpr uint32_t IDESC_BASE = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BM >> 4) << 24);
+// kind::tf32: the same with A and B TF32 (format 2 in bits 7-9 and 10-12)
+constexpr uint32_t IDESC_BASE_TF32 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BM >> 4) << 24);
 constexpr long long WAIT_BUDGET = 4000000000LL;           // clock cycles (~2 s) per barrier wait
 }  // namespace um
 
@@ -108,6 +110,19 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint6
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
+// TF32 operands (FP32 storage): K = 8 per instruction, 32 bytes along K like a bf16 K16 slice
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ float to_tf32_rna(float v) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
                  : "memory");
@@ -154,7 +169,9 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
 //     overlapping the next tile's main loop.  A split output (T panels) is
 //     staged through swizzled shared memory so that each panel row segment is
 //     one 256-byte store.
-template <int OUT_SPLIT, bool MULTI>
+// TF32: the operands are 3xTF32 panels (FP32 [16 hi | 16 lo] per 128-byte row segment, a K step
+// of 16), the MMAs kind::tf32 with K = 8; the shared-memory layout of a stage is the same bytes.
+template <int OUT_SPLIT, bool MULTI, bool TF32 = false>
 __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, const __grid_constant__ TmaMaps maps) {
     using namespace um;
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -253,7 +270,8 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
             GTile next{};
             if (t + 1 < t1) next = g.tiles[t + 1];
             const int nsteps = tile.nsteps;
-            const uint32_t idesc = IDESC_BASE | ((uint32_t)(((tile.tn + 15) & ~15) >> 3) << 17);   // N = round16(tn)
+            const uint32_t idesc = (TF32 ? IDESC_BASE_TF32 : IDESC_BASE) |
+                                   ((uint32_t)(((tile.tn + 15) & ~15) >> 3) << 17);   // N = round16(tn)
             const int buf = lt & 1, buse = lt >> 1;
             if (buse >= 1 && !mbar_wait(bar(2 * STAGES + 2 + buf), (uint32_t)((buse - 1) & 1), s_fail, wb)) break;
             tc_fence_after();
@@ -269,11 +287,17 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
                     if (kk >= nk16) break;
-                    // 16 bf16 = 32 bytes along K; the lo halves sit 64 bytes after the hi halves
+                    // 16 bf16 (or 8 tf32) = 32 bytes along K; the lo halves sit 64 bytes after the hi halves
                     const uint64_t hi = (uint64_t)(kk * 32) >> 4, lo = (uint64_t)(64 + kk * 32) >> 4;
-                    umma_bf16(dacc, a + lo, b + hi, idesc, (k | kk) != 0 ? 1u : 0u);
-                    umma_bf16(dacc, a + hi, b + lo, idesc, 1);
-                    umma_bf16(dacc, a + hi, b + hi, idesc, 1);
+                    if (TF32) {
+                        umma_tf32(dacc, a + lo, b + hi, idesc, (k | kk) != 0 ? 1u : 0u);
+                        umma_tf32(dacc, a + hi, b + lo, idesc, 1);
+                        umma_tf32(dacc, a + hi, b + hi, idesc, 1);
+                    } else {
+                        umma_bf16(dacc, a + lo, b + hi, idesc, (k | kk) != 0 ? 1u : 0u);
+                        umma_bf16(dacc, a + hi, b + lo, idesc, 1);
+                        umma_bf16(dacc, a + hi, b + hi, idesc, 1);
+                    }
                 }
                 umma_commit(bar(STAGES + st));
             }
@@ -321,7 +345,36 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                     if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
                 }
                 const int tn = ncols - c0 < 64 ? ncols - c0 : 64;   // columns of this chunk
-                if (OUT_SPLIT == 1) {
+                if (OUT_SPLIT == 1 && TF32) {
+                    // 3xTF32 T panel rows: columns col0+c0 .. +63 are four 16-wide K steps, the
+                    // 512-byte row segment [hi 0-15 | lo 0-15 | hi 16-31 | lo 16-31 | ...]; columns
+                    // past the tile inside a written step are zeros.  Each lane writes its own row.
+                    if (rl < tile.tm) {
+                        float* C = (float*)g.C;
+                        float* row = C + tile.c_off + (int64_t)(tile.row0 + rl) * tile.ldc +
+                                     (int64_t)((tile.col0 + c0) >> 4) * 32;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            // K steps past the tile are not written: they may lie beyond the
+                            // panel row (its padded width is the block's K rounded up to 32)
+                            if (q * 16 >= tn) break;
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                float h[4], l[4];
+#pragma unroll
+                                for (int i = 0; i < 4; ++i) {
+                                    const int j = q * 16 + u * 4 + i;
+                                    const float x = j < tn ? __uint_as_float(v[j]) : 0.f;
+                                    h[i] = to_tf32_rna(x);
+                                    l[i] = to_tf32_rna(x - h[i]);
+                                }
+                                *reinterpret_cast<float4*>(row + q * 32 + u * 4) = make_float4(h[0], h[1], h[2], h[3]);
+                                *reinterpret_cast<float4*>(row + q * 32 + 16 + u * 4) =
+                                    make_float4(l[0], l[1], l[2], l[3]);
+                            }
+                        }
+                    }
+                } else if (OUT_SPLIT == 1) {
                     // T panel rows: columns col0+c0 .. +63 are two 32-wide K steps, i.e. the
                     // 256-byte row segment [hi 0-31 | lo 0-31 | hi 32-63 | lo 32-63] (16-byte
                     // units u = 8q + 4h + g: K step q, half h, columns 8g..8g+7).  Columns past
@@ -408,16 +461,31 @@ cudaError_t umma_init() {
         return e;
     UMMA_ATTR(0, false) UMMA_ATTR(1, false) UMMA_ATTR(2, false) UMMA_ATTR(0, true) UMMA_ATTR(1, true)
 #undef UMMA_ATTR
+#define UMMA_ATTR_TF32(O)                                                                                   \
+    if ((e = cudaFuncSetAttribute(gg_umma_kernel<O, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                  um::SMEM_BYTES)) != cudaSuccess)                                          \
+        return e;
+    UMMA_ATTR_TF32(0) UMMA_ATTR_TF32(1) UMMA_ATTR_TF32(2)
+#undef UMMA_ATTR_TF32
     return cudaSuccess;
 }
 
 // multi: the plan's tiles interleave nrhs right-hand sides (separate instances, so
 // that the single-vector epilogues keep their register budget)
-cudaError_t launch_gg_umma(int out_mode, bool multi, const GGArgs& a, const TmaMaps& maps, cudaStream_t st) {
+cudaError_t launch_gg_umma(int out_mode, bool multi, const GGArgs& a, const TmaMaps& maps, cudaStream_t st,
+                           bool tf32) {
     if (a.ntiles <= 0) return cudaSuccess;
     if (!a.steps || !a.cta_tiles || a.ncta <= 0 || !a.C) return cudaErrorInvalidValue;
     if (out_mode == 1 && !a.transC) return cudaErrorInvalidValue;   // the staged epilogue writes panel rows
     if (multi && (out_mode == 2 || (out_mode == 0 && a.vstride <= 0))) return cudaErrorInvalidValue;
+    if (tf32) {
+        if (multi) return cudaErrorInvalidValue;   // 3xTF32 plans have one right-hand side
+        if (out_mode == 1) gg_umma_kernel<1, false, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+        else if (out_mode == 2) gg_umma_kernel<2, false, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+        else if (out_mode == 0) gg_umma_kernel<0, false, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+        else return cudaErrorInvalidValue;
+        return cudaGetLastError();
+    }
     if (out_mode == 1 && !multi) gg_umma_kernel<1, false><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
     else if (out_mode == 1) gg_umma_kernel<1, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
     else if (out_mode == 2) gg_umma_kernel<2, false><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);

@@ -22,7 +22,7 @@ import numpy as np
 from . import _native as N
 from .blocks import Blocks, MpoSite, Symmetry
 
-PREC = {"fp64": N.PREC_FP64, "bf16x3": N.PREC_BF16X3}
+PREC = {"fp64": N.PREC_FP64, "bf16x3": N.PREC_BF16X3, "tf32x3": N.PREC_TF32X3}
 
 
 def _prec(p):
