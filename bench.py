@@ -717,6 +717,18 @@ def main():
     hsp = H.apply(v0, args.precision)
     hxv_rel_err = float(np.linalg.norm(hsp - h64) / np.linalg.norm(h64))
 
+    # ---- the alternative split form (3xTF32): device-resident HxV and its error
+    tf32 = None
+    if args.precision == "bf16x3" and rank == 0:
+        time_hxv(H, vin, vout, "tf32x3", n_iter=3, use_graph=True)
+        mst, mst2 = time_hxv(H, vin, vout, "tf32x3", n_iter=args.steps, use_graph=True)
+        htf = H.apply(v0, "tf32x3")
+        st_tf = H.stats("tf32x3")
+        tf32 = {"ms_per_hxv": mst, "hxv_per_s": 1000.0 / mst, "phase2_ms": mst2,
+                "rel_err_vs_fp64": float(np.linalg.norm(htf - h64) / np.linalg.norm(h64)),
+                "bf16x3_rel_err_vs_fp64": hxv_rel_err, "over_bf16x3_time": mst / ms,
+                "tensor_flops_phase2": st_tf["tensor_flops_phase2"]}
+
     energy = None
     if not args.no_energy and rank == 0:
         # Lanczos ground state of this pivot from the same start vector: a tight
@@ -726,11 +738,13 @@ def main():
         e_ref, _, s_ref = H.lanczos(v0, "fp64", max_iter=300, tol_eigval=1e-14, tol_state=1e-9)
         e64, x64, s64 = H.lanczos(v0, "fp64", max_iter=300, tol_eigval=1e-10, tol_state=1e-6)
         es, xs, ss = H.lanczos(v0, args.precision, max_iter=300, tol_eigval=1e-10, tol_state=1e-6, refine_iters=10)
+        et, _, stt = H.lanczos(v0, "tf32x3", max_iter=300, tol_eigval=1e-10, tol_state=1e-6, refine_iters=10)
         energy = {"E_ref_fp64": e_ref, "tolerances": {"tol_eigval": 1e-10, "tol_state": 1e-6, "refine_iters": 10},
                   "fp64": dict({k: s64[k] for k in keys}, rel_err=abs(e64 - e_ref) / abs(e_ref)),
                   "split": dict({k: ss[k] for k in keys}, rel_err=abs(es - e_ref) / abs(e_ref),
                                 energy_first_rel_err=abs(ss["energy_first"] - e_ref) / abs(e_ref)),
-                  "split_speedup": s64["ms_total"] / ss["ms_total"]}
+                  "split_speedup": s64["ms_total"] / ss["ms_total"],
+                  "tf32x3": dict({k: stt[k] for k in keys}, rel_err=abs(et - e_ref) / abs(e_ref))}
         if not args.no_cpu and world == 1:
             energy["oracle"] = oracle_check(Lenv, Renv, V, W1, W2, v0, h64, hsp, e_ref, e64, es, x64, xs)
 
@@ -800,6 +814,7 @@ def main():
                      "phase2_ms": ms64_2, "flops_executed": st64["flops_executed"]},
             "split_over_fp64": ms64 / ms,
             "hxv_split_rel_err_vs_fp64": hxv_rel_err,
+            "tf32x3": tf32,
             "energy": energy,
             "plan": {k: st_split[k] for k in ("n_tasks", "n_chains", "n_intermediates", "n_out_blocks",
                                               "n_tiles_phase1", "n_tiles_phase2", "flops_reference",
