@@ -300,6 +300,14 @@ int vmps_lanczos_ground(vmps_pivot* p, double* v, int precision, int max_iter,
 int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* sym, const vmps_blocks* A1, const double* a1,
                            const vmps_blocks* A2, const double* a2, const vmps_blocks* V, double* v,
                            int64_t nprod, const int64_t* prods);
+/* General grouped block products: C[k] = sum over the given (k, i, j) triples of
+ * coef[q] * A[i] * B[j] (coef NULL: all 1), one FP64 grouped GEMM on the device;
+ * C's blocks without a product are zero.  Used for the subspace-expansion term of
+ * RICH_SVD (Mps::enrich_left / enrich_right, Mps.h:3181-3600): alpha * w * L_a * A
+ * and alpha * w * A * R_b, each into its column (row) range of the expansion block. */
+int vmps_block_products(vmps_ctx* ctx, const vmps_symmetry* sym, const vmps_blocks* A, const double* a,
+                        const vmps_blocks* B, const double* b, const vmps_blocks* C, double* c,
+                        int64_t nprod, const int64_t* prods, const double* coef);
 /* The same with the products found here: for every A1 block (s1, qin, qmid) and A2
  * block (s3, qmid, qout), the V block (s13_of_pair[s1 * n3 + s3], qin, qout) if V has
  * it (abelian QNs: each pair of local states is one combined state).            */

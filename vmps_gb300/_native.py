@@ -132,6 +132,9 @@ _PROTOS = [
     ("vmps_two_site_contract", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
                                          C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks), f64p, C.c_int64,
                                          i64p]),
+    ("vmps_block_products", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
+                                      C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks), f64p, C.c_int64, i64p,
+                                      f64p]),
     ("vmps_two_site_contract_pairs", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,
                                                C.POINTER(vmps_blocks), f64p, C.POINTER(vmps_blocks), f64p, C.c_int,
                                                C.c_int, i32p]),

@@ -263,7 +263,7 @@ Plan make_split_plan(const ChainSet& cs, const DevLayout& X, const DevLayout& Y,
 // output block, one segment per product; output blocks without a product are
 // written with zeros.
 PhasePlan make_product_plan(const DevLayout& A, const DevLayout& B, const DevLayout& C,
-                            const std::vector<std::array<int64_t, 3>>& prods);
+                            const std::vector<std::array<int64_t, 3>>& prods, const double* coef = nullptr);
 // Static schedule of a split phase for the persistent tcgen05 engine on ncta
 // CTAs: K steps of kUmmaBK per segment with their TMA boxes, tiles assigned
 // longest-first to the least-loaded CTA and stored CTA by CTA.

@@ -2435,13 +2435,13 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
 // V[k] = sum of A1[i] A2[j] over the (k, i, j) products, one FP64 grouped GEMM
 static void two_site_contract(vmps_ctx* ctx, const BlockTable& t1, const double* a1, const BlockTable& t2,
                               const double* a2, const BlockTable& tv, double* v,
-                              const std::vector<std::array<int64_t, 3>>& pr) {
+                              const std::vector<std::array<int64_t, 3>>& pr, const double* coef = nullptr) {
     const DevLayout d1 = make_dev_layout(t1.rows, t1.cols), d2 = make_dev_layout(t2.rows, t2.cols),
                     dv = make_dev_layout(tv.rows, tv.cols);
     for (const auto& t : pr)
         if (t[0] < 0 || t[0] >= tv.n || t[1] < 0 || t[1] >= t1.n || t[2] < 0 || t[2] >= t2.n)
             throw std::invalid_argument("product index outside its block table");
-    PhasePlan ph = make_product_plan(d1, d2, dv, pr);
+    PhasePlan ph = make_product_plan(d1, d2, dv, pr, coef);
     cudaStream_t st = ctx->stream;
     // device buffers kept in the context between calls (a sweep makes one call per bond)
     if (!ctx->two_site) ctx->two_site.reset(new TwoSiteScratch());
@@ -2484,6 +2484,26 @@ extern "C" int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* symd, 
     std::vector<std::array<int64_t, 3>> pr((size_t)nprod);
     for (int64_t q = 0; q < nprod; ++q) pr[q] = {prods[3 * q], prods[3 * q + 1], prods[3 * q + 2]};
     two_site_contract(ctx, t1, a1, t2, a2, tv, v, pr);
+    API_END
+}
+
+// C[k] = sum over the products q = (k, i, j) of coef[q] * A[i] * B[j] (coef NULL: 1),
+// one FP64 grouped-GEMM launch; C blocks without a product come back zero
+extern "C" int vmps_block_products(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* A, const double* a,
+                                   const vmps_blocks* B, const double* b, const vmps_blocks* Ct, double* c,
+                                   int64_t nprod, const int64_t* prods, const double* coef) {
+    API_BEGIN
+    if (!ctx || !a || !b || !c || nprod < 0 || (nprod > 0 && !prods)) return set_err(VMPS_E_ARG, "bad argument");
+    require_device(ctx);
+    const Symmetry sym = make_sym(symd);
+    const BlockTable t1 = parse_blocks(sym, A, false), t2 = parse_blocks(sym, B, false),
+                     tc = parse_blocks(sym, Ct, false);
+    std::vector<std::array<int64_t, 3>> pr((size_t)nprod);
+    for (int64_t q = 0; q < nprod; ++q) {
+        pr[q] = {prods[3 * q], prods[3 * q + 1], prods[3 * q + 2]};
+        if (coef && !std::isfinite(coef[q])) return set_err(VMPS_E_NONFINITE, "product coefficient is not finite");
+    }
+    two_site_contract(ctx, t1, a, t2, b, tc, c, pr, coef);
     API_END
 }
 

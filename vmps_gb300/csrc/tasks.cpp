@@ -903,7 +903,7 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const 
 }
 
 PhasePlan make_product_plan(const DevLayout& A, const DevLayout& B, const DevLayout& C,
-                            const std::vector<std::array<int64_t, 3>>& prods) {
+                            const std::vector<std::array<int64_t, 3>>& prods, const double* coef) {
     PhasePlan ph;
     ph.transA = false; ph.transB = false; ph.transC = false;
     std::vector<std::vector<size_t>> by_out(C.rows.size());
@@ -924,7 +924,7 @@ PhasePlan make_product_plan(const DevLayout& A, const DevLayout& B, const DevLay
             s.b_off = B.off[j];
             s.term_begin = (int32_t)ph.terms.size();
             s.term_count = 1;
-            ph.terms.push_back(GTerm{A.off[i], 1.0});
+            ph.terms.push_back(GTerm{A.off[i], coef ? coef[q] : 1.0});
             s.lda = (int32_t)A.ld[i];
             s.ldb = (int32_t)B.ld[j];
             s.K = (int32_t)A.cols[i];

@@ -75,18 +75,27 @@ def _push_left(A_prev, Lfac):
 
 
 def dmrg1(ctx, model, mps, n_sweeps=2, precision="fp64", max_iter=100, tol_eigval=1e-12, tol_state=1e-8,
-          refine_iters=0, verbose=False, pool=None, probe=True):
+          refine_iters=0, verbose=False, pool=None, probe=True, enrich=0.0, enrich_decay=0.5, Dmax=None):
     """Run n_sweeps full sweeps of single-site DMRG; returns energies and timings.
     `mps` must be right-canonical with the gauge centre on site 0.  The QR / LQ gauge
     steps run on the host cores (`pool`, a hostla.SectorPool; one is made if none is
     given).  The result's `steps` lists every local solve: its energy and its HxV
-    counts per precision.  probe=False makes split-precision solves skip the FP64 probe."""
+    counts per precision.  probe=False makes split-precision solves skip the FP64 probe.
+
+    enrich > 0 turns on the subspace expansion of DMRG::BROOM::RICH_SVD (abelian
+    symmetries; enrich.py): after each local solve the bond about to be crossed is
+    enlarged by alpha * L A W (moving right) or alpha * A W R (moving left) and truncated
+    back to at most Dmax states (default: the largest bond dimension of the MPS), with
+    alpha = enrich * enrich_decay**sweep.  Bond bases then change during the sweep."""
+    if enrich > 0 and model.sym.nonabelian:
+        raise ValueError("the subspace expansion is implemented for abelian symmetries")
     with _probe_setting(probe):
         return _dmrg1(ctx, model, mps, n_sweeps, precision, max_iter, tol_eigval, tol_state, refine_iters, verbose,
-                      pool)
+                      pool, enrich, enrich_decay, Dmax)
 
 
-def _dmrg1(ctx, model, mps, n_sweeps, precision, max_iter, tol_eigval, tol_state, refine_iters, verbose, pool):
+def _dmrg1(ctx, model, mps, n_sweeps, precision, max_iter, tol_eigval, tol_state, refine_iters, verbose, pool,
+           enrich=0.0, enrich_decay=0.5, Dmax=None):
     sym, L = model.sym, model.L
     nq = sym.nq
     own_pool = pool is None
@@ -106,9 +115,13 @@ def _dmrg1(ctx, model, mps, n_sweeps, precision, max_iter, tol_eigval, tol_state
     energies, sweep_times, timers, solves, hxv, steps = [], [], [], [], 0, []
     E = None
     clock = time.perf_counter
+    if enrich > 0:
+        from .enrich import enrich_left, enrich_right
+        Dmax = Dmax if Dmax is not None else max(mps.bond_dim(b) for b in range(L + 1))
     for sweep in range(n_sweeps):
         ts = clock()
         tm = dict(lanczos=0.0, precalc=0.0, gauge=0.0, lr=0.0)
+        alpha = enrich * enrich_decay ** sweep
         counts = {}
         order = list(range(L)) + list(range(L - 1, -1, -1))
         for step, l in enumerate(order):
@@ -128,13 +141,19 @@ def _dmrg1(ctx, model, mps, n_sweeps, precision, max_iter, tol_eigval, tol_state
             tm["lanczos"] += t2 - t1
             mps.A[l].data[:] = v
             if right and l < L - 1:
-                gauge_step(mps.A[l], mps.A[l + 1], nq, "right", sym=mps.sym, pool=pool)
+                if alpha > 0:
+                    enrich_right(ctx, model, mps, l, envL[l], alpha, Dmax, pool=pool)
+                else:
+                    gauge_step(mps.A[l], mps.A[l + 1], nq, "right", sym=mps.sym, pool=pool)
                 t3 = clock()
                 e = EnvUpdate(ctx, sym, "L", envL[l], mps.A[l], model.W[l], mps.A[l])
                 envL[l + 1] = e.run(envL[l], mps.A[l], mps.A[l])
                 e.close()
             elif not right and l > 0:
-                gauge_step(mps.A[l], mps.A[l - 1], nq, "left", sym=mps.sym, pool=pool)
+                if alpha > 0:
+                    enrich_left(ctx, model, mps, l, envR[l + 1], alpha, Dmax, pool=pool)
+                else:
+                    gauge_step(mps.A[l], mps.A[l - 1], nq, "left", sym=mps.sym, pool=pool)
                 t3 = clock()
                 e = EnvUpdate(ctx, sym, "R", envR[l + 1], mps.A[l], model.W[l], mps.A[l])
                 envR[l] = e.run(envR[l + 1], mps.A[l], mps.A[l])
