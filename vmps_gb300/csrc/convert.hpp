@@ -1,9 +1,11 @@
 // Floating-point conversions built from integer operations.
 //
 // GB300's FP64 rate is a small fraction of its FP32 rate, and the double <->
-// float conversion instructions run at that rate.  The data-movement kernels
-// (vector split, epilogues) convert every element, so they use these exact
-// IEEE-754 conversions instead:
+// float conversion instructions run at that rate.  The kernels that narrow
+// every element of a vector (vector split, operand preparation) use these exact
+// IEEE-754 conversions instead; measured on the tcgen05 engine's FP64-output
+// epilogue the hardware widening (float -> double, exact) was faster than
+// f32_to_f64, so that epilogue uses the cast:
 //   f64_to_f32_rn : round to nearest, ties to even (the rounding of a C cast),
 //                   overflow to +-inf, results in the float subnormal range
 //                   rounded the same way, NaN -> the canonical quiet NaN;

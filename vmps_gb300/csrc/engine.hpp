@@ -269,9 +269,10 @@ PhasePlan make_product_plan(const DevLayout& A, const DevLayout& B, const DevLay
 // longest-first to the least-loaded CTA and stored CTA by CTA.
 void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B,
                   int kstep = kUmmaBK);
-// TMA box heights: A boxes 16/32/64/128 rows, B boxes a multiple of 32 up to
-// 256 (16 for the narrowest), the smallest that covers the tile
-int32_t box_rows_a(int32_t tm);
-int32_t box_rows_b(int32_t tn);
+// TMA box heights, the smallest that covers the tile: fine = the tile's rows
+// (columns) rounded up to 16; coarse (fewer descriptors) = A boxes of 16/32/64/128
+// rows, B boxes a multiple of 32 up to 256 (16 for the narrowest)
+int32_t box_rows_a(int32_t tm, bool fine = true);
+int32_t box_rows_b(int32_t tn, bool fine = true);
 
 }  // namespace vmps

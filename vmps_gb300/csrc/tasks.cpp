@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <set>
 #include <numeric>
 #include <queue>
 #include <unordered_set>
@@ -810,15 +811,16 @@ int32_t panel_kpad(int64_t K) {
     return (int32_t)((K + q - 1) / q * q);
 }
 
-int32_t box_rows_a(int32_t tm) {
+int32_t box_rows_a(int32_t tm, bool fine) {
+    if (fine) return std::min<int32_t>(128, std::max<int32_t>(16, (tm + 15) / 16 * 16));
     for (int32_t h : {16, 32, 64, 128})
         if (tm <= h) return h;
     return 128;
 }
 
-int32_t box_rows_b(int32_t tn) {
+int32_t box_rows_b(int32_t tn, bool fine) {
     if (tn <= 16) return 16;
-    return std::min<int32_t>(256, (tn + 31) / 32 * 32);
+    return std::min<int32_t>(256, fine ? (tn + 15) / 16 * 16 : (tn + 31) / 32 * 32);
 }
 
 void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const std::vector<OpBlock>& B,
@@ -867,6 +869,20 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const 
         idx.emplace(std::make_pair(cls, rows), i);
         return i;
     };
+    // box heights: the tile's extent rounded to 16 rows (fewer bytes through TMA) unless
+    // that needs more descriptors than a launch takes
+    bool fine = true;
+    {
+        std::set<std::pair<int32_t, int32_t>> ka, kb;
+        for (size_t i = 0; i < nt; ++i) {
+            const GTile& t = ph.tiles[i];
+            for (int s = t.seg_begin; s < t.seg_end; ++s) {
+                ka.insert({A[ph.seg_amap[s]].cls, box_rows_a(t.tm)});
+                kb.insert({B[ph.seg_bmap[s]].cls, box_rows_b(t.tn)});
+            }
+        }
+        fine = (int)ka.size() <= kMaxMapsA && (int)kb.size() <= kMaxMapsB;
+    }
     std::vector<GTile> tiles;
     tiles.reserve(nt);
     ph.cta_tiles.assign(ncta + 1, 0);
@@ -875,7 +891,7 @@ void schedule_tma(PhasePlan& ph, int ncta, const std::vector<OpBlock>& A, const 
             GTile t = ph.tiles[i];
             t.step0 = (int32_t)ph.steps.size();
             t.nsteps = nsteps[i];
-            const int32_t ha = box_rows_a(t.tm), hb = box_rows_b(t.tn);
+            const int32_t ha = box_rows_a(t.tm, fine), hb = box_rows_b(t.tn, fine);
             for (int s = t.seg_begin; s < t.seg_end; ++s) {
                 const OpBlock& oa = A[ph.seg_amap[s]];
                 const OpBlock& ob = B[ph.seg_bmap[s]];

@@ -27,7 +27,11 @@
 namespace vmps {
 namespace um {
 constexpr int BM = kUmmaTileM, BN = kUmmaTileN, BK = kUmmaBK, STAGES = 4;   // 128 x (<= 256) x 32
-constexpr int NT = 192;                                    // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+// warp 0 TMA, warp 1 MMA, then the epilogue warps: four for split (panel) outputs, whose
+// staging takes 8 KB of shared memory per warp, eight (two per tensor-memory lane quadrant,
+// alternate 64-column chunks) for FP32 / FP64 outputs
+constexpr int epi_warps(int out_split) { return out_split == 1 ? 4 : 8; }
+constexpr int nt_of(int out_split) { return 64 + 32 * epi_warps(out_split); }
 constexpr int ROW_BYTES = 128;                             // one K step of one row: 32 hi + 32 lo
 constexpr int A_BYTES = BM * ROW_BYTES;                    // A region: 16 KB
 constexpr int B_BYTES = BN * ROW_BYTES;                    // B region, at most: 32 KB
@@ -148,6 +152,18 @@ __device__ __forceinline__ void reg_fence16(uint32_t* r) {
                    "+r"(r[15]));
 }
 
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
+}
+// one 32-byte step record through the read-only path
+__device__ __forceinline__ TStep load_step(const TStep* p) {
+    const int4 a = __ldg(reinterpret_cast<const int4*>(p));
+    const int4 b = __ldg(reinterpret_cast<const int4*>(p) + 1);
+    TStep s;
+    s.amap = a.x; s.bmap = a.y; s.x = a.z; s.ay = a.w;
+    s.by = b.x; s.arows = b.y; s.brows = b.z; s.xa = b.w;
+    return s;
+}
 __device__ __forceinline__ void tmap_prefetch(const void* tmap) {
     asm volatile("prefetch.tensormap [%0];\n" ::"l"(tmap) : "memory");
 }
@@ -159,21 +175,24 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
 // Persistent, warp-specialised grouped GEMM on panel operands.  CTA b runs
 // tiles[cta_tiles[b] .. cta_tiles[b+1]) (a host-side longest-first schedule),
 // whose K steps are steps[tiles[.].step0 ...], contiguous per CTA.
-//   warp 0: keeps two windows of 32 step records in registers (one per lane,
-//     loaded one window ahead); lane 0 issues per step one TMA box of A and one
-//     of B into a 4-deep ring of stages ("full" barriers count the bytes);
+//   warp 0, lane 0: per step one TMA box of A and one of B into a 4-deep ring of
+//     stages ("full" barriers count the bytes), the step records read through L1
+//     and prefetched ahead;
 //   warp 1 (one lane): per step 2 x (lo*hi, hi*lo, hi*hi) tcgen05.mma into one
 //     of two TMEM accumulators, commit to the stage's "empty" barrier, and at
 //     the end of a tile to the accumulator's "full" barrier;
-//   warps 2-5: epilogue of their 32 accumulator lanes in 64-column chunks,
+//   warps 2..: epilogue of their 32 accumulator lanes in 64-column chunks,
 //     overlapping the next tile's main loop.  A split output (T panels) is
 //     staged through swizzled shared memory so that each panel row segment is
-//     one 256-byte store.
+//     one 256-byte store (four warps); FP32 / FP64 outputs have two warps per
+//     lane quadrant, taking alternate chunks (eight warps).
 // TF32: the operands are 3xTF32 panels (FP32 [16 hi | 16 lo] per 128-byte row segment, a K step
 // of 16), the MMAs kind::tf32 with K = 8; the shared-memory layout of a stage is the same bytes.
 template <int OUT_SPLIT, bool MULTI, bool TF32 = false>
-__global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, const __grid_constant__ TmaMaps maps) {
+__global__ void __launch_bounds__(um::nt_of(OUT_SPLIT), 1)
+    gg_umma_kernel(const GGArgs g, const __grid_constant__ TmaMaps maps) {
     using namespace um;
+    constexpr int EPI = epi_warps(OUT_SPLIT);
     extern __shared__ __align__(1024) unsigned char smraw[];
     const uint32_t raw = su32(smraw);
     const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
@@ -184,17 +203,13 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
     // [2S+4] drain of the MMAs issued
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
     volatile int* s_fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    // per stage: 1 when only the first K16 slice of its 32-wide K step lies inside
-    // the segment (written by the producer before the stage's expect-tx arrive,
-    // read by the MMA thread after the stage's full barrier)
-    volatile int* s_half = reinterpret_cast<volatile int*>(tmem_slot + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     auto bar = [&](int i) { return su32(&bars[i]); };
 
     if (tid == 0) {
         *s_fail = 0;
         for (int s = 0; s < STAGES; ++s) { mbar_init(bar(s), 1); mbar_init(bar(STAGES + s), 1); }
-        for (int b = 0; b < 2; ++b) { mbar_init(bar(2 * STAGES + b), 1); mbar_init(bar(2 * STAGES + 2 + b), 4); }
+        for (int b = 0; b < 2; ++b) { mbar_init(bar(2 * STAGES + b), 1); mbar_init(bar(2 * STAGES + 2 + b), EPI); }
         mbar_init(bar(2 * STAGES + 4), 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
@@ -211,56 +226,33 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
     const long long wb = g.wait_budget > 0 ? g.wait_budget : WAIT_BUDGET;
 
     if (warp == 0) {
-        // ---------------- TMA producer
+        // ---------------- TMA producer: one lane walks the CTA's K steps; their records
+        // come through L1, each 128-byte line prefetched 16 steps ahead
         for (int i = lane; i < kMaxMapsA; i += 32) tmap_prefetch(&maps.a[i]);
         for (int i = lane; i < kMaxMapsB; i += 32) tmap_prefetch(&maps.b[i]);
-        int S0 = 0, S1 = 0;
-        if (t0 < t1) {
-            S0 = g.tiles[t0].step0;
-            S1 = g.tiles[t1 - 1].step0 + g.tiles[t1 - 1].nsteps;
-        }
-        auto load_rec = [&](int idx) {
-            TStep r{};
-            if (idx < S1) r = g.steps[idx];
-            return r;
-        };
-        TStep cur = load_rec(S0 + lane), nxt = load_rec(S0 + 32 + lane);
-        int B = S0;   // cur holds steps [B, B+32), nxt [B+32, B+64)
-        int it = 0;
-        for (int j = S0; j < S1; ++j, ++it) {
-            if (j == B + 32) {
-                cur = nxt;
-                B += 32;
-                nxt = load_rec(B + 32 + lane);
+        if (lane == 0) {
+            int S0 = 0, S1 = 0;
+            if (t0 < t1) {
+                S0 = g.tiles[t0].step0;
+                S1 = g.tiles[t1 - 1].step0 + g.tiles[t1 - 1].nsteps;
             }
-            const int src = j - B;   // < 32
-            const int amap = __shfl_sync(0xffffffffu, cur.amap, src);
-            const int bmap = __shfl_sync(0xffffffffu, cur.bmap, src);
-            const int xf = __shfl_sync(0xffffffffu, cur.x, src);
-            const int x = xf & ~1;   // bit 0: the step's second K16 slice is padding
-            const int xa = __shfl_sync(0xffffffffu, cur.xa, src);
-            const int ay = __shfl_sync(0xffffffffu, cur.ay, src);
-            const int by = __shfl_sync(0xffffffffu, cur.by, src);
-            const int rows = __shfl_sync(0xffffffffu, cur.arows + cur.brows, src);
-            int go = 1;
-            if (lane == 0) {
+            for (int j = S0 & ~3; j < S0 + 16 && j < S1; j += 4) prefetch_l1(g.steps + j);
+            int it = 0;
+            for (int j = S0; j < S1; ++j, ++it) {
+                if (((j + 16) & 3) == 0 && j + 16 < S1) prefetch_l1(g.steps + j + 16);
+                const TStep r = load_step(g.steps + j);
                 const int st = it % STAGES, use = it / STAGES;
-                if (*s_fail || (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), s_fail, wb))) {
-                    go = 0;
-                } else {
-                    const uint32_t sb = ring + st * STAGE_BYTES;
-                    s_half[st] = xf & 1;
-                    mbar_expect_tx(bar(st), (uint32_t)(rows * ROW_BYTES));
-                    tma_load_2d(sb, &maps.a[amap], xa, ay, bar(st));
-                    tma_load_2d(sb + A_BYTES, &maps.b[bmap], x, by, bar(st));
-                }
+                if (use >= 1 && !mbar_wait(bar(STAGES + st), (uint32_t)((use - 1) & 1), s_fail, wb)) break;
+                const uint32_t sb = ring + st * STAGE_BYTES;
+                mbar_expect_tx(bar(st), (uint32_t)((r.arows + r.brows) * ROW_BYTES));
+                tma_load_2d(sb, &maps.a[r.amap], r.xa, r.ay, bar(st));
+                // bit 0 of x flags a step whose second K16 slice is padding
+                tma_load_2d(sb + A_BYTES, &maps.b[r.bmap], r.x & ~1, r.by, bar(st));
             }
-            if (!__shfl_sync(0xffffffffu, go, 0)) break;
-        }
-        // copies still in flight land before the CTA exits (a no-op when the MMA warp consumed them)
-        if (lane == 0)
+            // copies still in flight land before the CTA exits (a no-op when the MMA warp consumed them)
             for (int i = it - 1; i >= 0 && i >= it - STAGES; --i)
                 mbar_drain(bar(i % STAGES), (uint32_t)((i / STAGES) & 1), s_fail);
+        }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer (the next tile's record is fetched one tile ahead)
         int it = 0, lt = 0;
@@ -283,7 +275,7 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                 const uint32_t sb = ring + st * STAGE_BYTES;
                 const uint64_t a = sw128_desc(sb), b = sw128_desc(sb + A_BYTES);
                 // a padding half (zeros in A and B) adds nothing: its three MMAs are skipped
-                const int nk16 = s_half[st] ? 1 : BK / 16;
+                const int nk16 = (__ldg(&g.steps[tile.step0 + k].x) & 1) ? 1 : BK / 16;
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
                     if (kk >= nk16) break;
@@ -310,7 +302,9 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
         // ---------------- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
         const int sp = warp & 3;
         const int rl = sp * 32 + lane;   // tile row of this lane
-        unsigned char* so = stage_out + (warp - 2) * 8192;   // this warp's staging: 32 rows x 256 B
+        // chunks c0 = cfirst, cfirst + cstride, ... of every tile are this warp's
+        const int cfirst = EPI == 8 ? ((warp - 2) >> 2) * 64 : 0, cstride = EPI == 8 ? 128 : 64;
+        unsigned char* so = stage_out + (warp - 2) * 8192;   // this warp's staging: 32 rows x 256 B (split output)
         int lt = 0;
         for (int t = t0; t < t1; ++t, ++lt) {
             const GTile tile = g.tiles[t];
@@ -320,8 +314,15 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
             if (!ok) break;
             tc_fence_after();
             const int ncols = tile.tn;
+            if (cfirst >= ncols) {
+                // no chunk of this tile for this warp: its share of the accumulator is free
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
+                continue;
+            }
 #pragma unroll 1
-            for (int c0 = 0; c0 < ncols; c0 += 64) {
+            for (int c0 = cfirst; c0 < ncols; c0 += cstride) {
                 uint32_t v[64];
                 if (tile.nsteps > 0) {
                     const uint32_t ta = tmem + ((uint32_t)(sp * 32) << 16) + (uint32_t)(buf * ACC_COLS + c0);
@@ -338,8 +339,8 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
 #pragma unroll
                     for (int i = 0; i < 64; ++i) v[i] = 0u;
                 }
-                if (c0 + 64 >= ncols) {
-                    // the accumulator is free once its last columns sit in registers
+                if (c0 + cstride >= ncols) {
+                    // the accumulator is free once this warp's last columns sit in registers
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(bar(2 * STAGES + 2 + buf));
@@ -432,14 +433,14 @@ __global__ void __launch_bounds__(um::NT, 1) gg_umma_kernel(const GGArgs g, cons
                             base += (gr - i * tile.nrhs) * g.vstride;
                             gr = i;
                         }
-                        const int col0 = tile.col0 + c0;
+                        // element (gr, gc) at base + gr * rs + gc * cs
+                        const int64_t rs = g.transC ? tile.ldc : 1, cs = g.transC ? 1 : tile.ldc;
+                        const int64_t e0 = base + gr * rs + (int64_t)(tile.col0 + c0) * cs;
 #pragma unroll
                         for (int j = 0; j < 64; ++j) {
                             if (j < tn) {
-                                const int64_t gc = col0 + j;
-                                const int64_t e = base + (g.transC ? (gc + gr * tile.ldc) : (gr + gc * tile.ldc));
-                                if (OUT_SPLIT == 2) ((float*)g.C)[e] = __uint_as_float(v[j]);
-                                else ((double*)g.C)[e] = f32_to_f64(__uint_as_float(v[j]));
+                                if (OUT_SPLIT == 2) ((float*)g.C)[e0 + j * cs] = __uint_as_float(v[j]);
+                                else ((double*)g.C)[e0 + j * cs] = (double)__uint_as_float(v[j]);   // exact widening
                             }
                         }
                     }
@@ -480,17 +481,17 @@ cudaError_t launch_gg_umma(int out_mode, bool multi, const GGArgs& a, const TmaM
     if (multi && (out_mode == 2 || (out_mode == 0 && a.vstride <= 0))) return cudaErrorInvalidValue;
     if (tf32) {
         if (multi) return cudaErrorInvalidValue;   // 3xTF32 plans have one right-hand side
-        if (out_mode == 1) gg_umma_kernel<1, false, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-        else if (out_mode == 2) gg_umma_kernel<2, false, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-        else if (out_mode == 0) gg_umma_kernel<0, false, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+        if (out_mode == 1) gg_umma_kernel<1, false, true><<<a.ncta, um::nt_of(out_mode), um::SMEM_BYTES, st>>>(a, maps);
+        else if (out_mode == 2) gg_umma_kernel<2, false, true><<<a.ncta, um::nt_of(out_mode), um::SMEM_BYTES, st>>>(a, maps);
+        else if (out_mode == 0) gg_umma_kernel<0, false, true><<<a.ncta, um::nt_of(out_mode), um::SMEM_BYTES, st>>>(a, maps);
         else return cudaErrorInvalidValue;
         return cudaGetLastError();
     }
-    if (out_mode == 1 && !multi) gg_umma_kernel<1, false><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-    else if (out_mode == 1) gg_umma_kernel<1, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-    else if (out_mode == 2) gg_umma_kernel<2, false><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-    else if (out_mode == 0 && !multi) gg_umma_kernel<0, false><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
-    else if (out_mode == 0) gg_umma_kernel<0, true><<<a.ncta, um::NT, um::SMEM_BYTES, st>>>(a, maps);
+    if (out_mode == 1 && !multi) gg_umma_kernel<1, false><<<a.ncta, um::nt_of(out_mode), um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 1) gg_umma_kernel<1, true><<<a.ncta, um::nt_of(out_mode), um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 2) gg_umma_kernel<2, false><<<a.ncta, um::nt_of(out_mode), um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 0 && !multi) gg_umma_kernel<0, false><<<a.ncta, um::nt_of(out_mode), um::SMEM_BYTES, st>>>(a, maps);
+    else if (out_mode == 0) gg_umma_kernel<0, true><<<a.ncta, um::nt_of(out_mode), um::SMEM_BYTES, st>>>(a, maps);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }

@@ -127,6 +127,9 @@ def enrich_right(ctx, model, mps, l, Lenv, alpha, Dmax, pool=None):
     vac = sym.vacuum()
     comb = {"n": len(qloc), "index": {(s1, 0): [(tuple(q1), s1)] for s1, q1 in enumerate(qloc)}}
     A1, A2, disc, dmid = split_two_site(V, comb, qloc, [vac], din, dout, nq, Dmax, move="right", pool=pool, ctx=ctx)
+    # the split renormalises the kept singular values; truncateSVD does not (Biped.h:744-932),
+    # so S V^T gets back its scale and the state is unchanged when nothing is discarded
+    A2.data *= float(np.linalg.norm(V.data)) * np.sqrt(max(0.0, 1.0 - disc))
     # S V^T into site l+1 (only its columns of the old states meet A[l+1]); site l+1 gets
     # the full layout over the new bond basis (zero blocks for sectors the expansion added)
     SV = {tuple(A2.qin[i]): A2.block(i) for i in range(A2.n)}
@@ -214,6 +217,7 @@ def enrich_left(ctx, model, mps, l, Renv, alpha, Dmax, pool=None):
     vac = sym.vacuum()
     comb = {"n": len(qloc), "index": {(0, s3): [(tuple(q3), s3)] for s3, q3 in enumerate(qloc)}}
     A1, A2, disc, dmid = split_two_site(V, comb, [vac], qloc, din, dout, nq, Dmax, move="left", pool=pool, ctx=ctx)
+    A1.data *= float(np.linalg.norm(V.data)) * np.sqrt(max(0.0, 1.0 - disc))   # U S at its own scale
     # U S into site l-1 (only its rows of the old states meet A[l-1]), over the full layout
     US = {tuple(A1.qout[i]): A1.block(i) for i in range(A1.n)}
     Pv = mps.A[l - 1]
