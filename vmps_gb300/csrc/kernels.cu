@@ -241,9 +241,6 @@ __device__ __forceinline__ void piece_load4(const double* p, double (&x)[4]) {
     const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
     x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y;
 }
-__device__ __forceinline__ uint32_t bf16_pair(__nv_bfloat16 a, __nv_bfloat16 b) {
-    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
-}
 template <typename T>
 __global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np, const T* __restrict__ src,
                                    __nv_bfloat16* __restrict__ dst) {
@@ -268,16 +265,21 @@ __global__ void panel_split_kernel(const PanelPiece* __restrict__ pieces, int np
             }
             __nv_bfloat16* row = d + (int64_t)c * pc.dst_pitch;
             if (vstore && r0 + 4 <= rows) {
-                __nv_bfloat16 h[4], l[4];
+                // hi = bf16(v), lo = bf16(v - hi), two elements per conversion
+                uint32_t h[2], l[2];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const float v = piece_value(x[q], unit, pc.scale);
-                    h[q] = __float2bfloat16_rn(v);
-                    l[q] = __float2bfloat16_rn(v - __bfloat162float(h[q]));
+                for (int q = 0; q < 2; ++q) {
+                    const float v0 = piece_value(x[2 * q], unit, pc.scale);
+                    const float v1 = piece_value(x[2 * q + 1], unit, pc.scale);
+                    const __nv_bfloat162 hv = __floats2bfloat162_rn(v0, v1);
+                    const float2 hf = __bfloat1622float2(hv);
+                    const __nv_bfloat162 lv = __floats2bfloat162_rn(v0 - hf.x, v1 - hf.y);
+                    h[q] = *reinterpret_cast<const uint32_t*>(&hv);
+                    l[q] = *reinterpret_cast<const uint32_t*>(&lv);
                 }
                 const int p = panel_pos(r0);   // r0 % 4 == 0: the four stay in one 32-group
-                *reinterpret_cast<uint2*>(row + p) = make_uint2(bf16_pair(h[0], h[1]), bf16_pair(h[2], h[3]));
-                *reinterpret_cast<uint2*>(row + p + 32) = make_uint2(bf16_pair(l[0], l[1]), bf16_pair(l[2], l[3]));
+                *reinterpret_cast<uint2*>(row + p) = make_uint2(h[0], h[1]);
+                *reinterpret_cast<uint2*>(row + p + 32) = make_uint2(l[0], l[1]);
             } else {
 #pragma unroll
                 for (int q = 0; q < 4; ++q)

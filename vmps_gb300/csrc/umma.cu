@@ -167,10 +167,6 @@ __device__ __forceinline__ TStep load_step(const TStep* p) {
 __device__ __forceinline__ void tmap_prefetch(const void* tmap) {
     asm volatile("prefetch.tensormap [%0];\n" ::"l"(tmap) : "memory");
 }
-__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
-    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(a)) |
-           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(b)) << 16);
-}
 
 // Persistent, warp-specialised grouped GEMM on panel operands.  CTA b runs
 // tiles[cta_tiles[b] .. cta_tiles[b+1]) (a host-side longest-first schedule),
@@ -388,10 +384,12 @@ __global__ void __launch_bounds__(um::nt_of(OUT_SPLIT), 1)
                             const int j = cg * 8 + 2 * i;
                             const float a = j < tn ? __uint_as_float(v[j]) : 0.f;
                             const float b = j + 1 < tn ? __uint_as_float(v[j + 1]) : 0.f;
-                            const float ha = __bfloat162float(__float2bfloat16_rn(a));
-                            const float hb = __bfloat162float(__float2bfloat16_rn(b));
-                            h[i] = pack_bf16x2(a, b);
-                            l[i] = pack_bf16x2(a - ha, b - hb);
+                            // hi = bf16(x), lo = bf16(x - hi), two elements per conversion
+                            const __nv_bfloat162 hv = __floats2bfloat162_rn(a, b);
+                            const float2 hf = __bfloat1622float2(hv);
+                            const __nv_bfloat162 lv = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+                            h[i] = *reinterpret_cast<const uint32_t*>(&hv);
+                            l[i] = *reinterpret_cast<const uint32_t*>(&lv);
                         }
                         const int q = cg >> 2, gq = cg & 3;
                         const int uh = q * 8 + gq, ul = q * 8 + 4 + gq;
