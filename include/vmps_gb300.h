@@ -405,6 +405,17 @@ typedef struct {
 } vmps_cheb_stats;
 int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs, int nmom, double a, double b,
                            int precision, double* mu, vmps_cheb_stats* stats);
+/* The same with moments per part: the layout of V is cut at block boundaries
+ * part_blocks[0] = 0 < part_blocks[1] < ... < part_blocks[nparts] = number of V blocks
+ * (nparts <= 8) and mu (nrhs x nparts x nmom) holds the moments of each part of each
+ * vector.  On a union pivot whose parts are sectors of different quantum numbers
+ * (each part closed under H; see vmps_gb300/union.py), part j of vector k is a start
+ * vector of its own: one grouped launch per step advances nrhs x nparts vectors with
+ * different block layouts (C5: c_k|0> for both spin projections at once).  The
+ * reference runs one polyIter chain per start vector (DmrgLinearAlgebra.h:550-566). */
+int vmps_chebyshev_moments_parts(vmps_pivot* p, const double* v0, int nrhs, int nmom, double a, double b,
+                                 int precision, int nparts, const int64_t* part_blocks, double* mu,
+                                 vmps_cheb_stats* stats);
 
 /* ---- environment updates (contract_L / contract_R, FULL mode) -----------------
  * Step 1 builds the task list and the output Tripod layout; the caller reads the

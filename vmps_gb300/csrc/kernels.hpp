@@ -124,17 +124,22 @@ cudaError_t launch_lz_mdot(const void* K, int fp32, int64_t ld, int m, int64_t n
 cudaError_t launch_lz_to_f32(const double* x, float* y, int64_t n, cudaStream_t st);
 
 // ---- Chebyshev recursion over many right-hand sides (lanczos.cu) -------------------
+constexpr int kChebMaxParts = 8;
 struct ChebArgs {
     const double* w;      // H t_n, nrhs vectors at stride vs
     const double* tn;     // t_n
     const double* tprev;  // t_{n-1} (read from step 1 on; zero before)
     double* tnext;        // t_{n+1}
-    double* part;         // per-chunk partial sums [nrhs][2][nchunk]
-    double* mu;           // moments [nrhs][nmom]
+    double* part;         // per-chunk partial sums [nrhs][nparts][2][nchunk]
+    double* mu;           // moments [nrhs][nparts][nmom]
     unsigned* ctl;        // [0] step n, [1] block counter (zero on entry)
     int64_t n, vs;        // vector length (padded layout), stride between vectors
     int nrhs, nmom, nchunk;
     double inv_a, b;      // the recursion runs on (H - b) / a
+    // moments per part: part j of every vector is elements [pbeg[j], pbeg[j+1]) (nparts 1:
+    // the whole vector); nchunk covers the longest part
+    int nparts;
+    int64_t pbeg[kChebMaxParts + 1];
 };
 cudaError_t launch_cheb_step(const ChebArgs& a, int per_thread, cudaStream_t st);
 

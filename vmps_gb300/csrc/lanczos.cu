@@ -397,25 +397,27 @@ __global__ void lz_to_f32_kernel(const double* __restrict__ x, float* __restrict
 }
 
 // One step of the Chebyshev recursion for nrhs vectors at once (grid: chunks x
-// right-hand sides).  Step n makes t_{n+1} = c_a (H t_n - b t_n) - c_p t_{n-1}
+// right-hand sides x parts).  Step n makes t_{n+1} = c_a (H t_n - b t_n) - c_p t_{n-1}
 // with (c_a, c_p) = (1/a, 0) for n = 0 and (2/a, 1) after, and accumulates in
 // FP64 the two inner products of the moment doubling relations
 //   mu_{2n} = 2 <t_n, t_n> - mu_0,  mu_{2n+1} = 2 <t_{n+1}, t_n> - mu_1
-// (mu_0 = <t_0, t_0>, mu_1 = <t_1, t_0> at n = 0).  The last block to finish
-// writes the moments and advances n.
+// (mu_0 = <t_0, t_0>, mu_1 = <t_1, t_0> at n = 0), per part of the vector (the
+// element ranges of different start vectors sharing one layout).  The last block
+// to finish writes the moments and advances n.
 template <int E>
 __global__ void __launch_bounds__(kLzThreads) cheb_step_kernel(ChebArgs a) {
     const int step = (int)a.ctl[0];
     const double ca = step == 0 ? a.inv_a : 2.0 * a.inv_a, cp = step == 0 ? 0.0 : 1.0;
-    const int k = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k = blockIdx.y, pj = blockIdx.z, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t base = (int64_t)k * a.vs;
-    const int64_t e0 = (int64_t)blockIdx.x * (E * kLzThreads) + threadIdx.x;
+    const int64_t pe = a.pbeg[pj + 1];
+    const int64_t e0 = a.pbeg[pj] + (int64_t)blockIdx.x * (E * kLzThreads) + threadIdx.x;
     __shared__ double red[2][kLzWarps];
     double s0 = 0, s1 = 0;
 #pragma unroll
     for (int u = 0; u < E; ++u) {
         const int64_t e = e0 + u * kLzThreads;
-        if (e < a.n) {
+        if (e < pe) {
             const double x = a.tn[base + e];
             const double v = fma(ca, fma(-a.b, x, a.w[base + e]), -cp * a.tprev[base + e]);
             a.tnext[base + e] = v;
@@ -430,17 +432,17 @@ __global__ void __launch_bounds__(kLzThreads) cheb_step_kernel(ChebArgs a) {
     if (threadIdx.x < 2) {
         double t = 0;
         for (int q = 0; q < kLzWarps; ++q) t += red[threadIdx.x][q];
-        a.part[((int64_t)k * 2 + threadIdx.x) * a.nchunk + blockIdx.x] = t;
+        a.part[(((int64_t)k * a.nparts + pj) * 2 + threadIdx.x) * a.nchunk + blockIdx.x] = t;
     }
-    // last block of the whole grid (both dimensions)
+    // last block of the whole grid
     __shared__ bool last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(a.ctl + 1, 1u) == gridDim.x * gridDim.y - 1;
+    if (threadIdx.x == 0) last = atomicAdd(a.ctl + 1, 1u) == gridDim.x * gridDim.y * gridDim.z - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
-    for (int r = warp; r < a.nrhs; r += kLzWarps) {
+    for (int r = warp; r < a.nrhs * a.nparts; r += kLzWarps) {
         const double d0 = lz_row_sum(a.part, 2 * r, a.nchunk, lane);
         const double d1 = lz_row_sum(a.part, 2 * r + 1, a.nchunk, lane);
         if (lane == 0) {
@@ -544,10 +546,13 @@ cudaError_t launch_lz_to_f32(const double* x, float* y, int64_t n, cudaStream_t 
 
 cudaError_t launch_cheb_step(const ChebArgs& a, int per_thread, cudaStream_t st) {
     if (a.nrhs < 1 || a.nrhs > 65535 || a.n <= 0 || a.nchunk < 1 || a.nmom < 1 || !a.w || !a.tn || !a.tprev ||
-        !a.tnext || !a.part || !a.mu || !a.ctl)
+        !a.tnext || !a.part || !a.mu || !a.ctl || a.nparts < 1 || a.nparts > kChebMaxParts)
         return cudaErrorInvalidValue;
-    if ((int64_t)a.nchunk * per_thread * kLzThreads < a.n || a.vs < a.n) return cudaErrorInvalidValue;
-    const dim3 grid(a.nchunk, a.nrhs);
+    if (a.vs < a.n || a.pbeg[0] != 0 || a.pbeg[a.nparts] != a.n) return cudaErrorInvalidValue;
+    for (int j = 0; j < a.nparts; ++j)
+        if (a.pbeg[j + 1] <= a.pbeg[j] || (int64_t)a.nchunk * per_thread * kLzThreads < a.pbeg[j + 1] - a.pbeg[j])
+            return cudaErrorInvalidValue;
+    const dim3 grid(a.nchunk, a.nrhs, a.nparts);
 #define LZ_CALL(EE) cheb_step_kernel<EE><<<grid, kLzThreads, 0, st>>>(a);
     switch (per_thread) {
         case 1: LZ_CALL(1); break;

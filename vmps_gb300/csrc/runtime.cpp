@@ -2338,27 +2338,46 @@ extern "C" int vmps_spectral_bounds(vmps_pivot* p, const double* v, int iters, d
 // right-hand sides (split precision: one grouped multi-RHS launch pair; FP64:
 // the plain HxV per vector) and cheb_step_kernel (update and FP64 moments).
 // The three vector buffers rotate, so three graphs cover every step.
-extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs, int nmom, double a, double b,
-                                      int prec, double* mu, vmps_cheb_stats* stats) {
+// the moments of nrhs start vectors, per part (block ranges [part_blocks[j], part_blocks[j+1])
+// of the vector layout; nparts 1 with part_blocks null: the whole vector)
+static int chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs, int nmom, double a, double b, int prec,
+                             int nparts, const int64_t* part_blocks, double* mu, vmps_cheb_stats* stats) {
     API_BEGIN
     if (!p || !v0 || !mu || nrhs < 1 || nrhs > 65535 || nmom < 1) return set_err(VMPS_E_ARG, "bad argument");
+    if (nparts < 1 || nparts > kChebMaxParts || (nparts > 1 && !part_blocks))
+        return set_err(VMPS_E_ARG, "parts: 1 to 8 block ranges");
+    int64_t pbeg[kChebMaxParts + 1];
+    {
+        const int64_t nb = p->Vt.n;
+        for (int j = 0; j <= nparts; ++j) {
+            const int64_t bj = part_blocks ? part_blocks[j] : (j == 0 ? 0 : nb);
+            if (bj < 0 || bj > nb || (j == 0 && bj != 0) || (j == nparts && bj != nb) ||
+                (j > 0 && bj <= (part_blocks ? part_blocks[j - 1] : 0)))
+                return set_err(VMPS_E_ARG, "part boundaries must rise from block 0 to the last block");
+            pbeg[j] = j == nparts ? p->Vd.total : p->Vd.off[bj];
+        }
+    }
     if (!(a > 0) || !std::isfinite(a) || !std::isfinite(b)) return set_err(VMPS_E_ARG, "scale a must be > 0");
-    if (prec == VMPS_PREC_TF32X3) return set_err(VMPS_E_UNSUPPORTED, "3xTF32 runs single-vector HxVs");
-    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "unknown precision");
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3 && prec != VMPS_PREC_TF32X3)
+        return set_err(VMPS_E_ARG, "unknown precision");
     if (p->pen.npen > 0 && nrhs > kPenMaxRhs)
         return set_err(VMPS_E_UNSUPPORTED, "a pivot with a projector takes at most 64 right-hand sides");
     require_device(p->ctx);
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t st = p->st();
-    DevPlan& dp = prec == VMPS_PREC_BF16X3 ? get_multi_plan(p, nrhs) : get_plan(p, VMPS_PREC_FP64);
+    // BF16x3: one grouped launch pair for all right-hand sides; FP64 and 3xTF32: the
+    // single-vector plan once per right-hand side
+    DevPlan& dp = prec == VMPS_PREC_BF16X3 ? get_multi_plan(p, nrhs) : get_plan(p, prec);
     const int64_t dim = p->Vt.total, n = p->Vd.total;
     const size_t vbytes = (size_t)nrhs * n * 8;
     DBuf B[3], Wb, part, mud, ctl;
     for (DBuf& x : B) x.alloc(vbytes, st, true);
     Wb.alloc(vbytes, st, true);
-    const LzShape sh = lz_shape(n, p->ctx->num_sms);
-    part.alloc((size_t)nrhs * 2 * sh.nchunk * 8, st, false);
-    mud.alloc((size_t)nrhs * nmom * 8, st, true);
+    int64_t longest = 0;
+    for (int j = 0; j < nparts; ++j) longest = std::max(longest, pbeg[j + 1] - pbeg[j]);
+    const LzShape sh = lz_shape(longest, p->ctx->num_sms);
+    part.alloc((size_t)nrhs * nparts * 2 * sh.nchunk * 8, st, false);
+    mud.alloc((size_t)nrhs * nparts * nmom * 8, st, true);
     ctl.alloc(64, st, true);
     ensure_staging(p);
     for (int k = 0; k < nrhs; ++k)
@@ -2385,6 +2404,8 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
         c.nchunk = sh.nchunk;
         c.inv_a = 1.0 / a;
         c.b = b;
+        c.nparts = nparts;
+        for (int j = 0; j <= nparts; ++j) c.pbeg[j] = pbeg[j];
         Operands ops = pivot_ops(p);
         cudaGraph_t gr = nullptr;
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -2414,7 +2435,7 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
     CK(cudaEventRecord(p->ctx->ev0, st));
     for (int i = 0; i < steps; ++i) CK(cudaGraphLaunch(g[i % 3], st));
     CK(cudaEventRecord(p->ctx->ev1, st));
-    CK(cudaMemcpyAsync(mu, mud.p, (size_t)nrhs * nmom * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(mu, mud.p, (size_t)nrhs * nparts * nmom * 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     check_device_error(p->ctx);
     float ms = 0;
@@ -2427,6 +2448,17 @@ extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs,
         stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     API_END
+}
+
+extern "C" int vmps_chebyshev_moments(vmps_pivot* p, const double* v0, int nrhs, int nmom, double a, double b,
+                                      int prec, double* mu, vmps_cheb_stats* stats) {
+    return chebyshev_moments(p, v0, nrhs, nmom, a, b, prec, 1, nullptr, mu, stats);
+}
+
+extern "C" int vmps_chebyshev_moments_parts(vmps_pivot* p, const double* v0, int nrhs, int nmom, double a, double b,
+                                            int prec, int nparts, const int64_t* part_blocks, double* mu,
+                                            vmps_cheb_stats* stats) {
+    return chebyshev_moments(p, v0, nrhs, nmom, a, b, prec, nparts, part_blocks, mu, stats);
 }
 
 // contract_AA2 (tensors/DmrgContractions.h:1870-1927, abelian): the two-site

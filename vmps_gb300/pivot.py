@@ -113,17 +113,27 @@ class _Pivot:
         N.check(N.lib().vmps_spectral_bounds(self._h, v.ctypes.data_as(N.f64p), iters, C.byref(lo), C.byref(hi)))
         return lo.value, hi.value
 
-    def chebyshev_moments(self, v0: np.ndarray, nmom: int, a: float, b: float, precision="fp64"):
+    def chebyshev_moments(self, v0: np.ndarray, nmom: int, a: float, b: float, precision="fp64", parts=None):
         """Moments mu[k, n] = <v0_k| T_n((H - b)/a) |v0_k> of the rows of v0 (nrhs x dim),
-        advanced together on the device; returns (mu, stats)."""
+        advanced together on the device; returns (mu, stats).  parts: block-index
+        boundaries [0, b1, ..., nblocks] of the vector layout (a union pivot's sectors);
+        mu is then nrhs x nparts x nmom, the moments of each part of each row."""
         v0 = np.ascontiguousarray(np.atleast_2d(v0), dtype=np.float64)
         if v0.shape[1] != self.dim:
             raise ValueError(f"vectors have {v0.shape[1]} elements, layout needs {self.dim}")
-        mu = np.empty((v0.shape[0], nmom))
         st = N.vmps_cheb_stats()
-        N.check(N.lib().vmps_chebyshev_moments(self._h, v0.ctypes.data_as(N.f64p), v0.shape[0], nmom, float(a),
-                                               float(b), _prec(precision), mu.ctypes.data_as(N.f64p),
-                                               C.byref(st)))
+        if parts is None:
+            mu = np.empty((v0.shape[0], nmom))
+            N.check(N.lib().vmps_chebyshev_moments(self._h, v0.ctypes.data_as(N.f64p), v0.shape[0], nmom, float(a),
+                                                   float(b), _prec(precision), mu.ctypes.data_as(N.f64p),
+                                                   C.byref(st)))
+        else:
+            pb = np.ascontiguousarray(parts, dtype=np.int64)
+            mu = np.empty((v0.shape[0], len(pb) - 1, nmom))
+            N.check(N.lib().vmps_chebyshev_moments_parts(self._h, v0.ctypes.data_as(N.f64p), v0.shape[0], nmom,
+                                                         float(a), float(b), _prec(precision), len(pb) - 1,
+                                                         pb.ctypes.data_as(N.i64p), mu.ctypes.data_as(N.f64p),
+                                                         C.byref(st)))
         return mu, st.as_dict()
 
     def autotune(self, trials=5) -> dict:
