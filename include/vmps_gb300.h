@@ -305,6 +305,13 @@ int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* sym, const vmps_b
  * C's blocks without a product are zero.  Used for the subspace-expansion term of
  * RICH_SVD (Mps::enrich_left / enrich_right, Mps.h:3181-3600): alpha * w * L_a * A
  * and alpha * w * A * R_b, each into its column (row) range of the expansion block. */
+/* 6j symbols {j1 j2 j3; j4 j5 j6} for n argument sets, each given as the multiplet
+ * dimensions q = 2j + 1 (q[6*i .. 6*i+5]); zero where a triangle rule fails.  The Racah
+ * formula the task builder folds into its SU(2) prefactors (the reference takes
+ * coupling_6j for SU2::coeff_6j, symmetry/SU2.h:378-386); callers use it for host-side
+ * recoupling, e.g. the SU(2) two-site contraction and split (contract_AA2 /
+ * split_AA2, tensors/DmrgContractions.h:1870-1927, 2461-2631).  Host only.     */
+int vmps_su2_coupling_6j(int64_t n, const int32_t* q, double* out);
 int vmps_block_products(vmps_ctx* ctx, const vmps_symmetry* sym, const vmps_blocks* A, const double* a,
                         const vmps_blocks* B, const double* b, const vmps_blocks* C, double* c,
                         int64_t nprod, const int64_t* prods, const double* coef);

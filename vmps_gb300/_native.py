@@ -152,6 +152,7 @@ _PROTOS = [
     ("vmps_spectral_bounds", C.c_int, [C.c_void_p, f64p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("vmps_chebyshev_moments", C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, f64p,
                                          C.POINTER(vmps_cheb_stats)]),
+    ("vmps_su2_coupling_6j", C.c_int, [C.c_int64, i32p, f64p]),
     ("vmps_chebyshev_moments_parts", C.c_int, [C.c_void_p, f64p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
                                               C.c_int, i64p, f64p, C.POINTER(vmps_cheb_stats)]),
     ("vmps_dvec_create", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),

@@ -2521,6 +2521,19 @@ extern "C" int vmps_two_site_contract(vmps_ctx* ctx, const vmps_symmetry* symd, 
 
 // C[k] = sum over the products q = (k, i, j) of coef[q] * A[i] * B[j] (coef NULL: 1),
 // one FP64 grouped-GEMM launch; C blocks without a product come back zero
+// 6j symbols for host-side SU(2) recoupling, arguments as multiplet dimensions q = 2j + 1
+extern "C" int vmps_su2_coupling_6j(int64_t n, const int32_t* q, double* out) {
+    API_BEGIN
+    if (n < 0 || (n > 0 && (!q || !out))) return set_err(VMPS_E_ARG, "bad argument");
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t* a = q + 6 * i;
+        for (int j = 0; j < 6; ++j)
+            if (a[j] < 1) return set_err(VMPS_E_ARG, "multiplet dimensions must be >= 1");
+        out[i] = coupling_6j(a[0] - 1, a[1] - 1, a[2] - 1, a[3] - 1, a[4] - 1, a[5] - 1);
+    }
+    API_END
+}
+
 extern "C" int vmps_block_products(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_blocks* A, const double* a,
                                    const vmps_blocks* B, const double* b, const vmps_blocks* Ct, double* c,
                                    int64_t nprod, const int64_t* prods, const double* coef) {

@@ -28,6 +28,7 @@ import numpy as np
 
 from .mps import contract_two_sites, gauge_step, split_two_site
 from .pivot import EnvUpdate, PivotMatrix1, PivotMatrix2, left_vacuum, right_target
+from .su2 import contract_two_sites_su2, split_two_site_su2
 
 
 class SweepResult(dict):
@@ -190,7 +191,9 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
     ground state of PivotMatrix2(L[l], R[l+2], W[l], W[l+1]); split_AA2 with a truncated SVD
     (at most Dmax states over all sectors of the middle bond) returns the two sites, the
     orthonormal one feeds contract_L (left-to-right) or contract_R (right-to-left).  Bond
-    bases grow and shrink with the SVD.  Abelian symmetries.
+    bases grow and shrink with the SVD.  With SU(2) components the contraction and the
+    split are the non-abelian branches (su2.py: coeff_twoSiteGate / coeff_splitAA
+    recoupling, multiplets kept by their singular values, host SVD).
 
     `mps` must be right-canonical with the gauge centre on site 0.  A sweep is a
     left-to-right pass over bonds 0..L-2 followed by a right-to-left pass over L-2..0.
@@ -210,8 +213,7 @@ def dmrg2(ctx, model, mps, n_sweeps=2, Dmax=None, precision="fp64", max_iter=100
 def _dmrg2(ctx, model, mps, n_sweeps, Dmax, precision, max_iter, tol_eigval, tol_state, refine_iters, eps_svd,
            pool, factor, verbose, window, split_device):
     sym, L, nq = model.sym, model.L, model.sym.nq
-    if sym.nonabelian:
-        raise ValueError("dmrg2 supports abelian symmetries")
+    su2 = sym.nonabelian
     Dmax = Dmax if Dmax is not None else max(mps.bond_dim(l) for l in range(L + 1))
     qloc = model.qloc
     own_pool = pool is None
@@ -245,7 +247,10 @@ def _dmrg2(ctx, model, mps, n_sweeps, Dmax, precision, max_iter, tol_eigval, tol
                 A1, A2 = mps.A[l], mps.A[l + 1]
                 din = {tuple(A1.qin[i]): int(A1.rows[i]) for i in range(A1.n)}
                 dout = {tuple(A2.qout[i]): int(A2.cols[i]) for i in range(A2.n)}
-                V, comb = contract_two_sites(sym, A1, A2, qloc, qloc, nq, return_basis=True, ctx=ctx)
+                if su2:
+                    V, comb = contract_two_sites_su2(sym, A1, A2, qloc, qloc, ctx=ctx)
+                else:
+                    V, comb = contract_two_sites(sym, A1, A2, qloc, qloc, nq, return_basis=True, ctx=ctx)
                 t1 = clock()
                 H = PivotMatrix2(ctx, sym, envL[l], envR[l + 2], model.W[l], model.W[l + 1], V)
                 H.prepare("fp64" if refine_iters > 0 else precision)
@@ -258,9 +263,13 @@ def _dmrg2(ctx, model, mps, n_sweeps, Dmax, precision, max_iter, tol_eigval, tol
                 H.close()
                 t3 = clock()
                 V.data[:] = v
-                A1, A2, disc, dmid = split_two_site(V, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
-                                                    eps_svd=eps_svd, pool=pool, factor=factor,
-                                                    ctx=ctx if split_device else None)
+                if su2:
+                    A1, A2, disc, dmid = split_two_site_su2(V, comb, sym, qloc, qloc, din, dout, Dmax, move=move,
+                                                            eps_svd=eps_svd)
+                else:
+                    A1, A2, disc, dmid = split_two_site(V, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
+                                                        eps_svd=eps_svd, pool=pool, factor=factor,
+                                                        ctx=ctx if split_device else None)
                 mps.A[l], mps.A[l + 1] = A1, A2
                 mps.dims[l + 1] = dmid
                 disc_max = max(disc_max, disc)
