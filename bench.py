@@ -334,8 +334,9 @@ def su2_cylinder_bench(ctx, args):
     """Config C3: Hubbard SU(2)xU(1), width-4 cylinder as a 64-site snake, U/t=8, 1/8 hole
     doping (N=56, S=0), MPO w=10, D=2000 multiplets (~5,800 states); the two-site pivot of
     the middle.  Device-resident HxV (CUDA graph, events) in FP64 and split precision, the
-    split error, the Lanczos ground state of the pivot in both precisions, and one
-    single-site DMRG sweep of the cylinder in each precision."""
+    split error, the Lanczos ground state of the pivot in both precisions, one single-site
+    DMRG sweep of the cylinder in each precision and two-site DMRG (SU(2) two-site
+    contraction and split) over a window of the middle in each precision."""
     from vmps_gb300.pivot import DeviceVector, PivotMatrix2, time_hxv
     from vmps_gb300.workloads import hubbard_su2xu1_cylinder_two_site
     model, mps, Lenv, Renv, W1, W2, V, info = hubbard_su2xu1_cylinder_two_site(ctx)
@@ -385,7 +386,23 @@ def su2_cylinder_bench(ctx, args):
                       "timers_s": [{k: round(v, 4) for k, v in t.items()} for t in r["timers"]]}
     sweep["trace"] = step_trace(runs["split"], runs["fp64"])
     sweep["sweep_speedup"] = sweep["fp64"]["s_per_sweep"][0] / sweep["split"]["s_per_sweep"][0]
+    # two-site DMRG (SU(2) contract_AA2 / split_AA2) over a window of four bonds in the middle
+    # (eight steps), from the same seeded MPS in each precision, Dmax = 2000 multiplets
+    from vmps_gb300.dmrg import dmrg2
+    lo, hi = 30, 34
+    mps1 = RandomMPS(model, (1, info["N"]), 2000, seed=3, profile="gaussian", sigma=[3.0, 3.0]).canonicalize(lo, lo + 1)
+    two, runs2 = {}, {}
+    for tag, prec, kw in (("split", args.precision, dict(refine_iters=10)), ("fp64", "fp64", {})):
+        r = dmrg2(ctx, model, copy.deepcopy(mps1), n_sweeps=1, Dmax=2000, precision=prec, window=(lo, hi), **tol, **kw)
+        runs2[tag] = r
+        two[tag] = {"s": r["sweep_times"][0], "E": r["energies"][-1], "lanczos": r["solves"],
+                    "timers_s": {k: round(v, 4) for k, v in r["timers"][0].items()}}
+    two["window"] = [lo, hi]
+    two["steps"] = 2 * (hi - lo)
+    two["trace"] = step_trace(runs2["split"], runs2["fp64"])
+    two["step_speedup"] = two["fp64"]["s"] / two["split"]["s"]
     return dict(info, n_tasks=st64["n_tasks"], flops_per_hxv=st64["flops_merged"], single_site_sweep=sweep,
+                two_site_window=two,
                 hxv_fp64={"ms": ms64, "per_s": 1e3 / ms64, "tflops": st64["flops_merged"] / ms64 * 1e-9},
                 hxv_split={"ms": mss, "per_s": 1e3 / mss, "tflops_useful": sts["flops_merged"] / mss * 1e-9,
                            "tensor_tflops_issued": (sts["tensor_flops_phase1"] + sts["tensor_flops_phase2"]) /
