@@ -23,8 +23,9 @@ def _blocks(B):
     return out
 
 
-def transfer_hxv(direction, nq, Abra, Aket, W, LReigen, ab, order, V, vin, dot_weight):
-    """direction 'L' / 'R'; Abra/Aket/W: cell site tensors; LReigen: Biped; V: Tripod layout, vin its data"""
+def transfer_hxv(direction, nq, Abra, Aket, W, LReigen, ab, order, V, vin, dot_weight, sym=None):
+    """direction 'L' / 'R'; Abra/Aket/W: cell site tensors; LReigen: Biped; V: Tripod layout, vin its data;
+    sym: the symmetry's component kinds (None: U(1) throughout)"""
     inv = {v: k for k, v in order.items()}
     abq, abi = inv[ab]
     n = len(W)
@@ -35,7 +36,7 @@ def transfer_hxv(direction, nq, Abra, Aket, W, LReigen, ab, order, V, vin, dot_w
             mode = "FIXED_COLS" if l == n - 1 else ("FIXED_ROWS" if l == 0 else "FULL")
         else:
             mode = "FIXED_ROWS" if l == 0 else ("FIXED_COLS" if l == n - 1 else "FULL")
-        env = OracleEnv(direction, nq, E, Abra[l], W[l], Aket[l], mode=mode, fixed_ab=ab, order=order)
+        env = OracleEnv(direction, nq, E, Abra[l], W[l], Aket[l], mode=mode, fixed_ab=ab, order=order, sym=sym)
         E = env.run(E, Abra[l], Aket[l])
     T = _blocks(E)
     Vb = _blocks(V.like(np.array(vin, dtype=np.float64)))
