@@ -415,62 +415,99 @@ def su2_cylinder_bench(ctx, args):
 
 
 def vumps_bench(ctx, args):
-    """Config C4 pieces on a frozen cell: spin-1/2 Heisenberg with SU(2), ~470 multiplets
-    (7,000 states, D=512 requested) at the middle of a 60-site chain, the two-site cell
-    of sites 29-30 whose outer bonds carry the same basis.  Times the MpoTransferMatrix
-    application (the cell chain of contract_L plans), the GMRES environment solve
-    (FP64, and split precision with FP64 iterative refinement), and the HAC / HC
-    pivot HxVs (PivotMatrix1 / PivotMatrix0) of the cell in both precisions."""
+    """Config C4: the spin-1/2 Heisenberg chain with SU(2) as a uniform MPS: a seeded random
+    N(0,1) state with 512 multiplets per bond, gauge fixed (AL C = C AR).  A one-site cell
+    cannot carry it (the bond spin alternates between integer and half-integer), so the
+    cell has two sites.  Times and reports, in FP64 and in split precision: the MPO
+    environments (the triangular slot build, GMRES on the transfer operator for the
+    identity slots), the energy density and the VUMPS gradient norm |H_AC(AC) - AL H_C(C)|,
+    each against the same steps on the oracle; the transfer-operator application and the
+    H_AC / H_C HxVs alone."""
     from vmps_gb300 import models
-    from vmps_gb300.blocks import Blocks
-    from vmps_gb300.mps import RandomMPS
-    from vmps_gb300.pivot import DeviceVector, EnvUpdate, PivotMatrix0, PivotMatrix1, time_hxv
+    from vmps_gb300.pivot import DeviceVector, PivotMatrix0, PivotMatrix1, time_hxv
+    from vmps_gb300.uniform import UniformEnvironment, UniformMPS, bond_bases_su2
     from vmps_gb300.vumps import MpoTransferMatrix
-    from vmps_gb300.workloads import build_envs
-    m = models.heisenberg_su2(60)
-    c = 29
-    # the cell sites left-normalised (the transfer operator of a left-canonical uniform
-    # MPS has spectral radius 1); the gauge centre sits at c + 2
-    mps = RandomMPS(m, (1,), 512, seed=4).canonicalize(c + 2, c + 2)
-    Lenv, Renv = build_envs(ctx, m, mps, c, c + 1)
-    rng = np.random.default_rng(5)
-    ent = [(0, q, q, rng.standard_normal((d, d))) for q, d in sorted(mps.dims[c].items())]
-    LR = Blocks.from_entries(m.sym.nq, ent)
-    order = m.basis_order_map(c)
-    vac = m.sym.vacuum()
-    ab = sorted(v for (q, i), v in order.items() if tuple(q) == vac)[0]
-    A, W = [mps.A[c], mps.A[c + 1]], [m.W[c], m.W[c + 1]]
-    T = MpoTransferMatrix(ctx, m.sym, "L", A, A, W, LR, ab, order, Lenv)
-    out = {"multiplets": sum(mps.dims[c].values()), "states": sum(q[0] * n for q, n in mps.dims[c].items()),
-           "dim_transfer_vector": int(Lenv.data.size)}
-    v = rng.standard_normal(Lenv.data.size)
-    for p in ("fp64", "bf16x3"):
+    m = models.heisenberg_su2(8)
+    order, W = m.basis_order_map(4), [m.W[4], m.W[5]]
+    dims = bond_bases_su2(512, 20)
+    t0 = time.perf_counter()
+    u = UniformMPS(m, dims, seed=4)
+    g = u.gauge()
+    out = {"multiplets_per_bond": [sum(d.values()) for d in dims],
+           "states_per_bond": [sum(q[0] * n for q, n in d.items()) for d in dims], "cell": 2,
+           "gauge": dict(g, s=round(time.perf_counter() - t0, 2))}
+    res = {}
+    for prec in ("fp64", args.precision):
+        E = UniformEnvironment(ctx, m, u, W, order, precision=prec, tol=1e-12)
+        t0 = time.perf_counter()
+        E.left()
+        E.right()
+        t1 = time.perf_counter()
+        gn, parts = E.gradient()
+        t2 = time.perf_counter()
+        res[prec] = {"e": E.energy_density(), "gradient_norm": gn, "environments_s": round(t1 - t0, 3),
+                     "gradient_s": round(t2 - t1, 3), "gmres": E.info}
+        if prec == "fp64":
+            E64 = E
+    out["environments"] = res
+    if not args.no_cpu:
+        import oracle
+        from oracle.vumps_cpu import transfer_hxv
+        oracle.set_threads(os.cpu_count() or 1)
+        sym = m.sym
+
+        def env(side, mode, fixed_ab, order_, Eo, Abra, Wl, Aket):
+            return oracle.OracleEnv(side, sym.nq, Eo, Abra, Wl, Aket, mode=mode, fixed_ab=fixed_ab, order=order_,
+                                    sym=sym).run(Eo, Abra, Aket)
+
+        class OracleTransfer(MpoTransferMatrix):
+            def __init__(self, side, A, Wl, LR, ab, order_, V):
+                self.sym, self.V, self.ab = sym, V, ab
+                self.ab_key = {v: k for k, v in order_.items()}[ab]
+                self.args = (side, A, Wl, LR, ab, order_)
+
+            def hxv(self, vin, precision="fp64"):
+                side, A, Wl, LR, ab, order_ = self.args
+                return transfer_hxv(side, sym.nq, A, A, Wl, LR, ab, order_, self.V, vin, sym.dot_weight, sym=sym)
+
+            def close(self):
+                pass
+
+        def transfer(side, A, Wl, LR, ab, order_, V, b):
+            return OracleTransfer(side, A, Wl, LR, ab, order_, V).solve_linear(b, tol=1e-12, dimK=100)
+
+        def apply(kind, L, R, Wl, V, x):
+            if kind == 1:
+                return oracle.OraclePivot(1, sym.nq, L, R, V, Wl, sym=sym).hxv(x)
+            return oracle.OraclePivot(0, sym.nq, L, R, V, sym=sym).hxv(x)
+        t0 = time.perf_counter()
+        ref = UniformEnvironment(None, m, u, W, order, env=env, transfer=transfer, apply=apply)
+        ref.left()
+        ref.right()
+        g_ref, _ = ref.gradient()
+        e_ref = ref.energy_density()
+        out["oracle"] = {"e": e_ref, "gradient_norm": g_ref, "s": round(time.perf_counter() - t0, 1)}
+        for prec, r in res.items():
+            r["e_rel_err_vs_oracle"] = abs(r["e"] - e_ref) / abs(e_ref)
+            r["gradient_rel_err_vs_oracle"] = abs(r["gradient_norm"] - g_ref) / g_ref
+    # the pieces alone: transfer operator (left, identity slot) and H_AC / H_C HxVs
+    R = {q: M @ M.T for q, M in u.C[0].items()}
+    V = E64._identity(E64.last).like()
+    T = MpoTransferMatrix(ctx, m.sym, "L", u.AL, u.AL, W, E64._blocks_of(R), E64.last, order, V)
+    v = np.random.default_rng(5).standard_normal(V.data.size)
+    for p in ("fp64", args.precision):
         T.hxv(v, p)
         t0 = time.perf_counter()
         for _ in range(5):
             T.hxv(v, p)
         out[f"transfer_hxv_ms_{p}"] = (time.perf_counter() - t0) / 5 * 1e3
-    b = T.rhs(rng.standard_normal(Lenv.data.size), 0.3) * T.slot_mask()
-    t0 = time.perf_counter()
-    x64, i64 = T.solve_linear(b, tol=1e-10, dimK=100)
-    t1 = time.perf_counter()
-    xs, isp = T.solve_linear_refined(b, tol=1e-10, inner_tol=1e-4, dimK=100)
-    t2 = time.perf_counter()
-    out["gmres_fp64"] = {"s": t1 - t0, "iterations": i64["iterations"], "residual": i64["residual"]}
-    out["gmres_split_refined"] = dict(isp, s=t2 - t1)
-    out["gmres_solution_rel_diff"] = float(np.sqrt(T.dot(xs - x64, xs - x64) / T.dot(x64, x64)))
     T.close()
-    # HAC: one-site pivot of site c; HC: zero-site pivot of bond c+1
-    Rc1 = _right_env(ctx, m, mps, Renv, c)      # sites >= c + 1
-    HAC = PivotMatrix1(ctx, m.sym, Lenv, Rc1, m.W[c], mps.A[c])
-    e = EnvUpdate(ctx, m.sym, "L", Lenv, mps.A[c], m.W[c], mps.A[c])
-    Lc1 = e.run(Lenv, mps.A[c], mps.A[c])       # sites <= c
-    e.close()
-    C = Blocks.from_entries(m.sym.nq, [(0, q, q, rng.standard_normal((d, d))) for q, d in sorted(mps.dims[c + 1].items())])
-    HC = PivotMatrix0(ctx, m.sym, Lc1, Rc1, C)
-    for name, H, vec in (("hac", HAC, mps.A[c].data), ("hc", HC, C.data)):
+    L1 = E64.env("L", "FULL", 0, order, E64.L, u.AL[0], W[0], u.AL[0])
+    HAC = PivotMatrix1(ctx, m.sym, E64.L, E64.env("R", "FULL", 0, order, E64.R, u.AR[1], W[1], u.AR[1]), W[0], u.AC[0])
+    HC = PivotMatrix0(ctx, m.sym, L1, E64.env("R", "FULL", 0, order, E64.R, u.AR[1], W[1], u.AR[1]), u.C_blocks(1))
+    for name, H, vec in (("hac", HAC, u.AC[0].data), ("hc", HC, u.C_blocks(1).data)):
         a, bb = DeviceVector(H, vec), DeviceVector(H)
-        for p in ("fp64", "bf16x3"):
+        for p in ("fp64", args.precision):
             time_hxv(H, a, bb, p, n_iter=3)
             out[f"{name}_hxv_ms_{p}"] = time_hxv(H, a, bb, p, n_iter=20)[0]
         out[f"{name}_dim"] = H.dim
@@ -478,15 +515,6 @@ def vumps_bench(ctx, args):
         bb.close()
         H.close()
     return out
-
-
-def _right_env(ctx, m, mps, Renv, site):
-    """R environment of sites >= site + 1 from the one of sites >= site + 2 (Renv)"""
-    from vmps_gb300.pivot import EnvUpdate
-    e = EnvUpdate(ctx, m.sym, "R", Renv, mps.A[site + 1], m.W[site + 1], mps.A[site + 1])
-    R = e.run(Renv, mps.A[site + 1], mps.A[site + 1])
-    e.close()
-    return R
 
 
 def chebyshev_bench(ctx, args):
