@@ -30,7 +30,7 @@ import numpy as np
 from .blocks import Blocks, MpoSite
 from .mps import contract_two_sites, two_site_layout
 from .pivot import EnvUpdate, PivotMatrix2, left_vacuum, right_target
-from .union import UnionPivot2, concat_blocks, tag_blocks, tagged_symmetry
+from .union import UnionPivot2, aux_tag, bra_ket_tag, concat_blocks, tag_blocks, tagged_symmetry
 
 
 def standing_wave(L: int, n: int) -> np.ndarray:
@@ -161,8 +161,8 @@ class SpectralPivot:
             RO = self.env("R", RO, relabel(mps.A[j], dq), W[j], mps.A[j])
         # the charge-changing step as a tagged pivot: ket blocks tag 0, bra blocks tag 1
         tsym = tagged_symmetry(sym)
-        Lt, Rt = _bra_ket_tag(LO, "L"), _bra_ket_tag(RO, "R")
-        W1, W2 = _aux_tag(W[l]), _aux_tag(W[l + 1])
+        Lt, Rt = bra_ket_tag(LO, "L"), bra_ket_tag(RO, "R")
+        W1, W2 = aux_tag(W[l]), aux_tag(W[l + 1])
         V = concat_blocks([tag_blocks(self.V0, 0), tag_blocks(Vb, 1)])
         x = np.concatenate([self.V0.data, np.zeros(Vb.data.size)])
         y = self.apply2(tsym, Lt, Rt, W1, W2, V, x)
@@ -172,25 +172,3 @@ class SpectralPivot:
         """one pivot over the spins' sectors (parts in the order of self.spins)"""
         return UnionPivot2(ctx or self.ctx, self.sym, self.model.W[self.l], self.model.W[self.l + 1],
                            [self.sector(s) for s in self.spins])
-
-
-def _bra_ket_tag(E: Blocks, side: str) -> Blocks:
-    """an operator environment between bra (tag 1) and ket (tag 0): an L block's rows are
-    the bra's (qin), an R block's rows the ket's (contract_L = Abra^dagger L Aket,
-    contract_R = Aket R Abra^dagger); the middle (auxiliary) quantum number carries the
-    difference, tag 1"""
-    def t(q, v):
-        q = np.asarray(q, dtype=np.int32).reshape(len(q), -1)
-        return np.concatenate([q, np.full((len(q), 1), v, dtype=np.int32)], axis=1)
-    tin, tout = (1, 0) if side == "L" else (0, 1)
-    return Blocks(E.nq + 1, t(E.qin, tin), t(E.qout, tout), E.leg, E.rows, E.cols, data=E.data, qmid=t(E.qmid, 1),
-                  offset=E.offset)
-
-
-def _aux_tag(W: MpoSite) -> MpoSite:
-    """an operator site between the tagged bases: auxiliary quantum numbers tag 1, local and
-    operator ones tag 0"""
-    t = MpoSite(W.nq + 1, [tuple(q) + (0,) for q in W.qloc], [tuple(q) + (0,) for q in W.qop])
-    for i in range(W.nnz):
-        t.add(W.s1[i], W.s2[i], W.k[i], tuple(W.qin[i]) + (1,), tuple(W.qout[i]) + (1,), W.row[i], W.col[i], W.val[i])
-    return t

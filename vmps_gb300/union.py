@@ -101,3 +101,25 @@ class UnionPivot2:
 
     def close(self):
         self.H.close()
+
+
+def bra_ket_tag(E: Blocks, side: str) -> Blocks:
+    """an operator environment between bra (tag 1) and ket (tag 0): an L block's rows are
+    the bra's (qin), an R block's rows the ket's (contract_L = Abra^dagger L Aket,
+    contract_R = Aket R Abra^dagger); the middle (auxiliary) quantum number carries the
+    difference, tag 1"""
+    def t(q, v):
+        q = np.asarray(q, dtype=np.int32).reshape(len(q), -1)
+        return np.concatenate([q, np.full((len(q), 1), v, dtype=np.int32)], axis=1)
+    tin, tout = (1, 0) if side == "L" else (0, 1)
+    return Blocks(E.nq + 1, t(E.qin, tin), t(E.qout, tout), E.leg, E.rows, E.cols, data=E.data, qmid=t(E.qmid, 1),
+                  offset=E.offset)
+
+
+def aux_tag(W: MpoSite) -> MpoSite:
+    """an operator site between the tagged bases: auxiliary quantum numbers tag 1, local and
+    operator ones tag 0"""
+    t = MpoSite(W.nq + 1, [tuple(q) + (0,) for q in W.qloc], [tuple(q) + (0,) for q in W.qop])
+    for i in range(W.nnz):
+        t.add(W.s1[i], W.s2[i], W.k[i], tuple(W.qin[i]) + (1,), tuple(W.qout[i]) + (1,), W.row[i], W.col[i], W.val[i])
+    return t
