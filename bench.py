@@ -614,6 +614,84 @@ def chebyshev_bench(ctx, args):
     return out
 
 
+def mps_chebyshev_bench(ctx, args):
+    """The Chebyshev recursion of whole MPS (MpsCompressor::polyCompress, solvers/
+    MpsCompressor.h:1372-1564, in polyIter, DmrgLinearAlgebra.h:550-566): Hubbard L=32,
+    U=4, U(1)xU(1); ground state |0> at D=384 (two-site DMRG, FP64); start vector
+    c_{k,up}|0> (k = pi 8/33) fitted as an MPS of charge (31, -1) from a seeded random MPS
+    (two sweeps); then t_{n+1} = 2 H' t_n - t_{n-1}, H' = (H - b)/a, each vector fitted by
+    one two-site sweep of at most 384 states per bond (vmps_gb300.compress: per step one
+    tagged two-site application per distinct source MPS, H t_n and t_n as one summed MPO,
+    contract_L / contract_R between the fitted and the source MPS, the truncated split
+    through the Gram matrix on the device, singular values below 1e-7 of the largest
+    dropped), 16 moments in FP64 and in split precision.  The bounds: E_0 of the ground
+    state and -E_0(-H) in the (31, -1) sector (DMRG at D=64), 5 % margin.  The oracle
+    (its contract_L / contract_R and two-site HxV on the host's cores) runs the first
+    moment's fit from the same FP64 start vector."""
+    from vmps_gb300 import models
+    from vmps_gb300.compress import Compressor, copy_mps
+    from vmps_gb300.dmrg import dmrg2
+    from vmps_gb300.mps import RandomMPS
+    from vmps_gb300.spectral import annihilator, annihilator_mpo, standing_wave
+    L, D, n, nmom, eps = 32, 384, 8, 16, 1e-7
+    model = models.hubbard_u1xu1(L, t=1.0, U=4.0)
+    t0 = time.perf_counter()
+    gs = RandomMPS(model, (L, 0), D, seed=5).canonicalize(0, 0)
+    E0 = float(dmrg2(ctx, model, gs, n_sweeps=3, Dmax=D, precision="fp64")["energies"][-1])
+    dq = annihilator(model, "up")[1]
+    Q = tuple(a + b for a, b in zip((L, 0), dq))
+    neg = models.hubbard_u1xu1(L, t=-1.0, U=-4.0)
+    top = RandomMPS(neg, Q, 64, seed=6).canonicalize(0, 0)
+    Emax = -float(dmrg2(ctx, neg, top, n_sweeps=3, Dmax=64, precision="fp64")["energies"][-1])
+    t_setup = time.perf_counter() - t0
+    a, b = (Emax - E0) / (2 * 0.95), (Emax + E0) / 2
+    W = annihilator_mpo(model, standing_wave(L, n), "up")
+
+    def start(comp):
+        psi0 = RandomMPS(model, Q, D, seed=17)
+        return psi0, comp.fit(psi0, [(W, gs, 1.0)], Dmax=D, sweeps=2, eps_svd=eps)
+
+    def moments(comp, psi0, nm):
+        comp.applications = 0
+        t0 = time.perf_counter()
+        mu, info = comp.chebyshev_moments(psi0, nm, a, b, Dmax=D, sweeps=1, eps_svd=eps)
+        dt = time.perf_counter() - t0
+        return mu, {"s_total": round(dt, 3), "s_per_moment": dt / (nm - 1),
+                    "two_site_applications": comp.applications, "discarded_max": max(info["discarded"]),
+                    "max_bond": info["max_bond"]}
+    res = {}
+    for prec in ("fp64", args.precision):
+        comp = Compressor(ctx, model, precision=prec, factor="eigh")
+        t0 = time.perf_counter()
+        psi0, d0 = start(comp)
+        ts = time.perf_counter() - t0
+        mu, r = moments(comp, psi0, nmom)
+        res[prec] = dict(r, start_s=round(ts, 3), start_discarded=d0, mu_first=[float(x) for x in mu[:4]])
+        if prec == "fp64":
+            mu64, psi64 = mu, psi0
+        else:
+            res[prec]["moment_rel_err_vs_fp64"] = float(np.max(np.abs(mu - mu64)) / abs(mu64[0]))
+    out = {"workload": "hubbard_u1xu1_L32_D384_c_k_up_mps_chebyshev", "E0": E0, "Emax_sector": Emax,
+           "bounds_margin": 0.05, "setup_s": round(t_setup, 2), "nmom": nmom, "n_k": float(mu64[0]),
+           "Dmax": D, "eps_svd": eps, "sweeps_per_moment": 1, "runs": res}
+    if not args.no_cpu:
+        import oracle
+        oracle.set_threads(os.cpu_count() or 1)
+
+        def env(side, E, Abra, Wl, Aket):
+            return (oracle.contract_L if side == "L" else oracle.contract_R)(Wl.nq, E, Abra, Wl, Aket)
+
+        def apply2(sym, Le, Re, W1, W2, V, x):
+            return oracle.OraclePivot(2, sym.nq, Le, Re, V, W1, W2).hxv(x)
+        comp = Compressor(None, model, env=env, apply2=apply2, factor="eigh")
+        mu, r = moments(comp, copy_mps(psi64), 2)
+        out["oracle"] = {"moments": 1, "s_per_moment": r["s_per_moment"], "threads": os.cpu_count() or 1,
+                         "sample": "the fit of t_1 (one sweep) from the FP64 start vector",
+                         "moment_rel_err_vs_engine_fp64": float(np.max(np.abs(mu - mu64[:2])) / abs(mu64[0])),
+                         "speedup_engine_fp64": r["s_per_moment"] / res["fp64"]["s_per_moment"]}
+    return out
+
+
 def cpu_model():
     """CPU model string of the host (lscpu's "Model name", else /proc/cpuinfo)."""
     try:
@@ -745,6 +823,7 @@ def main():
     ap.add_argument("--no-chebyshev", action="store_true")
     ap.add_argument("--no-su2", action="store_true")
     ap.add_argument("--no-vumps", action="store_true")
+    ap.add_argument("--no-mps-chebyshev", action="store_true")
     ap.add_argument("--no-window", action="store_true", help="skip the D=4096 two-site window")
     ap.add_argument("--no-tune-small", action="store_true", help="skip the autotuner on the smaller pivots")
     args = ap.parse_args()
@@ -887,6 +966,9 @@ def main():
     vum = None
     if not args.no_vumps and rank == 0:
         vum = vumps_bench(ctx, args)
+    mcheb = None
+    if not args.no_mps_chebyshev and rank == 0:
+        mcheb = mps_chebyshev_bench(ctx, args)
 
     tune_small = None
     if rank == 0 and args.precision == "bf16x3" and not args.no_tune_small:
@@ -932,6 +1014,7 @@ def main():
             "chebyshev": cheb,
             "su2xu1_cylinder": su2,
             "vumps_cell": vum,
+            "mps_chebyshev": mcheb,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -1,0 +1,167 @@
+"""MPS compression (vmps_gb300.compress) on the host: the two-site variational fit of
+sums of operator-MPS products and the Chebyshev recursion of whole MPS, run with the
+oracle's contract_L / contract_R and two-site HxV in place of the engine's, against
+dense vectors and matrices of small chains (MpsCompressor::prodCompress / polyCompress,
+solvers/MpsCompressor.h:961-1564; polyIter, DmrgLinearAlgebra.h:550-566)."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import ed
+from vmps_gb300 import models
+from vmps_gb300.compress import Compressor, copy_mps, identity_mpo
+from vmps_gb300.mps import RandomMPS
+
+
+def _oracle_env(side, E, Abra, W, Aket):
+    return (oracle.contract_L if side == "L" else oracle.contract_R)(W.nq, E, Abra, W, Aket)
+
+
+def _oracle_apply2(sym, L, R, W1, W2, V, x):
+    return oracle.OraclePivot(2, sym.nq, L, R, V, W1, W2).hxv(x)
+
+
+def _dense(mps):
+    """the state in the kron basis of the MPO's local indices, site 0 most significant"""
+    return ed.right_isometry(mps, 0)[0]
+
+
+def _setup(L, D, seed=3):
+    model = models.hubbard_u1xu1(L, t=1.0, U=4.0)
+    psi = RandomMPS(model, (L, 0), D, seed=seed)
+    comp = Compressor(None, model, env=_oracle_env, apply2=_oracle_apply2)
+    return model, psi, comp
+
+
+def test_identity_mpo_and_overlap():
+    model, psi, comp = _setup(4, 16)
+    for W in comp.I:
+        dense = np.zeros((model.d, model.d))
+        for i in range(W.nnz):
+            assert W.row[i] == 0 and W.col[i] == 0
+            dense[W.s1[i], W.s2[i]] += W.val[i]
+        assert np.array_equal(dense, np.eye(model.d))
+    phi = RandomMPS(model, (4, 0), 16, seed=8)
+    assert comp.overlap(phi, psi) == pytest.approx(float(_dense(phi) @ _dense(psi)), rel=1e-12, abs=1e-14)
+
+
+def test_fit_of_h_psi_is_exact_with_complete_bases():
+    """phi = 0.7 H psi - 0.3 psi; bonds free to grow to the complete bases"""
+    model, psi, comp = _setup(6, 64)
+    H = ed.mpo_to_dense(model)
+    phi = copy_mps(psi)
+    disc = comp.fit(phi, [(model.W, psi, 0.7), (comp.I, psi, -0.3)], Dmax=256, sweeps=1)
+    ref = 0.7 * H @ _dense(psi) - 0.3 * _dense(psi)
+    assert disc < 1e-14
+    assert np.linalg.norm(_dense(phi) - ref) < 1e-11 * np.linalg.norm(ref)
+
+
+def test_truncated_fit_improves_on_its_start_and_keeps_dmax():
+    """with Dmax below the target's bond dimension the fit is the best MPS of that size
+    it finds: its error is below that of the start (psi itself, rescaled) and each
+    bond keeps at most Dmax states"""
+    model, psi, comp = _setup(6, 64)
+    H = ed.mpo_to_dense(model)
+    ref = H @ _dense(psi)
+    phi = copy_mps(psi)
+    disc = comp.fit(phi, [(model.W, psi, 1.0)], Dmax=12, sweeps=3)
+    assert disc > 0
+    assert max(sum(d.values()) for d in phi.dims) <= 12
+    x = _dense(psi)
+    start_err = np.linalg.norm(ref - (x @ ref) / (x @ x) * x)
+    err = np.linalg.norm(_dense(phi) - ref)
+    assert err < 0.5 * start_err
+    # the fitted state is the projection of the target onto its own manifold: <phi|ref> = <phi|phi>
+    f = _dense(phi)
+    assert f @ ref == pytest.approx(f @ f, rel=1e-9)
+
+
+def test_mps_chebyshev_moments_equal_dense_recursion():
+    model, psi, comp = _setup(4, 16)
+    H = ed.mpo_to_dense(model)
+    x = _dense(psi)
+    w = np.linalg.eigvalsh(H)
+    a, b = 1.05 * (w[-1] - w[0]) / 2, (w[-1] + w[0]) / 2
+    nmom = 8
+    mu, info = comp.chebyshev_moments(psi, nmom, a, b, Dmax=64, sweeps=1)
+    t0, t1 = x, (H @ x - b * x) / a
+    ref = [x @ t0, x @ t1]
+    for _ in range(2, nmom):
+        t0, t1 = t1, 2 * (H @ t1 - b * t1) / a - t0
+        ref.append(x @ t1)
+    assert max(info["discarded"]) < 1e-14
+    assert np.allclose(mu, ref, rtol=0, atol=1e-10 * abs(ref[0]))
+
+
+def _dense_mpo(W, d, end_q):
+    """the operator of an MPO site list (boundary states: vacuum index 0 on the left,
+    end_q index 0 on the right), kron basis, site 0 most significant"""
+    L = len(W)
+    keys = [set() for _ in range(L + 1)]
+    for l, w in enumerate(W):
+        for i in range(w.nnz):
+            keys[l].add((tuple(w.qin[i]), w.row[i]))
+            keys[l + 1].add((tuple(w.qout[i]), w.col[i]))
+    idx = [{k: n for n, k in enumerate(sorted(ks))} for ks in keys]
+    vac = tuple(0 for _ in end_q)
+    T = np.zeros((1, 1, len(idx[0])))
+    T[0, 0, idx[0][(vac, 0)]] = 1.0
+    for l, w in enumerate(W):
+        M = np.zeros((len(idx[l]), len(idx[l + 1]), d, d))
+        for i in range(w.nnz):
+            M[idx[l][(tuple(w.qin[i]), w.row[i])], idx[l + 1][(tuple(w.qout[i]), w.col[i])], w.s1[i], w.s2[i]] += w.val[i]
+        T = np.einsum("xya,abst->xsytb", T, M)
+        T = T.reshape(T.shape[0] * d, T.shape[2] * d, M.shape[1])
+    return T[:, :, idx[L][(tuple(end_q), 0)]]
+
+
+def test_mpo_sum_is_the_operator_sum():
+    from vmps_gb300.compress import mpo_sum
+    from vmps_gb300.spectral import annihilator, annihilator_mpo
+    model = models.hubbard_u1xu1(4, t=1.0, U=4.0)
+    I = identity_mpo(model)
+    S = mpo_sum([model.W, I], [0.7, -0.3], (0, 0))
+    assert np.allclose(_dense_mpo(S, model.d, (0, 0)), 0.7 * ed.mpo_to_dense(model) - 0.3 * np.eye(4 ** 4),
+                       rtol=0, atol=1e-13)
+    # two charge-changing operators with different auxiliary bases
+    dq = annihilator(model, "up")[1]
+    A1 = annihilator_mpo(model, [1.0, 0.5, 0.0, -2.0], "up")
+    A2 = annihilator_mpo(model, [0.0, 1.0, 3.0, 0.0], "up")
+    S = mpo_sum([A1, A2], [2.0, -1.0], dq)
+    ref = 2.0 * _dense_mpo(A1, model.d, dq) - _dense_mpo(A2, model.d, dq)
+    assert np.linalg.norm(ref) > 1
+    assert np.allclose(_dense_mpo(S, model.d, dq), ref, rtol=0, atol=1e-13)
+
+
+def _charged_start(model, psi, spin, n, comp):
+    """c_{k,spin}|psi>, k = pi n/(L+1), fitted from a random MPS of the target charge"""
+    from vmps_gb300.spectral import annihilator, annihilator_mpo, standing_wave
+    dq = annihilator(model, spin)[1]
+    W = annihilator_mpo(model, standing_wave(model.L, n), spin)
+    Q = tuple(a + b for a, b in zip(psi.Qtot, dq))
+    phi = RandomMPS(model, Q, 64, seed=17)
+    disc = comp.fit(phi, [(W, psi, 1.0)], Dmax=256, sweeps=2)
+    return phi, disc
+
+
+@pytest.mark.parametrize("spin,n", [("up", 1), ("dn", 4)])
+def test_charge_changing_fit_and_its_moments(spin, n):
+    """c_{k,s}|psi> as an MPS of charge Qtot + dq (the right boundary of its environments
+    carries dq), then the MPS Chebyshev moments in that sector, against dense c_k and the
+    dense recursion"""
+    from test_spectral import _dense_c
+    from vmps_gb300.spectral import standing_wave
+    model, psi, comp = _setup(6, 64)
+    phi, disc = _charged_start(model, psi, spin, n, comp)
+    ref = _dense_c(model, standing_wave(6, n), spin) @ _dense(psi)
+    assert disc < 1e-14
+    assert np.linalg.norm(_dense(phi) - ref) < 1e-11 * np.linalg.norm(ref)
+    H = ed.mpo_to_dense(model)
+    a, b = 1.01 * np.abs(H).sum(axis=1).max(), 0.0     # the spectrum lies inside [-a, a] (Gershgorin)
+    mu, _ = comp.chebyshev_moments(phi, 6, a, b, Dmax=256, sweeps=1)
+    t0, t1 = ref, (H @ ref - b * ref) / a
+    mref = [ref @ t0, ref @ t1]
+    for _ in range(2, 6):
+        t0, t1 = t1, 2 * (H @ t1 - b * t1) / a - t0
+        mref.append(ref @ t1)
+    assert np.allclose(mu, mref, rtol=0, atol=1e-10 * mref[0])

@@ -1,0 +1,287 @@
+"""MPS-level compression on the engine: variational fitting of a sum of operator-MPS
+products by two-site sweeps (MpsCompressor::prodCompress / polyCompress,
+solvers/MpsCompressor.h:961-1564), and the Chebyshev recursion of whole MPS built on
+it (polyIter, DmrgLinearAlgebra.h:550-566).  Abelian symmetries.
+
+fit(phi, terms): phi ~ sum_i c_i O_i psi_i, with O_i an MPO (the Hamiltonian, or the
+identity for a plain MPS term).  phi is right-canonical with its centre on site 0; per
+two-site step (l, l+1) the optimal two-site tensor of phi, with its other sites
+orthonormal, is
+
+    T = sum_i c_i  L_i[l] W_i[l] W_i[l+1] Psi_i(l, l+1) R_i[l+2],
+
+L_i / R_i the environments of O_i between phi (bra) and psi_i (ket) (contract_L /
+contract_R with Abra != Aket).  Each term is one two-site pivot application from psi_i's
+layout into phi's; the two layouts differ, so it runs as a pivot whose blocks carry a tag
+(0: ket, 1: bra; union.bra_ket_tag / aux_tag).  T is split by the truncated SVD (at most
+Dmax states over all sectors of the middle bond, the state's norm kept), and the
+environment of the sweep direction is updated.  The middle bond grows and shrinks with
+the split, so phi's bond dimensions adapt to the target.
+
+chebyshev_moments(psi0, nmom, a, b): t_0 = psi0, t_1 = (H - b)/a t_0, t_{n+1} =
+2 (H - b)/a t_n - t_{n-1}, each fitted as above (terms H t_n, t_n, t_{n-1}), and
+mu_n = <psi0|t_n> from the overlap environments.
+"""
+from __future__ import annotations
+
+import contextlib
+import copy
+
+import numpy as np
+
+from .blocks import Blocks, MpoSite
+from .hostla import SectorPool
+from .mps import contract_two_sites, right_normalize, split_two_site, two_site_layout
+from .pivot import EnvUpdate, PivotMatrix2, left_vacuum
+from .union import aux_tag, bra_ket_tag, concat_blocks, tag_blocks, tagged_symmetry
+
+
+def identity_mpo(model) -> list:
+    """the identity as an MPO (one auxiliary state, quantum number vacuum)"""
+    vac = model.sym.vacuum()
+    W = []
+    for _ in range(model.L):
+        w = MpoSite(model.sym.nq, list(model.qloc), [vac])
+        for s in range(len(model.qloc)):
+            w.add(s, s, 0, vac, vac, 0, 0, 1.0)
+        W.append(w)
+    return W
+
+
+def mpo_sum(mpos: list, coefs: list, end_q) -> list:
+    """sum_i c_i O_i of MPOs (site lists) as one MPO: the auxiliary bases of the inner bonds
+    side by side (the states of O_i after those of O_0..O_i-1 in each quantum-number
+    sector), the boundary states shared, c_i on site 0's entries of O_i.  Every O_i starts
+    in the vacuum state (index 0) and ends in state 0 of quantum number end_q (the charge
+    the operators carry); entries of the boundary sites that leave other boundary states
+    are never reached from the environments and are dropped."""
+    L, nq = len(mpos[0]), mpos[0][0].nq
+    vac, end_q = tuple(0 for _ in range(nq)), tuple(end_q)
+    out = [MpoSite(nq, list(mpos[0][l].qloc), []) for l in range(L)]
+    qops = [[] for _ in range(L)]
+    base = [dict() for _ in range(L + 1)]      # bond -> {aux QN: states placed so far}
+    for W, c in zip(mpos, coefs):
+        nstate = [dict() for _ in range(L + 1)]
+        for l in range(L):
+            w = W[l]
+            kmap = []
+            for q in w.qop:
+                if tuple(q) not in qops[l]:
+                    qops[l].append(tuple(q))
+                kmap.append(qops[l].index(tuple(q)))
+            for i in range(w.nnz):
+                q_in, q_out, r, col = tuple(w.qin[i]), tuple(w.qout[i]), w.row[i], w.col[i]
+                nstate[l][q_in] = max(nstate[l].get(q_in, 0), r + 1)
+                nstate[l + 1][q_out] = max(nstate[l + 1].get(q_out, 0), col + 1)
+                if l == 0 and (q_in != vac or r != 0):
+                    continue
+                if l == L - 1 and (q_out != end_q or col != 0):
+                    continue
+                r += base[l].get(q_in, 0) if l > 0 else 0
+                col += base[l + 1].get(q_out, 0) if l < L - 1 else 0
+                out[l].add(w.s1[i], w.s2[i], kmap[w.k[i]], q_in, q_out, r, col, (c if l == 0 else 1.0) * w.val[i])
+        for b in range(1, L):
+            for q, n in nstate[b].items():
+                base[b][q] = base[b].get(q, 0) + n
+    for l in range(L):
+        out[l].qop = qops[l]
+    return out
+
+
+def _dims_of(A: Blocks, side: str) -> dict:
+    q = A.qin if side == "in" else A.qout
+    n = A.rows if side == "in" else A.cols
+    return {tuple(q[i]): int(n[i]) for i in range(A.n)}
+
+
+def copy_mps(psi):
+    """a copy of an MPS object (its site tensors and bond bases copied)"""
+    m = copy.copy(psi)
+    m.A = [a.like(a.data.copy()) for a in psi.A]
+    m.dims = [dict(d) for d in psi.dims]
+    return m
+
+
+def right_canonical(psi, pool=None):
+    """psi with sites 1..L-1 right-orthonormal (the factors pushed into site 0), in place"""
+    carry = None
+    for l in range(psi.L - 1, 0, -1):
+        psi.A[l], carry = right_normalize(psi.A[l], psi.model.sym.nq, carry, pool=pool)
+    A = psi.A[0]
+    for i in range(A.n):
+        q = tuple(A.qout[i])
+        if q in carry:
+            A.block(i)[...] = A.block(i) @ carry[q]
+    return psi
+
+
+class Compressor:
+    """fits and overlaps of MPS of one model on the engine.  precision: that of the
+    two-site applications ("fp64" or a split form; the environments are FP64).
+    env(side, E, Abra, W, Aket) and apply2(sym, L, R, W1, W2, V, x) replace the engine's
+    environment update and two-site HxV (a host check runs the same sweeps on a CPU
+    restatement).  factor: the sector factorisation of the split, "svd" (LAPACK's SVD
+    on the host: singular values accurate down to the working precision, so a cut at
+    eps_svd = 1e-14 of the largest drops only rounding noise, as Biped::truncateSVD's
+    does) or "eigh" (the native Gram-matrix split, large sectors on the GPU: faster,
+    singular values below ~1e-8 of the largest are noise, so give eps_svd >= 1e-7).  The
+    host's share (sector factorisations, QRs) runs on `threads` threads (hostla.SectorPool;
+    default: up to 16 cores)."""
+
+    def __init__(self, ctx, model, precision="fp64", env=None, apply2=None, factor="svd", threads=None):
+        if model.sym.nonabelian:
+            raise ValueError("the compressor supports abelian symmetries")
+        self.ctx, self.model, self.sym = ctx, model, model.sym
+        self.precision = precision
+        self.I = identity_mpo(model)
+        self.tsym = tagged_symmetry(self.sym)
+        self._env = env or self._engine_env
+        self.apply2 = apply2 or self._engine_apply2
+        self.factor = factor
+        self.threads = threads
+        self._pool = None
+        self.applications = 0
+
+    # ---- engine steps
+    def _engine_env(self, side, E, Abra, W, Aket):
+        e = EnvUpdate(self.ctx, self.sym, side, E, Abra, W, Aket)
+        try:
+            return e.run(E, Abra, Aket, "fp64")
+        finally:
+            e.close()
+
+    def _engine_apply2(self, sym, L, R, W1, W2, V, x):
+        H = PivotMatrix2(self.ctx, sym, L, R, W1, W2, V)
+        try:
+            return H.apply(x, self.precision)
+        finally:
+            H.close()
+
+    def _apply(self, L, R, W1, W2, Vket: Blocks, Vbra: Blocks) -> np.ndarray:
+        """the two-site application of (L, W1, W2, R) to Vket, into Vbra's layout"""
+        V = concat_blocks([tag_blocks(Vket, 0), tag_blocks(Vbra, 1)])
+        x = np.concatenate([Vket.data, np.zeros(Vbra.data.size)])
+        y = self.apply2(self.tsym, bra_ket_tag(L, "L"), bra_ket_tag(R, "R"), aux_tag(W1), aux_tag(W2), V, x)
+        self.applications += 1
+        return y[Vket.data.size:]
+
+    def overlap(self, bra, ket) -> float:
+        """<bra|ket> of two MPS with the same total quantum number"""
+        E = left_vacuum(self.sym)
+        for l in range(self.model.L):
+            E = self._env("L", E, bra.A[l], self.I[l], ket.A[l])
+        return float(E.data.sum())
+
+    # ---- the fit
+    def fit(self, phi, terms: list, Dmax: int, sweeps: int = 2, eps_svd: float = 1e-14):
+        """phi ~ sum c_i O_i psi_i, terms = [(W_i (MPO site list), psi_i (MPS), c_i)]; phi is
+        updated in place (brought to right-canonical form first; it ends so, with its
+        centre on site 0).  The operators may change the charge: O_i carries phi.Qtot -
+        psi_i.Qtot (its MPO ends in that auxiliary quantum number).  Terms on the same
+        psi_i run as one MPO (mpo_sum), so each step costs one two-site application and
+        one environment update per distinct psi_i.  Returns the largest discarded weight
+        of the last sweep."""
+        if self._pool is not None:
+            return self._fit(phi, terms, Dmax, sweeps, eps_svd, self._pool)
+        with self._host_pool():
+            return self._fit(phi, terms, Dmax, sweeps, eps_svd, self._pool)
+
+    @contextlib.contextmanager
+    def _host_pool(self):
+        """one SectorPool for a batch of fits (opening one changes OpenBLAS's thread count)"""
+        if self._pool is not None:
+            yield self._pool
+            return
+        self._pool = SectorPool(self.threads)
+        try:
+            yield self._pool
+        finally:
+            self._pool.close()
+            self._pool = None
+
+    def _fit(self, phi, terms, Dmax, sweeps, eps_svd, pool):
+        sym, nq, qloc, L = self.sym, self.sym.nq, self.model.qloc, self.model.L
+        right_canonical(phi, pool)
+        ctx = self.ctx if getattr(self.ctx, "device", -1) >= 0 else None
+        groups = {}
+        for W, psi, c in terms:
+            groups.setdefault(id(psi), (psi, []))[1].append((W, c))
+        plan = []
+        for psi, lst in groups.values():
+            dq = tuple(int(a - b) for a, b in zip(phi.Qtot, psi.Qtot))
+            if len(lst) == 1:
+                W, c = lst[0]
+            else:
+                W, c = mpo_sum([w for w, _ in lst], [c for _, c in lst], dq), 1.0
+            # contract_R's right boundary: rows the ket's total charge, columns the bra's
+            RT = Blocks.from_entries(nq, [(0, tuple(psi.Qtot), tuple(phi.Qtot), dq, np.ones((1, 1)))], tripod=True)
+            plan.append((W, psi, c, RT))
+        nt = len(plan)
+        envL = [[None] * (L + 1) for _ in range(nt)]
+        envR = [[None] * (L + 1) for _ in range(nt)]
+        for t, (W, psi, _, RT) in enumerate(plan):
+            envL[t][0] = left_vacuum(sym)
+            envR[t][L] = RT
+            for l in range(L - 1, 1, -1):
+                envR[t][l] = self._env("R", envR[t][l + 1], phi.A[l], W[l], psi.A[l])
+        disc_max = 0.0
+        two_site = {}
+        for _ in range(sweeps):
+            disc_max = 0.0
+            for move, bonds in (("right", range(L - 1)), ("left", range(L - 2, -1, -1))):
+                for l in bonds:
+                    din, dout = _dims_of(phi.A[l], "in"), _dims_of(phi.A[l + 1], "out")
+                    Vb, comb = two_site_layout(sym, qloc, qloc, din, dout, nq)
+                    x = np.zeros(Vb.data.size)
+                    for t, (W, psi, c, _) in enumerate(plan):
+                        # the sources do not change during the fit: their two-site tensors are made once
+                        Vk = two_site.get((t, l))
+                        if Vk is None:
+                            Vk = two_site[(t, l)] = contract_two_sites(sym, psi.A[l], psi.A[l + 1], qloc, qloc, nq,
+                                                                       ctx=ctx, pool=pool)
+                        x += c * self._apply(envL[t][l], envR[t][l + 2], W[l], W[l + 1], Vk, Vb)
+                    Vb.data[:] = x
+                    nrm = float(np.linalg.norm(x))
+                    A1, A2, disc, dmid = split_two_site(Vb, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
+                                                        eps_svd=eps_svd, factor=self.factor,
+                                                        native=self.factor == "eigh", ctx=ctx, pool=pool)
+                    # the split renormalises the kept singular values: the fitted state keeps its norm
+                    scale = nrm * np.sqrt(max(0.0, 1.0 - disc))
+                    (A2 if move == "right" else A1).data[:] *= scale
+                    phi.A[l], phi.A[l + 1] = A1, A2
+                    phi.dims[l + 1] = dmid
+                    disc_max = max(disc_max, disc)
+                    for t, (W, psi, _, _) in enumerate(plan):
+                        if move == "right":
+                            envL[t][l + 1] = self._env("L", envL[t][l], A1, W[l], psi.A[l])
+                        else:
+                            envR[t][l + 1] = self._env("R", envR[t][l + 2], A2, W[l + 1], psi.A[l + 1])
+        return disc_max
+
+    # ---- the Chebyshev recursion of MPS
+    def chebyshev_moments(self, psi0, nmom: int, a: float, b: float, Dmax: int, sweeps: int = 2,
+                          eps_svd: float = 1e-14):
+        """mu_n = <psi0| T_n((H - b)/a) |psi0>, n < nmom, the vectors t_n fitted as MPS of at
+        most Dmax states per bond; returns (mu, info)"""
+        with self._host_pool():
+            return self._chebyshev(psi0, nmom, a, b, Dmax, sweeps, eps_svd)
+
+    def _chebyshev(self, psi0, nmom, a, b, Dmax, sweeps, eps_svd):
+        H = self.model.W
+        mu = np.zeros(nmom)
+        t0 = copy_mps(psi0)
+        mu[0] = self.overlap(psi0, t0)
+        disc = []
+        if nmom == 1:
+            return mu, {"discarded": disc}
+        t1 = copy_mps(t0)
+        disc.append(self.fit(t1, [(H, t0, 1.0 / a), (self.I, t0, -b / a)], Dmax, sweeps, eps_svd))
+        mu[1] = self.overlap(psi0, t1)
+        tp, tc = t0, t1
+        for n in range(2, nmom):
+            tn = copy_mps(tc)
+            disc.append(self.fit(tn, [(H, tc, 2.0 / a), (self.I, tc, -2.0 * b / a), (self.I, tp, -1.0)], Dmax,
+                                 sweeps, eps_svd))
+            mu[n] = self.overlap(psi0, tn)
+            tp, tc = tc, tn
+        return mu, {"discarded": disc, "max_bond": max(sum(d.values()) for d in tc.dims)}
