@@ -229,8 +229,10 @@ int vmps_tune_cache_clear(void);
  * 256, split-K 1..8), bypassing the tuner; the plan is rebuilt on next use.    */
 int vmps_pivot_set_tiling(vmps_pivot* p, int ncap1, int ncap2, int splitk);
 
-/* HxV with host buffers in the compact layout of V: Vout = H * Vin./* HxV with host buffers in the compact layout of V: Vout = H * Vin.
- * Host->device copy, the product and the device->host copy all happen here.
+/* HxV with host buffers in the compact layout of V: Vout = H * Vin.
+ * Host->device copy, the product and the device->host copy all happen here
+ * (split-precision plans of large vectors overlap the copies of some chunks with
+ * the compute of others).
  * Replaces HxV(PivotMatrixN, Vin, Vout), pivot/DmrgPivotMatrix1.h:124-129.  */
 int vmps_hxv(vmps_pivot* p, const double* vin, double* vout, int precision);
 
