@@ -899,6 +899,27 @@ def main():
     barrier(dist)
     e2e = world * args.steps / e2e_s
 
+    # ---- the pivot's task list matched on the GPU (default) and on the host: pivot creation
+    # (matching, plan-independent set-up, L/R upload) with each, median of 3
+    builder = {}
+    chains = {}
+    for name, env in (("device", None), ("host", "1")):
+        if env:
+            os.environ["VMPS_HOST_BUILDER"] = env
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            Hb = PivotMatrix2(ctx, model.sym, Lenv, Renv, W1, W2, V)
+            ts.append(time.perf_counter() - t0)
+            chains[name] = Hb.chains()
+            Hb.close()
+        os.environ.pop("VMPS_HOST_BUILDER", None)
+        builder[name + "_pivot_create_ms"] = 1e3 * float(np.median(ts))
+    builder["chains"] = int(len(chains["device"][0]))
+    builder["identical_chains"] = bool(np.array_equal(chains["device"][0], chains["host"][0]) and
+                                       np.array_equal(chains["device"][1], chains["host"][1]) and
+                                       chains["device"][2] == chains["host"][2])
+
     # ---- split vs FP64 numerics on this input
     h64 = H.apply(v0, "fp64")
     hsp = H.apply(v0, args.precision)
@@ -1000,6 +1021,7 @@ def main():
             "gpu_launches": ((3 + (1 if tune and tune["splitk"] > 1 else 0)) if args.precision == "bf16x3" else 2)
                             * args.steps,
             "autotune": {"headline_pivot": tune, "small_pivots": tune_small},
+            "task_builder": builder,
             "fp64": {"value": world * 1000.0 / ms64, "unit": "HxV/s", "ms_per_step": ms64,
                      "phase2_ms": ms64_2, "flops_executed": st64["flops_executed"]},
             "split_over_fp64": ms64 / ms,

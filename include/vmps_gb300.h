@@ -202,6 +202,12 @@ int vmps_pivot_destroy(vmps_pivot* p);
 int vmps_pivot_stats(const vmps_pivot* p, int precision, vmps_plan_stats* out);
 /* number of doubles of a PivotVector in the compact layout of V */
 int vmps_pivot_dim(const vmps_pivot* p, int64_t* out);
+/* The task list of a pivot as chains out += c * L[x] * V[y] * R[z] (block indices of
+ * the tables the pivot was made from), in the builder's order, and the reference's
+ * task count: the precalc_blockStructure result of the pivot
+ * (tensors/DmrgIndexGymnastics.h:487-590, 699-856).  cap = 0 returns the count only;
+ * otherwise idx holds 4 entries (out, x, y, z) and coef one per chain.               */
+int vmps_pivot_chains(const vmps_pivot* p, int64_t cap, int64_t* n, int64_t* idx, double* coef, int64_t* n_tasks);
 
 /* Autotuner of the split-precision grouped GEMM (the reference picks a product
  * order per chain, DmrgExternal.h:141-215; here the tile shape of the whole

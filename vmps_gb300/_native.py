@@ -127,6 +127,7 @@ _PROTOS = [
     ("vmps_pivot_destroy", C.c_int, [C.c_void_p]),
     ("vmps_pivot_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(vmps_plan_stats)]),
     ("vmps_pivot_dim", C.c_int, [C.c_void_p, i64p]),
+    ("vmps_pivot_chains", C.c_int, [C.c_void_p, C.c_int64, i64p, i64p, f64p, i64p]),
     ("vmps_hxv", C.c_int, [C.c_void_p, f64p, f64p, C.c_int]),
     ("vmps_hxv_multi", C.c_int, [C.c_void_p, f64p, f64p, C.c_int, C.c_int]),
     ("vmps_two_site_contract", C.c_int, [C.c_void_p, C.POINTER(vmps_symmetry), C.POINTER(vmps_blocks), f64p,

@@ -1138,6 +1138,15 @@ static int pivot_create_common(vmps_ctx* ctx, const Symmetry& sym, const vmps_bl
     return 0;
 }
 
+// The two-site task list of an abelian pivot is matched on the GPU of a device
+// context (builder.cu: the same chains in the same order as the host builder);
+// VMPS_HOST_BUILDER=1 keeps it on the host.
+static bool device_builder(const vmps_ctx* c, const Symmetry& sym) {
+    if (!c || c->device < 0 || sym.nonabelian()) return false;
+    const char* v = std::getenv("VMPS_HOST_BUILDER");
+    return !(v && *v && std::strcmp(v, "0") != 0);
+}
+
 static void pivot_finish(vmps_pivot* p, const double* Ldata, const double* Rdata) {
     // SU(2): fold sqrt(w_out / w_in) into each chain (weighted dot -> plain dot)
     p->vscale.assign(p->Vt.n, 1.0);
@@ -1246,7 +1255,8 @@ int vmps_pivot2_create(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_bloc
     std::unique_ptr<vmps_pivot> p;
     pivot_create_common(ctx, sym, L, Ldata, R, Rdata, V, p);
     MpoView W1 = parse_mpo(sym, W12), W2 = parse_mpo(sym, W34);
-    p->cs = build_pivot2(sym, p->Lt, p->Rt, W1, W2, p->Vt);
+    p->cs = device_builder(ctx, sym) ? build_pivot2_device(ctx->stream, sym, p->Lt, p->Rt, W1, W2, p->Vt)
+                                     : build_pivot2(sym, p->Lt, p->Rt, W1, W2, p->Vt);
     pivot_finish(p.get(), Ldata, Rdata);
     *out = p.release();
     API_END
@@ -1497,6 +1507,23 @@ int vmps_pivot_stats(const vmps_pivot* pc, int prec, vmps_plan_stats* out) {
     DevPlan& dp = get_plan(p, prec);
     fill_stats(p->cs, dp.plan, prec, out);
     API_END
+}
+
+int vmps_pivot_chains(const vmps_pivot* p, int64_t cap, int64_t* n, int64_t* idx, double* coef, int64_t* n_tasks) {
+    if (!p || !n) return set_err(VMPS_E_ARG, "null argument");
+    const auto& ch = p->cs.chains;
+    *n = (int64_t)ch.size();
+    if (n_tasks) *n_tasks = p->cs.n_tasks;
+    if (cap <= 0) return VMPS_OK;
+    if (cap < *n || !idx || !coef) return set_err(VMPS_E_ARG, "chain buffers smaller than the chain list");
+    for (size_t i = 0; i < ch.size(); ++i) {
+        idx[4 * i] = ch[i].out;
+        idx[4 * i + 1] = ch[i].x;
+        idx[4 * i + 2] = ch[i].y;
+        idx[4 * i + 3] = ch[i].z;
+        coef[i] = ch[i].c;
+    }
+    return VMPS_OK;
 }
 
 int vmps_pivot_dim(const vmps_pivot* p, int64_t* out) {

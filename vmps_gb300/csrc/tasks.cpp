@@ -222,6 +222,7 @@ MpoView parse_mpo(const Symmetry& sym, const vmps_mpo_site* W) {
 static inline double chain_flops(double m, double k, double n, double p) {
     return 2.0 * std::min(m * k * n + m * n * p, k * n * p + m * k * p);
 }
+double chain_flops_ref(double m, double k, double n, double p) { return chain_flops(m, k, n, p); }
 
 // ===========================================================================
 // 1-site effective Hamiltonian (PivotMatrix1)

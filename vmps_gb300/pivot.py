@@ -73,6 +73,17 @@ class _Pivot:
         N.check(N.lib().vmps_pivot_dim(self._h, C.byref(n)))
         return n.value
 
+    def chains(self):
+        """(idx, coef, n_tasks): the pivot's task list, idx rows (out, x, y, z)"""
+        n, nt = C.c_int64(), C.c_int64()
+        N.check(N.lib().vmps_pivot_chains(self._h, 0, C.byref(n), None, None, C.byref(nt)))
+        idx = np.zeros((max(n.value, 1), 4), dtype=np.int64)
+        coef = np.zeros(max(n.value, 1))
+        if n.value:
+            N.check(N.lib().vmps_pivot_chains(self._h, n.value, C.byref(n), idx.ctypes.data_as(N.i64p),
+                                              coef.ctypes.data_as(N.f64p), C.byref(nt)))
+        return idx[:n.value], coef[:n.value], nt.value
+
     def stats(self, precision="fp64") -> dict:
         s = N.vmps_plan_stats()
         N.check(N.lib().vmps_pivot_stats(self._h, _prec(precision), C.byref(s)))
