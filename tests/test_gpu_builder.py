@@ -1,15 +1,16 @@
-"""The device task-list builder of two-site pivots (builder.cu; precalc_blockStructure,
-tensors/DmrgIndexGymnastics.h:699-856): on a device context an abelian two-site pivot
-matches its chains on the GPU; with VMPS_HOST_BUILDER=1 the host builder makes them.
-Both give the same chain list in the same order (block indices and coefficients bit
-for bit) and the same reference task count, so the plans and the HxV bits agree too:
-Hubbard U(1)xU(1) pivots of the C2 chain, a Heisenberg U(1) pivot, and a union pivot
-(three quantum-number components, two sectors) of the C5 spectral workload."""
+"""The device task-list builder of one- and two-site pivots (builder.cu;
+precalc_blockStructure, tensors/DmrgIndexGymnastics.h:487-590 and :699-856): on a
+device context an abelian pivot matches its chains on the GPU; with
+VMPS_HOST_BUILDER=1 the host builder makes them.  Both give the same chain list in the
+same order (block indices and coefficients bit for bit) and the same reference task
+count, so the plans and the HxV bits agree too: Hubbard U(1)xU(1) pivots of the C2
+chain (two-site and one-site), Heisenberg U(1) pivots, and a union pivot (three
+quantum-number components, two sectors) of the C5 spectral workload."""
 import numpy as np
 import pytest
 
 from vmps_gb300 import models
-from vmps_gb300.pivot import PivotMatrix2
+from vmps_gb300.pivot import PivotMatrix1, PivotMatrix2
 from vmps_gb300.workloads import heisenberg_two_site, hubbard_two_site
 
 pytestmark = pytest.mark.gpu
@@ -67,5 +68,18 @@ def test_device_builder_equals_host_builder_union(gpu_ctx, monkeypatch):
     parts = [sp.sector(s) for s in ("up", "dn")]
     Hh, Hd = _both(monkeypatch, lambda: UnionPivot2(gpu_ctx, model.sym, model.W[l], model.W[l + 1], parts))
     _same(Hh.H, Hd.H, np.random.default_rng(3).standard_normal(Hh.H.dim))
+    Hh.close()
+    Hd.close()
+
+
+@pytest.mark.parametrize("case", ["hubbard", "heis"])
+def test_device_builder_equals_host_builder_one_site(gpu_ctx, monkeypatch, case):
+    from helpers import pivot1_case
+    if case == "hubbard":
+        model, mps, Lenv, Renv, W, V = pivot1_case("hubb", L=24, D=512, site=11, seed=5, profile="gaussian")
+    else:
+        model, mps, Lenv, Renv, W, V = pivot1_case("heis", L=24, D=256, site=11, seed=6, profile="gaussian")
+    Hh, Hd = _both(monkeypatch, lambda: PivotMatrix1(gpu_ctx, model.sym, Lenv, Renv, W, V))
+    _same(Hh, Hd, np.random.default_rng(4).standard_normal(Hh.dim))
     Hh.close()
     Hd.close()

@@ -1,23 +1,28 @@
-// Device task-list builder of the two-site effective Hamiltonian (abelian
-// symmetries): the matching of precalc_blockStructure for PivotMatrix2
-// (tensors/DmrgIndexGymnastics.h:699-856, its AAWWAA core :198-262) on the GPU.
+// Device task-list builder of the one- and two-site effective Hamiltonians
+// (abelian symmetries): the matching of precalc_blockStructure for PivotMatrix1 and
+// PivotMatrix2 (tensors/DmrgIndexGymnastics.h:487-590 with LAWA :32-77, and :699-856
+// with its AAWWAA core :198-262) on the GPU.
 //
-// It produces exactly the chain list of the host builder build_pivot2 (tasks.cpp),
-// in the same order: the host loop nest is
+// It produces exactly the chain list of the host builders build_pivot1 / build_pivot2
+// (tasks.cpp), in the same order.  The two-site loop nest is
 //     for (s1, s2, k12) with q(s2) + q(k12) = q(s1), for (s3, s4, k34) likewise,
 //       for the combined indices s1s3 of (s1, s3) and s2s4 of (s2, s4),
 //         for the L keys qL (in key order) with a two-site block (s1s3, Lin, Lin + q(s1s3)),
 //           q24 = the block (s2s4, Lout, Lout + q(s2s4)); the MPO nonzeros of W12 between
 //           Lmid and Lmid + q(k12), of W34 on to Rmid; the R key (qRin, qRout, Rmid);
 //           for the W12 x W34 nonzero pairs joined on the inner auxiliary index:
-//             chain {out q13, L block (qL, row12), in q24, R block (qR, col34), val12 * val34}.
-// The host enumerates the (s1, s2, k12, s3, s4, k34, s1s3, s2s4) combinations (a few
+//             chain {out q13, L block (qL, row12), in q24, R block (qR, col34), val12 * val34};
+// the one-site nest is the same with one MPO site: for (s1, s2, k), for qL, the blocks
+// (s1, Lin, Lin + q(s1)) and (s2, Lout, Lout + q(s2)), the nonzeros of W between Lmid
+// and Lmid + q(k), the R key, a task when one nonzero has both its L and R blocks.
+// The host enumerates the combinations of the local and operator indices (a few
 // hundred); one device thread takes one (combination, qL) candidate, so the candidate
 // index is the position in the host order.  A counting pass sums each thread block's
 // chains, one thread scans the block sums, and the emitting pass repeats the matching,
-// scans its block and writes every chain at its place.  The lookups (two-site blocks,
-// MPO nonzeros, R keys) are open-addressing hash tables built on the host with the
-// same hash the kernels probe with; every probe sequence is bounded by its table size.
+// scans its block and writes every chain at its place.  The lookups (blocks of the
+// vector, MPO nonzeros, R keys) are open-addressing hash tables built on the host with
+// the same hash the kernels probe with; every probe sequence is bounded by its table
+// size.  The tables travel in one upload into one device arena.
 #include "engine.hpp"
 
 #include <cuda_runtime.h>
@@ -25,6 +30,8 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <functional>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -82,8 +89,8 @@ struct Tables {
     // MPO sites: keys, hash slots -> key index, nonzeros
     const WKey* w_key[2]; const int32_t* w_slot[2]; uint32_t w_mask[2];
     const int32_t* nz_row[2]; const int32_t* nz_col[2]; const double* nz_val[2];
-    const DQN* qop[2];
-    // combined basis: QN of every combined index
+    const DQN* qop[2]; const DQN* qloc[2];
+    // combined basis (two-site): QN of every combined index
     const DQN* q_of; int ncomb;
 };
 // (s1, s2, k12, s3, s4, k34, s1s3, s2s4) of the host enumeration
@@ -137,10 +144,10 @@ __global__ void match_blocks_kernel(Tables t, int64_t* in13, int64_t* at24) {
 
 constexpr int kBuildThreads = 256;
 
-// one candidate (combination, qL): its chains counted (emit = false) or written from `at`
+// one two-site candidate (combination, qL): its chains counted (EMIT false) or written from `at`
 template <bool EMIT>
-__device__ inline int candidate(const Tables& t, const Combo* combos, const int64_t* in13, const int64_t* at24,
-                                int64_t idx, int64_t at, Chain* out, int* task) {
+__device__ inline int candidate2(const Tables& t, const Combo* combos, const int64_t* in13, const int64_t* at24,
+                                 int64_t idx, int64_t at, Chain* out, int* task) {
     const Combo cb = combos[idx / t.nkeys];
     const int qL = (int)(idx % t.nkeys);
     const int64_t q13 = in13[(int64_t)cb.s13 * t.nkeys + qL];
@@ -172,6 +179,44 @@ __device__ inline int candidate(const Tables& t, const Combo* combos, const int6
     return n;
 }
 
+// one one-site candidate ((s1, s2, k), qL)
+template <bool EMIT>
+__device__ inline int candidate1(const Tables& t, const Combo* combos, int64_t idx, int64_t at, Chain* out,
+                                 int* task) {
+    const Combo cb = combos[idx / t.nkeys];
+    const int qL = (int)(idx % t.nkeys);
+    const DQN lin = t.l_in[qL], lout = t.l_out[qL], lmid = t.l_mid[qL];
+    const DQN rout = qsum(lin, t.qloc[0][cb.s1]);
+    const int64_t qbra = find_v(t, cb.s1, lin, rout);
+    if (qbra < 0) return 0;
+    const DQN rin = qsum(lout, t.qloc[0][cb.s2]);
+    const int64_t qket = find_v(t, cb.s2, lout, rin);
+    if (qket < 0) return 0;
+    const DQN rmid = qsum(lmid, t.qop[0][cb.k12]);
+    const WKey* e = find_w(t, 0, cb.s1, cb.s2, cb.k12, lmid, rmid);
+    if (!e) return 0;
+    if (!qeq(qsum(rin, rmid), rout)) return 0;      // abelian triangle(Rin, Rmid, Rout)
+    const int qR = find_r(t, rin, rout, rmid);
+    if (qR < 0) return 0;
+    int n = 0;
+    for (int a = e->start; a < e->start + e->count; ++a) {
+        const int64_t la = aux_at(t.l_aux_off, t.l_aux, qL, t.nz_row[0][a]);
+        const int64_t rb = aux_at(t.r_aux_off, t.r_aux, qR, t.nz_col[0][a]);
+        if (la < 0 || rb < 0) continue;
+        if (EMIT) out[at + n] = Chain{qbra, la, qket, rb, t.nz_val[0][a]};
+        ++n;
+    }
+    if (n > 0) *task = 1;   // a task when one nonzero has both blocks
+    return n;
+}
+
+template <int SITES, bool EMIT>
+__device__ inline int candidate(const Tables& t, const Combo* combos, const int64_t* in13, const int64_t* at24,
+                                int64_t idx, int64_t at, Chain* out, int* task) {
+    if (SITES == 2) return candidate2<EMIT>(t, combos, in13, at24, idx, at, out, task);
+    return candidate1<EMIT>(t, combos, idx, at, out, task);
+}
+
 // exclusive scan of one value per thread over the block (kBuildThreads threads)
 __device__ inline int block_scan(int v, int* sh, int* total) {
     const int tid = threadIdx.x;
@@ -189,13 +234,14 @@ __device__ inline int block_scan(int v, int* sh, int* total) {
     return incl - v;
 }
 
+template <int SITES>
 __global__ void __launch_bounds__(kBuildThreads) count_kernel(Tables t, const Combo* combos, int64_t ncand,
                                                               const int64_t* in13, const int64_t* at24,
                                                               int64_t* block_sum, unsigned long long* tasks) {
     __shared__ int sh[kBuildThreads];
     const int64_t idx = blockIdx.x * (int64_t)kBuildThreads + threadIdx.x;
     int task = 0, n = 0;
-    if (idx < ncand) n = candidate<false>(t, combos, in13, at24, idx, 0, nullptr, &task);
+    if (idx < ncand) n = candidate<SITES, false>(t, combos, in13, at24, idx, 0, nullptr, &task);
     int total = 0;
     block_scan(n, sh, &total);
     if (threadIdx.x == 0) block_sum[blockIdx.x] = total;
@@ -215,6 +261,7 @@ __global__ void scan_sums_kernel(int64_t* block_sum, int64_t nb, int64_t* total)
     *total = acc;
 }
 
+template <int SITES>
 __global__ void __launch_bounds__(kBuildThreads) emit_kernel(Tables t, const Combo* combos, int64_t ncand,
                                                              const int64_t* in13, const int64_t* at24,
                                                              const int64_t* block_off, int64_t cap, Chain* out,
@@ -222,7 +269,7 @@ __global__ void __launch_bounds__(kBuildThreads) emit_kernel(Tables t, const Com
     __shared__ int sh[kBuildThreads];
     const int64_t idx = blockIdx.x * (int64_t)kBuildThreads + threadIdx.x;
     int task = 0, n = 0;
-    if (idx < ncand) n = candidate<false>(t, combos, in13, at24, idx, 0, nullptr, &task);
+    if (idx < ncand) n = candidate<SITES, false>(t, combos, in13, at24, idx, 0, nullptr, &task);
     int total = 0;
     const int pre = block_scan(n, sh, &total);
     const int64_t at = block_off[blockIdx.x] + pre;
@@ -231,34 +278,43 @@ __global__ void __launch_bounds__(kBuildThreads) emit_kernel(Tables t, const Com
         atomicExch(overflow, 1);
         return;
     }
-    candidate<true>(t, combos, in13, at24, idx, at, out, &task);
+    candidate<SITES, true>(t, combos, in13, at24, idx, at, out, &task);
 }
 
 void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string("device builder: ") + what + ": " + cudaGetErrorString(e));
 }
 
-// device copies of the tables, freed at scope exit
-struct DevBufs {
-    std::vector<void*> ptrs;
-    ~DevBufs() {
-        for (void* p : ptrs) cudaFree(p);
+// The tables of one build in one device allocation: host arrays packed into a staging
+// buffer at 256-byte aligned offsets (one upload), scratch placed after them.
+struct Arena {
+    std::vector<char> host;
+    size_t scratch = 0;    // bytes of device-only scratch after the uploaded part
+    char* dev = nullptr;
+    struct Fix { size_t off; bool scratch; std::function<void(char*)> set; };
+    std::vector<Fix> fixes;
+    ~Arena() {
+        if (dev) cudaFree(dev);
+    }
+    static size_t align(size_t x) { return (x + 255) / 256 * 256; }
+    template <typename T>
+    void put(const std::vector<T>& v, const T*& slot) {
+        const size_t off = align(host.size());
+        host.resize(off + std::max<size_t>(v.size(), 1) * sizeof(T), 0);
+        if (!v.empty()) std::memcpy(host.data() + off, v.data(), v.size() * sizeof(T));
+        fixes.push_back(Fix{off, false, [&slot](char* p) { slot = reinterpret_cast<const T*>(p); }});
     }
     template <typename T>
-    T* up(const std::vector<T>& v, cudaStream_t st) {
-        void* p = nullptr;
-        const size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
-        ck(cudaMalloc(&p, bytes), "cudaMalloc");
-        ptrs.push_back(p);
-        if (!v.empty()) ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
-        return static_cast<T*>(p);
+    void reserve(size_t n, T*& slot) {
+        scratch = align(scratch);
+        fixes.push_back(Fix{scratch, true, [&slot](char* p) { slot = reinterpret_cast<T*>(p); }});
+        scratch += std::max<size_t>(n, 1) * sizeof(T);
     }
-    template <typename T>
-    T* alloc(size_t n) {
-        void* p = nullptr;
-        ck(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc");
-        ptrs.push_back(p);
-        return static_cast<T*>(p);
+    void upload(cudaStream_t st) {
+        const size_t up = align(host.size());
+        ck(cudaMalloc((void**)&dev, up + scratch + 256), "cudaMalloc");
+        ck(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, st), "upload");
+        for (const Fix& f : fixes) f.set(dev + (f.scratch ? up + f.off : f.off));
     }
 };
 
@@ -282,19 +338,20 @@ DQN dq(const QN& q) {
     return d;
 }
 
-}  // namespace
-
-ChainSet build_pivot2_device(CUstream_st* st, const Symmetry& sym, const BlockTable& L, const BlockTable& R,
-                             const MpoView& W12, const MpoView& W34, const BlockTable& V) {
+// the matching of `nsites` MPO sites (W[0..nsites)) against L, R and the vector V
+ChainSet build_device(cudaStream_t st, const Symmetry& sym, const BlockTable& L, const BlockTable& R,
+                      const MpoView* const* W, int nsites, const BlockTable& V) {
     if (sym.nonabelian()) throw std::invalid_argument("the device builder takes abelian symmetries");
     ChainSet cs;
     const TripodView Lv = make_tripod_view(L), Rv = make_tripod_view(R);
-    const CombinedBasis cb = combine_bases(sym, W12.qloc, W34.qloc);
+    CombinedBasis cb;
+    if (nsites == 2) cb = combine_bases(sym, W[0]->qloc, W[1]->qloc);
     const int nkeys = (int)Lv.keys.size();
+    make_bipeds_view(V, nsites == 2 ? cb.n : W[0]->nloc);   // throws on a duplicate block
     if (nkeys == 0 || V.n == 0 || Rv.keys.empty()) return cs;
-    DevBufs B;
+    Arena A;
     Tables t{};
-    // two-site blocks (duplicates are refused as by make_bipeds_view)
+    // blocks of the vector
     std::vector<int32_t> v_leg((size_t)V.n);
     std::vector<DQN> v_qin((size_t)V.n), v_qout((size_t)V.n);
     std::vector<uint64_t> hv((size_t)V.n);
@@ -304,9 +361,8 @@ ChainSet build_pivot2_device(CUstream_st* st, const Symmetry& sym, const BlockTa
         v_qout[i] = dq(V.qout[i]);
         hv[i] = hash_v(v_leg[i], v_qin[i], v_qout[i]);
     }
-    make_bipeds_view(V, cb.n);   // throws on a duplicate block
     const auto v_slot = make_slots(hv, t.v_mask);
-    t.v_leg = B.up(v_leg, st); t.v_qin = B.up(v_qin, st); t.v_qout = B.up(v_qout, st); t.v_slot = B.up(v_slot, st);
+    A.put(v_leg, t.v_leg); A.put(v_qin, t.v_qin); A.put(v_qout, t.v_qout); A.put(v_slot, t.v_slot);
     // L and R keys with their auxiliary indices
     auto keys = [&](const TripodView& tv, std::vector<DQN>& qi, std::vector<DQN>& qo, std::vector<DQN>& qm,
                     std::vector<int32_t>& off, std::vector<int64_t>& aux) {
@@ -327,16 +383,16 @@ ChainSet build_pivot2_device(CUstream_st* st, const Symmetry& sym, const BlockTa
     std::vector<uint64_t> hr(ri.size());
     for (size_t i = 0; i < ri.size(); ++i) hr[i] = hash_r(ri[i], ro[i], rm[i]);
     const auto r_slot = make_slots(hr, t.r_mask);
-    t.l_in = B.up(li, st); t.l_out = B.up(lo, st); t.l_mid = B.up(lm, st);
-    t.l_aux_off = B.up(loff, st); t.l_aux = B.up(laux, st); t.nkeys = nkeys;
-    t.r_in = B.up(ri, st); t.r_out = B.up(ro, st); t.r_mid = B.up(rm, st); t.r_slot = B.up(r_slot, st);
-    t.r_aux_off = B.up(roff, st); t.r_aux = B.up(raux, st);
+    A.put(li, t.l_in); A.put(lo, t.l_out); A.put(lm, t.l_mid); A.put(loff, t.l_aux_off); A.put(laux, t.l_aux);
+    t.nkeys = nkeys;
+    A.put(ri, t.r_in); A.put(ro, t.r_out); A.put(rm, t.r_mid); A.put(r_slot, t.r_slot);
+    A.put(roff, t.r_aux_off); A.put(raux, t.r_aux);
     // MPO nonzeros by (s1, s2, k, qin, qout), each list in the host's order
-    const MpoView* W[2] = {&W12, &W34};
-    for (int w = 0; w < 2; ++w) {
-        std::vector<WKey> wk;
-        std::vector<int32_t> row, col;
-        std::vector<double> val;
+    std::vector<WKey> wk[2];
+    std::vector<int32_t> wrow[2], wcol[2], wslot[2];
+    std::vector<double> wval[2];
+    std::vector<DQN> wqop[2], wqloc[2];
+    for (int w = 0; w < nsites; ++w) {
         std::vector<uint64_t> hw;
         const MpoView& m = *W[w];
         for (int s1 = 0; s1 < m.nloc; ++s1)
@@ -347,60 +403,75 @@ ChainSet build_pivot2_device(CUstream_st* st, const Symmetry& sym, const BlockTa
                         e.s1 = s1; e.s2 = s2; e.k = k;
                         e.qin = dq(kv.first.q[0]);
                         e.qout = dq(kv.first.q[1]);
-                        e.start = (int32_t)row.size();
+                        e.start = (int32_t)wrow[w].size();
                         e.count = (int32_t)kv.second.size();
                         for (const MpoNz& z : kv.second) {
-                            row.push_back(z.row);
-                            col.push_back(z.col);
-                            val.push_back(z.val);
+                            wrow[w].push_back(z.row);
+                            wcol[w].push_back(z.col);
+                            wval[w].push_back(z.val);
                         }
                         hw.push_back(hash_w(s1, s2, k, e.qin, e.qout));
-                        wk.push_back(e);
+                        wk[w].push_back(e);
                     }
-        const auto ws = make_slots(hw, t.w_mask[w]);
-        t.w_key[w] = B.up(wk, st); t.w_slot[w] = B.up(ws, st);
-        t.nz_row[w] = B.up(row, st); t.nz_col[w] = B.up(col, st); t.nz_val[w] = B.up(val, st);
-        std::vector<DQN> qop;
-        for (const QN& q : m.qop) qop.push_back(dq(q));
-        t.qop[w] = B.up(qop, st);
+        wslot[w] = make_slots(hw, t.w_mask[w]);
+        for (const QN& q : m.qop) wqop[w].push_back(dq(q));
+        for (const QN& q : m.qloc) wqloc[w].push_back(dq(q));
+        A.put(wk[w], t.w_key[w]); A.put(wslot[w], t.w_slot[w]);
+        A.put(wrow[w], t.nz_row[w]); A.put(wcol[w], t.nz_col[w]); A.put(wval[w], t.nz_val[w]);
+        A.put(wqop[w], t.qop[w]); A.put(wqloc[w], t.qloc[w]);
     }
     std::vector<DQN> qof;
     for (const QN& q : cb.q_of) qof.push_back(dq(q));
-    t.q_of = B.up(qof, st);
+    A.put(qof, t.q_of);
     t.ncomb = cb.n;
     // the combinations of the host loop nest, in its order
     std::vector<Combo> combos;
-    const int n12 = W12.nloc, n34 = W34.nloc;
-    for (int s1 = 0; s1 < n12; ++s1)
-    for (int s2 = 0; s2 < n12; ++s2)
-    for (int k12 = 0; k12 < W12.nop; ++k12) {
-        if (!sym.triangle(W12.qloc[s2], W12.qop[k12], W12.qloc[s1])) continue;
+    const MpoView& W1 = *W[0];
+    for (int s1 = 0; s1 < W1.nloc; ++s1)
+    for (int s2 = 0; s2 < W1.nloc; ++s2)
+    for (int k12 = 0; k12 < W1.nop; ++k12) {
+        if (!sym.triangle(W1.qloc[s2], W1.qop[k12], W1.qloc[s1])) continue;
+        if (nsites == 1) {
+            combos.push_back(Combo{s1, s2, k12, 0, 0, 0, 0, 0});
+            continue;
+        }
+        const MpoView& W2 = *W[1];
+        const int n34 = W2.nloc;
         for (int s3 = 0; s3 < n34; ++s3)
         for (int s4 = 0; s4 < n34; ++s4)
-        for (int k34 = 0; k34 < W34.nop; ++k34) {
-            if (!sym.triangle(W34.qloc[s4], W34.qop[k34], W34.qloc[s3])) continue;
+        for (int k34 = 0; k34 < W2.nop; ++k34) {
+            if (!sym.triangle(W2.qloc[s4], W2.qop[k34], W2.qloc[s3])) continue;
             for (const auto& m13 : cb.index[s1 * n34 + s3])
                 for (const auto& m24 : cb.index[s2 * n34 + s4])
                     combos.push_back(Combo{s1, s2, k12, s3, s4, k34, m13.second, m24.second});
         }
     }
     if (combos.empty()) return cs;
-    const Combo* d_combos = B.up(combos, st);
-    const int64_t nmatch = (int64_t)cb.n * nkeys;
-    int64_t* in13 = B.alloc<int64_t>((size_t)nmatch);
-    int64_t* at24 = B.alloc<int64_t>((size_t)nmatch);
-    match_blocks_kernel<<<(unsigned)std::min<int64_t>((nmatch + 255) / 256, 4096), 256, 0, st>>>(t, in13, at24);
-    ck(cudaGetLastError(), "match_blocks_kernel");
+    const Combo* d_combos = nullptr;
+    A.put(combos, d_combos);
+    const int64_t nmatch = nsites == 2 ? (int64_t)cb.n * nkeys : 0;
     const int64_t ncand = (int64_t)combos.size() * nkeys;
     const int64_t nblk = (ncand + kBuildThreads - 1) / kBuildThreads;
     if (nblk > 0x7fffffff) throw std::invalid_argument("device builder: too many candidates");
-    int64_t* bsum = B.alloc<int64_t>((size_t)nblk);
-    int64_t* total = B.alloc<int64_t>(1);
-    unsigned long long* tasks = B.alloc<unsigned long long>(1);
-    int* overflow = B.alloc<int>(1);
+    int64_t *in13 = nullptr, *at24 = nullptr, *bsum = nullptr, *total = nullptr;
+    unsigned long long* tasks = nullptr;
+    int* overflow = nullptr;
+    A.reserve((size_t)nmatch, in13);
+    A.reserve((size_t)nmatch, at24);
+    A.reserve((size_t)nblk, bsum);
+    A.reserve(1, total);
+    A.reserve(1, tasks);
+    A.reserve(1, overflow);
+    A.upload(st);
     ck(cudaMemsetAsync(tasks, 0, sizeof(unsigned long long), st), "memset");
     ck(cudaMemsetAsync(overflow, 0, sizeof(int), st), "memset");
-    count_kernel<<<(unsigned)nblk, kBuildThreads, 0, st>>>(t, d_combos, ncand, in13, at24, bsum, tasks);
+    if (nsites == 2) {
+        match_blocks_kernel<<<(unsigned)std::min<int64_t>((nmatch + 255) / 256, 4096), 256, 0, st>>>(t, in13, at24);
+        ck(cudaGetLastError(), "match_blocks_kernel");
+        count_kernel<2><<<(unsigned)nblk, kBuildThreads, 0, st>>>(t, d_combos, ncand, in13, at24, bsum, tasks);
+    } else {
+        count_kernel<1><<<(unsigned)nblk, kBuildThreads, 0, st>>>(t, d_combos, ncand, in13, at24, bsum, tasks);
+    }
     ck(cudaGetLastError(), "count_kernel");
     scan_sums_kernel<<<1, 1, 0, st>>>(bsum, nblk, total);
     ck(cudaGetLastError(), "scan_sums_kernel");
@@ -411,8 +482,15 @@ ChainSet build_pivot2_device(CUstream_st* st, const Symmetry& sym, const BlockTa
     ck(cudaStreamSynchronize(st), "count");
     cs.n_tasks = (int64_t)ntasks;
     if (nchains == 0) return cs;
-    Chain* out = B.alloc<Chain>((size_t)nchains);
-    emit_kernel<<<(unsigned)nblk, kBuildThreads, 0, st>>>(t, d_combos, ncand, in13, at24, bsum, nchains, out, overflow);
+    Chain* out = nullptr;
+    ck(cudaMalloc((void**)&out, sizeof(Chain) * (size_t)nchains), "cudaMalloc");
+    std::unique_ptr<Chain, decltype(&cudaFree)> out_guard(out, &cudaFree);
+    if (nsites == 2)
+        emit_kernel<2><<<(unsigned)nblk, kBuildThreads, 0, st>>>(t, d_combos, ncand, in13, at24, bsum, nchains, out,
+                                                                   overflow);
+    else
+        emit_kernel<1><<<(unsigned)nblk, kBuildThreads, 0, st>>>(t, d_combos, ncand, in13, at24, bsum, nchains, out,
+                                                                   overflow);
     ck(cudaGetLastError(), "emit_kernel");
     cs.chains.resize((size_t)nchains);
     int ovf = 0;
@@ -425,6 +503,20 @@ ChainSet build_pivot2_device(CUstream_st* st, const Symmetry& sym, const BlockTa
         cs.flops_reference += chain_flops_ref((double)L.rows[c.x], (double)L.cols[c.x], (double)V.cols[c.y],
                                               (double)R.cols[c.z]);
     return cs;
+}
+
+}  // namespace
+
+ChainSet build_pivot2_device(CUstream_st* st, const Symmetry& sym, const BlockTable& L, const BlockTable& R,
+                             const MpoView& W12, const MpoView& W34, const BlockTable& V) {
+    const MpoView* W[2] = {&W12, &W34};
+    return build_device(st, sym, L, R, W, 2, V);
+}
+
+ChainSet build_pivot1_device(CUstream_st* st, const Symmetry& sym, const BlockTable& L, const BlockTable& R,
+                             const MpoView& W, const BlockTable& V) {
+    const MpoView* Ws[1] = {&W};
+    return build_device(st, sym, L, R, Ws, 1, V);
 }
 
 }  // namespace vmps

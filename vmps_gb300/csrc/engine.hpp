@@ -89,9 +89,12 @@ ChainSet build_pivot2(const Symmetry& sym, const BlockTable& L, const BlockTable
                       const MpoView& W12, const MpoView& W34, const BlockTable& V);
 ChainSet build_pivot0(const Symmetry& sym, const BlockTable& L, const BlockTable& R,
                       const BlockTable& V);
-// the same chain list as build_pivot2, matched on the GPU (abelian symmetries; builder.cu)
+// the same chain lists as build_pivot2 / build_pivot1, matched on the GPU (abelian
+// symmetries; builder.cu)
 ChainSet build_pivot2_device(CUstream_st* st, const Symmetry& sym, const BlockTable& L, const BlockTable& R,
                              const MpoView& W12, const MpoView& W34, const BlockTable& V);
+ChainSet build_pivot1_device(CUstream_st* st, const Symmetry& sym, const BlockTable& L, const BlockTable& R,
+                             const MpoView& W, const BlockTable& V);
 // the reference's chain cost (DmrgExternal.h:147-159), for the builders' flop counts
 double chain_flops_ref(double m, double k, double n, double p);
 // contract_L / contract_R modes (tensors/DmrgContractions.h:13, :100-104, :245-249):

@@ -1240,7 +1240,8 @@ int vmps_pivot1_create(vmps_ctx* ctx, const vmps_symmetry* symd, const vmps_bloc
     std::unique_ptr<vmps_pivot> p;
     pivot_create_common(ctx, sym, L, Ldata, R, Rdata, V, p);
     MpoView Wv = parse_mpo(sym, W);
-    p->cs = build_pivot1(sym, p->Lt, p->Rt, Wv, p->Vt);
+    p->cs = device_builder(ctx, sym) ? build_pivot1_device(ctx->stream, sym, p->Lt, p->Rt, Wv, p->Vt)
+                                     : build_pivot1(sym, p->Lt, p->Rt, Wv, p->Vt);
     pivot_finish(p.get(), Ldata, Rdata);
     *out = p.release();
     API_END
