@@ -165,3 +165,86 @@ def test_charge_changing_fit_and_its_moments(spin, n):
         t0, t1 = t1, 2 * (H @ t1 - b * t1) / a - t0
         mref.append(ref @ t1)
     assert np.allclose(mu, mref, rtol=0, atol=1e-10 * mref[0])
+
+
+# ---- SU(2): reduced tensors; checked against the two-site pivot of the same state, whose
+# space is the whole sector when the bases are complete (weighted dots, coeff_dot = q)
+
+def _su2_pivot_reference(model, psi, l):
+    """(V, Heff(x), dot(x, y)) of psi's two-site pivot (l, l+1) on the oracle"""
+    import copy
+    from vmps_gb300.pivot import left_vacuum, right_target
+    from vmps_gb300.su2 import contract_two_sites_su2
+    sym, nq = model.sym, model.sym.nq
+    m = copy.deepcopy(psi).canonicalize(l, l + 1)
+    Lenv = left_vacuum(sym)
+    for j in range(l):
+        Lenv = oracle.contract_L(nq, Lenv, m.A[j], model.W[j], m.A[j], sym=sym)
+    Renv = right_target(sym, m.Qtot)
+    for j in range(model.L - 1, l + 1, -1):
+        Renv = oracle.contract_R(nq, Renv, m.A[j], model.W[j], m.A[j], sym=sym)
+    V, _ = contract_two_sites_su2(sym, m.A[l], m.A[l + 1], model.qloc, model.qloc)
+    piv = oracle.OraclePivot(2, nq, Lenv, Renv, V, model.W[l], model.W[l + 1], sym=sym)
+    w = np.concatenate([np.full(int(V.rows[b] * V.cols[b]), sym.dot_weight(tuple(V.qout[b]))) for b in range(V.n)])
+    order = np.concatenate([np.arange(V.offset[b], V.offset[b] + V.rows[b] * V.cols[b]) for b in range(V.n)])
+    wt = np.zeros(V.data.size)
+    wt[order] = w
+    return V.data.copy(), piv.hxv, (lambda x, y: float(np.sum(wt * x * y)))
+
+
+def _su2_compressor(model):
+    sym = model.sym
+    env = lambda side, E, Abra, W, Aket: (oracle.contract_L if side == "L" else oracle.contract_R)(
+        W.nq, E, Abra, W, Aket, sym=sym)
+    apply2 = lambda tsym, Le, Re, W1, W2, V, x: oracle.OraclePivot(2, tsym.nq, Le, Re, V, W1, W2, sym=tsym).hxv(x)
+    return Compressor(None, model, env=env, apply2=apply2)
+
+
+@pytest.mark.parametrize("kind", ["heisenberg_su2", "hubbard_su2xu1"])
+def test_su2_fit_and_moments_equal_the_complete_pivot(kind):
+    if kind == "heisenberg_su2":
+        L, l = 10, 4
+        model, Q = models.heisenberg_su2(L), (1,)
+    else:
+        L, l = 6, 2
+        model, Q = models.hubbard_su2xu1_lattice(L, [(i, i + 1, 1.0) for i in range(L - 1)], U=4.0), (1, L)
+    psi = RandomMPS(model, Q, 64, seed=7)
+    comp = _su2_compressor(model)
+    v, heff, dot = _su2_pivot_reference(model, psi, l)
+    hv = heff(v)
+    # the norm and energy of psi, and the fit of H psi
+    assert comp.overlap(psi, psi) == pytest.approx(dot(v, v), rel=1e-11)
+    phi = copy_mps(psi)
+    disc = comp.fit(phi, [(model.W, psi, 1.0)], Dmax=1000, sweeps=1)
+    assert disc < 1e-14
+    assert comp.overlap(phi, phi) == pytest.approx(dot(hv, hv), rel=1e-10)
+    assert comp.overlap(psi, phi) == pytest.approx(dot(v, hv), rel=1e-10)
+    # Chebyshev moments of whole MPS against the pivot's recursion
+    a, b = (8.0, -1.0) if kind == "heisenberg_su2" else (20.0, 2.0)
+    mu, _ = comp.chebyshev_moments(psi, 8, a, b, Dmax=1000, sweeps=1)
+    t0, t1 = v, (heff(v) - b * v) / a
+    ref = [dot(v, t0), dot(v, t1)]
+    for _ in range(2, 8):
+        t0, t1 = t1, 2 * (heff(t1) - b * t1) / a - t0
+        ref.append(dot(v, t1))
+    assert np.allclose(mu, ref, rtol=0, atol=1e-10 * abs(ref[0]))
+
+
+@pytest.mark.parametrize("kind", ["hubbard_u1xu1", "heisenberg_su2"])
+def test_truncated_fit_is_a_projection(kind):
+    """with fewer states than the target needs, the fit is the projection of H psi onto the
+    fitted MPS's own tangent: <phi|H|psi> = <phi|phi> (<phi|H|psi> by contract_L through
+    the chain), every bond keeps at most Dmax states (multiplets for SU(2))"""
+    if kind == "heisenberg_su2":
+        model = models.heisenberg_su2(12)
+        psi = RandomMPS(model, (1,), 32, seed=9)
+        comp = _su2_compressor(model)
+        Dmax = 6
+    else:
+        model, psi, comp = _setup(6, 64)
+        Dmax = 12
+    phi = copy_mps(psi)
+    disc = comp.fit(phi, [(model.W, psi, 1.0)], Dmax=Dmax, sweeps=3)
+    assert disc > 0
+    assert max(sum(d.values()) for d in phi.dims) <= Dmax
+    assert comp.matrix_element(phi, model.W, psi) == pytest.approx(comp.overlap(phi, phi), rel=1e-9)

@@ -8,7 +8,9 @@ HxV, the two-site contraction and the split on the GPU:
   moments of the MPS recursion equal the dense vectors and the dense recursion (FP64
   to 1e-11 / 1e-10; split precision within 1e-5 of the first moment);
 * on a longer chain (L=10, bond dimension 24, no truncation) the engine's fit equals
-  the same sweeps run on the oracle's contractions to 1e-10."""
+  the same sweeps run on the oracle's contractions to 1e-10;
+* SU(2) and SU(2) x U(1) reduced MPS: the fit of H psi and the moments equal the two-site
+  pivot of psi on the oracle when the bases are complete."""
 import numpy as np
 import pytest
 
@@ -91,3 +93,35 @@ def test_engine_charge_changing_start_and_moments(gpu_ctx, precision, tol):
         t0, t1 = t1, 2 * (H @ t1) / a - t0
         mref.append(ref @ t1)
     assert np.max(np.abs(mu - mref)) < tol * mref[0]
+
+
+@pytest.mark.parametrize("kind", ["heisenberg_su2", "hubbard_su2xu1"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("bf16x3", 1e-5)])
+def test_engine_su2_fit_and_moments_equal_the_complete_pivot(gpu_ctx, kind, precision, tol):
+    """SU(2) reduced MPS on the engine (SU(2) environments, tagged SU(2) x U(1) pivots,
+    the SU(2) two-site contraction on the GPU): with complete bases the fit of H psi and
+    the MPS Chebyshev moments equal the two-site pivot of psi on the oracle"""
+    from test_compress import _su2_pivot_reference
+    if kind == "heisenberg_su2":
+        L, l = 10, 4
+        model, Q = models.heisenberg_su2(L), (1,)
+        a, b = 8.0, -1.0
+    else:
+        L, l = 6, 2
+        model, Q = models.hubbard_su2xu1_lattice(L, [(i, i + 1, 1.0) for i in range(L - 1)], U=4.0), (1, L)
+        a, b = 20.0, 2.0
+    psi = RandomMPS(model, Q, 64, seed=7)
+    comp = Compressor(gpu_ctx, model, precision=precision)
+    v, heff, dot = _su2_pivot_reference(model, psi, l)
+    hv = heff(v)
+    phi = copy_mps(psi)
+    comp.fit(phi, [(model.W, psi, 1.0)], Dmax=1000, sweeps=1)
+    assert abs(comp.overlap(phi, phi) - dot(hv, hv)) < max(tol, 1e-10) * dot(hv, hv)
+    assert abs(comp.overlap(psi, phi) - dot(v, hv)) < max(tol, 1e-10) * abs(dot(hv, hv)) ** 0.5 * dot(v, v) ** 0.5
+    mu, _ = comp.chebyshev_moments(psi, 8, a, b, Dmax=1000, sweeps=1)
+    t0, t1 = v, (heff(v) - b * v) / a
+    ref = [dot(v, t0), dot(v, t1)]
+    for _ in range(2, 8):
+        t0, t1 = t1, 2 * (heff(t1) - b * t1) / a - t0
+        ref.append(dot(v, t1))
+    assert np.max(np.abs(mu - ref)) < tol * abs(ref[0])

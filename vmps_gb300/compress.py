@@ -1,7 +1,9 @@
 """MPS-level compression on the engine: variational fitting of a sum of operator-MPS
 products by two-site sweeps (MpsCompressor::prodCompress / polyCompress,
 solvers/MpsCompressor.h:961-1564), and the Chebyshev recursion of whole MPS built on
-it (polyIter, DmrgLinearAlgebra.h:550-566).  Abelian symmetries.
+it (polyIter, DmrgLinearAlgebra.h:550-566).  Abelian symmetries, and SU(2) (or SU(2) x U(1))
+for operators that keep the total quantum number (the SU(2) two-site contraction and split
+of su2.py, reduced tensors throughout).
 
 fit(phi, terms): phi ~ sum_i c_i O_i psi_i, with O_i an MPO (the Hamiltonian, or the
 identity for a plain MPS term).  phi is right-canonical with its centre on site 0; per
@@ -32,6 +34,7 @@ import numpy as np
 from .blocks import Blocks, MpoSite
 from .hostla import SectorPool
 from .mps import contract_two_sites, right_normalize, split_two_site, two_site_layout
+from .su2 import contract_two_sites_su2, split_two_site_su2
 from .pivot import EnvUpdate, PivotMatrix2, left_vacuum
 from .union import aux_tag, bra_ket_tag, concat_blocks, tag_blocks, tagged_symmetry
 
@@ -48,15 +51,17 @@ def identity_mpo(model) -> list:
     return W
 
 
-def mpo_sum(mpos: list, coefs: list, end_q) -> list:
+def mpo_sum(mpos: list, coefs: list, end_q, vac=None) -> list:
     """sum_i c_i O_i of MPOs (site lists) as one MPO: the auxiliary bases of the inner bonds
     side by side (the states of O_i after those of O_0..O_i-1 in each quantum-number
     sector), the boundary states shared, c_i on site 0's entries of O_i.  Every O_i starts
     in the vacuum state (index 0) and ends in state 0 of quantum number end_q (the charge
-    the operators carry); entries of the boundary sites that leave other boundary states
-    are never reached from the environments and are dropped."""
+    the operators carry; vac: the vacuum, all zeros by default, (1, ...) for SU(2)
+    components); entries of the boundary sites that leave other boundary states are never
+    reached from the environments and are dropped."""
     L, nq = len(mpos[0]), mpos[0][0].nq
-    vac, end_q = tuple(0 for _ in range(nq)), tuple(end_q)
+    vac = tuple(0 for _ in range(nq)) if vac is None else tuple(vac)
+    end_q = tuple(end_q)
     out = [MpoSite(nq, list(mpos[0][l].qloc), []) for l in range(L)]
     qops = [[] for _ in range(L)]
     base = [dict() for _ in range(L + 1)]      # bond -> {aux QN: states placed so far}
@@ -104,9 +109,10 @@ def copy_mps(psi):
 
 def right_canonical(psi, pool=None):
     """psi with sites 1..L-1 right-orthonormal (the factors pushed into site 0), in place"""
+    sym = psi.model.sym if psi.model.sym.nonabelian else None   # SU(2): the weighted normalisation
     carry = None
     for l in range(psi.L - 1, 0, -1):
-        psi.A[l], carry = right_normalize(psi.A[l], psi.model.sym.nq, carry, pool=pool)
+        psi.A[l], carry = right_normalize(psi.A[l], psi.model.sym.nq, carry, sym=sym, pool=pool)
     A = psi.A[0]
     for i in range(A.n):
         q = tuple(A.qout[i])
@@ -129,8 +135,6 @@ class Compressor:
     default: up to 16 cores)."""
 
     def __init__(self, ctx, model, precision="fp64", env=None, apply2=None, factor="svd", threads=None):
-        if model.sym.nonabelian:
-            raise ValueError("the compressor supports abelian symmetries")
         self.ctx, self.model, self.sym = ctx, model, model.sym
         self.precision = precision
         self.I = identity_mpo(model)
@@ -167,9 +171,14 @@ class Compressor:
 
     def overlap(self, bra, ket) -> float:
         """<bra|ket> of two MPS with the same total quantum number"""
+        return self.matrix_element(bra, self.I, ket)
+
+    def matrix_element(self, bra, W, ket) -> float:
+        """<bra|O|ket> of an MPO O (site list) that keeps the total quantum number
+        (avg(bra, O, ket)): contract_L through the chain"""
         E = left_vacuum(self.sym)
         for l in range(self.model.L):
-            E = self._env("L", E, bra.A[l], self.I[l], ket.A[l])
+            E = self._env("L", E, bra.A[l], W[l], ket.A[l])
         return float(E.data.sum())
 
     # ---- the fit
@@ -207,12 +216,18 @@ class Compressor:
         for W, psi, c in terms:
             groups.setdefault(id(psi), (psi, []))[1].append((W, c))
         plan = []
+        su2 = sym.nonabelian
         for psi, lst in groups.values():
-            dq = tuple(int(a - b) for a, b in zip(phi.Qtot, psi.Qtot))
+            if tuple(phi.Qtot) == tuple(psi.Qtot):
+                dq = tuple(sym.vacuum())
+            elif su2:
+                raise ValueError("SU(2) fits take operators that keep the total quantum number")
+            else:
+                dq = tuple(int(a - b) for a, b in zip(phi.Qtot, psi.Qtot))
             if len(lst) == 1:
                 W, c = lst[0]
             else:
-                W, c = mpo_sum([w for w, _ in lst], [c for _, c in lst], dq), 1.0
+                W, c = mpo_sum([w for w, _ in lst], [c for _, c in lst], dq, sym.vacuum()), 1.0
             # contract_R's right boundary: rows the ket's total charge, columns the bra's
             RT = Blocks.from_entries(nq, [(0, tuple(psi.Qtot), tuple(phi.Qtot), dq, np.ones((1, 1)))], tripod=True)
             plan.append((W, psi, c, RT))
@@ -237,17 +252,26 @@ class Compressor:
                         # the sources do not change during the fit: their two-site tensors are made once
                         Vk = two_site.get((t, l))
                         if Vk is None:
-                            Vk = two_site[(t, l)] = contract_two_sites(sym, psi.A[l], psi.A[l + 1], qloc, qloc, nq,
-                                                                       ctx=ctx, pool=pool)
+                            if su2:
+                                Vk = contract_two_sites_su2(sym, psi.A[l], psi.A[l + 1], qloc, qloc, ctx=ctx)[0]
+                            else:
+                                Vk = contract_two_sites(sym, psi.A[l], psi.A[l + 1], qloc, qloc, nq, ctx=ctx,
+                                                        pool=pool)
+                            two_site[(t, l)] = Vk
                         x += c * self._apply(envL[t][l], envR[t][l + 2], W[l], W[l + 1], Vk, Vb)
                     Vb.data[:] = x
-                    nrm = float(np.linalg.norm(x))
-                    A1, A2, disc, dmid = split_two_site(Vb, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
-                                                        eps_svd=eps_svd, factor=self.factor,
-                                                        native=self.factor == "eigh", ctx=ctx, pool=pool)
-                    # the split renormalises the kept singular values: the fitted state keeps its norm
-                    scale = nrm * np.sqrt(max(0.0, 1.0 - disc))
-                    (A2 if move == "right" else A1).data[:] *= scale
+                    if su2:
+                        # the kept multiplets keep their singular values (and the state its norm)
+                        A1, A2, disc, dmid = split_two_site_su2(Vb, comb, sym, qloc, qloc, din, dout, Dmax,
+                                                                move=move, eps_svd=eps_svd, renormalise=False)
+                    else:
+                        nrm = float(np.linalg.norm(x))
+                        A1, A2, disc, dmid = split_two_site(Vb, comb, qloc, qloc, din, dout, nq, Dmax, move=move,
+                                                            eps_svd=eps_svd, factor=self.factor,
+                                                            native=self.factor == "eigh", ctx=ctx, pool=pool)
+                        # the split renormalises the kept singular values: the fitted state keeps its norm
+                        scale = nrm * np.sqrt(max(0.0, 1.0 - disc))
+                        (A2 if move == "right" else A1).data[:] *= scale
                     phi.A[l], phi.A[l + 1] = A1, A2
                     phi.dims[l + 1] = dmid
                     disc_max = max(disc_max, disc)

@@ -139,9 +139,12 @@ def contract_two_sites_su2(sym, A1: Blocks, A2: Blocks, qloc12, qloc34, ctx=None
     return V, comb
 
 
-def split_two_site_su2(V: Blocks, comb, sym, qloc12, qloc34, din, dout, Dmax, move="right", eps_svd=1e-14):
+def split_two_site_su2(V: Blocks, comb, sym, qloc12, qloc34, din, dout, Dmax, move="right", eps_svd=1e-14,
+                       renormalise=True):
     """(A1, A2, discarded weight, {Q: kept multiplets}) of the SU(2) two-site tensor V;
-    move="right": A1 = U (left-orthonormal), A2 = S V^T; move="left": A1 = U S, A2 = V^T"""
+    move="right": A1 = U (left-orthonormal), A2 = S V^T; move="left": A1 = U S, A2 = V^T.
+    renormalise=False keeps the kept singular values as they are (the truncated state
+    keeps its norm instead of getting norm 1)."""
     nq = sym.nq
     rc = Recoupling(sym)
     inv = {}
@@ -204,7 +207,7 @@ def split_two_site_su2(V: Blocks, comb, sym, qloc12, qloc34, din, dout, Dmax, mo
     for _, Q, i in kept:
         nkeep[Q] = max(nkeep.get(Q, 0), i + 1)
     dmid = {Q: n for Q, n in sorted(nkeep.items())}
-    norm = np.sqrt(kw) if kw > 0 else 1.0
+    norm = np.sqrt(kw) if kw > 0 and renormalise else 1.0
     A1 = site_layout(qloc12, din, dmid, nq, sym)
     A2 = site_layout(qloc34, dmid, dout, nq, sym)
     for i in range(A1.n):
