@@ -445,8 +445,16 @@ def vumps_bench(ctx, args):
         t1 = time.perf_counter()
         gn, parts = E.gradient()
         t2 = time.perf_counter()
+        # the same environments with the host GMRES loop over device operator applications
+        Eh = UniformEnvironment(ctx, m, u, W, order, precision=prec, tol=1e-12, solver="host")
+        t3 = time.perf_counter()
+        Eh.left()
+        Eh.right()
+        t4 = time.perf_counter()
         res[prec] = {"e": E.energy_density(), "gradient_norm": gn, "environments_s": round(t1 - t0, 3),
-                     "gradient_s": round(t2 - t1, 3), "gmres": E.info}
+                     "gradient_s": round(t2 - t1, 3), "gmres": E.info, "solver": "device",
+                     "environments_s_host_gmres": round(t4 - t3, 3),
+                     "host_gmres_e_rel_diff": abs(Eh.energy_density() - E.energy_density()) / abs(E.energy_density())}
         if prec == "fp64":
             E64 = E
     out["environments"] = res

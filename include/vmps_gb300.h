@@ -493,6 +493,27 @@ int vmps_transfer_create(vmps_ctx* ctx, const vmps_symmetry* sym, int dir, int n
                          const int32_t* order_index, const int64_t* order_value,
                          const vmps_blocks* V, vmps_transfer** out);
 int vmps_transfer_hxv(vmps_transfer* t, const double* vin, double* vout, int precision);
+/* Solves (1 - T + |R)(1|) x = b (the operator of vmps_transfer_hxv) on the transfer-vector
+ * space (the slot-ab blocks, dot weighted by coeff_dot) by restarted GMRES on the device:
+ * VumpsSolver's solve_linear (VUMPS/VumpsSolver.h:1907-1940) with the ALGS GMResSolver
+ * restated.  Krylov vectors stay on the device; one iteration = the operator, two
+ * classical Gram-Schmidt passes and a norm (deterministic reductions); the host keeps the
+ * Hessenberg matrix and its Givens rotations and reads one column per iteration.
+ * precision FP64: GMRES with the FP64 operator to tol (relative residual).  BF16X3:
+ * mixed-precision refinement -- the residual r = b - A x with the FP64 operator, the
+ * correction A d = r by GMRES with the split operator to inner_tol, x += d -- until the
+ * FP64 residual is below tol or max_outer rounds.  b, x: compact host vectors (x is
+ * overwritten; no initial guess).                                                     */
+typedef struct {
+    int32_t iterations;   /* GMRES iterations (operator applications in the Krylov loops) */
+    int32_t outer;        /* refinement rounds (BF16X3)                                   */
+    int32_t fp64_hxv;     /* FP64 operator applications outside the Krylov loops          */
+    int32_t restarts;
+    double  residual;     /* final relative residual |b - A x| / |b| (FP64 operator)      */
+    double  ms_total;
+} vmps_gmres_stats;
+int vmps_transfer_solve(vmps_transfer* t, const double* b, double* x, double tol, int dimK, int max_restarts,
+                        int precision, double inner_tol, int max_outer, vmps_gmres_stats* stats);
 int vmps_transfer_destroy(vmps_transfer* t);
 
 /* ---- allocation-free chain product -------------------------------------------

@@ -73,3 +73,48 @@ def test_transfer_su2_linear_and_split_consistent(gpu_ctx):
     assert rel_err(huv, 2.0 * hu - 0.5 * hv) < 1e-12
     assert rel_err(T.hxv(u, "bf16x3"), hu) < 2e-4
     T.close()
+
+
+@pytest.mark.parametrize("direction", ["L", "R"])
+@pytest.mark.parametrize("precision", ["fp64", "bf16x3"])
+def test_transfer_solve_on_the_device(gpu_ctx, direction, precision):
+    """vmps_transfer_solve (Krylov vectors on the device, two classical Gram-Schmidt passes,
+    Givens rotations on the host; BF16X3: FP64-residual refinement of split corrections)
+    reaches the tolerance in the FP64 residual and agrees with the host GMRES solution"""
+    m, mps, (A, W), LR, order, V = transfer_case("heis", direction, envs=_envs)
+    ab = _positions(order, m.sym)[0]
+    T = MpoTransferMatrix(gpu_ctx, m.sym, direction, A, A, W, LR, ab, order, V)
+    b = T.rhs(np.random.default_rng(3).standard_normal(V.data.size), 0.3) * T.slot_mask()
+    x_ref, _ = T.solve_linear(b, tol=1e-12, dimK=80)
+    x, info = T.solve_device(b, tol=1e-11, dimK=80, precision=precision)
+    r = (b - T.hxv(x)) * T.slot_mask()
+    res = np.sqrt(T.dot(r, r) / T.dot(b, b))
+    assert res < 1e-10, info
+    assert info["residual"] == pytest.approx(res, rel=1e-3, abs=1e-13)
+    assert info["iterations"] > 0
+    if precision == "bf16x3":
+        assert info["outer"] >= 1 and info["fp64_hxv"] >= 2
+    d = x - x_ref
+    assert np.sqrt(T.dot(d, d) / T.dot(x_ref, x_ref)) < 1e-8
+    # a zero right-hand side gives x = 0 and no iteration
+    z, zi = T.solve_device(np.zeros_like(b), precision=precision)
+    assert not np.any(z) and zi["iterations"] == 0
+    T.close()
+
+
+def test_transfer_solve_on_the_device_su2(gpu_ctx):
+    from vmps_gb300.pivot import contract_L, left_vacuum
+    m, mps, (A, W), LR, order, _ = transfer_case("su2", "L")
+    E = left_vacuum(m.sym)
+    for l in range(9):
+        E = contract_L(gpu_ctx, m.sym, E, mps.A[l], m.W[l], mps.A[l])
+    ab = _positions(order, m.sym)[-1]
+    T = MpoTransferMatrix(gpu_ctx, m.sym, "L", A, A, W, LR, ab, order, E)
+    b = T.rhs(np.random.default_rng(8).standard_normal(E.data.size), 0.1) * T.slot_mask()
+    x_ref, _ = T.solve_linear(b, tol=1e-12, dimK=80)
+    for precision in ("fp64", "bf16x3"):
+        x, info = T.solve_device(b, tol=1e-11, dimK=80, precision=precision)
+        d = x - x_ref
+        assert np.sqrt(T.dot(d, d) / T.dot(x_ref, x_ref)) < 1e-8, (precision, info)
+        assert info["residual"] < 1e-10
+    T.close()

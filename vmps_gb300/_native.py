@@ -77,6 +77,14 @@ class vmps_cheb_stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class vmps_gmres_stats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("outer", C.c_int32), ("fp64_hxv", C.c_int32), ("restarts", C.c_int32),
+                ("residual", C.c_double), ("ms_total", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class vmps_tune_info(C.Structure):
     _fields_ = [("ncap1", C.c_int32), ("ncap2", C.c_int32), ("splitk", C.c_int32), ("candidates", C.c_int32),
                 ("from_cache", C.c_int32), ("reserved", C.c_int32), ("ms_default", C.c_double),
@@ -186,6 +194,8 @@ _PROTOS = [
                                        C.c_int64, C.c_int64, i32p, i32p, i64p, C.POINTER(vmps_blocks),
                                        C.POINTER(C.c_void_p)]),
     ("vmps_transfer_hxv", C.c_int, [C.c_void_p, f64p, f64p, C.c_int]),
+    ("vmps_transfer_solve", C.c_int, [C.c_void_p, f64p, f64p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double,
+                                      C.c_int, C.POINTER(vmps_gmres_stats)]),
     ("vmps_transfer_destroy", C.c_int, [C.c_void_p]),
     ("vmps_chain_fp64_noalloc", C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
                                           C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_int32, C.c_double,

@@ -444,6 +444,11 @@ __global__ void axpy_kernel(double a, const double* __restrict__ x, double* __re
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         y[i] = fma(a, x[i], y[i]);
 }
+__global__ void hadamard_kernel(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out,
+                                int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = a[i] * b[i];
+}
 __global__ void scale_kernel(double a, double* __restrict__ x, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] *= a;
@@ -672,6 +677,12 @@ cudaError_t launch_mgs(const double* V, int nv, int64_t n, const double* coef, d
 }
 cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t st) {
     axpy_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>(a, x, y, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_hadamard(const double* a, const double* b, double* out, int64_t n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (!a || !b || !out) return cudaErrorInvalidValue;
+    hadamard_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>(a, b, out, n);
     return cudaGetLastError();
 }
 cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t st) {

@@ -68,6 +68,7 @@ cudaError_t launch_mdot(const double* V, int nv, int64_t n, const double* w, dou
 cudaError_t launch_mgs(const double* V, int nv, int64_t n, const double* coef, double* w, cudaStream_t st);
 cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t st);
 cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t st);
+cudaError_t launch_hadamard(const double* a, const double* b, double* out, int64_t n, cudaStream_t st);   // out = a * b
 cudaError_t launch_combine(const double* V, int nv, int64_t n, const double* c, double* y, cudaStream_t st);
 cudaError_t launch_finite(const double* x, int64_t n, int* bad, cudaStream_t st);
 // split-K partials of a grouped GEMM summed in order: out[e] = sum_j part[j * n + e] (double or float)

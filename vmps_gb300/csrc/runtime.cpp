@@ -2814,11 +2814,207 @@ struct vmps_transfer_s {
     DBuf dLR, dVout, stage_in, stage_out, pk, dTrace, dCombine, part, scal;
     int npk = 0, ntrace = 0, ncombine = 0;
     std::vector<char> prepped[2];
+    QN abq;                         // (QN, index) of the slot ab
+    int32_t abi = -1;
+    // device GMRES: Krylov basis (dimK + 1 vectors of the padded layout), work vectors,
+    // the slot mask and the masked dot weights, reduction scratch
+    DBuf gQ, gw, gr, gx, gb, gt, gd, gwm, gm, gpart, gh;
+    int gdim = -1;
     ~vmps_transfer_s() {
         for (vmps_env* e : chain) delete e;
     }
     cudaStream_t st() const { return ctx->stream; }
 };
+
+// T's operator (VumpsMpoTransferMatrix.h:99-212) on padded device vectors: the cell's
+// contract_L/R chain from din, then Vout = Vin - T Vin + LdotR * 1 on the slot-ab blocks
+static void transfer_apply(vmps_transfer* t, const double* din, double* dout, int prec) {
+    cudaStream_t st = t->st();
+    vmps_env* first = t->chain.front();
+    if (din != first->dE.as<double>() && first->Ed.total > 0)
+        CK(cudaMemcpyAsync(first->dE.p, din, (size_t)first->Ed.total * 8, cudaMemcpyDeviceToDevice, st));
+    for (size_t k = 0; k < t->chain.size(); ++k) {
+        vmps_env* e = t->chain[k];
+        DevPlan& dp = env_plan(e, prec);
+        Operands ops;
+        if (e->side == VMPS_ENV_LEFT) { ops.X = e->dB.as<double>(); ops.Z = e->dK.as<double>(); }
+        else { ops.X = e->dK.as<double>(); ops.Z = e->dB.as<double>(); }
+        ops.Y = e->dE.as<double>();
+        ops.O = e->dN.as<double>();
+        ops.err = t->ctx->err;
+        if (!t->prepped[prec][k]) {   // the site tensors are fixed: their split panels are made once
+            split_prepare(dp, ops.X, ops.Z, st);
+            t->prepped[prec][k] = 1;
+        }
+        run_plan(dp, ops, st);
+        if (k + 1 < t->chain.size() && e->Nd.total > 0)
+            CK(cudaMemcpyAsync(t->chain[k + 1]->dE.p, e->dN.p, (size_t)e->Nd.total * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    CK(launch_trace_pairs(t->dTrace.as<TracePair>(), t->ntrace, first->dE.as<double>(), t->dLR.as<double>(),
+                          t->part.as<double>(), t->scal.as<double>(), st));
+    CK(cudaMemsetAsync(dout, 0, (size_t)std::max<int64_t>(t->Vd.total, 1) * 8, st));
+    CK(launch_transfer_combine(t->dCombine.as<CombineBlock>(), t->ncombine, first->dE.as<double>(),
+                               t->chain.back()->dN.as<double>(), dout, t->scal.as<double>(), st));
+}
+
+// ---- device GMRES of the transfer operator --------------------------------------
+struct GmresNonFinite : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// buffers for a Krylov dimension dimK; the slot mask and its dot weights (coeff_dot(out),
+// VumpsMpoTransferMatrix.h:258-275) in the padded layout, padding zero
+static void transfer_gmres_setup(vmps_transfer* t, int dimK) {
+    cudaStream_t st = t->st();
+    const int64_t n = std::max<int64_t>(t->Vd.total, 1);
+    if (t->gdim < 0) {
+        std::vector<double> wm((size_t)n, 0.0), m((size_t)n, 0.0);
+        for (int64_t b = 0; b < t->Vt.n; ++b) {
+            if (!(t->Vt.qmid[b] == t->abq) || t->Vt.leg[b] != t->abi) continue;
+            const double w = t->sym.coeff_dot(t->Vt.qout[b]);
+            for (int64_t c = 0; c < t->Vt.cols[b]; ++c)
+                for (int64_t r = 0; r < t->Vt.rows[b]; ++r) {
+                    const int64_t e = t->Vd.off[b] + c * t->Vd.ld[b] + r;
+                    wm[(size_t)e] = w;
+                    m[(size_t)e] = 1.0;
+                }
+        }
+        upload_vec(t->gwm, wm, st);
+        upload_vec(t->gm, m, st);
+        for (DBuf* d : {&t->gw, &t->gr, &t->gx, &t->gb, &t->gt, &t->gd}) d->alloc((size_t)n * 8, st, true);
+        t->gdim = 0;
+    }
+    if (t->gdim < dimK) {
+        t->gQ.alloc((size_t)(dimK + 1) * (size_t)n * 8, st, true);
+        t->gpart.alloc((size_t)(dimK + 1) * (size_t)std::max(dot_nchunk(n), 1) * 8, st, true);
+        t->gh.alloc((size_t)(3 * (dimK + 1) + 8) * 8, st, true);
+        t->gdim = dimK;
+    }
+}
+
+// <x, y> on the slot-ab blocks with the coeff_dot weights (device reduction, value to the host)
+static double transfer_wdot(vmps_transfer* t, const double* x, const double* y) {
+    cudaStream_t st = t->st();
+    const int64_t n = t->Vd.total;
+    double* r = t->gr.as<double>();
+    double* h = t->gh.as<double>();
+    CK(launch_hadamard(t->gwm.as<double>(), y, r, n, st));
+    CK(launch_dot(x, r, n, t->gpart.as<double>(), h, st));
+    double v = 0;
+    CK(cudaMemcpyAsync(&v, h, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return v;
+}
+
+// r = mask * (b - A x) with the FP64 operator (r = mask * b when x is zero)
+static void transfer_residual(vmps_transfer* t, const double* b, const double* x, double* r, bool x_zero) {
+    cudaStream_t st = t->st();
+    const int64_t n = t->Vd.total;
+    CK(cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+    if (!x_zero) {
+        double* ax = t->dVout.as<double>();
+        transfer_apply(t, x, ax, VMPS_PREC_FP64);
+        CK(launch_axpy(-1.0, ax, r, n, st));
+    }
+    CK(launch_hadamard(t->gm.as<double>(), r, r, n, st));
+}
+
+// Restarted GMRES for A d = rhs (rhs masked), then x += d: cycles of at most dimK
+// iterations until |rhs - A d| <= abs_tol or max_restarts cycles; returns the iterations.
+// Arnoldi with two classical Gram-Schmidt passes under the weighted dot; the Hessenberg
+// matrix and its Givens rotations on the host, one column read back per iteration.
+static int transfer_gmres(vmps_transfer* t, const double* rhs, double* x, double abs_tol, int dimK,
+                          int max_restarts, int prec, int32_t* restarts) {
+    cudaStream_t st = t->st();
+    const int64_t n = t->Vd.total;
+    double* Q = t->gQ.as<double>();
+    double* w = t->gw.as<double>();
+    double* r = t->gr.as<double>();
+    double* d = t->gd.as<double>();                  // this call's solution
+    double* ax = t->dVout.as<double>();
+    const double* m = t->gm.as<double>();
+    const double* wm = t->gwm.as<double>();
+    const int ld = dimK + 1;
+    double* hd = t->gh.as<double>();                 // [h pass 1 (ld) | h pass 2 (ld) | norm (8) | y (ld)]
+    double* h2d = hd + ld;
+    double* nrm = hd + 2 * ld;
+    double* yd = nrm + 8;
+    std::vector<double> H((size_t)ld * dimK, 0.0), cs((size_t)dimK), sn((size_t)dimK), g((size_t)ld);
+    std::vector<double> col((size_t)(2 * ld + 1));
+    CK(cudaMemsetAsync(d, 0, (size_t)n * 8, st));
+    int its = 0;
+    for (int cycle = 0; cycle < max_restarts; ++cycle) {
+        // w = mask * (rhs - A d)
+        CK(cudaMemcpyAsync(w, rhs, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        if (cycle > 0) {
+            transfer_apply(t, d, ax, prec);
+            CK(launch_axpy(-1.0, ax, w, n, st));
+            CK(launch_hadamard(m, w, w, n, st));
+        }
+        const double beta = std::sqrt(std::max(0.0, transfer_wdot(t, w, w)));
+        if (!std::isfinite(beta)) throw GmresNonFinite("GMRES: non-finite residual");
+        if (beta <= abs_tol) break;
+        if (cycle > 0 && restarts) ++*restarts;
+        CK(cudaMemcpyAsync(Q, w, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+        CK(launch_scale(1.0 / beta, Q, n, st));
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int kk = 0;
+        for (int k = 0; k < dimK; ++k) {
+            transfer_apply(t, Q + (int64_t)k * n, ax, prec);
+            ++its;
+            CK(launch_hadamard(m, ax, w, n, st));
+            for (int pass = 0; pass < 2; ++pass) {
+                CK(launch_hadamard(wm, w, r, n, st));
+                CK(launch_mdot(Q, k + 1, n, r, t->gpart.as<double>(), pass ? h2d : hd, st));
+                CK(launch_mgs(Q, k + 1, n, pass ? h2d : hd, w, st));
+            }
+            CK(launch_hadamard(wm, w, r, n, st));
+            CK(launch_dot(w, r, n, t->gpart.as<double>(), nrm, st));
+            CK(cudaMemcpyAsync(col.data(), hd, sizeof(double) * (size_t)(k + 1), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(col.data() + ld, h2d, sizeof(double) * (size_t)(k + 1), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(col.data() + 2 * ld, nrm, sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            double* hk = H.data() + (size_t)k * ld;
+            for (int j = 0; j <= k; ++j) hk[j] = col[(size_t)j] + col[(size_t)(ld + j)];
+            const double hn = std::sqrt(std::max(0.0, col[(size_t)(2 * ld)]));
+            hk[k + 1] = hn;
+            for (int j = 0; j <= k + 1; ++j)
+                if (!std::isfinite(hk[j])) throw GmresNonFinite("GMRES: the operator produced non-finite values");
+            // the earlier rotations, then the one that zeroes hk[k+1]
+            for (int j = 0; j < k; ++j) {
+                const double a = cs[(size_t)j] * hk[j] + sn[(size_t)j] * hk[j + 1];
+                hk[j + 1] = -sn[(size_t)j] * hk[j] + cs[(size_t)j] * hk[j + 1];
+                hk[j] = a;
+            }
+            const double den = std::hypot(hk[k], hk[k + 1]);
+            cs[(size_t)k] = den > 0 ? hk[k] / den : 1.0;
+            sn[(size_t)k] = den > 0 ? hk[k + 1] / den : 0.0;
+            hk[k] = den;
+            hk[k + 1] = 0.0;
+            g[(size_t)k + 1] = -sn[(size_t)k] * g[(size_t)k];
+            g[(size_t)k] = cs[(size_t)k] * g[(size_t)k];
+            kk = k + 1;
+            if (hn <= 1e-14 * beta || std::abs(g[(size_t)k + 1]) <= abs_tol || k + 1 == dimK) break;
+            CK(cudaMemcpyAsync(Q + (int64_t)(k + 1) * n, w, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+            CK(launch_scale(1.0 / hn, Q + (int64_t)(k + 1) * n, n, st));
+        }
+        // y = R^-1 g (upper triangular, kk x kk), d += Q y
+        std::vector<double> y((size_t)kk, 0.0);
+        for (int i = kk - 1; i >= 0; --i) {
+            double sum = g[(size_t)i];
+            for (int j = i + 1; j < kk; ++j) sum -= H[(size_t)j * ld + i] * y[(size_t)j];
+            const double rii = H[(size_t)i * ld + i];
+            y[(size_t)i] = rii != 0 ? sum / rii : 0.0;
+        }
+        CK(cudaMemcpyAsync(yd, y.data(), sizeof(double) * (size_t)kk, cudaMemcpyHostToDevice, st));
+        CK(launch_combine(Q, kk, n, yd, ax, st));
+        CK(launch_axpy(1.0, ax, d, n, st));
+        CK(cudaStreamSynchronize(st));   // y is a host vector: keep it until its copy has run
+    }
+    CK(launch_axpy(1.0, d, x, n, st));
+    return its;
+}
 
 static std::vector<int32_t> block_key(const BlockTable& t, int64_t i, int nq, bool with_leg) {
     std::vector<int32_t> k;
@@ -2861,6 +3057,8 @@ int vmps_transfer_create(vmps_ctx* ctx, const vmps_symmetry* symd, int dir, int 
     std::unique_ptr<vmps_transfer> t(new vmps_transfer_s());
     t->ctx = ctx;
     t->sym = sym;
+    t->abq = abq;
+    t->abi = abi;
     t->Vt = parse_blocks(sym, V, true);
     t->Vd = make_dev_layout(t->Vt.rows, t->Vt.cols);
     t->LRt = parse_blocks(sym, LReigen, false);
@@ -2953,31 +3151,65 @@ int vmps_transfer_hxv(vmps_transfer* t, const double* vin, double* vout, int pre
     cudaStream_t st = t->st();
     vmps_env* first = t->chain.front();
     pack_in(t->ctx, t->pk, t->npk, vin, t->Vt.total, t->stage_in, first->dE.as<double>(), st);
-    for (size_t k = 0; k < t->chain.size(); ++k) {
-        vmps_env* e = t->chain[k];
-        DevPlan& dp = env_plan(e, prec);
-        Operands ops;
-        if (e->side == VMPS_ENV_LEFT) { ops.X = e->dB.as<double>(); ops.Z = e->dK.as<double>(); }
-        else { ops.X = e->dK.as<double>(); ops.Z = e->dB.as<double>(); }
-        ops.Y = e->dE.as<double>();
-        ops.O = e->dN.as<double>();
-        ops.err = t->ctx->err;
-        if (!t->prepped[prec][k]) {   // the site tensors are fixed: their split panels are made once
-            split_prepare(dp, ops.X, ops.Z, st);
-            t->prepped[prec][k] = 1;
-        }
-        run_plan(dp, ops, st);
-        if (k + 1 < t->chain.size() && e->Nd.total > 0)
-            CK(cudaMemcpyAsync(t->chain[k + 1]->dE.p, e->dN.p, (size_t)e->Nd.total * 8, cudaMemcpyDeviceToDevice, st));
-    }
-    CK(launch_trace_pairs(t->dTrace.as<TracePair>(), t->ntrace, first->dE.as<double>(), t->dLR.as<double>(),
-                          t->part.as<double>(), t->scal.as<double>(), st));
-    CK(cudaMemsetAsync(t->dVout.p, 0, (size_t)std::max<int64_t>(t->Vd.total, 1) * 8, st));
-    CK(launch_transfer_combine(t->dCombine.as<CombineBlock>(), t->ncombine, first->dE.as<double>(),
-                               t->chain.back()->dN.as<double>(), t->dVout.as<double>(), t->scal.as<double>(), st));
+    transfer_apply(t, first->dE.as<double>(), t->dVout.as<double>(), prec);
     pack_out(t->ctx, t->pk, t->npk, t->dVout.as<double>(), t->Vt.total, t->stage_out, vout, st);
     CK(cudaStreamSynchronize(st));
     check_device_error(t->ctx);
+    API_END
+}
+
+int vmps_transfer_solve(vmps_transfer* t, const double* b, double* x, double tol, int dimK, int max_restarts,
+                        int prec, double inner_tol, int max_outer, vmps_gmres_stats* stats) {
+    API_BEGIN
+    if (!t || !b || !x) return set_err(VMPS_E_ARG, "null argument");
+    if (prec != VMPS_PREC_FP64 && prec != VMPS_PREC_BF16X3) return set_err(VMPS_E_ARG, "FP64 or BF16X3");
+    if (!(tol > 0) || dimK < 1 || dimK > 1000 || max_restarts < 1 || max_outer < 1 || !(inner_tol > 0))
+        return set_err(VMPS_E_ARG, "GMRES needs tol > 0, 1 <= dimK <= 1000, max_restarts >= 1, max_outer >= 1");
+    CK(cudaSetDevice(t->ctx->device));
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t st = t->st();
+    transfer_gmres_setup(t, dimK);
+    const int64_t n = t->Vd.total;
+    double* db = t->gb.as<double>();
+    double* dx = t->gx.as<double>();
+    pack_in(t->ctx, t->pk, t->npk, b, t->Vt.total, t->stage_in, db, st);
+    CK(launch_hadamard(t->gm.as<double>(), db, db, n, st));   // the slot-ab part of b
+    CK(cudaMemsetAsync(dx, 0, (size_t)n * 8, st));
+    vmps_gmres_stats S{};
+    const double nb = std::sqrt(std::max(0.0, transfer_wdot(t, db, db)));
+    if (!std::isfinite(nb)) return set_err(VMPS_E_NONFINITE, "GMRES: non-finite right-hand side");
+    if (nb > 0) try {
+        if (prec == VMPS_PREC_FP64) {
+            S.iterations = transfer_gmres(t, db, dx, tol * nb, dimK, max_restarts, VMPS_PREC_FP64, &S.restarts);
+        } else {
+            // refinement: FP64 residuals, split-precision corrections
+            double* dr = t->gt.as<double>();
+            bool zero = true;
+            for (int outer = 0; outer < max_outer; ++outer) {
+                transfer_residual(t, db, dx, dr, zero);
+                if (!zero) ++S.fp64_hxv;
+                const double res = std::sqrt(std::max(0.0, transfer_wdot(t, dr, dr))) / nb;
+                if (res <= tol) break;
+                // d solves A d = r; x += d (the correction is accumulated straight into x)
+                const double rn = res * nb;
+                S.iterations += transfer_gmres(t, dr, dx, inner_tol * rn, dimK, 2, VMPS_PREC_BF16X3, &S.restarts);
+                S.outer = outer + 1;
+                zero = false;
+            }
+        }
+        double* dr = t->gt.as<double>();
+        transfer_residual(t, db, dx, dr, false);
+        ++S.fp64_hxv;
+        S.residual = std::sqrt(std::max(0.0, transfer_wdot(t, dr, dr))) / nb;
+    } catch (const GmresNonFinite& e) {
+        CK(cudaStreamSynchronize(st));
+        return set_err(VMPS_E_NONFINITE, e.what());
+    }
+    pack_out(t->ctx, t->pk, t->npk, dx, t->Vt.total, t->stage_out, x, st);
+    CK(cudaStreamSynchronize(st));
+    check_device_error(t->ctx);
+    S.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = S;
     API_END
 }
 

@@ -183,10 +183,15 @@ class UniformEnvironment:
     bond, the same at every bond of the cell)"""
 
     def __init__(self, ctx, model, u: UniformMPS, W: list, order: dict, precision="fp64", tol=1e-12, dimK=100,
-                 env=None, transfer=None, apply=None):
+                 env=None, transfer=None, apply=None, solver="device"):
+        """solver: "device" runs GMRES on the GPU (vmps_transfer_solve), "host" the host loop
+        of MpoTransferMatrix.solve_linear[_refined] over device operator applications"""
         self.ctx, self.model, self.u, self.W, self.order = ctx, model, u, list(W), order
         self.sym = model.sym
         self.precision, self.tol, self.dimK = precision, tol, dimK
+        if solver not in ("device", "host"):
+            raise ValueError("solver: 'device' or 'host'")
+        self.solver = solver
         self.env = env or self._engine_env
         self.transfer = transfer or self._engine_transfer
         self.apply = apply or self._engine_apply
@@ -209,6 +214,8 @@ class UniformEnvironment:
     def _engine_transfer(self, side, A, W, LR, ab, order, V, b):
         T = MpoTransferMatrix(self.ctx, self.sym, side, A, A, W, LR, ab, order, V)
         try:
+            if self.solver == "device":
+                return T.solve_device(b, tol=self.tol, dimK=self.dimK, precision=self.precision)
             if self.precision == "fp64":
                 return T.solve_linear(b, tol=self.tol, dimK=self.dimK)
             return T.solve_linear_refined(b, tol=self.tol, dimK=self.dimK)

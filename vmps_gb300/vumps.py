@@ -129,6 +129,20 @@ class MpoTransferMatrix:
         r = (b - self.hxv(x, precision)) * m
         return x, {"iterations": its, "residual": np.sqrt(self.dot(r, r)) / nb}
 
+    def solve_device(self, b: np.ndarray, tol=1e-10, dimK=200, max_restarts=20, precision="fp64", inner_tol=1e-4,
+                     max_outer=10):
+        """The same solves on the device (vmps_transfer_solve): Krylov vectors in device
+        memory, the Hessenberg matrix on the host.  precision "fp64": GMRES with the FP64
+        operator (solve_linear); "bf16x3": FP64-residual refinement with split-precision
+        GMRES corrections (solve_linear_refined).  Returns (x, info)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        st = N.vmps_gmres_stats()
+        N.check(N.lib().vmps_transfer_solve(self._h, b.ctypes.data_as(N.f64p), x.ctypes.data_as(N.f64p), float(tol),
+                                            int(dimK), int(max_restarts), 1 if precision == "bf16x3" else 0,
+                                            float(inner_tol), int(max_outer), C.byref(st)))
+        return x, st.as_dict()
+
     def solve_linear_refined(self, b: np.ndarray, tol=1e-10, inner_tol=1e-4, dimK=200, max_outer=10):
         """Mixed-precision iterative refinement: the residual r = b - H x with the FP64
         operator, the correction H d = r by GMRES with the split-precision operator to
