@@ -502,14 +502,17 @@ int vmps_transfer_hxv(vmps_transfer* t, const double* vin, double* vout, int pre
  * precision FP64: GMRES with the FP64 operator to tol (relative residual).  BF16X3:
  * mixed-precision refinement -- the residual r = b - A x with the FP64 operator, the
  * correction A d = r by GMRES with the split operator to inner_tol, x += d -- until the
- * FP64 residual is below tol or max_outer rounds.  b, x: compact host vectors (x is
- * overwritten; no initial guess).                                                     */
+ * FP64 residual is below tol; when a round does not halve the residual (or after
+ * max_outer rounds) FP64 GMRES finishes from the best x.  b, x: compact host vectors (x
+ * is overwritten; no initial guess).                                                   */
 typedef struct {
-    int32_t iterations;   /* GMRES iterations (operator applications in the Krylov loops) */
-    int32_t outer;        /* refinement rounds (BF16X3)                                   */
-    int32_t fp64_hxv;     /* FP64 operator applications outside the Krylov loops          */
+    int32_t iterations;       /* GMRES iterations (operator applications in the Krylov loops) */
+    int32_t fp64_iterations;  /* those with the FP64 operator                                 */
+    int32_t outer;            /* split-precision refinement rounds (BF16X3)                   */
+    int32_t fp64_hxv;         /* FP64 operator applications outside the Krylov loops          */
     int32_t restarts;
-    double  residual;     /* final relative residual |b - A x| / |b| (FP64 operator)      */
+    int32_t reserved;
+    double  residual;         /* final relative residual |b - A x| / |b| (FP64 operator)      */
     double  ms_total;
 } vmps_gmres_stats;
 int vmps_transfer_solve(vmps_transfer* t, const double* b, double* x, double tol, int dimK, int max_restarts,

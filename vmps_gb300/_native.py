@@ -78,7 +78,8 @@ class vmps_cheb_stats(C.Structure):
 
 
 class vmps_gmres_stats(C.Structure):
-    _fields_ = [("iterations", C.c_int32), ("outer", C.c_int32), ("fp64_hxv", C.c_int32), ("restarts", C.c_int32),
+    _fields_ = [("iterations", C.c_int32), ("fp64_iterations", C.c_int32), ("outer", C.c_int32),
+                ("fp64_hxv", C.c_int32), ("restarts", C.c_int32), ("reserved", C.c_int32),
                 ("residual", C.c_double), ("ms_total", C.c_double)]
 
     def as_dict(self):

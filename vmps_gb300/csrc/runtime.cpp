@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <limits>
 #include <cstdlib>
 #include <chrono>
 #include <cmath>
@@ -3181,18 +3182,35 @@ int vmps_transfer_solve(vmps_transfer* t, const double* b, double* x, double tol
     if (nb > 0) try {
         if (prec == VMPS_PREC_FP64) {
             S.iterations = transfer_gmres(t, db, dx, tol * nb, dimK, max_restarts, VMPS_PREC_FP64, &S.restarts);
+            S.fp64_iterations = S.iterations;
         } else {
-            // refinement: FP64 residuals, split-precision corrections
+            // refinement: FP64 residuals, split-precision corrections.  When a round does not
+            // halve the residual (the split operator's error times the condition number is no
+            // longer small), a round that made it worse is undone and FP64 GMRES finishes
             double* dr = t->gt.as<double>();
             bool zero = true;
-            for (int outer = 0; outer < max_outer; ++outer) {
+            double prev = std::numeric_limits<double>::infinity();
+            for (int outer = 0; outer <= max_outer; ++outer) {
                 transfer_residual(t, db, dx, dr, zero);
                 if (!zero) ++S.fp64_hxv;
-                const double res = std::sqrt(std::max(0.0, transfer_wdot(t, dr, dr))) / nb;
+                double res = std::sqrt(std::max(0.0, transfer_wdot(t, dr, dr))) / nb;
                 if (res <= tol) break;
+                if (res > 0.5 * prev || outer == max_outer) {
+                    if (res > prev) {   // the last correction (still in gd) made it worse
+                        CK(launch_axpy(-1.0, t->gd.as<double>(), dx, t->Vd.total, st));
+                        transfer_residual(t, db, dx, dr, false);
+                        ++S.fp64_hxv;
+                    }
+                    const int its = transfer_gmres(t, dr, dx, tol * nb, dimK, max_restarts, VMPS_PREC_FP64,
+                                                   &S.restarts);
+                    S.iterations += its;
+                    S.fp64_iterations += its;
+                    break;
+                }
+                prev = res;
                 // d solves A d = r; x += d (the correction is accumulated straight into x)
-                const double rn = res * nb;
-                S.iterations += transfer_gmres(t, dr, dx, inner_tol * rn, dimK, 2, VMPS_PREC_BF16X3, &S.restarts);
+                S.iterations += transfer_gmres(t, dr, dx, inner_tol * res * nb, dimK, 2, VMPS_PREC_BF16X3,
+                                               &S.restarts);
                 S.outer = outer + 1;
                 zero = false;
             }

@@ -134,7 +134,8 @@ class MpoTransferMatrix:
         """The same solves on the device (vmps_transfer_solve): Krylov vectors in device
         memory, the Hessenberg matrix on the host.  precision "fp64": GMRES with the FP64
         operator (solve_linear); "bf16x3": FP64-residual refinement with split-precision
-        GMRES corrections (solve_linear_refined).  Returns (x, info)."""
+        GMRES corrections (solve_linear_refined), FP64 GMRES finishing when a round does not
+        halve the residual.  Returns (x, info)."""
         b = np.ascontiguousarray(b, dtype=np.float64)
         x = np.zeros_like(b)
         st = N.vmps_gmres_stats()
