@@ -16,7 +16,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native as N
-from .blocks import Blocks, MpoSite, Symmetry
+from .blocks import Blocks, Symmetry
 
 
 class MpoTransferMatrix:
