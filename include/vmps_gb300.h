@@ -504,7 +504,8 @@ int vmps_transfer_hxv(vmps_transfer* t, const double* vin, double* vout, int pre
  * correction A d = r by GMRES with the split operator to inner_tol, x += d -- until the
  * FP64 residual is below tol; when a round does not halve the residual (or after
  * max_outer rounds) FP64 GMRES finishes from the best x.  b, x: compact host vectors (x
- * is overwritten; no initial guess).                                                   */
+ * is overwritten; no initial guess).  Device memory: dimK + 8 vectors of the padded
+ * layout, kept by the transfer operator for later solves.                              */
 typedef struct {
     int32_t iterations;       /* GMRES iterations (operator applications in the Krylov loops) */
     int32_t fp64_iterations;  /* those with the FP64 operator                                 */

@@ -248,3 +248,25 @@ def test_truncated_fit_is_a_projection(kind):
     assert disc > 0
     assert max(sum(d.values()) for d in phi.dims) <= Dmax
     assert comp.matrix_element(phi, model.W, psi) == pytest.approx(comp.overlap(phi, phi), rel=1e-9)
+
+
+def test_su2_fits_refuse_operators_that_change_the_total_quantum_number():
+    model = models.heisenberg_su2(6)
+    psi = RandomMPS(model, (1,), 16, seed=1)
+    phi = RandomMPS(model, (3,), 16, seed=2)
+    comp = _su2_compressor(model)
+    with pytest.raises(ValueError):
+        comp.fit(phi, [(model.W, psi, 1.0)], Dmax=16, sweeps=1)
+
+
+def test_mpo_sum_with_su2_vacuum():
+    """the summed MPO of H and the identity on an SU(2) chain keeps the vacuum (q = 1)
+    boundary states: <psi|(H + 2)|psi> = <psi|H|psi> + 2 <psi|psi>"""
+    from vmps_gb300.compress import mpo_sum
+    model = models.heisenberg_su2(8)
+    psi = RandomMPS(model, (1,), 32, seed=4)
+    comp = _su2_compressor(model)
+    S = mpo_sum([model.W, comp.I], [1.0, 2.0], (1,), model.sym.vacuum())
+    lhs = comp.matrix_element(psi, S, psi)
+    rhs = comp.matrix_element(psi, model.W, psi) + 2.0 * comp.overlap(psi, psi)
+    assert lhs == pytest.approx(rhs, rel=1e-12)
