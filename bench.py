@@ -703,6 +703,18 @@ def mps_chebyshev_bench(ctx, args):
     return out
 
 
+def optional_row(name, fn):
+    """one of the configuration rows beside the headline HxV: a failure is reported in the
+    row (and on stderr) instead of ending the run before the headline line is printed"""
+    try:
+        return fn()
+    except Exception as e:   # noqa: BLE001 -- reported, not swallowed
+        import traceback
+        traceback.print_exc()
+        print(f"bench row {name} failed: {e!r}", file=sys.stderr, flush=True)
+        return {"error": repr(e)}
+
+
 def cpu_model():
     """CPU model string of the host (lscpu's "Model name", else /proc/cpuinfo)."""
     try:
@@ -988,23 +1000,23 @@ def main():
 
     sweep = None
     if not args.no_sweep and rank == 0:
-        sweep = sweep_bench(ctx, args, with_cpu=not args.no_cpu and world == 1)
+        sweep = optional_row("dmrg_sweep", lambda: sweep_bench(ctx, args, with_cpu=not args.no_cpu and world == 1))
     cheb = None
     if not args.no_chebyshev and rank == 0:
-        cheb = chebyshev_bench(ctx, args)
+        cheb = optional_row("chebyshev", lambda: chebyshev_bench(ctx, args))
     su2 = None
     if not args.no_su2 and rank == 0:
-        su2 = su2_cylinder_bench(ctx, args)
+        su2 = optional_row("su2xu1_cylinder", lambda: su2_cylinder_bench(ctx, args))
     vum = None
     if not args.no_vumps and rank == 0:
-        vum = vumps_bench(ctx, args)
+        vum = optional_row("vumps_cell", lambda: vumps_bench(ctx, args))
     mcheb = None
     if not args.no_mps_chebyshev and rank == 0:
-        mcheb = mps_chebyshev_bench(ctx, args)
+        mcheb = optional_row("mps_chebyshev", lambda: mps_chebyshev_bench(ctx, args))
 
     tune_small = None
     if rank == 0 and args.precision == "bf16x3" and not args.no_tune_small:
-        tune_small = autotune_small(ctx)
+        tune_small = optional_row("autotune_small", lambda: autotune_small(ctx))
 
     cpu = None
     if not args.no_cpu and world == 1 and rank == 0:
