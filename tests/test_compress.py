@@ -270,3 +270,66 @@ def test_mpo_sum_with_su2_vacuum():
     lhs = comp.matrix_element(psi, S, psi)
     rhs = comp.matrix_element(psi, model.W, psi) + 2.0 * comp.overlap(psi, psi)
     assert lhs == pytest.approx(rhs, rel=1e-12)
+
+
+# ---- the MpsCompressor operations with their stopping rule (|phi - T|^2 <= tol)
+
+def _sz_mpo(model, j):
+    from vmps_gb300.models import ChainModel
+    sz = np.diag([0.5 * q[1] for q in model.qloc])
+    onehot = [1.0 if i == j else 0.0 for i in range(model.L)]
+    return ChainModel(model.sym, model.L, model.qloc, {"Sz": (sz, (0, 0))}, [], [("Sz", 1.0)], site_coef=onehot).W
+
+
+def test_mpo_adjoint_and_product_are_the_dense_operators():
+    from vmps_gb300.compress import mpo_adjoint, mpo_product
+    from vmps_gb300.spectral import annihilator_mpo
+    model = models.hubbard_u1xu1(4, t=1.0, U=4.0)
+    H = ed.mpo_to_dense(model)
+    S = _sz_mpo(model, 1)
+    dS = _dense_mpo(S, model.d, (0, 0))
+    assert np.allclose(_dense_mpo(mpo_product(model.W, model.W), model.d, (0, 0)), H @ H, rtol=0, atol=1e-12)
+    assert np.allclose(_dense_mpo(mpo_product(model.W, S), model.d, (0, 0)), H @ dS, rtol=0, atol=1e-12)
+    assert np.allclose(_dense_mpo(mpo_adjoint(model.W), model.d, (0, 0)), H.T, rtol=0, atol=1e-13)
+    with pytest.raises(ValueError):   # two auxiliary states at the end (the finished and the pending operator)
+        mpo_product(annihilator_mpo(model, [1.0, 0.0, 0.0, 0.0], "up"), model.W)
+
+
+def test_state_compress_reports_the_distance():
+    model, psi, comp = _setup(6, 64)
+    phi, info = comp.state_compress(psi, Dmax=6, tol=0.0, max_sweeps=3)
+    d = _dense(phi) - _dense(psi)
+    assert info["sweeps"] == 3 and info["discarded"] > 0
+    assert info["sqdist"] == pytest.approx(float(d @ d), rel=1e-8)
+    assert max(sum(q.values()) for q in phi.dims) <= 6
+    # a loose tolerance stops after min_sweeps
+    _, info2 = comp.state_compress(psi, Dmax=6, tol=1e9, max_sweeps=5, min_sweeps=2)
+    assert info2["sweeps"] == 2
+
+
+def test_prod_poly_and_lincombo_compress_against_dense():
+    model, psi, comp = _setup(6, 64)
+    H = ed.mpo_to_dense(model)
+    x = _dense(psi)
+    # W psi, converged (bases complete) and truncated
+    phi, info = comp.prod_compress(model.W, psi, Dmax=1000, tol=1e-18, max_sweeps=2)
+    assert info["target_norm2"] == pytest.approx(float((H @ x) @ (H @ x)), rel=1e-11)
+    assert np.linalg.norm(_dense(phi) - H @ x) < 1e-10 * np.linalg.norm(H @ x)
+    phi, info = comp.prod_compress(model.W, psi, Dmax=10, tol=0.0, max_sweeps=2)
+    d = _dense(phi) - H @ x
+    assert info["sqdist"] == pytest.approx(float(d @ d), rel=1e-6)
+    # H psi1 - b psi2
+    psi2 = RandomMPS(model, (6, 0), 64, seed=12)
+    y = _dense(psi2)
+    phi, info = comp.poly_compress(model.W, psi, 0.7, psi2, Dmax=12, tol=0.0, max_sweeps=2)
+    t = H @ x - 0.7 * y
+    assert info["target_norm2"] == pytest.approx(float(t @ t), rel=1e-11)
+    d = _dense(phi) - t
+    assert info["sqdist"] == pytest.approx(float(d @ d), rel=1e-6)
+    # 0.5 psi1 + 2 psi2 - psi3
+    psi3 = RandomMPS(model, (6, 0), 64, seed=13)
+    z = _dense(psi3)
+    phi, info = comp.lincombo_compress([psi, psi2, psi3], [0.5, 2.0, -1.0], Dmax=1000, tol=1e-18, max_sweeps=2)
+    t = 0.5 * x + 2.0 * y - z
+    assert np.linalg.norm(_dense(phi) - t) < 1e-10 * np.linalg.norm(t)
+    assert abs(info["sqdist"]) < 1e-9 * float(t @ t)

@@ -93,6 +93,82 @@ def mpo_sum(mpos: list, coefs: list, end_q, vac=None) -> list:
     return out
 
 
+def _bond_sectors(W: list) -> list:
+    """auxiliary sector dimensions of an MPO at every bond: [{QN: states}] (L + 1 bonds)"""
+    L = len(W)
+    dims = [dict() for _ in range(L + 1)]
+    for l, w in enumerate(W):
+        for i in range(w.nnz):
+            qi, qo = tuple(w.qin[i]), tuple(w.qout[i])
+            dims[l][qi] = max(dims[l].get(qi, 0), w.row[i] + 1)
+            dims[l + 1][qo] = max(dims[l + 1].get(qo, 0), w.col[i] + 1)
+    return dims
+
+
+def _clean(W: list, what: str):
+    dims = _bond_sectors(W)
+    for b in (0, len(W)):
+        if sum(dims[b].values()) != 1:
+            raise ValueError(f"{what}: the MPO needs a single auxiliary state at both ends")
+
+
+def mpo_adjoint(W: list) -> list:
+    """O^dagger of a real MPO with abelian quantum numbers: every site's local matrices
+    transposed, operator and auxiliary quantum numbers negated"""
+    out = []
+    for w in W:
+        t = MpoSite(w.nq, list(w.qloc), [tuple(-x for x in q) for q in w.qop])
+        for i in range(w.nnz):
+            t.add(w.s2[i], w.s1[i], w.k[i], tuple(-x for x in w.qin[i]), tuple(-x for x in w.qout[i]), w.row[i],
+                  w.col[i], w.val[i])
+        out.append(t)
+    return out
+
+
+def mpo_product(A: list, B: list) -> list:
+    """the operator product A B (B acts first) of two MPOs with abelian quantum numbers and a
+    single auxiliary state at both ends: W[s1, s3] = sum_s2 A[s1, s2] B[s2, s3] on the product
+    of the auxiliary bases, the states of each product sector in (QN_A, index_A, QN_B, index_B)
+    order, so that the two end states stay state 0; equal entries summed"""
+    _clean(A, "mpo_product")
+    _clean(B, "mpo_product")
+    L = len(A)
+    da, db = _bond_sectors(A), _bond_sectors(B)
+    index = []                      # bond -> {(qa, ia, qb, ib): (q, position in sector q)}
+    for b in range(L + 1):
+        pos, idx = {}, {}
+        for qa in sorted(da[b]):
+            for ia in range(da[b][qa]):
+                for qb in sorted(db[b]):
+                    for ib in range(db[b][qb]):
+                        q = tuple(x + y for x, y in zip(qa, qb))
+                        idx[(qa, ia, qb, ib)] = (q, pos.get(q, 0))
+                        pos[q] = pos.get(q, 0) + 1
+        index.append(idx)
+    out = []
+    for l in range(L):
+        wa, wb = A[l], B[l]
+        by_s2 = {}
+        for j in range(wb.nnz):
+            by_s2.setdefault(wb.s1[j], []).append(j)
+        qops, acc = [], {}
+        for i in range(wa.nnz):
+            for j in by_s2.get(wa.s2[i], ()):
+                qop = tuple(x + y for x, y in zip(wa.qop[wa.k[i]], wb.qop[wb.k[j]]))
+                if qop not in qops:
+                    qops.append(qop)
+                qi, ri = index[l][(tuple(wa.qin[i]), wa.row[i], tuple(wb.qin[j]), wb.row[j])]
+                qo, co = index[l + 1][(tuple(wa.qout[i]), wa.col[i], tuple(wb.qout[j]), wb.col[j])]
+                key = (wa.s1[i], wb.s2[j], qops.index(qop), qi, qo, ri, co)
+                acc[key] = acc.get(key, 0.0) + wa.val[i] * wb.val[j]
+        t = MpoSite(wa.nq, list(wa.qloc), qops)
+        for (s1, s3, k, qi, qo, ri, co), v in acc.items():
+            if v != 0.0:
+                t.add(s1, s3, k, qi, qo, ri, co, v)
+        out.append(t)
+    return out
+
+
 def _dims_of(A: Blocks, side: str) -> dict:
     q = A.qin if side == "in" else A.qout
     n = A.rows if side == "in" else A.cols
@@ -182,18 +258,24 @@ class Compressor:
         return float(E.data.sum())
 
     # ---- the fit
-    def fit(self, phi, terms: list, Dmax: int, sweeps: int = 2, eps_svd: float = 1e-14):
+    def fit(self, phi, terms: list, Dmax: int, sweeps: int = 2, eps_svd: float = 1e-14, target_norm2=None,
+            tol=None, min_sweeps: int = 1):
         """phi ~ sum c_i O_i psi_i, terms = [(W_i (MPO site list), psi_i (MPS), c_i)]; phi is
         updated in place (brought to right-canonical form first; it ends so, with its
         centre on site 0).  The operators may change the charge: O_i carries phi.Qtot -
         psi_i.Qtot (its MPO ends in that auxiliary quantum number).  Terms on the same
         psi_i run as one MPO (mpo_sum), so each step costs one two-site application and
         one environment update per distinct psi_i.  Returns the largest discarded weight
-        of the last sweep."""
+        of the last sweep.  With target_norm2 = <T|T> of the target and tol, the sweeps stop
+        as soon as the squared distance |phi - T|^2 = <T|T> - <phi|phi> (the fit is the
+        projection of T: <phi|T> = <phi|phi>) is at most tol, after min_sweeps and at most
+        `sweeps` full sweeps (two half-sweeps each, as MpsCompressor runs an even number);
+        self.last_fit holds the sweeps run and the last squared distance."""
+        ctl = (target_norm2, tol, min_sweeps)
         if self._pool is not None:
-            return self._fit(phi, terms, Dmax, sweeps, eps_svd, self._pool)
+            return self._fit(phi, terms, Dmax, sweeps, eps_svd, self._pool, ctl)
         with self._host_pool():
-            return self._fit(phi, terms, Dmax, sweeps, eps_svd, self._pool)
+            return self._fit(phi, terms, Dmax, sweeps, eps_svd, self._pool, ctl)
 
     @contextlib.contextmanager
     def _host_pool(self):
@@ -208,7 +290,7 @@ class Compressor:
             self._pool.close()
             self._pool = None
 
-    def _fit(self, phi, terms, Dmax, sweeps, eps_svd, pool):
+    def _fit(self, phi, terms, Dmax, sweeps, eps_svd, pool, ctl=(None, None, 1)):
         sym, nq, qloc, L = self.sym, self.sym.nq, self.model.qloc, self.model.L
         right_canonical(phi, pool)
         ctx = self.ctx if getattr(self.ctx, "device", -1) >= 0 else None
@@ -241,7 +323,9 @@ class Compressor:
                 envR[t][l] = self._env("R", envR[t][l + 1], phi.A[l], W[l], psi.A[l])
         disc_max = 0.0
         two_site = {}
-        for _ in range(sweeps):
+        target_norm2, tol, min_sweeps = ctl
+        self.last_fit = {"sweeps": 0, "sqdist": None}
+        for sweep in range(sweeps):
             disc_max = 0.0
             for move, bonds in (("right", range(L - 1)), ("left", range(L - 2, -1, -1))):
                 for l in bonds:
@@ -280,7 +364,61 @@ class Compressor:
                             envL[t][l + 1] = self._env("L", envL[t][l], A1, W[l], psi.A[l])
                         else:
                             envR[t][l + 1] = self._env("R", envR[t][l + 2], A2, W[l + 1], psi.A[l + 1])
+            self.last_fit["sweeps"] = sweep + 1
+            if target_norm2 is not None:
+                # centre on site 0, the other sites right-orthonormal: <phi|phi> is site 0's norm
+                n2 = self.overlap(phi, phi) if su2 else float(np.dot(phi.A[0].data, phi.A[0].data))
+                self.last_fit["sqdist"] = float(target_norm2 - n2)
+                if tol is not None and sweep + 1 >= min_sweeps and self.last_fit["sqdist"] <= tol:
+                    break
         return disc_max
+
+    # ---- the MpsCompressor operations (solvers/MpsCompressor.h:60-126)
+    def state_compress(self, psi, Dmax: int, tol: float = 1e-4, max_sweeps: int = 20, min_sweeps: int = 1,
+                       eps_svd: float = 1e-14):
+        """stateCompress: phi ~ psi with at most Dmax states per bond, sweeps until
+        |phi - psi|^2 <= tol; returns (phi, info)"""
+        phi = copy_mps(psi)
+        disc = self.fit(phi, [(self.I, psi, 1.0)], Dmax, max_sweeps, eps_svd, self.overlap(psi, psi), tol, min_sweeps)
+        return phi, dict(self.last_fit, discarded=disc)
+
+    def prod_compress(self, W, psi, Dmax: int, tol: float = 1e-4, max_sweeps: int = 20, min_sweeps: int = 1,
+                      phi=None, Wdag=None, eps_svd: float = 1e-14):
+        """prodCompress: phi ~ W psi, sweeps until |phi - W psi|^2 <= tol (<psi|W^dagger W|psi>
+        from the product MPO of Wdag = W^dagger and W; abelian symmetries).  phi: the start
+        (a copy of psi by default; give one of the target charge for operators that change
+        it).  Returns (phi, info)."""
+        if self.sym.nonabelian:
+            raise ValueError("prod_compress needs the product MPO W^dagger W: abelian symmetries")
+        P = mpo_product(Wdag if Wdag is not None else mpo_adjoint(W), W)
+        t2 = self.matrix_element(psi, P, psi)
+        phi = copy_mps(psi) if phi is None else phi
+        disc = self.fit(phi, [(W, psi, 1.0)], Dmax, max_sweeps, eps_svd, t2, tol, min_sweeps)
+        return phi, dict(self.last_fit, discarded=disc, target_norm2=t2)
+
+    def poly_compress(self, H, psi1, polyB: float, psi2, Dmax: int, tol: float = 1e-4, max_sweeps: int = 20,
+                      min_sweeps: int = 1, phi=None, eps_svd: float = 1e-14):
+        """polyCompress: phi ~ H psi1 - polyB psi2 for a Hermitian H (rescaled by the caller),
+        the step of an orthogonal-polynomial recursion; |T|^2 = <psi1|H H|psi1> - 2 polyB
+        <psi2|H|psi1> + polyB^2 <psi2|psi2>.  Returns (phi, info)."""
+        if self.sym.nonabelian:
+            raise ValueError("poly_compress needs the product MPO H H: abelian symmetries")
+        t2 = (self.matrix_element(psi1, mpo_product(H, H), psi1) - 2 * polyB * self.matrix_element(psi2, H, psi1)
+              + polyB * polyB * self.overlap(psi2, psi2))
+        phi = copy_mps(psi1) if phi is None else phi
+        disc = self.fit(phi, [(H, psi1, 1.0), (self.I, psi2, -polyB)], Dmax, max_sweeps, eps_svd, t2, tol,
+                        min_sweeps)
+        return phi, dict(self.last_fit, discarded=disc, target_norm2=t2)
+
+    def lincombo_compress(self, psis: list, factors: list, Dmax: int, guess=None, tol: float = 1e-4,
+                          max_sweeps: int = 20, min_sweeps: int = 1, eps_svd: float = 1e-14):
+        """lincomboCompress: phi ~ sum_i f_i psi_i (|T|^2 from the overlaps); guess: the
+        start (a copy of psis[0] by default).  Returns (phi, info)."""
+        t2 = sum(fi * fj * self.overlap(pi, pj) for pi, fi in zip(psis, factors) for pj, fj in zip(psis, factors))
+        phi = copy_mps(psis[0] if guess is None else guess)
+        disc = self.fit(phi, [(self.I, p, f) for p, f in zip(psis, factors)], Dmax, max_sweeps, eps_svd, t2, tol,
+                        min_sweeps)
+        return phi, dict(self.last_fit, discarded=disc, target_norm2=t2)
 
     # ---- the Chebyshev recursion of MPS
     def chebyshev_moments(self, psi0, nmom: int, a: float, b: float, Dmax: int, sweeps: int = 2,
