@@ -333,3 +333,20 @@ def test_prod_poly_and_lincombo_compress_against_dense():
     t = 0.5 * x + 2.0 * y - z
     assert np.linalg.norm(_dense(phi) - t) < 1e-10 * np.linalg.norm(t)
     assert abs(info["sqdist"]) < 1e-9 * float(t @ t)
+
+
+def test_edge_cases_two_sites_and_one_state():
+    """a two-site chain (one two-site step per half sweep) fits exactly; Dmax = 1 keeps one
+    state per bond and still returns the projection of the target onto that manifold"""
+    model, psi, comp = _setup(2, 16)
+    H = ed.mpo_to_dense(model)
+    x = _dense(psi)
+    phi = copy_mps(psi)
+    comp.fit(phi, [(model.W, psi, 1.0)], Dmax=16, sweeps=1)
+    assert np.linalg.norm(_dense(phi) - H @ x) < 1e-12 * np.linalg.norm(H @ x)
+    model, psi, comp = _setup(6, 64)
+    phi = copy_mps(psi)
+    disc = comp.fit(phi, [(model.W, psi, 1.0)], Dmax=1, sweeps=2)
+    assert disc > 0 and max(sum(d.values()) for d in phi.dims) == 1
+    f, t = _dense(phi), ed.mpo_to_dense(model) @ _dense(psi)
+    assert f @ t == pytest.approx(f @ f, rel=1e-9)
